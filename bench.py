@@ -1,0 +1,331 @@
+"""Benchmark: NEE path-contributions/s of the 3D temporal-correlation workload.
+
+Workload (one step = one render): the 3D correlation scene -- slab
+[-100,100]^2 x [0,20], sigs=[0,0.5], siga=[0,0.01], HG g=0.9, 64 point
+illuminations at z=-5 and 64 point views at z=25 on jittered 8x8 lattices,
+Brownian D=[0,1e-3], 8 lags -- with 2^22 paths (4 waves of 2^20), seeded
+synthetic inputs.  One contribution is one (path, scattering vertex,
+illumination, view, lag) term of the estimator.
+
+value : contributions / device time of the render (CUDA events on the
+        library's stream; scene tables resident in HBM).
+e2e   : the same metric through the public C-ABI call a MATLAB-style user
+        makes -- scene creation (host -> device upload of the config tables),
+        render, read-back of u and iter, scene destruction -- timed on the host.
+--impl reference: the reference has no CPU implementation and its CUDA
+        sources do not exist on the GPU host, so the reference arm times the
+        CPU FP64 restatement of its estimator (oracle/) on all host threads.
+
+Multi-GPU (torchrun): independent replicas with disjoint seeds ("replicas
+only": the paths are i.i.d., there is no exchange step); value is the sum of
+contributions over ranks divided by the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "NEE path-contributions/s at <=1e-5 err vs FP64 (vs plain FP32); p50/p99 latency"
+UNIT = "contributions/s"
+WORKLOAD = "correlation_3d"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            if not torch.cuda.is_available():
+                backend = "gloo"
+            else:
+                torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+        return dist, rank, ws
+    return None, 0, 1
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def _workload(seed: int, paths_log2: int):
+    from temporalspecklescode_gb300 import workloads as wl
+    waves = max(1, 1 << max(0, paths_log2 - 20))
+    batch = (1 << paths_log2) // waves
+    cfg, dims = wl.correlation_3d(batch_size=batch, full_iteration=waves, seed=seed)
+    return cfg, dims
+
+
+def cpu_baseline(sample_paths: int, threads: int):
+    """Time the CPU oracle (FP64 restatement, OpenMP) on a bounded sample."""
+    from temporalspecklescode_gb300 import config as cf
+    from tests.oracle_lib import Oracle
+    cfg, dims = _workload(0, 20)
+    cfg["simulation"]["batchSize"] = sample_paths
+    cfg["simulation"]["fullIteration"] = 1
+    pc = cf.prepare(cfg, dims)
+    oracle = Oracle()
+    t0 = time.perf_counter()
+    _, _, st = oracle.render(pc, 0, threads=threads)
+    dt = time.perf_counter() - t0
+    return st["contributions"] / dt, st, dt
+
+
+def run_reference(args, dist, rank, ws):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = args.ref_sample
+    times = []
+    contrib = 0
+    for i in range(args.warmup + args.steps):
+        v, st, dt = cpu_baseline(sample, threads)
+        if i >= args.warmup:
+            times.append(dt)
+            contrib = st["contributions"]
+    ms = 1000 * statistics.mean(times)
+    value = contrib / (ms / 1000)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "paths_per_step": sample, "note": "CPU FP64 restatement of the reference estimator"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample} paths of the {WORKLOAD} workload per step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, dist, rank, ws):
+    import numpy as np
+    from temporalspecklescode_gb300 import api, config as cf
+    api.load_library()
+    precision = cf.PRECISION_FP32 if args.precision == "fp32" else cf.PRECISION_SPLIT
+    cfg, dims = _workload(seed=1000 * rank, paths_log2=args.paths_log2)
+    scene = api.Scene(cfg, dims, precision)
+    lat = []
+    dev_ms = []
+    parts = {"ms_trace": [], "ms_contract_ms": [], "ms_contract_ss": []}
+    contrib = 0
+    launches = 0
+    for i in range(args.warmup):
+        scene.render(seed=i)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    _barrier(dist)
+    clocks.start()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        ts = time.perf_counter()
+        u, it = scene.render(seed=100 + i)
+        lat.append(1000 * (time.perf_counter() - ts))
+        tm = scene.timing()
+        dev_ms.append(tm["ms_total"])
+        for k in parts:
+            parts[k].append(tm[k])
+        launches += tm["launches"]
+        contrib += scene.stats()["contributions"]
+    wall = time.perf_counter() - t0
+    _barrier(dist)
+    clk = clocks.stop()
+    dev_total_s = sum(dev_ms) / 1000.0
+    dev_total_s = _max_over_ranks(dist, dev_total_s)
+    contrib_all = _sum_over_ranks(dist, float(contrib))
+    value = contrib_all / dev_total_s
+
+    # end to end through the C-ABI: create (upload) + render + read back + destroy
+    e2e_t = []
+    h2d = 0
+    for i in range(max(1, min(3, args.steps))):
+        ts = time.perf_counter()
+        with api.Scene(cfg, dims, precision) as s2:
+            u2, it2 = s2.render(seed=200 + i)
+        e2e_t.append(time.perf_counter() - ts)
+    pc = scene.prepared
+    for a in pc._keep:
+        h2d += a.nbytes
+    d2h = u.size * 16 + it.size * 8
+    e2e_s = _max_over_ranks(dist, statistics.mean(e2e_t))
+    e2e_value = _sum_over_ranks(dist, float(contrib / args.steps)) / e2e_s
+
+    peaks, pk_kind = _peaks()
+    # dominant kernel class and its roofline
+    mean = {k: statistics.mean(v) for k, v in parts.items()}
+    dom = max(mean, key=mean.get)
+    m = scene.meta
+    P = m["P"] * m["waves"]
+    Nl, Nv, Nt = m["Nl"], m["Nv"], m["Nt"]
+    if dom == "ms_contract_ms":
+        flops = 8.0 * Nl * Nv * Nt * P
+        achieved = flops / (mean[dom] / 1000) / 1e12
+        roof = {"kernel": "gemm (multiple-scattering contraction)", "bound": "tensor", "achieved": achieved,
+                "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                "peak_source": pk_kind}
+    else:
+        # algorithmic HBM bytes: the per-path rows the kernel class writes / reads
+        if dom == "ms_trace":
+            nbytes = P * (8.0 * Nt * (2 * Nl + 2 * Nv + Nl) + 4 * Nl * 2 + 16)
+            name = "trace_kernel (fused path tracing)"
+        else:
+            nbytes = P * (8.0 * Nt * (Nl + Nv) + 16)
+            name = "ss_kernel (single-scattering contraction)"
+        achieved = nbytes / (mean[dom] / 1000) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": pk_kind}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, st, dt = cpu_baseline(args.cpu_sample, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} paths of the {WORKLOAD} workload (oracle, FP64, OpenMP), {dt:.1f} s"}
+
+    lat_sorted = sorted(lat)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(dev_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64 (split: FP64 phase, compensated FP32 contraction)" if precision == 0 else "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "paths_per_step": P, "Nl": Nl, "Nv": Nv, "Nt": Nt, "dims": dims,
+                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "l2": "per-step working set (per-path rows) larger than L2"},
+        "latency_ms": {"p50": lat_sorted[len(lat) // 2], "p99": lat_sorted[min(len(lat) - 1, int(math.ceil(0.99 * len(lat))) - 1)]},
+        "phases_ms": mean,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": 1000 * e2e_s},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    scene.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="split", choices=["split", "fp32"])
+    ap.add_argument("--paths-log2", type=int, default=22)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 15)
+    ap.add_argument("--ref-sample", type=int, default=1 << 14)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    dist, rank, ws = _dist()
+    if args.impl == "reference":
+        run_reference(args, dist, rank, ws)
+    else:
+        run_gpu(args, dist, rank, ws)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

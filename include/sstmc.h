@@ -1,0 +1,212 @@
+/*
+ * sstmc.h -- C-ABI of the GB300-native next-event-estimation (NEE) speckle
+ * path tracer.  Plain C types only: pointers, sizes, integers and doubles.
+ *
+ * The boundary replaces the MATLAB MEX entry point of the reference
+ *   [u, iter] = sstmc2D(config) / sstmc3D(config)
+ *   (MatlabInterface.cu:1565-1825, mexFunction)
+ * and the object model it builds (Simulation / Scattering / Medium / Source /
+ * Sampler / Tracer, MatlabInterface.cu:1459-1563, 712-1457).  One
+ * sstmc_config carries every field of the MATLAB config struct; one
+ * sstmc_scene is the set of device-resident objects mexFunction constructs;
+ * sstmc_render is one call of Tracer::trace per rendering
+ * (NextEventEstimation.cuh:1461-1637).
+ *
+ * Output layout is the reference's: u is complex, Nl fastest, then Nv, then
+ * Nt, then renderings (MatlabInterface.cu:1731-1738), stored here as
+ * interleaved (re, im) doubles.  iter[r] = batchSize * fullIteration +
+ * zeroContributionPaths (MatlabInterface.cu:1796).
+ *
+ * Error codes keep the numeric values of the reference's ErrorType enum
+ * (Simulation.cuh:111-162) for every shared meaning; codes >= 100 are new.
+ */
+#ifndef SSTMC_H
+#define SSTMC_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Error codes: Simulation.cuh:111-162 (ErrorType)                      */
+/* ------------------------------------------------------------------ */
+#define SSTMC_NO_ERROR                 0
+#define SSTMC_DEVICE_ERROR             1
+#define SSTMC_ALLOCATION_ERROR         2
+#define SSTMC_KERNEL_ERROR             3
+#define SSTMC_CUBLAS_ERROR             4   /* reference: cuBLAS; here: contraction (GEMM) error */
+#define SSTMC_NOT_SUPPORTED            5
+#define SSTMC_MISC_ERROR               6
+/* 7..47 are the reference's per-kernel KERNEL_ERROR_* codes; the ones this
+ * build can raise keep their reference values: */
+#define SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousAttenuationKernel 44
+#define SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel      45
+/* new in this build */
+#define SSTMC_INVALID_CONFIG           100 /* the MEX layer raised a MATLAB error instead */
+#define SSTMC_TIMEOUT                  101 /* a bounded wait or a bounded device loop ran out */
+#define SSTMC_CANCELLED                102 /* a served request was cancelled */
+#define SSTMC_INVALID_HANDLE           103
+#define SSTMC_PATH_LIMIT               104 /* a path exceeded the vertex / retry limit */
+
+/* ------------------------------------------------------------------ */
+/* Enumerations mirroring the reference's string / enum values          */
+/* ------------------------------------------------------------------ */
+/* ScatteringNS::ScatteringType (Scattering.cuh:17-23) */
+#define SSTMC_SCATTERING_NOT_DEFINED      0
+#define SSTMC_SCATTERING_ISOTROPIC        1
+#define SSTMC_SCATTERING_TABULAR          2   /* not supported by this build */
+#define SSTMC_SCATTERING_HENYEY_GREENSTEIN 3
+#define SSTMC_SCATTERING_VMF_MIXTURE      4   /* not supported by this build */
+
+/* config.medium.type (MatlabInterface.cu:896, 942) */
+#define SSTMC_MEDIUM_HETEROGENEOUS 0
+#define SSTMC_MEDIUM_HOMOGENEOUS   1   /* mapped to a single-cell heterogeneous grid */
+
+/* config.<source>.type (MatlabInterface.cu:1101, 1137, 1161) */
+#define SSTMC_SOURCE_NONE          0   /* absent illumination2 / view2 */
+#define SSTMC_SOURCE_POINT         1
+#define SSTMC_SOURCE_FARFIELD      2
+#define SSTMC_SOURCE_GAUSSIANBEAM  3   /* not supported by this build */
+
+/* config.sampler.type (MatlabInterface.cu:1238, 1295) */
+#define SSTMC_SAMPLER_TEMPORAL              0
+#define SSTMC_SAMPLER_TEMPORAL_CORRELATION  1
+
+/* Contraction precision of the illumination x view accumulation. */
+#define SSTMC_PRECISION_SPLIT  0  /* default: FP64 path length + phase reduction, 3xTF32 tensor-core contraction */
+#define SSTMC_PRECISION_FP32   1  /* plain FP32 form: FP32 phase, FP32 SIMT contraction */
+
+#define SSTMC_MATERIAL_NUM 10     /* Simulation.cuh:32 (MATERIAL_NUM) */
+
+/* One source block of the config (illumination, view, illumination2, view2).
+ * MatlabInterface.cu:1062-1215 (buildSource). */
+typedef struct sstmc_source_cfg {
+    int32_t type;            /* SSTMC_SOURCE_* */
+    uint32_t count;          /* number of locations / directions */
+    const double* xyz;       /* count x 3 doubles (x, y, z); z ignored when dims == 2 */
+    int32_t is_area_source;  /* PointSource isAreaSource (default 0) */
+} sstmc_source_cfg;
+
+/* The whole MATLAB config struct (README.md:74-373). */
+typedef struct sstmc_config {
+    uint32_t dims;                 /* 2 (sstmc2D) or 3 (sstmc3D) */
+
+    /* config.simulation (MatlabInterface.cu:1459-1546, 1590-1671) */
+    uint32_t batch_size;           /* default 1024 */
+    uint32_t full_iteration;       /* default 1 */
+    uint32_t renderings_num;       /* default 1 */
+    double lambda;                 /* default 1; a single wavelength (Nw = 1) */
+    uint64_t seed;
+    int32_t device_number;         /* default 0 */
+
+    /* config.scattering (MatlabInterface.cu:712-888); one entry per material
+     * cell.  A single cell is duplicated into material 1 as the reference does
+     * (MatlabInterface.cu:750-760, 878-881). */
+    uint32_t scattering_num;       /* number of cells in scattering.type */
+    const int32_t* scattering_type;  /* SSTMC_SCATTERING_*, [scattering_num] */
+    const double* scattering_g;      /* HG anisotropy g, [scattering_num] (ignored for Isotropic) */
+
+    /* config.medium (MatlabInterface.cu:890-1060) */
+    int32_t medium_type;           /* SSTMC_MEDIUM_* */
+    const double* x_axis; uint32_t x_axis_size;
+    const double* y_axis; uint32_t y_axis_size;
+    const double* z_axis; uint32_t z_axis_size;   /* 3D only */
+    const uint32_t* material_grid; /* (nx-1)(ny-1)(nz-1) entries, x fastest */
+    const double* sigs;            /* [material count] */
+    const double* siga;            /* [material count] or NULL (zeros) */
+    /* Homogeneous medium: box and scalars (used when medium_type == HOMOGENEOUS) */
+    double box_min[3];
+    double box_max[3];
+    double homogeneous_sigs;
+
+    /* config.illumination / view / illumination2 / view2 */
+    sstmc_source_cfg illumination;
+    sstmc_source_cfg view;
+    sstmc_source_cfg illumination2;
+    sstmc_source_cfg view2;
+
+    /* config.sampler (MatlabInterface.cu:1217-1372) */
+    int32_t sampler_type;          /* SSTMC_SAMPLER_* */
+    const double* t; uint32_t t_num;
+    const double* D;               /* [material count], non-negative */
+    const double* U;               /* [material count x 3] (x, y, z) */
+    int32_t is_temporal_amplitude; /* default 1 */
+    int32_t is_forced_inside_bin;  /* default 0; 1 is not supported */
+
+    /* config.tracer (MatlabInterface.cu:1374-1457) */
+    int32_t is_cbs;                /* default 0; 1 is not supported */
+
+    /* build-specific */
+    int32_t precision;             /* SSTMC_PRECISION_* */
+} sstmc_config;
+
+typedef struct sstmc_scene sstmc_scene;
+
+/* Fill cfg with the reference's defaults (batchSize 1024, fullIteration 1,
+ * renderingsNum 1, lambda 1, isTemporalAmplitude true, ...). */
+void sstmc_config_init(sstmc_config* cfg);
+
+/* Build the device-resident scene: replaces buildSimulation .. buildTracer
+ * (MatlabInterface.cu:1677-1700).  The config arrays are copied; the caller
+ * may free them after the call. */
+int32_t sstmc_scene_create(const sstmc_config* cfg, sstmc_scene** out);
+
+/* Nl, Nv, Nt of the scene (Sampler::getIlluminationSize/getViewSize/
+ * getSamplerSize, SamplerInterface.cuh:147-151). */
+int32_t sstmc_scene_shape(const sstmc_scene* scene, uint32_t* nl, uint32_t* nv, uint32_t* nt);
+
+/* Render renderings_num fields / correlations: the loop of
+ * MatlabInterface.cu:1783-1801 (trace, iter, seed++ per rendering).
+ * u_out: 2 * Nl * Nv * Nt * renderings_num doubles (interleaved complex),
+ * iter_out: renderings_num doubles (may be NULL).  seed overrides
+ * cfg.seed for the first rendering. */
+int32_t sstmc_render(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
+
+/* Number of NEE path-contributions (sum over traced paths of vertices * Nl *
+ * Nv * Nt) and of voxel DDA steps of the last sstmc_render call. */
+int32_t sstmc_last_stats(const sstmc_scene* scene, uint64_t* contributions,
+                         uint64_t* dda_steps, uint64_t* vertices, uint64_t* paths);
+
+/* Device time of the last sstmc_render in milliseconds, measured with CUDA
+ * events on the scene's stream: ms[0] whole render, ms[1] path tracing,
+ * ms[2] multiple-scattering contraction, ms[3] single-scattering
+ * contraction; launches = kernels launched.  No reference counterpart (the
+ * reference's TIME_REC std::clock buckets, NextEventEstimation.cuh:107-156). */
+int32_t sstmc_last_timing(const sstmc_scene* scene, double* ms, uint64_t* launches);
+
+int32_t sstmc_scene_destroy(sstmc_scene* scene);
+
+/* Text of an error code (MatlabInterface.cu:24-272, getErrorMsg). */
+const char* sstmc_error_string(int32_t code);
+
+/* Detail text of the last failed sstmc_scene_create (config validation). */
+const char* sstmc_last_error_text(void);
+
+/* ------------------------------------------------------------------ */
+/* Per-path debug trace (parity tests): run one wave of `paths` paths  */
+/* with path ids [first_path, first_path + paths) and copy the         */
+/* per-path quantities to host arrays.  Any pointer may be NULL.        */
+/* ------------------------------------------------------------------ */
+typedef struct sstmc_path_trace {
+    int32_t* misses;        /* [paths] missed first-vertex attempts */
+    int32_t* vertices;      /* [paths] scattering vertices B */
+    uint32_t* vertex_hash;  /* [paths] hash of vertex positions + materials */
+    uint32_t* dda_steps;    /* [paths] voxel steps of all NEE rays */
+    float* x1;              /* [paths x 3] first vertex */
+    int32_t* m1;            /* [paths] first vertex material */
+    double* a_ms;           /* [paths x Nt x Nl x 2] illumination vector of the multiple-scattering term */
+    double* s_ms;           /* [paths x Nt x Nv x 2] summed view vector of the multiple-scattering term */
+    double* a_ss;           /* [paths x Nt x Nl x 2] illumination vector of the single-scattering term */
+    double* b_ss;           /* [paths x Nt x Nv x 2] view vector of the single-scattering term */
+} sstmc_path_trace;
+
+int32_t sstmc_trace_paths(sstmc_scene* scene, uint64_t seed, uint32_t first_path,
+                          uint32_t paths, sstmc_path_trace* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SSTMC_H */

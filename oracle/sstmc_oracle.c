@@ -1,0 +1,1334 @@
+/*
+ * sstmc_oracle.c -- TEST INFRASTRUCTURE: CPU oracle of the NEE speckle path
+ * tracer (see sstmc_oracle.h).  Tests, smoke() and the bench's CPU baseline
+ * are its only callers.
+ *
+ * Reference files restated here (paths inside chabner/temporalSpecklesCode):
+ *   estimator / loop        Implementation/Tracer/NextEventEstimation.cuh:643-1637
+ *   field sampler           Implementation/Sampler/TemporalSampler.cuh:139-937, 1324-1610
+ *   correlation sampler     Implementation/Sampler/TemporalSamplerCorrelation.cuh:111-1087
+ *   voxel medium            Implementation/Medium/HeterogeneousMedium.cuh:257-738
+ *   medium box helpers      Interface/MediumInterface.cuh:138-222, 239-266
+ *   far-field source        Implementation/Source/FarField.cuh:69-263, 439-599
+ *   point source            Implementation/Source/PointSource.cuh:70-446
+ *   temporal source terms   Interface/SourceInterface.cuh:184-354
+ *   scattering (Iso, HG)    Implementation/Scattering.cuh:484-611, 891-1261
+ *   vectors / directions    VectorType.cuh:155-362
+ *   config semantics        MatlabInterface.cu:712-1457, 1565-1801
+ *
+ * Build: gcc -O2 -fPIC -shared -fopenmp -ffp-contract=off (oracle/Makefile).
+ */
+#include "sstmc_oracle.h"
+#include "oracle_math.h"
+
+#include <stdlib.h>
+#include <stdio.h>
+#include <math.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OM SSTMC_MATERIAL_NUM
+#define O_PI 3.14159265358979323846
+#define O_ISO_AMP2 0.398942280401432678
+#define O_ISO_AMP3 0.282094791773878143
+#define O_ISO_PDF2 0.159154943091895336
+#define O_ISO_PDF3 0.079577471545947668
+#define O_MAX_ATTEMPTS   (1u << 20)
+#define O_MAX_VERTICES   (1u << 20)
+#define O_MAX_WOODCOCK   (1u << 22)
+
+typedef struct { float x, y, z; } f3;
+
+/* ------------------------------------------------------------------ */
+/* scene                                                              */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int type, n, is_area;
+    float* p;        /* n*3 point location or unit direction (float) */
+    float* inv;      /* n*3 inverse direction (far field) */
+    float* tang;     /* n*3 tangent point */
+    float* pt;       /* n*3 perpendicular T */
+    float* ps;       /* n*3 perpendicular S (3D) */
+    float* mint; float* maxt; float* mins; float* maxs;
+    double* sprob;   /* n: far-field projected-box sampling probability */
+} o_src;
+
+typedef struct {
+    int dims, M;
+    int scat_type[OM];
+    float g_f[OM];
+    double gup[OM], gd1[OM], gd2[OM];
+    int iso_all;
+    /* medium */
+    int n[3];             /* edges per axis (n[2] = 0 in 2D) */
+    float* ax[3];
+    double* axd[3];
+    unsigned char* grid;
+    float sigt_f[OM], inv_maxsigt_f, accept_f[OM], survive_f[OM];
+    float bmin[3], bmax[3], center[3], radius[3], inv_radius[3];
+    /* sources: 0 illumination, 1 view, 2 illumination2, 3 view2 */
+    o_src src[4];
+    int correlation;
+    int Nt;
+    double* ticks;        /* correlation: raw ticks; */
+    float* ticks_f;
+    /* field temporal: sorted ticks */
+    int neg;
+    float* disp_scale;    /* [OM][Nt] sqrt(2 dims D |dt|) */
+    float* disp_u;        /* [OM][Nt][3] dt*U */
+    int moving[OM];
+    double D[OM];
+    float U_f[OM][3];
+    int temporal_amp;
+    double lambda;
+    unsigned P, full_iter;
+} o_scene;
+
+static void o_free_scene(o_scene* S)
+{
+    for (int i = 0; i < 4; ++i) {
+        o_src* s = &S->src[i];
+        free(s->p); free(s->inv); free(s->tang); free(s->pt); free(s->ps);
+        free(s->mint); free(s->maxt); free(s->mins); free(s->maxs); free(s->sprob);
+    }
+    for (int a = 0; a < 3; ++a) { free(S->ax[a]); free(S->axd[a]); }
+    free(S->grid); free(S->ticks); free(S->ticks_f); free(S->disp_scale); free(S->disp_u);
+}
+
+/* Far-field tables: FarField.cuh:71-127 (fillBuffers) in double, stored as float. */
+static int o_prep_farfield(o_src* s, const sstmc_source_cfg* c, int dims,
+                           const double bmin[3], const double bmax[3])
+{
+    int n = (int)c->count;
+    s->p = calloc((size_t)n * 3, sizeof(float)); s->inv = calloc((size_t)n * 3, sizeof(float));
+    s->tang = calloc((size_t)n * 3, sizeof(float)); s->pt = calloc((size_t)n * 3, sizeof(float));
+    s->ps = calloc((size_t)n * 3, sizeof(float));
+    s->mint = calloc(n, sizeof(float)); s->maxt = calloc(n, sizeof(float));
+    s->mins = calloc(n, sizeof(float)); s->maxs = calloc(n, sizeof(float));
+    s->sprob = calloc(n, sizeof(double));
+    if (!s->p || !s->inv || !s->tang || !s->pt || !s->ps || !s->mint || !s->maxt || !s->mins || !s->maxs || !s->sprob)
+        return SSTMC_ALLOCATION_ERROR;
+    double center[3], radius[3];
+    for (int i = 0; i < 3; ++i) { center[i] = (bmax[i] + bmin[i]) * 0.5; radius[i] = (bmax[i] - bmin[i]) * 0.5; }
+    double rc = radius[0] > radius[1] ? radius[0] : radius[1];
+    if (dims == 3 && radius[2] > rc) rc = radius[2];
+    rc = rc + 1e-12;
+    for (int k = 0; k < n; ++k) {
+        double v[3] = { c->xyz[3 * k], c->xyz[3 * k + 1], dims == 3 ? c->xyz[3 * k + 2] : 0.0 };
+        double nrm = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (!(nrm > 0.0)) return SSTMC_INVALID_CONFIG;
+        double inr = 1.0 / nrm;
+        double d[3] = { v[0] * inr, v[1] * inr, v[2] * inr };
+        double op[3] = { -d[0], -d[1], -d[2] };
+        double tg[3], T[3], Sv[3] = { 0, 0, 0 };
+        for (int i = 0; i < 3; ++i) tg[i] = center[i] + rc * op[i];
+        if (dims == 3) {
+            if (fabs(1.0 - fabs(op[2])) <= 1e-12) {
+                T[0] = 1; T[1] = 0; T[2] = 0; Sv[0] = 0; Sv[1] = 1; Sv[2] = 0;
+            } else {
+                T[0] = -op[1]; T[1] = op[0]; T[2] = 0.0;
+                double tn = 1.0 / sqrt(T[0] * T[0] + T[1] * T[1]);
+                T[0] = T[0] * tn; T[1] = T[1] * tn;
+                Sv[0] = T[1] * op[2] - T[2] * op[1];
+                Sv[1] = T[2] * op[0] - T[0] * op[2];
+                Sv[2] = T[0] * op[1] - T[1] * op[0];
+            }
+        } else {
+            T[0] = -op[1]; T[1] = op[0]; T[2] = 0.0;
+        }
+        double mnT = 0, mxT = 0, mnS = 0, mxS = 0;
+        int corners = dims == 3 ? 8 : 4;
+        for (int q = 0; q < corners; ++q) {
+            double cc[3] = { (q & 1) ? bmax[0] : bmin[0], (q & 2) ? bmax[1] : bmin[1],
+                             dims == 3 ? ((q & 4) ? bmax[2] : bmin[2]) : 0.0 };
+            double pT = (cc[0] - tg[0]) * T[0] + (cc[1] - tg[1]) * T[1] + (cc[2] - tg[2]) * T[2];
+            double pS = (cc[0] - tg[0]) * Sv[0] + (cc[1] - tg[1]) * Sv[1] + (cc[2] - tg[2]) * Sv[2];
+            if (q == 0 || pT < mnT) mnT = pT;
+            if (q == 0 || pT > mxT) mxT = pT;
+            if (q == 0 || pS < mnS) mnS = pS;
+            if (q == 0 || pS > mxS) mxS = pS;
+        }
+        for (int i = 0; i < 3; ++i) {
+            s->p[3 * k + i] = (float)d[i];
+            s->inv[3 * k + i] = (float)(fabs(d[i]) < 1e-12 ? 1e12 : 1.0 / d[i]);
+            s->tang[3 * k + i] = (float)tg[i];
+            s->pt[3 * k + i] = (float)T[i];
+            s->ps[3 * k + i] = (float)Sv[i];
+        }
+        s->mint[k] = (float)mnT; s->maxt[k] = (float)mxT;
+        s->mins[k] = (float)mnS; s->maxs[k] = (float)mxS;
+        s->sprob[k] = dims == 3 ? 1.0 / ((mxT - mnT) * (mxS - mnS)) : 1.0 / (mxT - mnT);
+    }
+    return SSTMC_NO_ERROR;
+}
+
+static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const double bmin[3], const double bmax[3])
+{
+    memset(s, 0, sizeof(*s));
+    s->type = c->type; s->n = (int)c->count; s->is_area = c->is_area_source ? 1 : 0;
+    if (c->type == SSTMC_SOURCE_NONE) return SSTMC_NO_ERROR;
+    if (c->count == 0 || c->xyz == NULL) return SSTMC_INVALID_CONFIG;
+    if (c->type == SSTMC_SOURCE_FARFIELD) return o_prep_farfield(s, c, dims, bmin, bmax);
+    if (c->type != SSTMC_SOURCE_POINT) return SSTMC_NOT_SUPPORTED;
+    s->p = calloc((size_t)s->n * 3, sizeof(float));
+    if (!s->p) return SSTMC_ALLOCATION_ERROR;
+    for (int k = 0; k < s->n; ++k) {
+        s->p[3 * k] = (float)c->xyz[3 * k];
+        s->p[3 * k + 1] = (float)c->xyz[3 * k + 1];
+        s->p[3 * k + 2] = dims == 3 ? (float)c->xyz[3 * k + 2] : 0.0f;
+    }
+    return SSTMC_NO_ERROR;
+}
+
+/* Config normalisation and validation: MatlabInterface.cu:712-1372. */
+static int o_build_scene(const sstmc_config* cfg, o_scene* S)
+{
+    memset(S, 0, sizeof(*S));
+    if (cfg->dims != 2 && cfg->dims != 3) return SSTMC_INVALID_CONFIG;
+    int dims = S->dims = (int)cfg->dims;
+    if (cfg->is_cbs) return SSTMC_NOT_SUPPORTED;
+    if (cfg->is_forced_inside_bin) return SSTMC_NOT_SUPPORTED;
+    if (cfg->batch_size == 0 || cfg->full_iteration == 0) return SSTMC_INVALID_CONFIG;
+    if (!(cfg->lambda > 0)) return SSTMC_INVALID_CONFIG;
+    S->P = cfg->batch_size; S->full_iter = cfg->full_iteration; S->lambda = cfg->lambda;
+
+    /* scattering: a single cell is duplicated into material 1 */
+    if (cfg->scattering_num == 0 || cfg->scattering_num > OM || !cfg->scattering_type) return SSTMC_INVALID_CONFIG;
+    int M = (int)cfg->scattering_num;
+    for (int m = 0; m < OM; ++m) S->scat_type[m] = SSTMC_SCATTERING_NOT_DEFINED;
+    for (int m = 0; m < M; ++m) {
+        int ty = cfg->scattering_type[m];
+        double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
+        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return SSTMC_NOT_SUPPORTED;
+        if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(fabs(g) < 1.0)) return SSTMC_INVALID_CONFIG;
+        int targets[2] = { m, 1 };
+        int nt = (M == 1) ? 2 : 1;
+        for (int q = 0; q < nt; ++q) {
+            int mm = targets[q];
+            S->scat_type[mm] = ty;
+            S->g_f[mm] = (float)g;
+            S->gup[mm] = dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * O_PI)) : (1.0 - g * g) / (4.0 * O_PI);
+            S->gd1[mm] = 1.0 + g * g;
+            S->gd2[mm] = -2.0 * g;
+        }
+    }
+    if (M == 1) M = 2;
+    S->M = M;
+    S->iso_all = 1;
+    for (int m = 0; m < OM; ++m) {
+        if (S->scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(fabs(S->g_f[m]) < 0.0001f)) S->iso_all = 0;
+    }
+
+    /* medium */
+    double bmin[3] = { 0, 0, 0 }, bmax[3] = { 0, 0, 0 };
+    double sigs[OM] = { 0 }, siga[OM] = { 0 };
+    if (cfg->medium_type == SSTMC_MEDIUM_HOMOGENEOUS) {
+        if (M != 2) return SSTMC_INVALID_CONFIG;
+        for (int a = 0; a < dims; ++a) {
+            if (!(cfg->box_max[a] > cfg->box_min[a])) return SSTMC_INVALID_CONFIG;
+            S->n[a] = 2;
+            S->axd[a] = malloc(2 * sizeof(double)); S->ax[a] = malloc(2 * sizeof(float));
+            S->ax[a][0] = (float)cfg->box_min[a]; S->ax[a][1] = (float)cfg->box_max[a];
+        }
+        S->grid = malloc(1); S->grid[0] = 1;
+        sigs[1] = cfg->homogeneous_sigs;
+    } else if (cfg->medium_type == SSTMC_MEDIUM_HETEROGENEOUS) {
+        const double* axes[3] = { cfg->x_axis, cfg->y_axis, cfg->z_axis };
+        uint32_t sizes[3] = { cfg->x_axis_size, cfg->y_axis_size, cfg->z_axis_size };
+        size_t cells = 1;
+        for (int a = 0; a < dims; ++a) {
+            if (!axes[a] || sizes[a] < 2) return SSTMC_INVALID_CONFIG;
+            S->n[a] = (int)sizes[a];
+            S->axd[a] = malloc(sizes[a] * sizeof(double)); S->ax[a] = malloc(sizes[a] * sizeof(float));
+            for (uint32_t i = 0; i < sizes[a]; ++i) {
+                S->ax[a][i] = (float)axes[a][i];
+                if (i > 0 && !(S->ax[a][i] > S->ax[a][i - 1])) return SSTMC_INVALID_CONFIG;
+            }
+            cells *= (size_t)(sizes[a] - 1);
+        }
+        if (!cfg->material_grid || !cfg->sigs) return SSTMC_INVALID_CONFIG;
+        S->grid = malloc(cells);
+        for (size_t i = 0; i < cells; ++i) {
+            uint32_t m = cfg->material_grid[i];
+            if (m == 0 || m >= (uint32_t)M) return SSTMC_INVALID_CONFIG; /* MatlabInterface.cu:979-991 */
+            S->grid[i] = (unsigned char)m;
+        }
+        for (int m = 0; m < M; ++m) { sigs[m] = cfg->sigs[m]; siga[m] = cfg->siga ? cfg->siga[m] : 0.0; }
+    } else {
+        return SSTMC_NOT_SUPPORTED;
+    }
+    for (int a = 0; a < dims; ++a) for (int i = 0; i < S->n[a]; ++i) S->axd[a][i] = (double)S->ax[a][i];
+    for (int a = 0; a < dims; ++a) {
+        S->bmin[a] = S->ax[a][0]; S->bmax[a] = S->ax[a][S->n[a] - 1];
+        bmin[a] = S->axd[a][0]; bmax[a] = S->axd[a][S->n[a] - 1];
+        double c = (bmax[a] + bmin[a]) * 0.5, r = (bmax[a] - bmin[a]) * 0.5;
+        S->center[a] = (float)c; S->radius[a] = (float)r;
+        S->inv_radius[a] = fabsf(S->radius[a]) < 1e-12f ? 1e12f : 1.0f / S->radius[a];
+    }
+    float maxsigt = 0.0f;
+    for (int m = 0; m < OM; ++m) {
+        if (sigs[m] < 0 || siga[m] < 0) return SSTMC_INVALID_CONFIG;
+        float ss = (float)sigs[m], sa = (float)siga[m];
+        S->sigt_f[m] = ss + sa;
+        S->survive_f[m] = S->sigt_f[m] > 0.0f ? ss / S->sigt_f[m] : 1.0f;
+        if (S->sigt_f[m] > maxsigt) maxsigt = S->sigt_f[m];
+    }
+    if (!(maxsigt > 0.0f)) return SSTMC_INVALID_CONFIG;
+    S->inv_maxsigt_f = 1.0f / maxsigt;
+    for (int m = 0; m < OM; ++m) S->accept_f[m] = S->sigt_f[m] / maxsigt;
+
+    /* sources */
+    const sstmc_source_cfg* sc[4] = { &cfg->illumination, &cfg->view, &cfg->illumination2, &cfg->view2 };
+    for (int i = 0; i < 4; ++i) {
+        int e = o_prep_source(&S->src[i], sc[i], dims, bmin, bmax);
+        if (e) return e;
+    }
+    if (S->src[0].type == SSTMC_SOURCE_NONE || S->src[1].type == SSTMC_SOURCE_NONE) return SSTMC_INVALID_CONFIG;
+
+    /* sampler */
+    if (!cfg->t || cfg->t_num == 0) return SSTMC_INVALID_CONFIG;
+    S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
+    if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return SSTMC_INVALID_CONFIG;
+    if (S->correlation) {
+        if (S->src[2].type == SSTMC_SOURCE_NONE || S->src[3].type == SSTMC_SOURCE_NONE) return SSTMC_INVALID_CONFIG;
+        if (S->src[2].n != S->src[0].n || S->src[3].n != S->src[1].n) return SSTMC_INVALID_CONFIG;
+        if (S->src[2].type != S->src[0].type || S->src[3].type != S->src[1].type) return SSTMC_NOT_SUPPORTED;
+    }
+    S->temporal_amp = cfg->is_temporal_amplitude ? 1 : 0;
+    int Nt = S->Nt = (int)cfg->t_num;
+    S->ticks = malloc(Nt * sizeof(double)); S->ticks_f = malloc(Nt * sizeof(float));
+    for (int t = 0; t < Nt; ++t) { S->ticks[t] = cfg->t[t]; S->ticks_f[t] = (float)cfg->t[t]; }
+    for (int m = 0; m < OM; ++m) {
+        S->D[m] = (m < M && cfg->D) ? cfg->D[m] : 0.0;
+        if (S->D[m] < 0) return SSTMC_INVALID_CONFIG; /* MatlabInterface.cu:1278-1283 */
+        for (int i = 0; i < 3; ++i) S->U_f[m][i] = (m < M && cfg->U && (i < dims)) ? (float)cfg->U[3 * m + i] : 0.0f;
+    }
+    /* field sampler: ticks sorted around the mean, TemporalSampler.cuh:958-1150 */
+    S->disp_scale = calloc((size_t)OM * Nt, sizeof(float));
+    S->disp_u = calloc((size_t)OM * Nt * 3, sizeof(float));
+    {
+        double mean = 0;
+        for (int t = 0; t < Nt; ++t) mean += S->ticks[t];
+        mean = mean / Nt;
+        int* used = calloc(Nt, sizeof(int));
+        int* negl = malloc(Nt * sizeof(int));
+        int* posl = malloc(Nt * sizeof(int));
+        int nn = 0, np = 0;
+        for (int t = 0; t < Nt; ++t) { if (S->ticks[t] - mean < 0) nn++; else np++; }
+        for (int a = 0; a < nn; ++a) {
+            int first = 1, idx = 0; double best = 0;
+            for (int t = 0; t < Nt; ++t) if (!used[t] && S->ticks[t] - mean < 0) {
+                if (first || mean - S->ticks[t] < best) { first = 0; best = mean - S->ticks[t]; idx = t; }
+            }
+            used[idx] = 1; negl[a] = idx;
+        }
+        for (int a = 0; a < np; ++a) {
+            int first = 1, idx = 0; double best = 0;
+            for (int t = 0; t < Nt; ++t) if (!used[t] && S->ticks[t] - mean >= 0) {
+                if (first || S->ticks[t] - mean < best) { first = 0; best = S->ticks[t] - mean; idx = t; }
+            }
+            used[idx] = 1; posl[a] = idx;
+        }
+        S->neg = nn;
+        double* dt = malloc(Nt * sizeof(double));
+        int cn = 0, cp = 0, prev = -1;
+        for (int j = 0; j < Nt; ++j) {
+            int tick;
+            if (j < nn) { tick = negl[cn]; if (cn == 0) prev = -1; cn++; }
+            else { tick = posl[cp]; if (cp == 0) prev = -1; cp++; }
+            dt[j] = prev < 0 ? S->ticks[tick] - mean : S->ticks[tick] - S->ticks[prev];
+            prev = tick;
+        }
+        for (int m = 0; m < OM; ++m) {
+            S->moving[m] = (S->D[m] != 0.0) || S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f;
+            for (int j = 0; j < Nt; ++j) {
+                S->disp_scale[m * Nt + j] = (float)sqrt(2.0 * dims * S->D[m] * fabs(dt[j]));
+                double U[3] = { m < M && cfg->U ? cfg->U[3 * m] : 0.0, m < M && cfg->U ? cfg->U[3 * m + 1] : 0.0,
+                                (m < M && cfg->U && dims == 3) ? cfg->U[3 * m + 2] : 0.0 };
+                for (int i = 0; i < 3; ++i) S->disp_u[(m * Nt + j) * 3 + i] = (float)(dt[j] * U[i]);
+            }
+        }
+        free(dt); free(used); free(negl); free(posl);
+    }
+    return SSTMC_NO_ERROR;
+}
+
+/* ------------------------------------------------------------------ */
+/* FP32 walk (decision path)                                          */
+/* ------------------------------------------------------------------ */
+static inline int o_inside(const o_scene* S, const float p[3])
+{
+    int in = p[0] >= S->bmin[0] && p[0] <= S->bmax[0] && p[1] >= S->bmin[1] && p[1] <= S->bmax[1];
+    if (S->dims == 3) in = in && p[2] >= S->bmin[2] && p[2] <= S->bmax[2];
+    return in;
+}
+
+/* Cell c with ax[c] <= x < ax[c+1]; clamped to [0, n-2]
+ * (Simulation.cuh:325-367 binarySearchKernel, plus the clamp at the max edge). */
+static inline int o_bin(const float* ax, int n, float x)
+{
+    int lo = 0, hi = n; /* count of ax[k] <= x in [lo, hi] */
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (ax[mid] <= x) lo = mid + 1; else hi = mid;
+    }
+    int c = lo - 1;
+    if (c < 0) c = 0;
+    if (c > n - 2) c = n - 2;
+    return c;
+}
+
+static inline int o_cell(const o_scene* S, const float p[3])
+{
+    int ix = o_bin(S->ax[0], S->n[0], p[0]);
+    int iy = o_bin(S->ax[1], S->n[1], p[1]);
+    int idx = ix + iy * (S->n[0] - 1);
+    if (S->dims == 3) idx += o_bin(S->ax[2], S->n[2], p[2]) * (S->n[0] - 1) * (S->n[1] - 1);
+    return idx;
+}
+
+/* Does a ray from an outside point hit the box?  HeterogeneousMedium.cuh:269-383 (bdDistance). */
+static int o_points_toward(const o_scene* S, const float p[3], const float d[3])
+{
+    int D = S->dims;
+    float o[3], inv[3], dist[3];
+    float mx = 0.0f;
+    for (int i = 0; i < D; ++i) {
+        o[i] = p[i] - S->center[i];
+        float a = fabsf(o[i]) * S->inv_radius[i];
+        if (i == 0 || a > mx) mx = a;
+        inv[i] = fabsf(d[i]) < 1e-12f ? 1e12f : 1.0f / d[i];
+    }
+    float winding = mx <= 1.0f ? -1.0f : 1.0f;
+    for (int i = 0; i < D; ++i) {
+        float sg = d[i] < 0.0f ? 1.0f : -1.0f;
+        dist[i] = inv[i] * (S->radius[i] * (winding * sg) - o[i]);
+    }
+    for (int i = 0; i < D; ++i) {
+        if (!(dist[i] >= 0.0f)) continue;
+        int ok = 1;
+        for (int j = 0; j < D; ++j) {
+            if (j == i) continue;
+            if (!(fabsf(fmaf(d[j], dist[i], o[j])) < S->radius[j])) ok = 0;
+        }
+        if (ok) return 1;
+    }
+    return 0;
+}
+
+static inline void o_normalize32(int dims, const float v[3], float out[3])
+{
+    float s = dims == 3 ? fmaf(v[0], v[0], fmaf(v[1], v[1], v[2] * v[2])) : fmaf(v[0], v[0], v[1] * v[1]);
+    if (!(s > 0.0f)) {
+        out[0] = 0.0f; out[1] = dims == 3 ? 0.0f : 1.0f; out[2] = dims == 3 ? 1.0f : 0.0f;
+        return;
+    }
+    float inv = 1.0f / sqrtf(s);
+    out[0] = v[0] * inv; out[1] = v[1] * inv; out[2] = dims == 3 ? v[2] * inv : 0.0f;
+}
+
+static inline void o_random_direction(int dims, o_stream* rs, float out[3])
+{
+    if (dims == 2) {
+        float s, c;
+        o_sincospif(2.0f * o_uniform(rs), &s, &c);
+        out[0] = s; out[1] = c; out[2] = 0.0f;
+    } else {
+        float sp, cp;
+        o_sincospif(2.0f * o_uniform(rs), &sp, &cp);
+        float ct = fmaf(o_uniform(rs), 2.0f, -1.0f);
+        float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        out[0] = st * cp; out[1] = st * sp; out[2] = ct;
+    }
+}
+
+/* Scattering::newDirection: Scattering.cuh:1039-1115, VectorType.cuh:261-282. */
+static void o_sample_direction(const o_scene* S, int m, const float din[3], o_stream* rs, float out[3])
+{
+    int ty = S->scat_type[m];
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) { o_random_direction(S->dims, rs, out); return; }
+    float g = S->g_f[m];
+    float c;
+    if (fabsf(g) < 0.001f) {
+        c = o_uniform(rs) * 2.0f - 1.0f;
+    } else {
+        float xi = o_uniform(rs);
+        if (S->dims == 2) {
+            float a = (1.0f - g) / (1.0f + g);
+            float sp, cp;
+            o_sincospif(xi, &sp, &cp);
+            float s2 = sp * sp;
+            float ac = a * cp;
+            float ac2 = ac * ac;
+            c = (s2 - ac2) / (s2 + ac2);
+        } else {
+            float gg = g * g;
+            float s = (1.0f - gg) / fmaf(2.0f * g, xi, 1.0f - g);
+            c = ((1.0f + gg) - s * s) / (2.0f * g);
+        }
+    }
+    float sa = (o_uniform(rs) < 0.5f ? -1.0f : 1.0f) * sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    if (S->dims == 2) {
+        out[0] = din[0] * c - din[1] * sa;
+        out[1] = din[0] * sa + din[1] * c;
+        out[2] = 0.0f;
+    } else {
+        float sphi, cphi;
+        o_sincospif(2.0f * o_uniform(rs), &sphi, &cphi);
+        if (fabsf(din[2]) > 1.0f - 1e-6f) {
+            out[0] = sa * cphi; out[1] = sa * sphi; out[2] = c * (signbit(din[2]) ? -1.0f : 1.0f);
+        } else {
+            float st = sqrtf(1.0f - din[2] * din[2]);
+            float nx = (din[0] * din[2]) * cphi - din[1] * sphi;
+            float ny = (din[1] * din[2]) * cphi + din[0] * sphi;
+            out[0] = (sa * nx) / st + din[0] * c;
+            out[1] = (sa * ny) / st + din[1] * c;
+            out[2] = ((-sa) * cphi) * st + din[2] * c;
+        }
+    }
+}
+
+/* Woodcock free flight + absorption roulette: HeterogeneousMedium.cuh:576-678.
+ * Returns 0 and writes the new vertex (material 0 = left the medium or absorbed). */
+static int o_woodcock(const o_scene* S, const float o[3], const float d[3], o_stream* rs, float out[3], int* mat)
+{
+    float dist = 0.0f;
+    float p[3] = { o[0], o[1], o[2] };
+    int m = 0;
+    unsigned steps = 0;
+    for (;;) {
+        if (++steps > O_MAX_WOODCOCK) return SSTMC_PATH_LIMIT;
+        float u = o_uniform(rs);
+        dist = dist + (-o_logf(u)) * S->inv_maxsigt_f;
+        for (int i = 0; i < S->dims; ++i) p[i] = fmaf(dist, d[i], o[i]);
+        if (!o_inside(S, p)) {
+            if (!o_points_toward(S, p, d)) break;
+        } else {
+            m = S->grid[o_cell(S, p)];
+            if (o_uniform(rs) <= S->accept_f[m]) break;
+        }
+    }
+    out[0] = p[0]; out[1] = p[1]; out[2] = S->dims == 3 ? p[2] : 0.0f;
+    if (o_inside(S, p)) {
+        *mat = (o_uniform(rs) > S->survive_f[m]) ? 0 : m;
+    } else {
+        *mat = 0;
+    }
+    return 0;
+}
+
+/* First vertex source sampling: FarField.cuh:129-205, PointSource.cuh:72-90. */
+static void o_sample_source(const o_scene* S, const o_src* src, o_stream* rs, float x0[3], float d0[3])
+{
+    int D = S->dims;
+    int l = (int)ceilf(o_uniform(rs) * (float)src->n) - 1;
+    if (l < 0) l = 0;
+    if (l > src->n - 1) l = src->n - 1;
+    if (src->type == SSTMC_SOURCE_POINT) {
+        for (int i = 0; i < 3; ++i) x0[i] = src->p[3 * l + i];
+        o_random_direction(D, rs, d0);
+        return;
+    }
+    const float* dir = src->p + 3 * l;
+    float st = src->mint[l] + o_uniform(rs) * (src->maxt[l] - src->mint[l]);
+    float pt[3];
+    for (int i = 0; i < 3; ++i) pt[i] = src->tang[3 * l + i] + st * src->pt[3 * l + i];
+    if (D == 3) {
+        float ss = src->mins[l] + o_uniform(rs) * (src->maxs[l] - src->mins[l]);
+        for (int i = 0; i < 3; ++i) pt[i] = pt[i] + ss * src->ps[3 * l + i];
+    }
+    float sh[3], dist[3];
+    for (int i = 0; i < D; ++i) {
+        sh[i] = pt[i] - S->center[i];
+        float sg = dir[i] < 0.0f ? 1.0f : -1.0f;
+        dist[i] = src->inv[3 * l + i] * (S->radius[i] * sg - sh[i]);
+    }
+    float bd = 0.0f;
+    for (int i = 0; i < D; ++i) {
+        int ok = dist[i] >= 0.0f;
+        for (int j = 0; j < D && ok; ++j) {
+            if (j == i) continue;
+            if (!(fabsf(fmaf(dir[j], dist[i], sh[j])) < S->radius[j])) ok = 0;
+        }
+        if (ok) { bd = dist[i]; break; }
+    }
+    float step = bd + 1e-12f;
+    for (int i = 0; i < 3; ++i) { x0[i] = pt[i] + step * dir[i]; d0[i] = dir[i]; }
+    if (D == 2) { x0[2] = 0.0f; d0[2] = 0.0f; }
+}
+
+/* FP32 parametric voxel traversal: the decision path of
+ * HeterogeneousMedium.cuh:386-573; returns the number of voxel steps. */
+static uint32_t o_dda32(const o_scene* S, const float o[3], const float d[3], float* tau)
+{
+    int D = S->dims;
+    if (tau) *tau = 0.0f;
+    if (!o_inside(S, o)) return 0;
+    float inv[3], sg[3];
+    int bin[3];
+    for (int i = 0; i < D; ++i) {
+        inv[i] = fabsf(d[i]) < 1e-12f ? (d[i] >= 0.0f ? 1e12f : -1e12f) : 1.0f / d[i];
+        sg[i] = d[i] < 0.0f ? -1.0f : 1.0f;
+        bin[i] = o_bin(S->ax[i], S->n[i], o[i]);
+    }
+    float t = 0.0f, acc = 0.0f;
+    uint32_t steps = 0;
+    for (;;) {
+        float tn[3];
+        for (int i = 0; i < D; ++i) {
+            float face = S->ax[i][bin[i] + (sg[i] > 0.0f ? 1 : 0)];
+            tn[i] = (face - o[i]) * inv[i];
+        }
+        int a;
+        if (D == 2) a = tn[0] < tn[1] ? 0 : 1;
+        else a = (tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2);
+        int idx = bin[0] + bin[1] * (S->n[0] - 1);
+        if (D == 3) idx += bin[2] * (S->n[0] - 1) * (S->n[1] - 1);
+        acc = fmaf(tn[a] - t, S->sigt_f[S->grid[idx]], acc);
+        t = tn[a];
+        steps++;
+        if ((sg[a] < 0.0f && bin[a] == 0) || (sg[a] > 0.0f && bin[a] == S->n[a] - 2)) break;
+        bin[a] += sg[a] > 0.0f ? 1 : -1;
+    }
+    if (tau) *tau = acc;
+    return steps;
+}
+
+/* FP64 optical depth of the same ray (value path of the oracle). */
+static double o_tau64(const o_scene* S, const double o[3], const double d[3])
+{
+    int D = S->dims;
+    for (int i = 0; i < D; ++i) if (!(o[i] >= S->axd[i][0] && o[i] <= S->axd[i][S->n[i] - 1])) return 0.0;
+    double inv[3]; int sg[3], bin[3];
+    for (int i = 0; i < D; ++i) {
+        inv[i] = fabs(d[i]) < 1e-12 ? (d[i] >= 0.0 ? 1e12 : -1e12) : 1.0 / d[i];
+        sg[i] = d[i] < 0.0 ? -1 : 1;
+        int lo = 0, hi = S->n[i];
+        while (lo < hi) { int mid = (lo + hi) >> 1; if (S->axd[i][mid] <= o[i]) lo = mid + 1; else hi = mid; }
+        int c = lo - 1; if (c < 0) c = 0; if (c > S->n[i] - 2) c = S->n[i] - 2;
+        bin[i] = c;
+    }
+    double t = 0.0, acc = 0.0;
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+        double tn[3];
+        for (int i = 0; i < D; ++i) tn[i] = (S->axd[i][bin[i] + (sg[i] > 0 ? 1 : 0)] - o[i]) * inv[i];
+        int a;
+        if (D == 2) a = tn[0] < tn[1] ? 0 : 1;
+        else a = (tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2);
+        int idx = bin[0] + bin[1] * (S->n[0] - 1);
+        if (D == 3) idx += bin[2] * (S->n[0] - 1) * (S->n[1] - 1);
+        double seg = tn[a] - t;
+        if (seg > 0) acc += seg * (double)S->sigt_f[S->grid[idx]];
+        if (tn[a] > t) t = tn[a];
+        if ((sg[a] < 0 && bin[a] == 0) || (sg[a] > 0 && bin[a] == S->n[a] - 2)) break;
+        bin[a] += sg[a];
+    }
+    return acc;
+}
+
+/* Scattering::amplitude / pdf device implementations, Scattering.cuh:895-1023 (FP64). */
+static inline double o_amp(const o_scene* S, int m, double c)
+{
+    int ty = S->scat_type[m];
+    if (ty == SSTMC_SCATTERING_ISOTROPIC) return S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3;
+    if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
+        double dn = fma(S->gd2[m], c, S->gd1[m]);
+        return S->dims == 2 ? sqrt(S->gup[m] / dn) : sqrt(S->gup[m] / (dn * sqrt(dn)));
+    }
+    return 0.0;
+}
+
+static inline double o_pdf(const o_scene* S, int m, double c)
+{
+    int ty = S->scat_type[m];
+    if (ty == SSTMC_SCATTERING_ISOTROPIC) return S->dims == 2 ? O_ISO_PDF2 : O_ISO_PDF3;
+    if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
+        double dn = fma(S->gd2[m], c, S->gd1[m]);
+        return S->dims == 2 ? S->gup[m] / dn : S->gup[m] / (dn * sqrt(dn));
+    }
+    return 0.0;
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 NEE helpers                                                   */
+/* ------------------------------------------------------------------ */
+static inline void o_norm64(const double v[3], double out[3])
+{
+    double s = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    if (!(s > 0)) { out[0] = 0; out[1] = 0; out[2] = 1; return; }
+    double r = 1.0 / sqrt(s);
+    out[0] = v[0] * r; out[1] = v[1] * r; out[2] = v[2] * r;
+}
+
+static inline void o_dir64(const float a[3], const float b[3], double out[3]) /* normalize(b - a) */
+{
+    double v[3] = { (double)b[0] - a[0], (double)b[1] - a[1], (double)b[2] - a[2] };
+    o_norm64(v, out);
+}
+
+static inline double o_dot(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+static inline void o_cexp2pi(double ph, double* re, double* im)
+{
+    double f = ph - floor(ph);
+    *re = cos(2.0 * O_PI * f); *im = sin(2.0 * O_PI * f);
+}
+
+typedef struct { double re, im; } oc;
+static inline oc oc_mul(oc a, oc b) { oc r = { a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re }; return r; }
+static inline oc oc_conj(oc a) { oc r = { a.re, -a.im }; return r; }
+static inline oc oc_scale(oc a, double s) { oc r = { a.re * s, a.im * s }; return r; }
+
+typedef struct { float x[3]; int valid; oc g; uint64_t steps; } o_gmemo;
+
+/* Optical depth of one NEE ray from float point x along float dir df (FP32 steps
+ * counted; FP64 value). */
+static double o_ray(const o_scene* S, const float x[3], const float df[3], const double dd[3], uint64_t* steps)
+{
+    *steps += o_dda32(S, x, df, NULL);
+    double xd[3] = { x[0], x[1], x[2] };
+    return o_tau64(S, xd, dd);
+}
+
+/* First point probability term P_l(x): FarField.cuh:469-499, PointSource.cuh:92-115, 263-294. */
+static double o_pfirst(const o_scene* S, const o_src* s, int l, const float x[3], uint64_t* steps)
+{
+    if (s->type == SSTMC_SOURCE_FARFIELD) {
+        float df[3] = { -s->p[3 * l], -s->p[3 * l + 1], -s->p[3 * l + 2] };
+        double dd[3] = { df[0], df[1], df[2] };
+        return exp(-o_ray(S, x, df, dd, steps)) * s->sprob[l];
+    }
+    const float* sp = s->p + 3 * l;
+    float diff[3] = { sp[0] - x[0], sp[1] - x[1], sp[2] - x[2] };
+    float df[3]; o_normalize32(S->dims, diff, df);
+    double dd[3]; o_dir64(x, sp, dd);
+    double T = exp(-o_ray(S, x, df, dd, steps));
+    double v[3] = { (double)x[0] - sp[0], (double)x[1] - sp[1], (double)x[2] - sp[2] };
+    double r = sqrt(o_dot(v, v));
+    return S->dims == 3 ? T / (4.0 * O_PI * r * r) : T * (8.0 * O_PI) / r;
+}
+
+/* NEE vector g at x for source element k: FarField.cuh:223-263 (gDirectionKernel),
+ * PointSource.cuh:117-172 (gPointKernel).  role: 0 illumination, 1 view. */
+static oc o_g(const o_scene* S, const o_src* s, int k, const float x[3], int role, uint64_t* steps)
+{
+    oc g;
+    if (s->type == SSTMC_SOURCE_FARFIELD) {
+        const float* d = s->p + 3 * k;
+        float sgn = role == 0 ? -1.0f : 1.0f;
+        float df[3] = { sgn * d[0], sgn * d[1], sgn * d[2] };
+        double dd[3] = { df[0], df[1], df[2] };
+        double T = exp(-o_ray(S, x, df, dd, steps));
+        double dx = (double)d[0] * x[0] + (double)d[1] * x[1] + (double)d[2] * x[2];
+        double ph = (role == 0 ? 1.0 : -1.0) * dx / S->lambda;
+        double a = sqrt(T);
+        o_cexp2pi(ph, &g.re, &g.im);
+        g.re *= a; g.im *= a;
+        return g;
+    }
+    const float* sp = s->p + 3 * k;
+    float diff[3] = { sp[0] - x[0], sp[1] - x[1], sp[2] - x[2] };
+    float df[3]; o_normalize32(S->dims, diff, df);
+    double dd[3]; o_dir64(x, sp, dd);
+    double T = exp(-o_ray(S, x, df, dd, steps));
+    double v[3] = { (double)x[0] - sp[0], (double)x[1] - sp[1], (double)x[2] - sp[2] };
+    double r = sqrt(o_dot(v, v));
+    double at = S->dims == 3 ? T * O_ISO_AMP3 / (r * r) : T / r;
+    if (s->is_area) at *= (S->dims == 3 ? fabs(v[2]) : fabs(v[1])) / r;
+    double a = sqrt(at);
+    o_cexp2pi(r / S->lambda, &g.re, &g.im);
+    g.re *= a; g.im *= a;
+    return g;
+}
+
+/* Memoised o_g: the NEE vector is a pure function of (source slot, element,
+ * position); a tick-invariant vertex reuses it and its DDA step count. */
+static oc o_gm(const o_scene* S, o_gmemo* memo, const o_src* s, int k, const float x[3], int role, uint64_t* steps)
+{
+    o_gmemo* e = memo + k;
+    if (e->valid && e->x[0] == x[0] && e->x[1] == x[1] && e->x[2] == x[2]) {
+        *steps += e->steps;
+        return e->g;
+    }
+    uint64_t st = 0;
+    oc g = o_g(S, s, k, x, role, &st);
+    e->x[0] = x[0]; e->x[1] = x[1]; e->x[2] = x[2]; e->valid = 1; e->g = g; e->steps = st;
+    *steps += st;
+    return g;
+}
+
+/* Incoming direction from source element k to scatterer x (illumination side):
+ * far field d_k, point normalize(x - s_k).  For the view side the outgoing
+ * direction toward the view: far d_k, point normalize(s_k - x). */
+static void o_src_dir(const o_src* s, int k, const float x[3], int toward_source, double out[3])
+{
+    if (s->type == SSTMC_SOURCE_FARFIELD) {
+        out[0] = s->p[3 * k]; out[1] = s->p[3 * k + 1]; out[2] = s->p[3 * k + 2];
+        return;
+    }
+    if (toward_source) o_dir64(x, s->p + 3 * k, out);
+    else o_dir64(s->p + 3 * k, x, out);
+}
+
+/* Source -> scatterer a -> point b amplitude (threePointFunction):
+ * FarField.cuh:546-554, PointSource.cuh:317-345.  role 0 illumination, 1 view. */
+static double o_f3(const o_scene* S, const o_src* s, int k, const float a[3], const float b[3], int m, int role)
+{
+    double ab[3]; o_dir64(a, b, ab);
+    if (s->type == SSTMC_SOURCE_FARFIELD) {
+        double d[3] = { s->p[3 * k], s->p[3 * k + 1], s->p[3 * k + 2] };
+        double c = o_dot(d, ab);
+        return o_amp(S, m, role == 0 ? c : -c);
+    }
+    if (S->iso_all) return S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3;
+    double in[3]; o_dir64(s->p + 3 * k, a, in);
+    return o_amp(S, m, o_dot(in, ab));
+}
+
+/* Single-scattering amplitude illumination l -> x -> view v (threePointFunctionSingle):
+ * FarField.cuh:556-599, PointSource.cuh:347-405. */
+static double o_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v, const float x[3], int m)
+{
+    if (il->type == SSTMC_SOURCE_POINT && S->iso_all) return S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3;
+    double in[3], out[3];
+    if (il->type == SSTMC_SOURCE_FARFIELD) { in[0] = il->p[3 * l]; in[1] = il->p[3 * l + 1]; in[2] = il->p[3 * l + 2]; }
+    else o_dir64(il->p + 3 * l, x, in);
+    if (vw->type == SSTMC_SOURCE_FARFIELD) { out[0] = vw->p[3 * v]; out[1] = vw->p[3 * v + 1]; out[2] = vw->p[3 * v + 2]; }
+    else o_dir64(x, vw->p + 3 * v, out);
+    return o_amp(S, m, o_dot(in, out));
+}
+
+/* ------------------------------------------------------------------ */
+/* one path                                                           */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int cap, B;
+    float* x;     /* cap*3 */
+    int* m;
+    float* xi;
+    float* xt;    /* cap*Nt*3 (field) */
+} o_verts;
+
+static int o_verts_grow(o_verts* V, int Nt)
+{
+    int nc = V->cap ? V->cap * 2 : 64;
+    float* x = realloc(V->x, (size_t)nc * 3 * sizeof(float));
+    if (!x) return SSTMC_ALLOCATION_ERROR;
+    V->x = x;
+    int* m = realloc(V->m, (size_t)nc * sizeof(int));
+    if (!m) return SSTMC_ALLOCATION_ERROR;
+    V->m = m;
+    float* xi = realloc(V->xi, (size_t)nc * sizeof(float));
+    if (!xi) return SSTMC_ALLOCATION_ERROR;
+    V->xi = xi;
+    float* xt = realloc(V->xt, (size_t)nc * Nt * 3 * sizeof(float));
+    if (!xt) return SSTMC_ALLOCATION_ERROR;
+    V->xt = xt;
+    V->cap = nc;
+    return 0;
+}
+
+/* Per-tick positions of a vertex (field sampler): TemporalSampler.cuh:376-436, 540-647, 778-937. */
+static void o_temporal_positions(const o_scene* S, uint64_t seed, uint32_t pid, uint32_t b, const float x[3], int m, float* xt)
+{
+    int Nt = S->Nt;
+    if (!S->moving[m]) {
+        for (int t = 0; t < Nt; ++t) { xt[3 * t] = x[0]; xt[3 * t + 1] = x[1]; xt[3 * t + 2] = x[2]; }
+        return;
+    }
+    float cur[3] = { 0, 0, 0 };
+    float buf[3];
+    for (int j = 0; j < Nt; ++j) {
+        float sc = S->disp_scale[m * Nt + j];
+        const float* du = S->disp_u + (m * Nt + j) * 3;
+        float disp[3] = { du[0], du[1], du[2] };
+        if (sc != 0.0f) {
+            o_stream ts;
+            o_stream_init(&ts, seed, pid, b, O_PURPOSE_TEMPORAL | ((uint32_t)j << 8));
+            float w[3];
+            o_random_direction(S->dims, &ts, w);
+            float u1 = o_uniform(&ts), u2 = o_uniform(&ts);
+            float r = sqrtf(-2.0f * o_logf(u1));
+            float s, c;
+            o_sincospif(2.0f * u2, &s, &c);
+            float dr = (r * c) * sc;
+            for (int i = 0; i < S->dims; ++i) disp[i] = fmaf(dr, w[i], du[i]);
+        }
+        if (j == 0 || j == S->neg) { cur[0] = x[0]; cur[1] = x[1]; cur[2] = x[2]; }
+        for (int i = 0; i < S->dims; ++i) cur[i] = cur[i] + disp[i];
+        /* sorted index j -> output tick index */
+        int t = j < S->neg ? S->neg - 1 - j : j;
+        buf[0] = cur[0]; buf[1] = cur[1]; buf[2] = cur[2];
+        xt[3 * t] = buf[0]; xt[3 * t + 1] = buf[1]; xt[3 * t + 2] = buf[2];
+    }
+}
+
+/* Walk one path: vertices x_1..x_B.  Returns error code; misses counted. */
+static int o_walk(const o_scene* S, uint64_t seed, uint32_t pid, int u1side, o_verts* V, int* misses)
+{
+    const o_src* first = (S->correlation && !u1side) ? &S->src[2] : &S->src[0];
+    float x0[3], d0[3], x1[3];
+    int m1 = 0;
+    *misses = 0;
+    V->B = 0;
+    uint32_t att;
+    o_stream rs;
+    for (att = 0; att < O_MAX_ATTEMPTS; ++att) {
+        o_stream_init(&rs, seed, pid, 1u, O_PURPOSE_WALK | (att << 8));
+        o_sample_source(S, first, &rs, x0, d0);
+        int e = o_woodcock(S, x0, d0, &rs, x1, &m1);
+        if (e) return e;
+        if (m1 > 0) break;
+        (*misses)++;
+    }
+    if (att == O_MAX_ATTEMPTS) return SSTMC_PATH_LIMIT;
+    if (V->cap < 1 && o_verts_grow(V, S->Nt)) return SSTMC_ALLOCATION_ERROR;
+    V->x[0] = x1[0]; V->x[1] = x1[1]; V->x[2] = x1[2]; V->m[0] = m1;
+    V->xi[0] = S->correlation ? 0.0f : o_uniform(&rs);
+    if (!S->correlation) o_temporal_positions(S, seed, pid, 1u, x1, m1, V->xt);
+    V->B = 1;
+    float prev[3] = { x0[0], x0[1], x0[2] };
+    for (uint32_t b = 1; ; ++b) {
+        if (b >= O_MAX_VERTICES) return SSTMC_PATH_LIMIT;
+        const float* cur = V->x + 3 * (b - 1);
+        int mb = V->m[b - 1];
+        o_stream_init(&rs, seed, pid, b + 1, O_PURPOSE_WALK);
+        float diff[3] = { cur[0] - prev[0], cur[1] - prev[1], cur[2] - prev[2] };
+        float din[3]; o_normalize32(S->dims, diff, din);
+        float nd[3]; o_sample_direction(S, mb, din, &rs, nd);
+        float xn[3]; int mn = 0;
+        int e = o_woodcock(S, cur, nd, &rs, xn, &mn);
+        if (e) return e;
+        if (mn == 0) break;
+        if ((int)b >= V->cap && o_verts_grow(V, S->Nt)) return SSTMC_ALLOCATION_ERROR;
+        cur = V->x + 3 * (b - 1);
+        prev[0] = cur[0]; prev[1] = cur[1]; prev[2] = cur[2];
+        V->x[3 * b] = xn[0]; V->x[3 * b + 1] = xn[1]; V->x[3 * b + 2] = xn[2];
+        V->m[b] = mn;
+        V->xi[b] = S->correlation ? 0.0f : o_uniform(&rs);
+        if (!S->correlation) o_temporal_positions(S, seed, pid, b + 1, xn, mn, V->xt + (size_t)b * S->Nt * 3);
+        V->B = (int)b + 1;
+    }
+    return 0;
+}
+
+static uint32_t o_vertex_hash(const o_scene* S, const o_verts* V)
+{
+    uint32_t h = 2166136261u;
+    for (int b = 0; b < V->B; ++b) {
+        h = o_hash_mix(h, o_f2u(V->x[3 * b]));
+        h = o_hash_mix(h, o_f2u(V->x[3 * b + 1]));
+        if (S->dims == 3) h = o_hash_mix(h, o_f2u(V->x[3 * b + 2]));
+        h = o_hash_mix(h, (uint32_t)V->m[b]);
+    }
+    return h;
+}
+
+/* correlation sampler shift x + h*U(m), h = -/+ tau/2 (TemporalSamplerCorrelation.cuh:229-255) */
+static inline void o_shift(const o_scene* S, const float x[3], int m, float tau, float sign, float out[3])
+{
+    float h = tau * (0.5f * sign);
+    out[0] = fmaf(h, S->U_f[m][0], x[0]);
+    out[1] = fmaf(h, S->U_f[m][1], x[1]);
+    out[2] = S->dims == 3 ? fmaf(h, S->U_f[m][2], x[2]) : 0.0f;
+}
+
+typedef struct {
+    o_gmemo* memo[4];                 /* per source slot: last NEE vector of each element */
+    oc *a_ms, *s_ms, *a_ss, *b_ss;   /* [Nt][Nl] / [Nt][Nv] */
+    oc *gl1, *gl2;                    /* [Nt][Nl] illumination NEE vectors at x1 */
+    double* P1; double* P2;           /* [Nl] */
+} o_work;
+
+/* Evaluate the NEE vectors of one walked path and accumulate into V (if not NULL).
+ * Field mode: NextEventEstimation.cuh:1016-1136 (single), 1138-1458 (multiple).
+ * Correlation mode: the same, with TemporalSamplerCorrelation.cuh and
+ * SourceInterface.cuh:220-354 temporal factors. */
+static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint64_t* steps)
+{
+    int Nl = S->src[0].n, Nv = S->src[1].n, Nt = S->Nt, B = V->B, D = S->dims;
+    const o_src *il = &S->src[0], *vw = &S->src[1], *il2 = &S->src[2], *vw2 = &S->src[3];
+    const float* x1 = V->x;
+    int m1 = V->m[0];
+    double k2 = (2.0 * O_PI / S->lambda) * (2.0 * O_PI / S->lambda);
+    memset(W->a_ms, 0, sizeof(oc) * Nt * Nl); memset(W->s_ms, 0, sizeof(oc) * Nt * Nv);
+
+    if (!S->correlation) {
+        double p1 = 0;
+        for (int l = 0; l < Nl; ++l) { W->P1[l] = o_pfirst(S, il, l, x1, steps); p1 += W->P1[l]; }
+        p1 = p1 / Nl;
+        double sq1 = sqrt(p1);
+        oc e1; o_cexp2pi((double)V->xi[0], &e1.re, &e1.im);
+        for (int t = 0; t < Nt; ++t) {
+            const float* x1t = V->xt + 3 * t;
+            for (int l = 0; l < Nl; ++l) {
+                W->gl1[t * Nl + l] = o_gm(S, W->memo[0], il, l, x1t, 0, steps);
+                W->a_ss[t * Nl + l] = oc_scale(oc_mul(W->gl1[t * Nl + l], e1), 1.0 / sq1);
+            }
+            for (int v = 0; v < Nv; ++v) W->b_ss[t * Nv + v] = o_gm(S, W->memo[1], vw, v, x1t, 1, steps);
+        }
+        if (Vacc) {
+            for (int t = 0; t < Nt; ++t) {
+                const float* pos = S->temporal_amp ? V->xt + 3 * t : x1;
+                for (int v = 0; v < Nv; ++v) for (int l = 0; l < Nl; ++l) {
+                    double w = o_fs(S, il, l, vw, v, pos, m1);
+                    oc c = oc_scale(oc_mul(W->a_ss[t * Nl + l], W->b_ss[t * Nv + v]), w);
+                    oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
+                    dst->re += c.re; dst->im += c.im;
+                }
+            }
+        }
+        if (B < 2) return;
+        const float* x2 = V->x + 3;
+        double x12[3]; o_dir64(x1, x2, x12);
+        double p2 = 0;
+        for (int l = 0; l < Nl; ++l) {
+            double in[3]; o_src_dir(il, l, x1, 0, in);
+            p2 += W->P1[l] * o_pdf(S, m1, o_dot(in, x12));
+        }
+        p2 = p2 / Nl;
+        double sq2 = sqrt(p2);
+        for (int t = 0; t < Nt; ++t) {
+            const float* pa = S->temporal_amp ? V->xt + 3 * t : x1;
+            const float* pb = S->temporal_amp ? V->xt + (size_t)Nt * 3 + 3 * t : x2;
+            for (int l = 0; l < Nl; ++l)
+                W->a_ms[t * Nl + l] = oc_scale(W->gl1[t * Nl + l], o_f3(S, il, l, pa, pb, m1, 0) / sq2);
+        }
+        for (int t = 0; t < Nt; ++t) {
+            double L = 0;
+            for (int b = 1; b < B; ++b) {
+                const float* xa = V->xt + ((size_t)(b - 1) * Nt + t) * 3;
+                const float* xb = V->xt + ((size_t)b * Nt + t) * 3;
+                double dv[3] = { (double)xb[0] - xa[0], (double)xb[1] - xa[1], (double)xb[2] - xa[2] };
+                L += sqrt(o_dot(dv, dv));
+                const float* pa = S->temporal_amp ? xb : V->x + 3 * b;
+                const float* pb = S->temporal_amp ? xa : V->x + 3 * (b - 1);
+                oc ph; o_cexp2pi(L / S->lambda + (double)V->xi[b], &ph.re, &ph.im);
+                for (int v = 0; v < Nv; ++v) {
+                    oc g = o_gm(S, W->memo[1], vw, v, xb, 1, steps);
+                    double f = o_f3(S, vw, v, pa, pb, V->m[b], 1);
+                    oc c = oc_scale(oc_mul(g, ph), f);
+                    W->s_ms[t * Nv + v].re += c.re; W->s_ms[t * Nv + v].im += c.im;
+                }
+            }
+        }
+    } else {
+        double p1 = 0;
+        for (int l = 0; l < Nl; ++l) {
+            double a = o_pfirst(S, il, l, x1, steps), b2 = o_pfirst(S, il2, l, x1, steps);
+            W->P1[l] = 0.5 * (a + b2);
+            p1 += W->P1[l];
+        }
+        p1 = p1 / Nl;
+        for (int t = 0; t < Nt; ++t) {
+            float tau = S->ticks_f[t];
+            float xm[3], xp[3];
+            o_shift(S, x1, m1, tau, -1.0f, xm); o_shift(S, x1, m1, tau, 1.0f, xp);
+            for (int l = 0; l < Nl; ++l) {
+                oc g1 = o_gm(S, W->memo[0], il, l, xm, 0, steps), g2 = o_gm(S, W->memo[2], il2, l, xp, 0, steps);
+                W->gl1[t * Nl + l] = g1; W->gl2[t * Nl + l] = g2;
+                W->a_ss[t * Nl + l] = oc_scale(oc_mul(g1, oc_conj(g2)), 1.0 / p1);
+            }
+            for (int v = 0; v < Nv; ++v) {
+                oc g1 = o_gm(S, W->memo[1], vw, v, xm, 1, steps), g2 = o_gm(S, W->memo[3], vw2, v, xp, 1, steps);
+                W->b_ss[t * Nv + v] = oc_mul(g1, oc_conj(g2));
+            }
+        }
+        int scalarFs = il->type == SSTMC_SOURCE_POINT && vw->type == SSTMC_SOURCE_POINT && S->iso_all;
+        if (Vacc) {
+            for (int t = 0; t < Nt; ++t) {
+                float xm[3]; o_shift(S, x1, m1, S->ticks_f[t], -1.0f, xm);
+                double dtD = k2 * fabs(S->D[m1] * S->ticks[t]);
+                for (int v = 0; v < Nv; ++v) {
+                    double o1[3], o2[3];
+                    o_src_dir(vw, v, x1, 1, o1); o_src_dir(vw2, v, x1, 1, o2);
+                    for (int l = 0; l < Nl; ++l) {
+                        double w;
+                        if (scalarFs) {
+                            w = (D == 2 ? O_ISO_AMP2 : O_ISO_AMP3) * (D == 2 ? O_ISO_AMP2 : O_ISO_AMP3);
+                        } else {
+                            double in1[3], in2[3];
+                            o_src_dir(il, l, x1, 0, in1); o_src_dir(il2, l, x1, 0, in2);
+                            double q[3];
+                            for (int i = 0; i < 3; ++i) q[i] = 0.5 * (in1[i] + in2[i] - o1[i] - o2[i]);
+                            w = o_fs(S, il, l, vw, v, xm, m1) * o_fs(S, il2, l, vw2, v, xm, m1) * exp(-dtD * o_dot(q, q));
+                        }
+                        oc c = oc_scale(oc_mul(W->a_ss[t * Nl + l], W->b_ss[t * Nv + v]), w);
+                        oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
+                        dst->re += c.re; dst->im += c.im;
+                    }
+                }
+            }
+        }
+        if (B < 2) return;
+        const float* x2 = V->x + 3;
+        int m2 = V->m[1];
+        double x12[3]; o_dir64(x1, x2, x12);
+        double p2 = 0;
+        for (int l = 0; l < Nl; ++l) {
+            double in[3]; o_src_dir(il, l, x1, 0, in);
+            p2 += W->P1[l] * o_pdf(S, m1, o_dot(in, x12));
+        }
+        p2 = p2 / Nl;
+        for (int t = 0; t < Nt; ++t) {
+            float tau = S->ticks_f[t];
+            float pa[3], pb[3];
+            o_shift(S, x1, m1, tau, -1.0f, pa); o_shift(S, x2, m2, tau, -1.0f, pb);
+            double dtD = k2 * fabs(S->D[m1] * S->ticks[t]);
+            for (int l = 0; l < Nl; ++l) {
+                oc g1 = W->gl1[t * Nl + l], g2 = W->gl2[t * Nl + l];
+                double f1 = o_f3(S, il, l, pa, pb, m1, 0), f2 = o_f3(S, il2, l, pa, pb, m1, 0);
+                double in1[3], in2[3], q[3];
+                o_src_dir(il, l, x1, 0, in1); o_src_dir(il2, l, x1, 0, in2);
+                for (int i = 0; i < 3; ++i) q[i] = 0.5 * (in1[i] + in2[i]) - x12[i];
+                double c1 = exp(-dtD * o_dot(q, q));
+                oc a = oc_mul(oc_scale(g1, f1 / p2), oc_conj(oc_scale(g2, f2)));
+                W->a_ms[t * Nl + l] = oc_scale(a, c1);
+            }
+        }
+        double MT = 0;
+        for (int b = 1; b < B; ++b) {
+            const float* xb = V->x + 3 * b;
+            const float* xa = V->x + 3 * (b - 1);
+            int mb = V->m[b], ma = V->m[b - 1];
+            if (b >= 2) {
+                double u[3], w[3];
+                o_dir64(V->x + 3 * (b - 2), xa, u); o_dir64(xa, xb, w);
+                double q[3] = { u[0] - w[0], u[1] - w[1], u[2] - w[2] };
+                MT += S->D[ma] * o_dot(q, q);
+            }
+            double back[3]; o_dir64(xb, xa, back);
+            for (int t = 0; t < Nt; ++t) {
+                float tau = S->ticks_f[t];
+                float xm[3], xp[3], pa[3], pb[3];
+                o_shift(S, xb, mb, tau, -1.0f, xm); o_shift(S, xb, mb, tau, 1.0f, xp);
+                o_shift(S, xb, mb, tau, -1.0f, pa); o_shift(S, xa, ma, tau, -1.0f, pb);
+                double pt = exp(-k2 * fabs(S->ticks[t]) * MT);
+                double dtD = k2 * fabs(S->D[mb] * S->ticks[t]);
+                for (int v = 0; v < Nv; ++v) {
+                    oc g1 = o_gm(S, W->memo[1], vw, v, xm, 1, steps), g2 = o_gm(S, W->memo[3], vw2, v, xp, 1, steps);
+                    double f1 = o_f3(S, vw, v, pa, pb, mb, 1), f2 = o_f3(S, vw2, v, pa, pb, mb, 1);
+                    double o1[3], o2[3], q[3];
+                    o_src_dir(vw, v, xb, 1, o1); o_src_dir(vw2, v, xb, 1, o2);
+                    for (int i = 0; i < 3; ++i) q[i] = 0.5 * (-o1[i] - o2[i]) - back[i];
+                    double c1 = exp(-dtD * o_dot(q, q));
+                    oc c = oc_mul(oc_scale(g1, f1 * pt), oc_conj(oc_scale(g2, f2)));
+                    c = oc_scale(c, c1);
+                    W->s_ms[t * Nv + v].re += c.re; W->s_ms[t * Nv + v].im += c.im;
+                }
+            }
+        }
+    }
+    if (Vacc) {
+        for (int t = 0; t < Nt; ++t)
+            for (int v = 0; v < Nv; ++v) {
+                oc s = W->s_ms[t * Nv + v];
+                for (int l = 0; l < Nl; ++l) {
+                    oc c = oc_mul(W->a_ms[t * Nl + l], s);
+                    oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
+                    dst->re += c.re; dst->im += c.im;
+                }
+            }
+    }
+}
+
+static int o_work_alloc(const o_scene* S, o_work* W)
+{
+    int Nl = S->src[0].n, Nv = S->src[1].n, Nt = S->Nt;
+    W->a_ms = calloc((size_t)Nt * Nl, sizeof(oc)); W->a_ss = calloc((size_t)Nt * Nl, sizeof(oc));
+    W->s_ms = calloc((size_t)Nt * Nv, sizeof(oc)); W->b_ss = calloc((size_t)Nt * Nv, sizeof(oc));
+    for (int i = 0; i < 4; ++i) W->memo[i] = calloc(S->src[i].n > 0 ? (size_t)S->src[i].n : 1, sizeof(o_gmemo));
+    for (int i = 0; i < 4; ++i) if (!W->memo[i]) return SSTMC_ALLOCATION_ERROR;
+    W->gl1 = calloc((size_t)Nt * Nl, sizeof(oc)); W->gl2 = calloc((size_t)Nt * Nl, sizeof(oc));
+    W->P1 = calloc(Nl, sizeof(double)); W->P2 = calloc(Nl, sizeof(double));
+    return (W->a_ms && W->a_ss && W->s_ms && W->b_ss && W->gl1 && W->gl2 && W->P1 && W->P2) ? 0 : SSTMC_ALLOCATION_ERROR;
+}
+
+static void o_work_free(o_work* W)
+{
+    for (int i = 0; i < 4; ++i) free(W->memo[i]);
+    free(W->a_ms); free(W->a_ss); free(W->s_ms); free(W->b_ss); free(W->gl1); free(W->gl2); free(W->P1); free(W->P2);
+}
+
+/* correlation u1/u2 split of a wave: TemporalSamplerCorrelation.cuh:369-372, 611-656 */
+static uint32_t o_u1_count(const o_scene* S, uint64_t seed, uint32_t wave)
+{
+    o_stream ws;
+    o_stream_init(&ws, seed, wave, 0u, O_PURPOSE_WAVE);
+    int c = (int)ceilf(o_uniform(&ws) * (float)(S->P + 1u)) - 1;
+    if (c < 0) c = 0;
+    if (c > (int)S->P) c = (int)S->P;
+    return (uint32_t)c;
+}
+
+/* ------------------------------------------------------------------ */
+/* API                                                                */
+/* ------------------------------------------------------------------ */
+int32_t oracle_render(const sstmc_config* cfg, uint64_t seed, uint32_t first_wave,
+                      uint32_t waves, int32_t threads, double* u_out, double* iter_out, uint64_t* stats)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (err) { o_free_scene(&S); return err; }
+    int Nl = S.src[0].n, Nv = S.src[1].n, Nt = S.Nt;
+    size_t nout = (size_t)Nl * Nv * Nt;
+#ifdef _OPENMP
+    int nthr = threads > 0 ? threads : omp_get_max_threads();
+#else
+    int nthr = 1;
+    (void)threads;
+#endif
+    oc* part = calloc(nout * (size_t)nthr, sizeof(oc));
+    uint64_t* st = calloc((size_t)nthr * 5, sizeof(uint64_t));
+    int* errs = calloc(nthr, sizeof(int));
+    if (!part || !st || !errs) { free(part); free(st); free(errs); o_free_scene(&S); return SSTMC_ALLOCATION_ERROR; }
+    uint64_t total = (uint64_t)waves * S.P;
+#pragma omp parallel num_threads(nthr)
+    {
+#ifdef _OPENMP
+        int tid = omp_get_thread_num();
+#else
+        int tid = 0;
+#endif
+        o_verts V; memset(&V, 0, sizeof(V));
+        o_work W;
+        int e = o_work_alloc(&S, &W);
+        if (!e) e = o_verts_grow(&V, Nt);
+        if (e) errs[tid] = e;
+        oc* acc = part + nout * (size_t)tid;
+        uint64_t* sst = st + 5 * tid;
+#pragma omp for schedule(static)
+        for (int64_t q = 0; q < (int64_t)total; ++q) {
+            if (errs[tid]) continue;
+            uint32_t wave = first_wave + (uint32_t)(q / S.P);
+            uint32_t slot = (uint32_t)(q % S.P);
+            uint32_t pid = wave * S.P + slot;
+            int u1side = 1;
+            if (S.correlation) u1side = slot < o_u1_count(&S, seed, wave);
+            int misses = 0;
+            int we = o_walk(&S, seed, pid, u1side, &V, &misses);
+            if (we) { errs[tid] = we; continue; }
+            uint64_t steps = 0;
+            o_nee(&S, &V, &W, acc, &steps);
+            sst[0] += (uint64_t)V.B * Nl * Nv * Nt;
+            sst[1] += steps;
+            sst[2] += (uint64_t)V.B;
+            sst[3] += 1;
+            sst[4] += (uint64_t)misses;
+        }
+        o_work_free(&W);
+        free(V.x); free(V.m); free(V.xi); free(V.xt);
+    }
+    for (int t = 0; t < nthr; ++t) if (errs[t]) { err = errs[t]; break; }
+    if (!err) {
+        for (size_t i = 0; i < nout; ++i) {
+            double re = 0, im = 0;
+            for (int t = 0; t < nthr; ++t) { re += part[nout * t + i].re; im += part[nout * t + i].im; }
+            u_out[2 * i] = re; u_out[2 * i + 1] = im;
+        }
+        uint64_t misses = 0, agg[4] = { 0, 0, 0, 0 };
+        for (int t = 0; t < nthr; ++t) { for (int k = 0; k < 4; ++k) agg[k] += st[5 * t + k]; misses += st[5 * t + 4]; }
+        if (iter_out) *iter_out = (double)total + (double)misses;
+        if (stats) for (int k = 0; k < 4; ++k) stats[k] = agg[k];
+    }
+    free(part); free(st); free(errs);
+    o_free_scene(&S);
+    return err;
+}
+
+int32_t oracle_trace_paths(const sstmc_config* cfg, uint64_t seed, uint32_t first_path,
+                           uint32_t paths, sstmc_path_trace* out)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (err) { o_free_scene(&S); return err; }
+    int Nl = S.src[0].n, Nv = S.src[1].n, Nt = S.Nt;
+    o_verts V; memset(&V, 0, sizeof(V));
+    o_work W;
+    err = o_work_alloc(&S, &W);
+    if (!err) err = o_verts_grow(&V, Nt);
+    for (uint32_t i = 0; i < paths && !err; ++i) {
+        uint32_t pid = first_path + i;
+        uint32_t wave = pid / S.P, slot = pid % S.P;
+        int u1side = 1;
+        if (S.correlation) u1side = slot < o_u1_count(&S, seed, wave);
+        int misses = 0;
+        err = o_walk(&S, seed, pid, u1side, &V, &misses);
+        if (err) break;
+        uint64_t steps = 0;
+        o_nee(&S, &V, &W, NULL, &steps);
+        if (out->misses) out->misses[i] = misses;
+        if (out->vertices) out->vertices[i] = V.B;
+        if (out->vertex_hash) out->vertex_hash[i] = o_vertex_hash(&S, &V);
+        if (out->dda_steps) out->dda_steps[i] = (uint32_t)steps;
+        if (out->x1) for (int k = 0; k < 3; ++k) out->x1[3 * i + k] = V.x[k];
+        if (out->m1) out->m1[i] = V.m[0];
+        for (int t = 0; t < Nt; ++t) {
+            for (int l = 0; l < Nl; ++l) {
+                size_t o = (((size_t)i * Nt + t) * Nl + l) * 2;
+                if (out->a_ms) { out->a_ms[o] = W.a_ms[t * Nl + l].re; out->a_ms[o + 1] = W.a_ms[t * Nl + l].im; }
+                if (out->a_ss) { out->a_ss[o] = W.a_ss[t * Nl + l].re; out->a_ss[o + 1] = W.a_ss[t * Nl + l].im; }
+            }
+            for (int v = 0; v < Nv; ++v) {
+                size_t o = (((size_t)i * Nt + t) * Nv + v) * 2;
+                if (out->s_ms) { out->s_ms[o] = W.s_ms[t * Nv + v].re; out->s_ms[o + 1] = W.s_ms[t * Nv + v].im; }
+                if (out->b_ss) { out->b_ss[o] = W.b_ss[t * Nv + v].re; out->b_ss[o + 1] = W.b_ss[t * Nv + v].im; }
+            }
+        }
+    }
+    o_work_free(&W);
+    free(V.x); free(V.m); free(V.xi); free(V.xt);
+    o_free_scene(&S);
+    return err;
+}
+
+int32_t oracle_dda(const sstmc_config* cfg, const float* o, const float* d, double* tau32, double* tau64)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (err) { o_free_scene(&S); return -err; }
+    float o3[3] = { o[0], o[1], S.dims == 3 ? o[2] : 0.0f }, d3[3] = { d[0], d[1], S.dims == 3 ? d[2] : 0.0f };
+    float t32 = 0;
+    uint32_t steps = o_dda32(&S, o3, d3, &t32);
+    double od[3] = { o3[0], o3[1], o3[2] }, dd[3] = { d3[0], d3[1], d3[2] };
+    if (tau32) *tau32 = t32;
+    if (tau64) *tau64 = o_tau64(&S, od, dd);
+    o_free_scene(&S);
+    return (int32_t)steps;
+}
+
+int32_t oracle_phase(const sstmc_config* cfg, int32_t m, double c, double* amp, double* pdf)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (!err) {
+        if (amp) *amp = o_amp(&S, m, c);
+        if (pdf) *pdf = o_pdf(&S, m, c);
+    }
+    o_free_scene(&S);
+    return err;
+}
+
+int32_t oracle_sample_cos(const sstmc_config* cfg, int32_t m, uint64_t seed, uint32_t n, float* out)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (!err) {
+        float din[3] = { 0.0f, S.dims == 2 ? 1.0f : 0.0f, S.dims == 3 ? 1.0f : 0.0f };
+        for (uint32_t i = 0; i < n; ++i) {
+            o_stream rs;
+            o_stream_init(&rs, seed, i, 0u, O_PURPOSE_WALK);
+            float nd[3];
+            o_sample_direction(&S, m, din, &rs, nd);
+            out[i] = S.dims == 2 ? nd[1] : nd[2];
+        }
+    }
+    o_free_scene(&S);
+    return err;
+}
+
+float oracle_logf(float x) { return o_logf(x); }
+void oracle_sincospif(float x, float* s, float* c) { o_sincospif(x, s, c); }
+void oracle_philox(const uint32_t key[2], const uint32_t ctr[4], uint32_t out[4]) { o_philox(key, ctr, out); }

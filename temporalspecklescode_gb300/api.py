@@ -1,0 +1,173 @@
+"""Python host API over the C-ABI (include/sstmc.h).
+
+``sstmc2D(config)`` / ``sstmc3D(config)`` return ``(u, iter)`` like the
+reference's MEX functions (README.md:355-373, MatlabInterface.cu:1565-1825):
+``u`` complex, shape (Nl, Nv, Nt, renderingsNum); ``iter`` shape
+(renderingsNum,), with ``iter[r] = batchSize * fullIteration + missed first
+vertices``.  Normalise a field by ``sqrt(iter)`` and a correlation by ``iter``.
+
+The CUDA library must be built (``__graft_entry__.build()``); there is no CPU
+fallback: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Any, Dict, Optional, Tuple
+
+import numpy as np
+
+from . import _build
+from . import config as cf
+
+_LIB: Optional[C.CDLL] = None
+
+
+class SstmcError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"sstmc error {code}: {what}")
+
+
+def load_library() -> C.CDLL:
+    """Load the in-tree CUDA library; raise if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.lib_path()
+    if not os.path.exists(path):
+        raise ImportError(f"{path} not found: build the CUDA library first (__graft_entry__.build())")
+    lib = C.CDLL(path)
+    i32, u32, u64, vp = C.c_int32, C.c_uint32, C.c_uint64, C.c_void_p
+    dp = C.POINTER(C.c_double)
+    lib.sstmc_config_init.argtypes = [C.POINTER(cf.SstmcConfig)]
+    lib.sstmc_config_init.restype = None
+    lib.sstmc_scene_create.argtypes = [C.POINTER(cf.SstmcConfig), C.POINTER(vp)]
+    lib.sstmc_scene_create.restype = i32
+    lib.sstmc_scene_shape.argtypes = [vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]
+    lib.sstmc_scene_shape.restype = i32
+    lib.sstmc_render.argtypes = [vp, u64, dp, dp]
+    lib.sstmc_render.restype = i32
+    lib.sstmc_last_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
+    lib.sstmc_last_stats.restype = i32
+    lib.sstmc_last_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(u64)]
+    lib.sstmc_last_timing.restype = i32
+    lib.sstmc_scene_destroy.argtypes = [vp]
+    lib.sstmc_scene_destroy.restype = i32
+    lib.sstmc_error_string.argtypes = [i32]
+    lib.sstmc_error_string.restype = C.c_char_p
+    lib.sstmc_last_error_text.argtypes = []
+    lib.sstmc_last_error_text.restype = C.c_char_p
+    lib.sstmc_trace_paths.argtypes = [vp, u64, u32, u32, C.POINTER(cf.PathTrace)]
+    lib.sstmc_trace_paths.restype = i32
+    _LIB = lib
+    return lib
+
+
+def error_string(code: int) -> str:
+    return load_library().sstmc_error_string(code).decode()
+
+
+def _check(code: int, extra: str = "") -> None:
+    if code != 0:
+        msg = error_string(code)
+        raise SstmcError(code, msg + (f" ({extra})" if extra else ""))
+
+
+class Scene:
+    """A device-resident scene (the objects mexFunction builds, MatlabInterface.cu:1677-1700)."""
+
+    def __init__(self, config: Dict[str, Any], dims: int, precision: int = cf.PRECISION_SPLIT):
+        self.lib = load_library()
+        self.prepared = cf.prepare(config, dims, precision)
+        self.meta = self.prepared.meta
+        h = C.c_void_p()
+        code = self.lib.sstmc_scene_create(self.prepared.ptr(), C.byref(h))
+        if code != 0:
+            detail = self.lib.sstmc_last_error_text().decode()
+            raise SstmcError(code, error_string(code) + (f": {detail}" if detail else ""))
+        self.handle = h
+        nl, nv, nt = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(self.lib.sstmc_scene_shape(h, C.byref(nl), C.byref(nv), C.byref(nt)))
+        self.Nl, self.Nv, self.Nt = nl.value, nv.value, nt.value
+        self.renders = self.meta["R"]
+
+    def render(self, seed: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray]:
+        seed = self.prepared.struct.seed if seed is None else int(seed)
+        n = self.Nl * self.Nv * self.Nt
+        u = np.zeros(2 * n * self.renders, dtype=np.float64)
+        it = np.zeros(self.renders, dtype=np.float64)
+        code = self.lib.sstmc_render(self.handle, C.c_uint64(seed), u.ctypes.data_as(C.POINTER(C.c_double)),
+                                     it.ctypes.data_as(C.POINTER(C.c_double)))
+        _check(code)
+        uc = (u[0::2] + 1j * u[1::2]).reshape(self.renders, self.Nt, self.Nv, self.Nl)
+        return np.transpose(uc, (3, 2, 1, 0)), it
+
+    def stats(self) -> Dict[str, int]:
+        v = [C.c_uint64() for _ in range(4)]
+        _check(self.lib.sstmc_last_stats(self.handle, *[C.byref(x) for x in v]))
+        return {"contributions": v[0].value, "dda_steps": v[1].value, "vertices": v[2].value, "paths": v[3].value}
+
+    def timing(self) -> Dict[str, float]:
+        ms = (C.c_double * 4)()
+        n = C.c_uint64()
+        _check(self.lib.sstmc_last_timing(self.handle, ms, C.byref(n)))
+        return {"ms_total": ms[0], "ms_trace": ms[1], "ms_contract_ms": ms[2], "ms_contract_ss": ms[3], "launches": n.value}
+
+    def trace_paths(self, seed: int, first_path: int, paths: int) -> Dict[str, np.ndarray]:
+        """Per-path quantities of paths [first_path, first_path + paths) (parity tests)."""
+        out, tr = _alloc_trace(paths, self.Nl, self.Nv, self.Nt)
+        _check(self.lib.sstmc_trace_paths(self.handle, C.c_uint64(seed), C.c_uint32(first_path), C.c_uint32(paths), C.byref(tr)))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.sstmc_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _alloc_trace(paths: int, Nl: int, Nv: int, Nt: int):
+    out = {
+        "misses": np.zeros(paths, np.int32), "vertices": np.zeros(paths, np.int32),
+        "vertex_hash": np.zeros(paths, np.uint32), "dda_steps": np.zeros(paths, np.uint32),
+        "x1": np.zeros((paths, 3), np.float32), "m1": np.zeros(paths, np.int32),
+        "a_ms": np.zeros((paths, Nt, Nl, 2)), "s_ms": np.zeros((paths, Nt, Nv, 2)),
+        "a_ss": np.zeros((paths, Nt, Nl, 2)), "b_ss": np.zeros((paths, Nt, Nv, 2)),
+    }
+    tr = cf.PathTrace()
+    tr.misses = out["misses"].ctypes.data_as(C.POINTER(C.c_int32))
+    tr.vertices = out["vertices"].ctypes.data_as(C.POINTER(C.c_int32))
+    tr.vertex_hash = out["vertex_hash"].ctypes.data_as(C.POINTER(C.c_uint32))
+    tr.dda_steps = out["dda_steps"].ctypes.data_as(C.POINTER(C.c_uint32))
+    tr.x1 = out["x1"].ctypes.data_as(C.POINTER(C.c_float))
+    tr.m1 = out["m1"].ctypes.data_as(C.POINTER(C.c_int32))
+    for k in ("a_ms", "s_ms", "a_ss", "b_ss"):
+        setattr(tr, k, out[k].ctypes.data_as(C.POINTER(C.c_double)))
+    return out, tr
+
+
+def _run(config: Dict[str, Any], dims: int, precision: int):
+    with Scene(config, dims, precision) as s:
+        return s.render()
+
+
+def sstmc2D(config: Dict[str, Any], precision: int = cf.PRECISION_SPLIT):
+    """[u, iter] = sstmc2D(config)"""
+    return _run(config, 2, precision)
+
+
+def sstmc3D(config: Dict[str, Any], precision: int = cf.PRECISION_SPLIT):
+    """[u, iter] = sstmc3D(config)"""
+    return _run(config, 3, precision)

@@ -1,0 +1,461 @@
+// api.cpp -- C-ABI of include/sstmc.h: scene lifetime, render, debug traces.
+//
+// sstmc_render replaces the rendering loop of mexFunction
+// (MatlabInterface.cu:1783-1801): per rendering, trace renderings' paths
+// (fullIteration waves of batchSize paths, NextEventEstimation.cuh:1475),
+// accumulate u, report iter = batchSize * fullIteration + missed first
+// vertices (:1796), then seed + 1 for the next rendering (:1799-1800).
+// Paths are processed in chunks of path ids sized to a device-memory budget;
+// a path's random stream depends only on (seed, path id), so the chunking is
+// invisible in the result.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "contract.h"
+#include "scene.h"
+#include "sstmc_internal.h"
+#include "trace.h"
+
+namespace sstmc {
+
+namespace {
+
+int pow2ceil(int n)
+{
+    int p = 1;
+    while (p < n) p <<= 1;
+    return p;
+}
+
+size_t budget_bytes()
+{
+    const char* e = std::getenv("SSTMC_CHUNK_BYTES");
+    if (e) { const long long v = std::atoll(e); if (v > 0) return (size_t)v; }
+    return (size_t)2 << 30;
+}
+
+}  // namespace
+
+size_t Engine::bytes_per_path(const Scene& S)
+{
+    const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
+    return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16;
+}
+
+int Engine::ensure(Scene& S, uint32_t paths)
+{
+    if (cap >= paths && a_ms) return SSTMC_NO_ERROR;
+    release();
+    const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (cudaMalloc(p, bytes ? bytes : 1) != cudaSuccess) return false;
+        return true;
+    };
+    bool ok = alloc((void**)&a_ms, paths * Nt * Nl * sizeof(float2)) && alloc((void**)&s_ms, paths * Nt * Nv * sizeof(float2))
+           && alloc((void**)&a_ss, paths * Nt * Nl * sizeof(float2)) && alloc((void**)&b_ss, paths * Nt * Nv * sizeof(float2))
+           && alloc((void**)&g2, S.correlation ? paths * Nt * Nl * sizeof(float2) : 8)
+           && alloc((void**)&pl, paths * Nl * sizeof(float)) && alloc((void**)&x1, paths * 3 * sizeof(float))
+           && alloc((void**)&x1t, S.correlation ? 8 : paths * Nt * 3 * sizeof(float))
+           && alloc((void**)&m1, paths) && alloc((void**)&totals, 8 * sizeof(unsigned long long))
+           && alloc((void**)&err, sizeof(int)) && alloc((void**)&V, Nt * Nv * Nl * sizeof(double2));
+    if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
+    cap = paths;
+    return SSTMC_NO_ERROR;
+}
+
+void Engine::release()
+{
+    void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W };
+    for (void* p : ps) if (p) cudaFree(p);
+    a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
+    pl = x1 = x1t = nullptr;
+    m1 = nullptr; totals = nullptr; err = nullptr; V = nullptr; W = nullptr;
+    cap = 0;
+}
+
+// Far-field x far-field single-scattering weight per (material, t, v, l):
+// Scattering.cuh:1118-1188 (amplitudeKernel<2>) for the field sampler; for the
+// correlation sampler the u1, u2 amplitudes and the temporal factor of
+// SourceInterface.cuh:221-270.
+int Engine::prepare_ss_tables(Scene& S)
+{
+    if (W) return SSTMC_NO_ERROR;
+    const DevScene& D = S.dev;
+    const int Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
+    const size_t per = (size_t)Nt * Nv * Nl;
+    std::vector<float> h(per * kMat, 0.0f);
+    const Scene::HostSource& il = S.hsrc[0];
+    const Scene::HostSource& vw = S.hsrc[1];
+    const Scene::HostSource& il2 = S.correlation ? S.hsrc[2] : S.hsrc[0];
+    const Scene::HostSource& vw2 = S.correlation ? S.hsrc[3] : S.hsrc[1];
+    const double k2 = (2.0 * kPi / S.cfg_copy.lambda) * (2.0 * kPi / S.cfg_copy.lambda);
+    auto amp = [&](int m, double c) -> double {
+        if (D.scat_type[m] == SSTMC_SCATTERING_ISOTROPIC) return S.dims == 2 ? kIsoAmp2 : kIsoAmp3;
+        if (D.scat_type[m] != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return 0.0;
+        const double g = S.g_d[m];
+        const double gup = S.dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * kPi)) : (1.0 - g * g) / (4.0 * kPi);
+        const double dn = std::fma(-2.0 * g, c, 1.0 + g * g);
+        return S.dims == 2 ? std::sqrt(gup / dn) : std::sqrt(gup / (dn * std::sqrt(dn)));
+    };
+    for (int m : S.materials_present) {
+        const double Dm = S.D_d[m];
+        for (int t = 0; t < Nt; ++t)
+            for (int v = 0; v < Nv; ++v)
+                for (int l = 0; l < Nl; ++l) {
+                    double a1[3], a2[3], b1[3], b2[3];
+                    for (int i = 0; i < 3; ++i) {
+                        a1[i] = il.p[3 * l + i]; a2[i] = il2.p[3 * l + i];
+                        b1[i] = vw.p[3 * v + i]; b2[i] = vw2.p[3 * v + i];
+                    }
+                    double w = amp(m, a1[0] * b1[0] + a1[1] * b1[1] + a1[2] * b1[2]);
+                    if (S.correlation) {
+                        w *= amp(m, a2[0] * b2[0] + a2[1] * b2[1] + a2[2] * b2[2]);
+                        double q2 = 0;
+                        for (int i = 0; i < 3; ++i) { const double qi = 0.5 * (a1[i] + a2[i] - b1[i] - b2[i]); q2 += qi * qi; }
+                        w *= std::exp(-k2 * std::fabs(Dm * S.ticks[t]) * q2);
+                    }
+                    h[m * per + ((size_t)t * Nv + v) * Nl + l] = (float)w;
+                }
+    }
+    if (cudaMalloc((void**)&W, h.size() * sizeof(float)) != cudaSuccess) { W = nullptr; return SSTMC_ALLOCATION_ERROR; }
+    if (cudaMemcpy(W, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    return SSTMC_NO_ERROR;
+}
+
+void Engine::plan(const Scene& S, TraceParams& T, std::vector<std::pair<int, int>>* vchunks, std::vector<std::pair<int, int>>* tchunks) const
+{
+    const int Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
+    const int vw = std::min(32, pow2ceil(Nv));
+    const int tg = 32 / vw;
+    int tpl = (Nt + tg - 1) / tg;
+    if (tpl > kMaxSlots) tpl = kMaxSlots;
+    const int tn = std::min(Nt, tpl * tg);
+    const int vpl = std::max(1, kMaxSlots / tpl);
+    const int vn = std::min(Nv, vpl * vw);
+    T.vw = vw; T.tg = tg; T.tpl = tpl;
+    T.slots = ((vn + vw - 1) / vw) * tpl;
+    T.lw = std::min(32, pow2ceil(Nl)); T.lg = 32 / T.lw;
+    T.vwa = vw; T.tga = tg;
+    vchunks->clear(); tchunks->clear();
+    for (int v = 0; v < Nv; v += vn) vchunks->push_back({ v, std::min(vn, Nv - v) });
+    for (int t = 0; t < Nt; t += tn) tchunks->push_back({ t, std::min(tn, Nt - t) });
+}
+
+int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, PathDebug* dbg)
+{
+    TraceParams T;
+    std::memset(&T, 0, sizeof(T));
+    std::vector<std::pair<int, int>> vch, tch;
+    plan(S, T, &vch, &tch);
+    T.seed = seed; T.first_path = first; T.paths = n;
+    T.a_ms = a_ms; T.s_ms = s_ms; T.a_ss = a_ss; T.b_ss = b_ss; T.g2 = g2; T.pl = pl;
+    T.x1 = x1; T.x1t = S.correlation ? nullptr : x1t; T.m1 = m1; T.totals = totals; T.err = err;
+    if (dbg) { T.nvert = dbg->nvert; T.misses = dbg->misses; T.hash = dbg->hash; T.dda = dbg->dda; }
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 128;
+    const size_t smem = trace_smem_bytes(S.Nt, T.slots, threads);
+    if (smem > 48 * 1024) {
+        // attribute is set inside launch_trace; occupancy query below tolerates either state
+    }
+    per_sm = occupancy_blocks(threads, smem);
+    const int blocks = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_sm)));
+    bool first_pass = true;
+    for (auto& vc : vch) {
+        for (auto& tc : tch) {
+            T.pass0 = first_pass ? 1 : 0;
+            T.v0 = vc.first; T.vn = vc.second; T.t0 = tc.first; T.tn = tc.second;
+            const int e = launch_trace(S.dev, T, blocks, threads, stream);
+            if (e) return e;
+            launches++;
+            first_pass = false;
+        }
+    }
+    return SSTMC_NO_ERROR;
+}
+
+int Engine::contract_chunk(Scene& S, uint32_t n)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const bool compensated = S.precision == SSTMC_PRECISION_SPLIT;
+    GemmParams G;
+    std::memset(&G, 0, sizeof(G));
+    G.Nt = S.Nt; G.Nl = S.Nl; G.Nv = S.Nv; G.V = V; G.K = (int)n; G.compensated = compensated ? 1 : 0;
+    const int tiles = ((S.Nl + 31) / 32) * ((S.Nv + 31) / 32) * S.Nt;
+    const int ksplit = std::max(1, (4 * sms + tiles - 1) / tiles);
+    int kchunk = (int)((n + ksplit - 1) / ksplit);
+    kchunk = ((kchunk + 255) / 256) * 256;
+    G.kchunk = kchunk;
+    G.A = a_ms; G.B = s_ms;
+    int e = launch_gemm(G, stream);
+    if (e) return e;
+    launches++;
+    if (timing) cudaEventRecord(ev[3], stream);
+    const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD;
+    if (farfar) {
+        e = prepare_ss_tables(S);
+        if (e) return e;
+        const size_t per = (size_t)S.Nt * S.Nv * S.Nl;
+        G.A = a_ss; G.B = b_ss; G.mat = m1;
+        for (int m : S.materials_present) {
+            G.mat_sel = m;
+            G.W = W + (size_t)m * per;
+            e = launch_gemm(G, stream);
+            if (e) return e;
+            launches++;
+        }
+    } else {
+        SsParams P;
+        std::memset(&P, 0, sizeof(P));
+        P.a = a_ss; P.b = b_ss; P.x1 = x1; P.x1t = x1t; P.m1 = m1; P.K = (int)n; P.V = V;
+        P.compensated = compensated ? 1 : 0;
+        const int stiles = ((S.Nl + 15) / 16) * ((S.Nv + 15) / 16) * ((S.Nt + 7) / 8);
+        const int ks = std::max(1, (4 * sms + stiles - 1) / stiles);
+        int kc = (int)((n + ks - 1) / ks);
+        kc = ((kc + 255) / 256) * 256;
+        P.kchunk = kc;
+        e = launch_ss(S.dev, P, stream);
+        if (e) return e;
+        launches++;
+    }
+    return SSTMC_NO_ERROR;
+}
+
+int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out)
+{
+    const uint64_t total = (uint64_t)S.P * S.full_iter;
+    if (total > 0xffffffffull) return SSTMC_NOT_SUPPORTED;
+    uint32_t chunk = (uint32_t)std::min<uint64_t>(total, std::max<uint64_t>(256, budget_bytes() / bytes_per_path(S)));
+    chunk = std::max<uint32_t>(32, chunk);
+    int e = ensure(S, chunk);
+    if (e) return e;
+    const size_t nout = (size_t)S.Nt * S.Nv * S.Nl;
+    if (timing && init_events()) timing = false;
+    launches = 0;
+    if (cudaMemsetAsync(V, 0, nout * sizeof(double2), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (cudaMemsetAsync(totals, 0, 8 * sizeof(unsigned long long), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (cudaMemsetAsync(err, 0, sizeof(int), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    std::vector<float> t_trace, t_gemm, t_ss;
+    float t_all = 0.f;
+    if (timing) cudaEventRecord(ev[0], stream);
+    for (uint64_t first = 0; first < total; first += chunk) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(chunk, total - first);
+        if (timing) cudaEventRecord(ev[1], stream);
+        e = trace_chunk(S, seed, (uint32_t)first, n, nullptr);
+        if (e) return e;
+        if (timing) cudaEventRecord(ev[2], stream);
+        e = contract_chunk(S, n);
+        if (e) return e;
+        if (timing) {
+            cudaEventRecord(ev[4], stream);
+            cudaEventSynchronize(ev[4]);
+            float a = 0, b = 0, c = 0;
+            cudaEventElapsedTime(&a, ev[1], ev[2]);
+            cudaEventElapsedTime(&b, ev[2], ev[3]);
+            cudaEventElapsedTime(&c, ev[3], ev[4]);
+            t_trace.push_back(a); t_gemm.push_back(b); t_ss.push_back(c);
+        }
+    }
+    if (timing) {
+        cudaEventRecord(ev[5], stream);
+        cudaEventSynchronize(ev[5]);
+        cudaEventElapsedTime(&t_all, ev[0], ev[5]);
+        ms_trace = ms_gemm = ms_ss = 0;
+        for (size_t i = 0; i < t_trace.size(); ++i) { ms_trace += t_trace[i]; ms_gemm += t_gemm[i]; ms_ss += t_ss[i]; }
+        ms_total = t_all;
+    }
+    unsigned long long tot[8];
+    int herr = 0;
+    if (cudaMemcpyAsync(tot, totals, sizeof(tot), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (u_out && cudaMemcpyAsync(u_out, V, nout * sizeof(double2), cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+        return SSTMC_DEVICE_ERROR;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
+    if (herr) return herr;
+    if (iter_out) *iter_out = (double)total + (double)tot[2];
+    S.last_vertices = tot[0];
+    S.last_dda = tot[1];
+    S.last_paths = tot[3];
+    S.last_contrib = tot[0] * (uint64_t)S.Nl * S.Nv * S.Nt;
+    return SSTMC_NO_ERROR;
+}
+
+int Engine::init_events()
+{
+    if (ev[0]) return 0;
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return 1;
+    return 0;
+}
+
+void Engine::destroy_events()
+{
+    for (auto& e : ev) { if (e) cudaEventDestroy(e); e = nullptr; }
+}
+
+}  // namespace sstmc
+
+using namespace sstmc;
+
+struct sstmc_scene {
+    Scene scene;
+    Engine engine;
+    std::mutex mu;
+};
+
+extern "C" {
+
+void sstmc_config_init(sstmc_config* cfg)
+{
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->dims = 3;
+    cfg->batch_size = 1024;
+    cfg->full_iteration = 1;
+    cfg->renderings_num = 1;
+    cfg->lambda = 1.0;
+    cfg->is_temporal_amplitude = 1;
+    cfg->precision = SSTMC_PRECISION_SPLIT;
+}
+
+int32_t sstmc_scene_create(const sstmc_config* cfg, sstmc_scene** out)
+{
+    if (!cfg || !out) return SSTMC_INVALID_HANDLE;
+    *out = nullptr;
+    sstmc_scene* s = new (std::nothrow) sstmc_scene();
+    if (!s) return SSTMC_ALLOCATION_ERROR;
+    std::string why;
+    int e = build_scene(cfg, &s->scene, &why);
+    if (!e && cudaStreamCreateWithFlags(&s->engine.stream, cudaStreamNonBlocking) != cudaSuccess) e = SSTMC_DEVICE_ERROR;
+    if (e) {
+        set_last_error_text(why);
+        delete s;
+        return e;
+    }
+    *out = s;
+    return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_scene_shape(const sstmc_scene* s, uint32_t* nl, uint32_t* nv, uint32_t* nt)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    if (nl) *nl = (uint32_t)s->scene.Nl;
+    if (nv) *nv = (uint32_t)s->scene.Nv;
+    if (nt) *nt = (uint32_t)s->scene.Nt;
+    return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_render(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (cudaSetDevice(s->scene.device) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    const size_t nout = (size_t)s->scene.Nt * s->scene.Nv * s->scene.Nl;
+    for (uint32_t r = 0; r < s->scene.renders; ++r) {
+        const int e = s->engine.render_one(s->scene, seed + r, u_out ? u_out + 2 * nout * r : nullptr,
+                                           iter_out ? iter_out + r : nullptr);
+        if (e) return e;
+    }
+    return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_last_stats(const sstmc_scene* s, uint64_t* contributions, uint64_t* dda_steps, uint64_t* vertices, uint64_t* paths)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    if (contributions) *contributions = s->scene.last_contrib;
+    if (dda_steps) *dda_steps = s->scene.last_dda;
+    if (vertices) *vertices = s->scene.last_vertices;
+    if (paths) *paths = s->scene.last_paths;
+    return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_last_timing(const sstmc_scene* s, double* ms, uint64_t* launches)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    if (ms) {
+        ms[0] = s->engine.ms_total; ms[1] = s->engine.ms_trace;
+        ms[2] = s->engine.ms_gemm; ms[3] = s->engine.ms_ss;
+    }
+    if (launches) *launches = s->engine.launches;
+    return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_scene_destroy(sstmc_scene* s)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        cudaSetDevice(s->scene.device);
+        if (s->engine.stream) cudaStreamSynchronize(s->engine.stream);
+        s->engine.release();
+        s->engine.destroy_events();
+        if (s->engine.stream) cudaStreamDestroy(s->engine.stream);
+        s->engine.stream = nullptr;
+    }
+    delete s;
+    return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_trace_paths(sstmc_scene* s, uint64_t seed, uint32_t first_path, uint32_t paths, sstmc_path_trace* out)
+{
+    if (!s || !out) return SSTMC_INVALID_HANDLE;
+    if (paths == 0) return SSTMC_NO_ERROR;
+    std::lock_guard<std::mutex> lk(s->mu);
+    Scene& S = s->scene;
+    Engine& E = s->engine;
+    if (cudaSetDevice(S.device) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    int e = E.ensure(S, paths);
+    if (e) return e;
+    PathDebug dbg;
+    if (cudaMalloc((void**)&dbg.nvert, paths * sizeof(int)) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    cudaMalloc((void**)&dbg.misses, paths * sizeof(int));
+    cudaMalloc((void**)&dbg.hash, paths * sizeof(uint32_t));
+    cudaMalloc((void**)&dbg.dda, paths * sizeof(uint32_t));
+    cudaMemsetAsync(dbg.dda, 0, paths * sizeof(uint32_t), E.stream);
+    cudaMemsetAsync(E.totals, 0, 8 * sizeof(unsigned long long), E.stream);
+    cudaMemsetAsync(E.err, 0, sizeof(int), E.stream);
+    e = E.trace_chunk(S, seed, first_path, paths, &dbg);
+    int herr = 0;
+    if (!e) {
+        cudaMemcpyAsync(&herr, E.err, sizeof(int), cudaMemcpyDeviceToHost, E.stream);
+        if (cudaStreamSynchronize(E.stream) != cudaSuccess) e = SSTMC_KERNEL_ERROR;
+    }
+    if (!e && herr) e = herr;
+    if (!e) {
+        const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
+        if (out->misses) cudaMemcpy(out->misses, dbg.misses, paths * sizeof(int), cudaMemcpyDeviceToHost);
+        if (out->vertices) cudaMemcpy(out->vertices, dbg.nvert, paths * sizeof(int), cudaMemcpyDeviceToHost);
+        if (out->vertex_hash) cudaMemcpy(out->vertex_hash, dbg.hash, paths * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (out->dda_steps) cudaMemcpy(out->dda_steps, dbg.dda, paths * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+        if (out->x1) cudaMemcpy(out->x1, E.x1, paths * 3 * sizeof(float), cudaMemcpyDeviceToHost);
+        if (out->m1) {
+            std::vector<unsigned char> m(paths);
+            cudaMemcpy(m.data(), E.m1, paths, cudaMemcpyDeviceToHost);
+            for (uint32_t i = 0; i < paths; ++i) out->m1[i] = m[i];
+        }
+        auto copy_c = [&](double* dst, const float2* src, size_t n) {
+            if (!dst) return;
+            std::vector<float2> h(n);
+            cudaMemcpy(h.data(), src, n * sizeof(float2), cudaMemcpyDeviceToHost);
+            for (size_t i = 0; i < n; ++i) { dst[2 * i] = h[i].x; dst[2 * i + 1] = h[i].y; }
+        };
+        copy_c(out->a_ms, E.a_ms, paths * Nt * Nl);
+        copy_c(out->s_ms, E.s_ms, paths * Nt * Nv);
+        copy_c(out->a_ss, E.a_ss, paths * Nt * Nl);
+        copy_c(out->b_ss, E.b_ss, paths * Nt * Nv);
+    }
+    cudaFree(dbg.nvert); cudaFree(dbg.misses); cudaFree(dbg.hash); cudaFree(dbg.dda);
+    return e;
+}
+
+}  // extern "C"

@@ -1,0 +1,271 @@
+// contract.cu -- illumination x view contractions over paths (SIMT forms).
+//
+// The reference materialises the Nl x Nv x P broadcast product and sums it
+// with cublasZgemv against a ones vector (multipleResSingle / multipleResFinal,
+// NextEventEstimation.cuh:1016-1136, 1397-1458; MatrixOperations.cuh:192-516).
+// Here the sum over paths is a complex GEMM per tick,
+//     V[t][v][l] += sum_p A[p][t][l] * B[p][t][v],
+// with the paths as the K dimension.
+//
+// gemm_kernel: 32 x 32 output tile per CTA, K split across CTAs, FP32 partial
+// sums over 256-path windows folded into a compensated two-float accumulator
+// (Knuth TwoSum), FP64 atomic add of the CTA result.  The optional material
+// filter and weight table give the single-scattering term of far-field x
+// far-field scenes, whose amplitude depends only on (material, l, v, t).
+//
+// ss_kernel: the single-scattering term when the amplitude depends on the
+// scatterer position (point sources):
+//     V[t][v][l] += sum_p a[p][t][l] * b[p][t][v] * W(l, v, t, p).
+#include <cuda_runtime.h>
+
+#include "contract.h"
+#include "nee.cuh"
+
+namespace sstmc {
+
+namespace {
+
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float x)
+{
+    const float s = hi + x;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (x - bb);
+    hi = s;
+    lo += e;
+}
+
+constexpr int kTile = 32;
+constexpr int kKc = 32;
+constexpr int kFlush = 8;  // chunks per compensated flush (256 paths)
+
+__global__ void __launch_bounds__(256) gemm_kernel(const GemmParams G)
+{
+    __shared__ float2 As[kKc][kTile + 1];
+    __shared__ float2 Bs[kKc][kTile + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int l0 = blockIdx.x * kTile, v0 = blockIdx.y * kTile;
+    const int t = blockIdx.z % G.Nt, ks = blockIdx.z / G.Nt;
+    const int kb = ks * G.kchunk;
+    const int ke = min(G.K, kb + G.kchunk);
+    float2 acc[2][2];
+    float hr[2][2], lr[2][2], hi_[2][2], li[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) { acc[i][j] = make_float2(0.f, 0.f); hr[i][j] = lr[i][j] = hi_[i][j] = li[i][j] = 0.f; }
+    int chunk = 0;
+    for (int k = kb; k < ke; k += kKc, ++chunk) {
+        for (int idx = threadIdx.x; idx < kKc * kTile; idx += 256) {
+            const int pp = idx / kTile, c = idx % kTile;
+            const int p = k + pp;
+            float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+            if (p < ke && (G.mat == nullptr || G.mat[p] == G.mat_sel)) {
+                if (l0 + c < G.Nl) a = G.A[((size_t)p * G.Nt + t) * G.Nl + l0 + c];
+                if (v0 + c < G.Nv) b = G.B[((size_t)p * G.Nt + t) * G.Nv + v0 + c];
+            }
+            As[pp][c] = a;
+            Bs[pp][c] = b;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int pp = 0; pp < kKc; ++pp) {
+            const float2 a0 = As[pp][tx], a1 = As[pp][tx + 16];
+            const float2 b0 = Bs[pp][ty], b1 = Bs[pp][ty + 16];
+            const float2 av[2] = { a0, a1 }, bv[2] = { b0, b1 };
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    acc[i][j].x = fmaf(av[i].x, bv[j].x, fmaf(-av[i].y, bv[j].y, acc[i][j].x));
+                    acc[i][j].y = fmaf(av[i].x, bv[j].y, fmaf(av[i].y, bv[j].x, acc[i][j].y));
+                }
+        }
+        __syncthreads();
+        if (G.compensated && (chunk + 1) % kFlush == 0) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    two_sum_add(hr[i][j], lr[i][j], acc[i][j].x);
+                    two_sum_add(hi_[i][j], li[i][j], acc[i][j].y);
+                    acc[i][j] = make_float2(0.f, 0.f);
+                }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int l = l0 + tx + 16 * i, v = v0 + ty + 16 * j;
+            if (l >= G.Nl || v >= G.Nv) continue;
+            double re = (double)hr[i][j] + (double)lr[i][j] + (double)acc[i][j].x;
+            double im = (double)hi_[i][j] + (double)li[i][j] + (double)acc[i][j].y;
+            const size_t o = ((size_t)t * G.Nv + v) * G.Nl + l;
+            if (G.W) { const double w = G.W[o]; re *= w; im *= w; }
+            atomicAdd(&G.V[o].x, re);
+            atomicAdd(&G.V[o].y, im);
+        }
+}
+
+constexpr int kSsL = 16, kSsV = 16, kSsK = 16, kSsT = 8;
+
+// Single-scattering weight W(l, v, t) of one path.
+struct SsGeom {
+    V3 in1, in2, out1, out2;
+};
+
+__global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScene S, const SsParams G)
+{
+    __shared__ float2 as[kSsK][kSsT][kSsL];
+    __shared__ float2 bs[kSsK][kSsT][kSsV];
+    __shared__ float inx[kSsK][kSsL][6];
+    __shared__ float outx[kSsK][kSsV][6];
+    __shared__ float x1s[kSsK][3];
+    __shared__ int m1s[kSsK];
+    const int tl = threadIdx.x % kSsL, tv = threadIdx.x / kSsL;
+    const int l0 = blockIdx.x * kSsL, v0 = blockIdx.y * kSsV;
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const int tchunks = (Nt + kSsT - 1) / kSsT;
+    const int t0 = (blockIdx.z % tchunks) * kSsT;
+    const int tn = min(kSsT, Nt - t0);
+    const int ks = blockIdx.z / tchunks;
+    const int kb = ks * G.kchunk, ke = min(G.K, kb + G.kchunk);
+    const bool corr = S.correlation != 0;
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    const DevSource& il2 = corr ? S.src[2] : S.src[0];
+    const DevSource& vw2 = corr ? S.src[3] : S.src[1];
+    const bool scalar_fs = il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT && S.iso_all;
+    float2 acc[kSsT];
+    float hr[kSsT], lr[kSsT], hi_[kSsT], li[kSsT];
+#pragma unroll
+    for (int i = 0; i < kSsT; ++i) { acc[i] = make_float2(0.f, 0.f); hr[i] = lr[i] = hi_[i] = li[i] = 0.f; }
+    int chunk = 0;
+    for (int k = kb; k < ke; k += kSsK, ++chunk) {
+        // stage rows and geometry
+        for (int idx = threadIdx.x; idx < kSsK * kSsT * kSsL; idx += 256) {
+            const int pp = idx / (kSsT * kSsL), r = idx % (kSsT * kSsL);
+            const int tt = r / kSsL, c = r % kSsL;
+            const int p = k + pp;
+            float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+            if (p < ke && tt < tn) {
+                if (l0 + c < Nl) a = G.a[((size_t)p * Nt + t0 + tt) * Nl + l0 + c];
+                if (v0 + c < Nv) b = G.b[((size_t)p * Nt + t0 + tt) * Nv + v0 + c];
+            }
+            as[pp][tt][c] = a;
+            bs[pp][tt][c] = b;
+        }
+        if (threadIdx.x < kSsK) {
+            const int p = k + threadIdx.x;
+            if (p < ke) {
+                x1s[threadIdx.x][0] = G.x1[3 * p]; x1s[threadIdx.x][1] = G.x1[3 * p + 1]; x1s[threadIdx.x][2] = G.x1[3 * p + 2];
+                m1s[threadIdx.x] = G.m1[p];
+            } else {
+                x1s[threadIdx.x][0] = x1s[threadIdx.x][1] = x1s[threadIdx.x][2] = 0.f;
+                m1s[threadIdx.x] = 0;
+            }
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < kSsK * kSsL; idx += 256) {
+            const int pp = idx / kSsL, c = idx % kSsL;
+            const V3 x = V3{ x1s[pp][0], x1s[pp][1], x1s[pp][2] };
+            const int l = min(l0 + c, Nl - 1), v = min(v0 + c, Nv - 1);
+            const V3 i1 = src_in(il, l, x), i2 = src_in(il2, l, x);
+            const V3 o1 = src_out(vw, v, x), o2 = src_out(vw2, v, x);
+            inx[pp][c][0] = i1.x; inx[pp][c][1] = i1.y; inx[pp][c][2] = i1.z;
+            inx[pp][c][3] = i2.x; inx[pp][c][4] = i2.y; inx[pp][c][5] = i2.z;
+            outx[pp][c][0] = o1.x; outx[pp][c][1] = o1.y; outx[pp][c][2] = o1.z;
+            outx[pp][c][3] = o2.x; outx[pp][c][4] = o2.y; outx[pp][c][5] = o2.z;
+        }
+        __syncthreads();
+        for (int pp = 0; pp < kSsK; ++pp) {
+            const int m = m1s[pp];
+            if (m == 0) continue;
+            const V3 i1 = V3{ inx[pp][tl][0], inx[pp][tl][1], inx[pp][tl][2] };
+            const V3 i2 = V3{ inx[pp][tl][3], inx[pp][tl][4], inx[pp][tl][5] };
+            const V3 o1 = V3{ outx[pp][tv][0], outx[pp][tv][1], outx[pp][tv][2] };
+            const V3 o2 = V3{ outx[pp][tv][3], outx[pp][tv][4], outx[pp][tv][5] };
+            float w0, c = 0.0f;
+            if (scalar_fs) {
+                w0 = corr ? S.iso_amp * S.iso_amp : S.iso_amp;
+            } else if (!corr) {
+                w0 = (il.type == SSTMC_SOURCE_POINT && S.iso_all) ? S.iso_amp : amp_dirs(S, m, i1, o1);
+            } else {
+                const bool pi = il.type == SSTMC_SOURCE_POINT && S.iso_all;
+                w0 = (pi ? S.iso_amp : amp_dirs(S, m, i1, o1)) * (pi ? S.iso_amp : amp_dirs(S, m, i2, o2));
+                const V3 qv = V3{ 0.5f * (i1.x + i2.x - o1.x - o2.x), 0.5f * (i1.y + i2.y - o1.y - o2.y), 0.5f * (i1.z + i2.z - o1.z - o2.z) };
+                c = S.k2 * S.D[m] * dot3(qv, qv);
+            }
+            // scatterer evaluation point that moves with the tick: field sampler with
+            // temporal amplitude (TemporalSampler.cuh:272-300) or correlation-sampler
+            // drift U (TemporalSamplerCorrelation.cuh:293-315)
+            const bool vary = !scalar_fs && (corr ? S.static_corr[m] == 0 : (S.temporal_amp && S.moving[m]));
+            const V3 xp = V3{ x1s[pp][0], x1s[pp][1], x1s[pp][2] };
+            const int lg = min(l0 + tl, Nl - 1), vg = min(v0 + tv, Nv - 1);
+#pragma unroll
+            for (int tt = 0; tt < kSsT; ++tt) {
+                if (tt >= tn) break;
+                float w = (corr && !scalar_fs) ? w0 * expf(-c * S.abs_ticks[t0 + tt]) : w0;
+                if (vary) {
+                    V3 xt;
+                    if (corr) xt = shift_u(S, xp, m, S.ticks_f[t0 + tt], -1.0f);
+                    else {
+                        const float* q = G.x1t + ((size_t)(k + pp) * Nt + t0 + tt) * 3;
+                        xt = V3{ q[0], q[1], q[2] };
+                    }
+                    const bool pi = il.type == SSTMC_SOURCE_POINT && S.iso_all;
+                    const float f1 = pi ? S.iso_amp : amp_dirs(S, m, src_in(il, lg, xt), src_out(vw, vg, xt));
+                    if (!corr) w = f1;
+                    else {
+                        const float f2 = pi ? S.iso_amp : amp_dirs(S, m, src_in(il2, lg, xt), src_out(vw2, vg, xt));
+                        w = f1 * f2 * expf(-c * S.abs_ticks[t0 + tt]);
+                    }
+                }
+                const float2 ab = c_mul(as[pp][tt][tl], bs[pp][tt][tv]);
+                acc[tt].x = fmaf(ab.x, w, acc[tt].x);
+                acc[tt].y = fmaf(ab.y, w, acc[tt].y);
+            }
+        }
+        __syncthreads();
+        if (G.compensated && (chunk + 1) % 16 == 0) {
+#pragma unroll
+            for (int tt = 0; tt < kSsT; ++tt) {
+                two_sum_add(hr[tt], lr[tt], acc[tt].x);
+                two_sum_add(hi_[tt], li[tt], acc[tt].y);
+                acc[tt] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    const int l = l0 + tl, v = v0 + tv;
+    if (l >= Nl || v >= Nv) return;
+#pragma unroll
+    for (int tt = 0; tt < kSsT; ++tt) {
+        if (tt >= tn) break;
+        const size_t o = ((size_t)(t0 + tt) * Nv + v) * Nl + l;
+        atomicAdd(&G.V[o].x, (double)hr[tt] + (double)lr[tt] + (double)acc[tt].x);
+        atomicAdd(&G.V[o].y, (double)hi_[tt] + (double)li[tt] + (double)acc[tt].y);
+    }
+}
+
+}  // namespace
+
+int launch_gemm(const GemmParams& G, cudaStream_t stream)
+{
+    if (G.K <= 0) return SSTMC_NO_ERROR;
+    const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
+    dim3 grid((G.Nl + kTile - 1) / kTile, (G.Nv + kTile - 1) / kTile, G.Nt * ksplit);
+    gemm_kernel<<<grid, 256, 0, stream>>>(G);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
+}
+
+int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
+{
+    if (G.K <= 0) return SSTMC_NO_ERROR;
+    const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
+    const int tchunks = (S.Nt + kSsT - 1) / kSsT;
+    dim3 grid((S.src[0].n + kSsL - 1) / kSsL, (S.src[1].n + kSsV - 1) / kSsV, tchunks * ksplit);
+    ss_kernel<<<grid, 256, 0, stream>>>(S, G);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
+}
+
+}  // namespace sstmc

@@ -1,0 +1,40 @@
+// contract.h -- launch interface of the contraction kernels (contract.cu, gemm_tc.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "scene.h"
+
+namespace sstmc {
+
+// V[t][v][l] += sum_{p < K} A[p][t][l] * B[p][t][v]  (times W[t][v][l] if W),
+// restricted to rows with mat[p] == mat_sel when mat is given.
+struct GemmParams {
+    const float2* A;
+    const float2* B;
+    int K, Nt, Nl, Nv;
+    const unsigned char* mat;
+    int mat_sel;
+    const float* W;
+    double2* V;
+    int kchunk;
+    int compensated;
+};
+
+// V[t][v][l] += sum_p a[p][t][l] * b[p][t][v] * W(l, v, t, p), W from the
+// scatterer position x1[p] / x1t[p][t] and material m1[p].
+struct SsParams {
+    const float2* a;
+    const float2* b;
+    const float* x1;
+    const float* x1t;
+    const unsigned char* m1;
+    int K;
+    double2* V;
+    int kchunk;
+    int compensated;
+};
+
+int launch_gemm(const GemmParams& G, cudaStream_t stream);
+int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream);
+
+}  // namespace sstmc

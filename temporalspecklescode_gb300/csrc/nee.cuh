@@ -1,0 +1,179 @@
+// nee.cuh -- per-vertex NEE quantities (value path: FP32, with the phase
+// argument reduction in FP64 in the split-precision form).
+//
+//   g, far field      FarField.cuh:223-263   sqrt(T) exp(+/- 2 pi i d.x / lambda)
+//   g, point source   PointSource.cuh:117-172 sqrt(T c / r^(D-1)) exp(2 pi i r / lambda)
+//   P_l (first point) FarField.cuh:469-499, PointSource.cuh:92-115, 263-294
+//   f (three points)  FarField.cuh:546-554, PointSource.cuh:317-345, Scattering.cuh:895-955
+//   pdf               Scattering.cuh:959-1023
+// Henyey-Greenstein amplitudes are evaluated from the difference of the two
+// unit directions, 1 + g^2 - 2 g cos = (1 - g)^2 + g |a - b|^2, which keeps
+// full FP32 relative accuracy for strongly forward scattering (g = 0.9).
+#pragma once
+#include "walk.cuh"
+
+namespace sstmc {
+
+constexpr int kRoleIllum = 0;
+constexpr int kRoleView = 1;
+
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 c_mulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }  // a * conj(b)
+__device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+__device__ __forceinline__ V3 sub3(const V3& a, const V3& b) { return V3{ a.x - b.x, a.y - b.y, a.z - b.z }; }
+__device__ __forceinline__ float dot3(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 unit3(const V3& v)
+{
+    const float s = dot3(v, v);
+    if (!(s > 0.0f)) return V3{ 0.f, 0.f, 1.f };
+    const float r = rsqrtf(s);
+    return V3{ v.x * r, v.y * r, v.z * r };
+}
+
+// exp(2 pi i f)
+__device__ __forceinline__ float2 unit_phase(float f)
+{
+    float s, c;
+    sincospif(2.0f * f, &s, &c);
+    return make_float2(c, s);
+}
+
+// reduce a phase measured in cycles: FP64 in the split form, FP32 in the plain form
+__device__ __forceinline__ float frac_cycles(double ph) { return (float)(ph - rint(ph)); }
+
+__device__ __forceinline__ float amp_dirs(const DevScene& S, int m, const V3& a, const V3& b)
+{
+    const int ty = S.scat_type[m];
+    if (ty == SSTMC_SCATTERING_ISOTROPIC) return S.iso_amp;
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return 0.0f;
+    const float g = S.g[m];
+    const V3 d = sub3(a, b);
+    const float omg = 1.0f - g;
+    const float dn = fmaf(g, dot3(d, d), omg * omg);
+    return S.dims == 2 ? sqrtf(S.gup[m] / dn) : sqrtf(S.gup[m] / (dn * sqrtf(dn)));
+}
+
+__device__ __forceinline__ float pdf_dirs(const DevScene& S, int m, const V3& a, const V3& b)
+{
+    const int ty = S.scat_type[m];
+    if (ty == SSTMC_SCATTERING_ISOTROPIC) return S.iso_pdf;
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return 0.0f;
+    const float g = S.g[m];
+    const V3 d = sub3(a, b);
+    const float omg = 1.0f - g;
+    const float dn = fmaf(g, dot3(d, d), omg * omg);
+    return S.dims == 2 ? S.gup[m] / dn : S.gup[m] / (dn * sqrtf(dn));
+}
+
+// Direction of travel from source element k into scatterer x (illumination side).
+__device__ __forceinline__ V3 src_in(const DevSource& s, int k, const V3& x)
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) return load3(s.p, k);
+    return unit3(sub3(x, load3(s.p, k)));
+}
+
+// Direction of travel from scatterer x toward view element k.
+__device__ __forceinline__ V3 src_out(const DevSource& s, int k, const V3& x)
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) return load3(s.p, k);
+    return unit3(sub3(load3(s.p, k), x));
+}
+
+// P_l(x): attenuation toward illumination element l times its sampling density.
+__device__ inline float pfirst(const DevScene& S, const DevSource& s, int l, const V3& x, uint32_t& steps)
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) {
+        const V3 d = load3(s.p, l);
+        const V3 nd = V3{ -d.x, -d.y, -d.z };
+        return expf(-dda(S, x, nd, steps)) * s.sprob[l];
+    }
+    const V3 sp = load3(s.p, l);
+    const V3 dir = normalize32(S.dims, V3{ fsb(sp.x, x.x), fsb(sp.y, x.y), fsb(sp.z, x.z) });
+    const float T = expf(-dda(S, x, dir, steps));
+    const V3 v = sub3(x, sp);
+    const float r2 = dot3(v, v);
+    const float k4pi = (float)(4.0 * kPi), k8pi = (float)(8.0 * kPi);
+    return S.dims == 3 ? T / (k4pi * r2) : T * k8pi / sqrtf(r2);
+}
+
+// NEE vector of source element k at scatterer x.  with_phase = false returns
+// the real amplitude sqrt(attenuation): used where the phase cancels exactly
+// (u1 * conj(u2) with both fields evaluated at the same point and source).
+__device__ inline float2 gvec(const DevScene& S, const DevSource& s, int k, const V3& x, int role, bool with_phase, uint32_t& steps)
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) {
+        const V3 d = load3(s.p, k);
+        const V3 dir = role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d;
+        const float a = sqrtf(expf(-dda(S, x, dir, steps)));
+        if (!with_phase) return make_float2(a, 0.0f);
+        float f;
+        if (S.precision == SSTMC_PRECISION_SPLIT) {
+            const double dx = fma((double)d.x, (double)x.x, fma((double)d.y, (double)x.y, (double)d.z * (double)x.z));
+            f = frac_cycles((role == kRoleIllum ? dx : -dx) * S.inv_lambda);
+        } else {
+            const float dx = d.x * x.x + d.y * x.y + d.z * x.z;
+            const float ph = (role == kRoleIllum ? dx : -dx) * S.inv_lambda_f;
+            f = ph - rintf(ph);
+        }
+        return c_scale(unit_phase(f), a);
+    }
+    const V3 sp = load3(s.p, k);
+    const V3 dir = normalize32(S.dims, V3{ fsb(sp.x, x.x), fsb(sp.y, x.y), fsb(sp.z, x.z) });
+    const float T = expf(-dda(S, x, dir, steps));
+    double r = 0.0;
+    float rf;
+    if (S.precision == SSTMC_PRECISION_SPLIT) {
+        const double dx = (double)x.x - (double)sp.x, dy = (double)x.y - (double)sp.y, dz = (double)x.z - (double)sp.z;
+        r = sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+        rf = (float)r;
+    } else {
+        const V3 v = sub3(x, sp);
+        rf = sqrtf(dot3(v, v));
+    }
+    float at = S.dims == 3 ? T * kIsoAmp3 / (rf * rf) : T / rf;
+    if (s.is_area) at *= fabsf(S.dims == 3 ? x.z - sp.z : x.y - sp.y) / rf;
+    const float a = sqrtf(at);
+    if (!with_phase) return make_float2(a, 0.0f);
+    float f;
+    if (S.precision == SSTMC_PRECISION_SPLIT) f = frac_cycles(r * S.inv_lambda);
+    else { const float ph = rf * S.inv_lambda_f; f = ph - rintf(ph); }
+    return c_scale(unit_phase(f), a);
+}
+
+// f for the illumination side: element l -> scatterer pa -> point pb.
+__device__ __forceinline__ float famp_illum(const DevScene& S, const DevSource& s, int l, const V3& pa, const V3& pb, int m)
+{
+    if (s.type == SSTMC_SOURCE_POINT && S.iso_all) return S.iso_amp;
+    return amp_dirs(S, m, src_in(s, l, pa), unit3(sub3(pb, pa)));
+}
+
+// f for the view side: point pb (previous vertex) -> scatterer pa -> view element v.
+__device__ __forceinline__ float famp_view(const DevScene& S, const DevSource& s, int v, const V3& pa, const V3& pb, int m)
+{
+    if (s.type == SSTMC_SOURCE_POINT && S.iso_all) return S.iso_amp;
+    return amp_dirs(S, m, unit3(sub3(pa, pb)), src_out(s, v, pa));
+}
+
+// Correlation-sampler shift x + h U(m), h = -/+ tau/2 (TemporalSamplerCorrelation.cuh:229-255).
+__device__ __forceinline__ V3 shift_u(const DevScene& S, const V3& x, int m, float tau, float sign)
+{
+    const float h = fm(tau, fm(0.5f, sign));
+    return V3{ ffma(h, S.U[m][0], x.x), ffma(h, S.U[m][1], x.y), S.dims == 3 ? ffma(h, S.U[m][2], x.z) : 0.0f };
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace sstmc

@@ -1,0 +1,354 @@
+// scene.cpp -- config validation and scene tables (host side).
+//
+// Config semantics follow MatlabInterface.cu:712-1372 (buildScattering,
+// buildMedium, buildSource, buildSampler): a single scattering cell is
+// duplicated into material 1 (:750-760), material 0 may not appear inside the
+// grid (:979-991), D must be non-negative (:1278-1283), correlation sources
+// must come in same-size pairs (:1304-1320).  Far-field tables restate
+// FarField.cuh:71-127 (fillBuffers) and MediumInterface.cuh:138-199
+// (projectBoxToLine) in double precision and are stored as float; the field
+// sampler's tick ordering restates TemporalSampler.cuh:958-1150.
+//
+// Compiled with -ffp-contract=off: the float tables must be bit-identical to
+// any other host restatement of the same formulas.
+#include "scene.h"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+namespace sstmc {
+
+Scene::~Scene()
+{
+    for (void* p : dev_allocs) cudaFree(p);
+}
+
+namespace {
+
+template <class T>
+int upload(Scene* s, const std::vector<T>& v, const T** out)
+{
+    if (v.empty()) { *out = nullptr; return SSTMC_NO_ERROR; }
+    void* d = nullptr;
+    if (cudaMalloc(&d, v.size() * sizeof(T)) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    s->dev_allocs.push_back(d);
+    if (cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    *out = static_cast<const T*>(d);
+    return SSTMC_NO_ERROR;
+}
+
+int prep_farfield(Scene::HostSource* s, const sstmc_source_cfg* c, int dims, const double bmin[3], const double bmax[3])
+{
+    const int n = (int)c->count;
+    s->p.assign(3 * n, 0.f); s->inv.assign(3 * n, 0.f); s->tang.assign(3 * n, 0.f);
+    s->pt.assign(3 * n, 0.f); s->ps.assign(3 * n, 0.f);
+    s->mint.assign(n, 0.f); s->maxt.assign(n, 0.f); s->mins.assign(n, 0.f); s->maxs.assign(n, 0.f);
+    s->sprob.assign(n, 0.f); s->sprob_d.assign(n, 0.0);
+    double center[3], radius[3];
+    for (int i = 0; i < 3; ++i) { center[i] = (bmax[i] + bmin[i]) * 0.5; radius[i] = (bmax[i] - bmin[i]) * 0.5; }
+    double rc = radius[0] > radius[1] ? radius[0] : radius[1];
+    if (dims == 3 && radius[2] > rc) rc = radius[2];
+    rc = rc + 1e-12;
+    for (int k = 0; k < n; ++k) {
+        double v[3] = { c->xyz[3 * k], c->xyz[3 * k + 1], dims == 3 ? c->xyz[3 * k + 2] : 0.0 };
+        double nrm = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (!(nrm > 0.0)) return SSTMC_INVALID_CONFIG;
+        double inr = 1.0 / nrm;
+        double d[3] = { v[0] * inr, v[1] * inr, v[2] * inr };
+        double op[3] = { -d[0], -d[1], -d[2] };
+        double tg[3], T[3], S[3] = { 0, 0, 0 };
+        for (int i = 0; i < 3; ++i) tg[i] = center[i] + rc * op[i];
+        if (dims == 3) {
+            if (std::fabs(1.0 - std::fabs(op[2])) <= 1e-12) {
+                T[0] = 1; T[1] = 0; T[2] = 0; S[0] = 0; S[1] = 1; S[2] = 0;
+            } else {
+                T[0] = -op[1]; T[1] = op[0]; T[2] = 0.0;
+                double tn = 1.0 / std::sqrt(T[0] * T[0] + T[1] * T[1]);
+                T[0] = T[0] * tn; T[1] = T[1] * tn;
+                S[0] = T[1] * op[2] - T[2] * op[1];
+                S[1] = T[2] * op[0] - T[0] * op[2];
+                S[2] = T[0] * op[1] - T[1] * op[0];
+            }
+        } else {
+            T[0] = -op[1]; T[1] = op[0]; T[2] = 0.0;
+        }
+        double mnT = 0, mxT = 0, mnS = 0, mxS = 0;
+        const int corners = dims == 3 ? 8 : 4;
+        for (int q = 0; q < corners; ++q) {
+            double cc[3] = { (q & 1) ? bmax[0] : bmin[0], (q & 2) ? bmax[1] : bmin[1],
+                             dims == 3 ? ((q & 4) ? bmax[2] : bmin[2]) : 0.0 };
+            double pT = (cc[0] - tg[0]) * T[0] + (cc[1] - tg[1]) * T[1] + (cc[2] - tg[2]) * T[2];
+            double pS = (cc[0] - tg[0]) * S[0] + (cc[1] - tg[1]) * S[1] + (cc[2] - tg[2]) * S[2];
+            if (q == 0 || pT < mnT) mnT = pT;
+            if (q == 0 || pT > mxT) mxT = pT;
+            if (q == 0 || pS < mnS) mnS = pS;
+            if (q == 0 || pS > mxS) mxS = pS;
+        }
+        for (int i = 0; i < 3; ++i) {
+            s->p[3 * k + i] = (float)d[i];
+            s->inv[3 * k + i] = (float)(std::fabs(d[i]) < 1e-12 ? 1e12 : 1.0 / d[i]);
+            s->tang[3 * k + i] = (float)tg[i];
+            s->pt[3 * k + i] = (float)T[i];
+            s->ps[3 * k + i] = (float)S[i];
+        }
+        s->mint[k] = (float)mnT; s->maxt[k] = (float)mxT;
+        s->mins[k] = (float)mnS; s->maxs[k] = (float)mxS;
+        s->sprob_d[k] = dims == 3 ? 1.0 / ((mxT - mnT) * (mxS - mnS)) : 1.0 / (mxT - mnT);
+        s->sprob[k] = (float)s->sprob_d[k];
+    }
+    return SSTMC_NO_ERROR;
+}
+
+int prep_source(Scene::HostSource* s, const sstmc_source_cfg* c, int dims, const double bmin[3], const double bmax[3])
+{
+    s->type = c->type; s->n = (int)c->count; s->is_area = c->is_area_source ? 1 : 0;
+    if (c->type == SSTMC_SOURCE_NONE) { s->n = 0; return SSTMC_NO_ERROR; }
+    if (c->count == 0 || c->xyz == nullptr) return SSTMC_INVALID_CONFIG;
+    if (c->type == SSTMC_SOURCE_FARFIELD) return prep_farfield(s, c, dims, bmin, bmax);
+    if (c->type != SSTMC_SOURCE_POINT) return SSTMC_NOT_SUPPORTED;
+    s->p.assign(3 * s->n, 0.f);
+    for (int k = 0; k < s->n; ++k) {
+        s->p[3 * k] = (float)c->xyz[3 * k];
+        s->p[3 * k + 1] = (float)c->xyz[3 * k + 1];
+        s->p[3 * k + 2] = dims == 3 ? (float)c->xyz[3 * k + 2] : 0.0f;
+    }
+    return SSTMC_NO_ERROR;
+}
+
+bool same_source(const Scene::HostSource& a, const Scene::HostSource& b)
+{
+    return a.type == b.type && a.n == b.n && a.is_area == b.is_area && a.p == b.p;
+}
+
+}  // namespace
+
+int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
+{
+    auto fail = [&](int code, const char* msg) { if (why) *why = msg; return code; };
+    if (cfg->dims != 2 && cfg->dims != 3) return fail(SSTMC_INVALID_CONFIG, "dims must be 2 or 3");
+    const int dims = S->dims = (int)cfg->dims;
+    if (cfg->is_cbs) return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS is not supported");
+    if (cfg->is_forced_inside_bin) return fail(SSTMC_NOT_SUPPORTED, "sampler.isForcedInsideBin is not supported");
+    if (cfg->batch_size == 0 || cfg->full_iteration == 0 || cfg->renderings_num == 0)
+        return fail(SSTMC_INVALID_CONFIG, "batchSize, fullIteration and renderingsNum must be positive");
+    if (!(cfg->lambda > 0)) return fail(SSTMC_INVALID_CONFIG, "lambda must be positive");
+    S->cfg_copy = *cfg;
+    S->P = cfg->batch_size; S->full_iter = cfg->full_iteration; S->renders = cfg->renderings_num;
+    S->seed = cfg->seed; S->device = cfg->device_number; S->precision = cfg->precision;
+    DevScene& D = S->dev;
+    std::memset(&D, 0, sizeof(D));
+    D.dims = dims; D.P = S->P; D.precision = cfg->precision;
+
+    // scattering
+    if (cfg->scattering_num == 0 || cfg->scattering_num > (uint32_t)kMat || !cfg->scattering_type)
+        return fail(SSTMC_INVALID_CONFIG, "scattering.type must have 1..10 cells");
+    int M = (int)cfg->scattering_num;
+    for (int m = 0; m < kMat; ++m) D.scat_type[m] = SSTMC_SCATTERING_NOT_DEFINED;
+    for (int m = 0; m < M; ++m) {
+        const int ty = cfg->scattering_type[m];
+        const double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
+        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN)
+            return fail(SSTMC_NOT_SUPPORTED, "only Isotropic and HenyeyGreenstein scattering are supported");
+        if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(g) < 1.0)) return fail(SSTMC_INVALID_CONFIG, "|g| must be < 1");
+        const int targets[2] = { m, 1 };
+        const int nt = (M == 1) ? 2 : 1;
+        for (int q = 0; q < nt; ++q) {
+            const int mm = targets[q];
+            D.scat_type[mm] = ty;
+            S->g_d[mm] = g;
+            D.g[mm] = (float)g;
+            D.gup[mm] = (float)(dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * kPi)) : (1.0 - g * g) / (4.0 * kPi));
+            D.gd1[mm] = (float)(1.0 + g * g);
+            D.gd2[mm] = (float)(-2.0 * g);
+        }
+    }
+    if (M == 1) M = 2;
+    S->M = M;
+    D.iso_all = 1;
+    for (int m = 0; m < kMat; ++m)
+        if (D.scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(D.g[m]) < 0.0001f)) D.iso_all = 0;
+    D.iso_amp = dims == 2 ? kIsoAmp2 : kIsoAmp3;
+    D.iso_pdf = dims == 2 ? kIsoPdf2 : kIsoPdf3;
+
+    // medium
+    double bmin[3] = { 0, 0, 0 }, bmax[3] = { 0, 0, 0 };
+    double sigs[kMat] = { 0 }, siga[kMat] = { 0 };
+    if (cfg->medium_type == SSTMC_MEDIUM_HOMOGENEOUS) {
+        if (M != 2) return fail(SSTMC_INVALID_CONFIG, "Homogeneous medium cannot have heterogeneous material.");
+        for (int a = 0; a < dims; ++a) {
+            if (!(cfg->box_max[a] > cfg->box_min[a])) return fail(SSTMC_INVALID_CONFIG, "boxMax must exceed boxMin");
+            S->ax[a] = { (float)cfg->box_min[a], (float)cfg->box_max[a] };
+        }
+        S->grid = { 1 };
+        sigs[1] = cfg->homogeneous_sigs;
+    } else if (cfg->medium_type == SSTMC_MEDIUM_HETEROGENEOUS) {
+        const double* axes[3] = { cfg->x_axis, cfg->y_axis, cfg->z_axis };
+        const uint32_t sizes[3] = { cfg->x_axis_size, cfg->y_axis_size, cfg->z_axis_size };
+        size_t cells = 1;
+        for (int a = 0; a < dims; ++a) {
+            if (!axes[a] || sizes[a] < 2) return fail(SSTMC_INVALID_CONFIG, "medium axes need at least 2 edges");
+            S->ax[a].resize(sizes[a]);
+            for (uint32_t i = 0; i < sizes[a]; ++i) {
+                S->ax[a][i] = (float)axes[a][i];
+                if (i > 0 && !(S->ax[a][i] > S->ax[a][i - 1])) return fail(SSTMC_INVALID_CONFIG, "medium axes must increase");
+            }
+            cells *= (size_t)(sizes[a] - 1);
+        }
+        if (!cfg->material_grid || !cfg->sigs) return fail(SSTMC_INVALID_CONFIG, "materialGrid and sigs are required");
+        S->grid.resize(cells);
+        for (size_t i = 0; i < cells; ++i) {
+            const uint32_t m = cfg->material_grid[i];
+            if (m == 0) return fail(SSTMC_INVALID_CONFIG, "Material 0 is only allowed outside the grid.");
+            if (m >= (uint32_t)M) return fail(SSTMC_INVALID_CONFIG, "materialGrid names an undefined material.");
+            S->grid[i] = (unsigned char)m;
+        }
+        for (int m = 0; m < M; ++m) { sigs[m] = cfg->sigs[m]; siga[m] = cfg->siga ? cfg->siga[m] : 0.0; }
+    } else {
+        return fail(SSTMC_NOT_SUPPORTED, "unsupported medium type");
+    }
+    {
+        bool seen[kMat] = { false };
+        for (unsigned char m : S->grid) seen[m] = true;
+        S->materials_present.clear();
+        for (int m = 1; m < kMat; ++m) if (seen[m]) S->materials_present.push_back(m);
+    }
+    for (int a = 0; a < dims; ++a) {
+        D.n[a] = (int)S->ax[a].size();
+        D.bmin[a] = S->ax[a].front(); D.bmax[a] = S->ax[a].back();
+        bmin[a] = (double)S->ax[a].front(); bmax[a] = (double)S->ax[a].back();
+        const double c = (bmax[a] + bmin[a]) * 0.5, r = (bmax[a] - bmin[a]) * 0.5;
+        D.center[a] = (float)c; D.radius[a] = (float)r;
+        D.inv_radius[a] = std::fabs(D.radius[a]) < 1e-12f ? 1e12f : 1.0f / D.radius[a];
+    }
+    float maxsigt = 0.0f;
+    for (int m = 0; m < kMat; ++m) {
+        if (sigs[m] < 0 || siga[m] < 0) return fail(SSTMC_INVALID_CONFIG, "sigs and siga must be non-negative");
+        const float ss = (float)sigs[m], sa = (float)siga[m];
+        D.sigt[m] = ss + sa;
+        D.survive[m] = D.sigt[m] > 0.0f ? ss / D.sigt[m] : 1.0f;
+        if (D.sigt[m] > maxsigt) maxsigt = D.sigt[m];
+    }
+    if (!(maxsigt > 0.0f)) return fail(SSTMC_INVALID_CONFIG, "the medium has no extinction (max sigt = 0)");
+    D.inv_maxsigt = 1.0f / maxsigt;
+    for (int m = 0; m < kMat; ++m) D.accept[m] = D.sigt[m] / maxsigt;
+
+    // sources
+    const sstmc_source_cfg* sc[4] = { &cfg->illumination, &cfg->view, &cfg->illumination2, &cfg->view2 };
+    for (int i = 0; i < 4; ++i) {
+        const int e = prep_source(&S->hsrc[i], sc[i], dims, bmin, bmax);
+        if (e) return fail(e, "invalid source");
+    }
+    if (S->hsrc[0].type == SSTMC_SOURCE_NONE || S->hsrc[1].type == SSTMC_SOURCE_NONE)
+        return fail(SSTMC_INVALID_CONFIG, "illumination and view are required");
+    S->Nl = S->hsrc[0].n; S->Nv = S->hsrc[1].n;
+
+    // sampler
+    if (!cfg->t || cfg->t_num == 0) return fail(SSTMC_INVALID_CONFIG, "sampler.t is required");
+    S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
+    if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return fail(SSTMC_INVALID_CONFIG, "unsupported sampler");
+    D.correlation = S->correlation ? 1 : 0;
+    if (S->correlation) {
+        if (S->hsrc[2].type == SSTMC_SOURCE_NONE || S->hsrc[3].type == SSTMC_SOURCE_NONE)
+            return fail(SSTMC_INVALID_CONFIG, "For correlation sampler, illumination2 and view2 must be entered");
+        if (S->hsrc[2].n != S->hsrc[0].n || S->hsrc[3].n != S->hsrc[1].n)
+            return fail(SSTMC_INVALID_CONFIG, "illumination2 / view2 must have the sizes of illumination / view");
+        if (S->hsrc[2].type != S->hsrc[0].type || S->hsrc[3].type != S->hsrc[1].type)
+            return fail(SSTMC_NOT_SUPPORTED, "illumination2 / view2 must have the types of illumination / view");
+        D.sym = same_source(S->hsrc[0], S->hsrc[2]) && same_source(S->hsrc[1], S->hsrc[3]);
+    }
+    D.temporal_amp = cfg->is_temporal_amplitude ? 1 : 0;
+    const int Nt = S->Nt = D.Nt = (int)cfg->t_num;
+    S->ticks.assign(cfg->t, cfg->t + Nt);
+    S->ticks_f.resize(Nt); S->abs_ticks.resize(Nt);
+    for (int t = 0; t < Nt; ++t) { S->ticks_f[t] = (float)S->ticks[t]; S->abs_ticks[t] = std::fabs(S->ticks_f[t]); }
+    double Dm[kMat];
+    double Um[kMat][3];
+    for (int m = 0; m < kMat; ++m) {
+        Dm[m] = (m < M && cfg->D) ? cfg->D[m] : 0.0;
+        if (Dm[m] < 0) return fail(SSTMC_INVALID_CONFIG, "D values in temporal sampler must be non-negative");
+        for (int i = 0; i < 3; ++i) Um[m][i] = (m < M && cfg->U && i < dims) ? cfg->U[3 * m + i] : 0.0;
+        D.D[m] = (float)Dm[m];
+        S->D_d[m] = Dm[m];
+        for (int i = 0; i < 3; ++i) D.U[m][i] = (float)Um[m][i];
+        D.static_corr[m] = D.U[m][0] == 0.0f && D.U[m][1] == 0.0f && D.U[m][2] == 0.0f;
+    }
+    // field sampler: ticks sorted around their mean (TemporalSampler.cuh:958-1150)
+    {
+        double mean = 0;
+        for (int t = 0; t < Nt; ++t) mean += S->ticks[t];
+        mean = mean / Nt;
+        std::vector<int> used(Nt, 0), negl, posl;
+        int nn = 0, np = 0;
+        for (int t = 0; t < Nt; ++t) { if (S->ticks[t] - mean < 0) nn++; else np++; }
+        for (int a = 0; a < nn; ++a) {
+            bool first = true; int idx = 0; double best = 0;
+            for (int t = 0; t < Nt; ++t) if (!used[t] && S->ticks[t] - mean < 0) {
+                if (first || mean - S->ticks[t] < best) { first = false; best = mean - S->ticks[t]; idx = t; }
+            }
+            used[idx] = 1; negl.push_back(idx);
+        }
+        for (int a = 0; a < np; ++a) {
+            bool first = true; int idx = 0; double best = 0;
+            for (int t = 0; t < Nt; ++t) if (!used[t] && S->ticks[t] - mean >= 0) {
+                if (first || S->ticks[t] - mean < best) { first = false; best = S->ticks[t] - mean; idx = t; }
+            }
+            used[idx] = 1; posl.push_back(idx);
+        }
+        D.neg = nn;
+        std::vector<double> dt(Nt);
+        int cn = 0, cp = 0, prev = -1;
+        for (int j = 0; j < Nt; ++j) {
+            int tick;
+            if (j < nn) { tick = negl[cn]; if (cn == 0) prev = -1; cn++; }
+            else { tick = posl[cp]; if (cp == 0) prev = -1; cp++; }
+            dt[j] = prev < 0 ? S->ticks[tick] - mean : S->ticks[tick] - S->ticks[prev];
+            prev = tick;
+        }
+        S->disp_scale.assign((size_t)kMat * Nt, 0.f);
+        S->disp_u.assign((size_t)kMat * Nt * 3, 0.f);
+        for (int m = 0; m < kMat; ++m) {
+            D.moving[m] = (Dm[m] != 0.0) || D.U[m][0] != 0.0f || D.U[m][1] != 0.0f || D.U[m][2] != 0.0f;
+            for (int j = 0; j < Nt; ++j) {
+                S->disp_scale[m * Nt + j] = (float)std::sqrt(2.0 * dims * Dm[m] * std::fabs(dt[j]));
+                for (int i = 0; i < 3; ++i) S->disp_u[(m * Nt + j) * 3 + i] = (float)(dt[j] * Um[m][i]);
+            }
+        }
+    }
+    D.inv_lambda = 1.0 / cfg->lambda;
+    D.inv_lambda_f = (float)D.inv_lambda;
+    D.k2 = (float)((2.0 * kPi / cfg->lambda) * (2.0 * kPi / cfg->lambda));
+
+    // upload
+    if (cudaSetDevice(S->device) != cudaSuccess) return fail(SSTMC_DEVICE_ERROR, "cudaSetDevice failed");
+    int e = 0;
+    for (int a = 0; a < dims && !e; ++a) e = upload(S, S->ax[a], &D.ax[a]);
+    if (!e) e = upload(S, S->grid, &D.grid);
+    if (!e) e = upload(S, S->disp_scale, &D.disp_scale);
+    if (!e) e = upload(S, S->disp_u, &D.disp_u);
+    if (!e) e = upload(S, S->ticks_f, &D.ticks_f);
+    if (!e) e = upload(S, S->abs_ticks, &D.abs_ticks);
+    for (int i = 0; i < 4 && !e; ++i) {
+        Scene::HostSource& h = S->hsrc[i];
+        DevSource& d = D.src[i];
+        d.type = h.type; d.n = h.n; d.is_area = h.is_area;
+        if (h.type == SSTMC_SOURCE_NONE) continue;
+        e = upload(S, h.p, &d.p);
+        if (!e && h.type == SSTMC_SOURCE_FARFIELD) {
+            e = upload(S, h.inv, &d.inv);
+            if (!e) e = upload(S, h.tang, &d.tang);
+            if (!e) e = upload(S, h.pt, &d.pt);
+            if (!e) e = upload(S, h.ps, &d.ps);
+            if (!e) e = upload(S, h.mint, &d.mint);
+            if (!e) e = upload(S, h.maxt, &d.maxt);
+            if (!e) e = upload(S, h.mins, &d.mins);
+            if (!e) e = upload(S, h.maxs, &d.maxs);
+            if (!e) e = upload(S, h.sprob, &d.sprob);
+        }
+    }
+    if (e) return fail(e, "device allocation failed");
+    return SSTMC_NO_ERROR;
+}
+
+}  // namespace sstmc

@@ -1,0 +1,105 @@
+// scene.h -- per-scene device descriptor and its host-side construction.
+//
+// The reference keeps every plugin's state in process-global __constant__
+// symbols (MediumNS::mediumGpuData, HeterogeneousMediumNS::*, ScatteringNS::*,
+// TemporalSamplerNS::*, Simulation.cuh:168-173), which allows one scene per
+// process.  Here a scene is a plain descriptor (DevScene) passed to every
+// kernel by value, pointing at device buffers the Scene owns, so any number
+// of scenes can be resident at once.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/sstmc.h"
+
+namespace sstmc {
+
+constexpr int kMat = SSTMC_MATERIAL_NUM;
+constexpr uint32_t kMaxAttempts = 1u << 20;
+constexpr uint32_t kMaxVertices = 1u << 20;
+constexpr uint32_t kMaxWoodcock = 1u << 22;
+constexpr double kPi = 3.14159265358979323846;
+constexpr float kIsoAmp2 = 0.398942280401432678f;
+constexpr float kIsoAmp3 = 0.282094791773878143f;
+constexpr float kIsoPdf2 = 0.159154943091895336f;
+constexpr float kIsoPdf3 = 0.079577471545947668f;
+
+// Source element tables.  FarField: p = unit direction and the sampling
+// tables of FarField.cuh:71-127 (fillBuffers).  PointSource: p = location.
+struct DevSource {
+    int type, n, is_area, pad;
+    const float* p;      // n*3
+    const float* inv;    // n*3 inverse direction
+    const float* tang;   // n*3 tangent point of the blocking circle
+    const float* pt;     // n*3 perpendicular T
+    const float* ps;     // n*3 perpendicular S (3D)
+    const float* mint;
+    const float* maxt;
+    const float* mins;
+    const float* maxs;
+    const float* sprob;  // projected-box sampling probability q_l
+};
+
+struct DevScene {
+    int dims, correlation, Nt, neg;
+    int temporal_amp, iso_all, precision, sym;  // sym: illumination2 == illumination and view2 == view
+    uint32_t P;
+    int n[3];
+    const float* ax[3];
+    const unsigned char* grid;
+    int scat_type[kMat];
+    float g[kMat], gup[kMat], gd1[kMat], gd2[kMat];
+    float sigt[kMat], accept[kMat], survive[kMat];
+    float inv_maxsigt;
+    float bmin[3], bmax[3], center[3], radius[3], inv_radius[3];
+    int moving[kMat];
+    int static_corr[kMat];       // correlation: U == 0 (shifted positions coincide)
+    float D[kMat];
+    float U[kMat][3];
+    const float* disp_scale;     // [kMat][Nt]
+    const float* disp_u;         // [kMat][Nt][3]
+    const float* ticks_f;        // [Nt] raw ticks (correlation)
+    const float* abs_ticks;      // [Nt]
+    double inv_lambda;
+    float inv_lambda_f;
+    float k2;                    // (2 pi / lambda)^2
+    float iso_amp, iso_pdf;
+    DevSource src[4];            // illumination, view, illumination2, view2
+};
+
+// Host-owned scene: normalised config, float tables and device buffers.
+struct Scene {
+    sstmc_config cfg_copy;       // scalars only: its pointers are not owned and not used after creation
+    int dims = 0, M = 0, Nl = 0, Nv = 0, Nt = 0;
+    uint32_t P = 0, full_iter = 1, renders = 1;
+    uint64_t seed = 0;
+    int device = 0;
+    int precision = SSTMC_PRECISION_SPLIT;
+    bool correlation = false;
+    // host tables (also kept for the W tables and tests)
+    struct HostSource {
+        int type = 0, n = 0, is_area = 0;
+        std::vector<float> p, inv, tang, pt, ps, mint, maxt, mins, maxs, sprob;
+        std::vector<double> sprob_d;
+    } hsrc[4];
+    std::vector<float> ax[3];
+    std::vector<unsigned char> grid;
+    std::vector<float> disp_scale, disp_u, ticks_f, abs_ticks;
+    std::vector<double> ticks;
+    double g_d[kMat] = { 0 };    // HG g per material (double, for the weight tables)
+    double D_d[kMat] = { 0 };    // Brownian D per material
+    DevScene dev{};
+    std::vector<void*> dev_allocs;
+    // materials present in the grid
+    std::vector<int> materials_present;
+    // last render statistics
+    uint64_t last_contrib = 0, last_dda = 0, last_vertices = 0, last_paths = 0;
+
+    ~Scene();
+};
+
+// Build (validation + tables) and upload.  Returns an SSTMC_* code.
+int build_scene(const sstmc_config* cfg, Scene* s, std::string* why);
+
+}  // namespace sstmc

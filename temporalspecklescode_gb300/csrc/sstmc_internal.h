@@ -1,0 +1,57 @@
+// sstmc_internal.h -- render engine state shared by api.cpp and serve.cpp.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "scene.h"
+#include "trace.h"
+
+namespace sstmc {
+
+constexpr int kMaxSlots = 32;  // view-accumulator slots per lane (8 KB of shared memory per warp)
+
+struct PathDebug {
+    int* nvert = nullptr;
+    int* misses = nullptr;
+    uint32_t* hash = nullptr;
+    uint32_t* dda = nullptr;
+};
+
+// Device buffers of one scene's renders: the per-path rows of a chunk of
+// paths, the FP64 accumulator and the far-field single-scattering weights.
+struct Engine {
+    cudaStream_t stream = nullptr;
+    uint32_t cap = 0;
+    float2 *a_ms = nullptr, *s_ms = nullptr, *a_ss = nullptr, *b_ss = nullptr, *g2 = nullptr;
+    float *pl = nullptr, *x1 = nullptr, *x1t = nullptr;
+    unsigned char* m1 = nullptr;
+    unsigned long long* totals = nullptr;
+    int* err = nullptr;
+    double2* V = nullptr;
+    float* W = nullptr;
+    // device timing of the last render: events around each kernel class
+    cudaEvent_t ev[8] = { nullptr };
+    double ms_trace = 0, ms_gemm = 0, ms_ss = 0, ms_total = 0;
+    uint64_t launches = 0;
+    bool timing = true;
+
+    static size_t bytes_per_path(const Scene& S);
+    int ensure(Scene& S, uint32_t paths);
+    void release();
+    int prepare_ss_tables(Scene& S);
+    void plan(const Scene& S, TraceParams& T, std::vector<std::pair<int, int>>* vchunks,
+              std::vector<std::pair<int, int>>* tchunks) const;
+    int trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, PathDebug* dbg);
+    int contract_chunk(Scene& S, uint32_t n);
+    int render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out);
+    int init_events();
+    void destroy_events();
+};
+
+int occupancy_blocks(int threads, size_t smem);
+void set_last_error_text(const std::string& s);
+
+}  // namespace sstmc

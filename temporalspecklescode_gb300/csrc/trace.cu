@@ -1,0 +1,434 @@
+// trace.cu -- the fused path-tracing kernel: one warp per path.
+//
+// Replaces the reference's per-bounce wavefront of ~30-60 synchronous launches
+// (NextEventEstimation::trace, NextEventEstimation.cuh:1461-1637): sampling
+// (TemporalSampler::sampleFirst/Second/Next, TemporalSampler.cuh:1324-1462;
+// TemporalCorrelationSampler.cuh:600-760), the per-vertex NEE vectors
+// (twoPointsThroughput / threePointsThroughput / pathContribution), the path
+// probabilities (pathProbabilitySingle/Multiple, NEE.cuh:853-1009) and the
+// per-path view-vector sum (multipleResMultiple's GvSum, NEE.cuh:1138-1395)
+// all happen in registers of one warp.  Lanes replay the same warp-uniform
+// FP32 walk and split the NEE work over (source element, tick) items, so
+// dead paths need no compaction (the reference's P x P permutation GEMMs,
+// NEE.cuh:681-759) and nothing per-vertex is written to HBM.  Per path the
+// kernel writes four rows -- the illumination and view vectors of the
+// multiple- and single-scattering terms -- which the contraction consumes.
+#include <cuda_runtime.h>
+
+#include "nee.cuh"
+#include "sstmc_internal.h"
+#include "trace.h"
+
+namespace sstmc {
+
+namespace {
+
+__device__ __forceinline__ uint32_t u1_count(const DevScene& S, uint64_t seed, uint32_t wave)
+{
+    Stream ws;
+    ws.init(seed, wave, 0u, kPurposeWave);
+    int c = (int)ceilf(fm(ws.uniform(), (float)(S.P + 1u))) - 1;
+    c = c < 0 ? 0 : (c > (int)S.P ? (int)S.P : c);
+    return (uint32_t)c;
+}
+
+__device__ __forceinline__ uint32_t hash_vertex(const DevScene& S, uint32_t h, const V3& x, int m)
+{
+    h = hash_mix(h, __float_as_uint(x.x));
+    h = hash_mix(h, __float_as_uint(x.y));
+    if (S.dims == 3) h = hash_mix(h, __float_as_uint(x.z));
+    return hash_mix(h, (uint32_t)m);
+}
+
+// Per-tick positions of a vertex of the field sampler (TemporalSampler.cuh:376-436,
+// 540-647, 778-937): Brownian displacement N(0, 2 dims D |dt|) along a random
+// direction plus dt U per sorted tick, cumulated outward from the mean tick.
+// Warp-cooperative; buf holds Nt*3 floats in output-tick order.
+__device__ void temporal_positions(const DevScene& S, uint64_t seed, uint32_t pid, uint32_t b,
+                                   const V3& x, int m, float* buf, int lane)
+{
+    const int Nt = S.Nt;
+    if (!S.moving[m]) {
+        for (int t = lane; t < Nt; t += 32) { buf[3 * t] = x.x; buf[3 * t + 1] = x.y; buf[3 * t + 2] = x.z; }
+        __syncwarp();
+        return;
+    }
+    for (int j = lane; j < Nt; j += 32) {
+        const float sc = S.disp_scale[m * Nt + j];
+        const float* du = S.disp_u + (m * Nt + j) * 3;
+        float dp[3] = { du[0], du[1], du[2] };
+        if (sc != 0.0f) {
+            Stream ts;
+            ts.init(seed, pid, b, kPurposeTemporal | ((uint32_t)j << 8));
+            const V3 w = random_direction(S.dims, ts);
+            const float u1 = ts.uniform();
+            const float u2 = ts.uniform();
+            const float r = fsq(fm(-2.0f, walk_logf(u1)));
+            float s, c;
+            walk_sincospif(fm(2.0f, u2), s, c);
+            const float dr = fm(fm(r, c), sc);
+            dp[0] = ffma(dr, w.x, du[0]);
+            dp[1] = ffma(dr, w.y, du[1]);
+            if (S.dims == 3) dp[2] = ffma(dr, w.z, du[2]);
+        }
+        buf[3 * j] = dp[0]; buf[3 * j + 1] = dp[1]; buf[3 * j + 2] = dp[2];
+    }
+    __syncwarp();
+    if (lane == 0) {
+        float c0 = x.x, c1 = x.y, c2 = x.z;
+        for (int j = 0; j < Nt; ++j) {
+            if (j == 0 || j == S.neg) { c0 = x.x; c1 = x.y; c2 = x.z; }
+            c0 = fa(c0, buf[3 * j]);
+            c1 = fa(c1, buf[3 * j + 1]);
+            if (S.dims == 3) c2 = fa(c2, buf[3 * j + 2]);
+            buf[3 * j] = c0; buf[3 * j + 1] = c1; buf[3 * j + 2] = c2;
+        }
+        // sorted index j -> output tick: the negative group is reversed
+        for (int j = 0; j < S.neg / 2; ++j) {
+            const int k = S.neg - 1 - j;
+            for (int i = 0; i < 3; ++i) { const float tmp = buf[3 * j + i]; buf[3 * j + i] = buf[3 * k + i]; buf[3 * k + i] = tmp; }
+        }
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ V3 tick_pos(const float* buf, int t) { return V3{ buf[3 * t], buf[3 * t + 1], buf[3 * t + 2] }; }
+
+__device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, int lane)
+{
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    if (T.pass0) {
+        for (int i = lane; i < Nt * Nl; i += 32) {
+            T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
+            T.a_ss[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
+        }
+        for (int i = lane; i < Nt * Nv; i += 32) T.b_ss[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
+    }
+    for (int t = T.t0; t < T.t0 + T.tn; ++t)
+        for (int v = T.v0 + lane; v < T.v0 + T.vn; v += 32) T.s_ms[((size_t)q * Nt + t) * Nv + v] = make_float2(0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+{
+    extern __shared__ double smem_d[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n, D = S.dims;
+    const bool corr = S.correlation != 0;
+    const bool split = S.precision == SSTMC_PRECISION_SPLIT;
+    // per-warp shared scratch: L[Nt] doubles, view accumulators [slots][32] float2
+    // (lane-major, conflict-free), two Nt*3 float tick-position buffers
+    const int nwb = blockDim.x >> 5;
+    double* Ls = smem_d + (size_t)wib * Nt;
+    float2* accs = reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)wib * T.slots * 32 + lane;
+    float* fbase = reinterpret_cast<float*>(reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)nwb * T.slots * 32);
+    float* bufA = fbase + (size_t)wib * 6 * Nt;
+    float* bufB = bufA + 3 * Nt;
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    const DevSource& il2 = S.src[2];
+    const DevSource& vw2 = S.src[3];
+
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t q = gw; q < T.paths; q += nw) {
+        const uint32_t pid = T.first_path + q;
+        const uint32_t slot = pid % S.P, wave = pid / S.P;
+        const bool side1 = !corr || slot < u1_count(S, T.seed, wave);
+        const DevSource& fsrc = side1 ? il : il2;
+
+        // ---- first vertex, with miss resampling (NEE.cuh:643-679) ----
+        V3 x0, d0, x1;
+        int m1 = 0;
+        uint32_t att = 0;
+        Stream rs;
+        bool ok = true;
+        for (att = 0; att < kMaxAttempts; ++att) {
+            rs.init(T.seed, pid, 1u, kPurposeWalk | (att << 8));
+            sample_source(S, fsrc, rs, x0, d0);
+            if (!woodcock(S, x0, d0, rs, x1, m1)) { ok = false; break; }
+            if (m1 > 0) break;
+        }
+        if (att >= kMaxAttempts) ok = false;
+        if (!ok) {
+            if (lane == 0) atomicExch(T.err, SSTMC_PATH_LIMIT);
+            zero_rows(S, T, q, lane);
+            continue;
+        }
+        const float xi1 = corr ? 0.0f : rs.uniform();
+        float* xtc = bufA;   // tick positions of the current vertex
+        float* xtn = bufB;   // tick positions of the new vertex
+        if (!corr) {
+            temporal_positions(S, T.seed, pid, 1u, x1, m1, xtc, lane);
+            for (int t = lane; t < Nt; t += 32) Ls[t] = 0.0;
+            __syncwarp();
+        }
+        const bool mov1 = !corr && S.moving[m1];
+        if (T.pass0 && T.x1t && !corr)
+            for (int i = lane; i < 3 * Nt; i += 32) T.x1t[(size_t)q * 3 * Nt + i] = xtc[i];
+        uint32_t steps = 0;
+        uint32_t h = hash_vertex(S, 2166136261u, x1, m1);
+        float p1inv = 0.0f;
+
+        // ---- illumination side at x1: P_l, Gl0, single-scattering rows ----
+        if (T.pass0) {
+            float ps = 0.0f;
+            for (int l = lane; l < Nl; l += 32) {
+                float P = pfirst(S, il, l, x1, steps);
+                if (corr) P = 0.5f * (P + pfirst(S, il2, l, x1, steps));
+                T.pl[(size_t)q * Nl + l] = P;
+                ps += P;
+            }
+            const float p1 = warp_sum(ps) / (float)Nl;
+            p1inv = corr ? 1.0f / p1 : 1.0f / sqrtf(p1);
+            const float2 e1 = corr ? make_float2(1.f, 0.f) : unit_phase(xi1);
+            const bool st1 = corr ? S.static_corr[m1] != 0 : !mov1;
+            const bool nophase = corr && S.sym && st1;
+            for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
+                uint32_t sts = 0;
+                if (st1) {
+                    g1s = gvec(S, il, l, x1, kRoleIllum, !nophase, sts);
+                    if (corr) g2s = nophase ? g1s : gvec(S, il2, l, x1, kRoleIllum, true, sts);
+                    if (nophase) sts *= 2;
+                }
+                for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                    float2 g1, g2 = make_float2(0.f, 0.f);
+                    if (st1) { g1 = g1s; g2 = g2s; steps += sts; }
+                    else if (!corr) g1 = gvec(S, il, l, tick_pos(xtc, t), kRoleIllum, true, steps);
+                    else {
+                        const float tau = S.ticks_f[t];
+                        g1 = gvec(S, il, l, shift_u(S, x1, m1, tau, -1.0f), kRoleIllum, true, steps);
+                        g2 = gvec(S, il2, l, shift_u(S, x1, m1, tau, 1.0f), kRoleIllum, true, steps);
+                    }
+                    const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                    T.a_ms[o] = g1;  // raw illumination vector, finished at x2
+                    if (corr) {
+                        T.g2[o] = g2;
+                        T.a_ss[o] = c_scale(c_mulc(g1, g2), p1inv);
+                    } else {
+                        T.a_ss[o] = c_scale(c_mul(g1, e1), p1inv);
+                    }
+                }
+            }
+            for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
+                float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
+                uint32_t sts = 0;
+                if (st1) {
+                    g1s = gvec(S, vw, v, x1, kRoleView, !nophase, sts);
+                    if (corr) g2s = nophase ? g1s : gvec(S, vw2, v, x1, kRoleView, true, sts);
+                    if (nophase) sts *= 2;
+                }
+                for (int t = lane / T.vwa; t < Nt; t += T.tga) {
+                    float2 b;
+                    if (st1) { b = corr ? c_mulc(g1s, g2s) : g1s; steps += sts; }
+                    else if (!corr) b = gvec(S, vw, v, tick_pos(xtc, t), kRoleView, true, steps);
+                    else {
+                        const float tau = S.ticks_f[t];
+                        const float2 g1 = gvec(S, vw, v, shift_u(S, x1, m1, tau, -1.0f), kRoleView, true, steps);
+                        const float2 g2 = gvec(S, vw2, v, shift_u(S, x1, m1, tau, 1.0f), kRoleView, true, steps);
+                        b = c_mulc(g1, g2);
+                    }
+                    T.b_ss[((size_t)q * Nt + t) * Nv + v] = b;
+                }
+            }
+        }
+
+        // ---- later vertices ----
+        for (int i = 0; i < T.slots; ++i) accs[32 * i] = make_float2(0.f, 0.f);
+        V3 prev = x0, cur = x1;
+        int mcur = m1;
+        uint32_t B = 1;
+        float MT = 0.0f;
+        for (uint32_t b = 2;; ++b) {
+            if (b > kMaxVertices) { ok = false; break; }
+            rs.init(T.seed, pid, b, kPurposeWalk);
+            const V3 din = normalize32(D, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
+            const V3 nd = sample_direction(S, mcur, din, rs);
+            V3 xn;
+            int mn = 0;
+            if (!woodcock(S, cur, nd, rs, xn, mn)) { ok = false; break; }
+            if (mn == 0) break;
+            const float xin = corr ? 0.0f : rs.uniform();
+            B = b;
+            h = hash_vertex(S, h, xn, mn);
+            if (corr && b >= 3) {
+                // momentum transfer of the inner vertex cur (TemporalSamplerCorrelation.cuh:144-179)
+                const V3 u = unit3(sub3(cur, prev)), w = unit3(sub3(xn, cur));
+                const V3 dq = sub3(u, w);
+                MT += S.D[mcur] * dot3(dq, dq);
+            }
+            if (!corr) {
+                temporal_positions(S, T.seed, pid, b, xn, mn, xtn, lane);
+                for (int t = lane; t < Nt; t += 32) {
+                    const V3 a = tick_pos(xtc, t), c = tick_pos(xtn, t);
+                    if (split) {
+                        const double dx = (double)c.x - (double)a.x, dy = (double)c.y - (double)a.y, dz = (double)c.z - (double)a.z;
+                        Ls[t] += sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+                    } else {
+                        const V3 dd = sub3(c, a);
+                        Ls[t] = (double)((float)Ls[t] + sqrtf(dot3(dd, dd)));
+                    }
+                }
+                __syncwarp();
+            }
+
+            // multiple-scattering illumination vector at x2 (NEE.cuh:1525-1559, 889-1009)
+            if (b == 2 && T.pass0) {
+                const V3 x12 = unit3(sub3(xn, x1));
+                float ps = 0.0f;
+                for (int l = lane; l < Nl; l += 32)
+                    ps += T.pl[(size_t)q * Nl + l] * pdf_dirs(S, m1, src_in(il, l, x1), x12);
+                const float p2 = warp_sum(ps) / (float)Nl;
+                const float p2inv = corr ? 1.0f / p2 : 1.0f / sqrtf(p2);
+                for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                    for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                        const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                        const float2 g1 = T.a_ms[o];
+                        if (!corr) {
+                            const V3 pa = S.temporal_amp ? tick_pos(xtc, t) : x1;
+                            const V3 pb = S.temporal_amp ? tick_pos(xtn, t) : xn;
+                            T.a_ms[o] = c_scale(g1, famp_illum(S, il, l, pa, pb, m1) * p2inv);
+                        } else {
+                            const float tau = S.ticks_f[t];
+                            const V3 pa = shift_u(S, x1, m1, tau, -1.0f), pb = shift_u(S, xn, mn, tau, -1.0f);
+                            const float f1 = famp_illum(S, il, l, pa, pb, m1);
+                            const float f2 = famp_illum(S, il2, l, pa, pb, m1);
+                            const V3 i1 = src_in(il, l, x1), i2 = src_in(il2, l, x1);
+                            const V3 qv = V3{ 0.5f * (i1.x + i2.x) - x12.x, 0.5f * (i1.y + i2.y) - x12.y, 0.5f * (i1.z + i2.z) - x12.z };
+                            const float c1 = expf(-S.k2 * S.D[m1] * S.abs_ticks[t] * dot3(qv, qv));
+                            T.a_ms[o] = c_scale(c_mulc(g1, T.g2[o]), f1 * f2 * p2inv * c1);
+                        }
+                    }
+                }
+            }
+
+            // view vectors at vertex b, summed over the path (multipleResMultiple)
+            const bool stn = corr ? S.static_corr[mn] != 0 : !S.moving[mn];
+            const bool nophase = corr && S.sym && stn;
+            const float ptk = corr ? S.k2 * MT : 0.0f;
+            int j = 0;
+            for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
+                float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
+                uint32_t sts = 0;
+                float c1k = 0.0f, f12s = 0.0f;
+                if (stn) {
+                    g1s = gvec(S, vw, v, xn, kRoleView, corr ? !nophase : true, sts);
+                    if (corr) g2s = nophase ? g1s : gvec(S, vw2, v, xn, kRoleView, true, sts);
+                    if (nophase) sts *= 2;
+                }
+                if (corr) {
+                    const V3 o1 = src_out(vw, v, xn), o2 = src_out(vw2, v, xn);
+                    const V3 back = unit3(sub3(cur, xn));
+                    const V3 qv = V3{ -0.5f * (o1.x + o2.x) - back.x, -0.5f * (o1.y + o2.y) - back.y, -0.5f * (o1.z + o2.z) - back.z };
+                    c1k = S.k2 * S.D[mn] * dot3(qv, qv);
+                    if (stn && S.static_corr[mcur]) {
+                        f12s = famp_view(S, vw, v, xn, cur, mn) * famp_view(S, vw2, v, xn, cur, mn);
+                    }
+                }
+                int k = 0;
+                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
+                    float2 c;
+                    if (!corr) {
+                        const V3 xb = tick_pos(xtn, t);
+                        const float2 g = stn ? g1s : gvec(S, vw, v, xb, kRoleView, true, steps);
+                        if (stn) steps += sts;
+                        const V3 pa = S.temporal_amp ? xb : xn;
+                        const V3 pb = S.temporal_amp ? tick_pos(xtc, t) : cur;
+                        const float f = famp_view(S, vw, v, pa, pb, mn);
+                        float fr;
+                        if (split) fr = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
+                        else { const float ph = (float)Ls[t] * S.inv_lambda_f + xin; fr = ph - rintf(ph); }
+                        c = c_scale(c_mul(g, unit_phase(fr)), f);
+                    } else {
+                        const float tau = S.ticks_f[t];
+                        float2 g1, g2;
+                        if (stn) { g1 = g1s; g2 = g2s; steps += sts; }
+                        else {
+                            g1 = gvec(S, vw, v, shift_u(S, xn, mn, tau, -1.0f), kRoleView, true, steps);
+                            g2 = gvec(S, vw2, v, shift_u(S, xn, mn, tau, 1.0f), kRoleView, true, steps);
+                        }
+                        float f12;
+                        if (stn && S.static_corr[mcur]) f12 = f12s;
+                        else {
+                            const V3 pa = shift_u(S, xn, mn, tau, -1.0f), pb = shift_u(S, cur, mcur, tau, -1.0f);
+                            f12 = famp_view(S, vw, v, pa, pb, mn) * famp_view(S, vw2, v, pa, pb, mn);
+                        }
+                        const float dec = expf(-(c1k + ptk) * S.abs_ticks[t]);
+                        c = c_scale(c_mulc(g1, g2), f12 * dec);
+                    }
+                    float2* a = accs + 32 * (j * T.tpl + k);
+                    const float2 av = *a;
+                    *a = make_float2(av.x + c.x, av.y + c.y);
+                }
+            }
+            prev = cur;
+            cur = xn;
+            mcur = mn;
+            float* tmp = xtc; xtc = xtn; xtn = tmp;
+        }
+        if (!ok) {
+            if (lane == 0) atomicExch(T.err, SSTMC_PATH_LIMIT);
+            zero_rows(S, T, q, lane);
+            continue;
+        }
+        if (T.pass0 && B < 2) {
+            for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
+        }
+        // write the summed view vector of this chunk
+        {
+            int j = 0;
+            for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
+                int k = 0;
+                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
+                    T.s_ms[((size_t)q * Nt + t) * Nv + v] = accs[32 * (j * T.tpl + k)];
+                }
+            }
+        }
+        const uint32_t wsteps = warp_sum_u32(steps);
+        if (lane == 0) {
+            if (T.pass0) {
+                if (T.nvert) T.nvert[q] = (int)B;
+                if (T.misses) T.misses[q] = (int)att;
+                if (T.hash) T.hash[q] = h;
+                if (T.m1) T.m1[q] = (unsigned char)m1;
+                if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
+                atomicAdd(T.totals + 0, (unsigned long long)B);
+                atomicAdd(T.totals + 2, (unsigned long long)att);
+                atomicAdd(T.totals + 3, 1ull);
+            }
+            if (T.dda) atomicAdd(T.dda + q, wsteps);
+            atomicAdd(T.totals + 1, (unsigned long long)wsteps);
+        }
+    }
+}
+
+}  // namespace
+
+size_t trace_smem_bytes(int Nt, int slots, int threads)
+{
+    const int warps = threads / 32;
+    return (size_t)warps * Nt * sizeof(double) + (size_t)warps * slots * 32 * sizeof(float2)
+         + (size_t)warps * 6 * Nt * sizeof(float);
+}
+
+int occupancy_blocks(int threads, size_t smem)
+{
+    if (smem > 48 * 1024) cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_kernel, threads, smem) != cudaSuccess) n = 1;
+    return n > 0 ? n : 1;
+}
+
+int launch_trace(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream)
+{
+    const size_t smem = trace_smem_bytes(S.Nt, T.slots, threads);
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return SSTMC_KERNEL_ERROR;
+    }
+    trace_kernel<<<blocks, threads, smem, stream>>>(S, T);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
+
+}  // namespace sstmc

@@ -1,0 +1,40 @@
+// trace.h -- launch interface of the path-tracing kernel (trace.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "scene.h"
+
+namespace sstmc {
+
+// One launch traces paths [first_path, first_path + paths) of a rendering.
+// Path id = wave * batchSize + slot.  Rows are indexed by q = id - first_path.
+struct TraceParams {
+    uint64_t seed;
+    uint32_t first_path, paths;
+    int pass0;            // 1: write the illumination rows, single-scattering rows and stats
+    int v0, vn, t0, tn;   // view / tick chunk accumulated by this pass
+    int vw, tg, tpl;      // lanes: view = v0 + lane % vw + vw*j, tick = t0 + lane / vw + tg*k, k < tpl
+    int slots;            // accumulator slots per lane (vpl * tpl)
+    int lw, lg;           // illumination-side lane split (all ticks)
+    int vwa, tga;         // single-scattering view-side lane split (all views, all ticks)
+    float2* a_ms;         // [paths][Nt][Nl]
+    float2* s_ms;         // [paths][Nt][Nv]
+    float2* a_ss;         // [paths][Nt][Nl]
+    float2* b_ss;         // [paths][Nt][Nv]
+    float2* g2;           // [paths][Nt][Nl] (correlation scratch)
+    float* pl;            // [paths][Nl] first-point probability terms
+    float* x1;            // [paths][3]
+    float* x1t;           // [paths][Nt][3] or null
+    unsigned char* m1;    // [paths]
+    int* nvert;           // [paths] or null
+    int* misses;          // [paths] or null
+    uint32_t* hash;       // [paths] or null
+    uint32_t* dda;        // [paths] or null (accumulated over passes)
+    unsigned long long* totals;  // [0] vertices, [1] dda steps, [2] misses, [3] paths
+    int* err;
+};
+
+size_t trace_smem_bytes(int Nt, int slots, int threads);
+int launch_trace(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream);
+
+}  // namespace sstmc

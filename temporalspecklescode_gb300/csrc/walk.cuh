@@ -1,0 +1,271 @@
+// walk.cuh -- FP32 random walk and voxel traversal (decision path).
+//
+// Restates, per path and on the GPU:
+//   Woodcock free flight + absorption roulette  HeterogeneousMedium.cuh:576-678
+//   outside-point "ray hits box" test           HeterogeneousMedium.cuh:269-383 (bdDistance)
+//   voxel lookup                                Simulation.cuh:325-367, HeterogeneousMedium.cuh:260-267
+//   voxel traversal (attenuation)               HeterogeneousMedium.cuh:386-573
+//   far-field / point first-vertex sampling     FarField.cuh:129-205, PointSource.cuh:72-90
+//   phase-function sampling (Iso, HG)           Scattering.cuh:1039-1115
+//   direction rotation, random direction        VectorType.cuh:261-282, 316-362
+// The traversal is parametric (face distances from the ray origin, not from
+// an advanced point) so rounding does not accumulate along long rays.
+#pragma once
+#include "device_math.cuh"
+#include "scene.h"
+
+namespace sstmc {
+
+struct V3 { float x, y, z; };
+
+__device__ __forceinline__ float comp(const V3& v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+__device__ __forceinline__ V3 load3(const float* p, int k) { return V3{ p[3 * k], p[3 * k + 1], p[3 * k + 2] }; }
+
+__device__ __forceinline__ bool inside(const DevScene& S, const V3& p)
+{
+    bool in = p.x >= S.bmin[0] && p.x <= S.bmax[0] && p.y >= S.bmin[1] && p.y <= S.bmax[1];
+    if (S.dims == 3) in = in && p.z >= S.bmin[2] && p.z <= S.bmax[2];
+    return in;
+}
+
+// cell c with ax[c] <= x < ax[c+1], clamped to [0, n-2]
+__device__ __forceinline__ int bin_of(const float* ax, int n, float x)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(ax + mid) <= x) lo = mid + 1; else hi = mid;
+    }
+    int c = lo - 1;
+    c = c < 0 ? 0 : c;
+    c = c > n - 2 ? n - 2 : c;
+    return c;
+}
+
+__device__ __forceinline__ int material_at(const DevScene& S, const V3& p)
+{
+    const int ix = bin_of(S.ax[0], S.n[0], p.x);
+    const int iy = bin_of(S.ax[1], S.n[1], p.y);
+    int idx = ix + iy * (S.n[0] - 1);
+    if (S.dims == 3) idx += bin_of(S.ax[2], S.n[2], p.z) * (S.n[0] - 1) * (S.n[1] - 1);
+    return __ldg(S.grid + idx);
+}
+
+__device__ inline bool points_toward(const DevScene& S, const V3& p, const V3& d)
+{
+    const int D = S.dims;
+    float o[3], inv[3], dist[3];
+    float mx = 0.0f;
+    for (int i = 0; i < D; ++i) {
+        o[i] = fsb(comp(p, i), S.center[i]);
+        const float a = fm(fabsf(o[i]), S.inv_radius[i]);
+        if (i == 0 || a > mx) mx = a;
+        const float di = comp(d, i);
+        inv[i] = fabsf(di) < 1e-12f ? 1e12f : fdv(1.0f, di);
+    }
+    const float winding = mx <= 1.0f ? -1.0f : 1.0f;
+    for (int i = 0; i < D; ++i) {
+        const float sg = comp(d, i) < 0.0f ? 1.0f : -1.0f;
+        dist[i] = fm(inv[i], fsb(fm(S.radius[i], winding * sg), o[i]));
+    }
+    for (int i = 0; i < D; ++i) {
+        if (!(dist[i] >= 0.0f)) continue;
+        bool ok = true;
+        for (int j = 0; j < D; ++j) {
+            if (j == i) continue;
+            if (!(fabsf(ffma(comp(d, j), dist[i], o[j])) < S.radius[j])) ok = false;
+        }
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ V3 normalize32(int dims, const V3& v)
+{
+    const float s = dims == 3 ? ffma(v.x, v.x, ffma(v.y, v.y, fm(v.z, v.z))) : ffma(v.x, v.x, fm(v.y, v.y));
+    if (!(s > 0.0f)) return dims == 3 ? V3{ 0.f, 0.f, 1.f } : V3{ 0.f, 1.f, 0.f };
+    const float inv = fdv(1.0f, fsq(s));
+    return V3{ fm(v.x, inv), fm(v.y, inv), dims == 3 ? fm(v.z, inv) : 0.0f };
+}
+
+__device__ __forceinline__ V3 random_direction(int dims, Stream& rs)
+{
+    if (dims == 2) {
+        float s, c;
+        walk_sincospif(fm(2.0f, rs.uniform()), s, c);
+        return V3{ s, c, 0.0f };
+    }
+    float sp, cp;
+    walk_sincospif(fm(2.0f, rs.uniform()), sp, cp);
+    const float ct = ffma(rs.uniform(), 2.0f, -1.0f);
+    const float st = fsq(fmaxf(0.0f, fsb(1.0f, fm(ct, ct))));
+    return V3{ fm(st, cp), fm(st, sp), ct };
+}
+
+__device__ inline V3 sample_direction(const DevScene& S, int m, const V3& din, Stream& rs)
+{
+    if (S.scat_type[m] != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return random_direction(S.dims, rs);
+    const float g = S.g[m];
+    float c;
+    if (fabsf(g) < 0.001f) {
+        c = fsb(fm(rs.uniform(), 2.0f), 1.0f);
+    } else {
+        const float xi = rs.uniform();
+        if (S.dims == 2) {
+            const float a = fdv(fsb(1.0f, g), fa(1.0f, g));
+            float sp, cp;
+            walk_sincospif(xi, sp, cp);
+            const float s2 = fm(sp, sp);
+            const float ac = fm(a, cp);
+            const float ac2 = fm(ac, ac);
+            c = fdv(fsb(s2, ac2), fa(s2, ac2));
+        } else {
+            const float gg = fm(g, g);
+            const float s = fdv(fsb(1.0f, gg), ffma(fm(2.0f, g), xi, fsb(1.0f, g)));
+            c = fdv(fsb(fa(1.0f, gg), fm(s, s)), fm(2.0f, g));
+        }
+    }
+    const float sgn = rs.uniform() < 0.5f ? -1.0f : 1.0f;
+    const float sa = fm(sgn, fsq(fmaxf(0.0f, fsb(1.0f, fm(c, c)))));
+    if (S.dims == 2) {
+        return V3{ fsb(fm(din.x, c), fm(din.y, sa)), fa(fm(din.x, sa), fm(din.y, c)), 0.0f };
+    }
+    float sphi, cphi;
+    walk_sincospif(fm(2.0f, rs.uniform()), sphi, cphi);
+    if (fabsf(din.z) > 1.0f - 1e-6f) {
+        return V3{ fm(sa, cphi), fm(sa, sphi), fm(c, signbit(din.z) ? -1.0f : 1.0f) };
+    }
+    const float st = fsq(fsb(1.0f, fm(din.z, din.z)));
+    const float nx = fsb(fm(fm(din.x, din.z), cphi), fm(din.y, sphi));
+    const float ny = fa(fm(fm(din.y, din.z), cphi), fm(din.x, sphi));
+    return V3{ fa(fdv(fm(sa, nx), st), fm(din.x, c)),
+               fa(fdv(fm(sa, ny), st), fm(din.y, c)),
+               fa(fm(fm(-sa, cphi), st), fm(din.z, c)) };
+}
+
+// Woodcock free flight from o along d; returns false if the step limit ran out.
+__device__ inline bool woodcock(const DevScene& S, const V3& o, const V3& d, Stream& rs, V3& out, int& mat)
+{
+    float dist = 0.0f;
+    V3 p = o;
+    int m = 0;
+    uint32_t steps = 0;
+    for (;;) {
+        if (++steps > kMaxWoodcock) return false;
+        const float u = rs.uniform();
+        dist = fa(dist, fm(-walk_logf(u), S.inv_maxsigt));
+        p.x = ffma(dist, d.x, o.x);
+        p.y = ffma(dist, d.y, o.y);
+        if (S.dims == 3) p.z = ffma(dist, d.z, o.z);
+        if (!inside(S, p)) {
+            if (!points_toward(S, p, d)) break;
+        } else {
+            m = material_at(S, p);
+            if (rs.uniform() <= S.accept[m]) break;
+        }
+    }
+    if (S.dims == 2) p.z = 0.0f;
+    out = p;
+    if (inside(S, p)) mat = (rs.uniform() > S.survive[m]) ? 0 : m;
+    else mat = 0;
+    return true;
+}
+
+__device__ inline void sample_source(const DevScene& S, const DevSource& src, Stream& rs, V3& x0, V3& d0)
+{
+    const int D = S.dims;
+    int l = (int)ceilf(fm(rs.uniform(), (float)src.n)) - 1;
+    l = l < 0 ? 0 : (l > src.n - 1 ? src.n - 1 : l);
+    if (src.type == SSTMC_SOURCE_POINT) {
+        x0 = load3(src.p, l);
+        d0 = random_direction(D, rs);
+        return;
+    }
+    const V3 dir = load3(src.p, l);
+    const float mnt = src.mint[l], mxt = src.maxt[l];
+    const float st = fa(mnt, fm(rs.uniform(), fsb(mxt, mnt)));
+    const V3 tg = load3(src.tang, l), pt = load3(src.pt, l);
+    float p[3] = { fa(tg.x, fm(st, pt.x)), fa(tg.y, fm(st, pt.y)), fa(tg.z, fm(st, pt.z)) };
+    if (D == 3) {
+        const float mns = src.mins[l], mxs = src.maxs[l];
+        const float ss = fa(mns, fm(rs.uniform(), fsb(mxs, mns)));
+        const V3 ps = load3(src.ps, l);
+        p[0] = fa(p[0], fm(ss, ps.x)); p[1] = fa(p[1], fm(ss, ps.y)); p[2] = fa(p[2], fm(ss, ps.z));
+    }
+    const V3 inv = load3(src.inv, l);
+    float sh[3], dist[3];
+    for (int i = 0; i < D; ++i) {
+        sh[i] = fsb(p[i], S.center[i]);
+        const float sg = comp(dir, i) < 0.0f ? 1.0f : -1.0f;
+        dist[i] = fm(comp(inv, i), fsb(fm(S.radius[i], sg), sh[i]));
+    }
+    float bd = 0.0f;
+    for (int i = 0; i < D; ++i) {
+        bool ok = dist[i] >= 0.0f;
+        for (int j = 0; j < D && ok; ++j) {
+            if (j == i) continue;
+            if (!(fabsf(ffma(comp(dir, j), dist[i], sh[j])) < S.radius[j])) ok = false;
+        }
+        if (ok) { bd = dist[i]; break; }
+    }
+    const float step = fa(bd, 1e-12f);
+    x0 = V3{ fa(p[0], fm(step, dir.x)), fa(p[1], fm(step, dir.y)), D == 3 ? fa(p[2], fm(step, dir.z)) : 0.0f };
+    d0 = V3{ dir.x, dir.y, D == 3 ? dir.z : 0.0f };
+}
+
+// FP32 parametric voxel traversal from o along d.  Returns the optical depth;
+// `steps` counts the voxels crossed.  Termination: every iteration moves one
+// axis' cell index monotonically toward that axis' far edge.
+__device__ inline float dda(const DevScene& S, const V3& o, const V3& d, uint32_t& steps)
+{
+    const int D = S.dims;
+    if (!inside(S, o)) return 0.0f;
+    // single cell: one step (same arithmetic as the general loop's first step)
+    if (S.n[0] == 2 && S.n[1] == 2 && (D == 2 || S.n[2] == 2)) {
+        float tn[3] = { 0.0f, 0.0f, 0.0f };
+        for (int i = 0; i < D; ++i) {
+            const float di = comp(d, i);
+            const float inv = fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di);
+            const float face = di < 0.0f ? S.bmin[i] : S.bmax[i];
+            tn[i] = fm(fsb(face, comp(o, i)), inv);
+        }
+        const int a = D == 2 ? (tn[0] < tn[1] ? 0 : 1) : ((tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2));
+        steps += 1;
+        return ffma(tn[a], S.sigt[__ldg(S.grid)], 0.0f);
+    }
+    float inv[3];
+    int sg[3], bin[3];
+    for (int i = 0; i < D; ++i) {
+        const float di = comp(d, i);
+        inv[i] = fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di);
+        sg[i] = di < 0.0f ? -1 : 1;
+        bin[i] = bin_of(S.ax[i], S.n[i], comp(o, i));
+    }
+    if (D == 2) { inv[2] = 0.0f; sg[2] = 1; bin[2] = 0; }
+    const int sx = S.n[0] - 1, sxy = (S.n[0] - 1) * (S.n[1] - 1);
+    float t = 0.0f, acc = 0.0f;
+    uint32_t n = 0;
+    const uint32_t limit = (uint32_t)(S.n[0] + S.n[1] + (D == 3 ? S.n[2] : 0)) + 4u;
+    for (;;) {
+        float tn[3];
+        for (int i = 0; i < D; ++i) {
+            const float face = __ldg(S.ax[i] + bin[i] + (sg[i] > 0 ? 1 : 0));
+            tn[i] = fm(fsb(face, comp(o, i)), inv[i]);
+        }
+        int a;
+        if (D == 2) a = tn[0] < tn[1] ? 0 : 1;
+        else a = (tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2);
+        const int idx = bin[0] + bin[1] * sx + (D == 3 ? bin[2] * sxy : 0);
+        const float tna = tn[a];
+        acc = ffma(fsb(tna, t), S.sigt[__ldg(S.grid + idx)], acc);
+        t = tna;
+        ++n;
+        const int ba = bin[a];
+        if ((sg[a] < 0 && ba == 0) || (sg[a] > 0 && ba == S.n[a] - 2) || n >= limit) break;
+        bin[a] = ba + sg[a];
+    }
+    steps += n;
+    return acc;
+}
+
+}  // namespace sstmc

@@ -1,0 +1,179 @@
+"""Seeded synthetic scenes of the benchmark configurations.
+
+Each function returns ``(config, dims)`` with ``config`` a MATLAB-style dict
+(see :mod:`config`).  The reference publishes no benchmark scenes; these are
+the synthetic stand-ins with the stated shapes and value distributions.
+Random draws use ``numpy.random.default_rng(seed)``.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def _farfield_fan(n: int, half_angle: float = math.pi / 6):
+    th = -half_angle + np.arange(n) * (2 * half_angle) / (n - 1)
+    return {"x": np.sin(th), "y": np.cos(th)}
+
+
+def speckle_2d(batch_size: int = 1024, full_iteration: int = 64, n_dirs: int = 16, seed: int = 0):
+    """2D plain method: single-bin box [-50,50]^2, sigs=[0,1], HG g=0.8,
+    16 far-field illuminations and views over [-pi/6, pi/6] about +y, t=[0]."""
+    d = _farfield_fan(n_dirs)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "renderingsNum": 1,
+                       "lambda": 1.0, "seed": seed},
+        "scattering": {"type": ["HG", "HG"], "amplitudeFunction": [0.8, 0.8]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-50.0, 50.0], "yAxis": [-50.0, 50.0],
+                   "materialGrid": np.ones((1, 1), dtype=np.uint32), "sigs": [0.0, 1.0], "siga": [0.0, 0.0]},
+        "illumination": {"type": "FarField", "direction": d},
+        "view": {"type": "FarField", "direction": d},
+        "sampler": {"type": "TemporalSampler", "t": [0.0], "D": [0.0, 0.0], "U": {"x": [0.0, 0.0], "y": [0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
+def _jittered_lattice(n_side: int, half: float, rng: np.random.Generator):
+    cell = 2 * half / n_side
+    c = -half + cell * (np.arange(n_side) + 0.5)
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    X = X.ravel() + rng.uniform(-cell / 4, cell / 4, X.size)
+    Y = Y.ravel() + rng.uniform(-cell / 4, cell / 4, Y.size)
+    return X, Y
+
+
+def correlation_3d(batch_size: int = 1 << 20, full_iteration: int = 4, n_side: int = 8, n_lags: int = 8,
+                   dt: float = 1.0, seed: int = 0, lattice_seed: int = 2):
+    """3D temporal correlation: slab x,y in [-100,100], z in [0,20], sigs=[0,0.5],
+    siga=[0,0.01], HG g=0.9; 64 point illuminations on a jittered 8x8 lattice in
+    z=-5 and 64 point views in z=25; Brownian D=[0,1e-3], U=0; 8 lags k*dt."""
+    rng = np.random.default_rng(lattice_seed)
+    ix, iy = _jittered_lattice(n_side, 100.0, rng)
+    vx, vy = _jittered_lattice(n_side, 100.0, rng)
+    ill = {"type": "PointSource", "location": {"x": ix, "y": iy, "z": np.full(ix.size, -5.0)}}
+    view = {"type": "PointSource", "location": {"x": vx, "y": vy, "z": np.full(vx.size, 25.0)}}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "renderingsNum": 1,
+                       "lambda": 1.0, "seed": seed},
+        "scattering": {"type": ["HG", "HG"], "amplitudeFunction": [0.9, 0.9]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-100.0, 100.0], "yAxis": [-100.0, 100.0], "zAxis": [0.0, 20.0],
+                   "materialGrid": np.ones((1, 1, 1), dtype=np.uint32), "sigs": [0.0, 0.5], "siga": [0.0, 0.01]},
+        "illumination": ill,
+        "view": view,
+        "illumination2": ill,
+        "view2": view,
+        "sampler": {"type": "TemporalCorrelationSampler", "t": dt * np.arange(1, n_lags + 1),
+                    "D": [0.0, 1e-3], "U": {"x": [0.0, 0.0], "y": [0.0, 0.0], "z": [0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
+def _cone_dirs(n: int, half_angle_deg: float, rng: np.random.Generator):
+    ca = math.cos(math.radians(half_angle_deg))
+    ct = rng.uniform(ca, 1.0, n)
+    ph = rng.uniform(0.0, 2 * math.pi, n)
+    st = np.sqrt(1 - ct * ct)
+    return {"x": st * np.cos(ph), "y": st * np.sin(ph), "z": ct}
+
+
+def transmission_matrix_3d(batch_size: int = 1 << 18, full_iteration: int = 64, n_dirs: int = 1024,
+                           grid=(64, 64, 32), seed: int = 0):
+    """3D heterogeneous transmission matrix: 64x64x32 voxels over [-64,64]^2 x [0,64],
+    materials iid uniform {1..4} (seed 1), sigs=[0,.5,1,2,4], siga=[0,.01,.01,.02,.05],
+    HG g=0.85; 1024 far-field illuminations and views on a 20-degree cone about +z
+    (seeds 3, 4)."""
+    nx, ny, nz = grid
+    grid_rng = np.random.default_rng(1)
+    mg = grid_rng.integers(1, 5, size=(nx, ny, nz)).astype(np.uint32)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "renderingsNum": 1,
+                       "lambda": 1.0, "seed": seed},
+        "scattering": {"type": ["HG"] * 5, "amplitudeFunction": [0.85] * 5},
+        "medium": {"type": "Heterogeneous", "xAxis": np.linspace(-64, 64, nx + 1), "yAxis": np.linspace(-64, 64, ny + 1),
+                   "zAxis": np.linspace(0, 64, nz + 1), "materialGrid": mg,
+                   "sigs": [0.0, 0.5, 1.0, 2.0, 4.0], "siga": [0.0, 0.01, 0.01, 0.02, 0.05]},
+        "illumination": {"type": "FarField", "direction": _cone_dirs(n_dirs, 20.0, np.random.default_rng(3))},
+        "view": {"type": "FarField", "direction": _cone_dirs(n_dirs, 20.0, np.random.default_rng(4))},
+        "sampler": {"type": "TemporalSampler", "t": [0.0], "D": [0.0] * 5,
+                    "U": {"x": [0.0] * 5, "y": [0.0] * 5, "z": [0.0] * 5}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
+def tracking_2d(batch_size: int = 1 << 17, full_iteration: int = 64, n_dirs: int = 128, frames: int = 32,
+                seed: int = 0):
+    """2D spatio-temporal tracking in the form the reference can express: a static
+    256x256 grid over [-128,128]^2 whose disc (radius 16, material 2, sigs=4)
+    scatterers translate by (0.5, 0) per frame (sampler U of material 2), over
+    32 frames t=0..31; background sigs=1, siga=0, HG g=0.7; 128 far-field
+    illuminations and views over [-pi/6, pi/6] about +y."""
+    n = 256
+    c = -128 + (np.arange(n) + 0.5)
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    mg = np.where(X * X + Y * Y <= 16 * 16, 2, 1).astype(np.uint32)
+    d = _farfield_fan(n_dirs)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "renderingsNum": 1,
+                       "lambda": 1.0, "seed": seed},
+        "scattering": {"type": ["HG"] * 3, "amplitudeFunction": [0.7] * 3},
+        "medium": {"type": "Heterogeneous", "xAxis": np.linspace(-128, 128, n + 1), "yAxis": np.linspace(-128, 128, n + 1),
+                   "materialGrid": mg, "sigs": [0.0, 1.0, 4.0], "siga": [0.0, 0.0, 0.0]},
+        "illumination": {"type": "FarField", "direction": d},
+        "view": {"type": "FarField", "direction": d},
+        "sampler": {"type": "TemporalSampler", "t": np.arange(frames, dtype=float), "D": [0.0, 0.0, 0.0],
+                    "U": {"x": [0.0, 0.0, 0.5], "y": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
+WORKLOADS = {
+    "speckle_2d": speckle_2d,
+    "correlation_3d": correlation_3d,
+    "transmission_matrix_3d": transmission_matrix_3d,
+    "tracking_2d": tracking_2d,
+}
+
+
+def _lattice_axis(lo: float, hi: float, h: float, R: float) -> np.ndarray:
+    """Edges lo:h/2:hi (hi appended if missing), every second edge moved to the
+    previous edge + R, as examples/mcxValidation3D.m:32-54 builds them."""
+    n = int(np.floor((hi - lo) / (h / 2) + 1e-9)) + 1
+    ax = lo + (h / 2) * np.arange(n)
+    if ax[-1] != hi:
+        ax = np.append(ax, hi)
+    ax[1::2] = ax[0:-1:2][: ax[1::2].size] + R
+    return ax
+
+
+def mcx_validation_3d(fx: dict, batch_size: int = 10000, full_iteration: int = 10, seed: int = 0):
+    """The MCX validation scene of examples/mcxValidation3D.m (units: cm, s):
+    a 1 cm cube of static scatterers with a lattice of dynamic R x R rods
+    (Brownian D), isotropic scattering, point source and point view on the
+    z = 0 face viSep apart, lambda = 500 nm, correlation sampler."""
+    dims_ = fx["dims"]
+    h, R = fx["h"], fx["R"]
+    xa = _lattice_axis(-dims_[0] / 2, dims_[0] / 2, h, R)
+    za = _lattice_axis(0.0, dims_[2], h, R)
+    ya = np.array([-dims_[1] / 2, dims_[1] / 2])
+    mg = np.ones((xa.size - 1, 1, za.size - 1), dtype=np.uint32)
+    mg[0::2, :, 0::2] = 2
+    s = 1.0 / fx["MFP"]
+    src = {"type": "PointSource", "location": {"x": [-fx["viSep"] / 2], "y": [0.0], "z": [0.0]}}
+    view = {"type": "PointSource", "location": {"x": [fx["viSep"] / 2], "y": [0.0], "z": [0.0]}}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "renderingsNum": 1,
+                       "lambda": 500e-9 * 100, "seed": seed},
+        "scattering": {"type": ["HG"] * 3, "amplitudeFunction": [0.0, 0.0, 0.0]},
+        "medium": {"type": "Heterogeneous", "xAxis": xa, "yAxis": ya, "zAxis": za, "materialGrid": mg,
+                   "sigs": [0.0, s, s], "siga": [0.0, 0.0, 0.0]},
+        "illumination": src, "view": view, "illumination2": src, "view2": view,
+        "sampler": {"type": "TemporalCorrelationSampler", "t": np.asarray(fx["t"]), "D": [0.0, 0.0, fx["D"]],
+                    "U": {"x": [0.0] * 3, "y": [0.0] * 3, "z": [0.0] * 3}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3

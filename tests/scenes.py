@@ -1,0 +1,110 @@
+"""Scaled-down scenes for the parity tests: every sampler x source x medium
+combination the path supports, at sizes the oracle finishes in seconds."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+from temporalspecklescode_gb300 import workloads as wl
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def mcx_fixture():
+    with open(os.path.join(GOLDEN, "mcx_validation.json")) as f:
+        return json.load(f)
+
+
+def field_point_3d(moving: bool = True, area: bool = False, batch_size=64, full_iteration=2):
+    """3D field sampler with point sources, Brownian + drift motion (ticks around their mean)."""
+    rng = np.random.default_rng(7)
+    ill = {"type": "PointSource", "location": {"x": rng.uniform(-8, 8, 6), "y": rng.uniform(-8, 8, 6), "z": np.full(6, -2.0)},
+           "isAreaSource": area}
+    view = {"type": "PointSource", "location": {"x": rng.uniform(-8, 8, 5), "y": rng.uniform(-8, 8, 5), "z": np.full(5, 12.0)}}
+    grid = rng.integers(1, 3, size=(4, 3, 5)).astype(np.uint32)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.7, "seed": 3},
+        "scattering": {"type": ["HG", "HG", "Isotropic"], "amplitudeFunction": [0.5, 0.6, 0.0]},
+        "medium": {"type": "Heterogeneous", "xAxis": np.linspace(-10, 10, 5), "yAxis": [-10.0, -2.0, 3.0, 10.0],
+                   "zAxis": np.linspace(0, 10, 6), "materialGrid": grid, "sigs": [0.0, 0.6, 1.1], "siga": [0.0, 0.02, 0.05]},
+        "illumination": ill, "view": view,
+        "sampler": {"type": "TemporalSampler", "t": [0.0, 1.0, 2.5, -1.5, 4.0],
+                    "D": [0.0, 2e-3 if moving else 0.0, 5e-3 if moving else 0.0],
+                    "U": {"x": [0.0, 0.01 if moving else 0.0, 0.0], "y": [0.0, 0.0, 0.02 if moving else 0.0], "z": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
+def corr_far_2d_drift(batch_size=64, full_iteration=2):
+    """2D correlation sampler, far-field, different u1/u2 view sets, drift U != 0."""
+    d = wl._farfield_fan(6)
+    d2 = wl._farfield_fan(5, 0.4)
+    grid = np.array([[1, 2], [2, 1], [1, 1]], dtype=np.uint32)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 1.0, "seed": 5},
+        "scattering": {"type": ["HG", "HG", "HG"], "amplitudeFunction": [0.3, 0.3, 0.85]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-6.0, -1.0, 2.0, 6.0], "yAxis": [-5.0, 0.5, 5.0],
+                   "materialGrid": grid, "sigs": [0.0, 0.8, 1.5], "siga": [0.0, 0.01, 0.0]},
+        "illumination": {"type": "FarField", "direction": d}, "view": {"type": "FarField", "direction": d2},
+        "illumination2": {"type": "FarField", "direction": {"x": d["x"] * 0.98 + 0.02, "y": d["y"]}},
+        "view2": {"type": "FarField", "direction": d2},
+        "sampler": {"type": "TemporalCorrelationSampler", "t": [0.5, 1.0, 3.0],
+                    "D": [0.0, 1e-3, 4e-3], "U": {"x": [0.0, 0.05, 0.0], "y": [0.0, 0.0, -0.03]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
+def point_2d_iso(correlation: bool, batch_size=64, full_iteration=2):
+    """2D point sources, isotropic scattering, single bin (scalar single-scattering amplitude)."""
+    ill = {"type": "PointSource", "location": {"x": [-3.0, 0.0, 2.5], "y": [-7.0, -7.0, -7.0]}}
+    view = {"type": "PointSource", "location": {"x": [-2.0, 1.0, 3.0, 4.0], "y": [7.0, 7.0, 7.0, 7.0]}}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.5, "seed": 11},
+        "scattering": {"type": ["Isotropic"], "amplitudeFunction": [0.0]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-5.0, 5.0], "yAxis": [-5.0, 5.0],
+                   "materialGrid": np.ones((1, 1), np.uint32), "sigs": [0.0, 0.7], "siga": [0.0, 0.05]},
+        "illumination": ill, "view": view,
+        "sampler": {"type": "TemporalCorrelationSampler" if correlation else "TemporalSampler", "t": [0.0, 2.0],
+                    "D": [0.0, 1e-2], "U": {"x": [0.0, 0.0], "y": [0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    if correlation:
+        cfg["illumination2"] = ill
+        cfg["view2"] = view
+    return cfg, 2
+
+
+def homogeneous_3d(batch_size=64, full_iteration=1):
+    d = {"x": [0.0, 0.1, -0.2], "y": [0.0, 0.05, 0.1], "z": [1.0, 0.99, 0.97]}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 1.0, "seed": 2},
+        "scattering": {"type": ["HG"], "amplitudeFunction": [0.7]},
+        "medium": {"type": "Homogeneous", "boxMin": {"x": [-5.0], "y": [-5.0], "z": [0.0]},
+                   "boxMax": {"x": [5.0], "y": [5.0], "z": [4.0]}, "sigs": 1.0},
+        "illumination": {"type": "FarField", "direction": d}, "view": {"type": "FarField", "direction": d},
+        "sampler": {"type": "TemporalSampler", "t": [0.0], "D": [0.0, 0.0],
+                    "U": {"x": [0.0, 0.0], "y": [0.0, 0.0], "z": [0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
+def small_scenes():
+    """name -> (config, dims)"""
+    return {
+        "speckle_2d": wl.speckle_2d(batch_size=96, full_iteration=2),
+        "correlation_3d": wl.correlation_3d(batch_size=96, full_iteration=2, n_side=4, n_lags=4),
+        "transmission_matrix_3d": wl.transmission_matrix_3d(batch_size=32, full_iteration=2, n_dirs=24, grid=(16, 16, 8)),
+        "tracking_2d": wl.tracking_2d(batch_size=16, full_iteration=2, n_dirs=8, frames=4),
+        "mcx_3d": wl.mcx_validation_3d(mcx_fixture(), batch_size=48, full_iteration=1),
+        "field_point_3d": field_point_3d(),
+        "field_point_3d_area": field_point_3d(moving=False, area=True),
+        "corr_far_2d_drift": corr_far_2d_drift(),
+        "point_2d_iso_field": point_2d_iso(False),
+        "point_2d_iso_corr": point_2d_iso(True),
+        "homogeneous_3d": homogeneous_3d(),
+    }

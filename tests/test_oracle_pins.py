@@ -1,0 +1,148 @@
+"""Pins of the CPU oracle before it is trusted as the parity checker.
+
+* Philox4x32-10 against the published Random123 known-answer vectors.
+* The portable FP32 log / sin(pi x) / cos(pi x) of the decision path against
+  libm (accuracy) -- the GPU restates the same operations bit for bit.
+* Henyey-Greenstein pdf normalisation in 2D and 3D (Scattering.cuh:500-572)
+  and |amplitude|^2 == pdf; the HG sampler against the pdf (chi^2).
+* Voxel traversal against brute-force fine marching and analytic box exits.
+* The reference's own validation fixture: the MCX temporal correlation curve
+  of examples/mcxValidation3D.m (tests/golden/mcx_validation.json).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from temporalspecklescode_gb300 import config as cf
+from temporalspecklescode_gb300 import workloads as wl
+from tests.scenes import mcx_fixture
+
+
+def test_philox_known_answers(oracle):
+    assert oracle.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert oracle.philox([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert oracle.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_portable_log_accuracy(oracle):
+    xs = np.concatenate([(np.arange(1, 2 ** 16 + 1) * 2.0 ** -16), np.float32(2.0 ** -24) * np.arange(1, 2000)])
+    xs = xs.astype(np.float32)
+    got = np.array([oracle.logf(float(x)) for x in xs[::7]], dtype=np.float64)
+    ref = np.log(xs[::7].astype(np.float64))
+    err = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)
+    # a few ulp relative, absolute 1e-7 near x = 1
+    assert np.all((err < 4e-7) | (np.abs(got - ref) < 2e-7))
+
+
+def test_portable_sincospi_accuracy(oracle):
+    xs = np.linspace(0.0, 2.0, 40001, dtype=np.float32)
+    s = np.zeros(xs.size)
+    c = np.zeros(xs.size)
+    for i, x in enumerate(xs):
+        s[i], c[i] = oracle.sincospif(float(x))
+    xd = xs.astype(np.float64)
+    assert np.max(np.abs(s - np.sin(np.pi * xd))) < 3e-7
+    assert np.max(np.abs(c - np.cos(np.pi * xd))) < 3e-7
+
+
+@pytest.mark.parametrize("dims,g", [(2, 0.8), (3, 0.9), (2, 0.0), (3, -0.4)])
+def test_hg_normalisation(oracle, dims, g):
+    cfg, _ = wl.speckle_2d() if dims == 2 else wl.correlation_3d(n_side=2, n_lags=1)
+    cfg["scattering"] = {"type": ["HG", "HG"], "amplitudeFunction": [g, g]}
+    pc = cf.prepare(cfg, dims)
+    if dims == 2:
+        th = np.linspace(-np.pi, np.pi, 200001)
+        vals = np.array([oracle.phase(pc, 1, math.cos(t)) for t in th[::10]])
+        integral = np.trapezoid(vals[:, 1], th[::10])
+    else:
+        mu = np.linspace(-1, 1, 200001)
+        vals = np.array([oracle.phase(pc, 1, m) for m in mu[::10]])
+        integral = 2 * np.pi * np.trapezoid(vals[:, 1], mu[::10])
+    assert abs(integral - 1.0) < 2e-3
+    assert np.allclose(vals[:, 0] ** 2, vals[:, 1], rtol=1e-12)
+
+
+@pytest.mark.parametrize("dims,g", [(2, 0.8), (3, 0.9), (3, 0.0005), (2, -0.5)])
+def test_hg_sampler_matches_pdf(oracle, dims, g):
+    cfg, _ = wl.speckle_2d() if dims == 2 else wl.correlation_3d(n_side=2, n_lags=1)
+    cfg["scattering"] = {"type": ["HG", "HG"], "amplitudeFunction": [g, g]}
+    pc = cf.prepare(cfg, dims)
+    n = 200000
+    c = oracle.sample_cos(pc, 1, 5, n).astype(np.float64)
+    edges = np.linspace(-1, 1, 41)
+    hist, _ = np.histogram(c, edges)
+    if abs(g) < 0.001:
+        # |g| < 0.001: uniform cosine (Scattering.cuh:1049-1052)
+        p = np.full(40, 1 / 40)
+    elif dims == 3:
+        cdf = lambda m: (1 - g * g) / (2 * g) * (1 / np.sqrt(1 + g * g - 2 * g * m) - 1 / (1 + g))
+        p = np.diff(cdf(edges))
+    else:
+        # 2D: the angle is wrapped Cauchy; integrate the pdf over theta for each cos bin
+        th = np.linspace(0, np.pi, 400001)
+        pdf = (1 - g * g) / (2 * np.pi * (1 + g * g - 2 * g * np.cos(th))) * 2
+        cth = np.cos(th)
+        p = np.array([np.trapezoid(np.where((cth >= a) & (cth < b), pdf, 0.0), th) for a, b in zip(edges[:-1], edges[1:])])
+        p = p / p.sum()
+    exp = p * n
+    chi2 = np.sum((hist - exp) ** 2 / np.maximum(exp, 1e-9))
+    assert chi2 < 90, chi2  # 39 dof; p < 1e-5 above ~90
+
+
+def test_dda_against_fine_marching(oracle):
+    cfg, dims = wl.transmission_matrix_3d(grid=(16, 16, 8))
+    pc = cf.prepare(cfg, dims)
+    med = cfg["medium"]
+    ax = [np.asarray(med[k], dtype=np.float32).astype(np.float64) for k in ("xAxis", "yAxis", "zAxis")]
+    grid = np.asarray(med["materialGrid"])
+    sigs = np.asarray(med["sigs"]) + np.asarray(med["siga"])
+    sigt = (np.asarray(med["sigs"], np.float32) + np.asarray(med["siga"], np.float32)).astype(np.float64)
+    rng = np.random.default_rng(3)
+    for _ in range(40):
+        o = np.array([rng.uniform(-60, 60), rng.uniform(-60, 60), rng.uniform(1, 63)], dtype=np.float32)
+        d = rng.normal(size=3)
+        d = (d / np.linalg.norm(d)).astype(np.float32)
+        steps, t32, t64 = oracle.dda(pc, o, d)
+        # brute force: march in tiny steps
+        od, dd = o.astype(np.float64), d.astype(np.float64)
+        bmin = np.array([a[0] for a in ax]); bmax = np.array([a[-1] for a in ax])
+        with np.errstate(divide="ignore"):
+            tx = np.where(dd > 0, (bmax - od) / dd, np.where(dd < 0, (bmin - od) / dd, np.inf))
+        tend = tx.min()
+        ts = np.linspace(0, tend, 200001)
+        mid = 0.5 * (ts[1:] + ts[:-1])
+        pts = od[None, :] + mid[:, None] * dd[None, :]
+        idx = [np.clip(np.searchsorted(a, pts[:, i], side="right") - 1, 0, a.size - 2) for i, a in enumerate(ax)]
+        tau = np.sum(sigt[grid[idx[0], idx[1], idx[2]]] * np.diff(ts))
+        assert abs(t64 - tau) < 2e-3 * max(1.0, tau), (t64, tau)
+        assert abs(t32 - t64) < 1e-4 * max(1.0, tau)
+        # each step enters a new voxel: at least the number of distinct voxels visited
+        assert steps >= len({(a, b, c) for a, b, c in zip(*idx)}) - 2
+    del sigs
+
+
+def test_single_cell_exit_is_analytic(oracle):
+    cfg, dims = wl.speckle_2d()
+    pc = cf.prepare(cfg, dims)
+    d = np.float32([0.6, 0.8]).astype(np.float64)
+    steps, t32, t64 = oracle.dda(pc, (10.0, -20.0, 0.0), (float(d[0]), float(d[1]), 0.0))
+    assert steps == 1
+    assert abs(t64 - min((50 - 10) / d[0], (50 + 20) / d[1])) < 1e-9
+
+
+def test_oracle_reproduces_mcx_validation_curve(oracle):
+    """The reference validates its correlation sampler against MCX
+    (examples/mcxValidation3D.m).  With 1.6e5 paths the oracle reproduces the
+    decay of the MCX curve over all 51 lags within 3% and its level within 12%
+    (the reference itself uses 1e7 paths for this plot)."""
+    fx = mcx_fixture()
+    cfg, dims = wl.mcx_validation_3d(fx, batch_size=40000, full_iteration=4)
+    pc = cf.prepare(cfg, dims)
+    u, it, st = oracle.render(pc, seed=1)
+    c = np.abs(u[0, 0, :]) / it
+    mcx = np.asarray(fx["mcx_res"])
+    shape = (c / c[0]) / (mcx / mcx[0])
+    assert np.max(np.abs(shape - 1)) < 0.03, shape
+    assert abs(c[0] / mcx[0] - 1) < 0.12, c[0] / mcx[0]
