@@ -167,7 +167,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     if (smem > 48 * 1024) {
         // attribute is set inside launch_trace; occupancy query below tolerates either state
     }
-    per_sm = occupancy_blocks(threads, smem);
+    per_sm = occupancy_blocks(S.dev, threads, smem);
     const int blocks = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_sm)));
     bool first_pass = true;
     for (auto& vc : vch) {

@@ -247,6 +247,144 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
     }
 }
 
+// Single-scattering term of the correlation sampler when the u1 and u2
+// sources are identical and every scatterer is static (U = 0): the rows are
+// real (|g|^2) and Fs1 Fs2 TS = pdf(cos) exp(-k^2 D |tau| |in - out|^2)
+// (SourceInterface.cuh:221-270 with q = in - out).  Each thread owns a 2 x 2
+// (illumination, view) block and all ticks of a chunk.
+constexpr int kFl = 32, kFv = 32, kFk = 16, kFt = 8;
+
+constexpr size_t kFastSmem = sizeof(float) * (2 * kFk * kFt * kFl + 6 * kFk * kFl) + sizeof(int) * kFk
+                           + sizeof(double) * 4 * kFt * 256;
+
+__global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__ DevScene S, const SsParams G)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double* accd = reinterpret_cast<double*>(smem_raw);                       // [4*kFt][256] FP64 window sums
+    float* as = reinterpret_cast<float*>(accd + 4 * kFt * 256);              // [kFk][kFt][kFl]
+    float* bs = as + kFk * kFt * kFl;                                         // [kFk][kFt][kFv]
+    float* inx = bs + kFk * kFt * kFv;                                        // [kFk][3][kFl]
+    float* outx = inx + kFk * 3 * kFl;                                        // [kFk][3][kFv]
+    int* m1s = reinterpret_cast<int*>(outx + kFk * 3 * kFv);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int l0 = blockIdx.x * kFl, v0 = blockIdx.y * kFv;
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const int tchunks = (Nt + kFt - 1) / kFt;
+    const int t0 = (blockIdx.z % tchunks) * kFt;
+    const int tn = min(kFt, Nt - t0);
+    const int ks = blockIdx.z / tchunks;
+    const int kb = ks * G.kchunk, ke = min(G.K, kb + G.kchunk);
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    const bool geo = S.ticks_geometric != 0;
+    const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
+    float acc[2][2][kFt];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int t = 0; t < kFt; ++t) { acc[i][j][t] = 0.f; accd[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = 0.0; }
+    int chunk = 0;
+    for (int k = kb; k < ke; k += kFk, ++chunk) {
+        for (int idx = threadIdx.x; idx < kFk * kFt * kFl; idx += 256) {
+            const int pp = idx / (kFt * kFl), r = idx % (kFt * kFl);
+            const int tt = r / kFl, c = r % kFl;
+            const int p = k + pp;
+            float a = 0.f, b = 0.f;
+            if (p < ke && tt < tn) {
+                if (l0 + c < Nl) a = G.a[((size_t)p * Nt + t0 + tt) * Nl + l0 + c].x;
+                if (v0 + c < Nv) b = G.b[((size_t)p * Nt + t0 + tt) * Nv + v0 + c].x;
+            }
+            as[idx] = a;
+            bs[idx] = b;
+        }
+        for (int idx = threadIdx.x; idx < kFk * kFl; idx += 256) {
+            const int pp = idx / kFl, c = idx % kFl;
+            const int p = min(k + pp, ke - 1);
+            const V3 x = V3{ G.x1[3 * p], G.x1[3 * p + 1], G.x1[3 * p + 2] };
+            const V3 i1 = fsrc_in(il, min(l0 + c, Nl - 1), x);
+            const V3 o1 = fsrc_out(vw, min(v0 + c, Nv - 1), x);
+            inx[(pp * 3 + 0) * kFl + c] = i1.x; inx[(pp * 3 + 1) * kFl + c] = i1.y; inx[(pp * 3 + 2) * kFl + c] = i1.z;
+            outx[(pp * 3 + 0) * kFv + c] = o1.x; outx[(pp * 3 + 1) * kFv + c] = o1.y; outx[(pp * 3 + 2) * kFv + c] = o1.z;
+            if (c == 0) m1s[pp] = (k + pp < ke) ? (int)G.m1[k + pp] : 0;
+        }
+        __syncthreads();
+        for (int pp = 0; pp < kFk; ++pp) {
+            const int m = m1s[pp];
+            if (m == 0) continue;
+            const int ty_ = S.scat_type[m];
+            const float g = S.g[m], omg = 1.0f - g, gup = S.gup[m];
+            const float c1 = S.k2 * S.D[m];
+            float w[2][2], e[2][2], estep[2][2], cq[2][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const int cl = tx + 16 * i, cv = ty + 16 * j;
+                    const float dx = inx[(pp * 3 + 0) * kFl + cl] - outx[(pp * 3 + 0) * kFv + cv];
+                    const float dy = inx[(pp * 3 + 1) * kFl + cl] - outx[(pp * 3 + 1) * kFv + cv];
+                    const float dz = inx[(pp * 3 + 2) * kFl + cl] - outx[(pp * 3 + 2) * kFv + cv];
+                    const float q2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    float pdf;
+                    if (ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
+                        const float r = rsqrtf(fmaf(g, q2, omg * omg));
+                        pdf = S.dims == 2 ? gup * r * r : gup * r * r * r;
+                    } else {
+                        pdf = ty_ == SSTMC_SCATTERING_ISOTROPIC ? S.iso_pdf : 0.0f;
+                    }
+                    // scalar single-scattering amplitude (point x point, isotropic): the
+                    // temporal factor is not applied (NextEventEstimation.cuh:1024-1032)
+                    w[i][j] = scalar_fs ? S.iso_amp * S.iso_amp : pdf;
+                    cq[i][j] = scalar_fs ? 0.0f : c1 * q2;
+                    e[i][j] = __expf(-cq[i][j] * S.abs_ticks[t0]);
+                    estep[i][j] = geo ? __expf(-cq[i][j] * S.abs_ticks[0]) : 0.0f;
+                }
+#pragma unroll
+            for (int tt = 0; tt < kFt; ++tt) {
+                if (tt >= tn) break;
+                const float* ar = as + (pp * kFt + tt) * kFl;
+                const float* br = bs + (pp * kFt + tt) * kFv;
+                const float av[2] = { ar[tx], ar[tx + 16] }, bv[2] = { br[ty], br[ty + 16] };
+#pragma unroll
+                for (int i = 0; i < 2; ++i)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        float wt;
+                        if (geo) { wt = w[i][j] * e[i][j]; e[i][j] *= estep[i][j]; }
+                        else wt = w[i][j] * __expf(-cq[i][j] * S.abs_ticks[t0 + tt]);
+                        acc[i][j][tt] = fmaf(av[i] * bv[j], wt, acc[i][j][tt]);
+                    }
+            }
+        }
+        __syncthreads();
+        if ((chunk + 1) % 16 == 0) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+#pragma unroll
+                    for (int t = 0; t < kFt; ++t) {
+                        accd[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] += (double)acc[i][j][t];
+                        acc[i][j][t] = 0.f;
+                    }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int l = l0 + tx + 16 * i, v = v0 + ty + 16 * j;
+            if (l >= Nl || v >= Nv) continue;
+#pragma unroll
+            for (int tt = 0; tt < kFt; ++tt) {
+                if (tt >= tn) break;
+                const size_t o = ((size_t)(t0 + tt) * Nv + v) * Nl + l;
+                atomicAdd(&G.V[o].x, accd[((i * 2 + j) * kFt + tt) * 256 + threadIdx.x] + (double)acc[i][j][tt]);
+            }
+        }
+}
+
 }  // namespace
 
 int launch_gemm(const GemmParams& G, cudaStream_t stream)
@@ -261,6 +399,14 @@ int launch_gemm(const GemmParams& G, cudaStream_t stream)
 int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
 {
     if (G.K <= 0) return SSTMC_NO_ERROR;
+    if (S.correlation && S.sym && S.all_static_corr) {
+        const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
+        const int tchunks = (S.Nt + kFt - 1) / kFt;
+        dim3 grid((S.src[0].n + kFl - 1) / kFl, (S.src[1].n + kFv - 1) / kFv, tchunks * ksplit);
+        cudaFuncSetAttribute(ss_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem);
+        ss_fast_kernel<<<grid, 256, kFastSmem, stream>>>(S, G);
+        return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
+    }
     const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
     const int tchunks = (S.Nt + kSsT - 1) / kSsT;
     dim3 grid((S.src[0].n + kSsL - 1) / kSsL, (S.src[1].n + kSsV - 1) / kSsV, tchunks * ksplit);

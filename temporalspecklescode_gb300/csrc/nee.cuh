@@ -80,6 +80,87 @@ __device__ __forceinline__ V3 src_out(const DevSource& s, int k, const V3& x)
     return unit3(sub3(load3(s.p, k), x));
 }
 
+// ---- value-path helpers (fast intrinsics; no decision depends on them) ----
+
+__device__ __forceinline__ V3 funit(const V3& v)
+{
+    const float s = dot3(v, v);
+    if (!(s > 0.0f)) return V3{ 0.f, 0.f, 1.f };
+    const float r = rsqrtf(s);
+    return V3{ v.x * r, v.y * r, v.z * r };
+}
+
+// Optical depth to the box edge of a single-cell medium.  The traversal of a
+// single cell always takes exactly one step, so the step count does not
+// depend on the arithmetic and fast reciprocals are used.
+__device__ __forceinline__ float tau_single(const DevScene& S, const V3& o, const V3& d)
+{
+    float best = 3.0e38f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (i == 2 && S.dims == 2) break;
+        const float di = comp(d, i);
+        const float inv = fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : __fdividef(1.0f, di);
+        const float face = di < 0.0f ? S.bmin[i] : S.bmax[i];
+        best = fminf(best, (face - comp(o, i)) * inv);
+    }
+    return best * S.sigt[S.grid_m0];
+}
+
+// Optical depth from x along the exact direction d (a table direction), with
+// the voxel-step count of the bit-exact traversal.
+__device__ __forceinline__ float tau_dir(const DevScene& S, const V3& x, const V3& d, uint32_t& steps)
+{
+    if (S.single) {
+        if (!inside(S, x)) return 0.0f;
+        steps += 1;
+        return tau_single(S, x, d);
+    }
+    return dda(S, x, d, steps);
+}
+
+// Optical depth from x toward the point s.  Multi-cell media traverse along
+// the IEEE-normalised direction (decision path); a single cell needs no exact
+// direction.
+__device__ __forceinline__ float tau_to_point(const DevScene& S, const V3& x, const V3& s, uint32_t& steps)
+{
+    if (S.single) {
+        if (!inside(S, x)) return 0.0f;
+        steps += 1;
+        return tau_single(S, x, funit(sub3(s, x)));
+    }
+    const V3 dir = normalize32(S.dims, V3{ fsb(s.x, x.x), fsb(s.y, x.y), fsb(s.z, x.z) });
+    return dda(S, x, dir, steps);
+}
+
+// Henyey-Greenstein pdf / amplitude from two unit directions with fast
+// intrinsics: dn = (1 - g)^2 + g |a - b|^2, pdf = gup dn^(-(D-1)/2... )
+__device__ __forceinline__ float pdf_fast(const DevScene& S, int m, const V3& a, const V3& b)
+{
+    const int ty = S.scat_type[m];
+    if (ty == SSTMC_SCATTERING_ISOTROPIC) return S.iso_pdf;
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return 0.0f;
+    const float g = S.g[m];
+    const V3 d = sub3(a, b);
+    const float omg = 1.0f - g;
+    const float dn = fmaf(g, dot3(d, d), omg * omg);
+    const float r = rsqrtf(dn);
+    return S.dims == 2 ? S.gup[m] * r * r : S.gup[m] * r * r * r;
+}
+
+__device__ __forceinline__ float amp_fast(const DevScene& S, int m, const V3& a, const V3& b)
+{
+    const int ty = S.scat_type[m];
+    if (ty == SSTMC_SCATTERING_ISOTROPIC) return S.iso_amp;
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return 0.0f;
+    const float g = S.g[m];
+    const V3 d = sub3(a, b);
+    const float omg = 1.0f - g;
+    const float dn = fmaf(g, dot3(d, d), omg * omg);
+    const float r = rsqrtf(dn);
+    return S.dims == 2 ? S.sgup[m] * r : S.sgup[m] * r * sqrtf(r);
+}
+
 // P_l(x): attenuation toward illumination element l times its sampling density.
 __device__ inline float pfirst(const DevScene& S, const DevSource& s, int l, const V3& x, uint32_t& steps)
 {
@@ -142,6 +223,18 @@ __device__ inline float2 gvec(const DevScene& S, const DevSource& s, int k, cons
 }
 
 // f for the illumination side: element l -> scatterer pa -> point pb.
+__device__ __forceinline__ V3 fsrc_in(const DevSource& s, int k, const V3& x)
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) return load3(s.p, k);
+    return funit(sub3(x, load3(s.p, k)));
+}
+
+__device__ __forceinline__ V3 fsrc_out(const DevSource& s, int k, const V3& x)
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) return load3(s.p, k);
+    return funit(sub3(load3(s.p, k), x));
+}
+
 __device__ __forceinline__ float famp_illum(const DevScene& S, const DevSource& s, int l, const V3& pa, const V3& pb, int m)
 {
     if (s.type == SSTMC_SOURCE_POINT && S.iso_all) return S.iso_amp;

@@ -160,6 +160,7 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
             S->g_d[mm] = g;
             D.g[mm] = (float)g;
             D.gup[mm] = (float)(dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * kPi)) : (1.0 - g * g) / (4.0 * kPi));
+            D.sgup[mm] = (float)std::sqrt(dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * kPi)) : (1.0 - g * g) / (4.0 * kPi));
             D.gd1[mm] = (float)(1.0 + g * g);
             D.gd2[mm] = (float)(-2.0 * g);
         }
@@ -222,6 +223,8 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         D.center[a] = (float)c; D.radius[a] = (float)r;
         D.inv_radius[a] = std::fabs(D.radius[a]) < 1e-12f ? 1e12f : 1.0f / D.radius[a];
     }
+    D.single = (S->grid.size() == 1) ? 1 : 0;
+    D.grid_m0 = S->grid[0];
     float maxsigt = 0.0f;
     for (int m = 0; m < kMat; ++m) {
         if (sigs[m] < 0 || siga[m] < 0) return fail(SSTMC_INVALID_CONFIG, "sigs and siga must be non-negative");
@@ -274,6 +277,11 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         for (int i = 0; i < 3; ++i) D.U[m][i] = (float)Um[m][i];
         D.static_corr[m] = D.U[m][0] == 0.0f && D.U[m][1] == 0.0f && D.U[m][2] == 0.0f;
     }
+    D.all_static_corr = 1;
+    for (int m = 0; m < kMat; ++m) if (!D.static_corr[m]) D.all_static_corr = 0;
+    D.ticks_geometric = S->abs_ticks[0] > 0.0f;
+    for (int t = 0; t < Nt; ++t)
+        if (S->abs_ticks[t] != (float)(t + 1) * S->abs_ticks[0]) D.ticks_geometric = 0;
     // field sampler: ticks sorted around their mean (TemporalSampler.cuh:958-1150)
     {
         double mean = 0;

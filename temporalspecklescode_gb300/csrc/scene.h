@@ -44,12 +44,15 @@ struct DevSource {
 struct DevScene {
     int dims, correlation, Nt, neg;
     int temporal_amp, iso_all, precision, sym;  // sym: illumination2 == illumination and view2 == view
+    int single, grid_m0;          // single-cell medium and its material
+    int all_static_corr;          // no material drifts (U == 0 everywhere)
+    int ticks_geometric;          // |t_k| == (k + 1) |t_0| for every tick
     uint32_t P;
     int n[3];
     const float* ax[3];
     const unsigned char* grid;
     int scat_type[kMat];
-    float g[kMat], gup[kMat], gd1[kMat], gd2[kMat];
+    float g[kMat], gup[kMat], sgup[kMat], gd1[kMat], gd2[kMat];
     float sigt[kMat], accept[kMat], survive[kMat];
     float inv_maxsigt;
     float bmin[3], bmax[3], center[3], radius[3], inv_radius[3];

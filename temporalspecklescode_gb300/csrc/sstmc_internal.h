@@ -51,7 +51,7 @@ struct Engine {
     void destroy_events();
 };
 
-int occupancy_blocks(int threads, size_t smem);
+int occupancy_blocks(const DevScene& S, int threads, size_t smem);
 void set_last_error_text(const std::string& s);
 
 }  // namespace sstmc

@@ -108,13 +108,118 @@ __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, i
         for (int v = T.v0 + lane; v < T.v0 + T.vn; v += 32) T.s_ms[((size_t)q * Nt + t) * Nv + v] = make_float2(0.f, 0.f);
 }
 
+// ---- NEE vectors, specialised on the source type (PT: point source) ----
+
+// |g|^2 of source element k at x: the attenuation weight T c / r^(D-1)
+// (point source, PointSource.cuh:117-172) or T (far field, FarField.cuh:223-263).
+template <bool PT>
+__device__ __forceinline__ float gweight(const DevScene& S, const DevSource& s, int k, const V3& x, int role, uint32_t& steps)
+{
+    if constexpr (!PT) {
+        const V3 d = load3(s.p, k);
+        return expf(-tau_dir(S, x, role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d, steps));
+    } else {
+        const V3 sp = load3(s.p, k);
+        const float T = expf(-tau_to_point(S, x, sp, steps));
+        const V3 v = sub3(x, sp);
+        const float r2 = dot3(v, v);
+        float at = S.dims == 3 ? __fdividef(T * kIsoAmp3, r2) : T * rsqrtf(r2);
+        if (s.is_area) at *= fabsf(S.dims == 3 ? v.z : v.y) * rsqrtf(r2);
+        return at;
+    }
+}
+
+// g with its phase.  Split precision: the argument d.x / lambda (far field)
+// or r / lambda (point source) is formed and reduced modulo one cycle in FP64.
+template <bool PT>
+__device__ __forceinline__ float2 gcomplex(const DevScene& S, const DevSource& s, int k, const V3& x, int role, uint32_t& steps)
+{
+    const bool split = S.precision == SSTMC_PRECISION_SPLIT;
+    float f, a;
+    if constexpr (!PT) {
+        const V3 d = load3(s.p, k);
+        a = sqrtf(expf(-tau_dir(S, x, role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d, steps)));
+        if (split) {
+            const double dx = fma((double)d.x, (double)x.x, fma((double)d.y, (double)x.y, (double)d.z * (double)x.z));
+            f = frac_cycles((role == kRoleIllum ? dx : -dx) * S.inv_lambda);
+        } else {
+            const float dx = d.x * x.x + d.y * x.y + d.z * x.z;
+            const float ph = (role == kRoleIllum ? dx : -dx) * S.inv_lambda_f;
+            f = ph - rintf(ph);
+        }
+    } else {
+        const V3 sp = load3(s.p, k);
+        const float T = expf(-tau_to_point(S, x, sp, steps));
+        const V3 v = sub3(x, sp);
+        const float r2 = dot3(v, v);
+        float at = S.dims == 3 ? __fdividef(T * kIsoAmp3, r2) : T * rsqrtf(r2);
+        if (s.is_area) at *= fabsf(S.dims == 3 ? v.z : v.y) * rsqrtf(r2);
+        a = sqrtf(at);
+        if (split) {
+            const double dx = (double)x.x - (double)sp.x, dy = (double)x.y - (double)sp.y, dz = (double)x.z - (double)sp.z;
+            f = frac_cycles(sqrt(fma(dx, dx, fma(dy, dy, dz * dz))) * S.inv_lambda);
+        } else {
+            const float ph = sqrtf(r2) * S.inv_lambda_f;
+            f = ph - rintf(ph);
+        }
+    }
+    return c_scale(unit_phase(f), a);
+}
+
+template <bool PT>
+__device__ __forceinline__ float pfirst_t(const DevScene& S, const DevSource& s, int l, const V3& x, uint32_t& steps)
+{
+    if constexpr (!PT) {
+        const V3 d = load3(s.p, l);
+        return expf(-tau_dir(S, x, V3{ -d.x, -d.y, -d.z }, steps)) * s.sprob[l];
+    } else {
+        const V3 sp = load3(s.p, l);
+        const float T = expf(-tau_to_point(S, x, sp, steps));
+        const V3 v = sub3(x, sp);
+        const float r2 = dot3(v, v);
+        return S.dims == 3 ? __fdividef(T, (float)(4.0 * kPi) * r2) : T * (float)(8.0 * kPi) * rsqrtf(r2);
+    }
+}
+
+// f: illumination element l -> scatterer pa -> pb (FarField.cuh:546-554, PointSource.cuh:317-345)
+template <bool PT>
+__device__ __forceinline__ float fillum(const DevScene& S, const DevSource& s, int l, const V3& pa, const V3& pb, int m)
+{
+    if (PT && S.iso_all) return S.iso_amp;
+    return amp_fast(S, m, fsrc_in(s, l, pa), funit(sub3(pb, pa)));
+}
+
+// f: pb -> scatterer pa -> view element v
+template <bool PT>
+__device__ __forceinline__ float fview(const DevScene& S, const DevSource& s, int v, const V3& pa, const V3& pb, int m)
+{
+    if (PT && S.iso_all) return S.iso_amp;
+    return amp_fast(S, m, funit(sub3(pa, pb)), fsrc_out(s, v, pa));
+}
+
+// f^2 for identical u1 / u2 sources: the pdf (|amplitude|^2 = pdf)
+template <bool PT>
+__device__ __forceinline__ float fillum2(const DevScene& S, const DevSource& s, int l, const V3& pa, const V3& pb, int m)
+{
+    if (PT && S.iso_all) return S.iso_amp * S.iso_amp;
+    return pdf_fast(S, m, fsrc_in(s, l, pa), funit(sub3(pb, pa)));
+}
+
+template <bool PT>
+__device__ __forceinline__ float fview2(const DevScene& S, const DevSource& s, int v, const V3& pa, const V3& pb, int m)
+{
+    if (PT && S.iso_all) return S.iso_amp * S.iso_amp;
+    return pdf_fast(S, m, funit(sub3(pa, pb)), fsrc_out(s, v, pa));
+}
+
+// CORR: correlation sampler; ILP / VWP: illumination / view sources are point sources.
+template <bool CORR, bool ILP, bool VWP>
 __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     extern __shared__ double smem_d[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n, D = S.dims;
-    const bool corr = S.correlation != 0;
     const bool split = S.precision == SSTMC_PRECISION_SPLIT;
     // per-warp shared scratch: L[Nt] doubles, view accumulators [slots][32] float2
     // (lane-major, conflict-free), two Nt*3 float tick-position buffers
@@ -128,13 +233,14 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
     const DevSource& vw = S.src[1];
     const DevSource& il2 = S.src[2];
     const DevSource& vw2 = S.src[3];
+    const float k2 = S.k2;
 
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t pid = T.first_path + q;
         const uint32_t slot = pid % S.P, wave = pid / S.P;
-        const bool side1 = !corr || slot < u1_count(S, T.seed, wave);
+        const bool side1 = !CORR || slot < u1_count(S, T.seed, wave);
         const DevSource& fsrc = side1 ? il : il2;
 
         // ---- first vertex, with miss resampling (NEE.cuh:643-679) ----
@@ -155,81 +261,109 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
             zero_rows(S, T, q, lane);
             continue;
         }
-        const float xi1 = corr ? 0.0f : rs.uniform();
+        const float xi1 = CORR ? 0.0f : rs.uniform();
         float* xtc = bufA;   // tick positions of the current vertex
         float* xtn = bufB;   // tick positions of the new vertex
-        if (!corr) {
+        bool mov1 = false;
+        if constexpr (!CORR) {
             temporal_positions(S, T.seed, pid, 1u, x1, m1, xtc, lane);
             for (int t = lane; t < Nt; t += 32) Ls[t] = 0.0;
             __syncwarp();
+            mov1 = S.moving[m1] != 0;
+            if (T.pass0 && T.x1t)
+                for (int i = lane; i < 3 * Nt; i += 32) T.x1t[(size_t)q * 3 * Nt + i] = xtc[i];
         }
-        const bool mov1 = !corr && S.moving[m1];
-        if (T.pass0 && T.x1t && !corr)
-            for (int i = lane; i < 3 * Nt; i += 32) T.x1t[(size_t)q * 3 * Nt + i] = xtc[i];
         uint32_t steps = 0;
         uint32_t h = hash_vertex(S, 2166136261u, x1, m1);
-        float p1inv = 0.0f;
 
         // ---- illumination side at x1: P_l, Gl0, single-scattering rows ----
         if (T.pass0) {
             float ps = 0.0f;
             for (int l = lane; l < Nl; l += 32) {
-                float P = pfirst(S, il, l, x1, steps);
-                if (corr) P = 0.5f * (P + pfirst(S, il2, l, x1, steps));
+                uint32_t st = 0;
+                float P = pfirst_t<ILP>(S, il, l, x1, st);
+                if (CORR) {
+                    if (S.sym) st *= 2;
+                    else P = 0.5f * (P + pfirst_t<ILP>(S, il2, l, x1, st));
+                }
+                steps += st;
                 T.pl[(size_t)q * Nl + l] = P;
                 ps += P;
             }
             const float p1 = warp_sum(ps) / (float)Nl;
-            p1inv = corr ? 1.0f / p1 : 1.0f / sqrtf(p1);
-            const float2 e1 = corr ? make_float2(1.f, 0.f) : unit_phase(xi1);
-            const bool st1 = corr ? S.static_corr[m1] != 0 : !mov1;
-            const bool nophase = corr && S.sym && st1;
-            for (int l = lane % T.lw; l < Nl; l += T.lw) {
-                float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
-                uint32_t sts = 0;
-                if (st1) {
-                    g1s = gvec(S, il, l, x1, kRoleIllum, !nophase, sts);
-                    if (corr) g2s = nophase ? g1s : gvec(S, il2, l, x1, kRoleIllum, true, sts);
-                    if (nophase) sts *= 2;
-                }
-                for (int t = lane / T.lw; t < Nt; t += T.lg) {
-                    float2 g1, g2 = make_float2(0.f, 0.f);
-                    if (st1) { g1 = g1s; g2 = g2s; steps += sts; }
-                    else if (!corr) g1 = gvec(S, il, l, tick_pos(xtc, t), kRoleIllum, true, steps);
-                    else {
-                        const float tau = S.ticks_f[t];
-                        g1 = gvec(S, il, l, shift_u(S, x1, m1, tau, -1.0f), kRoleIllum, true, steps);
-                        g2 = gvec(S, il2, l, shift_u(S, x1, m1, tau, 1.0f), kRoleIllum, true, steps);
+            const float p1inv = CORR ? 1.0f / p1 : 1.0f / sqrtf(p1);
+            if constexpr (CORR) {
+                const bool st1 = S.static_corr[m1] != 0;
+                const bool realg = S.sym && st1;
+                for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                    float w = 0.0f;
+                    float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
+                    uint32_t sts = 0;
+                    if (realg) { w = gweight<ILP>(S, il, l, x1, kRoleIllum, sts); sts *= 2; }
+                    else if (st1) { g1s = gcomplex<ILP>(S, il, l, x1, kRoleIllum, sts); g2s = gcomplex<ILP>(S, il2, l, x1, kRoleIllum, sts); }
+                    for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                        const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                        if (realg) {
+                            steps += sts;
+                            T.a_ms[o] = make_float2(w, 0.f);
+                            T.a_ss[o] = make_float2(w * p1inv, 0.f);
+                        } else {
+                            float2 g1 = g1s, g2 = g2s;
+                            if (st1) steps += sts;
+                            else {
+                                const float tau = S.ticks_f[t];
+                                g1 = gcomplex<ILP>(S, il, l, shift_u(S, x1, m1, tau, -1.0f), kRoleIllum, steps);
+                                g2 = gcomplex<ILP>(S, il2, l, shift_u(S, x1, m1, tau, 1.0f), kRoleIllum, steps);
+                            }
+                            T.a_ms[o] = g1;
+                            T.g2[o] = g2;
+                            T.a_ss[o] = c_scale(c_mulc(g1, g2), p1inv);
+                        }
                     }
-                    const size_t o = ((size_t)q * Nt + t) * Nl + l;
-                    T.a_ms[o] = g1;  // raw illumination vector, finished at x2
-                    if (corr) {
-                        T.g2[o] = g2;
-                        T.a_ss[o] = c_scale(c_mulc(g1, g2), p1inv);
-                    } else {
-                        T.a_ss[o] = c_scale(c_mul(g1, e1), p1inv);
+                }
+                for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
+                    float w = 0.0f;
+                    float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
+                    uint32_t sts = 0;
+                    if (realg) { w = gweight<VWP>(S, vw, v, x1, kRoleView, sts); sts *= 2; }
+                    else if (st1) { g1s = gcomplex<VWP>(S, vw, v, x1, kRoleView, sts); g2s = gcomplex<VWP>(S, vw2, v, x1, kRoleView, sts); }
+                    for (int t = lane / T.vwa; t < Nt; t += T.tga) {
+                        float2 b;
+                        if (realg) { steps += sts; b = make_float2(w, 0.f); }
+                        else if (st1) { steps += sts; b = c_mulc(g1s, g2s); }
+                        else {
+                            const float tau = S.ticks_f[t];
+                            b = c_mulc(gcomplex<VWP>(S, vw, v, shift_u(S, x1, m1, tau, -1.0f), kRoleView, steps),
+                                       gcomplex<VWP>(S, vw2, v, shift_u(S, x1, m1, tau, 1.0f), kRoleView, steps));
+                        }
+                        T.b_ss[((size_t)q * Nt + t) * Nv + v] = b;
                     }
                 }
-            }
-            for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
-                float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
-                uint32_t sts = 0;
-                if (st1) {
-                    g1s = gvec(S, vw, v, x1, kRoleView, !nophase, sts);
-                    if (corr) g2s = nophase ? g1s : gvec(S, vw2, v, x1, kRoleView, true, sts);
-                    if (nophase) sts *= 2;
-                }
-                for (int t = lane / T.vwa; t < Nt; t += T.tga) {
-                    float2 b;
-                    if (st1) { b = corr ? c_mulc(g1s, g2s) : g1s; steps += sts; }
-                    else if (!corr) b = gvec(S, vw, v, tick_pos(xtc, t), kRoleView, true, steps);
-                    else {
-                        const float tau = S.ticks_f[t];
-                        const float2 g1 = gvec(S, vw, v, shift_u(S, x1, m1, tau, -1.0f), kRoleView, true, steps);
-                        const float2 g2 = gvec(S, vw2, v, shift_u(S, x1, m1, tau, 1.0f), kRoleView, true, steps);
-                        b = c_mulc(g1, g2);
+            } else {
+                const float2 e1 = unit_phase(xi1);
+                for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                    float2 gs = make_float2(0.f, 0.f);
+                    uint32_t sts = 0;
+                    if (!mov1) gs = gcomplex<ILP>(S, il, l, x1, kRoleIllum, sts);
+                    for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                        float2 g = gs;
+                        if (!mov1) steps += sts;
+                        else g = gcomplex<ILP>(S, il, l, tick_pos(xtc, t), kRoleIllum, steps);
+                        const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                        T.a_ms[o] = g;
+                        T.a_ss[o] = c_scale(c_mul(g, e1), p1inv);
                     }
-                    T.b_ss[((size_t)q * Nt + t) * Nv + v] = b;
+                }
+                for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
+                    float2 gs = make_float2(0.f, 0.f);
+                    uint32_t sts = 0;
+                    if (!mov1) gs = gcomplex<VWP>(S, vw, v, x1, kRoleView, sts);
+                    for (int t = lane / T.vwa; t < Nt; t += T.tga) {
+                        float2 g = gs;
+                        if (!mov1) steps += sts;
+                        else g = gcomplex<VWP>(S, vw, v, tick_pos(xtc, t), kRoleView, steps);
+                        T.b_ss[((size_t)q * Nt + t) * Nv + v] = g;
+                    }
                 }
             }
         }
@@ -249,16 +383,15 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
             int mn = 0;
             if (!woodcock(S, cur, nd, rs, xn, mn)) { ok = false; break; }
             if (mn == 0) break;
-            const float xin = corr ? 0.0f : rs.uniform();
+            const float xin = CORR ? 0.0f : rs.uniform();
             B = b;
             h = hash_vertex(S, h, xn, mn);
-            if (corr && b >= 3) {
+            if (CORR && b >= 3) {
                 // momentum transfer of the inner vertex cur (TemporalSamplerCorrelation.cuh:144-179)
-                const V3 u = unit3(sub3(cur, prev)), w = unit3(sub3(xn, cur));
-                const V3 dq = sub3(u, w);
+                const V3 dq = sub3(funit(sub3(cur, prev)), funit(sub3(xn, cur)));
                 MT += S.D[mcur] * dot3(dq, dq);
             }
-            if (!corr) {
+            if constexpr (!CORR) {
                 temporal_positions(S, T.seed, pid, b, xn, mn, xtn, lane);
                 for (int t = lane; t < Nt; t += 32) {
                     const V3 a = tick_pos(xtc, t), c = tick_pos(xtn, t);
@@ -275,91 +408,118 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
 
             // multiple-scattering illumination vector at x2 (NEE.cuh:1525-1559, 889-1009)
             if (b == 2 && T.pass0) {
-                const V3 x12 = unit3(sub3(xn, x1));
+                const V3 x12 = funit(sub3(xn, x1));
                 float ps = 0.0f;
                 for (int l = lane; l < Nl; l += 32)
-                    ps += T.pl[(size_t)q * Nl + l] * pdf_dirs(S, m1, src_in(il, l, x1), x12);
+                    ps += T.pl[(size_t)q * Nl + l] * pdf_fast(S, m1, fsrc_in(il, l, x1), x12);
                 const float p2 = warp_sum(ps) / (float)Nl;
-                const float p2inv = corr ? 1.0f / p2 : 1.0f / sqrtf(p2);
-                for (int l = lane % T.lw; l < Nl; l += T.lw) {
-                    for (int t = lane / T.lw; t < Nt; t += T.lg) {
-                        const size_t o = ((size_t)q * Nt + t) * Nl + l;
-                        const float2 g1 = T.a_ms[o];
-                        if (!corr) {
-                            const V3 pa = S.temporal_amp ? tick_pos(xtc, t) : x1;
-                            const V3 pb = S.temporal_amp ? tick_pos(xtn, t) : xn;
-                            T.a_ms[o] = c_scale(g1, famp_illum(S, il, l, pa, pb, m1) * p2inv);
-                        } else {
-                            const float tau = S.ticks_f[t];
-                            const V3 pa = shift_u(S, x1, m1, tau, -1.0f), pb = shift_u(S, xn, mn, tau, -1.0f);
-                            const float f1 = famp_illum(S, il, l, pa, pb, m1);
-                            const float f2 = famp_illum(S, il2, l, pa, pb, m1);
-                            const V3 i1 = src_in(il, l, x1), i2 = src_in(il2, l, x1);
-                            const V3 qv = V3{ 0.5f * (i1.x + i2.x) - x12.x, 0.5f * (i1.y + i2.y) - x12.y, 0.5f * (i1.z + i2.z) - x12.z };
-                            const float c1 = expf(-S.k2 * S.D[m1] * S.abs_ticks[t] * dot3(qv, qv));
-                            T.a_ms[o] = c_scale(c_mulc(g1, T.g2[o]), f1 * f2 * p2inv * c1);
+                const float p2inv = CORR ? 1.0f / p2 : 1.0f / sqrtf(p2);
+                if constexpr (CORR) {
+                    const bool stf = S.static_corr[m1] && S.static_corr[mn];
+                    const bool realg = S.sym && S.static_corr[m1];
+                    const float c1base = k2 * S.D[m1];
+                    for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                        const V3 i1 = fsrc_in(il, l, x1);
+                        const V3 i2 = S.sym ? i1 : fsrc_in(il2, l, x1);
+                        const V3 qv = V3{ 0.5f * (i1.x + i2.x) - x12.x, 0.5f * (i1.y + i2.y) - x12.y, 0.5f * (i1.z + i2.z) - x12.z };
+                        const float c1k = c1base * dot3(qv, qv);
+                        float f12s = 0.0f;
+                        if (stf) f12s = S.sym ? fillum2<ILP>(S, il, l, x1, xn, m1) : fillum<ILP>(S, il, l, x1, xn, m1) * fillum<ILP>(S, il2, l, x1, xn, m1);
+                        for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                            const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                            float f12 = f12s;
+                            if (!stf) {
+                                const float tau = S.ticks_f[t];
+                                const V3 pa = shift_u(S, x1, m1, tau, -1.0f), pb = shift_u(S, xn, mn, tau, -1.0f);
+                                f12 = S.sym ? fillum2<ILP>(S, il, l, pa, pb, m1) : fillum<ILP>(S, il, l, pa, pb, m1) * fillum<ILP>(S, il2, l, pa, pb, m1);
+                            }
+                            const float sc = f12 * p2inv * __expf(-c1k * S.abs_ticks[t]);
+                            if (realg) T.a_ms[o] = make_float2(T.a_ms[o].x * sc, 0.f);
+                            else T.a_ms[o] = c_scale(c_mulc(T.a_ms[o], T.g2[o]), sc);
+                        }
+                    }
+                } else {
+                    const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
+                    for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                        const float fs = stf ? fillum<ILP>(S, il, l, x1, xn, m1) : 0.0f;
+                        for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                            const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                            const float f = stf ? fs : fillum<ILP>(S, il, l, tick_pos(xtc, t), tick_pos(xtn, t), m1);
+                            T.a_ms[o] = c_scale(T.a_ms[o], f * p2inv);
                         }
                     }
                 }
             }
 
             // view vectors at vertex b, summed over the path (multipleResMultiple)
-            const bool stn = corr ? S.static_corr[mn] != 0 : !S.moving[mn];
-            const bool nophase = corr && S.sym && stn;
-            const float ptk = corr ? S.k2 * MT : 0.0f;
-            int j = 0;
-            for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
-                float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
-                uint32_t sts = 0;
-                float c1k = 0.0f, f12s = 0.0f;
-                if (stn) {
-                    g1s = gvec(S, vw, v, xn, kRoleView, corr ? !nophase : true, sts);
-                    if (corr) g2s = nophase ? g1s : gvec(S, vw2, v, xn, kRoleView, true, sts);
-                    if (nophase) sts *= 2;
-                }
-                if (corr) {
-                    const V3 o1 = src_out(vw, v, xn), o2 = src_out(vw2, v, xn);
-                    const V3 back = unit3(sub3(cur, xn));
+            if constexpr (CORR) {
+                const bool stn = S.static_corr[mn] != 0;
+                const bool realv = S.sym && stn;
+                const bool stf = stn && S.static_corr[mcur];
+                const float ptk = k2 * MT;
+                const float c1base = k2 * S.D[mn];
+                const V3 back = funit(sub3(cur, xn));
+                int j = 0;
+                for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
+                    const V3 o1 = fsrc_out(vw, v, xn);
+                    const V3 o2 = S.sym ? o1 : fsrc_out(vw2, v, xn);
                     const V3 qv = V3{ -0.5f * (o1.x + o2.x) - back.x, -0.5f * (o1.y + o2.y) - back.y, -0.5f * (o1.z + o2.z) - back.z };
-                    c1k = S.k2 * S.D[mn] * dot3(qv, qv);
-                    if (stn && S.static_corr[mcur]) {
-                        f12s = famp_view(S, vw, v, xn, cur, mn) * famp_view(S, vw2, v, xn, cur, mn);
+                    const float ck = c1base * dot3(qv, qv) + ptk;
+                    uint32_t sts = 0;
+                    float w = 0.0f;
+                    float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
+                    if (realv) { w = gweight<VWP>(S, vw, v, xn, kRoleView, sts); sts *= 2; }
+                    else if (stn) { g1s = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts); g2s = gcomplex<VWP>(S, vw2, v, xn, kRoleView, sts); }
+                    float f12s = 0.0f;
+                    if (stf) f12s = S.sym ? fview2<VWP>(S, vw, v, xn, cur, mn) : fview<VWP>(S, vw, v, xn, cur, mn) * fview<VWP>(S, vw2, v, xn, cur, mn);
+                    int k = 0;
+                    for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
+                        const float tau = S.ticks_f[t];
+                        float f12 = f12s;
+                        if (!stf) {
+                            const V3 pa = shift_u(S, xn, mn, tau, -1.0f), pb = shift_u(S, cur, mcur, tau, -1.0f);
+                            f12 = S.sym ? fview2<VWP>(S, vw, v, pa, pb, mn) : fview<VWP>(S, vw, v, pa, pb, mn) * fview<VWP>(S, vw2, v, pa, pb, mn);
+                        }
+                        const float dec = f12 * __expf(-ck * S.abs_ticks[t]);
+                        float2 c;
+                        if (realv) { steps += sts; c = make_float2(w * dec, 0.f); }
+                        else {
+                            float2 g1 = g1s, g2 = g2s;
+                            if (stn) steps += sts;
+                            else {
+                                g1 = gcomplex<VWP>(S, vw, v, shift_u(S, xn, mn, tau, -1.0f), kRoleView, steps);
+                                g2 = gcomplex<VWP>(S, vw2, v, shift_u(S, xn, mn, tau, 1.0f), kRoleView, steps);
+                            }
+                            c = c_scale(c_mulc(g1, g2), dec);
+                        }
+                        float2* a = accs + 32 * (j * T.tpl + k);
+                        const float2 av = *a;
+                        *a = make_float2(av.x + c.x, av.y + c.y);
                     }
                 }
-                int k = 0;
-                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
-                    float2 c;
-                    if (!corr) {
-                        const V3 xb = tick_pos(xtn, t);
-                        const float2 g = stn ? g1s : gvec(S, vw, v, xb, kRoleView, true, steps);
+            } else {
+                const bool stn = !S.moving[mn];
+                const bool stf = !S.temporal_amp || (stn && !S.moving[mcur]);
+                int j = 0;
+                for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
+                    uint32_t sts = 0;
+                    float2 gs = make_float2(0.f, 0.f);
+                    if (stn) gs = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts);
+                    const float fs = stf ? fview<VWP>(S, vw, v, xn, cur, mn) : 0.0f;
+                    int k = 0;
+                    for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
+                        float2 g = gs;
                         if (stn) steps += sts;
-                        const V3 pa = S.temporal_amp ? xb : xn;
-                        const V3 pb = S.temporal_amp ? tick_pos(xtc, t) : cur;
-                        const float f = famp_view(S, vw, v, pa, pb, mn);
+                        else g = gcomplex<VWP>(S, vw, v, tick_pos(xtn, t), kRoleView, steps);
+                        const float f = stf ? fs : fview<VWP>(S, vw, v, tick_pos(xtn, t), tick_pos(xtc, t), mn);
                         float fr;
                         if (split) fr = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
                         else { const float ph = (float)Ls[t] * S.inv_lambda_f + xin; fr = ph - rintf(ph); }
-                        c = c_scale(c_mul(g, unit_phase(fr)), f);
-                    } else {
-                        const float tau = S.ticks_f[t];
-                        float2 g1, g2;
-                        if (stn) { g1 = g1s; g2 = g2s; steps += sts; }
-                        else {
-                            g1 = gvec(S, vw, v, shift_u(S, xn, mn, tau, -1.0f), kRoleView, true, steps);
-                            g2 = gvec(S, vw2, v, shift_u(S, xn, mn, tau, 1.0f), kRoleView, true, steps);
-                        }
-                        float f12;
-                        if (stn && S.static_corr[mcur]) f12 = f12s;
-                        else {
-                            const V3 pa = shift_u(S, xn, mn, tau, -1.0f), pb = shift_u(S, cur, mcur, tau, -1.0f);
-                            f12 = famp_view(S, vw, v, pa, pb, mn) * famp_view(S, vw2, v, pa, pb, mn);
-                        }
-                        const float dec = expf(-(c1k + ptk) * S.abs_ticks[t]);
-                        c = c_scale(c_mulc(g1, g2), f12 * dec);
+                        const float2 c = c_scale(c_mul(g, unit_phase(fr)), f);
+                        float2* a = accs + 32 * (j * T.tpl + k);
+                        const float2 av = *a;
+                        *a = make_float2(av.x + c.x, av.y + c.y);
                     }
-                    float2* a = accs + 32 * (j * T.tpl + k);
-                    const float2 av = *a;
-                    *a = make_float2(av.x + c.x, av.y + c.y);
                 }
             }
             prev = cur;
@@ -380,9 +540,8 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
             int j = 0;
             for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                 int k = 0;
-                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
+                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k)
                     T.s_ms[((size_t)q * Nt + t) * Nv + v] = accs[32 * (j * T.tpl + k)];
-                }
             }
         }
         const uint32_t wsteps = warp_sum_u32(steps);
@@ -412,22 +571,37 @@ size_t trace_smem_bytes(int Nt, int slots, int threads)
          + (size_t)warps * 6 * Nt * sizeof(float);
 }
 
-int occupancy_blocks(int threads, size_t smem)
+using TraceFn = void (*)(DevScene, TraceParams);
+
+static TraceFn pick(const DevScene& S)
 {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const bool ip = S.src[0].type == SSTMC_SOURCE_POINT, vp = S.src[1].type == SSTMC_SOURCE_POINT;
+    if (S.correlation) {
+        if (ip) return vp ? (TraceFn)trace_kernel<true, true, true> : (TraceFn)trace_kernel<true, true, false>;
+        return vp ? (TraceFn)trace_kernel<true, false, true> : (TraceFn)trace_kernel<true, false, false>;
+    }
+    if (ip) return vp ? (TraceFn)trace_kernel<false, true, true> : (TraceFn)trace_kernel<false, true, false>;
+    return vp ? (TraceFn)trace_kernel<false, false, true> : (TraceFn)trace_kernel<false, false, false>;
+}
+
+int occupancy_blocks(const DevScene& S, int threads, size_t smem)
+{
+    TraceFn f = pick(S);
+    if (smem > 48 * 1024) cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, trace_kernel, threads, smem) != cudaSuccess) n = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess) n = 1;
     return n > 0 ? n : 1;
 }
 
 int launch_trace(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream)
 {
     const size_t smem = trace_smem_bytes(S.Nt, T.slots, threads);
+    TraceFn f = pick(S);
     if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return SSTMC_KERNEL_ERROR;
     }
-    trace_kernel<<<blocks, threads, smem, stream>>>(S, T);
+    f<<<blocks, threads, smem, stream>>>(S, T);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 
