@@ -65,7 +65,11 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&pl, paths * Nl * sizeof(float)) && alloc((void**)&x1, paths * 3 * sizeof(float))
            && alloc((void**)&x1t, S.correlation ? 8 : paths * Nt * 3 * sizeof(float))
            && alloc((void**)&m1, paths) && alloc((void**)&totals, 8 * sizeof(unsigned long long))
-           && alloc((void**)&err, sizeof(int)) && alloc((void**)&V, Nt * Nv * Nl * sizeof(double2));
+           && alloc((void**)&err, sizeof(int)) && alloc((void**)&V, Nt * Nv * Nl * sizeof(double2))
+           && alloc((void**)&counts, paths * sizeof(uint32_t)) && alloc((void**)&misses, paths * sizeof(uint32_t))
+           && alloc((void**)&offsets, paths * sizeof(uint32_t))
+           && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
+           && alloc((void**)&vtotal, sizeof(unsigned long long));
     if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
     cap = paths;
     return SSTMC_NO_ERROR;
@@ -73,8 +77,9 @@ int Engine::ensure(Scene& S, uint32_t paths)
 
 void Engine::release()
 {
-    void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W };
+    void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts };
     for (void* p : ps) if (p) cudaFree(p);
+    counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
     pl = x1 = x1t = nullptr;
     m1 = nullptr; totals = nullptr; err = nullptr; V = nullptr; W = nullptr;
@@ -151,30 +156,53 @@ void Engine::plan(const Scene& S, TraceParams& T, std::vector<std::pair<int, int
 
 int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, PathDebug* dbg)
 {
+    // 1. random walk: count, scan, write (pathwalk.cu)
+    WalkParams Wp;
+    std::memset(&Wp, 0, sizeof(Wp));
+    Wp.seed = seed; Wp.first_path = first; Wp.paths = n;
+    Wp.counts = counts; Wp.misses = misses; Wp.offsets = offsets; Wp.block_sums = block_sums; Wp.total = vtotal;
+    Wp.err = err; Wp.hash = dbg ? dbg->hash : nullptr;
+    int e = launch_walk_count(S.dev, Wp, stream);
+    if (e) return e;
+    launches += 4;
+    unsigned long long nverts = 0;
+    if (cudaMemcpyAsync(&nverts, vtotal, sizeof(nverts), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
+    if (nverts > verts_cap) {
+        if (verts) cudaFree(verts);
+        verts = nullptr;
+        const size_t cap = (size_t)(nverts * 5 / 4) + 1024;
+        if (cudaMalloc((void**)&verts, cap * sizeof(float4)) != cudaSuccess) { verts_cap = 0; return SSTMC_ALLOCATION_ERROR; }
+        verts_cap = cap;
+    }
+    Wp.verts = verts;
+    e = launch_walk_write(S.dev, Wp, stream);
+    if (e) return e;
+    launches++;
+
+    // 2. NEE vectors per path (trace.cu)
     TraceParams T;
     std::memset(&T, 0, sizeof(T));
     std::vector<std::pair<int, int>> vch, tch;
     plan(S, T, &vch, &tch);
     T.seed = seed; T.first_path = first; T.paths = n;
+    T.verts = verts; T.counts = counts; T.offsets = offsets; T.misses = misses;
     T.a_ms = a_ms; T.s_ms = s_ms; T.a_ss = a_ss; T.b_ss = b_ss; T.g2 = g2; T.pl = pl;
     T.x1 = x1; T.x1t = S.correlation ? nullptr : x1t; T.m1 = m1; T.totals = totals; T.err = err;
-    if (dbg) { T.nvert = dbg->nvert; T.misses = dbg->misses; T.hash = dbg->hash; T.dda = dbg->dda; }
-    int dev = 0, sms = 0, per_sm = 0;
+    if (dbg) T.dda = dbg->dda;
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int threads = 128;
     const size_t smem = trace_smem_bytes(S.Nt, T.slots, threads);
-    if (smem > 48 * 1024) {
-        // attribute is set inside launch_trace; occupancy query below tolerates either state
-    }
-    per_sm = occupancy_blocks(S.dev, threads, smem);
+    const int per_sm = occupancy_blocks(S.dev, threads, smem);
     const int blocks = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_sm)));
     bool first_pass = true;
     for (auto& vc : vch) {
         for (auto& tc : tch) {
             T.pass0 = first_pass ? 1 : 0;
             T.v0 = vc.first; T.vn = vc.second; T.t0 = tc.first; T.tn = tc.second;
-            const int e = launch_trace(S.dev, T, blocks, threads, stream);
+            e = launch_trace(S.dev, T, blocks, threads, stream);
             if (e) return e;
             launches++;
             first_pass = false;
@@ -417,10 +445,8 @@ int32_t sstmc_trace_paths(sstmc_scene* s, uint64_t seed, uint32_t first_path, ui
     int e = E.ensure(S, paths);
     if (e) return e;
     PathDebug dbg;
-    if (cudaMalloc((void**)&dbg.nvert, paths * sizeof(int)) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
-    cudaMalloc((void**)&dbg.misses, paths * sizeof(int));
-    cudaMalloc((void**)&dbg.hash, paths * sizeof(uint32_t));
-    cudaMalloc((void**)&dbg.dda, paths * sizeof(uint32_t));
+    if (cudaMalloc((void**)&dbg.hash, paths * sizeof(uint32_t)) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    if (cudaMalloc((void**)&dbg.dda, paths * sizeof(uint32_t)) != cudaSuccess) { cudaFree(dbg.hash); return SSTMC_ALLOCATION_ERROR; }
     cudaMemsetAsync(dbg.dda, 0, paths * sizeof(uint32_t), E.stream);
     cudaMemsetAsync(E.totals, 0, 8 * sizeof(unsigned long long), E.stream);
     cudaMemsetAsync(E.err, 0, sizeof(int), E.stream);
@@ -433,8 +459,8 @@ int32_t sstmc_trace_paths(sstmc_scene* s, uint64_t seed, uint32_t first_path, ui
     if (!e && herr) e = herr;
     if (!e) {
         const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
-        if (out->misses) cudaMemcpy(out->misses, dbg.misses, paths * sizeof(int), cudaMemcpyDeviceToHost);
-        if (out->vertices) cudaMemcpy(out->vertices, dbg.nvert, paths * sizeof(int), cudaMemcpyDeviceToHost);
+        if (out->misses) cudaMemcpy(out->misses, E.misses, paths * sizeof(int), cudaMemcpyDeviceToHost);
+        if (out->vertices) cudaMemcpy(out->vertices, E.counts, paths * sizeof(int), cudaMemcpyDeviceToHost);
         if (out->vertex_hash) cudaMemcpy(out->vertex_hash, dbg.hash, paths * sizeof(uint32_t), cudaMemcpyDeviceToHost);
         if (out->dda_steps) cudaMemcpy(out->dda_steps, dbg.dda, paths * sizeof(uint32_t), cudaMemcpyDeviceToHost);
         if (out->x1) cudaMemcpy(out->x1, E.x1, paths * 3 * sizeof(float), cudaMemcpyDeviceToHost);
@@ -454,7 +480,7 @@ int32_t sstmc_trace_paths(sstmc_scene* s, uint64_t seed, uint32_t first_path, ui
         copy_c(out->a_ss, E.a_ss, paths * Nt * Nl);
         copy_c(out->b_ss, E.b_ss, paths * Nt * Nv);
     }
-    cudaFree(dbg.nvert); cudaFree(dbg.misses); cudaFree(dbg.hash); cudaFree(dbg.dda);
+    cudaFree(dbg.hash); cudaFree(dbg.dda);
     return e;
 }
 

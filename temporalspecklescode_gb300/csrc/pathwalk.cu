@@ -1,0 +1,187 @@
+// pathwalk.cu -- the random walk, one thread per path.
+//
+// Samples the first vertex with miss resampling (NextEventEstimation.cuh:643-679,
+// FarField.cuh:129-205 / PointSource.cuh:72-90 + Woodcock free flight,
+// HeterogeneousMedium.cuh:576-678) and every later vertex (phase-function
+// direction, Scattering.cuh:1039-1115, then free flight) until the path leaves
+// the medium or is absorbed.  The walk is run twice over the same Philox
+// streams: the first pass counts each path's vertices, an exclusive scan turns
+// the counts into offsets, and the second pass writes the vertices compactly
+// (16 bytes each: position and a packed word holding the material and the
+// per-vertex phase draw).  The NEE kernel then reads them with no walk code.
+#include <cuda_runtime.h>
+
+#include "pathwalk.h"
+#include "walk.cuh"
+
+namespace sstmc {
+
+namespace {
+
+__device__ __forceinline__ uint32_t u1_count_w(const DevScene& S, uint64_t seed, uint32_t wave)
+{
+    Stream ws;
+    ws.init(seed, wave, 0u, kPurposeWave);
+    int c = (int)ceilf(fm(ws.uniform(), (float)(S.P + 1u))) - 1;
+    c = c < 0 ? 0 : (c > (int)S.P ? (int)S.P : c);
+    return (uint32_t)c;
+}
+
+__device__ __forceinline__ uint32_t hash_v(const DevScene& S, uint32_t h, const V3& x, int m)
+{
+    h = hash_mix(h, __float_as_uint(x.x));
+    h = hash_mix(h, __float_as_uint(x.y));
+    if (S.dims == 3) h = hash_mix(h, __float_as_uint(x.z));
+    return hash_mix(h, (uint32_t)m);
+}
+
+__device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
+{
+    const uint32_t k = (uint32_t)(xi * 16777216.0f);  // xi = k * 2^-24 exactly
+    return make_float4(x.x, x.y, x.z, __uint_as_float((k << 4) | (uint32_t)m));
+}
+
+template <bool WRITE>
+__global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
+{
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= W.paths) return;
+    if (WRITE && W.counts[q] == 0) {  // the count pass hit a limit: nothing to write
+        if (W.hash) W.hash[q] = 2166136261u;
+        return;
+    }
+    const uint32_t pid = W.first_path + q;
+    const uint32_t slot = pid % S.P, wave = pid / S.P;
+    const bool corr = S.correlation != 0;
+    const bool side1 = !corr || slot < u1_count_w(S, W.seed, wave);
+    const DevSource& fsrc = side1 ? S.src[0] : S.src[2];
+    V3 x0, d0, x1;
+    int m1 = 0;
+    uint32_t att;
+    Stream rs;
+    bool ok = true;
+    for (att = 0; att < kMaxAttempts; ++att) {
+        rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
+        sample_source(S, fsrc, rs, x0, d0);
+        if (!woodcock(S, x0, d0, rs, x1, m1)) { ok = false; break; }
+        if (m1 > 0) break;
+    }
+    if (att >= kMaxAttempts) ok = false;
+    float4* out = nullptr;
+    if (WRITE) out = W.verts + W.offsets[q];
+    uint32_t B = 0;
+    uint32_t h = 2166136261u;
+    if (ok) {
+        const float xi1 = corr ? 0.0f : rs.uniform();
+        B = 1;
+        if (WRITE) {
+            out[0] = pack_vertex(x1, m1, xi1);
+            h = hash_v(S, h, x1, m1);
+        }
+        V3 prev = x0, cur = x1;
+        int mcur = m1;
+        for (uint32_t b = 2;; ++b) {
+            if (b > kMaxVertices) { ok = false; break; }
+            rs.init(W.seed, pid, b, kPurposeWalk);
+            const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
+            const V3 nd = sample_direction(S, mcur, din, rs);
+            V3 xn;
+            int mn = 0;
+            if (!woodcock(S, cur, nd, rs, xn, mn)) { ok = false; break; }
+            if (mn == 0) break;
+            const float xin = corr ? 0.0f : rs.uniform();
+            if (WRITE) {
+                if (b - 1 >= W.counts[q]) { ok = false; break; }  // replay disagrees with the count pass
+                out[b - 1] = pack_vertex(xn, mn, xin);
+                h = hash_v(S, h, xn, mn);
+            }
+            B = b;
+            prev = cur;
+            cur = xn;
+            mcur = mn;
+        }
+    }
+    if (!ok) {
+        atomicExch(W.err, SSTMC_PATH_LIMIT);
+        B = 0;
+    }
+    if (!WRITE) {
+        W.counts[q] = B;
+        W.misses[q] = att;
+    } else {
+        if (W.hash) W.hash[q] = h;
+    }
+}
+
+// Exclusive scan of counts[0, n) into offsets (three phases: per-block scan,
+// scan of block totals, block offset add).  total[0] = sum.
+constexpr int kScanBlock = 1024;
+
+__global__ void scan_block_kernel(const uint32_t* counts, uint32_t* offsets, uint32_t* block_sums, uint32_t n)
+{
+    __shared__ uint32_t s[kScanBlock];
+    const uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
+    const uint32_t v = i < n ? counts[i] : 0u;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+        const uint32_t add = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0u;
+        __syncthreads();
+        s[threadIdx.x] += add;
+        __syncthreads();
+    }
+    if (i < n) offsets[i] = s[threadIdx.x] - v;
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void scan_totals_kernel(uint32_t* block_sums, uint32_t nb, unsigned long long* total)
+{
+    __shared__ unsigned long long s[kScanBlock];
+    unsigned long long run = 0;
+    for (uint32_t base = 0; base < nb; base += kScanBlock) {
+        const uint32_t i = base + threadIdx.x;
+        const unsigned long long v = i < nb ? block_sums[i] : 0ull;
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < kScanBlock; o <<= 1) {
+            const unsigned long long add = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0ull;
+            __syncthreads();
+            s[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < nb) block_sums[i] = (uint32_t)(run + s[threadIdx.x] - v);
+        const unsigned long long last = s[kScanBlock - 1];
+        __syncthreads();
+        run += last;
+    }
+    if (threadIdx.x == 0) *total = run;
+}
+
+__global__ void scan_add_kernel(uint32_t* offsets, const uint32_t* block_sums, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) offsets[i] += block_sums[blockIdx.x];
+}
+
+}  // namespace
+
+int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
+{
+    const int threads = 128;
+    walk_kernel<false><<<(W.paths + threads - 1) / threads, threads, 0, stream>>>(S, W);
+    if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
+    const uint32_t nb = (W.paths + kScanBlock - 1) / kScanBlock;
+    scan_block_kernel<<<nb, kScanBlock, 0, stream>>>(W.counts, W.offsets, W.block_sums, W.paths);
+    scan_totals_kernel<<<1, kScanBlock, 0, stream>>>(W.block_sums, nb, W.total);
+    scan_add_kernel<<<nb, kScanBlock, 0, stream>>>(W.offsets, W.block_sums, W.paths);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
+
+int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t stream)
+{
+    const int threads = 128;
+    walk_kernel<true><<<(W.paths + threads - 1) / threads, threads, 0, stream>>>(S, W);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
+}
+
+}  // namespace sstmc

@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "scene.h"
+#include "pathwalk.h"
 #include "trace.h"
 
 namespace sstmc {
@@ -14,8 +15,6 @@ namespace sstmc {
 constexpr int kMaxSlots = 32;  // view-accumulator slots per lane (8 KB of shared memory per warp)
 
 struct PathDebug {
-    int* nvert = nullptr;
-    int* misses = nullptr;
     uint32_t* hash = nullptr;
     uint32_t* dda = nullptr;
 };
@@ -28,6 +27,10 @@ struct Engine {
     float2 *a_ms = nullptr, *s_ms = nullptr, *a_ss = nullptr, *b_ss = nullptr, *g2 = nullptr;
     float *pl = nullptr, *x1 = nullptr, *x1t = nullptr;
     unsigned char* m1 = nullptr;
+    uint32_t *counts = nullptr, *misses = nullptr, *offsets = nullptr, *block_sums = nullptr;
+    unsigned long long* vtotal = nullptr;
+    float4* verts = nullptr;
+    size_t verts_cap = 0;
     unsigned long long* totals = nullptr;
     int* err = nullptr;
     double2* V = nullptr;

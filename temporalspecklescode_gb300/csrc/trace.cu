@@ -239,29 +239,16 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t pid = T.first_path + q;
-        const uint32_t slot = pid % S.P, wave = pid / S.P;
-        const bool side1 = !CORR || slot < u1_count(S, T.seed, wave);
-        const DevSource& fsrc = side1 ? il : il2;
-
-        // ---- first vertex, with miss resampling (NEE.cuh:643-679) ----
-        V3 x0, d0, x1;
-        int m1 = 0;
-        uint32_t att = 0;
-        Stream rs;
-        bool ok = true;
-        for (att = 0; att < kMaxAttempts; ++att) {
-            rs.init(T.seed, pid, 1u, kPurposeWalk | (att << 8));
-            sample_source(S, fsrc, rs, x0, d0);
-            if (!woodcock(S, x0, d0, rs, x1, m1)) { ok = false; break; }
-            if (m1 > 0) break;
-        }
-        if (att >= kMaxAttempts) ok = false;
-        if (!ok) {
-            if (lane == 0) atomicExch(T.err, SSTMC_PATH_LIMIT);
+        const uint32_t B = T.counts[q];
+        if (B == 0) {  // the walk hit a limit (error already flagged)
             zero_rows(S, T, q, lane);
             continue;
         }
-        const float xi1 = CORR ? 0.0f : rs.uniform();
+        const float4* vq = T.verts + T.offsets[q];
+        const float4 v1 = vq[0];
+        const V3 x1 = V3{ v1.x, v1.y, v1.z };
+        const int m1 = (int)(__float_as_uint(v1.w) & 15u);
+        const float xi1 = (float)(__float_as_uint(v1.w) >> 4) * (1.0f / 16777216.0f);
         float* xtc = bufA;   // tick positions of the current vertex
         float* xtn = bufB;   // tick positions of the new vertex
         bool mov1 = false;
@@ -274,7 +261,6 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
                 for (int i = lane; i < 3 * Nt; i += 32) T.x1t[(size_t)q * 3 * Nt + i] = xtc[i];
         }
         uint32_t steps = 0;
-        uint32_t h = hash_vertex(S, 2166136261u, x1, m1);
 
         // ---- illumination side at x1: P_l, Gl0, single-scattering rows ----
         if (T.pass0) {
@@ -370,22 +356,14 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
 
         // ---- later vertices ----
         for (int i = 0; i < T.slots; ++i) accs[32 * i] = make_float2(0.f, 0.f);
-        V3 prev = x0, cur = x1;
+        V3 prev = x1, cur = x1;
         int mcur = m1;
-        uint32_t B = 1;
         float MT = 0.0f;
-        for (uint32_t b = 2;; ++b) {
-            if (b > kMaxVertices) { ok = false; break; }
-            rs.init(T.seed, pid, b, kPurposeWalk);
-            const V3 din = normalize32(D, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
-            const V3 nd = sample_direction(S, mcur, din, rs);
-            V3 xn;
-            int mn = 0;
-            if (!woodcock(S, cur, nd, rs, xn, mn)) { ok = false; break; }
-            if (mn == 0) break;
-            const float xin = CORR ? 0.0f : rs.uniform();
-            B = b;
-            h = hash_vertex(S, h, xn, mn);
+        for (uint32_t b = 2; b <= B; ++b) {
+            const float4 vb = vq[b - 1];
+            const V3 xn = V3{ vb.x, vb.y, vb.z };
+            const int mn = (int)(__float_as_uint(vb.w) & 15u);
+            const float xin = (float)(__float_as_uint(vb.w) >> 4) * (1.0f / 16777216.0f);
             if (CORR && b >= 3) {
                 // momentum transfer of the inner vertex cur (TemporalSamplerCorrelation.cuh:144-179)
                 const V3 dq = sub3(funit(sub3(cur, prev)), funit(sub3(xn, cur)));
@@ -527,11 +505,6 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
             mcur = mn;
             float* tmp = xtc; xtc = xtn; xtn = tmp;
         }
-        if (!ok) {
-            if (lane == 0) atomicExch(T.err, SSTMC_PATH_LIMIT);
-            zero_rows(S, T, q, lane);
-            continue;
-        }
         if (T.pass0 && B < 2) {
             for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
         }
@@ -547,13 +520,10 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
         const uint32_t wsteps = warp_sum_u32(steps);
         if (lane == 0) {
             if (T.pass0) {
-                if (T.nvert) T.nvert[q] = (int)B;
-                if (T.misses) T.misses[q] = (int)att;
-                if (T.hash) T.hash[q] = h;
                 if (T.m1) T.m1[q] = (unsigned char)m1;
                 if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
                 atomicAdd(T.totals + 0, (unsigned long long)B);
-                atomicAdd(T.totals + 2, (unsigned long long)att);
+                atomicAdd(T.totals + 2, (unsigned long long)T.misses[q]);
                 atomicAdd(T.totals + 3, 1ull);
             }
             if (T.dda) atomicAdd(T.dda + q, wsteps);

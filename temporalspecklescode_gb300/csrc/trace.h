@@ -17,6 +17,10 @@ struct TraceParams {
     int slots;            // accumulator slots per lane (vpl * tpl)
     int lw, lg;           // illumination-side lane split (all ticks)
     int vwa, tga;         // single-scattering view-side lane split (all views, all ticks)
+    const float4* verts;      // vertices of the walk (pathwalk.cu), path q at offsets[q]
+    const uint32_t* counts;   // [paths] vertices (0: the walk hit a limit)
+    const uint32_t* offsets;  // [paths]
+    const uint32_t* misses;   // [paths]
     float2* a_ms;         // [paths][Nt][Nl]
     float2* s_ms;         // [paths][Nt][Nv]
     float2* a_ss;         // [paths][Nt][Nl]
@@ -26,9 +30,6 @@ struct TraceParams {
     float* x1;            // [paths][3]
     float* x1t;           // [paths][Nt][3] or null
     unsigned char* m1;    // [paths]
-    int* nvert;           // [paths] or null
-    int* misses;          // [paths] or null
-    uint32_t* hash;       // [paths] or null
     uint32_t* dda;        // [paths] or null (accumulated over passes)
     unsigned long long* totals;  // [0] vertices, [1] dda steps, [2] misses, [3] paths
     int* err;
