@@ -254,16 +254,19 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
 // (illumination, view) block and all ticks of a chunk.
 constexpr int kFl = 32, kFv = 32, kFk = 16, kFt = 8;
 
-constexpr size_t kFastSmem = sizeof(float) * (2 * kFk * kFt * kFl + 6 * kFk * kFl) + sizeof(int) * kFk
+constexpr size_t kFastSmem = sizeof(float) * (2 * kFk * kFl + 6 * kFk * kFl) + sizeof(int) * kFk
                            + sizeof(double) * 4 * kFt * 256;
 
+// Rows here are tick-invariant (static scatterers, identical u1 / u2
+// sources), so only the first tick's rows are read; the tick dependence is
+// the decay exp(-c |t|), chained multiplicatively for geometric ticks.
 __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__ DevScene S, const SsParams G)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* accd = reinterpret_cast<double*>(smem_raw);                       // [4*kFt][256] FP64 window sums
-    float* as = reinterpret_cast<float*>(accd + 4 * kFt * 256);              // [kFk][kFt][kFl]
-    float* bs = as + kFk * kFt * kFl;                                         // [kFk][kFt][kFv]
-    float* inx = bs + kFk * kFt * kFv;                                        // [kFk][3][kFl]
+    float* as = reinterpret_cast<float*>(accd + 4 * kFt * 256);              // [kFk][kFl]
+    float* bs = as + kFk * kFl;                                               // [kFk][kFv]
+    float* inx = bs + kFk * kFv;                                              // [kFk][3][kFl]
     float* outx = inx + kFk * 3 * kFl;                                        // [kFk][3][kFv]
     int* m1s = reinterpret_cast<int*>(outx + kFk * 3 * kFv);
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -278,6 +281,7 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     const DevSource& vw = S.src[1];
     const bool geo = S.ticks_geometric != 0;
     const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
+    const float tau0 = S.abs_ticks[0], taus = S.abs_ticks[t0];
     float acc[2][2][kFt];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -287,27 +291,23 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             for (int t = 0; t < kFt; ++t) { acc[i][j][t] = 0.f; accd[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = 0.0; }
     int chunk = 0;
     for (int k = kb; k < ke; k += kFk, ++chunk) {
-        for (int idx = threadIdx.x; idx < kFk * kFt * kFl; idx += 256) {
-            const int pp = idx / (kFt * kFl), r = idx % (kFt * kFl);
-            const int tt = r / kFl, c = r % kFl;
+        for (int idx = threadIdx.x; idx < kFk * kFl; idx += 256) {
+            const int pp = idx / kFl, c = idx % kFl;
             const int p = k + pp;
             float a = 0.f, b = 0.f;
-            if (p < ke && tt < tn) {
-                if (l0 + c < Nl) a = G.a[((size_t)p * Nt + t0 + tt) * Nl + l0 + c].x;
-                if (v0 + c < Nv) b = G.b[((size_t)p * Nt + t0 + tt) * Nv + v0 + c].x;
+            if (p < ke) {
+                if (l0 + c < Nl) a = G.a[(size_t)p * Nt * Nl + l0 + c].x;
+                if (v0 + c < Nv) b = G.b[(size_t)p * Nt * Nv + v0 + c].x;
             }
             as[idx] = a;
             bs[idx] = b;
-        }
-        for (int idx = threadIdx.x; idx < kFk * kFl; idx += 256) {
-            const int pp = idx / kFl, c = idx % kFl;
-            const int p = min(k + pp, ke - 1);
-            const V3 x = V3{ G.x1[3 * p], G.x1[3 * p + 1], G.x1[3 * p + 2] };
+            const int pc = min(p, ke - 1);
+            const V3 x = V3{ G.x1[3 * pc], G.x1[3 * pc + 1], G.x1[3 * pc + 2] };
             const V3 i1 = fsrc_in(il, min(l0 + c, Nl - 1), x);
             const V3 o1 = fsrc_out(vw, min(v0 + c, Nv - 1), x);
             inx[(pp * 3 + 0) * kFl + c] = i1.x; inx[(pp * 3 + 1) * kFl + c] = i1.y; inx[(pp * 3 + 2) * kFl + c] = i1.z;
             outx[(pp * 3 + 0) * kFv + c] = o1.x; outx[(pp * 3 + 1) * kFv + c] = o1.y; outx[(pp * 3 + 2) * kFv + c] = o1.z;
-            if (c == 0) m1s[pp] = (k + pp < ke) ? (int)G.m1[k + pp] : 0;
+            if (c == 0) m1s[pp] = p < ke ? (int)G.m1[p] : 0;
         }
         __syncthreads();
         for (int pp = 0; pp < kFk; ++pp) {
@@ -316,7 +316,8 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             const int ty_ = S.scat_type[m];
             const float g = S.g[m], omg = 1.0f - g, gup = S.gup[m];
             const float c1 = S.k2 * S.D[m];
-            float w[2][2], e[2][2], estep[2][2], cq[2][2];
+            const float av[2] = { as[pp * kFl + tx], as[pp * kFl + tx + 16] };
+            const float bv[2] = { bs[pp * kFv + ty], bs[pp * kFv + ty + 16] };
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -335,27 +336,22 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                     }
                     // scalar single-scattering amplitude (point x point, isotropic): the
                     // temporal factor is not applied (NextEventEstimation.cuh:1024-1032)
-                    w[i][j] = scalar_fs ? S.iso_amp * S.iso_amp : pdf;
-                    cq[i][j] = scalar_fs ? 0.0f : c1 * q2;
-                    e[i][j] = __expf(-cq[i][j] * S.abs_ticks[t0]);
-                    estep[i][j] = geo ? __expf(-cq[i][j] * S.abs_ticks[0]) : 0.0f;
-                }
+                    const float base = av[i] * bv[j] * (scalar_fs ? S.iso_amp * S.iso_amp : pdf);
+                    const float cq = scalar_fs ? 0.0f : c1 * q2;
+                    if (geo) {
+                        float e = __expf(-cq * taus);
+                        const float es = __expf(-cq * tau0);
 #pragma unroll
-            for (int tt = 0; tt < kFt; ++tt) {
-                if (tt >= tn) break;
-                const float* ar = as + (pp * kFt + tt) * kFl;
-                const float* br = bs + (pp * kFt + tt) * kFv;
-                const float av[2] = { ar[tx], ar[tx + 16] }, bv[2] = { br[ty], br[ty + 16] };
+                        for (int tt = 0; tt < kFt; ++tt) {
+                            if (tt < tn) acc[i][j][tt] = fmaf(base, e, acc[i][j][tt]);
+                            e *= es;
+                        }
+                    } else {
 #pragma unroll
-                for (int i = 0; i < 2; ++i)
-#pragma unroll
-                    for (int j = 0; j < 2; ++j) {
-                        float wt;
-                        if (geo) { wt = w[i][j] * e[i][j]; e[i][j] *= estep[i][j]; }
-                        else wt = w[i][j] * __expf(-cq[i][j] * S.abs_ticks[t0 + tt]);
-                        acc[i][j][tt] = fmaf(av[i] * bv[j], wt, acc[i][j][tt]);
+                        for (int tt = 0; tt < kFt; ++tt)
+                            if (tt < tn) acc[i][j][tt] = fmaf(base, __expf(-cq * S.abs_ticks[t0 + tt]), acc[i][j][tt]);
                     }
-            }
+                }
         }
         __syncthreads();
         if ((chunk + 1) % 16 == 0) {

@@ -23,23 +23,6 @@ namespace sstmc {
 
 namespace {
 
-__device__ __forceinline__ uint32_t u1_count(const DevScene& S, uint64_t seed, uint32_t wave)
-{
-    Stream ws;
-    ws.init(seed, wave, 0u, kPurposeWave);
-    int c = (int)ceilf(fm(ws.uniform(), (float)(S.P + 1u))) - 1;
-    c = c < 0 ? 0 : (c > (int)S.P ? (int)S.P : c);
-    return (uint32_t)c;
-}
-
-__device__ __forceinline__ uint32_t hash_vertex(const DevScene& S, uint32_t h, const V3& x, int m)
-{
-    h = hash_mix(h, __float_as_uint(x.x));
-    h = hash_mix(h, __float_as_uint(x.y));
-    if (S.dims == 3) h = hash_mix(h, __float_as_uint(x.z));
-    return hash_mix(h, (uint32_t)m);
-}
-
 // Per-tick positions of a vertex of the field sampler (TemporalSampler.cuh:376-436,
 // 540-647, 778-937): Brownian displacement N(0, 2 dims D |dt|) along a random
 // direction plus dt U per sorted tick, cumulated outward from the mean tick.
@@ -214,7 +197,7 @@ __device__ __forceinline__ float fview2(const DevScene& S, const DevSource& s, i
 
 // CORR: correlation sampler; ILP / VWP: illumination / view sources are point sources.
 template <bool CORR, bool ILP, bool VWP>
-__global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+__global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     extern __shared__ double smem_d[];
     const int lane = threadIdx.x & 31;
@@ -229,11 +212,16 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
     float* fbase = reinterpret_cast<float*>(reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)nwb * T.slots * 32);
     float* bufA = fbase + (size_t)wib * 6 * Nt;
     float* bufB = bufA + 3 * Nt;
+    float* tk_abs = fbase + (size_t)nwb * 6 * Nt;   // block-wide copies of |t| and t
+    float* tk_raw = tk_abs + Nt;
+    for (int t = threadIdx.x; t < Nt; t += blockDim.x) { tk_abs[t] = S.abs_ticks[t]; tk_raw[t] = S.ticks_f[t]; }
+    __syncthreads();
     const DevSource& il = S.src[0];
     const DevSource& vw = S.src[1];
     const DevSource& il2 = S.src[2];
     const DevSource& vw2 = S.src[3];
     const float k2 = S.k2;
+    const bool geo = S.ticks_geometric != 0;
 
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
@@ -297,7 +285,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
                             float2 g1 = g1s, g2 = g2s;
                             if (st1) steps += sts;
                             else {
-                                const float tau = S.ticks_f[t];
+                                const float tau = tk_raw[t];
                                 g1 = gcomplex<ILP>(S, il, l, shift_u(S, x1, m1, tau, -1.0f), kRoleIllum, steps);
                                 g2 = gcomplex<ILP>(S, il2, l, shift_u(S, x1, m1, tau, 1.0f), kRoleIllum, steps);
                             }
@@ -318,7 +306,7 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
                         if (realg) { steps += sts; b = make_float2(w, 0.f); }
                         else if (st1) { steps += sts; b = c_mulc(g1s, g2s); }
                         else {
-                            const float tau = S.ticks_f[t];
+                            const float tau = tk_raw[t];
                             b = c_mulc(gcomplex<VWP>(S, vw, v, shift_u(S, x1, m1, tau, -1.0f), kRoleView, steps),
                                        gcomplex<VWP>(S, vw2, v, shift_u(S, x1, m1, tau, 1.0f), kRoleView, steps));
                         }
@@ -403,15 +391,19 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
                         const float c1k = c1base * dot3(qv, qv);
                         float f12s = 0.0f;
                         if (stf) f12s = S.sym ? fillum2<ILP>(S, il, l, x1, xn, m1) : fillum<ILP>(S, il, l, x1, xn, m1) * fillum<ILP>(S, il2, l, x1, xn, m1);
-                        for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                        const int tfirst = lane / T.lw;
+                        float e = tfirst < Nt ? __expf(-c1k * tk_abs[tfirst]) : 0.0f;
+                        const float estep = geo ? __expf(-c1k * tk_abs[0] * (float)T.lg) : 0.0f;
+                        for (int t = tfirst; t < Nt; t += T.lg) {
                             const size_t o = ((size_t)q * Nt + t) * Nl + l;
                             float f12 = f12s;
                             if (!stf) {
-                                const float tau = S.ticks_f[t];
+                                const float tau = tk_raw[t];
                                 const V3 pa = shift_u(S, x1, m1, tau, -1.0f), pb = shift_u(S, xn, mn, tau, -1.0f);
                                 f12 = S.sym ? fillum2<ILP>(S, il, l, pa, pb, m1) : fillum<ILP>(S, il, l, pa, pb, m1) * fillum<ILP>(S, il2, l, pa, pb, m1);
                             }
-                            const float sc = f12 * p2inv * __expf(-c1k * S.abs_ticks[t]);
+                            const float sc = f12 * p2inv * (geo ? e : __expf(-c1k * tk_abs[t]));
+                            e *= estep;
                             if (realg) T.a_ms[o] = make_float2(T.a_ms[o].x * sc, 0.f);
                             else T.a_ms[o] = c_scale(c_mulc(T.a_ms[o], T.g2[o]), sc);
                         }
@@ -451,14 +443,18 @@ __global__ void __launch_bounds__(128) trace_kernel(const __grid_constant__ DevS
                     float f12s = 0.0f;
                     if (stf) f12s = S.sym ? fview2<VWP>(S, vw, v, xn, cur, mn) : fview<VWP>(S, vw, v, xn, cur, mn) * fview<VWP>(S, vw2, v, xn, cur, mn);
                     int k = 0;
-                    for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
-                        const float tau = S.ticks_f[t];
+                    const int tfirst = T.t0 + lane / T.vw;
+                    float e = tfirst < T.t0 + T.tn ? __expf(-ck * tk_abs[tfirst]) : 0.0f;
+                    const float estep = geo ? __expf(-ck * tk_abs[0] * (float)T.tg) : 0.0f;
+                    for (int t = tfirst; t < T.t0 + T.tn; t += T.tg, ++k) {
+                        const float tau = tk_raw[t];
                         float f12 = f12s;
                         if (!stf) {
                             const V3 pa = shift_u(S, xn, mn, tau, -1.0f), pb = shift_u(S, cur, mcur, tau, -1.0f);
                             f12 = S.sym ? fview2<VWP>(S, vw, v, pa, pb, mn) : fview<VWP>(S, vw, v, pa, pb, mn) * fview<VWP>(S, vw2, v, pa, pb, mn);
                         }
-                        const float dec = f12 * __expf(-ck * S.abs_ticks[t]);
+                        const float dec = f12 * (geo ? e : __expf(-ck * tk_abs[t]));
+                        e *= estep;
                         float2 c;
                         if (realv) { steps += sts; c = make_float2(w * dec, 0.f); }
                         else {
@@ -538,7 +534,7 @@ size_t trace_smem_bytes(int Nt, int slots, int threads)
 {
     const int warps = threads / 32;
     return (size_t)warps * Nt * sizeof(double) + (size_t)warps * slots * 32 * sizeof(float2)
-         + (size_t)warps * 6 * Nt * sizeof(float);
+         + (size_t)warps * 6 * Nt * sizeof(float) + 2 * (size_t)Nt * sizeof(float);
 }
 
 using TraceFn = void (*)(DevScene, TraceParams);
