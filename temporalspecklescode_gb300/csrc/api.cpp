@@ -39,7 +39,10 @@ size_t budget_bytes()
 {
     const char* e = std::getenv("SSTMC_CHUNK_BYTES");
     if (e) { const long long v = std::atoll(e); if (v > 0) return (size_t)v; }
-    return (size_t)2 << 30;
+    // a quarter of the free device memory, at most 16 GiB
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return (size_t)2 << 30;
+    return std::min<size_t>((size_t)16 << 30, std::max<size_t>((size_t)256 << 20, fr / 4));
 }
 
 }  // namespace

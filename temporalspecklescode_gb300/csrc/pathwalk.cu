@@ -11,6 +11,8 @@
 // per-vertex phase draw).  The NEE kernel then reads them with no walk code.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pathwalk.h"
 #include "walk.cuh"
 
@@ -41,75 +43,82 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
     return make_float4(x.x, x.y, x.z, __uint_as_float((k << 4) | (uint32_t)m));
 }
 
+// Flattened walk: each thread owns paths q = tid, tid + nthreads, ... and
+// samples one vertex (or one first-vertex attempt) per iteration, moving on
+// to its next path as soon as one ends, so the lanes of a warp stay on the
+// same free-flight code instead of idling behind the longest path.
 template <bool WRITE>
 __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
-    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= W.paths) return;
-    if (WRITE && W.counts[q] == 0) {  // the count pass hit a limit: nothing to write
-        if (W.hash) W.hash[q] = 2166136261u;
-        return;
-    }
-    const uint32_t pid = W.first_path + q;
-    const uint32_t slot = pid % S.P, wave = pid / S.P;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     const bool corr = S.correlation != 0;
-    const bool side1 = !corr || slot < u1_count_w(S, W.seed, wave);
-    const DevSource& fsrc = side1 ? S.src[0] : S.src[2];
-    V3 x0, d0, x1;
-    int m1 = 0;
-    uint32_t att;
-    Stream rs;
-    bool ok = true;
-    for (att = 0; att < kMaxAttempts; ++att) {
-        rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
-        sample_source(S, fsrc, rs, x0, d0);
-        if (!woodcock(S, x0, d0, rs, x1, m1)) { ok = false; break; }
-        if (m1 > 0) break;
-    }
-    if (att >= kMaxAttempts) ok = false;
+    uint32_t pid = 0, att = 0, b = 1, B = 0, h = 2166136261u;
+    V3 prev{ 0.f, 0.f, 0.f }, cur{ 0.f, 0.f, 0.f };
+    int mcur = 0;
     float4* out = nullptr;
-    if (WRITE) out = W.verts + W.offsets[q];
-    uint32_t B = 0;
-    uint32_t h = 2166136261u;
-    if (ok) {
-        const float xi1 = corr ? 0.0f : rs.uniform();
-        B = 1;
-        if (WRITE) {
-            out[0] = pack_vertex(x1, m1, xi1);
-            h = hash_v(S, h, x1, m1);
+    const DevSource* fsrc = &S.src[0];
+    // advance to the next path this thread owns that has work; false when done
+    auto start = [&](uint32_t qq) -> bool {
+        while (qq < W.paths) {
+            if (!WRITE || W.counts[qq] != 0) break;
+            if (W.hash) W.hash[qq] = 2166136261u;  // the count pass hit a limit: nothing to write
+            qq += nthreads;
         }
-        V3 prev = x0, cur = x1;
-        int mcur = m1;
-        for (uint32_t b = 2;; ++b) {
-            if (b > kMaxVertices) { ok = false; break; }
+        q = qq;
+        if (q >= W.paths) return false;
+        pid = W.first_path + q;
+        const uint32_t slot = pid % S.P, wave = pid / S.P;
+        fsrc = (!corr || slot < u1_count_w(S, W.seed, wave)) ? &S.src[0] : &S.src[2];
+        att = 0; b = 1; B = 0; h = 2166136261u;
+        if (WRITE) out = W.verts + W.offsets[q];
+        return true;
+    };
+    auto finish = [&](bool ok) {
+        if (!ok) { atomicExch(W.err, SSTMC_PATH_LIMIT); B = 0; }
+        if (!WRITE) { W.counts[q] = B; W.misses[q] = att; }
+        else if (W.hash) W.hash[q] = h;
+    };
+    if (!start(q)) return;
+    for (;;) {
+        Stream rs;
+        V3 o, d;
+        if (b == 1) {
+            rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
+            sample_source(S, *fsrc, rs, o, d);
+        } else {
             rs.init(W.seed, pid, b, kPurposeWalk);
             const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
-            const V3 nd = sample_direction(S, mcur, din, rs);
-            V3 xn;
-            int mn = 0;
-            if (!woodcock(S, cur, nd, rs, xn, mn)) { ok = false; break; }
-            if (mn == 0) break;
-            const float xin = corr ? 0.0f : rs.uniform();
-            if (WRITE) {
-                if (b - 1 >= W.counts[q]) { ok = false; break; }  // replay disagrees with the count pass
-                out[b - 1] = pack_vertex(xn, mn, xin);
-                h = hash_v(S, h, xn, mn);
-            }
-            B = b;
-            prev = cur;
-            cur = xn;
-            mcur = mn;
+            d = sample_direction(S, mcur, din, rs);
+            o = cur;
         }
-    }
-    if (!ok) {
-        atomicExch(W.err, SSTMC_PATH_LIMIT);
-        B = 0;
-    }
-    if (!WRITE) {
-        W.counts[q] = B;
-        W.misses[q] = att;
-    } else {
-        if (W.hash) W.hash[q] = h;
+        V3 xn;
+        int mn = 0;
+        bool ok = woodcock(S, o, d, rs, xn, mn);
+        bool done = !ok;
+        if (ok) {
+            if (b == 1) {
+                if (mn == 0) {
+                    if (++att >= kMaxAttempts) { ok = false; done = true; }
+                } else {
+                    const float xi = corr ? 0.0f : rs.uniform();
+                    if (WRITE) { out[0] = pack_vertex(xn, mn, xi); h = hash_v(S, h, xn, mn); }
+                    B = 1; prev = o; cur = xn; mcur = mn; b = 2;
+                }
+            } else if (mn == 0) {
+                done = true;
+            } else if (b > kMaxVertices || (WRITE && b - 1 >= W.counts[q])) {
+                ok = false; done = true;
+            } else {
+                const float xi = corr ? 0.0f : rs.uniform();
+                if (WRITE) { out[b - 1] = pack_vertex(xn, mn, xi); h = hash_v(S, h, xn, mn); }
+                B = b; prev = cur; cur = xn; mcur = mn; ++b;
+            }
+        }
+        if (done) {
+            finish(ok);
+            if (!start(q + nthreads)) return;
+        }
     }
 }
 
@@ -165,10 +174,21 @@ __global__ void scan_add_kernel(uint32_t* offsets, const uint32_t* block_sums, u
 
 }  // namespace
 
+static int walk_blocks(uint32_t paths)
+{
+    // about 8 paths per thread, at most 16 resident blocks of 128 threads per SM
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t want = (paths + 8 * 128 - 1) / (8 * 128);
+    const uint32_t cap = (uint32_t)sms * 16;
+    return (int)std::max<uint32_t>(1, std::min(want, cap));
+}
+
 int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
     const int threads = 128;
-    walk_kernel<false><<<(W.paths + threads - 1) / threads, threads, 0, stream>>>(S, W);
+    walk_kernel<false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
     if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
     const uint32_t nb = (W.paths + kScanBlock - 1) / kScanBlock;
     scan_block_kernel<<<nb, kScanBlock, 0, stream>>>(W.counts, W.offsets, W.block_sums, W.paths);
@@ -180,7 +200,7 @@ int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t strea
 int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
     const int threads = 128;
-    walk_kernel<true><<<(W.paths + threads - 1) / threads, threads, 0, stream>>>(S, W);
+    walk_kernel<true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
 }
 
