@@ -50,6 +50,7 @@ extern "C" {
 #define SSTMC_CANCELLED                102 /* a served request was cancelled */
 #define SSTMC_INVALID_HANDLE           103
 #define SSTMC_PATH_LIMIT               104 /* a path exceeded the vertex / retry limit */
+#define SSTMC_SCRATCH_LIMIT            105 /* sstmc_render_static: the request does not fit its static scratch */
 
 /* ------------------------------------------------------------------ */
 /* Enumerations mirroring the reference's string / enum values          */
@@ -164,6 +165,31 @@ int32_t sstmc_scene_shape(const sstmc_scene* scene, uint32_t* nl, uint32_t* nv, 
  * iter_out: renderings_num doubles (may be NULL).  seed overrides
  * cfg.seed for the first rendering. */
 int32_t sstmc_render(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
+
+/* sstmc_render without device memory allocation.  No counterpart in the
+ * reference: it is for callers that must not allocate device memory during a
+ * render -- a host that owns a fixed device-memory budget (a serving process
+ * whose admitted work must not fail later on an out-of-memory, or that must
+ * not stall other streams on the implicit device synchronisation of
+ * cudaFree), or a caller that has reserved all of the device for itself.
+ * Same arguments, result and statistics as sstmc_render (within the FP64
+ * accumulation-order tolerance); sstmc_last_timing is not updated.
+ *
+ * Every device buffer lives in one static scratch array of 64 MiB per device
+ * that is part of this library's device image: no cudaMalloc, cudaFree or
+ * allocating library routine is called.  The scratch holds the output
+ * (16 * Nl * Nv * Nt bytes), the far-field weight table (40 * Nl * Nv * Nt
+ * bytes when illumination and view are both far fields) and the per-path rows
+ * of one chunk of paths; a request whose output and tables leave no room for
+ * one path, or one of whose paths has more vertices than fit, returns
+ * SSTMC_SCRATCH_LIMIT (sstmc_last_error_text says what did not fit).
+ *
+ * The scratch is shared by every scene on a device: overlapping calls would
+ * race on it, so the library serialises sstmc_render_static calls per device
+ * (a call waits for any other one on that device to return).  The first call
+ * on a device looks up the scratch's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture. */
+int32_t sstmc_render_static(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
 
 /* Number of NEE path-contributions (sum over traced paths of vertices * Nl *
  * Nv * Nt) and of voxel DDA steps of the last sstmc_render call. */

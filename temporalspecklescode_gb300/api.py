@@ -48,6 +48,8 @@ def load_library() -> C.CDLL:
     lib.sstmc_scene_shape.restype = i32
     lib.sstmc_render.argtypes = [vp, u64, dp, dp]
     lib.sstmc_render.restype = i32
+    lib.sstmc_render_static.argtypes = [vp, u64, dp, dp]
+    lib.sstmc_render_static.restype = i32
     lib.sstmc_last_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
     lib.sstmc_last_stats.restype = i32
     lib.sstmc_last_timing.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(u64)]
@@ -93,13 +95,23 @@ class Scene:
         self.renders = self.meta["R"]
 
     def render(self, seed: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray]:
+        return self._render(self.lib.sstmc_render, seed)
+
+    def render_static(self, seed: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray]:
+        """``render`` with no device memory allocation: every device buffer is in
+        the library's 64 MiB per-device static scratch (sstmc_render_static)."""
+        return self._render(self.lib.sstmc_render_static, seed)
+
+    def _render(self, fn, seed: Optional[int]) -> Tuple[np.ndarray, np.ndarray]:
         seed = self.prepared.struct.seed if seed is None else int(seed)
         n = self.Nl * self.Nv * self.Nt
         u = np.zeros(2 * n * self.renders, dtype=np.float64)
         it = np.zeros(self.renders, dtype=np.float64)
-        code = self.lib.sstmc_render(self.handle, C.c_uint64(seed), u.ctypes.data_as(C.POINTER(C.c_double)),
-                                     it.ctypes.data_as(C.POINTER(C.c_double)))
-        _check(code)
+        code = fn(self.handle, C.c_uint64(seed), u.ctypes.data_as(C.POINTER(C.c_double)),
+                  it.ctypes.data_as(C.POINTER(C.c_double)))
+        if code != 0:
+            detail = self.lib.sstmc_last_error_text().decode()
+            raise SstmcError(code, error_string(code) + (f": {detail}" if detail else ""))
         uc = (u[0::2] + 1j * u[1::2]).reshape(self.renders, self.Nt, self.Nv, self.Nl)
         return np.transpose(uc, (3, 2, 1, 0)), it
 

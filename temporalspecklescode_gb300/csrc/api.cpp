@@ -172,6 +172,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     if (cudaMemcpyAsync(&nverts, vtotal, sizeof(nverts), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
     if (nverts > verts_cap) {
+        if (fixed) return SSTMC_SCRATCH_LIMIT;
         if (verts) cudaFree(verts);
         verts = nullptr;
         const size_t cap = (size_t)(nverts * 5 / 4) + 1024;
@@ -398,6 +399,14 @@ int32_t sstmc_render(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_
         if (e) return e;
     }
     return SSTMC_NO_ERROR;
+}
+
+int32_t sstmc_render_static(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (cudaSetDevice(s->scene.device) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    return render_static(s->scene, s->engine.stream, seed, u_out, iter_out);
 }
 
 int32_t sstmc_last_stats(const sstmc_scene* s, uint64_t* contributions, uint64_t* dda_steps, uint64_t* vertices, uint64_t* paths)

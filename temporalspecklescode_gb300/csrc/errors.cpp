@@ -38,6 +38,7 @@ extern "C" const char* sstmc_error_string(int32_t code)
     case SSTMC_CANCELLED: return "The request was cancelled.";
     case SSTMC_INVALID_HANDLE: return "Invalid handle.";
     case SSTMC_PATH_LIMIT: return "A path exceeded the vertex or first-vertex retry limit.";
+    case SSTMC_SCRATCH_LIMIT: return "The request does not fit the 64 MiB static scratch of sstmc_render_static; use sstmc_render.";
     default: return "Unknown error code.";
     }
 }

@@ -13,6 +13,7 @@
 namespace sstmc {
 
 constexpr int kMaxSlots = 32;  // view-accumulator slots per lane (8 KB of shared memory per warp)
+constexpr size_t kStaticScratchBytes = (size_t)64 << 20;  // per device, sstmc_render_static (static_render.cu)
 
 struct PathDebug {
     uint32_t* hash = nullptr;
@@ -40,6 +41,7 @@ struct Engine {
     double ms_trace = 0, ms_gemm = 0, ms_ss = 0, ms_total = 0;
     uint64_t launches = 0;
     bool timing = true;
+    bool fixed = false;   // buffers carved from a fixed scratch: a chunk that outgrows them fails, nothing is allocated
 
     static size_t bytes_per_path(const Scene& S);
     int ensure(Scene& S, uint32_t paths);
@@ -53,6 +55,9 @@ struct Engine {
     int init_events();
     void destroy_events();
 };
+
+// sstmc_render with every device buffer in a static scratch (static_render.cu).
+int render_static(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, double* iter_out);
 
 int occupancy_blocks(const DevScene& S, int threads, size_t smem);
 void set_last_error_text(const std::string& s);

@@ -1,0 +1,74 @@
+"""sstmc_render_static (every device buffer in the library's static scratch)
+against sstmc_render on the same scenes and seeds.
+
+Two static renders in a row must each agree with sstmc_render: the same
+iteration counts and integer statistics, and the field / correlation within
+the relative Frobenius tolerance below (the two entry points differ only in
+the order of the FP64 accumulation, so the true difference is ~1e-15).
+A request whose output does not fit the scratch is refused with
+SSTMC_SCRATCH_LIMIT, and the scratch is usable again afterwards.
+
+This file is collected last, so it also runs after every other test has used
+the library in the same process.
+"""
+import numpy as np
+import pytest
+
+from temporalspecklescode_gb300 import workloads as wl
+from tests.scenes import small_scenes
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-5
+SCRATCH_LIMIT = 105
+SCENES = small_scenes()
+# 4096 paths of 64 x 64 x 8 rows: several chunks of the 64 MiB scratch
+SCENES["correlation_3d_chunked"] = wl.correlation_3d(batch_size=2048, full_iteration=2, n_side=8, n_lags=8)
+
+
+def rel_fro(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def api():
+    from temporalspecklescode_gb300 import api as A
+    A.load_library()
+    return A
+
+
+@pytest.mark.parametrize("name", sorted(SCENES))
+def test_static_matches_render_twice(name, api):
+    cfg, dims = SCENES[name]
+    with api.Scene(cfg, dims) as s:
+        u_ref, it_ref = s.render(seed=31)
+        st_ref = s.stats()
+        for _ in range(2):
+            u, it = s.render_static(seed=31)
+            st = s.stats()
+            assert np.array_equal(it, it_ref), (name, it, it_ref)
+            assert st == st_ref, (name, st, st_ref)
+            err = rel_fro(u, u_ref)
+            assert err <= REL_TOL, (name, err)
+
+
+def test_static_refuses_output_larger_than_scratch(api):
+    # 512 x 512 far-field pairs x 16 ticks: 64 MiB of FP64 output alone
+    d = wl._farfield_fan(512)
+    cfg, dims = wl.speckle_2d(batch_size=32, full_iteration=1)
+    cfg["illumination"] = {"type": "FarField", "direction": d}
+    cfg["view"] = {"type": "FarField", "direction": d}
+    cfg["sampler"] = {"type": "TemporalSampler", "t": list(np.arange(16.0)), "D": [0.0, 0.0],
+                      "U": {"x": [0.0, 0.0], "y": [0.0, 0.0]}}
+    with api.Scene(cfg, dims) as s:
+        with pytest.raises(api.SstmcError) as ex:
+            s.render_static(seed=1)
+        assert ex.value.code == SCRATCH_LIMIT
+        assert "static scratch" in str(ex.value)
+    cfg, dims = SCENES["speckle_2d"]
+    with api.Scene(cfg, dims) as s:
+        u_ref, it_ref = s.render(seed=5)
+        u, it = s.render_static(seed=5)
+    assert np.array_equal(it, it_ref)
+    assert rel_fro(u, u_ref) <= REL_TOL
