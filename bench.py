@@ -198,6 +198,49 @@ def run_reference(args, dist, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes per path of the NEE kernel from one ncu capture of this workload
+# (dram__bytes_read.sum + dram__bytes_write.sum over 2^16 paths); the traffic
+# is per-path rows, so a launch's traffic scales with the paths it processes.
+NCU_NEE_DRAM_BYTES_PER_PATH = 1052254592 / 65536
+
+
+def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
+    """Per kernel class: time per step, algorithmic bytes or flops per launch,
+    achieved rate and the fraction of the measured peak."""
+    m = scene.meta
+    P = m["P"] * m["waves"]
+    Nl, Nv, Nt = m["Nl"], m["Nv"], m["Nt"]
+    g2 = 8.0 * Nt * Nl if (m.get("correlation") and not m.get("sym", True)) else 0.0
+    hbm, tc = peaks["hbm_gbs"], peaks["bf16_tflops"]
+    out = {}
+
+    def add(key, name, ms, bound, amount, traffic=None):
+        per_launch = amount / chunks
+        if bound == "hbm":
+            ach = amount / (ms / 1000) / 1e9
+            out[key] = {"kernel": name, "ms": ms, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                        "frac": ach / hbm, "peak_name": "hbm_gbs", "algorithmic_per_launch": per_launch,
+                        "traffic": traffic}
+        else:
+            ach = amount / (ms / 1000) / 1e12
+            out[key] = {"kernel": name, "ms": ms, "bound": "tensor", "achieved": ach, "peak": tc, "unit": "TFLOP/s",
+                        "frac": ach / tc, "peak_name": "bf16_tflops", "algorithmic_per_launch": per_launch,
+                        "traffic": traffic}
+
+    # NEE vectors: rows written + vertices, counts and offsets read
+    nee_bytes = P * (8.0 * Nt * (2 * Nl + 2 * Nv) + g2 + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
+    add("nee", "trace_kernel (NEE vectors)", mean["ms_nee"], "hbm", nee_bytes,
+        traffic=NCU_NEE_DRAM_BYTES_PER_PATH * P / chunks if WORKLOAD == "correlation_3d" else None)
+    # random walk: two passes over the same streams; vertices written once, counts / misses / offsets
+    add("walk", "walk_kernel (random walk, count + write)", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P)
+    # multiple-scattering contraction: 8 useful flops per complex multiply-add
+    add("gemm", "gemm_tc_kernel (multiple-scattering contraction, 3xTF32)", mean["ms_contract_ms"], "tensor",
+        8.0 * Nl * Nv * Nt * P)
+    # single-scattering contraction: tick-0 rows read (tick-invariant form)
+    add("ss", "ss_fast_kernel (single-scattering contraction)", mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv))
+    return out
+
+
 def run_gpu(args, dist, rank, ws):
     import numpy as np
     from temporalspecklescode_gb300 import api, config as cf
@@ -207,7 +250,9 @@ def run_gpu(args, dist, rank, ws):
     scene = api.Scene(cfg, dims, precision)
     lat = []
     dev_ms = []
-    parts = {"ms_trace": [], "ms_contract_ms": [], "ms_contract_ss": []}
+    parts = {"ms_trace": [], "ms_contract_ms": [], "ms_contract_ss": [], "ms_walk": [], "ms_nee": []}
+    chunks = 1
+    verts = 0
     contrib = 0
     launches = 0
     for i in range(args.warmup):
@@ -225,7 +270,10 @@ def run_gpu(args, dist, rank, ws):
         for k in parts:
             parts[k].append(tm[k])
         launches += tm["launches"]
-        contrib += scene.stats()["contributions"]
+        chunks = tm["chunks"]
+        st = scene.stats()
+        contrib += st["contributions"]
+        verts += st["vertices"]
     wall = time.perf_counter() - t0
     _barrier(dist)
     clk = clocks.stop()
@@ -250,29 +298,16 @@ def run_gpu(args, dist, rank, ws):
     e2e_value = _sum_over_ranks(dist, float(contrib / args.steps)) / e2e_s
 
     peaks, pk_kind = _peaks()
-    # dominant kernel class and its roofline
-    mean = {k: statistics.mean(v) for k, v in parts.items()}
-    dom = max(mean, key=mean.get)
     m = scene.meta
     P = m["P"] * m["waves"]
     Nl, Nv, Nt = m["Nl"], m["Nv"], m["Nt"]
-    if dom == "ms_contract_ms":
-        flops = 8.0 * Nl * Nv * Nt * P
-        achieved = flops / (mean[dom] / 1000) / 1e12
-        roof = {"kernel": "gemm (multiple-scattering contraction)", "bound": "tensor", "achieved": achieved,
-                "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-                "peak_source": pk_kind}
-    else:
-        # algorithmic HBM bytes: the per-path rows the kernel class writes / reads
-        if dom == "ms_trace":
-            nbytes = P * (8.0 * Nt * (2 * Nl + 2 * Nv + Nl) + 4 * Nl * 2 + 16)
-            name = "trace_kernel (fused path tracing)"
-        else:
-            nbytes = P * (8.0 * Nt * (Nl + Nv) + 16)
-            name = "ss_kernel (single-scattering contraction)"
-        achieved = nbytes / (mean[dom] / 1000) / 1e9
-        roof = {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": pk_kind}
+    mean = {k: statistics.mean(v) for k, v in parts.items()}
+    kernels = _kernel_rooflines(scene, mean, verts / args.steps, chunks, peaks)
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    d = kernels[dom]
+    roof = {"kernel": d["kernel"], "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"], "unit": d["unit"],
+            "frac": d["frac"], "traffic": d["traffic"], "peak_source": pk_kind + " (" + d["peak_name"] + ")",
+            "algorithmic_per_launch": d["algorithmic_per_launch"], "launches_per_step": chunks}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -285,7 +320,7 @@ def run_gpu(args, dist, rank, ws):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": statistics.mean(dev_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64 (split: FP64 phase, compensated FP32 contraction)" if precision == 0 else "f32",
+        "dtype": "f32+f64 (split: FP64 path length and phase, 3xTF32 tensor-core contraction)" if precision == 0 else "f32",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "paths_per_step": P, "Nl": Nl, "Nv": Nv, "Nt": Nt, "dims": dims,
                    "precision": args.precision, "parallelism": f"replicas{ws}",
@@ -296,6 +331,7 @@ def run_gpu(args, dist, rank, ws):
                 "ms_per_step": 1000 * e2e_s},
         "gpu_launches": int(launches),
         "roofline": roof,
+        "kernels": {k: {kk: vv for kk, vv in v.items() if kk not in ("peak_name",)} for k, v in kernels.items()},
         "cpu_baseline": cpu,
         "clocks": clk,
         "wall_s": wall,

@@ -197,10 +197,13 @@ int32_t sstmc_last_stats(const sstmc_scene* scene, uint64_t* contributions,
                          uint64_t* dda_steps, uint64_t* vertices, uint64_t* paths);
 
 /* Device time of the last sstmc_render in milliseconds, measured with CUDA
- * events on the scene's stream: ms[0] whole render, ms[1] path tracing,
- * ms[2] multiple-scattering contraction, ms[3] single-scattering
- * contraction; launches = kernels launched.  No reference counterpart (the
- * reference's TIME_REC std::clock buckets, NextEventEstimation.cuh:107-156). */
+ * events on the scene's stream: ms[0] whole render, ms[1] path tracing
+ * (ms[4] + ms[5]), ms[2] multiple-scattering contraction, ms[3]
+ * single-scattering contraction, ms[4] random walk (count, scan, write),
+ * ms[5] NEE vectors; launches[0] = kernels launched, launches[1] = chunks
+ * of paths.  ms: 6 doubles, launches: 2 integers.  No reference counterpart
+ * (the reference's TIME_REC std::clock buckets,
+ * NextEventEstimation.cuh:107-156). */
 int32_t sstmc_last_timing(const sstmc_scene* scene, double* ms, uint64_t* launches);
 
 int32_t sstmc_scene_destroy(sstmc_scene* scene);

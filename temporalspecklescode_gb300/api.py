@@ -121,10 +121,11 @@ class Scene:
         return {"contributions": v[0].value, "dda_steps": v[1].value, "vertices": v[2].value, "paths": v[3].value}
 
     def timing(self) -> Dict[str, float]:
-        ms = (C.c_double * 4)()
-        n = C.c_uint64()
-        _check(self.lib.sstmc_last_timing(self.handle, ms, C.byref(n)))
-        return {"ms_total": ms[0], "ms_trace": ms[1], "ms_contract_ms": ms[2], "ms_contract_ss": ms[3], "launches": n.value}
+        ms = (C.c_double * 6)()
+        n = (C.c_uint64 * 2)()
+        _check(self.lib.sstmc_last_timing(self.handle, ms, n))
+        return {"ms_total": ms[0], "ms_trace": ms[1], "ms_contract_ms": ms[2], "ms_contract_ss": ms[3],
+                "ms_walk": ms[4], "ms_nee": ms[5], "launches": n[0], "chunks": n[1]}
 
     def trace_paths(self, seed: int, first_path: int, paths: int) -> Dict[str, np.ndarray]:
         """Per-path quantities of paths [first_path, first_path + paths) (parity tests)."""

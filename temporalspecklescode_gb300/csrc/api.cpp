@@ -45,6 +45,14 @@ size_t budget_bytes()
     return std::min<size_t>((size_t)16 << 30, std::max<size_t>((size_t)256 << 20, fr / 4));
 }
 
+// The split-precision contraction runs on the tensor cores (gemm_tc.cu);
+// SSTMC_CONTRACTION=simt selects the SIMT form (gemm_kernel) instead.
+bool use_tensor_cores()
+{
+    const char* e = std::getenv("SSTMC_CONTRACTION");
+    return !(e && std::strcmp(e, "simt") == 0);
+}
+
 }  // namespace
 
 size_t Engine::bytes_per_path(const Scene& S)
@@ -183,6 +191,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     e = launch_walk_write(S.dev, Wp, stream);
     if (e) return e;
     launches++;
+    if (timing && ev[6]) cudaEventRecord(ev[6], stream);
 
     // 2. NEE vectors per path (trace.cu)
     TraceParams T;
@@ -230,7 +239,10 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     kchunk = ((kchunk + 255) / 256) * 256;
     G.kchunk = kchunk;
     G.A = a_ms; G.B = s_ms;
-    int e = launch_gemm(G, stream);
+    G.err = err;
+    const bool tc = use_tensor_cores() && gemm_tc_eligible(G);
+    auto gemm = [&](const GemmParams& P) { return tc ? launch_gemm_tc(P, stream) : launch_gemm(P, stream); };
+    int e = gemm(G);
     if (e) return e;
     launches++;
     if (timing) cudaEventRecord(ev[3], stream);
@@ -243,7 +255,7 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
         for (int m : S.materials_present) {
             G.mat_sel = m;
             G.W = W + (size_t)m * per;
-            e = launch_gemm(G, stream);
+            e = gemm(G);
             if (e) return e;
             launches++;
         }
@@ -278,8 +290,9 @@ int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out)
     if (cudaMemsetAsync(V, 0, nout * sizeof(double2), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     if (cudaMemsetAsync(totals, 0, 8 * sizeof(unsigned long long), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     if (cudaMemsetAsync(err, 0, sizeof(int), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
-    std::vector<float> t_trace, t_gemm, t_ss;
+    std::vector<float> t_trace, t_gemm, t_ss, t_walk;
     float t_all = 0.f;
+    chunks = 0;
     if (timing) cudaEventRecord(ev[0], stream);
     for (uint64_t first = 0; first < total; first += chunk) {
         const uint32_t n = (uint32_t)std::min<uint64_t>(chunk, total - first);
@@ -289,22 +302,26 @@ int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out)
         if (timing) cudaEventRecord(ev[2], stream);
         e = contract_chunk(S, n);
         if (e) return e;
+        chunks++;
         if (timing) {
             cudaEventRecord(ev[4], stream);
             cudaEventSynchronize(ev[4]);
-            float a = 0, b = 0, c = 0;
+            float a = 0, b = 0, c = 0, w = 0;
             cudaEventElapsedTime(&a, ev[1], ev[2]);
             cudaEventElapsedTime(&b, ev[2], ev[3]);
             cudaEventElapsedTime(&c, ev[3], ev[4]);
-            t_trace.push_back(a); t_gemm.push_back(b); t_ss.push_back(c);
+            cudaEventElapsedTime(&w, ev[1], ev[6]);
+            t_trace.push_back(a); t_gemm.push_back(b); t_ss.push_back(c); t_walk.push_back(w);
         }
     }
     if (timing) {
         cudaEventRecord(ev[5], stream);
         cudaEventSynchronize(ev[5]);
         cudaEventElapsedTime(&t_all, ev[0], ev[5]);
-        ms_trace = ms_gemm = ms_ss = 0;
-        for (size_t i = 0; i < t_trace.size(); ++i) { ms_trace += t_trace[i]; ms_gemm += t_gemm[i]; ms_ss += t_ss[i]; }
+        ms_trace = ms_gemm = ms_ss = ms_walk = 0;
+        for (size_t i = 0; i < t_trace.size(); ++i) {
+            ms_trace += t_trace[i]; ms_gemm += t_gemm[i]; ms_ss += t_ss[i]; ms_walk += t_walk[i];
+        }
         ms_total = t_all;
     }
     unsigned long long tot[8];
@@ -425,8 +442,9 @@ int32_t sstmc_last_timing(const sstmc_scene* s, double* ms, uint64_t* launches)
     if (ms) {
         ms[0] = s->engine.ms_total; ms[1] = s->engine.ms_trace;
         ms[2] = s->engine.ms_gemm; ms[3] = s->engine.ms_ss;
+        ms[4] = s->engine.ms_walk; ms[5] = s->engine.ms_trace - s->engine.ms_walk;
     }
-    if (launches) *launches = s->engine.launches;
+    if (launches) { launches[0] = s->engine.launches; launches[1] = s->engine.chunks; }
     return SSTMC_NO_ERROR;
 }
 

@@ -18,6 +18,7 @@ struct GemmParams {
     double2* V;
     int kchunk;
     int compensated;
+    int* err;             // tensor-core form: SSTMC_TIMEOUT if a bounded wait ran out
 };
 
 // V[t][v][l] += sum_p a[p][t][l] * b[p][t][v] * W(l, v, t, p), W from the
@@ -35,6 +36,9 @@ struct SsParams {
 };
 
 int launch_gemm(const GemmParams& G, cudaStream_t stream);
+// tcgen05 3xTF32 form of launch_gemm (gemm_tc.cu); chooses its own K split.
+bool gemm_tc_eligible(const GemmParams& G);
+int launch_gemm_tc(const GemmParams& G, cudaStream_t stream);
 int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream);
 
 }  // namespace sstmc

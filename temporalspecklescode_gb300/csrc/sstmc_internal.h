@@ -38,8 +38,8 @@ struct Engine {
     float* W = nullptr;
     // device timing of the last render: events around each kernel class
     cudaEvent_t ev[8] = { nullptr };
-    double ms_trace = 0, ms_gemm = 0, ms_ss = 0, ms_total = 0;
-    uint64_t launches = 0;
+    double ms_trace = 0, ms_gemm = 0, ms_ss = 0, ms_total = 0, ms_walk = 0;
+    uint64_t launches = 0, chunks = 0;
     bool timing = true;
     bool fixed = false;   // buffers carved from a fixed scratch: a chunk that outgrows them fails, nothing is allocated
 

@@ -101,3 +101,35 @@ def test_chunking_is_invisible(api, oracle, monkeypatch):
     uo, ito, _ = oracle.render(pc, 9)
     assert it[0] == ito
     assert rel_fro(u[..., 0], uo) <= REL_TOL
+
+
+@pytest.mark.parametrize("name", ["correlation_64x64", "speckle_2d", "transmission_matrix_3d", "corr_far_2d_drift"])
+def test_tensor_core_contraction_matches_simt(name, api, monkeypatch):
+    """The tcgen05 3xTF32 contraction (default) against the compensated SIMT
+    contraction on the same rows.  Both carry FP32-level rounding (~1e-7 per
+    product, amplified by the cancellation of the random-phase sum), so they
+    agree within 2e-6, inside the 1e-5 budget against the FP64 oracle."""
+    from temporalspecklescode_gb300 import workloads as wl
+    if name == "correlation_64x64":
+        cfg, dims = wl.correlation_3d(batch_size=4096, full_iteration=2, n_side=8, n_lags=8)
+    else:
+        cfg, dims = SCENES[name]
+    with api.Scene(cfg, dims) as s:
+        u_tc, it_tc = s.render(seed=21)
+        monkeypatch.setenv("SSTMC_CONTRACTION", "simt")
+        u_simt, it_simt = s.render(seed=21)
+    assert np.array_equal(it_tc, it_simt)
+    err = rel_fro(u_tc, u_simt)
+    assert err <= 2e-6, (name, err)
+
+
+def test_tensor_core_contraction_large_k_against_oracle(api, oracle):
+    """64 x 64 x 8 correlation over 16384 paths (K per CTA in the thousands,
+    many 128-path accumulation windows) against the FP64 oracle."""
+    from temporalspecklescode_gb300 import workloads as wl
+    cfg, dims = wl.correlation_3d(batch_size=8192, full_iteration=2, n_side=8, n_lags=8)
+    with api.Scene(cfg, dims) as s:
+        u, it = s.render(seed=4)
+    uo, ito, _ = oracle.render(cf.prepare(cfg, dims), 4)
+    assert it[0] == ito
+    assert rel_fro(u[..., 0], uo) <= REL_TOL
