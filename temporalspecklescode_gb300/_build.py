@@ -65,7 +65,7 @@ def build_library(verbose: bool = False, force: bool = False) -> str:
         objs = list(ex.map(compile_one, srcs))
     out = lib_path()
     if force or not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc, "-shared", "-o", out] + objs + ARCH + ["-lcuda"]
+        cmd = [nvcc, "-shared", "-o", out] + objs + ARCH
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

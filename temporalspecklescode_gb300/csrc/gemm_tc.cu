@@ -28,6 +28,7 @@
 // the error word, and every role then leaves its loop, waits for the MMAs it
 // issued and frees the tensor memory.
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -478,15 +479,32 @@ bool gemm_tc_eligible(const GemmParams& G)
         && reinterpret_cast<uintptr_t>(G.A) % 16 == 0 && reinterpret_cast<uintptr_t>(G.B) % 16 == 0;
 }
 
+// cuTensorMapEncodeTiled, resolved through the runtime so the library does
+// not link the driver library itself (it still loads on a host without one).
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess
+            || q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
 // [K paths][Nt ticks][rows floats] as a 3D tensor (rows fastest), box
 // box_rows x 1 x kKS; boxes past the tensor's edge are filled with zeros.
 static bool encode_rows(CUtensorMap* tm, const void* base, int rows, int Nt, int K, int box_rows)
 {
+    const PFN_cuTensorMapEncodeTiled_v12000 encode = encode_fn();
+    if (!encode) return false;
     cuuint64_t dims[3] = { (cuuint64_t)rows, (cuuint64_t)Nt, (cuuint64_t)K };
     cuuint64_t strides[2] = { (cuuint64_t)rows * 4u, (cuuint64_t)rows * 4u * (cuuint64_t)Nt };
     cuuint32_t box[3] = { (cuuint32_t)box_rows, 1u, (cuuint32_t)kKS };
     cuuint32_t estr[3] = { 1u, 1u, 1u };
-    return cuTensorMapEncodeTiled(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, estr,
+    return encode(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, estr,
                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
