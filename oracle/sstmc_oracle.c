@@ -390,7 +390,9 @@ static inline int o_cell(const o_scene* S, const float p[3])
 }
 
 /* Does a ray from an outside point hit the box?  HeterogeneousMedium.cuh:269-383 (bdDistance). */
-static int o_points_toward(const o_scene* S, const float p[3], const float d[3])
+/* Whether the ray from p along d hits the box; *hit = distance to the face it
+ * enters first (HeterogeneousMedium.cuh:269-383, bdDistance). */
+static int o_points_toward(const o_scene* S, const float p[3], const float d[3], float* hit)
 {
     int D = S->dims;
     float o[3], inv[3], dist[3];
@@ -413,7 +415,7 @@ static int o_points_toward(const o_scene* S, const float p[3], const float d[3])
             if (j == i) continue;
             if (!(fabsf(fmaf(d[j], dist[i], o[j])) < S->radius[j])) ok = 0;
         }
-        if (ok) return 1;
+        if (ok) { if (hit) *hit = dist[i]; return 1; }
     }
     return 0;
 }
@@ -504,7 +506,12 @@ static int o_woodcock(const o_scene* S, const float o[3], const float d[3], o_st
         dist = dist + (-o_logf(u)) * S->inv_maxsigt_f;
         for (int i = 0; i < S->dims; ++i) p[i] = fmaf(dist, d[i], o[i]);
         if (!o_inside(S, p)) {
-            if (!o_points_toward(S, p, d)) break;
+            /* still outside on a ray that enters the box: move on to the entry
+             * face (flight lengths are memoryless, so the first point inside
+             * keeps its distribution) */
+            float te = 0.0f;
+            if (!o_points_toward(S, p, d, &te)) break;
+            dist = dist + te;
         } else {
             m = S->grid[o_cell(S, p)];
             if (o_uniform(rs) <= S->accept_f[m]) break;

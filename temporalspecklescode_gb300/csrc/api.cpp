@@ -23,6 +23,7 @@
 #include "scene.h"
 #include "sstmc_internal.h"
 #include "trace.h"
+#include "viewsum.h"
 
 namespace sstmc {
 
@@ -43,6 +44,14 @@ size_t budget_bytes()
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return (size_t)2 << 30;
     return std::min<size_t>((size_t)16 << 30, std::max<size_t>((size_t)256 << 20, fr / 4));
+}
+
+// The view vectors of the common cases come from the view-side kernel
+// (viewsum.cu); SSTMC_VIEW_KERNEL=fused keeps them in the fused trace kernel.
+bool use_view_kernel()
+{
+    const char* e = std::getenv("SSTMC_VIEW_KERNEL");
+    return !(e && std::strcmp(e, "fused") == 0);
 }
 
 // The split-precision contraction runs on the tensor cores (gemm_tc.cu);
@@ -80,7 +89,7 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&counts, paths * sizeof(uint32_t)) && alloc((void**)&misses, paths * sizeof(uint32_t))
            && alloc((void**)&offsets, paths * sizeof(uint32_t))
            && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
-           && alloc((void**)&vtotal, sizeof(unsigned long long));
+           && alloc((void**)&vtotal, 2 * sizeof(unsigned long long));   // total + the walk's two path counters
     if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
     cap = paths;
     return SSTMC_NO_ERROR;
@@ -172,6 +181,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     std::memset(&Wp, 0, sizeof(Wp));
     Wp.seed = seed; Wp.first_path = first; Wp.paths = n;
     Wp.counts = counts; Wp.misses = misses; Wp.offsets = offsets; Wp.block_sums = block_sums; Wp.total = vtotal;
+    Wp.next = reinterpret_cast<uint32_t*>(vtotal + 1);
     Wp.err = err; Wp.hash = dbg ? dbg->hash : nullptr;
     int e = launch_walk_count(S.dev, Wp, stream);
     if (e) return e;
@@ -210,6 +220,27 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     const size_t smem = trace_smem_bytes(S.Nt, T.slots, threads);
     const int per_sm = occupancy_blocks(S.dev, threads, smem);
     const int blocks = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_sm)));
+    bool moving_any = false;
+    for (int m : S.materials_present) moving_any = moving_any || S.dev.moving[m] != 0;
+    if (use_view_kernel() && view_kernel_covers(S.dev, &moving_any)) {
+        // illumination side in the fused kernel, view side in viewsum.cu
+        T.pass0 = 1; T.views = 0;
+        T.v0 = 0; T.vn = S.Nv; T.t0 = 0; T.tn = S.Nt;
+        e = launch_trace(S.dev, T, blocks, threads, stream);
+        if (e) return e;
+        launches++;
+        const int vmax = view_max_views(), tmax = view_max_ticks(S.dev);
+        const int vblocks = std::max(1, std::min((int)((n + 3) / 4), sms * 8));
+        for (int v = 0; v < S.Nv; v += vmax)
+            for (int t = 0; t < S.Nt; t += tmax) {
+                T.v0 = v; T.vn = std::min(vmax, S.Nv - v); T.t0 = t; T.tn = std::min(tmax, S.Nt - t);
+                e = launch_view(S.dev, T, vblocks, threads, stream);
+                if (e) return e;
+                launches++;
+            }
+        return SSTMC_NO_ERROR;
+    }
+    T.views = 1;
     bool first_pass = true;
     for (auto& vc : vch) {
         for (auto& tc : tch) {

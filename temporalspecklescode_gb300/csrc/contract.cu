@@ -18,6 +18,8 @@
 //     V[t][v][l] += sum_p a[p][t][l] * b[p][t][v] * W(l, v, t, p).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "contract.h"
 #include "nee.cuh"
 
@@ -249,13 +251,19 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
 
 // Single-scattering term of the correlation sampler when the u1 and u2
 // sources are identical and every scatterer is static (U = 0): the rows are
-// real (|g|^2) and Fs1 Fs2 TS = pdf(cos) exp(-k^2 D |tau| |in - out|^2)
+// real (|g|^2) and Fs1 Fs2 TS = pdf(in, out) exp(-k^2 D |tau| |in - out|^2)
 // (SourceInterface.cuh:221-270 with q = in - out).  Each thread owns a 2 x 2
-// (illumination, view) block and all ticks of a chunk.
+// (illumination, view) block and all ticks of a chunk.  Per path the block
+// stages one float4 per illumination element (direction into the scatterer,
+// row value), one per view element (direction out, row value) and one per
+// path with the material constants, so the inner loop is branch-free:
+//   pdf = gup (omg2 + g q^2)^(-(D-1)/2)    (isotropic: g = 0, omg2 = 1)
+//   e_t = exp2(-c q^2 |tau_t|), c = k^2 D log2(e)
+// The scalar single-scattering amplitude of point x point isotropic scenes
+// (no temporal factor, NextEventEstimation.cuh:1024-1032) is g = 0, c = 0.
 constexpr int kFl = 32, kFv = 32, kFk = 16, kFt = 8;
 
-constexpr size_t kFastSmem = sizeof(float) * (2 * kFk * kFl + 6 * kFk * kFl) + sizeof(int) * kFk
-                           + sizeof(double) * 4 * kFt * 256;
+constexpr size_t kFastSmem = sizeof(float4) * (kFk * kFl + kFk * kFv + kFk) + sizeof(double) * 4 * kFt * 256;
 
 // Rows here are tick-invariant (static scatterers, identical u1 / u2
 // sources), so only the first tick's rows are read; the tick dependence is
@@ -264,11 +272,9 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double* accd = reinterpret_cast<double*>(smem_raw);                       // [4*kFt][256] FP64 window sums
-    float* as = reinterpret_cast<float*>(accd + 4 * kFt * 256);              // [kFk][kFl]
-    float* bs = as + kFk * kFl;                                               // [kFk][kFv]
-    float* inx = bs + kFk * kFv;                                              // [kFk][3][kFl]
-    float* outx = inx + kFk * 3 * kFl;                                        // [kFk][3][kFv]
-    int* m1s = reinterpret_cast<int*>(outx + kFk * 3 * kFv);
+    float4* sI = reinterpret_cast<float4*>(accd + 4 * kFt * 256);            // [kFk][kFl]
+    float4* sO = sI + kFk * kFl;                                              // [kFk][kFv]
+    float4* sM = sO + kFk * kFv;                                              // [kFk]
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int l0 = blockIdx.x * kFl, v0 = blockIdx.y * kFv;
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
@@ -280,6 +286,7 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     const DevSource& il = S.src[0];
     const DevSource& vw = S.src[1];
     const bool geo = S.ticks_geometric != 0;
+    const bool three = S.dims == 3;
     const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
     const float tau0 = S.abs_ticks[0], taus = S.abs_ticks[t0];
     float acc[2][2][kFt];
@@ -291,65 +298,68 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             for (int t = 0; t < kFt; ++t) { acc[i][j][t] = 0.f; accd[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = 0.0; }
     int chunk = 0;
     for (int k = kb; k < ke; k += kFk, ++chunk) {
-        for (int idx = threadIdx.x; idx < kFk * kFl; idx += 256) {
-            const int pp = idx / kFl, c = idx % kFl;
+        for (int idx = threadIdx.x; idx < kFk * (kFl + kFv); idx += 256) {
+            const bool isI = idx < kFk * kFl;
+            const int r = isI ? idx : idx - kFk * kFl;
+            const int pp = r / kFl, c = r % kFl;
             const int p = k + pp;
-            float a = 0.f, b = 0.f;
-            if (p < ke) {
-                if (l0 + c < Nl) a = G.a[(size_t)p * Nt * Nl + l0 + c].x;
-                if (v0 + c < Nv) b = G.b[(size_t)p * Nt * Nv + v0 + c].x;
-            }
-            as[idx] = a;
-            bs[idx] = b;
             const int pc = min(p, ke - 1);
             const V3 x = V3{ G.x1[3 * pc], G.x1[3 * pc + 1], G.x1[3 * pc + 2] };
-            const V3 i1 = fsrc_in(il, min(l0 + c, Nl - 1), x);
-            const V3 o1 = fsrc_out(vw, min(v0 + c, Nv - 1), x);
-            inx[(pp * 3 + 0) * kFl + c] = i1.x; inx[(pp * 3 + 1) * kFl + c] = i1.y; inx[(pp * 3 + 2) * kFl + c] = i1.z;
-            outx[(pp * 3 + 0) * kFv + c] = o1.x; outx[(pp * 3 + 1) * kFv + c] = o1.y; outx[(pp * 3 + 2) * kFv + c] = o1.z;
-            if (c == 0) m1s[pp] = p < ke ? (int)G.m1[p] : 0;
+            float val = 0.f;
+            V3 dir;
+            if (isI) {
+                if (p < ke && l0 + c < Nl) val = G.a[(size_t)p * Nt * Nl + l0 + c].x;
+                dir = fsrc_in(il, min(l0 + c, Nl - 1), x);
+                sI[r] = make_float4(dir.x, dir.y, dir.z, val);
+            } else {
+                if (p < ke && v0 + c < Nv) val = G.b[(size_t)p * Nt * Nv + v0 + c].x;
+                dir = fsrc_out(vw, min(v0 + c, Nv - 1), x);
+                sO[r] = make_float4(dir.x, dir.y, dir.z, val);
+            }
+        }
+        if (threadIdx.x < kFk) {
+            const int p = k + threadIdx.x;
+            const int m = p < ke ? (int)G.m1[p] : 0;
+            const int ty_ = S.scat_type[m];
+            float g = 0.f, omg2 = 1.f, gup = 0.f, c = 0.f;
+            if (m != 0) {
+                if (scalar_fs) gup = S.iso_amp * S.iso_amp;
+                else {
+                    c = S.k2 * S.D[m] * 1.44269504088896341f;
+                    if (ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN) { g = S.g[m]; omg2 = (1.0f - g) * (1.0f - g); gup = S.gup[m]; }
+                    else if (ty_ == SSTMC_SCATTERING_ISOTROPIC) gup = S.iso_pdf;
+                }
+            }
+            sM[threadIdx.x] = make_float4(g, omg2, gup, c);
         }
         __syncthreads();
+#pragma unroll 2
         for (int pp = 0; pp < kFk; ++pp) {
-            const int m = m1s[pp];
-            if (m == 0) continue;
-            const int ty_ = S.scat_type[m];
-            const float g = S.g[m], omg = 1.0f - g, gup = S.gup[m];
-            const float c1 = S.k2 * S.D[m];
-            const float av[2] = { as[pp * kFl + tx], as[pp * kFl + tx + 16] };
-            const float bv[2] = { bs[pp * kFv + ty], bs[pp * kFv + ty + 16] };
+            const float4 mc = sM[pp];
+            const float4 iv[2] = { sI[pp * kFl + tx], sI[pp * kFl + tx + 16] };
+            const float4 ov[2] = { sO[pp * kFv + ty], sO[pp * kFv + ty + 16] };
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
                 for (int j = 0; j < 2; ++j) {
-                    const int cl = tx + 16 * i, cv = ty + 16 * j;
-                    const float dx = inx[(pp * 3 + 0) * kFl + cl] - outx[(pp * 3 + 0) * kFv + cv];
-                    const float dy = inx[(pp * 3 + 1) * kFl + cl] - outx[(pp * 3 + 1) * kFv + cv];
-                    const float dz = inx[(pp * 3 + 2) * kFl + cl] - outx[(pp * 3 + 2) * kFv + cv];
+                    const float dx = iv[i].x - ov[j].x, dy = iv[i].y - ov[j].y, dz = iv[i].z - ov[j].z;
                     const float q2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    float pdf;
-                    if (ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
-                        const float r = rsqrtf(fmaf(g, q2, omg * omg));
-                        pdf = S.dims == 2 ? gup * r * r : gup * r * r * r;
-                    } else {
-                        pdf = ty_ == SSTMC_SCATTERING_ISOTROPIC ? S.iso_pdf : 0.0f;
-                    }
-                    // scalar single-scattering amplitude (point x point, isotropic): the
-                    // temporal factor is not applied (NextEventEstimation.cuh:1024-1032)
-                    const float base = av[i] * bv[j] * (scalar_fs ? S.iso_amp * S.iso_amp : pdf);
-                    const float cq = scalar_fs ? 0.0f : c1 * q2;
+                    const float r = rsqrtf(fmaf(mc.x, q2, mc.y));
+                    const float pdf = three ? mc.z * r * r * r : mc.z * r * r;
+                    const float base = iv[i].w * ov[j].w * pdf;
+                    const float cq = mc.w * q2;
                     if (geo) {
-                        float e = __expf(-cq * taus);
-                        const float es = __expf(-cq * tau0);
+                        const float es = exp2f(-cq * tau0);
+                        float e = t0 == 0 ? es : exp2f(-cq * taus);
 #pragma unroll
                         for (int tt = 0; tt < kFt; ++tt) {
-                            if (tt < tn) acc[i][j][tt] = fmaf(base, e, acc[i][j][tt]);
+                            acc[i][j][tt] = fmaf(base, e, acc[i][j][tt]);
                             e *= es;
                         }
                     } else {
 #pragma unroll
                         for (int tt = 0; tt < kFt; ++tt)
-                            if (tt < tn) acc[i][j][tt] = fmaf(base, __expf(-cq * S.abs_ticks[t0 + tt]), acc[i][j][tt]);
+                            if (tt < tn) acc[i][j][tt] = fmaf(base, exp2f(-cq * S.abs_ticks[t0 + tt]), acc[i][j][tt]);
                     }
                 }
         }
@@ -396,11 +406,20 @@ int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
 {
     if (G.K <= 0) return SSTMC_NO_ERROR;
     if (S.correlation && S.sym && S.all_static_corr) {
-        const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
+        // two resident blocks per SM: split the paths so the grid fills them
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int tchunks = (S.Nt + kFt - 1) / kFt;
+        const int tiles = ((S.src[0].n + kFl - 1) / kFl) * ((S.src[1].n + kFv - 1) / kFv) * tchunks;
+        const int want = std::max(1, (2 * sms) / tiles);
+        SsParams P = G;
+        P.kchunk = ((G.K + want - 1) / want + kFk - 1) / kFk * kFk;
+        const int ksplit = (G.K + P.kchunk - 1) / P.kchunk;
         dim3 grid((S.src[0].n + kFl - 1) / kFl, (S.src[1].n + kFv - 1) / kFv, tchunks * ksplit);
-        cudaFuncSetAttribute(ss_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem);
-        ss_fast_kernel<<<grid, 256, kFastSmem, stream>>>(S, G);
+        if (cudaFuncSetAttribute(ss_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem) != cudaSuccess)
+            return SSTMC_CUBLAS_ERROR;
+        ss_fast_kernel<<<grid, 256, kFastSmem, stream>>>(S, P);
         return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
     }
     const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;

@@ -42,29 +42,43 @@ __device__ __forceinline__ void philox4x32_10(uint32_t k0, uint32_t k1, uint32_t
 }
 
 // Sequential words of one (path, vertex, purpose) stream:
-// block j = Philox(key = seed, counter = (j, a, b, tag)).
+// block j = Philox(key = seed, counter = (j, a, b, tag)).  The walk primes the
+// first two blocks (8 words) at one point of its loop so that all lanes of a
+// warp run the two Philox evaluations together; later blocks are generated
+// on demand, 4 words at a time.  Priming changes when words are generated,
+// never which words a draw returns.
 struct Stream {
     uint32_t k0, k1, a, b, tag, block;
-    uint32_t w0, w1, w2, w3;
-    int idx;
+    uint32_t w0, w1, w2, w3, w4, w5, w6, w7;
+    int idx, n;
 
     __device__ __forceinline__ void init(uint64_t seed, uint32_t a_, uint32_t b_, uint32_t tag_)
     {
         k0 = (uint32_t)seed; k1 = (uint32_t)(seed >> 32);
-        a = a_; b = b_; tag = tag_; block = 0; idx = 4;
+        a = a_; b = b_; tag = tag_; block = 0; idx = 0; n = 0;
+    }
+    __device__ __forceinline__ void prime2()
+    {
+        uint32_t o[4];
+        philox4x32_10(k0, k1, 0u, a, b, tag, o);
+        w0 = o[0]; w1 = o[1]; w2 = o[2]; w3 = o[3];
+        philox4x32_10(k0, k1, 1u, a, b, tag, o);
+        w4 = o[0]; w5 = o[1]; w6 = o[2]; w7 = o[3];
+        block = 2; idx = 0; n = 8;
     }
     __device__ __forceinline__ uint32_t next()
     {
-        if (idx == 4) {
+        if (idx == n) {
             uint32_t o[4];
             philox4x32_10(k0, k1, block, a, b, tag, o);
             w0 = o[0]; w1 = o[1]; w2 = o[2]; w3 = o[3];
             block++;
-            idx = 0;
+            idx = 0; n = 4;
         }
-        uint32_t r = idx == 0 ? w0 : (idx == 1 ? w1 : (idx == 2 ? w2 : w3));
-        idx++;
-        return r;
+        const int i = idx++;
+        const uint32_t lo = i & 2 ? (i & 1 ? w3 : w2) : (i & 1 ? w1 : w0);
+        const uint32_t hi = i & 2 ? (i & 1 ? w7 : w6) : (i & 1 ? w5 : w4);
+        return i & 4 ? hi : lo;
     }
     // Uniform in (0, 1]: ((x >> 8) + 1) * 2^-24 (exact).
     __device__ __forceinline__ float uniform()

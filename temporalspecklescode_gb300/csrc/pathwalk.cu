@@ -43,27 +43,36 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
     return make_float4(x.x, x.y, x.z, __uint_as_float((k << 4) | (uint32_t)m));
 }
 
-// Flattened walk: each thread owns paths q = tid, tid + nthreads, ... and
-// samples one vertex (or one first-vertex attempt) per iteration, moving on
-// to its next path as soon as one ends, so the lanes of a warp stay on the
-// same free-flight code instead of idling behind the longest path.
+// Flattened walk: a thread samples one vertex (or one first-vertex attempt)
+// per iteration and takes a new path from a shared counter as soon as its
+// path ends (warp-aggregated atomics), so the lanes of a warp stay busy until
+// the whole pool is drawn.  The first two Philox blocks of each vertex are
+// generated at the top of the iteration, where all lanes are converged.
 template <bool WRITE>
 __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
-    const uint32_t nthreads = gridDim.x * blockDim.x;
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
     const bool corr = S.correlation != 0;
-    uint32_t pid = 0, att = 0, b = 1, B = 0, h = 2166136261u;
+    uint32_t q = 0, pid = 0, att = 0, b = 1, B = 0, h = 2166136261u;
     V3 prev{ 0.f, 0.f, 0.f }, cur{ 0.f, 0.f, 0.f };
     int mcur = 0;
     float4* out = nullptr;
     const DevSource* fsrc = &S.src[0];
-    // advance to the next path this thread owns that has work; false when done
+    // next path index for each active lane (one atomic per warp and call)
+    auto fetch = [&]() -> uint32_t {
+        const uint32_t mask = __activemask();
+        const int leader = __ffs(mask) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(W.next, (uint32_t)__popc(mask));
+        base = __shfl_sync(mask, base, leader);
+        return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    };
+    // move to the next path that has work; false when the pool is drawn
     auto start = [&](uint32_t qq) -> bool {
         while (qq < W.paths) {
             if (!WRITE || W.counts[qq] != 0) break;
             if (W.hash) W.hash[qq] = 2166136261u;  // the count pass hit a limit: nothing to write
-            qq += nthreads;
+            qq = fetch();
         }
         q = qq;
         if (q >= W.paths) return false;
@@ -79,15 +88,15 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
         if (!WRITE) { W.counts[q] = B; W.misses[q] = att; }
         else if (W.hash) W.hash[q] = h;
     };
-    if (!start(q)) return;
+    if (!start(fetch())) return;
     for (;;) {
         Stream rs;
+        rs.init(W.seed, pid, b, kPurposeWalk | (b == 1 ? att << 8 : 0u));
+        rs.prime2();
         V3 o, d;
         if (b == 1) {
-            rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
             sample_source(S, *fsrc, rs, o, d);
         } else {
-            rs.init(W.seed, pid, b, kPurposeWalk);
             const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
             d = sample_direction(S, mcur, din, rs);
             o = cur;
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
         }
         if (done) {
             finish(ok);
-            if (!start(q + nthreads)) return;
+            if (!start(fetch())) return;
         }
     }
 }
@@ -176,18 +185,20 @@ __global__ void scan_add_kernel(uint32_t* offsets, const uint32_t* block_sums, u
 
 static int walk_blocks(uint32_t paths)
 {
-    // about 8 paths per thread, at most 16 resident blocks of 128 threads per SM
+    // about 4 paths per thread, at most 8 resident blocks of 128 threads per SM
+    // (threads draw paths from the shared counter until the pool is empty)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t want = (paths + 8 * 128 - 1) / (8 * 128);
-    const uint32_t cap = (uint32_t)sms * 16;
+    const uint32_t want = (paths + 4 * 128 - 1) / (4 * 128);
+    const uint32_t cap = (uint32_t)sms * 8;
     return (int)std::max<uint32_t>(1, std::min(want, cap));
 }
 
 int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
     const int threads = 128;
+    if (cudaMemsetAsync(W.next, 0, 2 * sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     walk_kernel<false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
     if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
     const uint32_t nb = (W.paths + kScanBlock - 1) / kScanBlock;
@@ -200,7 +211,9 @@ int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t strea
 int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
     const int threads = 128;
-    walk_kernel<true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+    WalkParams Wn = W;
+    Wn.next = W.next + 1;   // the write pass draws from the second counter (zeroed with the first)
+    walk_kernel<true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, Wn);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
 }
 

@@ -17,6 +17,7 @@ struct WalkParams {
     float4* verts;           // [total] x, y, z, packed (k << 4 | material), xi = k * 2^-24
     uint32_t* hash;          // [paths] or null
     int* err;
+    uint32_t* next;          // [2] path counters of the count and write passes (zeroed by launch_walk_count)
 };
 
 // Count pass + exclusive scan of the counts.

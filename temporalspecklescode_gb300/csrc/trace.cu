@@ -87,8 +87,9 @@ __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, i
         }
         for (int i = lane; i < Nt * Nv; i += 32) T.b_ss[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
     }
-    for (int t = T.t0; t < T.t0 + T.tn; ++t)
-        for (int v = T.v0 + lane; v < T.v0 + T.vn; v += 32) T.s_ms[((size_t)q * Nt + t) * Nv + v] = make_float2(0.f, 0.f);
+    if (T.views)
+        for (int t = T.t0; t < T.t0 + T.tn; ++t)
+            for (int v = T.v0 + lane; v < T.v0 + T.vn; v += 32) T.s_ms[((size_t)q * Nt + t) * Nv + v] = make_float2(0.f, 0.f);
 }
 
 // ---- NEE vectors, specialised on the source type (PT: point source) ----
@@ -348,6 +349,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         int mcur = m1;
         float MT = 0.0f;
         for (uint32_t b = 2; b <= B; ++b) {
+            if (!T.views && b > 2) break;   // the view-side kernel sums the view vectors
             const float4 vb = vq[b - 1];
             const V3 xn = V3{ vb.x, vb.y, vb.z };
             const int mn = (int)(__float_as_uint(vb.w) & 15u);
@@ -422,7 +424,8 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             }
 
             // view vectors at vertex b, summed over the path (multipleResMultiple)
-            if constexpr (CORR) {
+            if (!T.views) {
+            } else if constexpr (CORR) {
                 const bool stn = S.static_corr[mn] != 0;
                 const bool realv = S.sym && stn;
                 const bool stf = stn && S.static_corr[mcur];
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
         }
         // write the summed view vector of this chunk
-        {
+        if (T.views) {
             int j = 0;
             for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                 int k = 0;

@@ -51,7 +51,9 @@ __device__ __forceinline__ int material_at(const DevScene& S, const V3& p)
     return __ldg(S.grid + idx);
 }
 
-__device__ inline bool points_toward(const DevScene& S, const V3& p, const V3& d)
+// Whether the ray from p along d hits the box; *hit = distance to the face it
+// enters (or leaves, from inside) first.
+__device__ inline bool points_toward(const DevScene& S, const V3& p, const V3& d, float* hit = nullptr)
 {
     const int D = S.dims;
     float o[3], inv[3], dist[3];
@@ -75,7 +77,7 @@ __device__ inline bool points_toward(const DevScene& S, const V3& p, const V3& d
             if (j == i) continue;
             if (!(fabsf(ffma(comp(d, j), dist[i], o[j])) < S.radius[j])) ok = false;
         }
-        if (ok) return true;
+        if (ok) { if (hit) *hit = dist[i]; return true; }
     }
     return false;
 }
@@ -143,7 +145,12 @@ __device__ inline V3 sample_direction(const DevScene& S, int m, const V3& din, S
                fa(fm(fm(-sa, cphi), st), fm(din.z, c)) };
 }
 
-// Woodcock free flight from o along d; returns false if the step limit ran out.
+// Woodcock free flight from o along d (HeterogeneousMedium.cuh:576-678);
+// returns false if the step limit ran out.  A tentative point outside the box
+// on a ray that still enters it moves on to the entry face: flight lengths
+// are memoryless, so the first point inside is the entry plus an exponential
+// step, as with further steps outside, but one lane no longer spins alone
+// through many small steps toward a far or grazing entry.
 __device__ inline bool woodcock(const DevScene& S, const V3& o, const V3& d, Stream& rs, V3& out, int& mat)
 {
     float dist = 0.0f;
@@ -158,7 +165,9 @@ __device__ inline bool woodcock(const DevScene& S, const V3& o, const V3& d, Str
         p.y = ffma(dist, d.y, o.y);
         if (S.dims == 3) p.z = ffma(dist, d.z, o.z);
         if (!inside(S, p)) {
-            if (!points_toward(S, p, d)) break;
+            float te = 0.0f;
+            if (!points_toward(S, p, d, &te)) break;
+            dist = fa(dist, te);
         } else {
             m = material_at(S, p);
             if (rs.uniform() <= S.accept[m]) break;

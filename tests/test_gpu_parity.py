@@ -133,3 +133,25 @@ def test_tensor_core_contraction_large_k_against_oracle(api, oracle):
     uo, ito, _ = oracle.render(cf.prepare(cfg, dims), 4)
     assert it[0] == ito
     assert rel_fro(u[..., 0], uo) <= REL_TOL
+
+
+@pytest.mark.parametrize("name", ["correlation_64x64", "speckle_2d", "correlation_3d", "transmission_matrix_3d", "mcx_3d",
+                                  "homogeneous_3d", "point_2d_iso_field", "point_2d_iso_corr"])
+def test_view_kernel_matches_fused_kernel(name, api, monkeypatch):
+    """The view-side kernel (default for static scenes) against the view loop
+    of the fused trace kernel: identical voxel-step counts and per-path view
+    rows within FP32 rounding."""
+    from temporalspecklescode_gb300 import workloads as wl
+    if name == "correlation_64x64":
+        cfg, dims = wl.correlation_3d(batch_size=512, full_iteration=1, n_side=8, n_lags=8)
+    else:
+        cfg, dims = SCENES[name]
+    with api.Scene(cfg, dims) as s:
+        a = s.trace_paths(seed=8, first_path=3, paths=256)
+        monkeypatch.setenv("SSTMC_VIEW_KERNEL", "fused")
+        b = s.trace_paths(seed=8, first_path=3, paths=256)
+    for k in ("misses", "vertices", "vertex_hash", "dda_steps"):
+        assert np.array_equal(a[k], b[k]), (name, k)
+    for k in ("a_ms", "s_ms", "a_ss", "b_ss"):
+        err = rel_fro(a[k], b[k])
+        assert err <= 2e-6, (name, k, err)
