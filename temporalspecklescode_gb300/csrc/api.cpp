@@ -223,10 +223,15 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     bool moving_any = false;
     for (int m : S.materials_present) moving_any = moving_any || S.dev.moving[m] != 0;
     if (use_view_kernel() && view_kernel_covers(S.dev, &moving_any)) {
-        // illumination side in the fused kernel, view side in viewsum.cu
+        // illumination side in the fused kernel (or illum_kernel), view side in viewsum.cu
         T.pass0 = 1; T.views = 0;
         T.v0 = 0; T.vn = S.Nv; T.t0 = 0; T.tn = S.Nt;
-        e = launch_trace(S.dev, T, blocks, threads, stream);
+        // ss_fast_kernel reads tick 0 of the tick-invariant rows; the far-field x
+        // far-field GEMM and the per-path debug trace read every tick
+        const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD;
+        T.ss_all_ticks = (dbg || farfar) ? 1 : 0;
+        if (illum_kernel_covers(S.dev)) e = launch_illum(S.dev, T, std::max(1, (int)((n + 3) / 4)), threads, stream);
+        else e = launch_trace(S.dev, T, blocks, threads, stream);
         if (e) return e;
         launches++;
         const int vmax = view_max_views(), tmax = view_max_ticks(S.dev);

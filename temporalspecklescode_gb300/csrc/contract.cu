@@ -261,20 +261,43 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
 //   e_t = exp2(-c q^2 |tau_t|), c = k^2 D log2(e)
 // The scalar single-scattering amplitude of point x point isotropic scenes
 // (no temporal factor, NextEventEstimation.cuh:1024-1032) is g = 0, c = 0.
+// The tick chain runs on packed FP32 pairs (two ticks per FMA / MUL).
 constexpr int kFl = 32, kFv = 32, kFk = 16, kFt = 8;
 
-constexpr size_t kFastSmem = sizeof(float4) * (kFk * kFl + kFk * kFv + kFk) + sizeof(double) * 4 * kFt * 256;
+constexpr size_t kFastSmem = sizeof(float4) * (kFk * kFl + kFk * kFv) + (sizeof(float2) + sizeof(float)) * kFk + sizeof(float2) * 4 * kFt * 256;
 
 // Rows here are tick-invariant (static scatterers, identical u1 / u2
 // sources), so only the first tick's rows are read; the tick dependence is
 // the decay exp(-c |t|), chained multiplicatively for geometric ticks.
+// Packed FP32 pairs (Blackwell f32x2 FMA / MUL): two ticks per instruction.
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi)
+{
+    return (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
+}
+__device__ __forceinline__ float pk_lo(unsigned long long v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float pk_hi(unsigned long long v) { return __uint_as_float((uint32_t)(v >> 32)); }
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+template <bool THREE, bool GEO>
 __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__ DevScene S, const SsParams G)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double* accd = reinterpret_cast<double*>(smem_raw);                       // [4*kFt][256] FP64 window sums
-    float4* sI = reinterpret_cast<float4*>(accd + 4 * kFt * 256);            // [kFk][kFl]
-    float4* sO = sI + kFk * kFl;                                              // [kFk][kFv]
-    float4* sM = sO + kFk * kFv;                                              // [kFk]
+    float2* accc = reinterpret_cast<float2*>(smem_raw);                       // [4*kFt][256] compensated (hi, lo) window sums
+    float4* sI = reinterpret_cast<float4*>(accc + 4 * kFt * 256);            // [kFk][kFl] (direction in, row x material coefficient)
+    float4* sO = sI + kFk * kFl;                                              // [kFk][kFv] (direction out, row)
+    float2* sM = reinterpret_cast<float2*>(sO + kFk * kFv);                   // [kFk] (g, omg2) ...
+    float* sC = reinterpret_cast<float*>(sM + kFk);                           // [kFk] c = k^2 D
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int l0 = blockIdx.x * kFl, v0 = blockIdx.y * kFv;
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
@@ -285,19 +308,32 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     const int kb = ks * G.kchunk, ke = min(G.K, kb + G.kchunk);
     const DevSource& il = S.src[0];
     const DevSource& vw = S.src[1];
-    const bool geo = S.ticks_geometric != 0;
-    const bool three = S.dims == 3;
     const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
     const float tau0 = S.abs_ticks[0], taus = S.abs_ticks[t0];
-    float acc[2][2][kFt];
+    unsigned long long acc[2][2][kFt / 2];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
+        for (int j = 0; j < 2; ++j) {
 #pragma unroll
-            for (int t = 0; t < kFt; ++t) { acc[i][j][t] = 0.f; accd[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = 0.0; }
+            for (int t = 0; t < kFt / 2; ++t) acc[i][j][t] = 0ull;
+#pragma unroll
+            for (int t = 0; t < kFt; ++t) accc[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = make_float2(0.f, 0.f);
+        }
     int chunk = 0;
     for (int k = kb; k < ke; k += kFk, ++chunk) {
+        if (threadIdx.x < kFk) {
+            const int p = k + threadIdx.x;
+            const int m = p < ke ? (int)G.m1[p] : 0;
+            const int ty_ = S.scat_type[m];
+            float g = 0.f, omg2 = 1.f, c = 0.f;
+            if (m != 0 && !scalar_fs) {
+                c = S.k2 * S.D[m];
+                if (ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN) { g = S.g[m]; omg2 = (1.0f - g) * (1.0f - g); }
+            }
+            sM[threadIdx.x] = make_float2(g, omg2);
+            sC[threadIdx.x] = c;
+        }
         for (int idx = threadIdx.x; idx < kFk * (kFl + kFv); idx += 256) {
             const bool isI = idx < kFk * kFl;
             const int r = isI ? idx : idx - kFk * kFl;
@@ -308,7 +344,16 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             float val = 0.f;
             V3 dir;
             if (isI) {
-                if (p < ke && l0 + c < Nl) val = G.a[(size_t)p * Nt * Nl + l0 + c].x;
+                if (p < ke && l0 + c < Nl) {
+                    // row value times the material's pdf coefficient
+                    const int m = (int)G.m1[p];
+                    const int ty_ = S.scat_type[m];
+                    const float coef = m == 0 ? 0.0f
+                                     : scalar_fs ? S.iso_amp * S.iso_amp
+                                     : ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN ? S.gup[m]
+                                     : ty_ == SSTMC_SCATTERING_ISOTROPIC ? S.iso_pdf : 0.0f;
+                    val = G.a[(size_t)p * Nt * Nl + l0 + c].x * coef;
+                }
                 dir = fsrc_in(il, min(l0 + c, Nl - 1), x);
                 sI[r] = make_float4(dir.x, dir.y, dir.z, val);
             } else {
@@ -317,25 +362,11 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 sO[r] = make_float4(dir.x, dir.y, dir.z, val);
             }
         }
-        if (threadIdx.x < kFk) {
-            const int p = k + threadIdx.x;
-            const int m = p < ke ? (int)G.m1[p] : 0;
-            const int ty_ = S.scat_type[m];
-            float g = 0.f, omg2 = 1.f, gup = 0.f, c = 0.f;
-            if (m != 0) {
-                if (scalar_fs) gup = S.iso_amp * S.iso_amp;
-                else {
-                    c = S.k2 * S.D[m] * 1.44269504088896341f;
-                    if (ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN) { g = S.g[m]; omg2 = (1.0f - g) * (1.0f - g); gup = S.gup[m]; }
-                    else if (ty_ == SSTMC_SCATTERING_ISOTROPIC) gup = S.iso_pdf;
-                }
-            }
-            sM[threadIdx.x] = make_float4(g, omg2, gup, c);
-        }
         __syncthreads();
 #pragma unroll 2
         for (int pp = 0; pp < kFk; ++pp) {
-            const float4 mc = sM[pp];
+            const float2 mc = sM[pp];
+            const float cm = sC[pp];
             const float4 iv[2] = { sI[pp * kFl + tx], sI[pp * kFl + tx + 16] };
             const float4 ov[2] = { sO[pp * kFv + ty], sO[pp * kFv + ty + 16] };
 #pragma unroll
@@ -345,34 +376,45 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                     const float dx = iv[i].x - ov[j].x, dy = iv[i].y - ov[j].y, dz = iv[i].z - ov[j].z;
                     const float q2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
                     const float r = rsqrtf(fmaf(mc.x, q2, mc.y));
-                    const float pdf = three ? mc.z * r * r * r : mc.z * r * r;
-                    const float base = iv[i].w * ov[j].w * pdf;
-                    const float cq = mc.w * q2;
-                    if (geo) {
-                        const float es = exp2f(-cq * tau0);
-                        float e = t0 == 0 ? es : exp2f(-cq * taus);
+                    const float r2 = r * r;
+                    const float base = iv[i].w * ov[j].w * (THREE ? r2 * r : r2);
+                    const float cq = cm * q2;
+                    if (GEO) {
+                        const float es = __expf(-cq * tau0);
+                        const float e0 = t0 == 0 ? es : __expf(-cq * taus);
+                        const float es2 = es * es;
+                        unsigned long long e = pk2(e0, e0 * es);
+                        const unsigned long long st = pk2(es2, es2), b2 = pk2(base, base);
 #pragma unroll
-                        for (int tt = 0; tt < kFt; ++tt) {
-                            acc[i][j][tt] = fmaf(base, e, acc[i][j][tt]);
-                            e *= es;
+                        for (int tt = 0; tt < kFt / 2; ++tt) {
+                            acc[i][j][tt] = fma2(b2, e, acc[i][j][tt]);
+                            if (tt + 1 < kFt / 2) e = mul2(e, st);
                         }
                     } else {
 #pragma unroll
-                        for (int tt = 0; tt < kFt; ++tt)
-                            if (tt < tn) acc[i][j][tt] = fmaf(base, exp2f(-cq * S.abs_ticks[t0 + tt]), acc[i][j][tt]);
+                        for (int tt = 0; tt < kFt / 2; ++tt) {
+                            const int ta = min(t0 + 2 * tt, Nt - 1), tb = min(t0 + 2 * tt + 1, Nt - 1);
+                            acc[i][j][tt] = fma2(pk2(base, base), pk2(__expf(-cq * S.abs_ticks[ta]), __expf(-cq * S.abs_ticks[tb])), acc[i][j][tt]);
+                        }
                     }
                 }
         }
         __syncthreads();
         if ((chunk + 1) % 16 == 0) {
+            // fold the 256-path window into the compensated (hi, lo) pairs
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
                 for (int j = 0; j < 2; ++j)
 #pragma unroll
-                    for (int t = 0; t < kFt; ++t) {
-                        accd[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] += (double)acc[i][j][t];
-                        acc[i][j][t] = 0.f;
+                    for (int t = 0; t < kFt / 2; ++t) {
+                        float2* c0 = accc + ((i * 2 + j) * kFt + 2 * t) * 256 + threadIdx.x;
+                        float2* c1 = c0 + 256;
+                        float2 a0 = *c0, a1 = *c1;
+                        two_sum_add(a0.x, a0.y, pk_lo(acc[i][j][t]));
+                        two_sum_add(a1.x, a1.y, pk_hi(acc[i][j][t]));
+                        *c0 = a0; *c1 = a1;
+                        acc[i][j][t] = 0ull;
                     }
         }
     }
@@ -386,7 +428,9 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             for (int tt = 0; tt < kFt; ++tt) {
                 if (tt >= tn) break;
                 const size_t o = ((size_t)(t0 + tt) * Nv + v) * Nl + l;
-                atomicAdd(&G.V[o].x, accd[((i * 2 + j) * kFt + tt) * 256 + threadIdx.x] + (double)acc[i][j][tt]);
+                const float last = (tt & 1) ? pk_hi(acc[i][j][tt >> 1]) : pk_lo(acc[i][j][tt >> 1]);
+                const float2 c = accc[((i * 2 + j) * kFt + tt) * 256 + threadIdx.x];
+                atomicAdd(&G.V[o].x, (double)c.x + (double)c.y + (double)last);
             }
         }
 }
@@ -417,9 +461,13 @@ int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
         P.kchunk = ((G.K + want - 1) / want + kFk - 1) / kFk * kFk;
         const int ksplit = (G.K + P.kchunk - 1) / P.kchunk;
         dim3 grid((S.src[0].n + kFl - 1) / kFl, (S.src[1].n + kFv - 1) / kFv, tchunks * ksplit);
-        if (cudaFuncSetAttribute(ss_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem) != cudaSuccess)
+        using Fn = void (*)(DevScene, SsParams);
+        const bool geo = S.ticks_geometric != 0;
+        Fn f = S.dims == 3 ? (geo ? (Fn)ss_fast_kernel<true, true> : (Fn)ss_fast_kernel<true, false>)
+                           : (geo ? (Fn)ss_fast_kernel<false, true> : (Fn)ss_fast_kernel<false, false>);
+        if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem) != cudaSuccess)
             return SSTMC_CUBLAS_ERROR;
-        ss_fast_kernel<<<grid, 256, kFastSmem, stream>>>(S, P);
+        f<<<grid, 256, kFastSmem, stream>>>(S, P);
         return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
     }
     const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;

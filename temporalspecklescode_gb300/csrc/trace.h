@@ -13,6 +13,7 @@ struct TraceParams {
     uint32_t first_path, paths;
     int pass0;            // 1: write the illumination rows, single-scattering rows and stats
     int views;            // 1: also sum the view vectors (s_ms); 0: they come from the view-side kernel (viewsum.cu)
+    int ss_all_ticks;     // illum_kernel: write the tick-invariant single-scattering rows for every tick (else tick 0 only)
     int v0, vn, t0, tn;   // view / tick chunk accumulated by this pass
     int vw, tg, tpl;      // lanes: view = v0 + lane % vw + vw*j, tick = t0 + lane / vw + tg*k, k < tpl
     int slots;            // accumulator slots per lane (vpl * tpl)

@@ -33,16 +33,199 @@ namespace {
 constexpr int kVB = 32;     // vertices per block
 constexpr int kNT = 8;      // ticks per pass (correlation)
 constexpr int kVPL = 4;     // views per lane per pass
+constexpr int kMaxIllum = 8;   // illumination elements per lane (illumination side: Nl <= 256)
 
 struct VRec {
-    float x, y, z;
-    float ux, uy, uz;       // unit direction x_{b-1} -> x_b
-    float mt;               // correlation: k^2 sum_{3 <= c <= b} D_{m(c-1)} |u_{c-1} - u_c|^2
-    uint32_t m;             // material | inside << 8
+    float x, y, z, mt;      // position; correlation: k^2 sum_{3 <= c <= b} D_{m(c-1)} |u_{c-1} - u_c|^2
+    float ux, uy, uz, k2d;  // unit direction x_{b-1} -> x_b; k^2 D_{m(b)}
+    float g, omg2, c, sig;  // phase-function constants: pdf or amplitude = c (omg2 + g q^2)^(-e); sig: sigma_t inside the box, else 0
+    float nx0, nx1, ny0, ny1;   // distances to the box faces: x - bmin, bmax - x (single-cell media)
+    float nz0, nz1;
+    uint32_t in;            // 1 inside the box
     double ph;              // field: L_b / lambda + xi_b reduced to [-1/2, 1/2] cycles
 };
 
-template <bool CORR, bool VWP>
+// (face - x) / d along the axis, face = bmin or bmax by the sign of d (the
+// reference's bdDistance, HeterogeneousMedium.cuh:269-383, for one cell)
+// Packed FP32 pairs (Blackwell f32x2 FMA / MUL)
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi)
+{
+    return (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
+}
+__device__ __forceinline__ float pk_lo(unsigned long long v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float pk_hi(unsigned long long v) { return __uint_as_float((uint32_t)(v >> 32)); }
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// distance to the face the direction component d heads for: n0 = x - bmin
+// (d < 0) or n1 = bmax - x, over |d| (|d| = 0: +inf, which fminf drops)
+__device__ __forceinline__ float face_t(float d, float n0, float n1)
+{
+    return (d < 0.0f ? n0 : n1) * __fdividef(1.0f, fabsf(d));
+}
+
+// Illumination side of the correlation sampler with identical u1 / u2
+// sources and static scatterers (the rows are real):
+//   P_l   = first-point probability terms (pathProbabilitySingle, NEE.cuh:853-887)
+//   a_ss  = |g_l(x1)|^2 / p1                     (single scattering)
+//   b_ss  = |g_v(x1)|^2
+//   a_ms  = |g_l(x1)|^2 pdf(l -> x1 -> x2) exp(-k^2 D |t| |q|^2) / p2
+//           (pathProbabilityMultiple, NEE.cuh:889-1009; C1_l1l2 of
+//            TemporalSamplerCorrelation.cuh:384-450)
+// Lane l + 32 k of the path's warp.  Each row is written once; the
+// single-scattering rows are tick-invariant, so only tick 0 is written
+// unless every tick is asked for (T.ss_all_ticks).
+template <int NLK, bool ilp, bool vwp>
+__device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams& T, uint32_t q, int lane,
+                                           uint32_t B, const float4* vq)
+{
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    const bool three = S.dims == 3;
+    const bool geo = S.ticks_geometric != 0;
+    const int tss = T.ss_all_ticks ? Nt : 1;
+    float2* ams = T.a_ms + (size_t)q * Nt * Nl;
+    float2* ass = T.a_ss + (size_t)q * Nt * Nl;
+    float2* bss = T.b_ss + (size_t)q * Nt * Nv;
+    if (B == 0) {   // the walk hit a limit (error already flagged)
+        for (int i = lane; i < Nt * Nl; i += 32) { ams[i] = make_float2(0.f, 0.f); ass[i] = make_float2(0.f, 0.f); }
+        for (int i = lane; i < Nt * Nv; i += 32) bss[i] = make_float2(0.f, 0.f);
+        return;
+    }
+    const float4 v1 = vq[0];
+    const float4 v2 = vq[B >= 2 ? 1 : 0];
+    const V3 x1 = V3{ v1.x, v1.y, v1.z };
+    const int m1 = (int)(__float_as_uint(v1.w) & 15u);
+    uint32_t steps = 0;
+    // |g_l|^2 and P_l from one attenuation evaluation per element
+    float wl[NLK], pl[NLK];
+    float ps = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NLK; ++k) {
+        const int l = lane + 32 * k;
+        wl[k] = 0.0f; pl[k] = 0.0f;
+        if (32 * k < Nl && l < Nl) {
+            uint32_t st = 0;
+            float P, w;
+            if constexpr (ilp) {
+                const V3 sp = load3(il.p, l);
+                const float Ta = __expf(-tau_to_point(S, x1, sp, st));
+                const V3 d = sub3(x1, sp);
+                const float r2 = dot3(d, d);
+                P = three ? __fdividef(Ta, (float)(4.0 * kPi) * r2) : Ta * (float)(8.0 * kPi) * rsqrtf(r2);
+                w = three ? __fdividef(Ta * kIsoAmp3, r2) : Ta * rsqrtf(r2);
+                if (il.is_area) w *= fabsf(three ? d.z : d.y) * rsqrtf(r2);
+            } else {
+                const V3 dr = load3(il.p, l);
+                const float Ta = __expf(-tau_dir(S, x1, V3{ -dr.x, -dr.y, -dr.z }, st));
+                P = Ta * il.sprob[l];
+                w = Ta;
+            }
+            // u1 and u2 rays (identical sources): the probability and every tick of the rows
+            steps += 2 * st + 2 * st * (uint32_t)Nt;
+            T.pl[(size_t)q * Nl + l] = P;
+            pl[k] = P;
+            ps += P;
+            wl[k] = w;
+        }
+    }
+    const float p1inv = 1.0f / (warp_sum(ps) / (float)Nl);
+#pragma unroll
+    for (int k = 0; k < NLK; ++k) {
+        const int l = lane + 32 * k;
+        if (32 * k < Nl && l < Nl)
+            for (int t = 0; t < tss; ++t) ass[(size_t)t * Nl + l] = make_float2(wl[k] * p1inv, 0.f);
+    }
+    for (int v = lane; v < Nv; v += 32) {
+        uint32_t st = 0;
+        float w;
+        if constexpr (vwp) {
+            const V3 sp = load3(vw.p, v);
+            const float Ta = __expf(-tau_to_point(S, x1, sp, st));
+            const V3 d = sub3(x1, sp);
+            const float r2 = dot3(d, d);
+            w = three ? __fdividef(Ta * kIsoAmp3, r2) : Ta * rsqrtf(r2);
+            if (vw.is_area) w *= fabsf(three ? d.z : d.y) * rsqrtf(r2);
+        } else {
+            w = __expf(-tau_dir(S, x1, load3(vw.p, v), st));
+        }
+        steps += 2 * st * (uint32_t)Nt;
+        for (int t = 0; t < tss; ++t) bss[(size_t)t * Nv + v] = make_float2(w, 0.f);
+    }
+    // multiple-scattering illumination vector at x2
+    if (B >= 2) {
+        const V3 x2 = V3{ v2.x, v2.y, v2.z };
+        const V3 x12 = funit(sub3(x2, x1));
+        float ps2 = 0.0f;
+        V3 i1s[NLK];
+#pragma unroll
+        for (int k = 0; k < NLK; ++k) {
+            const int l = lane + 32 * k;
+            i1s[k] = V3{ 0.f, 0.f, 1.f };
+            if (32 * k < Nl && l < Nl) {
+                i1s[k] = fsrc_in(il, l, x1);
+                ps2 += pl[k] * pdf_fast(S, m1, i1s[k], x12);
+            }
+        }
+        const float p2inv = 1.0f / (warp_sum(ps2) / (float)Nl);
+        const float c1base = S.k2 * S.D[m1];
+        const float tau0 = S.abs_ticks[0];
+#pragma unroll
+        for (int k = 0; k < NLK; ++k) {
+            const int l = lane + 32 * k;
+            if (!(32 * k < Nl && l < Nl)) continue;
+            const V3 qv = sub3(i1s[k], x12);
+            const float c1k = c1base * dot3(qv, qv);
+            const float f12 = (ilp && S.iso_all) ? S.iso_amp * S.iso_amp : pdf_fast(S, m1, i1s[k], x12);
+            const float base = wl[k] * f12 * p2inv;
+            if (geo) {
+                const float es = __expf(-c1k * tau0);
+                float e = es;
+                for (int t = 0; t < Nt; ++t) { ams[(size_t)t * Nl + l] = make_float2(base * e, 0.f); e *= es; }
+            } else {
+                for (int t = 0; t < Nt; ++t) ams[(size_t)t * Nl + l] = make_float2(base * __expf(-c1k * S.abs_ticks[t]), 0.f);
+            }
+        }
+    } else {
+        for (int i = lane; i < Nt * Nl; i += 32) ams[i] = make_float2(0.f, 0.f);
+    }
+    const uint32_t ws = warp_sum_u32(steps);
+    if (lane == 0) {
+        if (T.m1) T.m1[q] = (unsigned char)m1;
+        if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
+        atomicAdd(T.totals + 0, (unsigned long long)B);
+        atomicAdd(T.totals + 2, (unsigned long long)T.misses[q]);
+        atomicAdd(T.totals + 3, 1ull);
+        if (ws) {
+            if (T.dda) atomicAdd(T.dda + q, ws);
+            atomicAdd(T.totals + 1, (unsigned long long)ws);
+        }
+    }
+}
+
+// One warp per path (a kernel of its own: it needs few registers, so many
+// warps hide the latency of its row writes).
+template <int NLK, bool ILP, bool VWP>
+__global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t q = gw; q < T.paths; q += nw) illum_path<NLK, ILP, VWP>(S, T, q, lane, T.counts[q], T.verts + T.offsets[q]);
+}
+
+template <bool CORR, bool VWP, bool SINGLE>
 __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     extern __shared__ __align__(16) unsigned char vsm[];
@@ -56,21 +239,35 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
     const DevSource& vw = S.src[1];
     const bool split = S.precision == SSTMC_PRECISION_SPLIT;
     const bool geo = S.ticks_geometric != 0;
+    const bool three = S.dims == 3;
     const int t0 = T.t0, tn = T.tn;
     const int nv = T.vn;
+    const int vpl = (nv + 31) / 32;
     // ray steps per (vertex, view): one ray per tick (u1 and u2 for the correlation sampler)
     const uint32_t rays = (uint32_t)(CORR ? 2 * tn : tn);
+    // this lane's views: position or direction, and (far field) the reciprocal direction
+    V3 sv[kVPL];
+    V3 sinv[kVPL];
+#pragma unroll
+    for (int j = 0; j < kVPL; ++j) {
+        const int vi = min(lane + 32 * j, nv - 1);
+        sv[j] = load3(vw.p, T.v0 + vi);
+        if (!VWP) sinv[j] = V3{ __fdividef(1.0f, fabsf(sv[j].x)), __fdividef(1.0f, fabsf(sv[j].y)), __fdividef(1.0f, fabsf(sv[j].z)) };
+    }
+    // views of this lane inside the chunk (lanes past its last view count no rays)
+    const uint32_t nvalid = (uint32_t)max(0, min(kVPL, (nv - lane + 31) / 32));
 
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t B = T.counts[q];
         const float4* vq = T.verts + T.offsets[q];
-        float acc[kVPL][CORR ? kNT : 2];
+        // packed pairs: two ticks (correlation) or (re, im) (field)
+        unsigned long long acc[kVPL][CORR ? kNT / 2 : 1];
 #pragma unroll
         for (int j = 0; j < kVPL; ++j)
 #pragma unroll
-            for (int k = 0; k < (CORR ? kNT : 2); ++k) acc[j][k] = 0.0f;
+            for (int k = 0; k < (CORR ? kNT / 2 : 1); ++k) acc[j][k] = 0ull;
         uint32_t steps = 0;
         float mt_carry = 0.0f;
         double l_carry = 0.0;
@@ -86,10 +283,24 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                     const float4 c = vq[b - 1], p = vq[b - 2];
                     const V3 xc = V3{ c.x, c.y, c.z }, xp = V3{ p.x, p.y, p.z };
                     const V3 u = funit(sub3(xc, xp));
+                    const int m = (int)(__float_as_uint(c.w) & 15u);
                     VRec r;
-                    r.x = c.x; r.y = c.y; r.z = c.z; r.ux = u.x; r.uy = u.y; r.uz = u.z;
-                    r.m = (__float_as_uint(c.w) & 15u) | (inside(S, xc) ? 256u : 0u);
-                    r.mt = 0.0f;
+                    r.x = c.x; r.y = c.y; r.z = c.z; r.mt = 0.0f;
+                    r.ux = u.x; r.uy = u.y; r.uz = u.z; r.k2d = S.k2 * S.D[m];
+                    // pdf (correlation) or amplitude (field) of the phase function as
+                    // c (omg2 + g q^2)^(-e): isotropic is g = 0, omg2 = 1
+                    const int ty = S.scat_type[m];
+                    r.g = 0.0f; r.omg2 = 1.0f; r.c = 0.0f;
+                    if (VWP && S.iso_all) r.c = CORR ? S.iso_amp * S.iso_amp : S.iso_amp;
+                    else if (ty == SSTMC_SCATTERING_ISOTROPIC) r.c = CORR ? S.iso_pdf : S.iso_amp;
+                    else if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
+                        r.g = S.g[m]; r.omg2 = (1.0f - r.g) * (1.0f - r.g); r.c = CORR ? S.gup[m] : S.sgup[m];
+                    }
+                    r.in = inside(S, xc) ? 1u : 0u;
+                    r.sig = r.in ? S.sigt[S.grid_m0] : 0.0f;
+                    r.nx0 = c.x - S.bmin[0]; r.nx1 = S.bmax[0] - c.x;
+                    r.ny0 = c.y - S.bmin[1]; r.ny1 = S.bmax[1] - c.y;
+                    r.nz0 = c.z - S.bmin[2]; r.nz1 = S.bmax[2] - c.z;
                     r.ph = (double)((float)(__float_as_uint(c.w) >> 4) * (1.0f / 16777216.0f));   // xi_b
                     if (CORR && b >= 3) {
                         const float4 pp = vq[b - 3];
@@ -137,84 +348,89 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                 }
             }
             __syncwarp();
-            // ---- views of this lane over the block's vertices ----
+            // ---- every vertex of the block against this lane's views ----
+            for (int i = 0; i < nb; ++i) {
+                const VRec r = rec[i];
+                const V3 xb = V3{ r.x, r.y, r.z };
+                if (SINGLE) steps += r.in * rays * nvalid;
 #pragma unroll
-            for (int j = 0; j < kVPL; ++j) {
-                const int vi = lane + 32 * j;
-                if (vi >= nv) break;
-                const int v = T.v0 + vi;
-                const V3 sv = load3(vw.p, v);
-                for (int i = 0; i < nb; ++i) {
-                    const VRec r = rec[i];
-                    const V3 xb = V3{ r.x, r.y, r.z };
-                    const V3 ub = V3{ r.ux, r.uy, r.uz };
-                    const int mb = (int)(r.m & 15u);
-                    const bool xin = (r.m & 256u) != 0;
-                    // direction to the view and optical depth toward it
+                for (int j = 0; j < kVPL; ++j) {
+                    if (j >= vpl) break;
+                    const bool vok = lane + 32 * j < nv;   // lanes past the chunk's last view count no rays
+                    // direction to the view and optical depth toward it (to the grid edge)
                     V3 o;
-                    float tau = 0.0f, r2 = 1.0f;
-                    uint32_t st = 0;
+                    float tau, ri = 1.0f;
                     if constexpr (VWP) {
-                        const V3 d = sub3(sv, xb);
-                        r2 = dot3(d, d);
-                        const float ri = rsqrtf(r2);
+                        const V3 d = sub3(sv[j], xb);
+                        const float r2 = dot3(d, d);
+                        ri = rsqrtf(r2);
                         o = V3{ d.x * ri, d.y * ri, d.z * ri };
-                        if (S.single) { if (xin) { st = 1; tau = tau_single(S, xb, o); } }
-                        else tau = tau_to_point(S, xb, sv, st);
                     } else {
-                        o = sv;
-                        if (S.single) { if (xin) { st = 1; tau = tau_single(S, xb, o); } }
-                        else tau = tau_dir(S, xb, o, st);
+                        o = sv[j];
                     }
-                    steps += st * rays;
-                    const V3 df = sub3(ub, o);
+                    if constexpr (SINGLE) {
+                        float tm;
+                        if constexpr (VWP) {
+                            tm = fminf(face_t(o.x, r.nx0, r.nx1), face_t(o.y, r.ny0, r.ny1));
+                            if (three) tm = fminf(tm, face_t(o.z, r.nz0, r.nz1));
+                        } else {
+                            tm = fminf((o.x < 0.0f ? r.nx0 : r.nx1) * sinv[j].x, (o.y < 0.0f ? r.ny0 : r.ny1) * sinv[j].y);
+                            if (three) tm = fminf(tm, (o.z < 0.0f ? r.nz0 : r.nz1) * sinv[j].z);
+                        }
+                        tau = tm * r.sig;
+                    } else {
+                        uint32_t st = 0;
+                        tau = VWP ? tau_to_point(S, xb, sv[j], st) : tau_dir(S, xb, o, st);
+                        steps += vok ? st * rays : 0u;
+                    }
+                    const V3 df = V3{ r.ux - o.x, r.uy - o.y, r.uz - o.z };
                     const float q2 = dot3(df, df);
+                    const float rr = rsqrtf(fmaf(r.g, q2, r.omg2));
                     if constexpr (CORR) {
                         // |g|^2 (PointSource.cuh:117-172 / FarField.cuh:223-263) times the pdf
                         float w = __expf(-tau);
                         if constexpr (VWP) {
-                            w = S.dims == 3 ? __fdividef(w * kIsoAmp3, r2) : w * rsqrtf(r2);
-                            if (vw.is_area) w *= fabsf(S.dims == 3 ? sub3(xb, sv).z : sub3(xb, sv).y) * rsqrtf(r2);
+                            w = three ? w * kIsoAmp3 * ri * ri : w * ri;
+                            if (vw.is_area) w *= fabsf(three ? o.z : o.y);
                         }
-                        float pdf;
-                        if (VWP && S.iso_all) pdf = S.iso_amp * S.iso_amp;
-                        else {
-                            const int ty = S.scat_type[mb];
-                            if (ty == SSTMC_SCATTERING_ISOTROPIC) pdf = S.iso_pdf;
-                            else if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
-                                const float g = S.g[mb], omg = 1.0f - g;
-                                const float rr = rsqrtf(fmaf(g, q2, omg * omg));
-                                pdf = S.dims == 2 ? S.gup[mb] * rr * rr : S.gup[mb] * rr * rr * rr;
-                            } else pdf = 0.0f;
-                        }
+                        const float pdf = three ? r.c * rr * rr * rr : r.c * rr * rr;
                         // decorrelation exp(-k^2 |t| (D_b |q|^2 + MT_b)), q = u_b - o (TemporalSamplerCorrelation.cuh:384-450)
-                        const float ck = fmaf(S.k2 * S.D[mb], q2, r.mt);
-                        const float base_w = w * pdf;
+                        const float ck = fmaf(r.k2d, q2, r.mt);
+                        const float bw = w * pdf;
+                        const unsigned long long b2 = pk2(bw, bw);
                         if (geo) {
                             const float es = __expf(-ck * tk[0]);
-                            float e = t0 == 0 ? es : __expf(-ck * tk[t0]);
+                            const float e0 = t0 == 0 ? es : __expf(-ck * tk[t0]);
+                            const float es2 = es * es;
+                            unsigned long long e = pk2(e0, e0 * es);
+                            const unsigned long long st = pk2(es2, es2);
 #pragma unroll
-                            for (int k = 0; k < kNT; ++k)
-                                if (k < tn) { acc[j][k] = fmaf(base_w, e, acc[j][k]); e *= es; }
+                            for (int k = 0; k < kNT / 2; ++k) {
+                                acc[j][k] = fma2(b2, e, acc[j][k]);
+                                if (k + 1 < kNT / 2) e = mul2(e, st);
+                            }
                         } else {
 #pragma unroll
-                            for (int k = 0; k < kNT; ++k)
-                                if (k < tn) acc[j][k] = fmaf(base_w, __expf(-ck * tk[t0 + k]), acc[j][k]);
+                            for (int k = 0; k < kNT / 2; ++k) {
+                                const int ta = t0 + min(2 * k, tn - 1), tb = t0 + min(2 * k + 1, tn - 1);
+                                acc[j][k] = fma2(b2, pk2(__expf(-ck * tk[ta]), __expf(-ck * tk[tb])), acc[j][k]);
+                            }
                         }
                     } else {
                         // g f exp(2 pi i (phase of g + L_b / lambda + xi_b))
                         float a, f;
                         if constexpr (VWP) {
                             float at = __expf(-tau);
-                            at = S.dims == 3 ? __fdividef(at * kIsoAmp3, r2) : at * rsqrtf(r2);
-                            if (vw.is_area) at *= fabsf(S.dims == 3 ? sub3(xb, sv).z : sub3(xb, sv).y) * rsqrtf(r2);
+                            at = three ? at * kIsoAmp3 * ri * ri : at * ri;
+                            if (vw.is_area) at *= fabsf(three ? o.z : o.y);
                             a = sqrtf(at);
                             if (split) {
-                                const double dx = (double)xb.x - (double)sv.x, dy = (double)xb.y - (double)sv.y, dz = (double)xb.z - (double)sv.z;
+                                const double dx = (double)xb.x - (double)sv[j].x, dy = (double)xb.y - (double)sv[j].y,
+                                             dz = (double)xb.z - (double)sv[j].z;
                                 const double ph = sqrt(fma(dx, dx, fma(dy, dy, dz * dz))) * S.inv_lambda + r.ph;
                                 f = (float)(ph - rint(ph));
                             } else {
-                                const float ph = sqrtf(r2) * S.inv_lambda_f + (float)r.ph;
+                                const float ph = __fdividef(1.0f, ri) * S.inv_lambda_f + (float)r.ph;
                                 f = ph - rintf(ph);
                             }
                         } else {
@@ -228,22 +444,11 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                                 f = ph - rintf(ph);
                             }
                         }
-                        float amp;
-                        if (VWP && S.iso_all) amp = S.iso_amp;
-                        else {
-                            const int ty = S.scat_type[mb];
-                            if (ty == SSTMC_SCATTERING_ISOTROPIC) amp = S.iso_amp;
-                            else if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
-                                const float g = S.g[mb], omg = 1.0f - g;
-                                const float rr = rsqrtf(fmaf(g, q2, omg * omg));
-                                amp = S.dims == 2 ? S.sgup[mb] * rr : S.sgup[mb] * rr * sqrtf(rr);
-                            } else amp = 0.0f;
-                        }
+                        const float amp = three ? r.c * rr * sqrtf(rr) : r.c * rr;
                         float sp, cp;
                         sincospif(2.0f * f, &sp, &cp);
                         const float m = a * amp;
-                        acc[j][0] = fmaf(m, cp, acc[j][0]);
-                        acc[j][1] = fmaf(m, sp, acc[j][1]);
+                        acc[j][0] = fma2(pk2(m, m), pk2(cp, sp), acc[j][0]);
                     }
                 }
             }
@@ -253,14 +458,17 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
 #pragma unroll
         for (int j = 0; j < kVPL; ++j) {
             const int vi = lane + 32 * j;
-            if (vi >= nv) break;
+            if (j >= vpl || vi >= nv) break;
             const int v = T.v0 + vi;
             if constexpr (CORR) {
 #pragma unroll
                 for (int k = 0; k < kNT; ++k)
-                    if (k < tn) T.s_ms[((size_t)q * Nt + t0 + k) * Nv + v] = make_float2(acc[j][k], 0.0f);
+                    if (k < tn) {
+                        const float a = (k & 1) ? pk_hi(acc[j][k >> 1]) : pk_lo(acc[j][k >> 1]);
+                        T.s_ms[((size_t)q * Nt + t0 + k) * Nv + v] = make_float2(a, 0.0f);
+                    }
             } else {
-                const float2 c = make_float2(acc[j][0], acc[j][1]);
+                const float2 c = make_float2(pk_lo(acc[j][0]), pk_hi(acc[j][0]));
                 for (int t = t0; t < t0 + tn; ++t) T.s_ms[((size_t)q * Nt + t) * Nv + v] = c;
             }
         }
@@ -293,11 +501,36 @@ int launch_view(const DevScene& S, const TraceParams& T, int blocks, int threads
     const size_t smem = view_smem_bytes(S.Nt, threads);
     const bool vp = S.src[1].type == SSTMC_SOURCE_POINT;
     using Fn = void (*)(DevScene, TraceParams);
-    Fn f = S.correlation ? (vp ? (Fn)view_kernel<true, true> : (Fn)view_kernel<true, false>)
-                         : (vp ? (Fn)view_kernel<false, true> : (Fn)view_kernel<false, false>);
+    Fn f;
+    if (S.single)
+        f = S.correlation ? (vp ? (Fn)view_kernel<true, true, true> : (Fn)view_kernel<true, false, true>)
+                          : (vp ? (Fn)view_kernel<false, true, true> : (Fn)view_kernel<false, false, true>);
+    else
+        f = S.correlation ? (vp ? (Fn)view_kernel<true, true, false> : (Fn)view_kernel<true, false, false>)
+                          : (vp ? (Fn)view_kernel<false, true, false> : (Fn)view_kernel<false, false, false>);
     if (smem > 48 * 1024 && cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SSTMC_KERNEL_ERROR;
     f<<<blocks, threads, smem, stream>>>(S, T);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
+
+bool illum_kernel_covers(const DevScene& S)
+{
+    return S.correlation && S.sym && S.all_static_corr && S.src[0].n <= 32 * kMaxIllum;
+}
+
+int launch_illum(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream)
+{
+    const bool ip = S.src[0].type == SSTMC_SOURCE_POINT, vp = S.src[1].type == SSTMC_SOURCE_POINT;
+    using Fn = void (*)(DevScene, TraceParams);
+    Fn f;
+    if (S.src[0].n <= 64)
+        f = ip ? (vp ? (Fn)illum_kernel<2, true, true> : (Fn)illum_kernel<2, true, false>)
+               : (vp ? (Fn)illum_kernel<2, false, true> : (Fn)illum_kernel<2, false, false>);
+    else
+        f = ip ? (vp ? (Fn)illum_kernel<kMaxIllum, true, true> : (Fn)illum_kernel<kMaxIllum, true, false>)
+               : (vp ? (Fn)illum_kernel<kMaxIllum, false, true> : (Fn)illum_kernel<kMaxIllum, false, false>);
+    f<<<blocks, threads, 0, stream>>>(S, T);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 

@@ -17,5 +17,10 @@ int view_max_views();
 size_t view_smem_bytes(int Nt, int threads);
 // S[q][t][v] for t in [T.t0, T.t0 + T.tn), v in [T.v0, T.v0 + T.vn).
 int launch_view(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream);
+// Illumination side (P_l, a_ms, a_ss, b_ss, first-vertex stats) of the
+// correlation sampler with identical u1 / u2 sources and static scatterers,
+// Nl <= 256.
+bool illum_kernel_covers(const DevScene& S);
+int launch_illum(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream);
 
 }  // namespace sstmc
