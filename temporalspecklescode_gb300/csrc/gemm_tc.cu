@@ -12,18 +12,19 @@
 // Each FP32 operand x is split into TF32 parts hi = rna(x), lo = rna(x - hi),
 // and D accumulates hi*hi + hi*lo + lo*hi.
 //
-// One CTA owns a 128 x 64 tile of D for one tick and a range of paths:
-//   thread 0    issues TMA box loads (cp.async.bulk.tensor) of 32 paths x
-//               128 A rows and 32 paths x 64 B rows into a 3-deep raw ring;
-//   warps 0-2   split each raw box into TF32 hi / lo tiles stored in the
+// One CTA owns a 128 x 128 tile of D for one tick and a range of paths:
+//   warp 0      allocates tensor memory; one thread issues the TMA box loads
+//               (cp.async.bulk.tensor, 32 paths x 128 rows of A and of B)
+//               into a 3-deep raw ring and the tcgen05.mma (M = N = 128,
+//               K = 8) into one of two TMEM accumulators;
+//   warps 1-8   split each raw box into TF32 hi / lo tiles stored in the
 //               128-byte-swizzled K-major layout the MMA descriptors
-//               describe (3-deep ring);
-//   warp 3      allocates tensor memory; one thread issues tcgen05.mma
-//               (M = 128, N = 64, K = 8) into one of two TMEM accumulators;
-//   warps 4-11  drain an accumulator every 128 paths (tcgen05.ld) into
-//               compensated FP32 pairs (TwoSum), so FP32 rounding grows with
-//               a 128-path window rather than with the whole path range,
-//               and add the tile to V with FP64 atomics at the end.
+//               describe (2-deep ring), one 8-path group per warp;
+//   warps 9-12  drain an accumulator every 128 paths into compensated FP32
+//               (hi, lo) pairs kept in tensor memory too (TwoSum), so FP32
+//               rounding grows with a 128-path window rather than with the
+//               whole path range, and add the tile to V with FP64 atomics
+//               at the end.
 // Every mbarrier wait is bounded; a wait that runs out sets SSTMC_TIMEOUT in
 // the error word, and every role then leaves its loop, waits for the MMAs it
 // issued and frees the tensor memory.
@@ -41,26 +42,26 @@ namespace sstmc {
 namespace {
 
 constexpr int kTM = 128;          // D rows per CTA (64 illumination entries, re / im)
-constexpr int kTN = 64;           // D columns per CTA (32 view entries, re / im)
+constexpr int kTN = 128;          // D columns per CTA (64 view entries, re / im)
 constexpr int kKS = 32;           // paths per step: one 128-byte swizzle row of TF32
-constexpr int kStages = 3;        // hi / lo tiles in flight to the MMA
+constexpr int kStages = 2;        // hi / lo tiles in flight to the MMA
 constexpr int kRaw = 3;           // raw TMA boxes in flight from global memory
 constexpr int kWinSteps = 4;      // steps per accumulation window (128 paths)
-constexpr int kLoadWarps = 3;
-constexpr int kMmaWarp = kLoadWarps;
-constexpr int kEpiWarp0 = kLoadWarps + 1;
-constexpr int kEpiWarps = 8;
-constexpr int kThreads = (kLoadWarps + 1 + kEpiWarps) * 32;  // 384
-constexpr int kLoadThreads = kLoadWarps * 32;
+constexpr int kSplitWarps = 8;
+constexpr int kEpiWarps = 4;
+constexpr int kThreads = (1 + kSplitWarps + kEpiWarps) * 32;  // 416
+constexpr int kSplitThreads = kSplitWarps * 32;
 constexpr int kEpiThreads = kEpiWarps * 32;
 constexpr uint32_t kATile = kTM * kKS * 4;                   // 16 KB
-constexpr uint32_t kBTile = kTN * kKS * 4;                   // 8 KB
-constexpr uint32_t kStageBytes = 2 * kATile + 2 * kBTile;    // 48 KB: A hi, A lo, B hi, B lo
+constexpr uint32_t kBTile = kTN * kKS * 4;                   // 16 KB
+constexpr uint32_t kStageBytes = 2 * kATile + 2 * kBTile;    // 64 KB: A hi, A lo, B hi, B lo
 constexpr uint32_t kRawA = kKS * kTM * 4;                    // 16 KB: 32 paths x 128 floats
-constexpr uint32_t kRawBytes = kRawA + kKS * kTN * 4;        // + 8 KB: 32 paths x 64 floats
+constexpr uint32_t kRawBytes = kRawA + kKS * kTN * 4;        // + 16 KB: 32 paths x 128 floats
 constexpr uint32_t kBarBytes = 256;
 constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + (size_t)kRaw * kRawBytes + kBarBytes + 1024;
-constexpr uint32_t kTmemCols = 2 * kTN;                      // two accumulators
+// tensor memory: two accumulators, then the compensated hi and lo sums
+constexpr uint32_t kColD = 0, kColHi = 2 * kTN, kColLo = 3 * kTN;
+constexpr uint32_t kTmemCols = 4 * kTN;                      // 512: all of it
 constexpr unsigned long long kWaitNs = 2000000000ull;        // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
@@ -188,6 +189,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&r)[16])
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&r)[16])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+        ::"r"(taddr), "r"(__float_as_uint(r[0])), "r"(__float_as_uint(r[1])), "r"(__float_as_uint(r[2])), "r"(__float_as_uint(r[3])),
+          "r"(__float_as_uint(r[4])), "r"(__float_as_uint(r[5])), "r"(__float_as_uint(r[6])), "r"(__float_as_uint(r[7])),
+          "r"(__float_as_uint(r[8])), "r"(__float_as_uint(r[9])), "r"(__float_as_uint(r[10])), "r"(__float_as_uint(r[11])),
+          "r"(__float_as_uint(r[12])), "r"(__float_as_uint(r[13])), "r"(__float_as_uint(r[14])), "r"(__float_as_uint(r[15]))
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // byte offset of (row, 16-byte chunk) in a K-major 128-byte-swizzled tile
 __device__ __forceinline__ uint32_t sw128(uint32_t row, uint32_t chunk)
 {
@@ -240,30 +254,30 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm,
         : "memory");
 }
 
-// One thread's share of a step: 8 units of (row, 8 consecutive paths) read
-// from the raw box (RS floats per path), split into TF32 hi / lo and stored
-// as two 16-byte chunks of the swizzled hi and lo tiles.
-template <int RS>
-__device__ __forceinline__ void split_rows(const float* raw, unsigned char* hi_tile, uint32_t lo_delta, uint32_t valid,
-                                           const int (&src_off)[8], const uint32_t (&dst_off)[8])
+// One thread's share of a step: 4 rows (row0 + 32 r) of one 8-path group
+// kq, read from the raw box (128 floats per path), split into TF32 hi / lo
+// and stored as two 16-byte chunks of the swizzled hi and lo tiles.
+__device__ __forceinline__ void split_group(const float* raw, unsigned char* hi_tile, uint32_t lo_delta, uint32_t valid,
+                                            int row0, int kq)
 {
+    const uint32_t vq = (valid >> (8 * kq)) & 0xffu;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const float* src = raw + src_off[k];
+    for (int r = 0; r < 4; ++r) {
+        const int row = row0 + 32 * r;
+        const float* src = raw + kq * 8 * 128 + row;
         float x[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = src[j * RS];
-        if (valid != 0xffffffffu) {
-            const int kq8 = (src_off[k] / RS) & ~7;   // first path of this unit
-            const uint32_t vq = (valid >> kq8) & 0xffu;
+        for (int j = 0; j < 8; ++j) x[j] = src[j * 128];
+        if (vq != 0xffu) {
 #pragma unroll
             for (int j = 0; j < 8; ++j) x[j] = ((vq >> j) & 1u) ? x[j] : 0.0f;
         }
         float h[8], l[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) split_tf32(x[j], h[j], l[j]);
-        unsigned char* d0 = hi_tile + dst_off[k];
-        unsigned char* d1 = hi_tile + (dst_off[k] ^ 16u);
+        const uint32_t o0 = sw128((uint32_t)row, (uint32_t)(2 * kq));
+        unsigned char* d0 = hi_tile + o0;
+        unsigned char* d1 = hi_tile + (o0 ^ 16u);
         *reinterpret_cast<float4*>(d0) = make_float4(h[0], h[1], h[2], h[3]);
         *reinterpret_cast<float4*>(d1) = make_float4(h[4], h[5], h[6], h[7]);
         *reinterpret_cast<float4*>(d0 + lo_delta) = make_float4(l[0], l[1], l[2], l[3]);
@@ -308,8 +322,8 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
     const int m0 = tm * kTM, n0 = tn * kTN;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) { mbar_init(full_bar(s), kLoadThreads); mbar_init(empty_bar(s), 1); }
-        for (int r = 0; r < kRaw; ++r) { mbar_init(rfull_bar(r), 1); mbar_init(rempty_bar(r), kLoadThreads); }
+        for (int s = 0; s < kStages; ++s) { mbar_init(full_bar(s), kSplitThreads); mbar_init(empty_bar(s), 1); }
+        for (int r = 0; r < kRaw; ++r) { mbar_init(rfull_bar(r), 1); mbar_init(rempty_bar(r), kSplitThreads); }
         for (int b = 0; b < 2; ++b) { mbar_init(accfull_bar(b), 1); mbar_init(accempty_bar(b), kEpiThreads); }
         mbar_init(done_bar, 1);
         *abort = 0;
@@ -318,7 +332,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&P.tmA)) : "memory");
         asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&P.tmB)) : "memory");
     }
-    if (warp == kMmaWarp) {
+    if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -327,74 +341,33 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp < kLoadWarps) {
-        // ---------------- TMA producer (one thread) + split warps ----------------
-        const bool producer = threadIdx.x == 0;
-        int issued_raw = 0;
-        auto issue = [&](int j) -> bool {   // raw boxes of step j
-            const int r = j % kRaw;
-            if (j >= kRaw && !mbar_wait(rempty_bar(r), (uint32_t)((j / kRaw) - 1) & 1u, abort, G.err)) return false;
-            const uint32_t dst = raw_base + (uint32_t)r * kRawBytes;
-            mbar_expect_tx(rfull_bar(r), kRawBytes);
-            const int p0 = kb + j * kKS;
-            tma_load_3d(dst, &P.tmA, m0, t, p0, rfull_bar(r));
-            tma_load_3d(dst + kRawA, &P.tmB, n0, t, p0, rfull_bar(r));
-            issued_raw = j + 1;
-            return true;
-        };
-        bool ok = true;
-        if (producer)
-            for (int j = 0; j < min(kRaw - 1, nsteps) && ok; ++j) ok = issue(j);
-        // units of this thread: warps 0 and 1 split A (128 rows x 4 groups of
-        // 8 paths: rows lane + 32 (k & 3), groups 2 warp + k / 4), warp 2 splits
-        // B (64 rows x 4 groups: rows lane + 32 (k & 1), group k / 2)
-        int src_off[8];
-        uint32_t dst_off[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int row = warp < 2 ? lane + 32 * (k & 3) : lane + 32 * (k & 1);
-            const int kq = warp < 2 ? 2 * warp + (k >> 2) : (k >> 1);
-            src_off[k] = kq * 8 * (warp < 2 ? kTM : kTN) + row;
-            dst_off[k] = sw128((uint32_t)row, (uint32_t)(2 * kq));
-        }
-        for (int i = 0; i < nsteps; ++i) {
-            if (producer && ok && i + kRaw - 1 < nsteps) ok = issue(i + kRaw - 1);
-            const int r = i % kRaw, s = i % kStages;
-            if (!mbar_wait(rfull_bar(r), (uint32_t)(i / kRaw) & 1u, abort, G.err)) break;
-            if (i >= kStages && !mbar_wait(empty_bar(s), (uint32_t)((i / kStages) - 1) & 1u, abort, G.err)) break;
-            const int pbase = kb + i * kKS;
-            // paths of this step that count: inside [kb, ke) and of the selected material
-            const int nin = min(kKS, ke - pbase);
-            uint32_t valid = nin >= kKS ? 0xffffffffu : ((1u << nin) - 1u);
-            if (G.mat)
-                for (int j = 0; j < nin; ++j)
-                    if (G.mat[pbase + j] != G.mat_sel) valid &= ~(1u << j);
-            const float* rawf = reinterpret_cast<const float*>(smem + (size_t)kStages * kStageBytes + (size_t)r * kRawBytes);
-            unsigned char* stp = smem + (size_t)s * kStageBytes;
-            if (warp < 2) split_rows<kTM>(rawf, stp, kATile, valid, src_off, dst_off);
-            else split_rows<kTN>(rawf + kRawA / 4, stp + 2 * kATile, kBTile, valid, src_off, dst_off);
-            fence_proxy_async();
-            mbar_arrive(full_bar(s));
-            mbar_arrive(rempty_bar(r));
-        }
-        // every raw box this thread issued must land before the CTA ends
-        if (producer && nsteps > 0) {
-            for (int j = max(0, issued_raw - kRaw); j < issued_raw; ++j)
-                mbar_wait(rfull_bar(j % kRaw), (uint32_t)(j / kRaw) & 1u, abort, G.err, false);
-        }
-    } else if (warp == kMmaWarp) {
-        // ---------------- MMA issuer ----------------
+    if (warp == 0) {
+        // ---------------- TMA producer + MMA issuer (one thread) ----------------
         if (lane == 0) {
-            int issued = 0;
-            for (int i = 0; i < nsteps; ++i) {
+            int issued_raw = 0, issued = 0;
+            bool ok = true;
+            auto issue_raw = [&](int j) -> bool {
+                const int r = j % kRaw;
+                if (j >= kRaw && !mbar_wait(rempty_bar(r), (uint32_t)((j / kRaw) - 1) & 1u, abort, G.err)) return false;
+                const uint32_t dst = raw_base + (uint32_t)r * kRawBytes;
+                mbar_expect_tx(rfull_bar(r), kRawBytes);
+                const int p0 = kb + j * kKS;
+                tma_load_3d(dst, &P.tmA, m0, t, p0, rfull_bar(r));
+                tma_load_3d(dst + kRawA, &P.tmB, n0, t, p0, rfull_bar(r));
+                issued_raw = j + 1;
+                return true;
+            };
+            for (int j = 0; j < min(kRaw - 1, nsteps) && ok; ++j) ok = issue_raw(j);
+            for (int i = 0; i < nsteps && ok; ++i) {
+                if (i + kRaw - 1 < nsteps && !issue_raw(i + kRaw - 1)) { ok = false; break; }
                 const int s = i % kStages;
-                if (!mbar_wait(full_bar(s), (uint32_t)(i / kStages) & 1u, abort, G.err)) break;
+                if (!mbar_wait(full_bar(s), (uint32_t)(i / kStages) & 1u, abort, G.err)) { ok = false; break; }
                 const int w = i / kWinSteps, b = w & 1;
                 const bool first = (i % kWinSteps) == 0;
-                if (first && w >= 2 && !mbar_wait(accempty_bar(b), (uint32_t)((w >> 1) - 1) & 1u, abort, G.err)) break;
+                if (first && w >= 2 && !mbar_wait(accempty_bar(b), (uint32_t)((w >> 1) - 1) & 1u, abort, G.err)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t st = split_base + (uint32_t)s * kStageBytes;
-                const uint32_t d = tmem + (uint32_t)(b * kTN);
+                const uint32_t d = tmem + kColD + (uint32_t)(b * kTN);
 #pragma unroll
                 for (int k = 0; k < kKS / 8; ++k) {
                     const uint64_t ah = sdesc(st + 32u * k), al = sdesc(st + kATile + 32u * k);
@@ -407,38 +380,77 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
                 mma_commit(empty_bar(s));
                 if ((i % kWinSteps) == kWinSteps - 1 || i == nsteps - 1) mma_commit(accfull_bar(b));
             }
-            // every MMA issued by this thread has completed once done_bar flips
+            // every MMA issued here has completed once done_bar flips; every raw
+            // box issued here has landed once its rfull phase completed
             if (issued) {
                 mma_commit(done_bar);
                 mbar_wait(done_bar, 0u, abort, G.err, false);
             }
+            for (int j = max(0, issued_raw - kRaw); j < issued_raw; ++j)
+                mbar_wait(rfull_bar(j % kRaw), (uint32_t)(j / kRaw) & 1u, abort, G.err, false);
         }
         __syncwarp();
+    } else if (warp <= kSplitWarps) {
+        // ---------------- split warps: one 8-path group of A or B each ----------------
+        const int sw = warp - 1;
+        const bool isA = sw < 4;
+        const int kq = sw & 3;
+        for (int i = 0; i < nsteps; ++i) {
+            const int r = i % kRaw, s = i % kStages;
+            if (!mbar_wait(rfull_bar(r), (uint32_t)(i / kRaw) & 1u, abort, G.err)) break;
+            if (i >= kStages && !mbar_wait(empty_bar(s), (uint32_t)((i / kStages) - 1) & 1u, abort, G.err)) break;
+            const int pbase = kb + i * kKS;
+            // paths of this step that count: inside [kb, ke) and of the selected material
+            const int nin = min(kKS, ke - pbase);
+            uint32_t valid = nin >= kKS ? 0xffffffffu : ((1u << nin) - 1u);
+            if (G.mat)
+                for (int j = 0; j < nin; ++j)
+                    if (G.mat[pbase + j] != G.mat_sel) valid &= ~(1u << j);
+            const float* rawf = reinterpret_cast<const float*>(smem + (size_t)kStages * kStageBytes + (size_t)r * kRawBytes);
+            unsigned char* stp = smem + (size_t)s * kStageBytes;
+            if (isA) split_group(rawf, stp, kATile, valid, lane, kq);
+            else split_group(rawf + kRawA / 4, stp + 2 * kATile, kBTile, valid, lane, kq);
+            fence_proxy_async();
+            mbar_arrive(full_bar(s));
+            mbar_arrive(rempty_bar(r));
+        }
     } else {
-        // ---------------- accumulator drain ----------------
-        const int e = warp - kEpiWarp0;
-        const int q = warp & 3;          // TMEM lane quadrant this warp may access
-        const int h = e >> 2;            // column half (0: columns 0-31, 1: 32-63)
-        float hi[32], lo[32];
+        // ---------------- accumulator drain (lane quadrant warp & 3) ----------------
+        const int q = warp & 3;
+        const uint32_t row_addr = tmem + ((uint32_t)(32 * q) << 16);
+        {
+            float z[16];
 #pragma unroll
-        for (int c = 0; c < 32; ++c) { hi[c] = 0.0f; lo[c] = 0.0f; }
+            for (int c = 0; c < 16; ++c) z[c] = 0.0f;
+#pragma unroll
+            for (int c = 0; c < kTN / 16; ++c) { tmem_st16(row_addr + kColHi + 16u * c, z); tmem_st16(row_addr + kColLo + 16u * c, z); }
+            tmem_wait_st();
+        }
         const int nwin = (nsteps + kWinSteps - 1) / kWinSteps;
         bool ok = true;
         for (int w = 0; w < nwin && ok; ++w) {
             const int b = w & 1;
             ok = mbar_wait(accfull_bar(b), (uint32_t)(w >> 1) & 1u, abort, G.err, true, true);
-            ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld and the final shuffles need the whole warp
+            ok = __all_sync(0xffffffffu, ok);   // tcgen05.ld / st and the final shuffles need the whole warp
             if (!ok) break;
             tc_fence_after();
-            const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * kTN + h * 32);
-            float r0[16], r1[16];
-            tmem_ld16(ta, r0);
-            tmem_ld16(ta + 16u, r1);
-            tmem_wait_ld();
-            tc_fence_before();
-            mbar_arrive(accempty_bar(b));
+#pragma unroll 1
+            for (int c = 0; c < kTN / 16; ++c) {
+                float dv[16], hv[16], lv[16];
+                tmem_ld16(row_addr + kColD + (uint32_t)(b * kTN) + 16u * c, dv);
+                tmem_ld16(row_addr + kColHi + 16u * c, hv);
+                tmem_ld16(row_addr + kColLo + 16u * c, lv);
+                tmem_wait_ld();
+                if (c == kTN / 16 - 1) {   // the accumulator has been read: the MMA may reuse it
+                    tc_fence_before();
+                    mbar_arrive(accempty_bar(b));
+                }
 #pragma unroll
-            for (int c = 0; c < 16; ++c) { two_sum(hi[c], lo[c], r0[c]); two_sum(hi[16 + c], lo[16 + c], r1[c]); }
+                for (int e = 0; e < 16; ++e) two_sum(hv[e], lv[e], dv[e]);
+                tmem_st16(row_addr + kColHi + 16u * c, hv);
+                tmem_st16(row_addr + kColLo + 16u * c, lv);
+            }
+            tmem_wait_st();
         }
         if (ok && nwin > 0) {
             // rows m (even: Re a, odd: Im a) pair up across adjacent lanes
@@ -446,17 +458,24 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
             const int gm = m0 + m;
             const int l = gm >> 1;
             const bool odd = (gm & 1) != 0;
+#pragma unroll 1
+            for (int c = 0; c < kTN / 16; ++c) {
+                float hv[16], lv[16];
+                tmem_ld16(row_addr + kColHi + 16u * c, hv);
+                tmem_ld16(row_addr + kColLo + 16u * c, lv);
+                tmem_wait_ld();
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const double own = (double)hi[2 * j] + (double)lo[2 * j];
-                const double send = (double)hi[2 * j + 1] + (double)lo[2 * j + 1];
-                const double r = __shfl_xor_sync(0xffffffffu, send, 1);
-                const double val = odd ? own + r : own - r;   // odd: Im V = D[2l][2v+1] + D[2l+1][2v]; even: Re V
-                const int v = (n0 + h * 32 + 2 * j) >> 1;
-                if (l < G.Nl && v < G.Nv) {
-                    const size_t o = ((size_t)t * G.Nv + v) * G.Nl + l;
-                    const double wv = G.W ? (double)G.W[o] : 1.0;
-                    atomicAdd(odd ? &G.V[o].y : &G.V[o].x, val * wv);
+                for (int j = 0; j < 8; ++j) {
+                    const double own = (double)hv[2 * j] + (double)lv[2 * j];
+                    const double send = (double)hv[2 * j + 1] + (double)lv[2 * j + 1];
+                    const double r = __shfl_xor_sync(0xffffffffu, send, 1);
+                    const double val = odd ? own + r : own - r;   // odd: Im V = D[2l][2v+1] + D[2l+1][2v]; even: Re V
+                    const int v = (n0 + 16 * c + 2 * j) >> 1;
+                    if (l < G.Nl && v < G.Nv) {
+                        const size_t o = ((size_t)t * G.Nv + v) * G.Nl + l;
+                        const double wv = G.W ? (double)G.W[o] : 1.0;
+                        atomicAdd(odd ? &G.V[o].y : &G.V[o].x, val * wv);
+                    }
                 }
             }
         }
@@ -464,7 +483,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
 
     tc_fence_before();
     __syncthreads();
-    if (warp == kMmaWarp) {
+    if (warp == 0) {
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
     }
