@@ -295,9 +295,10 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* accc = reinterpret_cast<float2*>(smem_raw);                       // [4*kFt][256] compensated (hi, lo) window sums
     float4* sI = reinterpret_cast<float4*>(accc + 4 * kFt * 256);            // [kFk][kFl] (direction in, row x material coefficient)
-    float4* sO = sI + kFk * kFl;                                              // [kFk][kFv] (direction out, row)
-    float2* sM = reinterpret_cast<float2*>(sO + kFk * kFv);                   // [kFk] (g, omg2) ...
+    float* sO = reinterpret_cast<float*>(sI + kFk * kFl);                     // [kFk][4][kFv] (x, y, z, row), views contiguous
+    float2* sM = reinterpret_cast<float2*>(sO + kFk * 4 * kFv);               // [kFk] (g, omg2)
     float* sC = reinterpret_cast<float*>(sM + kFk);                           // [kFk] c = k^2 D
+    // thread: illumination elements l0 + tx + 16 i, view pair v0 + 2 ty + (0, 1)
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int l0 = blockIdx.x * kFl, v0 = blockIdx.y * kFv;
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
@@ -310,6 +311,7 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     const DevSource& vw = S.src[1];
     const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
     const float tau0 = S.abs_ticks[0], taus = S.abs_ticks[t0];
+    const unsigned long long neg1 = pk2(-1.0f, -1.0f);
     unsigned long long acc[2][2][kFt / 2];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
@@ -320,11 +322,34 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
 #pragma unroll
             for (int t = 0; t < kFt; ++t) accc[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = make_float2(0.f, 0.f);
         }
+    // staging items of a chunk: 4 per thread, idx = threadIdx.x + 256 u
+    // (u = 0, 1: illumination elements; u = 2, 3: view elements).  The next
+    // chunk's global loads are issued before the current chunk is computed.
+    float px[4], py[4], pz[4], pv[4];
+    int pm[4];
+    int mm = 0;
+    auto prefetch = [&](int k) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int idx = threadIdx.x + 256 * u;
+            const bool isI = u < 2;
+            const int r = isI ? idx : idx - kFk * kFl;
+            const int pp = r / kFl, c = r % kFl;
+            const int p = k + pp;
+            const int pc = min(p, ke - 1);
+            px[u] = G.x1[3 * pc]; py[u] = G.x1[3 * pc + 1]; pz[u] = G.x1[3 * pc + 2];
+            pm[u] = (int)G.m1[pc];
+            pv[u] = 0.f;
+            if (isI) { if (p < ke && l0 + c < Nl) pv[u] = G.a[(size_t)p * Nt * Nl + l0 + c].x; }
+            else if (p < ke && v0 + c < Nv) pv[u] = G.b[(size_t)p * Nt * Nv + v0 + c].x;
+        }
+        mm = (threadIdx.x < kFk && k + (int)threadIdx.x < ke) ? (int)G.m1[k + threadIdx.x] : 0;
+    };
+    prefetch(kb);
     int chunk = 0;
     for (int k = kb; k < ke; k += kFk, ++chunk) {
         if (threadIdx.x < kFk) {
-            const int p = k + threadIdx.x;
-            const int m = p < ke ? (int)G.m1[p] : 0;
+            const int m = mm;
             const int ty_ = S.scat_type[m];
             float g = 0.f, omg2 = 1.f, c = 0.f;
             if (m != 0 && !scalar_fs) {
@@ -334,57 +359,63 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             sM[threadIdx.x] = make_float2(g, omg2);
             sC[threadIdx.x] = c;
         }
-        for (int idx = threadIdx.x; idx < kFk * (kFl + kFv); idx += 256) {
-            const bool isI = idx < kFk * kFl;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int idx = threadIdx.x + 256 * u;
+            const bool isI = u < 2;
             const int r = isI ? idx : idx - kFk * kFl;
             const int pp = r / kFl, c = r % kFl;
             const int p = k + pp;
-            const int pc = min(p, ke - 1);
-            const V3 x = V3{ G.x1[3 * pc], G.x1[3 * pc + 1], G.x1[3 * pc + 2] };
-            float val = 0.f;
-            V3 dir;
+            const V3 x = V3{ px[u], py[u], pz[u] };
             if (isI) {
-                if (p < ke && l0 + c < Nl) {
-                    // row value times the material's pdf coefficient
-                    const int m = (int)G.m1[p];
-                    const int ty_ = S.scat_type[m];
-                    const float coef = m == 0 ? 0.0f
-                                     : scalar_fs ? S.iso_amp * S.iso_amp
-                                     : ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN ? S.gup[m]
-                                     : ty_ == SSTMC_SCATTERING_ISOTROPIC ? S.iso_pdf : 0.0f;
-                    val = G.a[(size_t)p * Nt * Nl + l0 + c].x * coef;
-                }
-                dir = fsrc_in(il, min(l0 + c, Nl - 1), x);
-                sI[r] = make_float4(dir.x, dir.y, dir.z, val);
+                // row value times the material's pdf coefficient
+                const int m = pm[u];
+                const int ty_ = S.scat_type[m];
+                const float coef = (p >= ke || m == 0) ? 0.0f
+                                 : scalar_fs ? S.iso_amp * S.iso_amp
+                                 : ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN ? S.gup[m]
+                                 : ty_ == SSTMC_SCATTERING_ISOTROPIC ? S.iso_pdf : 0.0f;
+                const V3 dir = fsrc_in(il, min(l0 + c, Nl - 1), x);
+                sI[r] = make_float4(dir.x, dir.y, dir.z, pv[u] * coef);
             } else {
-                if (p < ke && v0 + c < Nv) val = G.b[(size_t)p * Nt * Nv + v0 + c].x;
-                dir = fsrc_out(vw, min(v0 + c, Nv - 1), x);
-                sO[r] = make_float4(dir.x, dir.y, dir.z, val);
+                const V3 dir = fsrc_out(vw, min(v0 + c, Nv - 1), x);
+                float* o = sO + (size_t)pp * 4 * kFv + c;
+                o[0] = dir.x; o[kFv] = dir.y; o[2 * kFv] = dir.z; o[3 * kFv] = pv[u];
             }
         }
+        if (k + kFk < ke) prefetch(k + kFk);
         __syncthreads();
 #pragma unroll 2
         for (int pp = 0; pp < kFk; ++pp) {
             const float2 mc = sM[pp];
             const float cm = sC[pp];
-            const float4 iv[2] = { sI[pp * kFl + tx], sI[pp * kFl + tx + 16] };
-            const float4 ov[2] = { sO[pp * kFv + ty], sO[pp * kFv + ty + 16] };
+            const unsigned long long* op = reinterpret_cast<const unsigned long long*>(sO + (size_t)pp * 4 * kFv + 2 * ty);
+            const unsigned long long ox = op[0], oy = op[kFv / 2], oz = op[kFv], ob = op[3 * kFv / 2];
+            const unsigned long long g2 = pk2(mc.x, mc.x), omg = pk2(mc.y, mc.y), cq2 = pk2(cm, cm);
 #pragma unroll
-            for (int i = 0; i < 2; ++i)
+            for (int i = 0; i < 2; ++i) {
+                const float4 iv = sI[pp * kFl + tx + 16 * i];
+                // both views of the pair at once: q^2 = |in - out|^2, pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
+                const unsigned long long dx = fma2(ox, neg1, pk2(iv.x, iv.x));
+                const unsigned long long dy = fma2(oy, neg1, pk2(iv.y, iv.y));
+                const unsigned long long dz = fma2(oz, neg1, pk2(iv.z, iv.z));
+                const unsigned long long q2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+                const unsigned long long dn = fma2(g2, q2, omg);
+                const unsigned long long r = pk2(rsqrtf(pk_lo(dn)), rsqrtf(pk_hi(dn)));
+                const unsigned long long rr = mul2(r, r);
+                const unsigned long long base = mul2(mul2(THREE ? mul2(rr, r) : rr, ob), pk2(iv.w, iv.w));
+                const unsigned long long cq = mul2(cq2, q2);
 #pragma unroll
                 for (int j = 0; j < 2; ++j) {
-                    const float dx = iv[i].x - ov[j].x, dy = iv[i].y - ov[j].y, dz = iv[i].z - ov[j].z;
-                    const float q2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float r = rsqrtf(fmaf(mc.x, q2, mc.y));
-                    const float r2 = r * r;
-                    const float base = iv[i].w * ov[j].w * (THREE ? r2 * r : r2);
-                    const float cq = cm * q2;
+                    const float bj = j ? pk_hi(base) : pk_lo(base);
+                    const float cj = j ? pk_hi(cq) : pk_lo(cq);
+                    const unsigned long long b2 = pk2(bj, bj);
                     if (GEO) {
-                        const float es = __expf(-cq * tau0);
-                        const float e0 = t0 == 0 ? es : __expf(-cq * taus);
+                        const float es = __expf(-cj * tau0);
+                        const float e0 = t0 == 0 ? es : __expf(-cj * taus);
                         const float es2 = es * es;
                         unsigned long long e = pk2(e0, e0 * es);
-                        const unsigned long long st = pk2(es2, es2), b2 = pk2(base, base);
+                        const unsigned long long st = pk2(es2, es2);
 #pragma unroll
                         for (int tt = 0; tt < kFt / 2; ++tt) {
                             acc[i][j][tt] = fma2(b2, e, acc[i][j][tt]);
@@ -394,10 +425,11 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
 #pragma unroll
                         for (int tt = 0; tt < kFt / 2; ++tt) {
                             const int ta = min(t0 + 2 * tt, Nt - 1), tb = min(t0 + 2 * tt + 1, Nt - 1);
-                            acc[i][j][tt] = fma2(pk2(base, base), pk2(__expf(-cq * S.abs_ticks[ta]), __expf(-cq * S.abs_ticks[tb])), acc[i][j][tt]);
+                            acc[i][j][tt] = fma2(b2, pk2(__expf(-cj * S.abs_ticks[ta]), __expf(-cj * S.abs_ticks[tb])), acc[i][j][tt]);
                         }
                     }
                 }
+            }
         }
         __syncthreads();
         if ((chunk + 1) % 16 == 0) {
@@ -422,7 +454,7 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const int l = l0 + tx + 16 * i, v = v0 + ty + 16 * j;
+            const int l = l0 + tx + 16 * i, v = v0 + 2 * ty + j;
             if (l >= Nl || v >= Nv) continue;
 #pragma unroll
             for (int tt = 0; tt < kFt; ++tt) {
