@@ -230,7 +230,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         // far-field GEMM and the per-path debug trace read every tick
         const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD;
         T.ss_all_ticks = (dbg || farfar) ? 1 : 0;
-        if (illum_kernel_covers(S.dev)) e = launch_illum(S.dev, T, std::max(1, (int)((n + 3) / 4)), threads, stream);
+        if (illum_kernel_covers(S.dev)) e = launch_illum(S.dev, T, std::max(1, std::min((int)((n + 3) / 4), sms * 16)), threads, stream);
         else e = launch_trace(S.dev, T, blocks, threads, stream);
         if (e) return e;
         launches++;

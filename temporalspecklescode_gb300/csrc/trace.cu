@@ -226,6 +226,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
 
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long acc_v = 0, acc_s = 0, acc_m = 0, acc_p = 0;
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t pid = T.first_path + q;
         const uint32_t B = T.counts[q];
@@ -521,13 +522,20 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             if (T.pass0) {
                 if (T.m1) T.m1[q] = (unsigned char)m1;
                 if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
-                atomicAdd(T.totals + 0, (unsigned long long)B);
-                atomicAdd(T.totals + 2, (unsigned long long)T.misses[q]);
-                atomicAdd(T.totals + 3, 1ull);
+                acc_v += B;
+                acc_m += T.misses[q];
+                acc_p += 1;
             }
-            if (T.dda) atomicAdd(T.dda + q, wsteps);
-            atomicAdd(T.totals + 1, (unsigned long long)wsteps);
+            if (T.dda && wsteps) atomicAdd(T.dda + q, wsteps);
+            acc_s += wsteps;
         }
+    }
+    // one atomic per counter and warp (per-path atomics on four addresses serialise)
+    if (lane == 0) {
+        if (acc_v) atomicAdd(T.totals + 0, acc_v);
+        if (acc_s) atomicAdd(T.totals + 1, acc_s);
+        if (acc_m) atomicAdd(T.totals + 2, acc_m);
+        if (acc_p) atomicAdd(T.totals + 3, acc_p);
     }
 }
 

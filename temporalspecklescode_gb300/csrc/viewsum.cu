@@ -85,9 +85,48 @@ __device__ __forceinline__ float face_t(float d, float n0, float n1)
 // Lane l + 32 k of the path's warp.  Each row is written once; the
 // single-scattering rows are tick-invariant, so only tick 0 is written
 // unless every tick is asked for (T.ss_all_ticks).
-template <int NLK, bool ilp, bool vwp>
+// Optical depth from x toward the point s or along the direction d; single
+// cell: inside the box, one step to the face the ray heads for.
+template <bool SINGLE>
+__device__ __forceinline__ float tau_pt(const DevScene& S, const V3& x, const V3& sp, bool xin, uint32_t& st)
+{
+    if constexpr (SINGLE) {
+        if (!xin) return 0.0f;
+        st += 1;
+        return tau_single(S, x, funit(sub3(sp, x)));
+    } else {
+        return tau_to_point(S, x, sp, st);
+    }
+}
+
+template <bool SINGLE>
+__device__ __forceinline__ float tau_d(const DevScene& S, const V3& x, const V3& d, bool xin, uint32_t& st)
+{
+    if constexpr (SINGLE) {
+        if (!xin) return 0.0f;
+        st += 1;
+        return tau_single(S, x, d);
+    } else {
+        return tau_dir(S, x, d, st);
+    }
+}
+
+// Per-warp sums of the render statistics (lane 0 adds them to the global
+// counters once, when the warp has no paths left).
+struct WarpStats {
+    unsigned long long vertices = 0, steps = 0, misses = 0, paths = 0;
+    __device__ void flush(const TraceParams& T) const
+    {
+        if (vertices) atomicAdd(T.totals + 0, vertices);
+        if (steps) atomicAdd(T.totals + 1, steps);
+        if (misses) atomicAdd(T.totals + 2, misses);
+        if (paths) atomicAdd(T.totals + 3, paths);
+    }
+};
+
+template <int NLK, bool ilp, bool vwp, bool SINGLE>
 __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams& T, uint32_t q, int lane,
-                                           uint32_t B, const float4* vq)
+                                           uint32_t B, const float4* vq, const V3 (&lsrc)[NLK], WarpStats& ws_acc)
 {
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
     const DevSource& il = S.src[0];
@@ -107,6 +146,7 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
     const float4 v2 = vq[B >= 2 ? 1 : 0];
     const V3 x1 = V3{ v1.x, v1.y, v1.z };
     const int m1 = (int)(__float_as_uint(v1.w) & 15u);
+    const bool xin = inside(S, x1);
     uint32_t steps = 0;
     // |g_l|^2 and P_l from one attenuation evaluation per element
     float wl[NLK], pl[NLK];
@@ -119,16 +159,16 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
             uint32_t st = 0;
             float P, w;
             if constexpr (ilp) {
-                const V3 sp = load3(il.p, l);
-                const float Ta = __expf(-tau_to_point(S, x1, sp, st));
+                const V3 sp = lsrc[k];
+                const float Ta = __expf(-tau_pt<SINGLE>(S, x1, sp, xin, st));
                 const V3 d = sub3(x1, sp);
                 const float r2 = dot3(d, d);
                 P = three ? __fdividef(Ta, (float)(4.0 * kPi) * r2) : Ta * (float)(8.0 * kPi) * rsqrtf(r2);
                 w = three ? __fdividef(Ta * kIsoAmp3, r2) : Ta * rsqrtf(r2);
                 if (il.is_area) w *= fabsf(three ? d.z : d.y) * rsqrtf(r2);
             } else {
-                const V3 dr = load3(il.p, l);
-                const float Ta = __expf(-tau_dir(S, x1, V3{ -dr.x, -dr.y, -dr.z }, st));
+                const V3 dr = lsrc[k];
+                const float Ta = __expf(-tau_d<SINGLE>(S, x1, V3{ -dr.x, -dr.y, -dr.z }, xin, st));
                 P = Ta * il.sprob[l];
                 w = Ta;
             }
@@ -152,13 +192,13 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
         float w;
         if constexpr (vwp) {
             const V3 sp = load3(vw.p, v);
-            const float Ta = __expf(-tau_to_point(S, x1, sp, st));
+            const float Ta = __expf(-tau_pt<SINGLE>(S, x1, sp, xin, st));
             const V3 d = sub3(x1, sp);
             const float r2 = dot3(d, d);
             w = three ? __fdividef(Ta * kIsoAmp3, r2) : Ta * rsqrtf(r2);
             if (vw.is_area) w *= fabsf(three ? d.z : d.y) * rsqrtf(r2);
         } else {
-            w = __expf(-tau_dir(S, x1, load3(vw.p, v), st));
+            w = __expf(-tau_d<SINGLE>(S, x1, load3(vw.p, v), xin, st));
         }
         steps += 2 * st * (uint32_t)Nt;
         for (int t = 0; t < tss; ++t) bss[(size_t)t * Nv + v] = make_float2(w, 0.f);
@@ -169,13 +209,16 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
         const V3 x12 = funit(sub3(x2, x1));
         float ps2 = 0.0f;
         V3 i1s[NLK];
+        float pdf1[NLK];
 #pragma unroll
         for (int k = 0; k < NLK; ++k) {
             const int l = lane + 32 * k;
             i1s[k] = V3{ 0.f, 0.f, 1.f };
+            pdf1[k] = 0.0f;
             if (32 * k < Nl && l < Nl) {
-                i1s[k] = fsrc_in(il, l, x1);
-                ps2 += pl[k] * pdf_fast(S, m1, i1s[k], x12);
+                i1s[k] = ilp ? funit(sub3(x1, lsrc[k])) : lsrc[k];
+                pdf1[k] = pdf_fast(S, m1, i1s[k], x12);
+                ps2 += pl[k] * pdf1[k];
             }
         }
         const float p2inv = 1.0f / (warp_sum(ps2) / (float)Nl);
@@ -187,7 +230,7 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
             if (!(32 * k < Nl && l < Nl)) continue;
             const V3 qv = sub3(i1s[k], x12);
             const float c1k = c1base * dot3(qv, qv);
-            const float f12 = (ilp && S.iso_all) ? S.iso_amp * S.iso_amp : pdf_fast(S, m1, i1s[k], x12);
+            const float f12 = (ilp && S.iso_all) ? S.iso_amp * S.iso_amp : pdf1[k];
             const float base = wl[k] * f12 * p2inv;
             if (geo) {
                 const float es = __expf(-c1k * tau0);
@@ -204,25 +247,30 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
     if (lane == 0) {
         if (T.m1) T.m1[q] = (unsigned char)m1;
         if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
-        atomicAdd(T.totals + 0, (unsigned long long)B);
-        atomicAdd(T.totals + 2, (unsigned long long)T.misses[q]);
-        atomicAdd(T.totals + 3, 1ull);
-        if (ws) {
-            if (T.dda) atomicAdd(T.dda + q, ws);
-            atomicAdd(T.totals + 1, (unsigned long long)ws);
-        }
+        if (T.dda && ws) atomicAdd(T.dda + q, ws);
+        ws_acc.vertices += B;
+        ws_acc.misses += T.misses[q];
+        ws_acc.paths += 1;
+        ws_acc.steps += ws;
     }
 }
 
 // One warp per path (a kernel of its own: it needs few registers, so many
 // warps hide the latency of its row writes).
-template <int NLK, bool ILP, bool VWP>
+template <int NLK, bool ILP, bool VWP, bool SINGLE>
 __global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t q = gw; q < T.paths; q += nw) illum_path<NLK, ILP, VWP>(S, T, q, lane, T.counts[q], T.verts + T.offsets[q]);
+    // this lane's illumination elements (positions or directions), loaded once
+    V3 lsrc[NLK];
+#pragma unroll
+    for (int k = 0; k < NLK; ++k) lsrc[k] = load3(S.src[0].p, min(lane + 32 * k, S.src[0].n - 1));
+    WarpStats st;
+    for (uint32_t q = gw; q < T.paths; q += nw)
+        illum_path<NLK, ILP, VWP, SINGLE>(S, T, q, lane, T.counts[q], T.verts + T.offsets[q], lsrc, st);
+    if (lane == 0) st.flush(T);
 }
 
 template <bool CORR, bool VWP, bool SINGLE>
@@ -259,6 +307,7 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
 
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long warp_steps = 0;
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t B = T.counts[q];
         const float4* vq = T.verts + T.offsets[q];
@@ -475,9 +524,10 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
         const uint32_t ws = warp_sum_u32(steps);
         if (lane == 0 && ws) {
             if (T.dda) atomicAdd(T.dda + q, ws);
-            atomicAdd(T.totals + 1, (unsigned long long)ws);
+            warp_steps += ws;
         }
     }
+    if (lane == 0 && warp_steps) atomicAdd(T.totals + 1, warp_steps);
 }
 
 }  // namespace
@@ -524,12 +574,21 @@ int launch_illum(const DevScene& S, const TraceParams& T, int blocks, int thread
     const bool ip = S.src[0].type == SSTMC_SOURCE_POINT, vp = S.src[1].type == SSTMC_SOURCE_POINT;
     using Fn = void (*)(DevScene, TraceParams);
     Fn f;
-    if (S.src[0].n <= 64)
-        f = ip ? (vp ? (Fn)illum_kernel<2, true, true> : (Fn)illum_kernel<2, true, false>)
-               : (vp ? (Fn)illum_kernel<2, false, true> : (Fn)illum_kernel<2, false, false>);
-    else
-        f = ip ? (vp ? (Fn)illum_kernel<kMaxIllum, true, true> : (Fn)illum_kernel<kMaxIllum, true, false>)
-               : (vp ? (Fn)illum_kernel<kMaxIllum, false, true> : (Fn)illum_kernel<kMaxIllum, false, false>);
+    if (S.single) {
+        if (S.src[0].n <= 64)
+            f = ip ? (vp ? (Fn)illum_kernel<2, true, true, true> : (Fn)illum_kernel<2, true, false, true>)
+                   : (vp ? (Fn)illum_kernel<2, false, true, true> : (Fn)illum_kernel<2, false, false, true>);
+        else
+            f = ip ? (vp ? (Fn)illum_kernel<kMaxIllum, true, true, true> : (Fn)illum_kernel<kMaxIllum, true, false, true>)
+                   : (vp ? (Fn)illum_kernel<kMaxIllum, false, true, true> : (Fn)illum_kernel<kMaxIllum, false, false, true>);
+    } else {
+        if (S.src[0].n <= 64)
+            f = ip ? (vp ? (Fn)illum_kernel<2, true, true, false> : (Fn)illum_kernel<2, true, false, false>)
+                   : (vp ? (Fn)illum_kernel<2, false, true, false> : (Fn)illum_kernel<2, false, false, false>);
+        else
+            f = ip ? (vp ? (Fn)illum_kernel<kMaxIllum, true, true, false> : (Fn)illum_kernel<kMaxIllum, true, false, false>)
+                   : (vp ? (Fn)illum_kernel<kMaxIllum, false, true, false> : (Fn)illum_kernel<kMaxIllum, false, false, false>);
+    }
     f<<<blocks, threads, 0, stream>>>(S, T);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
