@@ -198,10 +198,16 @@ def run_reference(args, dist, rank, ws):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes per path of the NEE kernel from one ncu capture of this workload
-# (dram__bytes_read.sum + dram__bytes_write.sum over 2^16 paths); the traffic
-# is per-path rows, so a launch's traffic scales with the paths it processes.
-NCU_NEE_DRAM_BYTES_PER_PATH = 1052254592 / 65536
+# DRAM bytes (read + write) per path of each kernel class from one ncu capture
+# of this workload at 2^16 paths (profiles/kernels_correlation_3d_2p16.md);
+# every class streams per-path rows, so a launch's traffic scales with the
+# paths it processes.
+NCU_DRAM_BYTES_PER_PATH = {
+    "nee": (306547456 + 223163136) / 65536,    # illum_kernel + view_kernel
+    "walk": (60928 + 591872) / 65536,          # walk_kernel count + write
+    "gemm": 541137408 / 65536,                 # gemm_tc_kernel
+    "ss": 69278208 / 65536,                    # ss_fast_kernel
+}
 
 
 def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
@@ -210,34 +216,37 @@ def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
     m = scene.meta
     P = m["P"] * m["waves"]
     Nl, Nv, Nt = m["Nl"], m["Nv"], m["Nt"]
-    g2 = 8.0 * Nt * Nl if (m.get("correlation") and not m.get("sym", True)) else 0.0
     hbm, tc = peaks["hbm_gbs"], peaks["bf16_tflops"]
     out = {}
 
-    def add(key, name, ms, bound, amount, traffic=None):
+    def add(key, name, ms, bound, amount, note):
         per_launch = amount / chunks
+        traffic = NCU_DRAM_BYTES_PER_PATH[key] * P / chunks if WORKLOAD == "correlation_3d" else None
         if bound == "hbm":
             ach = amount / (ms / 1000) / 1e9
             out[key] = {"kernel": name, "ms": ms, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                         "frac": ach / hbm, "peak_name": "hbm_gbs", "algorithmic_per_launch": per_launch,
-                        "traffic": traffic}
+                        "traffic": traffic, "note": note}
         else:
             ach = amount / (ms / 1000) / 1e12
             out[key] = {"kernel": name, "ms": ms, "bound": "tensor", "achieved": ach, "peak": tc, "unit": "TFLOP/s",
                         "frac": ach / tc, "peak_name": "bf16_tflops", "algorithmic_per_launch": per_launch,
-                        "traffic": traffic}
+                        "traffic": traffic, "note": note}
 
-    # NEE vectors: rows written + vertices, counts and offsets read
-    nee_bytes = P * (8.0 * Nt * (2 * Nl + 2 * Nv) + g2 + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
-    add("nee", "trace_kernel (NEE vectors)", mean["ms_nee"], "hbm", nee_bytes,
-        traffic=NCU_NEE_DRAM_BYTES_PER_PATH * P / chunks if WORKLOAD == "correlation_3d" else None)
+    # NEE vectors (illum_kernel + view_kernel): rows written once (a_ms all ticks,
+    # tick-invariant single-scattering rows at tick 0, s_ms), P_l, the vertices read
+    nee_bytes = P * (8.0 * Nt * Nl + 8.0 * (Nl + Nv) + 8.0 * Nt * Nv + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
+    add("nee", "illum_kernel + view_kernel (NEE vectors)", mean["ms_nee"], "hbm", nee_bytes,
+        "FP32-issue bound: DRAM traffic equals the row bytes")
     # random walk: two passes over the same streams; vertices written once, counts / misses / offsets
-    add("walk", "walk_kernel (random walk, count + write)", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P)
-    # multiple-scattering contraction: 8 useful flops per complex multiply-add
+    add("walk", "walk_kernel (random walk, count + write)", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P,
+        "FP32-issue bound (IEEE-rounded decision path)")
+    # multiple-scattering contraction: 8 useful flops per complex multiply-add (3xTF32 issues 3 TF32 MMAs each)
     add("gemm", "gemm_tc_kernel (multiple-scattering contraction, 3xTF32)", mean["ms_contract_ms"], "tensor",
-        8.0 * Nl * Nv * Nt * P)
+        8.0 * Nl * Nv * Nt * P, "reads 8 Nt (Nl + Nv) bytes per path: HBM-bound at this shape")
     # single-scattering contraction: tick-0 rows read (tick-invariant form)
-    add("ss", "ss_fast_kernel (single-scattering contraction)", mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv))
+    add("ss", "ss_fast_kernel (single-scattering contraction)", mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv),
+        "FP32/SFU-issue bound: one exp and one rsqrt per (path, l, v)")
     return out
 
 
