@@ -191,6 +191,38 @@ int32_t sstmc_render(sstmc_scene* scene, uint64_t seed, double* u_out, double* i
  * with that device current; make that first call before any stream capture. */
 int32_t sstmc_render_static(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
 
+/* ------------------------------------------------------------------ */
+/* Serving: continuous batching of renders.  No counterpart in the      */
+/* reference (one scene per MEX call, MatlabInterface.cu:1565-1825).    */
+/* ------------------------------------------------------------------ */
+typedef struct sstmc_server sstmc_server;
+
+/* A request loop on `device` with `slots` worker threads.  A request
+ * reserves the device memory of its chunk buffers (sized to at most
+ * hbm_budget_bytes / slots); queued requests are admitted first-fit while
+ * the reservations in flight stay within hbm_budget_bytes (0: half of the
+ * free memory), and any request is admitted when nothing is in flight.
+ * Requests on different scenes run concurrently on their scenes' streams;
+ * requests on one scene run one after another. */
+int32_t sstmc_server_create(int32_t device, uint64_t hbm_budget_bytes, uint32_t slots, sstmc_server** out);
+/* Cancels queued requests, waits for the running ones, stops the loop. */
+int32_t sstmc_server_destroy(sstmc_server* server);
+/* Queue all renderings of `scene` starting at `seed` (sstmc_render's
+ * semantics and output layout).  The scene and the output buffers must stay
+ * valid until the ticket is done. */
+int32_t sstmc_submit(sstmc_server* server, sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out,
+                     uint64_t* ticket);
+/* done = 1 once the request finished; status = its sstmc_render code. */
+int32_t sstmc_poll(sstmc_server* server, uint64_t ticket, int32_t* done, int32_t* status);
+/* Wait up to timeout_s seconds: SSTMC_TIMEOUT if the request is still open. */
+int32_t sstmc_wait(sstmc_server* server, uint64_t ticket, double timeout_s, int32_t* status);
+/* A queued request completes with SSTMC_CANCELLED; a running one finishes. */
+int32_t sstmc_cancel(sstmc_server* server, uint64_t ticket);
+/* Latency (submit to done) percentiles over the completed requests and
+ * their contributions per second between the first start and the last end. */
+int32_t sstmc_server_stats(sstmc_server* server, double* p50_ms, double* p99_ms, double* contributions_per_s,
+                           uint64_t* completed);
+
 /* Number of NEE path-contributions (sum over traced paths of vertices * Nl *
  * Nv * Nt) and of voxel DDA steps of the last sstmc_render call. */
 int32_t sstmc_last_stats(const sstmc_scene* scene, uint64_t* contributions,

@@ -62,6 +62,20 @@ def load_library() -> C.CDLL:
     lib.sstmc_last_error_text.restype = C.c_char_p
     lib.sstmc_trace_paths.argtypes = [vp, u64, u32, u32, C.POINTER(cf.PathTrace)]
     lib.sstmc_trace_paths.restype = i32
+    lib.sstmc_server_create.argtypes = [i32, u64, u32, C.POINTER(vp)]
+    lib.sstmc_server_create.restype = i32
+    lib.sstmc_server_destroy.argtypes = [vp]
+    lib.sstmc_server_destroy.restype = i32
+    lib.sstmc_submit.argtypes = [vp, vp, u64, dp, dp, C.POINTER(u64)]
+    lib.sstmc_submit.restype = i32
+    lib.sstmc_poll.argtypes = [vp, u64, C.POINTER(i32), C.POINTER(i32)]
+    lib.sstmc_poll.restype = i32
+    lib.sstmc_wait.argtypes = [vp, u64, C.c_double, C.POINTER(i32)]
+    lib.sstmc_wait.restype = i32
+    lib.sstmc_cancel.argtypes = [vp, u64]
+    lib.sstmc_cancel.restype = i32
+    lib.sstmc_server_stats.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64)]
+    lib.sstmc_server_stats.restype = i32
     _LIB = lib
     return lib
 
@@ -136,6 +150,76 @@ class Scene:
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.lib.sstmc_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Request:
+    """A submitted render: its host output buffers stay alive with this object."""
+
+    def __init__(self, server: "Server", scene: Scene, seed: int):
+        self.server, self.scene, self.seed = server, scene, seed
+        n = scene.Nl * scene.Nv * scene.Nt
+        self._u = np.zeros(2 * n * scene.renders, dtype=np.float64)
+        self._it = np.zeros(scene.renders, dtype=np.float64)
+        t = C.c_uint64()
+        _check(server.lib.sstmc_submit(server.handle, scene.handle, C.c_uint64(seed),
+                                       self._u.ctypes.data_as(C.POINTER(C.c_double)),
+                                       self._it.ctypes.data_as(C.POINTER(C.c_double)), C.byref(t)))
+        self.ticket = t.value
+
+    def done(self) -> bool:
+        d, st = C.c_int32(), C.c_int32()
+        _check(self.server.lib.sstmc_poll(self.server.handle, C.c_uint64(self.ticket), C.byref(d), C.byref(st)))
+        return bool(d.value)
+
+    def wait(self, timeout: float = 600.0) -> int:
+        """Status of the finished render; raises SstmcError(SSTMC_TIMEOUT) if still open."""
+        st = C.c_int32()
+        _check(self.server.lib.sstmc_wait(self.server.handle, C.c_uint64(self.ticket), C.c_double(timeout), C.byref(st)))
+        return st.value
+
+    def cancel(self) -> None:
+        _check(self.server.lib.sstmc_cancel(self.server.handle, C.c_uint64(self.ticket)))
+
+    def result(self, timeout: float = 600.0) -> Tuple[np.ndarray, np.ndarray]:
+        _check(self.wait(timeout))
+        s = self.scene
+        uc = (self._u[0::2] + 1j * self._u[1::2]).reshape(s.renders, s.Nt, s.Nv, s.Nl)
+        return np.transpose(uc, (3, 2, 1, 0)), self._it.copy()
+
+
+class Server:
+    """Continuous batching of renders over resident scenes (sstmc_server_*)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, slots: int = 4):
+        self.lib = load_library()
+        h = C.c_void_p()
+        _check(self.lib.sstmc_server_create(C.c_int32(device), C.c_uint64(hbm_budget_bytes), C.c_uint32(slots), C.byref(h)))
+        self.handle = h
+
+    def submit(self, scene: Scene, seed: int) -> Request:
+        return Request(self, scene, seed)
+
+    def stats(self) -> Dict[str, float]:
+        p50, p99, cps, n = C.c_double(), C.c_double(), C.c_double(), C.c_uint64()
+        _check(self.lib.sstmc_server_stats(self.handle, C.byref(p50), C.byref(p99), C.byref(cps), C.byref(n)))
+        return {"p50_ms": p50.value, "p99_ms": p99.value, "contributions_per_s": cps.value, "completed": n.value}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.sstmc_server_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

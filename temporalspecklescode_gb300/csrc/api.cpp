@@ -70,13 +70,33 @@ size_t Engine::bytes_per_path(const Scene& S)
     return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16;
 }
 
+// Freed chunk buffers stay cached in the device's stream-ordered pool (up
+// to 32 GiB), so a scene created after another one was destroyed, or the
+// next served request, reuses that memory instead of mapping it again.
+static void keep_pool_memory(int device)
+{
+    static std::once_flag once[64];
+    if (device < 0 || device >= 64) return;
+    std::call_once(once[device], [device] {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
+        uint64_t keep = 0;
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        keep = std::max<uint64_t>(keep, (uint64_t)32 << 30);
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    });
+}
+
 int Engine::ensure(Scene& S, uint32_t paths)
 {
     if (cap >= paths && a_ms) return SSTMC_NO_ERROR;
+    keep_pool_memory(S.device);
     release();
     const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
+    // stream-ordered: freeing never synchronises the device (requests of a
+    // server run concurrently on other streams)
     auto alloc = [&](void** p, size_t bytes) {
-        if (cudaMalloc(p, bytes ? bytes : 1) != cudaSuccess) return false;
+        if (cudaMallocAsync(p, bytes ? bytes : 1, stream) != cudaSuccess) return false;
         return true;
     };
     bool ok = alloc((void**)&a_ms, paths * Nt * Nl * sizeof(float2)) && alloc((void**)&s_ms, paths * Nt * Nv * sizeof(float2))
@@ -98,7 +118,7 @@ int Engine::ensure(Scene& S, uint32_t paths)
 void Engine::release()
 {
     void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts };
-    for (void* p : ps) if (p) cudaFree(p);
+    for (void* p : ps) if (p) cudaFreeAsync(p, stream);
     counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
     pl = x1 = x1t = nullptr;
@@ -150,8 +170,9 @@ int Engine::prepare_ss_tables(Scene& S)
                     h[m * per + ((size_t)t * Nv + v) * Nl + l] = (float)w;
                 }
     }
-    if (cudaMalloc((void**)&W, h.size() * sizeof(float)) != cudaSuccess) { W = nullptr; return SSTMC_ALLOCATION_ERROR; }
-    if (cudaMemcpy(W, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    if (cudaMallocAsync((void**)&W, h.size() * sizeof(float), stream) != cudaSuccess) { W = nullptr; return SSTMC_ALLOCATION_ERROR; }
+    if (cudaMemcpyAsync(W, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, stream) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;   // h is freed on return
     return SSTMC_NO_ERROR;
 }
 
@@ -191,10 +212,10 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
     if (nverts > verts_cap) {
         if (fixed) return SSTMC_SCRATCH_LIMIT;
-        if (verts) cudaFree(verts);
+        if (verts) cudaFreeAsync(verts, stream);
         verts = nullptr;
         const size_t cap = (size_t)(nverts * 5 / 4) + 1024;
-        if (cudaMalloc((void**)&verts, cap * sizeof(float4)) != cudaSuccess) { verts_cap = 0; return SSTMC_ALLOCATION_ERROR; }
+        if (cudaMallocAsync((void**)&verts, cap * sizeof(float4), stream) != cudaSuccess) { verts_cap = 0; return SSTMC_ALLOCATION_ERROR; }
         verts_cap = cap;
     }
     Wp.verts = verts;
@@ -316,7 +337,8 @@ int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out)
 {
     const uint64_t total = (uint64_t)S.P * S.full_iter;
     if (total > 0xffffffffull) return SSTMC_NOT_SUPPORTED;
-    uint32_t chunk = (uint32_t)std::min<uint64_t>(total, std::max<uint64_t>(256, budget_bytes() / bytes_per_path(S)));
+    const size_t bud = budget ? budget : budget_bytes();
+    uint32_t chunk = (uint32_t)std::min<uint64_t>(total, std::max<uint64_t>(256, bud / bytes_per_path(S)));
     chunk = std::max<uint32_t>(32, chunk);
     int e = ensure(S, chunk);
     if (e) return e;
@@ -399,6 +421,50 @@ struct sstmc_scene {
     std::mutex mu;
 };
 
+namespace sstmc {
+
+// Every rendering of the scene's config (seed, seed + 1, ...), holding the
+// scene's lock.  budget: device bytes for the chunk buffers (0: the default);
+// release_after: return them to the stream-ordered pool afterwards (served
+// requests, whose reservation ends with the request).
+int32_t render_scene(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out, size_t budget, bool release_after,
+                     uint64_t* contributions)
+{
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (cudaSetDevice(s->scene.device) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    const size_t nout = (size_t)s->scene.Nt * s->scene.Nv * s->scene.Nl;
+    if (budget && budget != s->engine.budget) s->engine.release();
+    s->engine.budget = budget;
+    uint64_t contrib = 0;
+    int e = SSTMC_NO_ERROR;
+    for (uint32_t r = 0; r < s->scene.renders && !e; ++r) {
+        e = s->engine.render_one(s->scene, seed + r, u_out ? u_out + 2 * nout * r : nullptr, iter_out ? iter_out + r : nullptr);
+        contrib += s->scene.last_contrib;
+    }
+    if (release_after) {
+        s->engine.release();
+        if (cudaStreamSynchronize(s->engine.stream) != cudaSuccess && !e) e = SSTMC_DEVICE_ERROR;
+    }
+    if (contributions) *contributions = contrib;
+    return e;
+}
+
+// Device bytes a served render of the scene reserves with chunk buffers
+// sized to at most cap bytes: the per-path rows of one chunk, its vertices
+// (32 per path assumed) and the output accumulator.
+size_t scene_request_bytes(const sstmc_scene* s, size_t cap)
+{
+    const Scene& S = s->scene;
+    const uint64_t total = (uint64_t)S.P * S.full_iter;
+    const size_t bpp = Engine::bytes_per_path(S) + 32 * sizeof(float4);
+    const uint64_t chunk = std::min<uint64_t>(total, std::max<uint64_t>(256, cap / bpp));
+    return (size_t)chunk * bpp + (size_t)S.Nt * S.Nv * S.Nl * 16 + ((size_t)1 << 20);
+}
+
+int scene_device(const sstmc_scene* s) { return s->scene.device; }
+
+}  // namespace sstmc
+
 extern "C" {
 
 void sstmc_config_init(sstmc_config* cfg)
@@ -442,16 +508,7 @@ int32_t sstmc_scene_shape(const sstmc_scene* s, uint32_t* nl, uint32_t* nv, uint
 
 int32_t sstmc_render(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out)
 {
-    if (!s) return SSTMC_INVALID_HANDLE;
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (cudaSetDevice(s->scene.device) != cudaSuccess) return SSTMC_DEVICE_ERROR;
-    const size_t nout = (size_t)s->scene.Nt * s->scene.Nv * s->scene.Nl;
-    for (uint32_t r = 0; r < s->scene.renders; ++r) {
-        const int e = s->engine.render_one(s->scene, seed + r, u_out ? u_out + 2 * nout * r : nullptr,
-                                           iter_out ? iter_out + r : nullptr);
-        if (e) return e;
-    }
-    return SSTMC_NO_ERROR;
+    return s ? render_scene(s, seed, u_out, iter_out, 0, false, nullptr) : SSTMC_INVALID_HANDLE;
 }
 
 int32_t sstmc_render_static(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out)

@@ -41,6 +41,7 @@ struct Engine {
     double ms_trace = 0, ms_gemm = 0, ms_ss = 0, ms_total = 0, ms_walk = 0;
     uint64_t launches = 0, chunks = 0;
     bool timing = true;
+    size_t budget = 0;    // device bytes for the chunk buffers; 0: min(16 GiB, a quarter of free memory)
     bool fixed = false;   // buffers carved from a fixed scratch: a chunk that outgrows them fails, nothing is allocated
 
     static size_t bytes_per_path(const Scene& S);
@@ -55,6 +56,18 @@ struct Engine {
     int init_events();
     void destroy_events();
 };
+
+}  // namespace sstmc
+
+struct sstmc_scene;
+
+namespace sstmc {
+
+// Render entry shared by sstmc_render and the server (api.cpp).
+int32_t render_scene(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out, size_t budget, bool release_after,
+                     uint64_t* contributions);
+size_t scene_request_bytes(const sstmc_scene* s, size_t cap);
+int scene_device(const sstmc_scene* s);
 
 // sstmc_render with every device buffer in a static scratch (static_render.cu).
 int render_static(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, double* iter_out);
