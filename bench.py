@@ -350,6 +350,81 @@ def run_gpu(args, dist, rank, ws):
         print(json.dumps(line), flush=True)
 
 
+def _serving_media(seed: int):
+    """Eight seeded scenes of the serving mix: correlation slabs, 2D speckle,
+    transmission-matrix grids and tracking frames of mixed sizes."""
+    import random
+    from temporalspecklescode_gb300 import workloads as wl
+    rng = random.Random(seed)
+    media = []
+    for k in range(8):
+        kind = k % 4
+        paths_log2 = rng.randint(16, 20)
+        waves = max(1, 1 << max(0, paths_log2 - 18))
+        batch = (1 << paths_log2) // waves
+        if kind == 0:
+            media.append(wl.correlation_3d(batch_size=batch, full_iteration=waves, n_side=rng.choice([4, 6, 8]),
+                                           n_lags=rng.randint(1, 8), seed=k))
+        elif kind == 1:
+            media.append(wl.speckle_2d(batch_size=batch, full_iteration=waves, n_dirs=rng.choice([16, 32, 64, 128]), seed=k))
+        elif kind == 2:
+            media.append(wl.transmission_matrix_3d(batch_size=batch // 16, full_iteration=waves, n_dirs=rng.choice([16, 32, 64]),
+                                                   grid=(16, 16, 8), seed=k))
+        else:
+            media.append(wl.tracking_2d(batch_size=batch // 16, full_iteration=waves, n_dirs=rng.choice([16, 32]),
+                                        frames=rng.randint(2, 8), seed=k))
+    return media
+
+
+def run_serve(args):
+    """Serving mix: a Poisson stream of render requests over eight device-
+    resident scenes, through the server (continuous batching) and one by one."""
+    import random
+    from temporalspecklescode_gb300 import api
+    api.load_library()
+    media = _serving_media(5)
+    scenes = [api.Scene(cfg, dims) for cfg, dims in media]
+    rng = random.Random(5)
+    n_req = args.serve_requests
+    picks = [rng.randrange(len(scenes)) for _ in range(n_req)]
+    for s in scenes:          # warm-up: every kernel variant once
+        s.render(seed=1)
+    # one by one (sstmc_render), back to back
+    t0 = time.perf_counter()
+    contrib = 0
+    for i, k in enumerate(picks):
+        scenes[k].render(seed=100 + i)
+        contrib += scenes[k].stats()["contributions"]
+    one_s = time.perf_counter() - t0
+    one_rate = contrib / one_s
+    # served: Poisson arrivals at the one-by-one request rate x load
+    mean_gap = one_s / n_req / args.serve_load
+    with api.Server(slots=4) as srv:
+        reqs = []
+        t_next = time.perf_counter()
+        for i, k in enumerate(picks):
+            t_next += rng.expovariate(1.0 / mean_gap)
+            delay = t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            reqs.append(srv.submit(scenes[k], 100 + i))
+        for r in reqs:
+            r.result()
+        st = srv.stats()
+    for s in scenes:
+        s.close()
+    line = {
+        "metric": "served NEE path-contributions/s (Poisson request mix over 8 resident scenes); p50/p99 latency",
+        "value": st["contributions_per_s"], "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+        "latency_ms": {"p50": st["p50_ms"], "p99": st["p99_ms"]}, "requests": n_req, "completed": st["completed"],
+        "one_by_one": {"value": one_rate, "unit": UNIT, "seconds": one_s},
+        "config": {"workload": "serving_mix", "media": len(scenes), "slots": 4, "load": args.serve_load,
+                   "paths_per_request": "2^16 - 2^20", "seed": 5},
+        "data": "synthetic",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,7 +436,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 15)
     ap.add_argument("--ref-sample", type=int, default=1 << 14)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve", action="store_true", help="measure the serving mix instead of the headline workload")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-load", type=float, default=2.0, help="arrival rate / one-by-one completion rate")
     args = ap.parse_args()
+    if args.serve:
+        run_serve(args)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     dist, rank, ws = _dist()
     if args.impl == "reference":
