@@ -238,8 +238,8 @@ def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
     nee_bytes = P * (8.0 * Nt * Nl + 8.0 * (Nl + Nv) + 8.0 * Nt * Nv + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
     add("nee", "illum_kernel + view_kernel (NEE vectors)", mean["ms_nee"], "hbm", nee_bytes,
         "FP32-issue bound: DRAM traffic equals the row bytes")
-    # random walk: two passes over the same streams; vertices written once, counts / misses / offsets
-    add("walk", "walk_kernel (random walk, count + write)", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P,
+    # random walk: one pass into per-path slots + compaction; vertices written once, counts / misses / offsets
+    add("walk", "walk_kernel (single-pass random walk) + compaction", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P,
         "FP32-issue bound (IEEE-rounded decision path)")
     # multiple-scattering contraction: 8 useful flops per complex multiply-add (3xTF32 issues 3 TF32 MMAs each)
     add("gemm", "gemm_tc_kernel (multiple-scattering contraction, 3xTF32)", mean["ms_contract_ms"], "tensor",

@@ -67,7 +67,8 @@ bool use_tensor_cores()
 size_t Engine::bytes_per_path(const Scene& S)
 {
     const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
-    return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16;
+    return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16
+         + walk_slot_bytes_per_path();
 }
 
 // Freed chunk buffers stay cached in the device's stream-ordered pool (up
@@ -109,7 +110,10 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&counts, paths * sizeof(uint32_t)) && alloc((void**)&misses, paths * sizeof(uint32_t))
            && alloc((void**)&offsets, paths * sizeof(uint32_t))
            && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
-           && alloc((void**)&vtotal, 2 * sizeof(unsigned long long));   // total + the walk's two path counters
+           && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, the long-path count
+           && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
+           && alloc((void**)&ovf, (size_t)walk_overflow_blocks(paths) * kWalkSlotVerts * sizeof(float4))
+           && alloc((void**)&ovf_owner, (size_t)walk_overflow_blocks(paths) * sizeof(uint2));
     if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
     cap = paths;
     return SSTMC_NO_ERROR;
@@ -117,9 +121,11 @@ int Engine::ensure(Scene& S, uint32_t paths)
 
 void Engine::release()
 {
-    void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts };
+    void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts,
+                   slots, longq, ovf, ovf_owner };
     for (void* p : ps) if (p) cudaFreeAsync(p, stream);
     counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
+    slots = nullptr; longq = nullptr; ovf = nullptr; ovf_owner = nullptr;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
     pl = x1 = x1t = nullptr;
     m1 = nullptr; totals = nullptr; err = nullptr; V = nullptr; W = nullptr;
@@ -197,19 +203,31 @@ void Engine::plan(const Scene& S, TraceParams& T, std::vector<std::pair<int, int
 
 int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, PathDebug* dbg)
 {
-    // 1. random walk: count, scan, write (pathwalk.cu)
+    // 1. random walk: single pass, scan, compaction (pathwalk.cu)
     WalkParams Wp;
     std::memset(&Wp, 0, sizeof(Wp));
     Wp.seed = seed; Wp.first_path = first; Wp.paths = n;
     Wp.counts = counts; Wp.misses = misses; Wp.offsets = offsets; Wp.block_sums = block_sums; Wp.total = vtotal;
     Wp.next = reinterpret_cast<uint32_t*>(vtotal + 1);
     Wp.err = err; Wp.hash = dbg ? dbg->hash : nullptr;
+    // single pass: counts, the first 64 vertices of every path (slots) and
+    // the rest in overflow blocks; paths that found the pool empty are
+    // listed for a replay
+    Wp.slots = slots; Wp.list = longq; Wp.list_count = reinterpret_cast<uint32_t*>(vtotal + 2);
+    Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_count = Wp.list_count + 1; Wp.ovf_cap = walk_overflow_blocks(n);
     int e = launch_walk_count(S.dev, Wp, stream);
     if (e) return e;
     launches += 4;
-    unsigned long long nverts = 0;
-    if (cudaMemcpyAsync(&nverts, vtotal, sizeof(nverts), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    unsigned char hv[24];
+    if (cudaMemcpyAsync(hv, vtotal, sizeof(hv), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
+    unsigned long long nverts = 0;
+    uint32_t nlong = 0;
+    std::memcpy(&nverts, hv, 8);
+    std::memcpy(&nlong, hv + 16, 4);
+    uint32_t novf = 0;
+    std::memcpy(&novf, hv + 20, 4);
+    Wp.ovf_n = std::min(novf, Wp.ovf_cap);
     if (nverts > verts_cap) {
         if (fixed) return SSTMC_SCRATCH_LIMIT;
         if (verts) cudaFreeAsync(verts, stream);
@@ -219,9 +237,15 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         verts_cap = cap;
     }
     Wp.verts = verts;
-    e = launch_walk_write(S.dev, Wp, stream);
+    e = launch_walk_compact(Wp, stream);
     if (e) return e;
-    launches++;
+    launches += Wp.ovf_n ? 2 : 1;
+    if (nlong) {
+        Wp.list_n = nlong;
+        e = launch_walk_write(S.dev, Wp, stream);
+        if (e) return e;
+        launches++;
+    }
     if (timing && ev[6]) cudaEventRecord(ev[6], stream);
 
     // 2. NEE vectors per path (trace.cu)

@@ -20,6 +20,8 @@ namespace sstmc {
 
 namespace {
 
+constexpr uint32_t kSlotVerts = kWalkSlotVerts;
+
 __device__ __forceinline__ uint32_t u1_count_w(const DevScene& S, uint64_t seed, uint32_t wave)
 {
     Stream ws;
@@ -48,17 +50,30 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
 // path ends (warp-aggregated atomics), so the lanes of a warp stay busy until
 // the whole pool is drawn.  The first two Philox blocks of each vertex are
 // generated at the top of the iteration, where all lanes are converged.
-template <bool WRITE>
+// MODE kSlots: one pass that counts every path and writes its first
+//   kSlotVerts vertices into a fixed slot and the rest into overflow blocks
+//   of kSlotVerts vertices taken from a shared pool (compaction kernels then
+//   pack both); a path that finds the pool empty is listed for kWrite;
+// MODE kCount: count only;
+// MODE kWrite: replay paths (all, or the W.list of long ones) and write their
+//   vertices at their offsets.
+constexpr int kCount = 0, kWrite = 1, kSlots = 2;
+
+template <int MODE>
 __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
+    constexpr bool WRITE = MODE == kWrite;
+    constexpr bool COUNTS = MODE != kWrite;
     const uint32_t lane = threadIdx.x & 31u;
     const bool corr = S.correlation != 0;
+    const uint32_t pool = (WRITE && W.list) ? W.list_n : W.paths;
     uint32_t q = 0, pid = 0, att = 0, b = 1, B = 0, h = 2166136261u;
     V3 prev{ 0.f, 0.f, 0.f }, cur{ 0.f, 0.f, 0.f };
     int mcur = 0;
     float4* out = nullptr;
+    uint32_t o0 = 0;   // vertex index stored at out[0]
     const DevSource* fsrc = &S.src[0];
-    // next path index for each active lane (one atomic per warp and call)
+    // next pool index for each active lane (one atomic per warp and call)
     auto fetch = [&]() -> uint32_t {
         const uint32_t mask = __activemask();
         const int leader = __ffs(mask) - 1;
@@ -68,25 +83,45 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
         return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
     };
     // move to the next path that has work; false when the pool is drawn
-    auto start = [&](uint32_t qq) -> bool {
-        while (qq < W.paths) {
-            if (!WRITE || W.counts[qq] != 0) break;
-            if (W.hash) W.hash[qq] = 2166136261u;  // the count pass hit a limit: nothing to write
-            qq = fetch();
+    auto start = [&](uint32_t i) -> bool {
+        for (;;) {
+            if (i >= pool) return false;
+            q = (WRITE && W.list) ? W.list[i] : i;
+            if (!WRITE || W.counts[q] != 0) break;
+            if (W.hash) W.hash[q] = 2166136261u;  // the count pass hit a limit: nothing to write
+            i = fetch();
         }
-        q = qq;
-        if (q >= W.paths) return false;
         pid = W.first_path + q;
         const uint32_t slot = pid % S.P, wave = pid / S.P;
         fsrc = (!corr || slot < u1_count_w(S, W.seed, wave)) ? &S.src[0] : &S.src[2];
         att = 0; b = 1; B = 0; h = 2166136261u;
         if (WRITE) out = W.verts + W.offsets[q];
+        if (MODE == kSlots) out = W.slots + (size_t)q * kSlotVerts;
+        o0 = 0;
         return true;
     };
     auto finish = [&](bool ok) {
         if (!ok) { atomicExch(W.err, SSTMC_PATH_LIMIT); B = 0; }
-        if (!WRITE) { W.counts[q] = B; W.misses[q] = att; }
-        else if (W.hash) W.hash[q] = h;
+        if (COUNTS) { W.counts[q] = B; W.misses[q] = att; }
+        if (MODE != kCount && W.hash) W.hash[q] = h;
+        if (MODE == kSlots && ok && out == nullptr) W.list[atomicAdd(W.list_count, 1u)] = q;   // replayed by the write pass
+    };
+    auto store = [&](uint32_t k, const V3& x, int m, float xi) {   // vertex k (0-based)
+        if (WRITE) out[k] = pack_vertex(x, m, xi);
+        if (MODE == kSlots) {
+            if (k % kSlotVerts == 0 && k != 0 && out != nullptr) {   // slot or block full: take a block
+                const uint32_t blk = atomicAdd(W.ovf_count, 1u);
+                if (blk < W.ovf_cap) {
+                    W.ovf_owner[blk] = make_uint2(q, k / kSlotVerts);
+                    out = W.ovf + (size_t)blk * kSlotVerts;
+                    o0 = k;
+                } else {
+                    out = nullptr;
+                }
+            }
+            if (out != nullptr) out[k - o0] = pack_vertex(x, m, xi);
+        }
+        if (MODE != kCount) h = hash_v(S, h, x, m);
     };
     if (!start(fetch())) return;
     for (;;) {
@@ -111,7 +146,7 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
                     if (++att >= kMaxAttempts) { ok = false; done = true; }
                 } else {
                     const float xi = corr ? 0.0f : rs.uniform();
-                    if (WRITE) { out[0] = pack_vertex(xn, mn, xi); h = hash_v(S, h, xn, mn); }
+                    store(0, xn, mn, xi);
                     B = 1; prev = o; cur = xn; mcur = mn; b = 2;
                 }
             } else if (mn == 0) {
@@ -120,7 +155,7 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
                 ok = false; done = true;
             } else {
                 const float xi = corr ? 0.0f : rs.uniform();
-                if (WRITE) { out[b - 1] = pack_vertex(xn, mn, xi); h = hash_v(S, h, xn, mn); }
+                store(b - 1, xn, mn, xi);
                 B = b; prev = cur; cur = xn; mcur = mn; ++b;
             }
         }
@@ -128,6 +163,29 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
             finish(ok);
             if (!start(fetch())) return;
         }
+    }
+}
+
+// Packs the slots (first kSlotVerts vertices of every path) into the
+// compact vertex array at the offsets, thread per slot entry.
+__global__ void compact_kernel(const __grid_constant__ WalkParams W)
+{
+    const size_t total = (size_t)W.paths * kSlotVerts;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t q = (uint32_t)(i / kSlotVerts), k = (uint32_t)(i % kSlotVerts);
+        if (k < W.counts[q]) W.verts[W.offsets[q] + k] = W.slots[i];
+    }
+}
+
+// Packs the overflow blocks (vertices kSlotVerts j .. of their owner path).
+// A path whose walk found the pool empty is rewritten whole by the write pass.
+__global__ void compact_overflow_kernel(const __grid_constant__ WalkParams W)
+{
+    const size_t total = (size_t)W.ovf_n * kSlotVerts;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const uint2 own = W.ovf_owner[i / kSlotVerts];
+        const uint32_t v = own.y * kSlotVerts + (uint32_t)(i % kSlotVerts);
+        if (v < W.counts[own.x]) W.verts[W.offsets[own.x] + v] = W.ovf[i];
     }
 }
 
@@ -195,16 +253,43 @@ static int walk_blocks(uint32_t paths)
     return (int)std::max<uint32_t>(1, std::min(want, cap));
 }
 
-int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
+static int launch_scan(const WalkParams& W, cudaStream_t stream)
 {
-    const int threads = 128;
-    if (cudaMemsetAsync(W.next, 0, 2 * sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
-    walk_kernel<false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
-    if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
     const uint32_t nb = (W.paths + kScanBlock - 1) / kScanBlock;
     scan_block_kernel<<<nb, kScanBlock, 0, stream>>>(W.counts, W.offsets, W.block_sums, W.paths);
     scan_totals_kernel<<<1, kScanBlock, 0, stream>>>(W.block_sums, nb, W.total);
     scan_add_kernel<<<nb, kScanBlock, 0, stream>>>(W.offsets, W.block_sums, W.paths);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
+
+int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
+{
+    const int threads = 128;
+    if (cudaMemsetAsync(W.next, 0, 2 * sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (W.slots) {
+        if (cudaMemsetAsync(W.list_count, 0, sizeof(uint32_t), stream) != cudaSuccess
+            || cudaMemsetAsync(W.ovf_count, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+        walk_kernel<kSlots><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+    } else {
+        walk_kernel<kCount><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+    }
+    if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
+    return launch_scan(W, stream);
+}
+
+int launch_walk_compact(const WalkParams& W, cudaStream_t stream)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t total = (size_t)W.paths * kSlotVerts;
+    const int blocks = (int)std::min<size_t>((total + 255) / 256, (size_t)sms * 16);
+    compact_kernel<<<std::max(1, blocks), 256, 0, stream>>>(W);
+    if (W.ovf_n) {
+        const size_t ototal = (size_t)W.ovf_n * kSlotVerts;
+        const int oblocks = (int)std::min<size_t>((ototal + 255) / 256, (size_t)sms * 16);
+        compact_overflow_kernel<<<std::max(1, oblocks), 256, 0, stream>>>(W);
+    }
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 
@@ -213,8 +298,20 @@ int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t strea
     const int threads = 128;
     WalkParams Wn = W;
     Wn.next = W.next + 1;   // the write pass draws from the second counter (zeroed with the first)
-    walk_kernel<true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, Wn);
+    const uint32_t pool = W.list ? W.list_n : W.paths;
+    if (pool == 0) return SSTMC_NO_ERROR;
+    walk_kernel<kWrite><<<walk_blocks(pool), threads, 0, stream>>>(S, Wn);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
+}
+
+// One overflow block per 16 paths: paths longer than a slot are rare (about
+// 1 % at a mean of 14 vertices per path), so the pool runs dry only for
+// heavy-tailed scenes, whose overflowing paths then take the write pass.
+uint32_t walk_overflow_blocks(uint32_t paths) { return paths / 16 + 64; }
+
+size_t walk_slot_bytes_per_path()
+{
+    return kSlotVerts * sizeof(float4) + (kSlotVerts * sizeof(float4) + sizeof(uint2)) / 16 + 1 + sizeof(uint32_t);
 }
 
 }  // namespace sstmc

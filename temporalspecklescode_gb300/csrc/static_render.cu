@@ -96,7 +96,7 @@ size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 // Byte layout of the scratch for a chunk of n paths.
 struct Layout {
     size_t V, totals, err, vtotal, ticks, W, fixed_end;
-    size_t a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, counts, misses, offsets, block_sums, rows_end;
+    size_t a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, counts, misses, offsets, block_sums, slots, longq, ovf, ovf_owner, rows_end;
 };
 
 Layout layout(const Scene& S, bool farfar, uint32_t n)
@@ -108,7 +108,7 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.V = take(Nt * Nv * Nl * sizeof(double2));
     L.totals = take(8 * sizeof(unsigned long long));
     L.err = take(sizeof(int));
-    L.vtotal = take(2 * sizeof(unsigned long long));   // total + the walk's two path counters
+    L.vtotal = take(32);   // vertex total, the walk's two path counters, the long-path count
     L.ticks = take(farfar ? Nt * sizeof(double) : 0);
     L.W = take(farfar ? (size_t)kMat * Nt * Nv * Nl * sizeof(float) : 0);
     L.fixed_end = o;
@@ -125,6 +125,10 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.misses = take(n * sizeof(uint32_t));
     L.offsets = take(n * sizeof(uint32_t));
     L.block_sums = take(((n + 1023) / 1024 + 1) * sizeof(uint32_t));
+    L.slots = take((size_t)n * kWalkSlotVerts * sizeof(float4));
+    L.longq = take(n * sizeof(uint32_t));
+    L.ovf = take((size_t)walk_overflow_blocks(n) * kWalkSlotVerts * sizeof(float4));
+    L.ovf_owner = take((size_t)walk_overflow_blocks(n) * sizeof(uint2));
     L.rows_end = o;
     return L;
 }
@@ -148,6 +152,10 @@ void point_engine(Engine& E, unsigned char* base, const Layout& L)
     E.misses = reinterpret_cast<uint32_t*>(base + L.misses);
     E.offsets = reinterpret_cast<uint32_t*>(base + L.offsets);
     E.block_sums = reinterpret_cast<uint32_t*>(base + L.block_sums);
+    E.slots = reinterpret_cast<float4*>(base + L.slots);
+    E.longq = reinterpret_cast<uint32_t*>(base + L.longq);
+    E.ovf = reinterpret_cast<float4*>(base + L.ovf);
+    E.ovf_owner = reinterpret_cast<uint2*>(base + L.ovf_owner);
     E.verts = reinterpret_cast<float4*>(base + L.rows_end);
     E.verts_cap = L.rows_end < kStaticScratchBytes ? (kStaticScratchBytes - L.rows_end) / sizeof(float4) : 0;
 }

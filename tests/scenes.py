@@ -93,6 +93,26 @@ def homogeneous_3d(batch_size=64, full_iteration=1):
     return cfg, 3
 
 
+def long_paths_3d(batch_size=64, full_iteration=2):
+    """Point sources inside an optically thick homogeneous cube (optical
+    radius 20, no absorption): nearly every path runs past 64 vertices, so
+    the walk's overflow blocks are used, the overflow pool runs dry and the
+    write pass replays the rest."""
+    ill = {"type": "PointSource", "location": {"x": [0.0, 0.5], "y": [0.0, -0.5], "z": [5.0, 5.0]}}
+    view = {"type": "PointSource", "location": {"x": [0.0, 2.0, -1.0], "y": [0.0, 0.0, 1.0], "z": [12.0, 12.0, 12.0]}}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 1.0, "seed": 9},
+        "scattering": {"type": ["HG"], "amplitudeFunction": [0.4]},
+        "medium": {"type": "Homogeneous", "boxMin": {"x": [-5.0], "y": [-5.0], "z": [0.0]},
+                   "boxMax": {"x": [5.0], "y": [5.0], "z": [10.0]}, "sigs": 4.0},
+        "illumination": ill, "view": view, "illumination2": ill, "view2": view,
+        "sampler": {"type": "TemporalCorrelationSampler", "t": [0.5, 2.0],
+                    "D": [0.0, 1e-3], "U": {"x": [0.0, 0.0], "y": [0.0, 0.0], "z": [0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -107,4 +127,5 @@ def small_scenes():
         "point_2d_iso_field": point_2d_iso(False),
         "point_2d_iso_corr": point_2d_iso(True),
         "homogeneous_3d": homogeneous_3d(),
+        "long_paths_3d": long_paths_3d(),
     }
