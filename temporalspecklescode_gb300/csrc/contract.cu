@@ -261,15 +261,15 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
 //   e_t = exp2(-c q^2 |tau_t|), c = k^2 D log2(e)
 // The scalar single-scattering amplitude of point x point isotropic scenes
 // (no temporal factor, NextEventEstimation.cuh:1024-1032) is g = 0, c = 0.
-// The tick chain runs on packed FP32 pairs (two ticks per FMA / MUL).
+// The tick chain runs on packed FP32 pairs (the thread's two views per FMA / MUL).
 constexpr int kFl = 32, kFv = 32, kFk = 16, kFt = 8;
 
-constexpr size_t kFastSmem = sizeof(float4) * (kFk * kFl + kFk * kFv) + (sizeof(float2) + sizeof(float)) * kFk + sizeof(float2) * 4 * kFt * 256;
+constexpr size_t kFastSmem = sizeof(float4) * (2 * kFk * kFl + kFk * kFv + kFk) + sizeof(float2) * 4 * kFt * 256;
 
 // Rows here are tick-invariant (static scatterers, identical u1 / u2
 // sources), so only the first tick's rows are read; the tick dependence is
 // the decay exp(-c |t|), chained multiplicatively for geometric ticks.
-// Packed FP32 pairs (Blackwell f32x2 FMA / MUL): two ticks per instruction.
+// Packed FP32 pairs (Blackwell f32x2 FMA / MUL): two values per instruction.
 __device__ __forceinline__ unsigned long long pk2(float lo, float hi)
 {
     return (unsigned long long)__float_as_uint(lo) | ((unsigned long long)__float_as_uint(hi) << 32);
@@ -289,15 +289,32 @@ __device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigne
     return d;
 }
 
-template <bool THREE, bool GEO>
+__device__ __forceinline__ float ex2_fast(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_fast(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ unsigned long long ex2_2(unsigned long long a) { return pk2(ex2_fast(pk_lo(a)), ex2_fast(pk_hi(a))); }
+
+// Accumulators are packed over the thread's view pair, so the whole tick
+// chain runs on f32x2 values: per (path, illumination element, view pair)
+// 2 rsqrt + 2 ex2 and about 30 FP32 instructions for 8 ticks.
+// FIRST: the block's first tick is tick 0 (GEO chain starts at e_s).
+template <bool THREE, bool GEO, bool FIRST>
 __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__ DevScene S, const SsParams G)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* accc = reinterpret_cast<float2*>(smem_raw);                       // [4*kFt][256] compensated (hi, lo) window sums
-    float4* sI = reinterpret_cast<float4*>(accc + 4 * kFt * 256);            // [kFk][kFl] (direction in, row x material coefficient)
-    float* sO = reinterpret_cast<float*>(sI + kFk * kFl);                     // [kFk][4][kFv] (x, y, z, row), views contiguous
-    float2* sM = reinterpret_cast<float2*>(sO + kFk * 4 * kFv);               // [kFk] (g, omg2)
-    float* sC = reinterpret_cast<float*>(sM + kFk);                           // [kFk] c = k^2 D
+    float4* sI = reinterpret_cast<float4*>(accc + 4 * kFt * 256);            // [kFk][kFl][2] (x x y y) (z z w w), w = row x pdf coefficient
+    float* sO = reinterpret_cast<float*>(sI + 2 * kFk * kFl);                 // [kFk][4][kFv] (x, y, z, row), views contiguous
+    float4* sM = reinterpret_cast<float4*>(sO + kFk * 4 * kFv);               // [kFk] (g, omg2, cn, 0), 2^(cn q^2) = decay of the first tick
     // thread: illumination elements l0 + tx + 16 i, view pair v0 + 2 ty + (0, 1)
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int l0 = blockIdx.x * kFl, v0 = blockIdx.y * kFv;
@@ -310,18 +327,16 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     const DevSource& il = S.src[0];
     const DevSource& vw = S.src[1];
     const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
-    const float tau0 = S.abs_ticks[0], taus = S.abs_ticks[t0];
+    const float tau0 = S.abs_ticks[0];
     const unsigned long long neg1 = pk2(-1.0f, -1.0f);
-    unsigned long long acc[2][2][kFt / 2];
+    const float start_scale = (float)(t0 + 1);   // GEO: |t_t0| = (t0 + 1) |t_0|
+    unsigned long long acc[2][kFt];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
+        for (int t = 0; t < kFt; ++t) acc[i][t] = 0ull;
 #pragma unroll
-            for (int t = 0; t < kFt / 2; ++t) acc[i][j][t] = 0ull;
-#pragma unroll
-            for (int t = 0; t < kFt; ++t) accc[((i * 2 + j) * kFt + t) * 256 + threadIdx.x] = make_float2(0.f, 0.f);
-        }
+    for (int t = 0; t < 4 * kFt; ++t) accc[t * 256 + threadIdx.x] = make_float2(0.f, 0.f);
     // staging items of a chunk: 4 per thread, idx = threadIdx.x + 256 u
     // (u = 0, 1: illumination elements; u = 2, 3: view elements).  The next
     // chunk's global loads are issued before the current chunk is computed.
@@ -356,8 +371,9 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 c = S.k2 * S.D[m];
                 if (ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN) { g = S.g[m]; omg2 = (1.0f - g) * (1.0f - g); }
             }
-            sM[threadIdx.x] = make_float2(g, omg2);
-            sC[threadIdx.x] = c;
+            // exp(-c q^2 |t|) = 2^(cn q^2 |t| / |t_0|) (GEO) or 2^(cn q^2 |t|)
+            const float cn = -(GEO ? c * tau0 : c) * 1.44269504088896341f;
+            sM[threadIdx.x] = make_float4(g, omg2, cn, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -376,7 +392,9 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                                  : ty_ == SSTMC_SCATTERING_HENYEY_GREENSTEIN ? S.gup[m]
                                  : ty_ == SSTMC_SCATTERING_ISOTROPIC ? S.iso_pdf : 0.0f;
                 const V3 dir = fsrc_in(il, min(l0 + c, Nl - 1), x);
-                sI[r] = make_float4(dir.x, dir.y, dir.z, pv[u] * coef);
+                const float w = pv[u] * coef;
+                sI[2 * r] = make_float4(dir.x, dir.x, dir.y, dir.y);
+                sI[2 * r + 1] = make_float4(dir.z, dir.z, w, w);
             } else {
                 const V3 dir = fsrc_out(vw, min(v0 + c, Nv - 1), x);
                 float* o = sO + (size_t)pp * 4 * kFv + c;
@@ -387,46 +405,38 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
         __syncthreads();
 #pragma unroll 2
         for (int pp = 0; pp < kFk; ++pp) {
-            const float2 mc = sM[pp];
-            const float cm = sC[pp];
+            const float4 mc = sM[pp];
             const unsigned long long* op = reinterpret_cast<const unsigned long long*>(sO + (size_t)pp * 4 * kFv + 2 * ty);
             const unsigned long long ox = op[0], oy = op[kFv / 2], oz = op[kFv], ob = op[3 * kFv / 2];
-            const unsigned long long g2 = pk2(mc.x, mc.x), omg = pk2(mc.y, mc.y), cq2 = pk2(cm, cm);
+            const unsigned long long g2 = pk2(mc.x, mc.x), omg = pk2(mc.y, mc.y), cn2 = pk2(mc.z, mc.z);
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                const float4 iv = sI[pp * kFl + tx + 16 * i];
+                const ulonglong2 ia = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + tx + 16 * i)];
+                const ulonglong2 ib = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + tx + 16 * i) + 1];
                 // both views of the pair at once: q^2 = |in - out|^2, pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
-                const unsigned long long dx = fma2(ox, neg1, pk2(iv.x, iv.x));
-                const unsigned long long dy = fma2(oy, neg1, pk2(iv.y, iv.y));
-                const unsigned long long dz = fma2(oz, neg1, pk2(iv.z, iv.z));
+                const unsigned long long dx = fma2(ox, neg1, ia.x);
+                const unsigned long long dy = fma2(oy, neg1, ia.y);
+                const unsigned long long dz = fma2(oz, neg1, ib.x);
                 const unsigned long long q2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
                 const unsigned long long dn = fma2(g2, q2, omg);
-                const unsigned long long r = pk2(rsqrtf(pk_lo(dn)), rsqrtf(pk_hi(dn)));
+                const unsigned long long r = pk2(rsqrt_fast(pk_lo(dn)), rsqrt_fast(pk_hi(dn)));
                 const unsigned long long rr = mul2(r, r);
-                const unsigned long long base = mul2(mul2(THREE ? mul2(rr, r) : rr, ob), pk2(iv.w, iv.w));
-                const unsigned long long cq = mul2(cq2, q2);
+                const unsigned long long base = mul2(mul2(THREE ? mul2(rr, r) : rr, ob), ib.y);
+                const unsigned long long arg = mul2(cn2, q2);
+                if (GEO) {
+                    // e_t = e_s^(t + 1), e_s = exp(-c q^2 |t_0|): one ex2 per view, then a product chain
+                    const unsigned long long es = ex2_2(arg);
+                    unsigned long long e = FIRST ? es : ex2_2(mul2(arg, pk2(start_scale, start_scale)));
 #pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    const float bj = j ? pk_hi(base) : pk_lo(base);
-                    const float cj = j ? pk_hi(cq) : pk_lo(cq);
-                    const unsigned long long b2 = pk2(bj, bj);
-                    if (GEO) {
-                        const float es = __expf(-cj * tau0);
-                        const float e0 = t0 == 0 ? es : __expf(-cj * taus);
-                        const float es2 = es * es;
-                        unsigned long long e = pk2(e0, e0 * es);
-                        const unsigned long long st = pk2(es2, es2);
+                    for (int tt = 0; tt < kFt; ++tt) {
+                        acc[i][tt] = fma2(base, e, acc[i][tt]);
+                        if (tt + 1 < kFt) e = mul2(e, es);
+                    }
+                } else {
 #pragma unroll
-                        for (int tt = 0; tt < kFt / 2; ++tt) {
-                            acc[i][j][tt] = fma2(b2, e, acc[i][j][tt]);
-                            if (tt + 1 < kFt / 2) e = mul2(e, st);
-                        }
-                    } else {
-#pragma unroll
-                        for (int tt = 0; tt < kFt / 2; ++tt) {
-                            const int ta = min(t0 + 2 * tt, Nt - 1), tb = min(t0 + 2 * tt + 1, Nt - 1);
-                            acc[i][j][tt] = fma2(b2, pk2(__expf(-cj * S.abs_ticks[ta]), __expf(-cj * S.abs_ticks[tb])), acc[i][j][tt]);
-                        }
+                    for (int tt = 0; tt < kFt; ++tt) {
+                        const float ta = S.abs_ticks[min(t0 + tt, Nt - 1)];
+                        acc[i][tt] = fma2(base, ex2_2(mul2(arg, pk2(ta, ta))), acc[i][tt]);
                     }
                 }
             }
@@ -437,17 +447,15 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
 #pragma unroll
             for (int i = 0; i < 2; ++i)
 #pragma unroll
-                for (int j = 0; j < 2; ++j)
-#pragma unroll
-                    for (int t = 0; t < kFt / 2; ++t) {
-                        float2* c0 = accc + ((i * 2 + j) * kFt + 2 * t) * 256 + threadIdx.x;
-                        float2* c1 = c0 + 256;
-                        float2 a0 = *c0, a1 = *c1;
-                        two_sum_add(a0.x, a0.y, pk_lo(acc[i][j][t]));
-                        two_sum_add(a1.x, a1.y, pk_hi(acc[i][j][t]));
-                        *c0 = a0; *c1 = a1;
-                        acc[i][j][t] = 0ull;
-                    }
+                for (int t = 0; t < kFt; ++t) {
+                    float2* c0 = accc + ((i * 2 + 0) * kFt + t) * 256 + threadIdx.x;
+                    float2* c1 = accc + ((i * 2 + 1) * kFt + t) * 256 + threadIdx.x;
+                    float2 a0 = *c0, a1 = *c1;
+                    two_sum_add(a0.x, a0.y, pk_lo(acc[i][t]));
+                    two_sum_add(a1.x, a1.y, pk_hi(acc[i][t]));
+                    *c0 = a0; *c1 = a1;
+                    acc[i][t] = 0ull;
+                }
         }
     }
 #pragma unroll
@@ -460,7 +468,7 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             for (int tt = 0; tt < kFt; ++tt) {
                 if (tt >= tn) break;
                 const size_t o = ((size_t)(t0 + tt) * Nv + v) * Nl + l;
-                const float last = (tt & 1) ? pk_hi(acc[i][j][tt >> 1]) : pk_lo(acc[i][j][tt >> 1]);
+                const float last = j ? pk_hi(acc[i][tt]) : pk_lo(acc[i][tt]);
                 const float2 c = accc[((i * 2 + j) * kFt + tt) * 256 + threadIdx.x];
                 atomicAdd(&G.V[o].x, (double)c.x + (double)c.y + (double)last);
             }
@@ -494,9 +502,10 @@ int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
         const int ksplit = (G.K + P.kchunk - 1) / P.kchunk;
         dim3 grid((S.src[0].n + kFl - 1) / kFl, (S.src[1].n + kFv - 1) / kFv, tchunks * ksplit);
         using Fn = void (*)(DevScene, SsParams);
-        const bool geo = S.ticks_geometric != 0;
-        Fn f = S.dims == 3 ? (geo ? (Fn)ss_fast_kernel<true, true> : (Fn)ss_fast_kernel<true, false>)
-                           : (geo ? (Fn)ss_fast_kernel<false, true> : (Fn)ss_fast_kernel<false, false>);
+        const bool geo = S.ticks_geometric != 0, first = tchunks == 1;
+        Fn f = S.dims == 3
+            ? (geo ? (first ? (Fn)ss_fast_kernel<true, true, true> : (Fn)ss_fast_kernel<true, true, false>) : (Fn)ss_fast_kernel<true, false, false>)
+            : (geo ? (first ? (Fn)ss_fast_kernel<false, true, true> : (Fn)ss_fast_kernel<false, true, false>) : (Fn)ss_fast_kernel<false, false, false>);
         if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem) != cudaSuccess)
             return SSTMC_CUBLAS_ERROR;
         f<<<grid, 256, kFastSmem, stream>>>(S, P);
