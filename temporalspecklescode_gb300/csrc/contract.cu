@@ -315,7 +315,9 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     float4* sI = reinterpret_cast<float4*>(accc + 4 * kFt * 256);            // [kFk][kFl][2] (x x y y) (z z w w), w = row x pdf coefficient
     float* sO = reinterpret_cast<float*>(sI + 2 * kFk * kFl);                 // [kFk][4][kFv] (x, y, z, row), views contiguous
     float4* sM = reinterpret_cast<float4*>(sO + kFk * 4 * kFv);               // [kFk] (g, omg2, cn, 0), 2^(cn q^2) = decay of the first tick
-    // thread: illumination elements l0 + tx + 16 i, view pair v0 + 2 ty + (0, 1)
+    // thread: view pair v0 + 2 tx + (0, 1), illumination elements l0 + ty + 16 i.
+    // A warp reads two illumination records (broadcast) and 16 consecutive
+    // view pairs (one 128-byte wavefront) from shared memory.
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int l0 = blockIdx.x * kFl, v0 = blockIdx.y * kFv;
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
@@ -406,13 +408,13 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
 #pragma unroll 2
         for (int pp = 0; pp < kFk; ++pp) {
             const float4 mc = sM[pp];
-            const unsigned long long* op = reinterpret_cast<const unsigned long long*>(sO + (size_t)pp * 4 * kFv + 2 * ty);
+            const unsigned long long* op = reinterpret_cast<const unsigned long long*>(sO + (size_t)pp * 4 * kFv + 2 * tx);
             const unsigned long long ox = op[0], oy = op[kFv / 2], oz = op[kFv], ob = op[3 * kFv / 2];
             const unsigned long long g2 = pk2(mc.x, mc.x), omg = pk2(mc.y, mc.y), cn2 = pk2(mc.z, mc.z);
 #pragma unroll
             for (int i = 0; i < 2; ++i) {
-                const ulonglong2 ia = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + tx + 16 * i)];
-                const ulonglong2 ib = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + tx + 16 * i) + 1];
+                const ulonglong2 ia = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i)];
+                const ulonglong2 ib = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i) + 1];
                 // both views of the pair at once: q^2 = |in - out|^2, pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
                 const unsigned long long dx = fma2(ox, neg1, ia.x);
                 const unsigned long long dy = fma2(oy, neg1, ia.y);
@@ -462,7 +464,7 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     for (int i = 0; i < 2; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const int l = l0 + tx + 16 * i, v = v0 + 2 * ty + j;
+            const int l = l0 + ty + 16 * i, v = v0 + 2 * tx + j;
             if (l >= Nl || v >= Nv) continue;
 #pragma unroll
             for (int tt = 0; tt < kFt; ++tt) {
