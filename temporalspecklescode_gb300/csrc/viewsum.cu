@@ -22,6 +22,8 @@
 // the fused trace kernel (trace.cu).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "nee.cuh"
 #include "trace.h"
 #include "viewsum.h"
@@ -45,6 +47,43 @@ struct VRec {
     double ph;              // field: L_b / lambda + xi_b reduced to [-1/2, 1/2] cycles
 };
 
+// Correlation-sampler vertex record: the operands of the packed (two views
+// per instruction) inner loop are stored twice, so a 128-bit shared-memory
+// broadcast yields f32x2 operands directly.
+struct __align__(16) CRec {
+    float x, x_, y, y_;         // position
+    float z, z_, ux, ux_;       // unit direction x_{b-1} -> x_b
+    float uy, uy_, uz, uz_;
+    float k2d, k2d_, mt, mt_;   // k^2 D_{m(b)}; k^2 sum_{3 <= c <= b} D_{m(c-1)} |u_{c-1} - u_c|^2
+    float g, g_, omg2, omg2_;   // pdf = cw (omg2 + g q^2)^(-(D-1)/2)
+    float cw, cw_, sig, sig_;   // cw: pdf coefficient (point views: times the point-source amplitude constant); sig: sigma_t inside
+    float nx0, nx1, ny0, ny1;   // distances to the box faces: x - bmin, bmax - x (single-cell media)
+    float nz0, nz1;
+    uint32_t in, pad;
+};
+static_assert(sizeof(CRec) == 128, "CRec layout");
+
+// PTX approximate transcendental instructions (flush-to-zero forms; the
+// arguments here are never subnormal)
+__device__ __forceinline__ float ex2_ftz(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_ftz(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_ftz(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // (face - x) / d along the axis, face = bmin or bmax by the sign of d (the
 // reference's bdDistance, HeterogeneousMedium.cuh:269-383, for one cell)
 // Packed FP32 pairs (Blackwell f32x2 FMA / MUL)
@@ -66,6 +105,14 @@ __device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigne
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long ex2_2(unsigned long long a) { return pk2(ex2_ftz(pk_lo(a)), ex2_ftz(pk_hi(a))); }
+__device__ __forceinline__ unsigned long long rsqrt_2(unsigned long long a) { return pk2(rsqrt_ftz(pk_lo(a)), rsqrt_ftz(pk_hi(a))); }
 
 // distance to the face the direction component d heads for: n0 = x - bmin
 // (d < 0) or n1 = bmax - x, over |d| (|d| = 0: +inf, which fminf drops)
@@ -273,21 +320,25 @@ __global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevS
     if (lane == 0) st.flush(T);
 }
 
-template <bool CORR, bool VWP, bool SINGLE>
+template <bool CORR, bool VWP, bool SINGLE, bool THREE>
 __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     extern __shared__ __align__(16) unsigned char vsm[];
+    constexpr size_t kRecBytes = CORR ? sizeof(CRec) : sizeof(VRec);
+    constexpr int kVPP = kVPL / 2;   // view pairs per lane (correlation)
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    VRec* rec = reinterpret_cast<VRec*>(vsm) + (size_t)wib * kVB;
-    float* tk = reinterpret_cast<float*>(reinterpret_cast<VRec*>(vsm) + (size_t)(blockDim.x >> 5) * kVB);
+    VRec* rec = reinterpret_cast<VRec*>(vsm + (size_t)wib * kVB * kRecBytes);
+    CRec* crec = reinterpret_cast<CRec*>(vsm + (size_t)wib * kVB * kRecBytes);
+    float* tk = reinterpret_cast<float*>(vsm + (size_t)(blockDim.x >> 5) * kVB * kRecBytes);
     const int Nt = S.Nt, Nv = S.src[1].n;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) tk[t] = S.abs_ticks[t];
     __syncthreads();
     const DevSource& vw = S.src[1];
     const bool split = S.precision == SSTMC_PRECISION_SPLIT;
     const bool geo = S.ticks_geometric != 0;
-    const bool three = S.dims == 3;
+    const bool three = THREE;
+    const bool area = vw.is_area != 0;
     const int t0 = T.t0, tn = T.tn;
     const int nv = T.vn;
     const int vpl = (nv + 31) / 32;
@@ -302,6 +353,20 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
         sv[j] = load3(vw.p, T.v0 + vi);
         if (!VWP) sinv[j] = V3{ __fdividef(1.0f, fabsf(sv[j].x)), __fdividef(1.0f, fabsf(sv[j].y)), __fdividef(1.0f, fabsf(sv[j].z)) };
     }
+    // correlation: the same views as f32x2 pairs (views lane + 64 P and lane + 64 P + 32)
+    unsigned long long pvx[kVPP], pvy[kVPP], pvz[kVPP];
+#pragma unroll
+    for (int P = 0; P < kVPP; ++P) {
+        pvx[P] = pk2(sv[2 * P].x, sv[2 * P + 1].x);
+        pvy[P] = pk2(sv[2 * P].y, sv[2 * P + 1].y);
+        pvz[P] = pk2(sv[2 * P].z, sv[2 * P + 1].z);
+    }
+    // exponent constants: exp(-k^2 |t| C) = 2^(C * (-|t| log2 e))
+    const float kLog2e = 1.44269504088896341f;
+    const unsigned long long neg1 = pk2(-1.0f, -1.0f);
+    const unsigned long long nl2e = pk2(-kLog2e, -kLog2e);
+    const unsigned long long nt0 = pk2(-tk[0] * kLog2e, -tk[0] * kLog2e);
+    const unsigned long long st0 = pk2((float)(t0 + 1), (float)(t0 + 1));   // geometric ticks: |t_t0| = (t0 + 1) |t_0|
     // views of this lane inside the chunk (lanes past its last view count no rays)
     const uint32_t nvalid = (uint32_t)max(0, min(kVPL, (nv - lane + 31) / 32));
 
@@ -311,12 +376,13 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t B = T.counts[q];
         const float4* vq = T.verts + T.offsets[q];
-        // packed pairs: two ticks (correlation) or (re, im) (field)
-        unsigned long long acc[kVPL][CORR ? kNT / 2 : 1];
+        // correlation: ticks of a view pair packed (acc[P][t] = (view 2P, view 2P + 1));
+        // field: (re, im) of each view
+        unsigned long long acc[CORR ? kVPP : kVPL][CORR ? kNT : 1];
 #pragma unroll
-        for (int j = 0; j < kVPL; ++j)
+        for (int j = 0; j < (CORR ? kVPP : kVPL); ++j)
 #pragma unroll
-            for (int k = 0; k < (CORR ? kNT / 2 : 1); ++k) acc[j][k] = 0ull;
+            for (int k = 0; k < (CORR ? kNT : 1); ++k) acc[j][k] = 0ull;
         uint32_t steps = 0;
         float mt_carry = 0.0f;
         double l_carry = 0.0;
@@ -333,31 +399,49 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                     const V3 xc = V3{ c.x, c.y, c.z }, xp = V3{ p.x, p.y, p.z };
                     const V3 u = funit(sub3(xc, xp));
                     const int m = (int)(__float_as_uint(c.w) & 15u);
-                    VRec r;
-                    r.x = c.x; r.y = c.y; r.z = c.z; r.mt = 0.0f;
-                    r.ux = u.x; r.uy = u.y; r.uz = u.z; r.k2d = S.k2 * S.D[m];
                     // pdf (correlation) or amplitude (field) of the phase function as
                     // c (omg2 + g q^2)^(-e): isotropic is g = 0, omg2 = 1
                     const int ty = S.scat_type[m];
-                    r.g = 0.0f; r.omg2 = 1.0f; r.c = 0.0f;
-                    if (VWP && S.iso_all) r.c = CORR ? S.iso_amp * S.iso_amp : S.iso_amp;
-                    else if (ty == SSTMC_SCATTERING_ISOTROPIC) r.c = CORR ? S.iso_pdf : S.iso_amp;
+                    float g = 0.0f, omg2 = 1.0f, cc = 0.0f;
+                    if (VWP && S.iso_all) cc = CORR ? S.iso_amp * S.iso_amp : S.iso_amp;
+                    else if (ty == SSTMC_SCATTERING_ISOTROPIC) cc = CORR ? S.iso_pdf : S.iso_amp;
                     else if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
-                        r.g = S.g[m]; r.omg2 = (1.0f - r.g) * (1.0f - r.g); r.c = CORR ? S.gup[m] : S.sgup[m];
+                        g = S.g[m]; omg2 = (1.0f - g) * (1.0f - g); cc = CORR ? S.gup[m] : S.sgup[m];
                     }
-                    r.in = inside(S, xc) ? 1u : 0u;
-                    r.sig = r.in ? S.sigt[S.grid_m0] : 0.0f;
-                    r.nx0 = c.x - S.bmin[0]; r.nx1 = S.bmax[0] - c.x;
-                    r.ny0 = c.y - S.bmin[1]; r.ny1 = S.bmax[1] - c.y;
-                    r.nz0 = c.z - S.bmin[2]; r.nz1 = S.bmax[2] - c.z;
-                    r.ph = (double)((float)(__float_as_uint(c.w) >> 4) * (1.0f / 16777216.0f));   // xi_b
-                    if (CORR && b >= 3) {
-                        const float4 pp = vq[b - 3];
-                        const V3 up = funit(sub3(xp, V3{ pp.x, pp.y, pp.z }));
-                        const V3 dq = sub3(up, u);
-                        dmt = S.D[__float_as_uint(p.w) & 15u] * dot3(dq, dq);
-                    }
-                    if (!CORR) {
+                    const bool in = inside(S, xc);
+                    const float sig = in ? S.sigt[S.grid_m0] : 0.0f;
+                    if constexpr (CORR) {
+                        CRec r;
+                        r.x = r.x_ = c.x; r.y = r.y_ = c.y; r.z = r.z_ = c.z;
+                        r.ux = r.ux_ = u.x; r.uy = r.uy_ = u.y; r.uz = r.uz_ = u.z;
+                        r.k2d = r.k2d_ = S.k2 * S.D[m];
+                        r.mt = r.mt_ = 0.0f;
+                        r.g = r.g_ = g; r.omg2 = r.omg2_ = omg2;
+                        // point views: |g_v|^2 = exp(-tau) kIsoAmp3 / r^2 (3D) or exp(-tau) / r (2D)
+                        r.cw = r.cw_ = (VWP && THREE) ? cc * kIsoAmp3 : cc;
+                        r.sig = r.sig_ = sig;
+                        r.nx0 = c.x - S.bmin[0]; r.nx1 = S.bmax[0] - c.x;
+                        r.ny0 = c.y - S.bmin[1]; r.ny1 = S.bmax[1] - c.y;
+                        r.nz0 = c.z - S.bmin[2]; r.nz1 = S.bmax[2] - c.z;
+                        r.in = in ? 1u : 0u; r.pad = 0u;
+                        if (b >= 3) {
+                            const float4 pp = vq[b - 3];
+                            const V3 up = funit(sub3(xp, V3{ pp.x, pp.y, pp.z }));
+                            const V3 dq = sub3(up, u);
+                            dmt = S.D[__float_as_uint(p.w) & 15u] * dot3(dq, dq);
+                        }
+                        crec[lane] = r;
+                    } else {
+                        VRec r;
+                        r.x = c.x; r.y = c.y; r.z = c.z; r.mt = 0.0f;
+                        r.ux = u.x; r.uy = u.y; r.uz = u.z; r.k2d = S.k2 * S.D[m];
+                        r.g = g; r.omg2 = omg2; r.c = cc;
+                        r.in = in ? 1u : 0u;
+                        r.sig = sig;
+                        r.nx0 = c.x - S.bmin[0]; r.nx1 = S.bmax[0] - c.x;
+                        r.ny0 = c.y - S.bmin[1]; r.ny1 = S.bmax[1] - c.y;
+                        r.nz0 = c.z - S.bmin[2]; r.nz1 = S.bmax[2] - c.z;
+                        r.ph = (double)((float)(__float_as_uint(c.w) >> 4) * (1.0f / 16777216.0f));   // xi_b
                         if (split) {
                             const double dx = (double)c.x - (double)p.x, dy = (double)c.y - (double)p.y, dz = (double)c.z - (double)p.z;
                             seg = sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
@@ -365,14 +449,14 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                             const V3 dd = sub3(xc, xp);
                             seg = (double)sqrtf(dot3(dd, dd));
                         }
+                        rec[lane] = r;
                     }
-                    rec[lane] = r;
                 }
                 if constexpr (CORR) {
                     float s = dmt;
 #pragma unroll
                     for (int o = 1; o < 32; o <<= 1) { const float n = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += n; }
-                    if (act) rec[lane].mt = S.k2 * (mt_carry + s);
+                    if (act) crec[lane].mt = crec[lane].mt_ = S.k2 * (mt_carry + s);
                     mt_carry += __shfl_sync(0xffffffffu, s, 31);
                 } else {
                     if (split) {
@@ -397,81 +481,148 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                 }
             }
             __syncwarp();
-            // ---- every vertex of the block against this lane's views ----
-            for (int i = 0; i < nb; ++i) {
-                const VRec r = rec[i];
-                const V3 xb = V3{ r.x, r.y, r.z };
-                if (SINGLE) steps += r.in * rays * nvalid;
+            if constexpr (CORR) {
+                // ---- every vertex of the block against this lane's view pairs ----
+                // |g_v|^2 pdf(u_b -> o) exp(-k^2 |t| (D_b |q|^2 + MT_b)), q = u_b - o
+                // (PointSource.cuh:117-172 / FarField.cuh:223-263, TemporalSamplerCorrelation.cuh:384-450)
+                for (int i = 0; i < nb; ++i) {
+                    const CRec* cr = crec + i;
+                    const ulonglong2 r0 = *reinterpret_cast<const ulonglong2*>(&cr->x);     // x, y
+                    const ulonglong2 r1 = *reinterpret_cast<const ulonglong2*>(&cr->z);     // z, ux
+                    const ulonglong2 r2 = *reinterpret_cast<const ulonglong2*>(&cr->uy);    // uy, uz
+                    const ulonglong2 r3 = *reinterpret_cast<const ulonglong2*>(&cr->k2d);   // k2d, mt
+                    const ulonglong2 r4 = *reinterpret_cast<const ulonglong2*>(&cr->g);     // g, omg2
+                    const ulonglong2 r5 = *reinterpret_cast<const ulonglong2*>(&cr->cw);    // cw, sig
+                    const float4 nf = *reinterpret_cast<const float4*>(&cr->nx0);
+                    const float4 nz = *reinterpret_cast<const float4*>(&cr->nz0);
+                    const uint32_t rin = __float_as_uint(nz.z);
+                    if (SINGLE) steps += rin * rays * nvalid;
 #pragma unroll
-                for (int j = 0; j < kVPL; ++j) {
-                    if (j >= vpl) break;
-                    const bool vok = lane + 32 * j < nv;   // lanes past the chunk's last view count no rays
-                    // direction to the view and optical depth toward it (to the grid edge)
-                    V3 o;
-                    float tau, ri = 1.0f;
-                    if constexpr (VWP) {
-                        const V3 d = sub3(sv[j], xb);
-                        const float r2 = dot3(d, d);
-                        ri = rsqrtf(r2);
-                        o = V3{ d.x * ri, d.y * ri, d.z * ri };
-                    } else {
-                        o = sv[j];
-                    }
-                    if constexpr (SINGLE) {
-                        float tm;
+                    for (int P = 0; P < kVPP; ++P) {
+                        if (2 * P >= vpl) break;
+                        // direction to the views (unit) and optical depth toward them
+                        unsigned long long ox, oy, oz, ri = 0ull;
                         if constexpr (VWP) {
-                            tm = fminf(face_t(o.x, r.nx0, r.nx1), face_t(o.y, r.ny0, r.ny1));
-                            if (three) tm = fminf(tm, face_t(o.z, r.nz0, r.nz1));
+                            const unsigned long long dx = fma2(r0.x, neg1, pvx[P]);
+                            const unsigned long long dy = fma2(r0.y, neg1, pvy[P]);
+                            const unsigned long long dz = THREE ? fma2(r1.x, neg1, pvz[P]) : 0ull;
+                            const unsigned long long d2 = fma2(dx, dx, THREE ? fma2(dy, dy, mul2(dz, dz)) : mul2(dy, dy));
+                            ri = rsqrt_2(d2);
+                            ox = mul2(dx, ri); oy = mul2(dy, ri); oz = THREE ? mul2(dz, ri) : 0ull;
                         } else {
-                            tm = fminf((o.x < 0.0f ? r.nx0 : r.nx1) * sinv[j].x, (o.y < 0.0f ? r.ny0 : r.ny1) * sinv[j].y);
-                            if (three) tm = fminf(tm, (o.z < 0.0f ? r.nz0 : r.nz1) * sinv[j].z);
+                            ox = pvx[P]; oy = pvy[P]; oz = pvz[P];
                         }
-                        tau = tm * r.sig;
-                    } else {
-                        uint32_t st = 0;
-                        tau = VWP ? tau_to_point(S, xb, sv[j], st) : tau_dir(S, xb, o, st);
-                        steps += vok ? st * rays : 0u;
-                    }
-                    const V3 df = V3{ r.ux - o.x, r.uy - o.y, r.uz - o.z };
-                    const float q2 = dot3(df, df);
-                    const float rr = rsqrtf(fmaf(r.g, q2, r.omg2));
-                    if constexpr (CORR) {
-                        // |g|^2 (PointSource.cuh:117-172 / FarField.cuh:223-263) times the pdf
-                        float w = __expf(-tau);
+                        unsigned long long tau2;
+                        if constexpr (SINGLE) {
+                            float tm[2];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const float oxh = h ? pk_hi(ox) : pk_lo(ox), oyh = h ? pk_hi(oy) : pk_lo(oy);
+                                // distance to the face the direction heads for (|o| = 0: +inf, dropped by fminf)
+                                const float ix = VWP ? rcp_ftz(fabsf(oxh)) : sinv[2 * P + h].x;
+                                const float iy = VWP ? rcp_ftz(fabsf(oyh)) : sinv[2 * P + h].y;
+                                float t = fminf((oxh < 0.0f ? nf.x : nf.y) * ix, (oyh < 0.0f ? nf.z : nf.w) * iy);
+                                if (THREE) {
+                                    const float ozh = h ? pk_hi(oz) : pk_lo(oz);
+                                    const float iz = VWP ? rcp_ftz(fabsf(ozh)) : sinv[2 * P + h].z;
+                                    t = fminf(t, (ozh < 0.0f ? nz.x : nz.y) * iz);
+                                }
+                                tm[h] = t;
+                            }
+                            tau2 = mul2(pk2(tm[0], tm[1]), r5.y);
+                        } else {
+                            float tt[2];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const V3 xb = V3{ pk_lo(r0.x), pk_lo(r0.y), pk_lo(r1.x) };
+                                uint32_t st = 0;
+                                const V3 oh = V3{ h ? pk_hi(ox) : pk_lo(ox), h ? pk_hi(oy) : pk_lo(oy), h ? pk_hi(oz) : pk_lo(oz) };
+                                tt[h] = VWP ? tau_to_point(S, xb, sv[2 * P + h], st) : tau_dir(S, xb, oh, st);
+                                steps += (lane + 32 * (2 * P + h) < nv) ? st * rays : 0u;
+                            }
+                            tau2 = pk2(tt[0], tt[1]);
+                        }
+                        // q = u_b - o, pdf = cw (omg2 + g q^2)^(-(D-1)/2)
+                        const unsigned long long qx = fma2(ox, neg1, r1.y);
+                        const unsigned long long qy = fma2(oy, neg1, r2.x);
+                        const unsigned long long qz = THREE ? fma2(oz, neg1, r2.y) : 0ull;
+                        const unsigned long long q2 = fma2(qx, qx, THREE ? fma2(qy, qy, mul2(qz, qz)) : mul2(qy, qy));
+                        const unsigned long long rr = rsqrt_2(fma2(r4.x, q2, r4.y));
+                        unsigned long long wgt = mul2(mul2(rr, rr), r5.x);
+                        if (THREE) wgt = mul2(wgt, rr);
                         if constexpr (VWP) {
-                            w = three ? w * kIsoAmp3 * ri * ri : w * ri;
-                            if (vw.is_area) w *= fabsf(three ? o.z : o.y);
+                            wgt = mul2(wgt, THREE ? mul2(ri, ri) : ri);
+                            if (area) {
+                                const unsigned long long oa = THREE ? oz : oy;
+                                wgt = mul2(wgt, pk2(fabsf(pk_lo(oa)), fabsf(pk_hi(oa))));
+                            }
                         }
-                        const float pdf = three ? r.c * rr * rr * rr : r.c * rr * rr;
-                        // decorrelation exp(-k^2 |t| (D_b |q|^2 + MT_b)), q = u_b - o (TemporalSamplerCorrelation.cuh:384-450)
-                        const float ck = fmaf(r.k2d, q2, r.mt);
-                        const float bw = w * pdf;
-                        const unsigned long long b2 = pk2(bw, bw);
+                        // decorrelation exponent C = D_b |q|^2 + MT_b, exp(-tau) folded into the first factor
+                        const unsigned long long ck = fma2(r3.x, q2, r3.y);
+                        const unsigned long long tl = mul2(tau2, nl2e);
                         if (geo) {
-                            const float es = __expf(-ck * tk[0]);
-                            const float e0 = t0 == 0 ? es : __expf(-ck * tk[t0]);
-                            const float es2 = es * es;
-                            unsigned long long e = pk2(e0, e0 * es);
-                            const unsigned long long st = pk2(es2, es2);
+                            const unsigned long long as = mul2(ck, nt0);
+                            const unsigned long long es = ex2_2(as);
+                            unsigned long long e = mul2(wgt, ex2_2(add2(tl, t0 == 0 ? as : mul2(as, st0))));
 #pragma unroll
-                            for (int k = 0; k < kNT / 2; ++k) {
-                                acc[j][k] = fma2(b2, e, acc[j][k]);
-                                if (k + 1 < kNT / 2) e = mul2(e, st);
+                            for (int k = 0; k < kNT; ++k) {
+                                acc[P][k] = add2(acc[P][k], e);
+                                if (k + 1 < kNT) e = mul2(e, es);
                             }
                         } else {
 #pragma unroll
-                            for (int k = 0; k < kNT / 2; ++k) {
-                                const int ta = t0 + min(2 * k, tn - 1), tb = t0 + min(2 * k + 1, tn - 1);
-                                acc[j][k] = fma2(b2, pk2(__expf(-ck * tk[ta]), __expf(-ck * tk[tb])), acc[j][k]);
+                            for (int k = 0; k < kNT; ++k) {
+                                const float nt = -tk[t0 + min(k, tn - 1)] * kLog2e;
+                                acc[P][k] = fma2(wgt, ex2_2(fma2(ck, pk2(nt, nt), tl)), acc[P][k]);
                             }
                         }
-                    } else {
+                    }
+                }
+            } else {
+                // ---- field: every vertex of the block against this lane's views ----
+                for (int i = 0; i < nb; ++i) {
+                    const VRec r = rec[i];
+                    const V3 xb = V3{ r.x, r.y, r.z };
+                    if (SINGLE) steps += r.in * rays * nvalid;
+#pragma unroll
+                    for (int j = 0; j < kVPL; ++j) {
+                        if (j >= vpl) break;
+                        const bool vok = lane + 32 * j < nv;   // lanes past the chunk's last view count no rays
+                        // direction to the view and optical depth toward it (to the grid edge)
+                        V3 o;
+                        float tau, ri = 1.0f;
+                        if constexpr (VWP) {
+                            const V3 d = sub3(sv[j], xb);
+                            const float r2 = dot3(d, d);
+                            ri = rsqrtf(r2);
+                            o = V3{ d.x * ri, d.y * ri, d.z * ri };
+                        } else {
+                            o = sv[j];
+                        }
+                        if constexpr (SINGLE) {
+                            float tm;
+                            if constexpr (VWP) {
+                                tm = fminf(face_t(o.x, r.nx0, r.nx1), face_t(o.y, r.ny0, r.ny1));
+                                if (three) tm = fminf(tm, face_t(o.z, r.nz0, r.nz1));
+                            } else {
+                                tm = fminf((o.x < 0.0f ? r.nx0 : r.nx1) * sinv[j].x, (o.y < 0.0f ? r.ny0 : r.ny1) * sinv[j].y);
+                                if (three) tm = fminf(tm, (o.z < 0.0f ? r.nz0 : r.nz1) * sinv[j].z);
+                            }
+                            tau = tm * r.sig;
+                        } else {
+                            uint32_t st = 0;
+                            tau = VWP ? tau_to_point(S, xb, sv[j], st) : tau_dir(S, xb, o, st);
+                            steps += vok ? st * rays : 0u;
+                        }
+                        const V3 df = V3{ r.ux - o.x, r.uy - o.y, r.uz - o.z };
+                        const float q2 = dot3(df, df);
+                        const float rr = rsqrtf(fmaf(r.g, q2, r.omg2));
                         // g f exp(2 pi i (phase of g + L_b / lambda + xi_b))
                         float a, f;
                         if constexpr (VWP) {
                             float at = __expf(-tau);
                             at = three ? at * kIsoAmp3 * ri * ri : at * ri;
-                            if (vw.is_area) at *= fabsf(three ? o.z : o.y);
+                            if (area) at *= fabsf(three ? o.z : o.y);
                             a = sqrtf(at);
                             if (split) {
                                 const double dx = (double)xb.x - (double)sv[j].x, dy = (double)xb.y - (double)sv[j].y,
@@ -513,7 +664,8 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
 #pragma unroll
                 for (int k = 0; k < kNT; ++k)
                     if (k < tn) {
-                        const float a = (k & 1) ? pk_hi(acc[j][k >> 1]) : pk_lo(acc[j][k >> 1]);
+                        const unsigned long long a2 = acc[j >> 1][k];
+                        const float a = (j & 1) ? pk_hi(a2) : pk_lo(a2);
                         T.s_ms[((size_t)q * Nt + t0 + k) * Nv + v] = make_float2(a, 0.0f);
                     }
             } else {
@@ -534,7 +686,7 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
 
 size_t view_smem_bytes(int Nt, int threads)
 {
-    return (size_t)(threads / 32) * kVB * sizeof(VRec) + (size_t)Nt * sizeof(float);
+    return (size_t)(threads / 32) * kVB * std::max(sizeof(VRec), sizeof(CRec)) + (size_t)Nt * sizeof(float);
 }
 
 int view_max_ticks(const DevScene& S) { return S.correlation ? kNT : S.Nt; }
@@ -552,12 +704,15 @@ int launch_view(const DevScene& S, const TraceParams& T, int blocks, int threads
     const bool vp = S.src[1].type == SSTMC_SOURCE_POINT;
     using Fn = void (*)(DevScene, TraceParams);
     Fn f;
+#define SSTMC_VIEW_PICK(C, V, SG)                                                                            \
+    (S.dims == 3 ? (Fn)view_kernel<C, V, SG, true> : (Fn)view_kernel<C, V, SG, false>)
     if (S.single)
-        f = S.correlation ? (vp ? (Fn)view_kernel<true, true, true> : (Fn)view_kernel<true, false, true>)
-                          : (vp ? (Fn)view_kernel<false, true, true> : (Fn)view_kernel<false, false, true>);
+        f = S.correlation ? (vp ? SSTMC_VIEW_PICK(true, true, true) : SSTMC_VIEW_PICK(true, false, true))
+                          : (vp ? SSTMC_VIEW_PICK(false, true, true) : SSTMC_VIEW_PICK(false, false, true));
     else
-        f = S.correlation ? (vp ? (Fn)view_kernel<true, true, false> : (Fn)view_kernel<true, false, false>)
-                          : (vp ? (Fn)view_kernel<false, true, false> : (Fn)view_kernel<false, false, false>);
+        f = S.correlation ? (vp ? SSTMC_VIEW_PICK(true, true, false) : SSTMC_VIEW_PICK(true, false, false))
+                          : (vp ? SSTMC_VIEW_PICK(false, true, false) : SSTMC_VIEW_PICK(false, false, false));
+#undef SSTMC_VIEW_PICK
     if (smem > 48 * 1024 && cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SSTMC_KERNEL_ERROR;
     f<<<blocks, threads, smem, stream>>>(S, T);
