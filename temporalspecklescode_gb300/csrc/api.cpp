@@ -110,7 +110,7 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&counts, paths * sizeof(uint32_t)) && alloc((void**)&misses, paths * sizeof(uint32_t))
            && alloc((void**)&offsets, paths * sizeof(uint32_t))
            && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
-           && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, the long-path count
+           && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' path counter
            && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
            && alloc((void**)&ovf, (size_t)walk_overflow_blocks(paths) * kWalkSlotVerts * sizeof(float4))
            && alloc((void**)&ovf_owner, (size_t)walk_overflow_blocks(paths) * sizeof(uint2));
@@ -275,12 +275,13 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         // far-field GEMM and the per-path debug trace read every tick
         const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD;
         T.ss_all_ticks = (dbg || farfar) ? 1 : 0;
+        T.work = reinterpret_cast<uint32_t*>(vtotal) + 6;   // bytes 24..27 of the counter block
         if (illum_kernel_covers(S.dev)) e = launch_illum(S.dev, T, std::max(1, std::min((int)((n + 3) / 4), sms * 16)), threads, stream);
         else e = launch_trace(S.dev, T, blocks, threads, stream);
         if (e) return e;
         launches++;
-        const int vmax = view_max_views(), tmax = view_max_ticks(S.dev);
-        const int vblocks = std::max(1, std::min((int)((n + 3) / 4), sms * 8));
+        const int vmax = view_max_views(S.dev), tmax = view_max_ticks(S.dev);
+        const int vblocks = std::max(1, (int)((n + 3) / 4));   // clamped to one resident wave by launch_view
         for (int v = 0; v < S.Nv; v += vmax)
             for (int t = 0; t < S.Nt; t += tmax) {
                 T.v0 = v; T.vn = std::min(vmax, S.Nv - v); T.t0 = t; T.tn = std::min(tmax, S.Nt - t);

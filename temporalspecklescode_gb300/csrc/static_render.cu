@@ -108,7 +108,7 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.V = take(Nt * Nv * Nl * sizeof(double2));
     L.totals = take(8 * sizeof(unsigned long long));
     L.err = take(sizeof(int));
-    L.vtotal = take(32);   // vertex total, the walk's two path counters, the long-path count
+    L.vtotal = take(32);   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' path counter
     L.ticks = take(farfar ? Nt * sizeof(double) : 0);
     L.W = take(farfar ? (size_t)kMat * Nt * Nv * Nl * sizeof(float) : 0);
     L.fixed_end = o;

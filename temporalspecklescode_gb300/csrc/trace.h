@@ -35,6 +35,7 @@ struct TraceParams {
     uint32_t* dda;        // [paths] or null (accumulated over passes)
     unsigned long long* totals;  // [0] vertices, [1] dda steps, [2] misses, [3] paths
     int* err;
+    uint32_t* work;       // [1] or null: path counter of the warp-per-path kernels (zeroed by their launchers)
 };
 
 size_t trace_smem_bytes(int Nt, int slots, int threads);

@@ -34,7 +34,8 @@ namespace {
 
 constexpr int kVB = 32;     // vertices per block
 constexpr int kNT = 8;      // ticks per pass (correlation)
-constexpr int kVPL = 4;     // views per lane per pass
+constexpr int kVPL = 4;     // views per lane per pass (field)
+constexpr int kVPP = 1;     // view pairs per lane per pass (correlation: 64 views, registers for 5 blocks of 128 threads)
 constexpr int kMaxIllum = 8;   // illumination elements per lane (illumination side: Nl <= 256)
 
 struct VRec {
@@ -156,6 +157,17 @@ __device__ __forceinline__ float tau_d(const DevScene& S, const V3& x, const V3&
     } else {
         return tau_dir(S, x, d, st);
     }
+}
+
+// Next path of a warp: warps start at their own index and then draw from
+// T.work (one atomic per path), so a warp that drew short paths takes more
+// of them; without a counter, a fixed stride over the paths.
+__device__ __forceinline__ uint32_t next_path(const TraceParams& T, uint32_t q, uint32_t nw, int lane)
+{
+    if (T.work == nullptr) return q + nw;
+    uint32_t c = 0;
+    if (lane == 0) c = atomicAdd(T.work, 1u);
+    return nw + __shfl_sync(0xffffffffu, c, 0);
 }
 
 // Per-warp sums of the render statistics (lane 0 adds them to the global
@@ -315,7 +327,7 @@ __global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevS
 #pragma unroll
     for (int k = 0; k < NLK; ++k) lsrc[k] = load3(S.src[0].p, min(lane + 32 * k, S.src[0].n - 1));
     WarpStats st;
-    for (uint32_t q = gw; q < T.paths; q += nw)
+    for (uint32_t q = gw; q < T.paths; q = next_path(T, q, nw, lane))
         illum_path<NLK, ILP, VWP, SINGLE>(S, T, q, lane, T.counts[q], T.verts + T.offsets[q], lsrc, st);
     if (lane == 0) st.flush(T);
 }
@@ -325,7 +337,6 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
 {
     extern __shared__ __align__(16) unsigned char vsm[];
     constexpr size_t kRecBytes = CORR ? sizeof(CRec) : sizeof(VRec);
-    constexpr int kVPP = kVPL / 2;   // view pairs per lane (correlation)
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     VRec* rec = reinterpret_cast<VRec*>(vsm + (size_t)wib * kVB * kRecBytes);
@@ -345,15 +356,16 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
     // ray steps per (vertex, view): one ray per tick (u1 and u2 for the correlation sampler)
     const uint32_t rays = (uint32_t)(CORR ? 2 * tn : tn);
     // this lane's views: position or direction, and (far field) the reciprocal direction
-    V3 sv[kVPL];
-    V3 sinv[kVPL];
+    constexpr int kVL = CORR ? 2 * kVPP : kVPL;   // views per lane
+    V3 sv[kVL];
+    V3 sinv[kVL];
 #pragma unroll
-    for (int j = 0; j < kVPL; ++j) {
+    for (int j = 0; j < kVL; ++j) {
         const int vi = min(lane + 32 * j, nv - 1);
         sv[j] = load3(vw.p, T.v0 + vi);
         if (!VWP) sinv[j] = V3{ __fdividef(1.0f, fabsf(sv[j].x)), __fdividef(1.0f, fabsf(sv[j].y)), __fdividef(1.0f, fabsf(sv[j].z)) };
     }
-    // correlation: the same views as f32x2 pairs (views lane + 64 P and lane + 64 P + 32)
+    // correlation: views lane + 32 (2 P) and lane + 32 (2 P + 1) as f32x2 pairs
     unsigned long long pvx[kVPP], pvy[kVPP], pvz[kVPP];
 #pragma unroll
     for (int P = 0; P < kVPP; ++P) {
@@ -368,12 +380,12 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
     const unsigned long long nt0 = pk2(-tk[0] * kLog2e, -tk[0] * kLog2e);
     const unsigned long long st0 = pk2((float)(t0 + 1), (float)(t0 + 1));   // geometric ticks: |t_t0| = (t0 + 1) |t_0|
     // views of this lane inside the chunk (lanes past its last view count no rays)
-    const uint32_t nvalid = (uint32_t)max(0, min(kVPL, (nv - lane + 31) / 32));
+    const uint32_t nvalid = (uint32_t)max(0, min(kVL, (nv - lane + 31) / 32));
 
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     unsigned long long warp_steps = 0;
-    for (uint32_t q = gw; q < T.paths; q += nw) {
+    for (uint32_t q = gw; q < T.paths; q = next_path(T, q, nw, lane)) {
         const uint32_t B = T.counts[q];
         const float4* vq = T.verts + T.offsets[q];
         // correlation: ticks of a view pair packed (acc[P][t] = (view 2P, view 2P + 1));
@@ -656,7 +668,7 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
         }
         // ---- write S[q][t][v] ----
 #pragma unroll
-        for (int j = 0; j < kVPL; ++j) {
+        for (int j = 0; j < kVL; ++j) {
             const int vi = lane + 32 * j;
             if (j >= vpl || vi >= nv) break;
             const int v = T.v0 + vi;
@@ -690,7 +702,7 @@ size_t view_smem_bytes(int Nt, int threads)
 }
 
 int view_max_ticks(const DevScene& S) { return S.correlation ? kNT : S.Nt; }
-int view_max_views() { return 32 * kVPL; }
+int view_max_views(const DevScene& S) { return S.correlation ? 64 * kVPP : 32 * kVPL; }
 
 bool view_kernel_covers(const DevScene& S, const bool* moving_any)
 {
@@ -715,6 +727,13 @@ int launch_view(const DevScene& S, const TraceParams& T, int blocks, int threads
 #undef SSTMC_VIEW_PICK
     if (smem > 48 * 1024 && cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SSTMC_KERNEL_ERROR;
+    // one wave of resident blocks (warps stride over the paths)
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)f, threads, smem) == cudaSuccess && occ > 0)
+        blocks = std::max(1, std::min(blocks, occ * sms));
+    if (T.work && cudaMemsetAsync(T.work, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     f<<<blocks, threads, smem, stream>>>(S, T);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
@@ -744,6 +763,7 @@ int launch_illum(const DevScene& S, const TraceParams& T, int blocks, int thread
             f = ip ? (vp ? (Fn)illum_kernel<kMaxIllum, true, true, false> : (Fn)illum_kernel<kMaxIllum, true, false, false>)
                    : (vp ? (Fn)illum_kernel<kMaxIllum, false, true, false> : (Fn)illum_kernel<kMaxIllum, false, false, false>);
     }
+    if (T.work && cudaMemsetAsync(T.work, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     f<<<blocks, threads, 0, stream>>>(S, T);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }

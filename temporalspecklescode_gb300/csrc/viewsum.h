@@ -13,7 +13,7 @@ namespace sstmc {
 bool view_kernel_covers(const DevScene& S, const bool* moving_any);
 // Largest tick and view chunk of one launch.
 int view_max_ticks(const DevScene& S);
-int view_max_views();
+int view_max_views(const DevScene& S);
 size_t view_smem_bytes(int Nt, int threads);
 // S[q][t][v] for t in [T.t0, T.t0 + T.tn), v in [T.v0, T.v0 + T.vn).
 int launch_view(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream);
