@@ -258,6 +258,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     T.a_ms = a_ms; T.s_ms = s_ms; T.a_ss = a_ss; T.b_ss = b_ss; T.g2 = g2; T.pl = pl;
     T.x1 = x1; T.x1t = S.correlation ? nullptr : x1t; T.m1 = m1; T.totals = totals; T.err = err;
     if (dbg) T.dda = dbg->dda;
+    rows_real = false;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -276,6 +277,11 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD;
         T.ss_all_ticks = (dbg || farfar) ? 1 : 0;
         T.work = reinterpret_cast<uint32_t*>(vtotal) + 6;   // bytes 24..27 of the counter block
+        // correlation rows are real here: with the tensor-core GEMM they are stored as
+        // floats (half the bytes); the debug trace reads the complex layout
+        rows_real = S.correlation && illum_kernel_covers(S.dev) && use_tensor_cores() && !dbg
+                 && S.precision == SSTMC_PRECISION_SPLIT && S.Nt % 2 == 0 && S.Nl % 2 == 0 && S.Nv % 2 == 0;
+        T.real_rows = rows_real ? 1 : 0;
         if (illum_kernel_covers(S.dev)) e = launch_illum(S.dev, T, std::max(1, std::min((int)((n + 3) / 4), sms * 16)), threads, stream);
         else e = launch_trace(S.dev, T, blocks, threads, stream);
         if (e) return e;
@@ -322,7 +328,9 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     G.kchunk = kchunk;
     G.A = a_ms; G.B = s_ms;
     G.err = err;
+    G.real = rows_real ? 1 : 0;
     const bool tc = use_tensor_cores() && gemm_tc_eligible(G);
+    if (G.real && !tc) return SSTMC_MISC_ERROR;   // real rows are written only for the tensor-core form
     auto gemm = [&](const GemmParams& P) { return tc ? launch_gemm_tc(P, stream) : launch_gemm(P, stream); };
     int e = gemm(G);
     if (e) return e;
@@ -333,7 +341,7 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
         e = prepare_ss_tables(S);
         if (e) return e;
         const size_t per = (size_t)S.Nt * S.Nv * S.Nl;
-        G.A = a_ss; G.B = b_ss; G.mat = m1;
+        G.A = a_ss; G.B = b_ss; G.mat = m1; G.real = 0;
         for (int m : S.materials_present) {
             G.mat_sel = m;
             G.W = W + (size_t)m * per;

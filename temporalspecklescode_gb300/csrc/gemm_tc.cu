@@ -9,6 +9,11 @@
 // The complex product is a real GEMM over interleaved (re, im) rows:
 // D[m][n] = sum_p a[p][m] b[p][n] with m = 2l + re/im, n = 2v + re/im, then
 // Re V = D[2l][2v] - D[2l+1][2v+1], Im V = D[2l][2v+1] + D[2l+1][2v].
+// Real rows (G.real, the correlation sampler with identical u1 / u2 sources
+// and static scatterers): two ticks of a path are 2 Nl (or 2 Nv) consecutive
+// floats, so the same 128-row tiles span a tick pair and D's diagonal blocks
+// (tick of m == tick of n) are the two ticks' products; the row bytes read
+// from HBM are half the complex form's.
 // Each FP32 operand x is split into TF32 parts hi = rna(x), lo = rna(x - hi),
 // and D accumulates hi*hi + hi*lo + lo*hi.
 //
@@ -237,8 +242,9 @@ __device__ __forceinline__ void two_sum(float& hi, float& lo, float x)
 struct TcParams {
     GemmParams G;
     int tiles_m, tiles_n;
-    CUtensorMap tmA;   // A viewed as [K paths][Nt][2 Nl floats], box 32 x 1 x 128
-    CUtensorMap tmB;   // B viewed as [K paths][Nt][2 Nv floats], box 32 x 1 x 64
+    int tdim;          // middle tensor dimension: Nt ticks (complex) or Nt / 2 tick pairs (real)
+    CUtensorMap tmA;   // A viewed as [K paths][tdim][2 Nl floats], box 32 x 1 x 128
+    CUtensorMap tmB;   // B viewed as [K paths][tdim][2 Nv floats], box 32 x 1 x 128
 };
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
@@ -314,8 +320,8 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
     int bid = blockIdx.x;
     const int tn = bid % P.tiles_n; bid /= P.tiles_n;
     const int tm = bid % P.tiles_m; bid /= P.tiles_m;
-    const int t = bid % G.Nt;
-    const int ks = bid / G.Nt;
+    const int t = bid % P.tdim;
+    const int ks = bid / P.tdim;
     const int kb = ks * G.kchunk;
     const int ke = min(G.K, kb + G.kchunk);
     const int nsteps = ke > kb ? (ke - kb + kKS - 1) / kKS : 0;
@@ -452,7 +458,30 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
             }
             tmem_wait_st();
         }
-        if (ok && nwin > 0) {
+        if (ok && nwin > 0 && G.real) {
+            // real rows: row m = tick (2 t + mt) of illumination l, column n = tick
+            // (2 t + nt) of view v; the same-tick blocks are the two ticks' sums
+            const int gm = m0 + 32 * q + lane;
+            const int mt = gm / G.Nl, l = gm - mt * G.Nl;
+            const int tick = 2 * t + mt;
+#pragma unroll 1
+            for (int c = 0; c < kTN / 16; ++c) {
+                float hv[16], lv[16];
+                tmem_ld16(row_addr + kColHi + 16u * c, hv);
+                tmem_ld16(row_addr + kColLo + 16u * c, lv);
+                tmem_wait_ld();
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int gn = n0 + 16 * c + e;
+                    const int nt = gn / G.Nv, v = gn - nt * G.Nv;
+                    if (nt == mt && mt < 2 && tick < G.Nt) {
+                        const size_t o = ((size_t)tick * G.Nv + v) * G.Nl + l;
+                        const double wv = G.W ? (double)G.W[o] : 1.0;
+                        atomicAdd(&G.V[o].x, ((double)hv[e] + (double)lv[e]) * wv);
+                    }
+                }
+            }
+        } else if (ok && nwin > 0) {
             // rows m (even: Re a, odd: Im a) pair up across adjacent lanes
             const int m = 32 * q + lane;
             const int gm = m0 + m;
@@ -491,10 +520,12 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
 
 }  // namespace
 
-// TMA needs 16-byte row strides: Nl and Nv even (odd counts use gemm_kernel).
+// TMA needs 16-byte row strides: Nl and Nv even (odd counts use gemm_kernel);
+// real rows pair ticks: Nt even.
 bool gemm_tc_eligible(const GemmParams& G)
 {
     return G.compensated != 0 && G.K > 0 && G.Nl > 0 && G.Nv > 0 && G.Nl % 2 == 0 && G.Nv % 2 == 0
+        && (!G.real || G.Nt % 2 == 0)
         && reinterpret_cast<uintptr_t>(G.A) % 16 == 0 && reinterpret_cast<uintptr_t>(G.B) % 16 == 0;
 }
 
@@ -535,16 +566,19 @@ int launch_gemm_tc(const GemmParams& G, cudaStream_t stream)
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     TcParams P;
     P.G = G;
+    if (G.real && G.Nt % 2 != 0) return SSTMC_CUBLAS_ERROR;
     P.tiles_m = (2 * G.Nl + kTM - 1) / kTM;
     P.tiles_n = (2 * G.Nv + kTN - 1) / kTN;
-    const long long tiles = (long long)P.tiles_m * P.tiles_n * G.Nt;
+    P.tdim = G.real ? G.Nt / 2 : G.Nt;
+    const long long tiles = (long long)P.tiles_m * P.tiles_n * P.tdim;
     int ksplit = (int)std::max<long long>(1, sms / std::max<long long>(1, tiles));
     const int win = kKS * kWinSteps;
     int kchunk = (G.K + ksplit - 1) / ksplit;
     kchunk = ((kchunk + win - 1) / win) * win;
     ksplit = (G.K + kchunk - 1) / kchunk;
     P.G.kchunk = kchunk;
-    if (!encode_rows(&P.tmA, G.A, 2 * G.Nl, G.Nt, G.K, kTM) || !encode_rows(&P.tmB, G.B, 2 * G.Nv, G.Nt, G.K, kTN))
+    // complex: 2 Nl floats (re, im) per tick; real: 2 Nl floats per tick pair
+    if (!encode_rows(&P.tmA, G.A, 2 * G.Nl, P.tdim, G.K, kTM) || !encode_rows(&P.tmB, G.B, 2 * G.Nv, P.tdim, G.K, kTN))
         return SSTMC_CUBLAS_ERROR;
     const long long grid = tiles * ksplit;
     if (grid <= 0 || grid > 0x7fffffffLL) return SSTMC_CUBLAS_ERROR;

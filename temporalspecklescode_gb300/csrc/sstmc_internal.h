@@ -30,6 +30,7 @@ struct Engine {
     unsigned char* m1 = nullptr;
     uint32_t *counts = nullptr, *misses = nullptr, *offsets = nullptr, *block_sums = nullptr;
     unsigned long long* vtotal = nullptr;
+    bool rows_real = false;       // the chunk's a_ms / s_ms are real floats (trace_chunk -> contract_chunk)
     float4* slots = nullptr;      // single-pass walk: first 64 vertices of each path of a chunk
     uint32_t* longq = nullptr;    // paths of the chunk that found the overflow pool empty
     float4* ovf = nullptr;        // overflow blocks of 64 vertices (pathwalk.cu)

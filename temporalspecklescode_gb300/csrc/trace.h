@@ -36,6 +36,7 @@ struct TraceParams {
     unsigned long long* totals;  // [0] vertices, [1] dda steps, [2] misses, [3] paths
     int* err;
     uint32_t* work;       // [1] or null: path counter of the warp-per-path kernels (zeroed by their launchers)
+    int real_rows;        // illum_kernel / view_kernel: a_ms and s_ms hold real floats [paths][Nt][Nl or Nv]
 };
 
 size_t trace_smem_bytes(int Nt, int slots, int threads);

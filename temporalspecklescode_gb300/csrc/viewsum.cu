@@ -194,10 +194,13 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
     const bool geo = S.ticks_geometric != 0;
     const int tss = T.ss_all_ticks ? Nt : 1;
     float2* ams = T.a_ms + (size_t)q * Nt * Nl;
+    float* amr = reinterpret_cast<float*>(T.a_ms) + (size_t)q * Nt * Nl;   // real rows
+    const bool real = T.real_rows != 0;
+    auto put_ams = [&](size_t i, float a) { if (real) amr[i] = a; else ams[i] = make_float2(a, 0.f); };
     float2* ass = T.a_ss + (size_t)q * Nt * Nl;
     float2* bss = T.b_ss + (size_t)q * Nt * Nv;
     if (B == 0) {   // the walk hit a limit (error already flagged)
-        for (int i = lane; i < Nt * Nl; i += 32) { ams[i] = make_float2(0.f, 0.f); ass[i] = make_float2(0.f, 0.f); }
+        for (int i = lane; i < Nt * Nl; i += 32) { put_ams(i, 0.f); ass[i] = make_float2(0.f, 0.f); }
         for (int i = lane; i < Nt * Nv; i += 32) bss[i] = make_float2(0.f, 0.f);
         return;
     }
@@ -294,13 +297,13 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
             if (geo) {
                 const float es = __expf(-c1k * tau0);
                 float e = es;
-                for (int t = 0; t < Nt; ++t) { ams[(size_t)t * Nl + l] = make_float2(base * e, 0.f); e *= es; }
+                for (int t = 0; t < Nt; ++t) { put_ams((size_t)t * Nl + l, base * e); e *= es; }
             } else {
-                for (int t = 0; t < Nt; ++t) ams[(size_t)t * Nl + l] = make_float2(base * __expf(-c1k * S.abs_ticks[t]), 0.f);
+                for (int t = 0; t < Nt; ++t) put_ams((size_t)t * Nl + l, base * __expf(-c1k * S.abs_ticks[t]));
             }
         }
     } else {
-        for (int i = lane; i < Nt * Nl; i += 32) ams[i] = make_float2(0.f, 0.f);
+        for (int i = lane; i < Nt * Nl; i += 32) put_ams(i, 0.f);
     }
     const uint32_t ws = warp_sum_u32(steps);
     if (lane == 0) {
@@ -678,7 +681,9 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                     if (k < tn) {
                         const unsigned long long a2 = acc[j >> 1][k];
                         const float a = (j & 1) ? pk_hi(a2) : pk_lo(a2);
-                        T.s_ms[((size_t)q * Nt + t0 + k) * Nv + v] = make_float2(a, 0.0f);
+                        const size_t o = ((size_t)q * Nt + t0 + k) * Nv + v;
+                        if (T.real_rows) reinterpret_cast<float*>(T.s_ms)[o] = a;
+                        else T.s_ms[o] = make_float2(a, 0.0f);
                     }
             } else {
                 const float2 c = make_float2(pk_lo(acc[j][0]), pk_hi(acc[j][0]));
