@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
             }
             if (out != nullptr) out[k - o0] = pack_vertex(x, m, xi);
         }
-        if (MODE != kCount) h = hash_v(S, h, x, m);
+        if (MODE != kCount && W.hash) h = hash_v(S, h, x, m);   // the debug trace's vertex hash
     };
     if (!start(fetch())) return;
     for (;;) {

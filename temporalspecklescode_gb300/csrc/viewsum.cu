@@ -159,17 +159,6 @@ __device__ __forceinline__ float tau_d(const DevScene& S, const V3& x, const V3&
     }
 }
 
-// Next path of a warp: warps start at their own index and then draw from
-// T.work (one atomic per path), so a warp that drew short paths takes more
-// of them; without a counter, a fixed stride over the paths.
-__device__ __forceinline__ uint32_t next_path(const TraceParams& T, uint32_t q, uint32_t nw, int lane)
-{
-    if (T.work == nullptr) return q + nw;
-    uint32_t c = 0;
-    if (lane == 0) c = atomicAdd(T.work, 1u);
-    return nw + __shfl_sync(0xffffffffu, c, 0);
-}
-
 // Per-warp sums of the render statistics (lane 0 adds them to the global
 // counters once, when the warp has no paths left).
 struct WarpStats {
@@ -330,7 +319,8 @@ __global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevS
 #pragma unroll
     for (int k = 0; k < NLK; ++k) lsrc[k] = load3(S.src[0].p, min(lane + 32 * k, S.src[0].n - 1));
     WarpStats st;
-    for (uint32_t q = gw; q < T.paths; q = next_path(T, q, nw, lane))
+    // a fixed stride: every path costs about the same here (Nl + Nv rays)
+    for (uint32_t q = gw; q < T.paths; q += nw)
         illum_path<NLK, ILP, VWP, SINGLE>(S, T, q, lane, T.counts[q], T.verts + T.offsets[q], lsrc, st);
     if (lane == 0) st.flush(T);
 }
@@ -388,7 +378,12 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     unsigned long long warp_steps = 0;
-    for (uint32_t q = gw; q < T.paths; q = next_path(T, q, nw, lane)) {
+    // warps start at their own path and then draw from T.work (path cost grows
+    // with its vertex count); the draw for the next path is issued first so
+    // its latency hides behind this path's work
+    for (uint32_t q = gw; q < T.paths;) {
+        uint32_t drawn = 0;
+        if (T.work != nullptr && lane == 0) drawn = atomicAdd(T.work, 1u);
         const uint32_t B = T.counts[q];
         const float4* vq = T.verts + T.offsets[q];
         // correlation: ticks of a view pair packed (acc[P][t] = (view 2P, view 2P + 1));
@@ -695,6 +690,7 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
             if (T.dda) atomicAdd(T.dda + q, ws);
             warp_steps += ws;
         }
+        q = T.work != nullptr ? nw + __shfl_sync(0xffffffffu, drawn, 0) : q + nw;
     }
     if (lane == 0 && warp_steps) atomicAdd(T.totals + 1, warp_steps);
 }
@@ -768,7 +764,6 @@ int launch_illum(const DevScene& S, const TraceParams& T, int blocks, int thread
             f = ip ? (vp ? (Fn)illum_kernel<kMaxIllum, true, true, false> : (Fn)illum_kernel<kMaxIllum, true, false, false>)
                    : (vp ? (Fn)illum_kernel<kMaxIllum, false, true, false> : (Fn)illum_kernel<kMaxIllum, false, false, false>);
     }
-    if (T.work && cudaMemsetAsync(T.work, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     f<<<blocks, threads, 0, stream>>>(S, T);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
