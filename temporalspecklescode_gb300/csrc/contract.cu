@@ -264,7 +264,9 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
 // The tick chain runs on packed FP32 pairs (the thread's two views per FMA / MUL).
 constexpr int kFl = 32, kFv = 32, kFk = 16, kFt = 8;
 
-constexpr size_t kFastSmem = sizeof(float4) * (2 * kFk * kFl + kFk * kFv + kFk) + sizeof(float2) * 4 * kFt * 256;
+// staging tiles double-buffered (one barrier per chunk) + the compensated window sums
+constexpr size_t kFastStage = sizeof(float4) * (2 * kFk * kFl + kFk * kFv + kFk);
+constexpr size_t kFastSmem = 2 * kFastStage + sizeof(float2) * 4 * kFt * 256;
 
 // Rows here are tick-invariant (static scatterers, identical u1 / u2
 // sources), so only the first tick's rows are read; the tick dependence is
@@ -312,9 +314,14 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* accc = reinterpret_cast<float2*>(smem_raw);                       // [4*kFt][256] compensated (hi, lo) window sums
-    float4* sI = reinterpret_cast<float4*>(accc + 4 * kFt * 256);            // [kFk][kFl][2] (x x y y) (z z w w), w = row x pdf coefficient
-    float* sO = reinterpret_cast<float*>(sI + 2 * kFk * kFl);                 // [kFk][4][kFv] (x, y, z, row), views contiguous
-    float4* sM = reinterpret_cast<float4*>(sO + kFk * 4 * kFv);               // [kFk] (g, omg2, cn, 0), 2^(cn q^2) = decay of the first tick
+    unsigned char* stage0 = reinterpret_cast<unsigned char*>(accc + 4 * kFt * 256);
+    // staging buffer b of a chunk:
+    //   sI [kFk][kFl][2] (x x y y) (z z w w), w = row x pdf coefficient
+    //   sO [kFk][4][kFv] (x, y, z, row), views contiguous
+    //   sM [kFk] (g, omg2, cn, 0), 2^(cn q^2) = decay of the first tick
+    auto sI_of = [&](int b) { return reinterpret_cast<float4*>(stage0 + (size_t)b * kFastStage); };
+    auto sO_of = [&](int b) { return reinterpret_cast<float*>(sI_of(b) + 2 * kFk * kFl); };
+    auto sM_of = [&](int b) { return reinterpret_cast<float4*>(sO_of(b) + kFk * 4 * kFv); };
     // thread: view pair v0 + 2 tx + (0, 1), illumination elements l0 + ty + 16 i.
     // A warp reads two illumination records (broadcast) and 16 consecutive
     // view pairs (one 128-byte wavefront) from shared memory.
@@ -365,6 +372,11 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     prefetch(kb);
     int chunk = 0;
     for (int k = kb; k < ke; k += kFk, ++chunk) {
+        // double-buffered: this chunk's buffer was last read two chunks ago, before
+        // the previous chunk's barrier, so one barrier per chunk suffices
+        float4* sI = sI_of(chunk & 1);
+        float* sO = sO_of(chunk & 1);
+        float4* sM = sM_of(chunk & 1);
         if (threadIdx.x < kFk) {
             const int m = mm;
             const int ty_ = S.scat_type[m];
@@ -443,7 +455,6 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 }
             }
         }
-        __syncthreads();
         if ((chunk + 1) % 16 == 0) {
             // fold the 256-path window into the compensated (hi, lo) pairs
 #pragma unroll
@@ -498,11 +509,6 @@ int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         const int tchunks = (S.Nt + kFt - 1) / kFt;
         const int tiles = ((S.src[0].n + kFl - 1) / kFl) * ((S.src[1].n + kFv - 1) / kFv) * tchunks;
-        const int want = std::max(1, (2 * sms) / tiles);
-        SsParams P = G;
-        P.kchunk = ((G.K + want - 1) / want + kFk - 1) / kFk * kFk;
-        const int ksplit = (G.K + P.kchunk - 1) / P.kchunk;
-        dim3 grid((S.src[0].n + kFl - 1) / kFl, (S.src[1].n + kFv - 1) / kFv, tchunks * ksplit);
         using Fn = void (*)(DevScene, SsParams);
         const bool geo = S.ticks_geometric != 0, first = tchunks == 1;
         Fn f = S.dims == 3
@@ -510,6 +516,14 @@ int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
             : (geo ? (first ? (Fn)ss_fast_kernel<false, true, true> : (Fn)ss_fast_kernel<false, true, false>) : (Fn)ss_fast_kernel<false, false, false>);
         if (cudaFuncSetAttribute((const void*)f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFastSmem) != cudaSuccess)
             return SSTMC_CUBLAS_ERROR;
+        // resident blocks per SM (two, by registers and shared memory): split the paths so the grid fills them
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)f, 256, kFastSmem) != cudaSuccess || occ < 1) occ = 1;
+        const int want = std::max(1, (occ * sms) / tiles);
+        SsParams P = G;
+        P.kchunk = ((G.K + want - 1) / want + kFk - 1) / kFk * kFk;
+        const int ksplit = (G.K + P.kchunk - 1) / P.kchunk;
+        dim3 grid((S.src[0].n + kFl - 1) / kFl, (S.src[1].n + kFv - 1) / kFv, tchunks * ksplit);
         f<<<grid, 256, kFastSmem, stream>>>(S, P);
         return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
     }
