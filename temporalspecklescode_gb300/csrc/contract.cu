@@ -337,7 +337,6 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
     const DevSource& vw = S.src[1];
     const bool scalar_fs = S.iso_all && il.type == SSTMC_SOURCE_POINT && vw.type == SSTMC_SOURCE_POINT;
     const float tau0 = S.abs_ticks[0];
-    const unsigned long long neg1 = pk2(-1.0f, -1.0f);
     const float start_scale = (float)(t0 + 1);   // GEO: |t_t0| = (t0 + 1) |t_0|
     unsigned long long acc[2][kFt];
 #pragma unroll
@@ -427,11 +426,19 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             for (int i = 0; i < 2; ++i) {
                 const ulonglong2 ia = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i)];
                 const ulonglong2 ib = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i) + 1];
-                // both views of the pair at once: q^2 = |in - out|^2, pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
-                const unsigned long long dx = fma2(ox, neg1, ia.x);
-                const unsigned long long dy = fma2(oy, neg1, ia.y);
-                const unsigned long long dz = fma2(oz, neg1, ib.x);
-                const unsigned long long q2 = fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)));
+                // q^2 = |in - out|^2 per view in scalar FP32 (packed f32x2 math issues to one
+                // FMA pipe only; scalar FMAs can use the other), then both views packed:
+                // pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
+                const float ix = pk_lo(ia.x), iy = pk_lo(ia.y), iz = pk_lo(ib.x);
+                float q2s[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float dxh = ix - (h ? pk_hi(ox) : pk_lo(ox));
+                    const float dyh = iy - (h ? pk_hi(oy) : pk_lo(oy));
+                    const float dzh = iz - (h ? pk_hi(oz) : pk_lo(oz));
+                    q2s[h] = fmaf(dxh, dxh, fmaf(dyh, dyh, dzh * dzh));
+                }
+                const unsigned long long q2 = pk2(q2s[0], q2s[1]);
                 const unsigned long long dn = fma2(g2, q2, omg);
                 const unsigned long long r = pk2(rsqrt_fast(pk_lo(dn)), rsqrt_fast(pk_hi(dn)));
                 const unsigned long long rr = mul2(r, r);
