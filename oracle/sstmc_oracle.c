@@ -71,6 +71,7 @@ typedef struct {
     /* sources: 0 illumination, 1 view, 2 illumination2, 3 view2 */
     o_src src[4];
     int correlation;
+    int cbs;              /* field sampler with coherent backscattering (reversed paths) */
     int Nt;
     double* ticks;        /* correlation: raw ticks; */
     float* ticks_f;
@@ -188,7 +189,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     memset(S, 0, sizeof(*S));
     if (cfg->dims != 2 && cfg->dims != 3) return SSTMC_INVALID_CONFIG;
     int dims = S->dims = (int)cfg->dims;
-    if (cfg->is_cbs) return SSTMC_NOT_SUPPORTED;
     if (cfg->is_forced_inside_bin) return SSTMC_NOT_SUPPORTED;
     if (cfg->batch_size == 0 || cfg->full_iteration == 0) return SSTMC_INVALID_CONFIG;
     if (!(cfg->lambda > 0)) return SSTMC_INVALID_CONFIG;
@@ -290,6 +290,9 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     /* sampler */
     if (!cfg->t || cfg->t_num == 0) return SSTMC_INVALID_CONFIG;
     S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
+    /* CBS of the correlation sampler (the C2-C4 cross terms) is not built */
+    if (cfg->is_cbs && S->correlation) return SSTMC_NOT_SUPPORTED;
+    S->cbs = cfg->is_cbs ? 1 : 0;
     if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return SSTMC_INVALID_CONFIG;
     if (S->correlation) {
         if (S->src[2].type == SSTMC_SOURCE_NONE || S->src[3].type == SSTMC_SOURCE_NONE) return SSTMC_INVALID_CONFIG;
@@ -945,6 +948,7 @@ static inline void o_shift(const o_scene* S, const float x[3], int m, float tau,
 typedef struct {
     o_gmemo* memo[4];                 /* per source slot: last NEE vector of each element */
     oc *a_ms, *s_ms, *a_ss, *b_ss;   /* [Nt][Nl] / [Nt][Nv] */
+    oc *ar_ms, *sr_ms;                /* CBS reversed path: GlSum [Nt][Nl], Gv0 [Nt][Nv] */
     oc *gl1, *gl2;                    /* [Nt][Nl] illumination NEE vectors at x1 */
     double* P1; double* P2;           /* [Nl] */
 } o_work;
@@ -961,6 +965,7 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
     int m1 = V->m[0];
     double k2 = (2.0 * O_PI / S->lambda) * (2.0 * O_PI / S->lambda);
     memset(W->a_ms, 0, sizeof(oc) * Nt * Nl); memset(W->s_ms, 0, sizeof(oc) * Nt * Nv);
+    memset(W->ar_ms, 0, sizeof(oc) * Nt * Nl); memset(W->sr_ms, 0, sizeof(oc) * Nt * Nv);
 
     if (!S->correlation) {
         double p1 = 0;
@@ -1002,6 +1007,12 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
             const float* pb = S->temporal_amp ? V->xt + (size_t)Nt * 3 + 3 * t : x2;
             for (int l = 0; l < Nl; ++l)
                 W->a_ms[t * Nl + l] = oc_scale(W->gl1[t * Nl + l], o_f3(S, il, l, pa, pb, m1, 0) / sq2);
+            /* CBS: the reversed path starts at the view, v -> x1 -> x2 (Gv0,
+             * NextEventEstimation.cuh:1533-1537 and :995-1004): the view's NEE vector at
+             * x1 times its three-point amplitude with the view as the path's first end */
+            if (S->cbs)
+                for (int v = 0; v < Nv; ++v)
+                    W->sr_ms[t * Nv + v] = oc_scale(W->b_ss[t * Nv + v], o_f3(S, vw, v, pa, pb, m1, 1) / sq2);
         }
         for (int t = 0; t < Nt; ++t) {
             double L = 0;
@@ -1019,6 +1030,16 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                     oc c = oc_scale(oc_mul(g, ph), f);
                     W->s_ms[t * Nv + v].re += c.re; W->s_ms[t * Nv + v].im += c.im;
                 }
+                /* CBS: the reversed path ends at the illumination, x_{b-1} -> x_b -> l
+                 * (GlSum, NextEventEstimation.cuh:1573-1580, :1212-1235): the same path
+                 * phase, the illumination's NEE vector and amplitude at x_b */
+                if (S->cbs)
+                    for (int l = 0; l < Nl; ++l) {
+                        oc g = o_gm(S, W->memo[0], il, l, xb, 0, steps);
+                        double f = o_f3(S, il, l, pa, pb, V->m[b], 0);
+                        oc c = oc_scale(oc_mul(g, ph), f);
+                        W->ar_ms[t * Nl + l].re += c.re; W->ar_ms[t * Nl + l].im += c.im;
+                    }
             }
         }
     } else {
@@ -1129,13 +1150,19 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
         }
     }
     if (Vacc) {
+        /* CBS: (direct + reversed) / sqrt(2) (NextEventEstimation.cuh:1385-1391, :1448-1454) */
+        const double sc = S->cbs ? sqrt(0.5) : 1.0;
         for (int t = 0; t < Nt; ++t)
             for (int v = 0; v < Nv; ++v) {
-                oc s = W->s_ms[t * Nv + v];
+                oc s = W->s_ms[t * Nv + v], sr = W->sr_ms[t * Nv + v];
                 for (int l = 0; l < Nl; ++l) {
                     oc c = oc_mul(W->a_ms[t * Nl + l], s);
+                    if (S->cbs) {
+                        oc r = oc_mul(W->ar_ms[t * Nl + l], sr);
+                        c.re += r.re; c.im += r.im;
+                    }
                     oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
-                    dst->re += c.re; dst->im += c.im;
+                    dst->re += c.re * sc; dst->im += c.im * sc;
                 }
             }
     }
@@ -1146,6 +1173,8 @@ static int o_work_alloc(const o_scene* S, o_work* W)
     int Nl = S->src[0].n, Nv = S->src[1].n, Nt = S->Nt;
     W->a_ms = calloc((size_t)Nt * Nl, sizeof(oc)); W->a_ss = calloc((size_t)Nt * Nl, sizeof(oc));
     W->s_ms = calloc((size_t)Nt * Nv, sizeof(oc)); W->b_ss = calloc((size_t)Nt * Nv, sizeof(oc));
+    W->ar_ms = calloc((size_t)Nt * Nl, sizeof(oc)); W->sr_ms = calloc((size_t)Nt * Nv, sizeof(oc));
+    if (!W->ar_ms || !W->sr_ms) return SSTMC_ALLOCATION_ERROR;
     for (int i = 0; i < 4; ++i) W->memo[i] = calloc(S->src[i].n > 0 ? (size_t)S->src[i].n : 1, sizeof(o_gmemo));
     for (int i = 0; i < 4; ++i) if (!W->memo[i]) return SSTMC_ALLOCATION_ERROR;
     W->gl1 = calloc((size_t)Nt * Nl, sizeof(oc)); W->gl2 = calloc((size_t)Nt * Nl, sizeof(oc));
@@ -1157,6 +1186,7 @@ static void o_work_free(o_work* W)
 {
     for (int i = 0; i < 4; ++i) free(W->memo[i]);
     free(W->a_ms); free(W->a_ss); free(W->s_ms); free(W->b_ss); free(W->gl1); free(W->gl2); free(W->P1); free(W->P2);
+    free(W->ar_ms); free(W->sr_ms);
 }
 
 /* correlation u1/u2 split of a wave: TemporalSamplerCorrelation.cuh:369-372, 611-656 */

@@ -68,6 +68,7 @@ size_t Engine::bytes_per_path(const Scene& S)
 {
     const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
     return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16
+         + (S.cfg_copy.is_cbs ? 8 * Nt * (Nl + Nv) : 0)   // CBS: the reversed path's rows
          + walk_slot_bytes_per_path();
 }
 
@@ -100,7 +101,8 @@ int Engine::ensure(Scene& S, uint32_t paths)
         if (cudaMallocAsync(p, bytes ? bytes : 1, stream) != cudaSuccess) return false;
         return true;
     };
-    bool ok = alloc((void**)&a_ms, paths * Nt * Nl * sizeof(float2)) && alloc((void**)&s_ms, paths * Nt * Nv * sizeof(float2))
+    const size_t rows = S.cfg_copy.is_cbs ? 2 * (size_t)paths : paths;   // CBS: direct rows, then the reversed path's
+    bool ok = alloc((void**)&a_ms, rows * Nt * Nl * sizeof(float2)) && alloc((void**)&s_ms, rows * Nt * Nv * sizeof(float2))
            && alloc((void**)&a_ss, paths * Nt * Nl * sizeof(float2)) && alloc((void**)&b_ss, paths * Nt * Nv * sizeof(float2))
            && alloc((void**)&g2, S.correlation ? paths * Nt * Nl * sizeof(float2) : 8)
            && alloc((void**)&pl, paths * Nl * sizeof(float)) && alloc((void**)&x1, paths * 3 * sizeof(float))
@@ -182,23 +184,30 @@ int Engine::prepare_ss_tables(Scene& S)
     return SSTMC_NO_ERROR;
 }
 
-void Engine::plan(const Scene& S, TraceParams& T, std::vector<std::pair<int, int>>* vchunks, std::vector<std::pair<int, int>>* tchunks) const
+// Lane split and chunks of the summed per-vertex vectors over Nx elements
+// (views, or illuminations for the CBS reversed pass) and Nt ticks.
+static void plan_elems(int Nt, int Nx, TraceParams& T, std::vector<std::pair<int, int>>* xchunks,
+                       std::vector<std::pair<int, int>>* tchunks)
 {
-    const int Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
-    const int vw = std::min(32, pow2ceil(Nv));
+    const int vw = std::min(32, pow2ceil(Nx));
     const int tg = 32 / vw;
     int tpl = (Nt + tg - 1) / tg;
     if (tpl > kMaxSlots) tpl = kMaxSlots;
     const int tn = std::min(Nt, tpl * tg);
     const int vpl = std::max(1, kMaxSlots / tpl);
-    const int vn = std::min(Nv, vpl * vw);
+    const int vn = std::min(Nx, vpl * vw);
     T.vw = vw; T.tg = tg; T.tpl = tpl;
     T.slots = ((vn + vw - 1) / vw) * tpl;
-    T.lw = std::min(32, pow2ceil(Nl)); T.lg = 32 / T.lw;
-    T.vwa = vw; T.tga = tg;
-    vchunks->clear(); tchunks->clear();
-    for (int v = 0; v < Nv; v += vn) vchunks->push_back({ v, std::min(vn, Nv - v) });
+    xchunks->clear(); tchunks->clear();
+    for (int v = 0; v < Nx; v += vn) xchunks->push_back({ v, std::min(vn, Nx - v) });
     for (int t = 0; t < Nt; t += tn) tchunks->push_back({ t, std::min(tn, Nt - t) });
+}
+
+void Engine::plan(const Scene& S, TraceParams& T, std::vector<std::pair<int, int>>* vchunks, std::vector<std::pair<int, int>>* tchunks) const
+{
+    plan_elems(S.Nt, S.Nv, T, vchunks, tchunks);
+    T.lw = std::min(32, pow2ceil(S.Nl)); T.lg = 32 / T.lw;
+    T.vwa = T.vw; T.tga = T.tg;
 }
 
 int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, PathDebug* dbg)
@@ -268,7 +277,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     const int blocks = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_sm)));
     bool moving_any = false;
     for (int m : S.materials_present) moving_any = moving_any || S.dev.moving[m] != 0;
-    if (use_view_kernel() && view_kernel_covers(S.dev, &moving_any)) {
+    if (use_view_kernel() && !S.cfg_copy.is_cbs && view_kernel_covers(S.dev, &moving_any)) {
         // illumination side in the fused kernel (or illum_kernel), view side in viewsum.cu
         T.pass0 = 1; T.views = 0;
         T.v0 = 0; T.vn = S.Nv; T.t0 = 0; T.tn = S.Nt;
@@ -309,6 +318,30 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
             first_pass = false;
         }
     }
+    if (S.cfg_copy.is_cbs) {
+        // field CBS: the reversed path's rows (Gv0 of the views, GlSum of the
+        // illuminations) into the second half of the row buffers, rows n .. 2n - 1,
+        // so one contraction over 2n rows sums the direct and reversed products
+        TraceParams R = T;
+        R.cbs = 1; R.views = 1;
+        R.a_ms = a_ms + (size_t)n * S.Nt * S.Nl;
+        R.s_ms = s_ms + (size_t)n * S.Nt * S.Nv;
+        std::vector<std::pair<int, int>> lch, tch2;
+        plan_elems(S.Nt, S.Nl, R, &lch, &tch2);
+        const size_t smem_r = trace_smem_bytes(S.Nt, R.slots, threads);
+        const int per_r = occupancy_blocks(S.dev, threads, smem_r);
+        const int blocks_r = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_r)));
+        bool first_r = true;
+        for (auto& lc : lch)
+            for (auto& tc : tch2) {
+                R.pass0 = first_r ? 1 : 0;
+                R.v0 = lc.first; R.vn = lc.second; R.t0 = tc.first; R.tn = tc.second;
+                e = launch_trace(S.dev, R, blocks_r, threads, stream);
+                if (e) return e;
+                launches++;
+                first_r = false;
+            }
+    }
     return SSTMC_NO_ERROR;
 }
 
@@ -320,10 +353,13 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     const bool compensated = S.precision == SSTMC_PRECISION_SPLIT;
     GemmParams G;
     std::memset(&G, 0, sizeof(G));
-    G.Nt = S.Nt; G.Nl = S.Nl; G.Nv = S.Nv; G.V = V; G.K = (int)n; G.compensated = compensated ? 1 : 0;
+    // field CBS: 2n rows (direct, then reversed) and V += (direct + reversed) / sqrt(2)
+    const bool cbs = S.cfg_copy.is_cbs != 0;
+    G.Nt = S.Nt; G.Nl = S.Nl; G.Nv = S.Nv; G.V = V; G.K = (int)(cbs ? 2 * n : n); G.compensated = compensated ? 1 : 0;
+    G.scale = cbs ? std::sqrt(0.5) : 1.0;
     const int tiles = ((S.Nl + 31) / 32) * ((S.Nv + 31) / 32) * S.Nt;
     const int ksplit = std::max(1, (4 * sms + tiles - 1) / tiles);
-    int kchunk = (int)((n + ksplit - 1) / ksplit);
+    int kchunk = (int)((G.K + ksplit - 1) / ksplit);
     kchunk = ((kchunk + 255) / 256) * 256;
     G.kchunk = kchunk;
     G.A = a_ms; G.B = s_ms;
@@ -341,7 +377,7 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
         e = prepare_ss_tables(S);
         if (e) return e;
         const size_t per = (size_t)S.Nt * S.Nv * S.Nl;
-        G.A = a_ss; G.B = b_ss; G.mat = m1; G.real = 0;
+        G.A = a_ss; G.B = b_ss; G.mat = m1; G.real = 0; G.K = (int)n; G.scale = 1.0;
         for (int m : S.materials_present) {
             G.mat_sel = m;
             G.W = W + (size_t)m * per;

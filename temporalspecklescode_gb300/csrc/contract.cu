@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(256) gemm_kernel(const GemmParams G)
             double im = (double)hi_[i][j] + (double)li[i][j] + (double)acc[i][j].y;
             const size_t o = ((size_t)t * G.Nv + v) * G.Nl + l;
             if (G.W) { const double w = G.W[o]; re *= w; im *= w; }
+            if (G.scale != 0.0) { re *= G.scale; im *= G.scale; }
             atomicAdd(&G.V[o].x, re);
             atomicAdd(&G.V[o].y, im);
         }

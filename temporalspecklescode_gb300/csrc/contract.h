@@ -20,6 +20,7 @@ struct GemmParams {
     int compensated;
     int* err;             // tensor-core form: SSTMC_TIMEOUT if a bounded wait ran out
     int real;             // tensor-core form: A, B hold real floats [K][Nt][Nl] / [K][Nt][Nv] (V gets the real part)
+    double scale;         // V += scale * sum (field CBS: 1 / sqrt(2)); 0 reads as 1
 };
 
 // V[t][v][l] += sum_p a[p][t][l] * b[p][t][v] * W(l, v, t, p), W from the

@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
                     const int nt = gn / G.Nv, v = gn - nt * G.Nv;
                     if (nt == mt && mt < 2 && tick < G.Nt) {
                         const size_t o = ((size_t)tick * G.Nv + v) * G.Nl + l;
-                        const double wv = G.W ? (double)G.W[o] : 1.0;
+                        const double wv = (G.W ? (double)G.W[o] : 1.0) * (G.scale != 0.0 ? G.scale : 1.0);
                         atomicAdd(&G.V[o].x, ((double)hv[e] + (double)lv[e]) * wv);
                     }
                 }
@@ -502,7 +502,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
                     const int v = (n0 + 16 * c + 2 * j) >> 1;
                     if (l < G.Nl && v < G.Nv) {
                         const size_t o = ((size_t)t * G.Nv + v) * G.Nl + l;
-                        const double wv = G.W ? (double)G.W[o] : 1.0;
+                        const double wv = (G.W ? (double)G.W[o] : 1.0) * (G.scale != 0.0 ? G.scale : 1.0);
                         atomicAdd(odd ? &G.V[o].y : &G.V[o].x, val * wv);
                     }
                 }

@@ -129,7 +129,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     auto fail = [&](int code, const char* msg) { if (why) *why = msg; return code; };
     if (cfg->dims != 2 && cfg->dims != 3) return fail(SSTMC_INVALID_CONFIG, "dims must be 2 or 3");
     const int dims = S->dims = (int)cfg->dims;
-    if (cfg->is_cbs) return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS is not supported");
     if (cfg->is_forced_inside_bin) return fail(SSTMC_NOT_SUPPORTED, "sampler.isForcedInsideBin is not supported");
     if (cfg->batch_size == 0 || cfg->full_iteration == 0 || cfg->renderings_num == 0)
         return fail(SSTMC_INVALID_CONFIG, "batchSize, fullIteration and renderingsNum must be positive");
@@ -251,6 +250,10 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     if (!cfg->t || cfg->t_num == 0) return fail(SSTMC_INVALID_CONFIG, "sampler.t is required");
     S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
     if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return fail(SSTMC_INVALID_CONFIG, "unsupported sampler");
+    // coherent backscattering is built for the field sampler (reversed-path
+    // rows); the correlation sampler's C2-C4 cross terms are not
+    if (cfg->is_cbs && S->correlation)
+        return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS with the TemporalCorrelationSampler is not supported");
     D.correlation = S->correlation ? 1 : 0;
     if (S->correlation) {
         if (S->hsrc[2].type == SSTMC_SOURCE_NONE || S->hsrc[3].type == SSTMC_SOURCE_NONE)

@@ -112,8 +112,9 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.ticks = take(farfar ? Nt * sizeof(double) : 0);
     L.W = take(farfar ? (size_t)kMat * Nt * Nv * Nl * sizeof(float) : 0);
     L.fixed_end = o;
-    L.a_ms = take(n * Nt * Nl * sizeof(float2));
-    L.s_ms = take(n * Nt * Nv * sizeof(float2));
+    const size_t rows = S.cfg_copy.is_cbs ? 2 * (size_t)n : n;   // CBS: direct rows, then the reversed path's
+    L.a_ms = take(rows * Nt * Nl * sizeof(float2));
+    L.s_ms = take(rows * Nt * Nv * sizeof(float2));
     L.a_ss = take(n * Nt * Nl * sizeof(float2));
     L.b_ss = take(n * Nt * Nv * sizeof(float2));
     L.g2 = take(S.correlation ? n * Nt * Nl * sizeof(float2) : 0);

@@ -80,6 +80,13 @@ __device__ __forceinline__ V3 tick_pos(const float* buf, int t) { return V3{ buf
 __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, int lane)
 {
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    if (T.cbs) {   // reversed pass: Gv0 rows (first pass) and this pass's GlSum entries
+        if (T.pass0)
+            for (int i = lane; i < Nt * Nv; i += 32) T.s_ms[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
+        for (int t = T.t0; t < T.t0 + T.tn; ++t)
+            for (int l = T.v0 + lane; l < T.v0 + T.vn; l += 32) T.a_ms[((size_t)q * Nt + t) * Nl + l] = make_float2(0.f, 0.f);
+        return;
+    }
     if (T.pass0) {
         for (int i = lane; i < Nt * Nl; i += 32) {
             T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
@@ -181,6 +188,26 @@ __device__ __forceinline__ float fview(const DevScene& S, const DevSource& s, in
     return amp_fast(S, m, funit(sub3(pa, pb)), fsrc_out(s, v, pa));
 }
 
+// CBS reversed path: view element v as the path's first end, v -> pa -> pb
+// (threePointFunction with the view attached at pa, NextEventEstimation.cuh:1533-1537)
+template <bool PT>
+__device__ __forceinline__ float fview_entry(const DevScene& S, const DevSource& s, int v, const V3& pa, const V3& pb, int m)
+{
+    if (PT && S.iso_all) return S.iso_amp;
+    const V3 o = fsrc_out(s, v, pa);
+    return amp_fast(S, m, V3{ -o.x, -o.y, -o.z }, funit(sub3(pb, pa)));
+}
+
+// CBS reversed path: illumination element l as the path's last end, pb -> pa -> l
+// (NextEventEstimation.cuh:1573-1580)
+template <bool PT>
+__device__ __forceinline__ float fillum_exit(const DevScene& S, const DevSource& s, int l, const V3& pa, const V3& pb, int m)
+{
+    if (PT && S.iso_all) return S.iso_amp;
+    const V3 i = fsrc_in(s, l, pa);
+    return amp_fast(S, m, funit(sub3(pa, pb)), V3{ -i.x, -i.y, -i.z });
+}
+
 // f^2 for identical u1 / u2 sources: the pdf (|amplitude|^2 = pdf)
 template <bool PT>
 __device__ __forceinline__ float fillum2(const DevScene& S, const DevSource& s, int l, const V3& pa, const V3& pb, int m)
@@ -247,13 +274,13 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             for (int t = lane; t < Nt; t += 32) Ls[t] = 0.0;
             __syncwarp();
             mov1 = S.moving[m1] != 0;
-            if (T.pass0 && T.x1t)
+            if (T.pass0 && !T.cbs && T.x1t)
                 for (int i = lane; i < 3 * Nt; i += 32) T.x1t[(size_t)q * 3 * Nt + i] = xtc[i];
         }
         uint32_t steps = 0;
 
         // ---- illumination side at x1: P_l, Gl0, single-scattering rows ----
-        if (T.pass0) {
+        if (T.pass0 && !T.cbs) {
             float ps = 0.0f;
             for (int l = lane; l < Nl; l += 32) {
                 uint32_t st = 0;
@@ -411,6 +438,18 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                             else T.a_ms[o] = c_scale(c_mulc(T.a_ms[o], T.g2[o]), sc);
                         }
                     }
+                } else if (T.cbs) {
+                    // Gv0 = g_v(x1) f(v -> x1 -> x2) / sqrt(p2) from the single-scattering
+                    // view rows of the first pass (NextEventEstimation.cuh:995-1004)
+                    const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
+                    for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
+                        const float fs = stf ? fview_entry<VWP>(S, vw, v, x1, xn, m1) : 0.0f;
+                        for (int t = lane / T.vwa; t < Nt; t += T.tga) {
+                            const size_t o = ((size_t)q * Nt + t) * Nv + v;
+                            const float f = stf ? fs : fview_entry<VWP>(S, vw, v, tick_pos(xtc, t), tick_pos(xtn, t), m1);
+                            T.s_ms[o] = c_scale(T.b_ss[o], f * p2inv);
+                        }
+                    }
                 } else {
                     const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
                     for (int l = lane % T.lw; l < Nl; l += T.lw) {
@@ -478,18 +517,26 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             } else {
                 const bool stn = !S.moving[mn];
                 const bool stf = !S.temporal_amp || (stn && !S.moving[mcur]);
+                // the view's vector at x_b (GvSum), or for the CBS reversed pass the
+                // illumination's vector at x_b with the illumination as the path's last end (GlSum)
+                auto gx = [&](int e, const V3& p, uint32_t& st) {
+                    return T.cbs ? gcomplex<ILP>(S, il, e, p, kRoleIllum, st) : gcomplex<VWP>(S, vw, e, p, kRoleView, st);
+                };
+                auto fx = [&](int e, const V3& pa, const V3& pb, int m) {
+                    return T.cbs ? fillum_exit<ILP>(S, il, e, pa, pb, m) : fview<VWP>(S, vw, e, pa, pb, m);
+                };
                 int j = 0;
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                     uint32_t sts = 0;
                     float2 gs = make_float2(0.f, 0.f);
-                    if (stn) gs = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts);
-                    const float fs = stf ? fview<VWP>(S, vw, v, xn, cur, mn) : 0.0f;
+                    if (stn) gs = gx(v, xn, sts);
+                    const float fs = stf ? fx(v, xn, cur, mn) : 0.0f;
                     int k = 0;
                     for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
                         float2 g = gs;
                         if (stn) steps += sts;
-                        else g = gcomplex<VWP>(S, vw, v, tick_pos(xtn, t), kRoleView, steps);
-                        const float f = stf ? fs : fview<VWP>(S, vw, v, tick_pos(xtn, t), tick_pos(xtc, t), mn);
+                        else g = gx(v, tick_pos(xtn, t), steps);
+                        const float f = stf ? fs : fx(v, tick_pos(xtn, t), tick_pos(xtc, t), mn);
                         float fr;
                         if (split) fr = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
                         else { const float ph = (float)Ls[t] * S.inv_lambda_f + xin; fr = ph - rintf(ph); }
@@ -506,20 +553,23 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             float* tmp = xtc; xtc = xtn; xtn = tmp;
         }
         if (T.pass0 && B < 2) {
-            for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
+            if (T.cbs) for (int i = lane; i < Nt * Nv; i += 32) T.s_ms[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
+            else for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
         }
         // write the summed view vector of this chunk
         if (T.views) {
             int j = 0;
             for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                 int k = 0;
-                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k)
-                    T.s_ms[((size_t)q * Nt + t) * Nv + v] = accs[32 * (j * T.tpl + k)];
+                for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
+                    if (T.cbs) T.a_ms[((size_t)q * Nt + t) * Nl + v] = accs[32 * (j * T.tpl + k)];
+                    else T.s_ms[((size_t)q * Nt + t) * Nv + v] = accs[32 * (j * T.tpl + k)];
+                }
             }
         }
         const uint32_t wsteps = warp_sum_u32(steps);
         if (lane == 0) {
-            if (T.pass0) {
+            if (T.pass0 && !T.cbs) {
                 if (T.m1) T.m1[q] = (unsigned char)m1;
                 if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
                 acc_v += B;

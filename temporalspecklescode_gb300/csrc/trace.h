@@ -37,6 +37,8 @@ struct TraceParams {
     int* err;
     uint32_t* work;       // [1] or null: path counter of the warp-per-path kernels (zeroed by their launchers)
     int real_rows;        // illum_kernel / view_kernel: a_ms and s_ms hold real floats [paths][Nt][Nl or Nv]
+    int cbs;              // field CBS, reversed pass (trace_kernel): s_ms <- Gv0 [paths][Nt][Nv] (pass0),
+                          // a_ms <- GlSum [paths][Nt][Nl]; v0 / vn then index illumination elements
 };
 
 size_t trace_smem_bytes(int Nt, int slots, int threads);

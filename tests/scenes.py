@@ -113,6 +113,54 @@ def long_paths_3d(batch_size=64, full_iteration=2):
     return cfg, 3
 
 
+def with_cbs(scene):
+    """The same scene with coherent backscattering (tracer.isCBS)."""
+    cfg, dims = scene
+    cfg = dict(cfg)
+    cfg["tracer"] = {"type": "nee", "isCBS": True}
+    return cfg, dims
+
+
+def reciprocal_far_3d(cbs: bool = True, batch_size=64, full_iteration=2):
+    """Far-field field scene whose views are the illuminations reversed
+    (d_v = -d_l, same order), HG scattering in a two-material grid: with CBS
+    the rendered field is symmetric, u[l=k][v=j] == u[l=j][v=k]."""
+    d = {"x": [0.0, 0.25, -0.2, 0.1], "y": [0.0, 0.1, 0.15, -0.3], "z": [1.0, 0.96, 0.97, 0.95]}
+    n = np.sqrt(np.array(d["x"]) ** 2 + np.array(d["y"]) ** 2 + np.array(d["z"]) ** 2)
+    dl = {k: np.array(v) / n for k, v in d.items()}
+    dv = {k: -v for k, v in dl.items()}
+    grid = np.array([[[1, 2], [2, 1]], [[2, 2], [1, 1]]], dtype=np.uint32)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.8, "seed": 4},
+        "scattering": {"type": ["HG", "HG", "HG"], "amplitudeFunction": [0.0, 0.6, 0.3]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-4.0, 0.5, 4.0], "yAxis": [-4.0, -1.0, 4.0], "zAxis": [0.0, 1.5, 3.0],
+                   "materialGrid": grid, "sigs": [0.0, 1.2, 0.8], "siga": [0.0, 0.02, 0.05]},
+        "illumination": {"type": "FarField", "direction": dl}, "view": {"type": "FarField", "direction": dv},
+        "sampler": {"type": "TemporalSampler", "t": [0.0, 1.0], "D": [0.0, 0.0, 0.0],
+                    "U": {"x": [0.0, 0.0, 0.0], "y": [0.0, 0.0, 0.0], "z": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee", "isCBS": cbs},
+    }
+    return cfg, 3
+
+
+def reciprocal_point_2d(cbs: bool = True, batch_size=64, full_iteration=2):
+    """2D point sources with the views at the illumination positions, HG
+    scattering and moving scatterers (temporal amplitude): with CBS the field
+    is symmetric in (l, v)."""
+    pts = {"x": [-3.0, 0.5, 2.5], "y": [-6.5, -6.5, -6.0]}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.6, "seed": 8},
+        "scattering": {"type": ["HG", "HG"], "amplitudeFunction": [0.5, 0.5]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-5.0, 5.0], "yAxis": [-5.0, 5.0],
+                   "materialGrid": np.ones((1, 1), np.uint32), "sigs": [0.0, 0.9], "siga": [0.0, 0.03]},
+        "illumination": {"type": "PointSource", "location": pts}, "view": {"type": "PointSource", "location": pts},
+        "sampler": {"type": "TemporalSampler", "t": [0.0, 1.5, -1.0],
+                    "D": [0.0, 3e-3], "U": {"x": [0.0, 0.02], "y": [0.0, 0.0]}},
+        "tracer": {"type": "nee", "isCBS": cbs},
+    }
+    return cfg, 2
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -128,4 +176,9 @@ def small_scenes():
         "point_2d_iso_corr": point_2d_iso(True),
         "homogeneous_3d": homogeneous_3d(),
         "long_paths_3d": long_paths_3d(),
+        "field_point_3d_cbs": with_cbs(field_point_3d()),
+        "point_2d_iso_field_cbs": with_cbs(point_2d_iso(False)),
+        "speckle_2d_cbs": with_cbs(wl.speckle_2d(batch_size=48, full_iteration=2, n_dirs=6)),
+        "reciprocal_far_3d_cbs": reciprocal_far_3d(),
+        "reciprocal_point_2d_cbs": reciprocal_point_2d(),
     }

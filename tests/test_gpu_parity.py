@@ -155,3 +155,25 @@ def test_view_kernel_matches_fused_kernel(name, api, monkeypatch):
     for k in ("a_ms", "s_ms", "a_ss", "b_ss"):
         err = rel_fro(a[k], b[k])
         assert err <= 2e-6, (name, k, err)
+
+
+@pytest.mark.parametrize("name", ["reciprocal_far_3d_cbs", "reciprocal_point_2d_cbs"])
+def test_cbs_reciprocity(name, api):
+    """Field CBS on the GPU: with the views the reversed illuminations the field
+    is symmetric in (l, v) (the reversed-path rows are the direct rows with the
+    sources' roles exchanged); FP32 rows, so to 1e-5."""
+    from tests.test_oracle_pins import _sym_err
+    cfg, dims = SCENES[name]
+    with api.Scene(cfg, dims) as s:
+        u, _ = s.render(seed=21)
+    assert _sym_err(u[..., 0]) < 1e-5
+
+
+def test_cbs_correlation_refused(api):
+    """tracer.isCBS with the correlation sampler is refused with SSTMC_NOT_SUPPORTED."""
+    from tests.scenes import with_cbs
+    from temporalspecklescode_gb300 import workloads as wl
+    cfg, dims = with_cbs(wl.correlation_3d(batch_size=8, full_iteration=1, n_side=2, n_lags=1))
+    with pytest.raises(api.SstmcError) as ei:
+        api.Scene(cfg, dims)
+    assert ei.value.code == 5

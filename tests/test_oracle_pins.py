@@ -146,3 +146,38 @@ def test_oracle_reproduces_mcx_validation_curve(oracle):
     shape = (c / c[0]) / (mcx / mcx[0])
     assert np.max(np.abs(shape - 1)) < 0.03, shape
     assert abs(c[0] / mcx[0] - 1) < 0.12, c[0] / mcx[0]
+
+
+def _sym_err(u):
+    """Relative asymmetry of u[l][v] over the first min(Nl, Nv) elements (all ticks)."""
+    n = min(u.shape[0], u.shape[1])
+    a = u[:n, :n]
+    d = a - np.transpose(a, (1, 0, 2))
+    return np.linalg.norm(d) / np.linalg.norm(a)
+
+
+@pytest.mark.parametrize("make", ["reciprocal_far_3d", "reciprocal_point_2d"])
+def test_cbs_reciprocity(oracle, make):
+    """Field CBS (NextEventEstimation.cuh:1212-1235, :1385-1391): with the views
+    the reversed illuminations, each path's reversed-path product for (l=k, v=j)
+    is its direct product for (l=j, v=k), so the rendered field is symmetric in
+    (l, v); without CBS it is not."""
+    from tests import scenes
+    res = {}
+    for cbs in (False, True):
+        cfg, dims = getattr(scenes, make)(cbs=cbs)
+        pc = cf.prepare(cfg, dims)
+        u, it, st = oracle.render(pc, 21)
+        res[cbs] = u[..., 0] if u.ndim == 4 else u
+    assert _sym_err(res[True]) < 1e-12
+    assert _sym_err(res[False]) > 1e-3
+
+
+def test_cbs_correlation_not_supported(oracle):
+    """The correlation sampler's CBS cross terms are not built: both the oracle
+    and the library refuse the configuration."""
+    from tests.scenes import with_cbs
+    cfg, dims = with_cbs(wl.correlation_3d(batch_size=8, full_iteration=1, n_side=2, n_lags=1))
+    pc = cf.prepare(cfg, dims)
+    with pytest.raises(Exception):
+        oracle.render(pc, 1)
