@@ -203,10 +203,10 @@ def run_reference(args, dist, rank, ws):
 # every class streams per-path rows, so a launch's traffic scales with the
 # paths it processes.
 NCU_DRAM_BYTES_PER_PATH = {
-    "nee": (306547456 + 223163136) / 65536,    # illum_kernel + view_kernel
-    "walk": (60928 + 591872) / 65536,          # walk_kernel count + write
-    "gemm": 541137408 / 65536,                 # gemm_tc_kernel
-    "ss": 69278208 / 65536,                    # ss_fast_kernel
+    "nee": (8356096 + 157391360 + 14813440 + 72855296) / 65536,   # illum_kernel + view_kernel
+    "walk": (241664 + 178944 + 18748672 + 1536) / 65536,          # walk_kernel<slots> + compact_kernel
+    "gemm": (269216256 + 3438592) / 65536,                         # gemm_tc_kernel (real rows)
+    "ss": (68522752 + 984320) / 65536,                             # ss_fast_kernel
 }
 
 
@@ -234,16 +234,19 @@ def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
                         "traffic": traffic, "note": note}
 
     # NEE vectors (illum_kernel + view_kernel): rows written once (a_ms all ticks,
-    # tick-invariant single-scattering rows at tick 0, s_ms), P_l, the vertices read
-    nee_bytes = P * (8.0 * Nt * Nl + 8.0 * (Nl + Nv) + 8.0 * Nt * Nv + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
+    # tick-invariant single-scattering rows at tick 0, s_ms), P_l, the vertices read.
+    # The correlation sampler's rows are real here: 4 bytes per (tick, element).
+    rb = 4.0 if m["correlation"] else 8.0
+    nee_bytes = P * (rb * Nt * Nl + 8.0 * (Nl + Nv) + rb * Nt * Nv + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
     add("nee", "illum_kernel + view_kernel (NEE vectors)", mean["ms_nee"], "hbm", nee_bytes,
         "FP32-issue bound: DRAM traffic equals the row bytes")
     # random walk: one pass into per-path slots + compaction; vertices written once, counts / misses / offsets
     add("walk", "walk_kernel (single-pass random walk) + compaction", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P,
         "FP32-issue bound (IEEE-rounded decision path)")
-    # multiple-scattering contraction: 8 useful flops per complex multiply-add (3xTF32 issues 3 TF32 MMAs each)
-    add("gemm", "gemm_tc_kernel (multiple-scattering contraction, 3xTF32)", mean["ms_contract_ms"], "tensor",
-        8.0 * Nl * Nv * Nt * P, "reads 8 Nt (Nl + Nv) bytes per path: HBM-bound at this shape")
+    # multiple-scattering contraction: HBM-bound at this shape (M = N = 128 per tick
+    # pair, 2 Nl Nv Nt flops per path against rb Nt (Nl + Nv) bytes read)
+    add("gemm", "gemm_tc_kernel (multiple-scattering contraction, 3xTF32)", mean["ms_contract_ms"], "hbm",
+        rb * Nt * (Nl + Nv) * P, "reads the a_ms and s_ms rows once; tensor pipe 23 % active (ncu)")
     # single-scattering contraction: tick-0 rows read (tick-invariant form)
     add("ss", "ss_fast_kernel (single-scattering contraction)", mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv),
         "FP32/SFU-issue bound: one exp and one rsqrt per (path, l, v)")
