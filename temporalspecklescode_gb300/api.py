@@ -255,16 +255,41 @@ def _alloc_trace(paths: int, Nl: int, Nv: int, Nt: int):
     return out, tr
 
 
+def wavelengths(config: Dict[str, Any]) -> np.ndarray:
+    """config.simulation.lambda as a vector (default [1])."""
+    sim = config.get("simulation", {}) or {}
+    return np.atleast_1d(np.asarray(sim.get("lambda", 1.0), dtype=np.float64)).ravel()
+
+
 def _run(config: Dict[str, Any], dims: int, precision: int):
-    with Scene(config, dims, precision) as s:
-        return s.render()
+    lam = wavelengths(config)
+    if lam.size <= 1:
+        with Scene(config, dims, precision) as s:
+            return s.render()
+    # Several wavelengths (MatlabInterface.cu:1512-1545).  The reference traces
+    # the paths once for all wavelengths but returns an Nl x Nv x Nt x R array
+    # (MatlabInterface.cu:1731-1738) for device buffers of Nl x Nv x Nw x Nt, so
+    # Nw > 1 overruns its output.  Here every wavelength renders the same paths
+    # (they are keyed by seed and path id, not by the wavelength) and u has the
+    # device layout's wavelength axis: (Nl, Nv, Nw, Nt, R).
+    us, it = [], None
+    for w in lam:
+        c = dict(config)
+        c["simulation"] = dict(config.get("simulation", {}) or {})
+        c["simulation"]["lambda"] = float(w)
+        with Scene(c, dims, precision) as s:
+            u, it = s.render()
+        us.append(u)
+    return np.stack(us, axis=2), it
 
 
 def sstmc2D(config: Dict[str, Any], precision: int = cf.PRECISION_SPLIT):
-    """[u, iter] = sstmc2D(config)"""
+    """[u, iter] = sstmc2D(config); u is (Nl, Nv, Nt, R), or (Nl, Nv, Nw, Nt, R)
+    for a vector of wavelengths."""
     return _run(config, 2, precision)
 
 
 def sstmc3D(config: Dict[str, Any], precision: int = cf.PRECISION_SPLIT):
-    """[u, iter] = sstmc3D(config)"""
+    """[u, iter] = sstmc3D(config); u is (Nl, Nv, Nt, R), or (Nl, Nv, Nw, Nt, R)
+    for a vector of wavelengths."""
     return _run(config, 3, precision)

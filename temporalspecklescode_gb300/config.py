@@ -192,7 +192,7 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
         raise ConfigError("batchSize, fullIteration and renderingsNum must be positive")
     lam = _arr(sim.get("lambda", 1.0))
     if lam.size != 1:
-        raise ConfigError("this build supports a single wavelength (Nw = 1)")
+        raise ConfigError("a scene has one wavelength; sstmc2D / sstmc3D render a lambda vector one wavelength at a time")
     c.lam = float(lam[0])
     c.seed = int(abs(sim.get("seed", 0)))
     c.device_number = int(sim.get("deviceNumber", 0))
@@ -203,9 +203,9 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
     types = sc["type"]
     if isinstance(types, str):
         types = [types]
-    amps = sc.get("amplitudeFunction", [0.0] * len(types))
-    if not isinstance(amps, (list, tuple)):
-        amps = [amps]
+    else:   # a list, or a MATLAB cell array read from a .mat file (object array)
+        types = [str(t) for t in np.atleast_1d(np.asarray(types, dtype=object))]
+    amps = np.atleast_1d(np.asarray(sc.get("amplitudeFunction", [0.0] * len(types)), dtype=np.float64)).tolist()
     st = np.zeros(len(types), dtype=np.int32)
     sg = np.zeros(len(types), dtype=np.float64)
     for i, t in enumerate(types):

@@ -177,3 +177,22 @@ def test_cbs_correlation_refused(api):
     with pytest.raises(api.SstmcError) as ei:
         api.Scene(cfg, dims)
     assert ei.value.code == 5
+
+
+def test_wavelength_vector_renders_each_wavelength(api):
+    """sstmc2D with a lambda vector: u gains a wavelength axis (Nl, Nv, Nw, Nt, R)
+    and each wavelength's slice is the single-wavelength render of the same paths."""
+    from tests.scenes import point_2d_iso
+    cfg, dims = point_2d_iso(False)
+    lams = [0.5, 0.65]
+    multi = dict(cfg)
+    multi["simulation"] = dict(cfg["simulation"], **{"lambda": lams})
+    u, it = api.sstmc2D(multi)
+    assert u.shape[2] == 2
+    for w, lam in enumerate(lams):
+        one = dict(cfg)
+        one["simulation"] = dict(cfg["simulation"], **{"lambda": lam})
+        uw, itw = api.sstmc2D(one)
+        assert np.array_equal(it, itw)
+        assert rel_fro(u[:, :, w], uw) <= 1e-12
+    assert rel_fro(u[:, :, 0], u[:, :, 1]) > 1e-3   # the phases differ
