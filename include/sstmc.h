@@ -58,7 +58,7 @@ extern "C" {
 /* ScatteringNS::ScatteringType (Scattering.cuh:17-23) */
 #define SSTMC_SCATTERING_NOT_DEFINED      0
 #define SSTMC_SCATTERING_ISOTROPIC        1
-#define SSTMC_SCATTERING_TABULAR          2   /* not supported by this build */
+#define SSTMC_SCATTERING_TABULAR          2   /* table of the complex amplitude (tabular_n / tabular_f) */
 #define SSTMC_SCATTERING_HENYEY_GREENSTEIN 3
 #define SSTMC_SCATTERING_VMF_MIXTURE      4   /* not supported by this build */
 
@@ -142,6 +142,15 @@ typedef struct sstmc_config {
 
     /* build-specific */
     int32_t precision;             /* SSTMC_PRECISION_* */
+
+    /* Tabular scattering (Scattering.cuh:191-482, MatlabInterface.cu:762-790):
+     * the number of entries of each material's complex amplitude table (0 for
+     * the other types) and the tables as (re, im) pairs, concatenated in
+     * material order.  A table spans the scattering angle 0..pi (3D) or
+     * 0..2pi (2D) in equal steps; it is normalised by its cross section at
+     * scene creation. */
+    const uint32_t* tabular_n;     /* [scattering_num] or NULL */
+    const double* tabular_f;       /* [2 x sum(tabular_n)] or NULL */
 } sstmc_config;
 
 typedef struct sstmc_scene sstmc_scene;

@@ -59,6 +59,11 @@ typedef struct {
     int dims, M;
     int scat_type[OM];
     float g_f[OM];
+    /* tabular scattering: per material entries and offset into the tables */
+    int tab_n[OM], tab_off[OM];
+    double* tab_f;        /* normalised amplitude (re, im) */
+    double* tab_pdf;      /* evaluation pdf */
+    float* tab_cos;       /* cos(icdf) of the sampler */
     double gup[OM], gd1[OM], gd2[OM];
     int iso_all;
     /* medium */
@@ -96,6 +101,7 @@ static void o_free_scene(o_scene* S)
     }
     for (int a = 0; a < 3; ++a) { free(S->ax[a]); free(S->axd[a]); }
     free(S->grid); free(S->ticks); free(S->ticks_f); free(S->disp_scale); free(S->disp_u);
+    free(S->tab_f); free(S->tab_pdf); free(S->tab_cos);
 }
 
 /* Far-field tables: FarField.cuh:71-127 (fillBuffers) in double, stored as float. */
@@ -184,6 +190,45 @@ static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const do
 }
 
 /* Config normalisation and validation: MatlabInterface.cu:712-1372. */
+/* Tables of one tabular material, Scattering.cuh:272-384 (setTabularScattering),
+ * in FP64: sampling weights |f_i|^2 (x sin(theta_i) in 3D, theta_i = i pi / (N-1)),
+ * their sum S, the cross section (S / N) 2 pi (x pi in 3D), the amplitude
+ * scaled by sqrt(1 / cross section), the inverse cdf as the lower bound of
+ * j / (N - 1) in the running sum of the normalised weights (angle = index x
+ * pi / (N - 1), 2 pi / (N - 1) in 2D), the evaluation pdf |f_n|^2 (x sin(theta_i)
+ * in 3D).  The sampler keeps cos(angle) in FP32. */
+static int o_tabular(const double* f, uint32_t N, int dims, double* fn, double* pdf, float* cosv)
+{
+    double* raw = malloc(sizeof(double) * N);
+    double* cdf = malloc(sizeof(double) * N);
+    if (!raw || !cdf) { free(raw); free(cdf); return SSTMC_ALLOCATION_ERROR; }
+    double sum = 0.0;
+    for (uint32_t i = 0; i < N; ++i) {
+        double a2 = f[2 * i] * f[2 * i] + f[2 * i + 1] * f[2 * i + 1];
+        raw[i] = dims == 2 ? a2 : a2 * sin(((double)i / (double)(N - 1)) * O_PI);
+        sum += raw[i];
+    }
+    double inv = 1.0 / sum, run = 0.0;
+    for (uint32_t i = 0; i < N; ++i) { run += raw[i] * inv; cdf[i] = run; }
+    double cross = (sum / (double)N) * 2.0 * O_PI * (dims == 3 ? O_PI : 1.0);
+    double sc = sqrt(1.0 / cross);
+    for (uint32_t i = 0; i < N; ++i) {
+        fn[2 * i] = f[2 * i] * sc;
+        fn[2 * i + 1] = f[2 * i + 1] * sc;
+        double a2 = fn[2 * i] * fn[2 * i] + fn[2 * i + 1] * fn[2 * i + 1];
+        pdf[i] = dims == 2 ? a2 : a2 * sin(((double)i / (double)(N - 1)) * O_PI);
+    }
+    double step = (dims == 2 ? 2.0 * O_PI : O_PI) / (double)(N - 1);
+    for (uint32_t j = 0; j < N; ++j) {
+        double th = (double)j / (double)(N - 1);
+        uint32_t lo = 0, hi = N;   /* first index with cdf >= th */
+        while (lo < hi) { uint32_t mid = lo + (hi - lo) / 2; if (cdf[mid] < th) lo = mid + 1; else hi = mid; }
+        cosv[j] = (float)cos((double)lo * step);
+    }
+    free(raw); free(cdf);
+    return 0;
+}
+
 static int o_build_scene(const sstmc_config* cfg, o_scene* S)
 {
     memset(S, 0, sizeof(*S));
@@ -198,15 +243,38 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     if (cfg->scattering_num == 0 || cfg->scattering_num > OM || !cfg->scattering_type) return SSTMC_INVALID_CONFIG;
     int M = (int)cfg->scattering_num;
     for (int m = 0; m < OM; ++m) S->scat_type[m] = SSTMC_SCATTERING_NOT_DEFINED;
+    size_t tab_total = 0, tab_pos = 0;
+    for (int m = 0; m < M; ++m)
+        if (cfg->scattering_type[m] == SSTMC_SCATTERING_TABULAR) {
+            if (!cfg->tabular_n || !cfg->tabular_f || cfg->tabular_n[m] < 2) return SSTMC_INVALID_CONFIG;
+            tab_total += cfg->tabular_n[m];
+        }
+    if (tab_total) {
+        S->tab_f = malloc(sizeof(double) * 2 * tab_total);
+        S->tab_pdf = malloc(sizeof(double) * tab_total);
+        S->tab_cos = malloc(sizeof(float) * tab_total);
+        if (!S->tab_f || !S->tab_pdf || !S->tab_cos) return SSTMC_ALLOCATION_ERROR;
+    }
     for (int m = 0; m < M; ++m) {
         int ty = cfg->scattering_type[m];
         double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
-        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return SSTMC_NOT_SUPPORTED;
+        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR)
+            return SSTMC_NOT_SUPPORTED;
         if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(fabs(g) < 1.0)) return SSTMC_INVALID_CONFIG;
+        int toff = 0, tn = 0;
+        if (ty == SSTMC_SCATTERING_TABULAR) {
+            tn = (int)cfg->tabular_n[m];
+            toff = (int)tab_pos;
+            int e = o_tabular(cfg->tabular_f + 2 * tab_pos, (uint32_t)tn, dims, S->tab_f + 2 * tab_pos, S->tab_pdf + tab_pos, S->tab_cos + tab_pos);
+            if (e) return e;
+            tab_pos += (size_t)tn;
+        }
         int targets[2] = { m, 1 };
         int nt = (M == 1) ? 2 : 1;
         for (int q = 0; q < nt; ++q) {
             int mm = targets[q];
+            S->tab_n[mm] = tn;
+            S->tab_off[mm] = toff;
             S->scat_type[mm] = ty;
             S->g_f[mm] = (float)g;
             S->gup[mm] = dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * O_PI)) : (1.0 - g * g) / (4.0 * O_PI);
@@ -219,6 +287,7 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     S->iso_all = 1;
     for (int m = 0; m < OM; ++m) {
         if (S->scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(fabs(S->g_f[m]) < 0.0001f)) S->iso_all = 0;
+        if (S->scat_type[m] == SSTMC_SCATTERING_TABULAR) S->iso_all = 0;
     }
 
     /* medium */
@@ -453,10 +522,16 @@ static inline void o_random_direction(int dims, o_stream* rs, float out[3])
 static void o_sample_direction(const o_scene* S, int m, const float din[3], o_stream* rs, float out[3])
 {
     int ty = S->scat_type[m];
-    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN) { o_random_direction(S->dims, rs, out); return; }
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR) { o_random_direction(S->dims, rs, out); return; }
     float g = S->g_f[m];
     float c;
-    if (fabsf(g) < 0.001f) {
+    if (ty == SSTMC_SCATTERING_TABULAR) {
+        /* Scattering.cuh:1030-1037: icdf entry round_num(xi N, N) (Simulation.cuh:287-298) */
+        int N = S->tab_n[m];
+        int k = (int)rintf(o_uniform(rs) * (float)N);
+        k = k < 0 ? 0 : (k >= N ? N - 1 : k);
+        c = S->tab_cos[S->tab_off[m] + k];
+    } else if (fabsf(g) < 0.001f) {
         c = o_uniform(rs) * 2.0f - 1.0f;
     } else {
         float xi = o_uniform(rs);
@@ -638,7 +713,20 @@ static double o_tau64(const o_scene* S, const double o[3], const double d[3])
     return acc;
 }
 
-/* Scattering::amplitude / pdf device implementations, Scattering.cuh:895-1023 (FP64). */
+/* Tabular entry of a scattering cosine: round_num(safeAcos(c) (N - 1) / pi, N),
+ * 2 pi in 2D (Scattering.cuh:907-917, Simulation.cuh:274-298; round half to even,
+ * clamped to the table). */
+static inline int o_tab_index(const o_scene* S, int m, double c)
+{
+    double th = c < -1.0 + 1e-12 ? O_PI : (c > 1.0 - 1e-12 ? 0.0 : acos(c));
+    int N = S->tab_n[m];
+    double x = th * (double)(N - 1) / (S->dims == 2 ? 2.0 * O_PI : O_PI);
+    int n = (int)nearbyint(x);
+    return n < 0 ? 0 : (n >= N ? N - 1 : n);
+}
+
+/* Scattering::amplitude / pdf device implementations, Scattering.cuh:895-1023 (FP64).
+ * o_amp: the real amplitudes (Isotropic, HG); o_ampc below adds the tabular one. */
 static inline double o_amp(const o_scene* S, int m, double c)
 {
     int ty = S->scat_type[m];
@@ -654,6 +742,7 @@ static inline double o_pdf(const o_scene* S, int m, double c)
 {
     int ty = S->scat_type[m];
     if (ty == SSTMC_SCATTERING_ISOTROPIC) return S->dims == 2 ? O_ISO_PDF2 : O_ISO_PDF3;
+    if (ty == SSTMC_SCATTERING_TABULAR) return S->tab_pdf[S->tab_off[m] + o_tab_index(S, m, c)];
     if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
         double dn = fma(S->gd2[m], c, S->gd1[m]);
         return S->dims == 2 ? S->gup[m] / dn : S->gup[m] / (dn * sqrt(dn));
@@ -690,6 +779,18 @@ typedef struct { double re, im; } oc;
 static inline oc oc_mul(oc a, oc b) { oc r = { a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re }; return r; }
 static inline oc oc_conj(oc a) { oc r = { a.re, -a.im }; return r; }
 static inline oc oc_scale(oc a, double s) { oc r = { a.re * s, a.im * s }; return r; }
+
+/* complex amplitude: the tabular table entry, else the real amplitude */
+static inline oc o_ampc(const o_scene* S, int m, double c)
+{
+    if (S->scat_type[m] == SSTMC_SCATTERING_TABULAR) {
+        int i = S->tab_off[m] + o_tab_index(S, m, c);
+        oc r = { S->tab_f[2 * i], S->tab_f[2 * i + 1] };
+        return r;
+    }
+    oc r = { o_amp(S, m, c), 0.0 };
+    return r;
+}
 
 typedef struct { float x[3]; int valid; oc g; uint64_t steps; } o_gmemo;
 
@@ -784,30 +885,30 @@ static void o_src_dir(const o_src* s, int k, const float x[3], int toward_source
 
 /* Source -> scatterer a -> point b amplitude (threePointFunction):
  * FarField.cuh:546-554, PointSource.cuh:317-345.  role 0 illumination, 1 view. */
-static double o_f3(const o_scene* S, const o_src* s, int k, const float a[3], const float b[3], int m, int role)
+static oc o_f3(const o_scene* S, const o_src* s, int k, const float a[3], const float b[3], int m, int role)
 {
     double ab[3]; o_dir64(a, b, ab);
     if (s->type == SSTMC_SOURCE_FARFIELD) {
         double d[3] = { s->p[3 * k], s->p[3 * k + 1], s->p[3 * k + 2] };
         double c = o_dot(d, ab);
-        return o_amp(S, m, role == 0 ? c : -c);
+        return o_ampc(S, m, role == 0 ? c : -c);
     }
-    if (S->iso_all) return S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3;
+    if (S->iso_all) { oc r = { S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3, 0.0 }; return r; }
     double in[3]; o_dir64(s->p + 3 * k, a, in);
-    return o_amp(S, m, o_dot(in, ab));
+    return o_ampc(S, m, o_dot(in, ab));
 }
 
 /* Single-scattering amplitude illumination l -> x -> view v (threePointFunctionSingle):
  * FarField.cuh:556-599, PointSource.cuh:347-405. */
-static double o_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v, const float x[3], int m)
+static oc o_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v, const float x[3], int m)
 {
-    if (il->type == SSTMC_SOURCE_POINT && S->iso_all) return S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3;
+    if (il->type == SSTMC_SOURCE_POINT && S->iso_all) { oc r = { S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3, 0.0 }; return r; }
     double in[3], out[3];
     if (il->type == SSTMC_SOURCE_FARFIELD) { in[0] = il->p[3 * l]; in[1] = il->p[3 * l + 1]; in[2] = il->p[3 * l + 2]; }
     else o_dir64(il->p + 3 * l, x, in);
     if (vw->type == SSTMC_SOURCE_FARFIELD) { out[0] = vw->p[3 * v]; out[1] = vw->p[3 * v + 1]; out[2] = vw->p[3 * v + 2]; }
     else o_dir64(x, vw->p + 3 * v, out);
-    return o_amp(S, m, o_dot(in, out));
+    return o_ampc(S, m, o_dot(in, out));
 }
 
 /* ------------------------------------------------------------------ */
@@ -985,8 +1086,8 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
             for (int t = 0; t < Nt; ++t) {
                 const float* pos = S->temporal_amp ? V->xt + 3 * t : x1;
                 for (int v = 0; v < Nv; ++v) for (int l = 0; l < Nl; ++l) {
-                    double w = o_fs(S, il, l, vw, v, pos, m1);
-                    oc c = oc_scale(oc_mul(W->a_ss[t * Nl + l], W->b_ss[t * Nv + v]), w);
+                    oc w = o_fs(S, il, l, vw, v, pos, m1);
+                    oc c = oc_mul(oc_mul(W->a_ss[t * Nl + l], W->b_ss[t * Nv + v]), w);
                     oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
                     dst->re += c.re; dst->im += c.im;
                 }
@@ -1006,13 +1107,13 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
             const float* pa = S->temporal_amp ? V->xt + 3 * t : x1;
             const float* pb = S->temporal_amp ? V->xt + (size_t)Nt * 3 + 3 * t : x2;
             for (int l = 0; l < Nl; ++l)
-                W->a_ms[t * Nl + l] = oc_scale(W->gl1[t * Nl + l], o_f3(S, il, l, pa, pb, m1, 0) / sq2);
+                W->a_ms[t * Nl + l] = oc_scale(oc_mul(W->gl1[t * Nl + l], o_f3(S, il, l, pa, pb, m1, 0)), 1.0 / sq2);
             /* CBS: the reversed path starts at the view, v -> x1 -> x2 (Gv0,
              * NextEventEstimation.cuh:1533-1537 and :995-1004): the view's NEE vector at
              * x1 times its three-point amplitude with the view as the path's first end */
             if (S->cbs)
                 for (int v = 0; v < Nv; ++v)
-                    W->sr_ms[t * Nv + v] = oc_scale(W->b_ss[t * Nv + v], o_f3(S, vw, v, pa, pb, m1, 1) / sq2);
+                    W->sr_ms[t * Nv + v] = oc_scale(oc_mul(W->b_ss[t * Nv + v], o_f3(S, vw, v, pa, pb, m1, 1)), 1.0 / sq2);
         }
         for (int t = 0; t < Nt; ++t) {
             double L = 0;
@@ -1026,8 +1127,8 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                 oc ph; o_cexp2pi(L / S->lambda + (double)V->xi[b], &ph.re, &ph.im);
                 for (int v = 0; v < Nv; ++v) {
                     oc g = o_gm(S, W->memo[1], vw, v, xb, 1, steps);
-                    double f = o_f3(S, vw, v, pa, pb, V->m[b], 1);
-                    oc c = oc_scale(oc_mul(g, ph), f);
+                    oc f = o_f3(S, vw, v, pa, pb, V->m[b], 1);
+                    oc c = oc_mul(oc_mul(g, ph), f);
                     W->s_ms[t * Nv + v].re += c.re; W->s_ms[t * Nv + v].im += c.im;
                 }
                 /* CBS: the reversed path ends at the illumination, x_{b-1} -> x_b -> l
@@ -1036,8 +1137,8 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                 if (S->cbs)
                     for (int l = 0; l < Nl; ++l) {
                         oc g = o_gm(S, W->memo[0], il, l, xb, 0, steps);
-                        double f = o_f3(S, il, l, pa, pb, V->m[b], 0);
-                        oc c = oc_scale(oc_mul(g, ph), f);
+                        oc f = o_f3(S, il, l, pa, pb, V->m[b], 0);
+                        oc c = oc_mul(oc_mul(g, ph), f);
                         W->ar_ms[t * Nl + l].re += c.re; W->ar_ms[t * Nl + l].im += c.im;
                     }
             }
@@ -1073,17 +1174,19 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                     double o1[3], o2[3];
                     o_src_dir(vw, v, x1, 1, o1); o_src_dir(vw2, v, x1, 1, o2);
                     for (int l = 0; l < Nl; ++l) {
-                        double w;
+                        oc w = { 0.0, 0.0 };
                         if (scalarFs) {
-                            w = (D == 2 ? O_ISO_AMP2 : O_ISO_AMP3) * (D == 2 ? O_ISO_AMP2 : O_ISO_AMP3);
+                            w.re = (D == 2 ? O_ISO_AMP2 : O_ISO_AMP3) * (D == 2 ? O_ISO_AMP2 : O_ISO_AMP3);
                         } else {
                             double in1[3], in2[3];
                             o_src_dir(il, l, x1, 0, in1); o_src_dir(il2, l, x1, 0, in2);
                             double q[3];
                             for (int i = 0; i < 3; ++i) q[i] = 0.5 * (in1[i] + in2[i] - o1[i] - o2[i]);
-                            w = o_fs(S, il, l, vw, v, xm, m1) * o_fs(S, il2, l, vw2, v, xm, m1) * exp(-dtD * o_dot(q, q));
+                            /* u1 amplitude x conj(u2 amplitude) (real unless tabular) */
+                            w = oc_scale(oc_mul(o_fs(S, il, l, vw, v, xm, m1), oc_conj(o_fs(S, il2, l, vw2, v, xm, m1))),
+                                         exp(-dtD * o_dot(q, q)));
                         }
-                        oc c = oc_scale(oc_mul(W->a_ss[t * Nl + l], W->b_ss[t * Nv + v]), w);
+                        oc c = oc_mul(oc_mul(W->a_ss[t * Nl + l], W->b_ss[t * Nv + v]), w);
                         oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
                         dst->re += c.re; dst->im += c.im;
                     }
@@ -1107,12 +1210,12 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
             double dtD = k2 * fabs(S->D[m1] * S->ticks[t]);
             for (int l = 0; l < Nl; ++l) {
                 oc g1 = W->gl1[t * Nl + l], g2 = W->gl2[t * Nl + l];
-                double f1 = o_f3(S, il, l, pa, pb, m1, 0), f2 = o_f3(S, il2, l, pa, pb, m1, 0);
+                oc f1 = o_f3(S, il, l, pa, pb, m1, 0), f2 = o_f3(S, il2, l, pa, pb, m1, 0);
                 double in1[3], in2[3], q[3];
                 o_src_dir(il, l, x1, 0, in1); o_src_dir(il2, l, x1, 0, in2);
                 for (int i = 0; i < 3; ++i) q[i] = 0.5 * (in1[i] + in2[i]) - x12[i];
                 double c1 = exp(-dtD * o_dot(q, q));
-                oc a = oc_mul(oc_scale(g1, f1 / p2), oc_conj(oc_scale(g2, f2)));
+                oc a = oc_mul(oc_scale(oc_mul(g1, f1), 1.0 / p2), oc_conj(oc_mul(g2, f2)));
                 W->a_ms[t * Nl + l] = oc_scale(a, c1);
             }
         }
@@ -1137,12 +1240,12 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                 double dtD = k2 * fabs(S->D[mb] * S->ticks[t]);
                 for (int v = 0; v < Nv; ++v) {
                     oc g1 = o_gm(S, W->memo[1], vw, v, xm, 1, steps), g2 = o_gm(S, W->memo[3], vw2, v, xp, 1, steps);
-                    double f1 = o_f3(S, vw, v, pa, pb, mb, 1), f2 = o_f3(S, vw2, v, pa, pb, mb, 1);
+                    oc f1 = o_f3(S, vw, v, pa, pb, mb, 1), f2 = o_f3(S, vw2, v, pa, pb, mb, 1);
                     double o1[3], o2[3], q[3];
                     o_src_dir(vw, v, xb, 1, o1); o_src_dir(vw2, v, xb, 1, o2);
                     for (int i = 0; i < 3; ++i) q[i] = 0.5 * (-o1[i] - o2[i]) - back[i];
                     double c1 = exp(-dtD * o_dot(q, q));
-                    oc c = oc_mul(oc_scale(g1, f1 * pt), oc_conj(oc_scale(g2, f2)));
+                    oc c = oc_mul(oc_scale(oc_mul(g1, f1), pt), oc_conj(oc_mul(g2, f2)));
                     c = oc_scale(c, c1);
                     W->s_ms[t * Nv + v].re += c.re; W->s_ms[t * Nv + v].im += c.im;
                 }
@@ -1341,8 +1444,21 @@ int32_t oracle_phase(const sstmc_config* cfg, int32_t m, double c, double* amp, 
     o_scene S;
     int err = o_build_scene(cfg, &S);
     if (!err) {
-        if (amp) *amp = o_amp(&S, m, c);
+        if (amp) *amp = o_ampc(&S, m, c).re;
         if (pdf) *pdf = o_pdf(&S, m, c);
+    }
+    o_free_scene(&S);
+    return err;
+}
+
+int32_t oracle_amplitude(const sstmc_config* cfg, int32_t m, double c, double* re, double* im)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (!err) {
+        oc a = o_ampc(&S, m, c);
+        if (re) *re = a.re;
+        if (im) *im = a.im;
     }
     o_free_scene(&S);
     return err;

@@ -45,6 +45,8 @@ int32_t oracle_trace_paths(const sstmc_config* cfg, uint64_t seed, uint32_t firs
 int32_t oracle_dda(const sstmc_config* cfg, const float* o, const float* d, double* tau32, double* tau64);
 /* Scattering amplitude and pdf of material m at cosine c (FP64). */
 int32_t oracle_phase(const sstmc_config* cfg, int32_t m, double c, double* amp, double* pdf);
+/* complex scattering amplitude of material m at cosine c (tabular: the table entry) */
+int32_t oracle_amplitude(const sstmc_config* cfg, int32_t m, double c, double* re, double* im);
 /* Sample `n` scattering cosines of material m (FP32 walk arithmetic). */
 int32_t oracle_sample_cos(const sstmc_config* cfg, int32_t m, uint64_t seed, uint32_t n, float* out);
 /* Portable FP32 math of the decision path, for bit-level tests. */

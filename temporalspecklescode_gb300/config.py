@@ -5,7 +5,8 @@ The dict mirrors the struct that the reference's MEX functions take,
 MatlabInterface.cu:712-1672):
 
     config['simulation']   batchSize, fullIteration, renderingsNum, lambda, seed, deviceNumber
-    config['scattering']   type (list of 'Isotropic' / 'HG' / 'HenyeyGreenstein'), amplitudeFunction (list of g)
+    config['scattering']   type (list of 'Isotropic' / 'HG' / 'HenyeyGreenstein' / 'Tabular'),
+                           amplitudeFunction (list: g for HG, a complex vector for Tabular)
     config['medium']       type 'Heterogeneous' (xAxis, yAxis, zAxis, materialGrid, sigs, siga)
                            or 'Homogeneous' (boxMin, boxMax, sigs)
     config['illumination'] / ['view'] / ['illumination2'] / ['view2']
@@ -99,6 +100,8 @@ class SstmcConfig(C.Structure):
         ("is_forced_inside_bin", C.c_int32),
         ("is_cbs", C.c_int32),
         ("precision", C.c_int32),
+        ("tabular_n", C.POINTER(C.c_uint32)),
+        ("tabular_f", C.POINTER(C.c_double)),
     ]
 
 
@@ -177,6 +180,24 @@ def _source(cfg: Dict[str, Any], name: str, dims: int, keep: list, required: boo
     return s
 
 
+def _amplitude_cells(raw: Any, types: list) -> list:
+    """scattering.amplitudeFunction as one entry per material: a scalar g (HG),
+    a vector of complex values (Tabular) or anything (Isotropic).  MATLAB passes
+    a cell array; a .mat reader gives a list, and a one-material cell may arrive
+    as the bare value."""
+    if isinstance(raw, (list, tuple)):
+        cells = list(raw)
+    elif isinstance(raw, np.ndarray) and raw.dtype == object:
+        cells = list(raw.ravel())
+    elif len(types) == 1:
+        cells = [raw]
+    else:
+        cells = list(np.atleast_1d(np.asarray(raw)).ravel())
+    if len(cells) < len(types):
+        cells += [0.0] * (len(types) - len(cells))
+    return cells
+
+
 def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT) -> PreparedConfig:
     """Convert a MATLAB-style config dict into the C-ABI struct."""
     if dims not in (2, 3):
@@ -205,9 +226,11 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
         types = [types]
     else:   # a list, or a MATLAB cell array read from a .mat file (object array)
         types = [str(t) for t in np.atleast_1d(np.asarray(types, dtype=object))]
-    amps = np.atleast_1d(np.asarray(sc.get("amplitudeFunction", [0.0] * len(types)), dtype=np.float64)).tolist()
+    amps = _amplitude_cells(sc.get("amplitudeFunction", [0.0] * len(types)), types)
     st = np.zeros(len(types), dtype=np.int32)
     sg = np.zeros(len(types), dtype=np.float64)
+    tn = np.zeros(len(types), dtype=np.uint32)
+    tabs = []
     for i, t in enumerate(types):
         if t == "Isotropic":
             st[i] = SCATTERING_ISOTROPIC
@@ -216,11 +239,21 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
             sg[i] = float(np.asarray(amps[i]).ravel()[0])
         elif t == "Tabular":
             st[i] = SCATTERING_TABULAR
+            f = np.asarray(amps[i], dtype=np.complex128).ravel()
+            if f.size < 2 or not np.all(np.isfinite(f)):
+                raise ConfigError(f"scattering.amplitudeFunction of tabular material {i} must be >= 2 finite values")
+            tn[i] = f.size
+            tabs.append(f)
         elif t in ("vMF", "VonMisesFisher"):
             st[i] = SCATTERING_VMF
         else:
             raise ConfigError(f"Unsupported scattering type in material {i}: {t}")
     keep += [st, sg]
+    if tabs:
+        tf = np.ascontiguousarray(np.concatenate(tabs).view(np.float64))   # (re, im) pairs
+        keep += [tn, tf]
+        c.tabular_n = tn.ctypes.data_as(C.POINTER(C.c_uint32))
+        c.tabular_f = tf.ctypes.data_as(_dp)
     c.scattering_num = len(types)
     c.scattering_type = st.ctypes.data_as(C.POINTER(C.c_int32))
     c.scattering_g = sg.ctypes.data_as(_dp)

@@ -372,7 +372,9 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     if (e) return e;
     launches++;
     if (timing) cudaEventRecord(ev[3], stream);
-    const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD;
+    // far-field x far-field: per-material weight tables on the tensor-core GEMM
+    // (real amplitudes; a tabular material's are complex and take ss_kernel)
+    const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD && !S.dev.has_tabular;
     if (farfar) {
         e = prepare_ss_tables(S);
         if (e) return e;

@@ -205,6 +205,34 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
             const bool vary = !scalar_fs && (corr ? S.static_corr[m] == 0 : (S.temporal_amp && S.moving[m]));
             const V3 xp = V3{ x1s[pp][0], x1s[pp][1], x1s[pp][2] };
             const int lg = min(l0 + tl, Nl - 1), vg = min(v0 + tv, Nv - 1);
+            if (is_tab(S, m)) {
+                // tabular scattering: complex amplitude of the angle between the
+                // incoming and outgoing directions (FP64, nee.cuh); correlation:
+                // u1 amplitude x conj(u2 amplitude) x the temporal factor
+                auto fs_tab = [&](const DevSource& a, const DevSource& bsrc, const V3& x) {
+                    double in[3], out[3];
+                    src_in64(a, lg, x, in);
+                    src_out64(bsrc, vg, x, out);
+                    return tab_amp(S, m, in[0] * out[0] + in[1] * out[1] + in[2] * out[2]);
+                };
+                for (int tt = 0; tt < kSsT; ++tt) {
+                    if (tt >= tn) break;
+                    V3 xq = xp;
+                    if (vary) {
+                        if (corr) xq = shift_u(S, xp, m, S.ticks_f[t0 + tt], -1.0f);
+                        else {
+                            const float* q = G.x1t + ((size_t)(k + pp) * Nt + t0 + tt) * 3;
+                            xq = V3{ q[0], q[1], q[2] };
+                        }
+                    }
+                    const float2 f1 = fs_tab(il, vw, xq);
+                    const float2 w = corr ? c_scale(c_mulc(f1, fs_tab(il2, vw2, xq)), expf(-c * S.abs_ticks[t0 + tt])) : f1;
+                    const float2 cv = c_mul(c_mul(as[pp][tt][tl], bs[pp][tt][tv]), w);
+                    acc[tt].x += cv.x;
+                    acc[tt].y += cv.y;
+                }
+                continue;
+            }
 #pragma unroll
             for (int tt = 0; tt < kSsT; ++tt) {
                 if (tt >= tn) break;
@@ -510,7 +538,7 @@ int launch_gemm(const GemmParams& G, cudaStream_t stream)
 int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
 {
     if (G.K <= 0) return SSTMC_NO_ERROR;
-    if (S.correlation && S.sym && S.all_static_corr) {
+    if (S.correlation && S.sym && S.all_static_corr && !S.has_tabular) {
         // two resident blocks per SM: split the paths so the grid fills them
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);

@@ -66,6 +66,73 @@ __device__ __forceinline__ float pdf_dirs(const DevScene& S, int m, const V3& a,
     return S.dims == 2 ? S.gup[m] / dn : S.gup[m] / (dn * sqrtf(dn));
 }
 
+// ---- tabular scattering: nearest table entry of the scattering angle ----
+// The angle is formed in FP64 from the FP32 positions (as the oracle does), so
+// the rounding to a table index agrees with the CPU restatement.
+
+// normalize(b - a) in FP64
+__device__ __forceinline__ void dir64(const V3& a, const V3& b, double o[3])
+{
+    const double x = (double)b.x - (double)a.x, y = (double)b.y - (double)a.y, z = (double)b.z - (double)a.z;
+    const double r = sqrt(x * x + y * y + z * z);
+    o[0] = x / r; o[1] = y / r; o[2] = z / r;
+}
+
+// round_num(safeAcos(c) (N - 1) / pi, N), 2 pi in 2D (Scattering.cuh:907-917,
+// Simulation.cuh:274-298; the FP64 safeAcos clamps within 1e-12 of +-1)
+__device__ __forceinline__ int tab_index(const DevScene& S, int m, double c)
+{
+    const double th = c < -1.0 + 1e-12 ? kPi : (c > 1.0 - 1e-12 ? 0.0 : acos(c));
+    const int N = S.tab_n[m];
+    const int n = __double2int_rn(th * (double)(N - 1) / (S.dims == 2 ? 2.0 * kPi : kPi));
+    return n < 0 ? 0 : (n >= N ? N - 1 : n);
+}
+
+__device__ __forceinline__ float2 tab_amp(const DevScene& S, int m, double c) { return S.tab_f[S.tab_off[m] + tab_index(S, m, c)]; }
+__device__ __forceinline__ float tab_pdf(const DevScene& S, int m, double c) { return S.tab_pdf[S.tab_off[m] + tab_index(S, m, c)]; }
+__device__ __forceinline__ bool is_tab(const DevScene& S, int m) { return S.has_tabular && S.scat_type[m] == SSTMC_SCATTERING_TABULAR; }
+
+// Scattering cosine of source element k attached at pa with the path
+// continuing to pb (threePointFunction, FarField.cuh:546-554,
+// PointSource.cuh:317-345): a far-field direction d (views: -d) against the
+// segment, or the direction from the point source into pa.
+__device__ __forceinline__ double f3_cos64(const DevSource& s, int k, const V3& pa, const V3& pb, bool view)
+{
+    double ab[3];
+    dir64(pa, pb, ab);
+    if (s.type == SSTMC_SOURCE_FARFIELD) {
+        const V3 d = load3(s.p, k);
+        const double c = (double)d.x * ab[0] + (double)d.y * ab[1] + (double)d.z * ab[2];
+        return view ? -c : c;
+    }
+    double in[3];
+    dir64(load3(s.p, k), pa, in);
+    return in[0] * ab[0] + in[1] * ab[1] + in[2] * ab[2];
+}
+
+// Incoming direction of illumination element l at x in FP64 (a far-field
+// direction as stored, or normalize(x - s_l))
+__device__ __forceinline__ void src_in64(const DevSource& s, int l, const V3& x, double o[3])
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) {
+        const V3 d = load3(s.p, l);
+        o[0] = d.x; o[1] = d.y; o[2] = d.z;
+        return;
+    }
+    dir64(load3(s.p, l), x, o);
+}
+
+// Outgoing direction toward view element v from x in FP64
+__device__ __forceinline__ void src_out64(const DevSource& s, int v, const V3& x, double o[3])
+{
+    if (s.type == SSTMC_SOURCE_FARFIELD) {
+        const V3 d = load3(s.p, v);
+        o[0] = d.x; o[1] = d.y; o[2] = d.z;
+        return;
+    }
+    dir64(x, load3(s.p, v), o);
+}
+
 // Direction of travel from source element k into scatterer x (illumination side).
 __device__ __forceinline__ V3 src_in(const DevSource& s, int k, const V3& x)
 {

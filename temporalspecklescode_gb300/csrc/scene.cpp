@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -124,6 +125,46 @@ bool same_source(const Scene::HostSource& a, const Scene::HostSource& b)
 
 }  // namespace
 
+// Tables of one tabular material (Scattering.cuh:272-384), in FP64 in the
+// reference's order of operations: the sampling weights |f_i|^2 (x sin(theta_i)
+// in 3D, theta_i = i pi / (N - 1)), their sum S, the cross section
+// (S / N) 2 pi (x pi in 3D), the amplitude scaled by sqrt(1 / cross section),
+// the inverse cdf by a lower bound of j / (N - 1) on the running sum of the
+// normalised weights (angle = index x pi / (N - 1), or 2 pi / (N - 1) in 2D),
+// and the evaluation pdf |f_n|^2 (x sin(theta_i) in 3D).
+static void tabular_tables(const double* f, uint32_t N, int dims, std::vector<double>& fn, std::vector<double>& pdf,
+                           std::vector<float>& cosv)
+{
+    std::vector<double> raw(N), cdf(N);
+    auto theta = [&](uint32_t i) { return ((double)i / (double)(N - 1)) * kPi; };
+    double sum = 0.0;
+    for (uint32_t i = 0; i < N; ++i) {
+        const double a2 = f[2 * i] * f[2 * i] + f[2 * i + 1] * f[2 * i + 1];
+        raw[i] = dims == 2 ? a2 : a2 * std::sin(theta(i));
+        sum += raw[i];
+    }
+    const double inv = 1.0 / sum;
+    double run = 0.0;
+    for (uint32_t i = 0; i < N; ++i) { run += raw[i] * inv; cdf[i] = run; }
+    const double cross = (sum / (double)N) * 2.0 * kPi * (dims == 3 ? kPi : 1.0);
+    const double sc = std::sqrt(1.0 / cross);
+    fn.resize(2 * N);
+    pdf.resize(N);
+    for (uint32_t i = 0; i < N; ++i) {
+        fn[2 * i] = f[2 * i] * sc;
+        fn[2 * i + 1] = f[2 * i + 1] * sc;
+        const double a2 = fn[2 * i] * fn[2 * i] + fn[2 * i + 1] * fn[2 * i + 1];
+        pdf[i] = dims == 2 ? a2 : a2 * std::sin(theta(i));
+    }
+    cosv.resize(N);
+    const double step = (dims == 2 ? 2.0 * kPi : kPi) / (double)(N - 1);
+    for (uint32_t j = 0; j < N; ++j) {
+        const double th = (double)j / (double)(N - 1);
+        const uint32_t idx = (uint32_t)(std::lower_bound(cdf.begin(), cdf.end(), th) - cdf.begin());
+        cosv[j] = (float)std::cos((double)idx * step);
+    }
+}
+
 int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
 {
     auto fail = [&](int code, const char* msg) { if (why) *why = msg; return code; };
@@ -145,16 +186,37 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         return fail(SSTMC_INVALID_CONFIG, "scattering.type must have 1..10 cells");
     int M = (int)cfg->scattering_num;
     for (int m = 0; m < kMat; ++m) D.scat_type[m] = SSTMC_SCATTERING_NOT_DEFINED;
+    size_t tab_pos = 0;   // running offset into cfg->tabular_f (entries)
     for (int m = 0; m < M; ++m) {
         const int ty = cfg->scattering_type[m];
         const double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
-        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN)
-            return fail(SSTMC_NOT_SUPPORTED, "only Isotropic and HenyeyGreenstein scattering are supported");
+        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR)
+            return fail(SSTMC_NOT_SUPPORTED, "only Isotropic, HenyeyGreenstein and Tabular scattering are supported");
         if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(g) < 1.0)) return fail(SSTMC_INVALID_CONFIG, "|g| must be < 1");
+        int toff = 0, tn = 0;
+        if (ty == SSTMC_SCATTERING_TABULAR) {
+            if (!cfg->tabular_n || !cfg->tabular_f || cfg->tabular_n[m] < 2)
+                return fail(SSTMC_INVALID_CONFIG, "a tabular material needs an amplitude table of at least 2 entries");
+            tn = (int)cfg->tabular_n[m];
+            std::vector<double> fn, pdf;
+            std::vector<float> cosv;
+            tabular_tables(cfg->tabular_f + 2 * tab_pos, (uint32_t)tn, dims, fn, pdf, cosv);
+            tab_pos += (size_t)tn;
+            toff = (int)S->tab_pdf.size();
+            for (int i = 0; i < tn; ++i) {
+                S->tab_f.push_back((float)fn[2 * i]); S->tab_f.push_back((float)fn[2 * i + 1]);
+                S->tab_f_d.push_back(fn[2 * i]); S->tab_f_d.push_back(fn[2 * i + 1]);
+                S->tab_pdf.push_back((float)pdf[i]);
+                S->tab_cos.push_back(cosv[i]);
+            }
+            D.has_tabular = 1;
+        }
         const int targets[2] = { m, 1 };
         const int nt = (M == 1) ? 2 : 1;
         for (int q = 0; q < nt; ++q) {
             const int mm = targets[q];
+            D.tab_off[mm] = toff;
+            D.tab_n[mm] = tn;
             D.scat_type[mm] = ty;
             S->g_d[mm] = g;
             D.g[mm] = (float)g;
@@ -168,7 +230,8 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     S->M = M;
     D.iso_all = 1;
     for (int m = 0; m < kMat; ++m)
-        if (D.scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(D.g[m]) < 0.0001f)) D.iso_all = 0;
+        if ((D.scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(D.g[m]) < 0.0001f))
+            || D.scat_type[m] == SSTMC_SCATTERING_TABULAR) D.iso_all = 0;
     D.iso_amp = dims == 2 ? kIsoAmp2 : kIsoAmp3;
     D.iso_pdf = dims == 2 ? kIsoPdf2 : kIsoPdf3;
 
@@ -335,6 +398,13 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     if (cudaSetDevice(S->device) != cudaSuccess) return fail(SSTMC_DEVICE_ERROR, "cudaSetDevice failed");
     int e = 0;
     for (int a = 0; a < dims && !e; ++a) e = upload(S, S->ax[a], &D.ax[a]);
+    if (!e && D.has_tabular) {
+        const float* tf = nullptr;
+        e = upload(S, S->tab_f, &tf);
+        D.tab_f = reinterpret_cast<const float2*>(tf);
+        if (!e) e = upload(S, S->tab_pdf, &D.tab_pdf);
+        if (!e) e = upload(S, S->tab_cos, &D.tab_cos);
+    }
     if (!e) e = upload(S, S->grid, &D.grid);
     if (!e) e = upload(S, S->disp_scale, &D.disp_scale);
     if (!e) e = upload(S, S->disp_u, &D.disp_u);

@@ -7,6 +7,8 @@
 // kernel by value, pointing at device buffers the Scene owns, so any number
 // of scenes can be resident at once.
 #pragma once
+#include <vector_types.h>   // float2
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -69,6 +71,13 @@ struct DevScene {
     float k2;                    // (2 pi / lambda)^2
     float iso_amp, iso_pdf;
     DevSource src[4];            // illumination, view, illumination2, view2
+    // tabular scattering (Scattering.cuh:191-482): per material its entries and
+    // the offset of its rows in the concatenated tables
+    int has_tabular;
+    int tab_n[kMat], tab_off[kMat];
+    const float2* tab_f;         // amplitude normalised by the cross section
+    const float* tab_pdf;        // evaluation pdf |f|^2 (x sin(theta) in 3D, as the reference)
+    const float* tab_cos;        // cos(icdf): the sampler's scattering cosines
 };
 
 // Host-owned scene: normalised config, float tables and device buffers.
@@ -91,6 +100,8 @@ struct Scene {
     std::vector<float> disp_scale, disp_u, ticks_f, abs_ticks;
     std::vector<double> ticks;
     double g_d[kMat] = { 0 };    // HG g per material (double, for the weight tables)
+    std::vector<float> tab_f, tab_pdf, tab_cos;   // tabular tables (device copies in dev.tab_*)
+    std::vector<double> tab_f_d;                  // normalised amplitudes (re, im) in FP64 (weight tables)
     double D_d[kMat] = { 0 };    // Brownian D per material
     DevScene dev{};
     std::vector<void*> dev_allocs;

@@ -405,9 +405,21 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             // multiple-scattering illumination vector at x2 (NEE.cuh:1525-1559, 889-1009)
             if (b == 2 && T.pass0) {
                 const V3 x12 = funit(sub3(xn, x1));
+                // tabular first material: complex amplitudes from an FP64 angle (nee.cuh)
+                const bool tab1 = is_tab(S, m1);
                 float ps = 0.0f;
-                for (int l = lane; l < Nl; l += 32)
-                    ps += T.pl[(size_t)q * Nl + l] * pdf_fast(S, m1, fsrc_in(il, l, x1), x12);
+                if (tab1) {
+                    double d12[3];
+                    dir64(x1, xn, d12);
+                    for (int l = lane; l < Nl; l += 32) {
+                        double in[3];
+                        src_in64(il, l, x1, in);
+                        ps += T.pl[(size_t)q * Nl + l] * tab_pdf(S, m1, in[0] * d12[0] + in[1] * d12[1] + in[2] * d12[2]);
+                    }
+                } else {
+                    for (int l = lane; l < Nl; l += 32)
+                        ps += T.pl[(size_t)q * Nl + l] * pdf_fast(S, m1, fsrc_in(il, l, x1), x12);
+                }
                 const float p2 = warp_sum(ps) / (float)Nl;
                 const float p2inv = CORR ? 1.0f / p2 : 1.0f / sqrtf(p2);
                 if constexpr (CORR) {
@@ -420,12 +432,32 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                         const V3 qv = V3{ 0.5f * (i1.x + i2.x) - x12.x, 0.5f * (i1.y + i2.y) - x12.y, 0.5f * (i1.z + i2.z) - x12.z };
                         const float c1k = c1base * dot3(qv, qv);
                         float f12s = 0.0f;
-                        if (stf) f12s = S.sym ? fillum2<ILP>(S, il, l, x1, xn, m1) : fillum<ILP>(S, il, l, x1, xn, m1) * fillum<ILP>(S, il2, l, x1, xn, m1);
+                        // tabular: u1 amplitude x conj(u2 amplitude), complex unless u1 == u2
+                        auto f12tab = [&](const V3& pa, const V3& pb) {
+                            const float2 f1 = tab_amp(S, m1, f3_cos64(il, l, pa, pb, false));
+                            if (S.sym) return make_float2(f1.x * f1.x + f1.y * f1.y, 0.f);
+                            return c_mulc(f1, tab_amp(S, m1, f3_cos64(il2, l, pa, pb, false)));
+                        };
+                        float2 f12cs = make_float2(0.f, 0.f);
+                        if (stf && tab1) f12cs = f12tab(x1, xn);
+                        else if (stf) f12s = S.sym ? fillum2<ILP>(S, il, l, x1, xn, m1) : fillum<ILP>(S, il, l, x1, xn, m1) * fillum<ILP>(S, il2, l, x1, xn, m1);
                         const int tfirst = lane / T.lw;
                         float e = tfirst < Nt ? __expf(-c1k * tk_abs[tfirst]) : 0.0f;
                         const float estep = geo ? __expf(-c1k * tk_abs[0] * (float)T.lg) : 0.0f;
                         for (int t = tfirst; t < Nt; t += T.lg) {
                             const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                            if (tab1) {
+                                float2 f12c = f12cs;
+                                if (!stf) {
+                                    const float tau = tk_raw[t];
+                                    f12c = f12tab(shift_u(S, x1, m1, tau, -1.0f), shift_u(S, xn, mn, tau, -1.0f));
+                                }
+                                const float sc = p2inv * (geo ? e : __expf(-c1k * tk_abs[t]));
+                                e *= estep;
+                                if (realg) T.a_ms[o] = make_float2(T.a_ms[o].x * f12c.x * sc, 0.f);
+                                else T.a_ms[o] = c_scale(c_mul(c_mulc(T.a_ms[o], T.g2[o]), f12c), sc);
+                                continue;
+                            }
                             float f12 = f12s;
                             if (!stf) {
                                 const float tau = tk_raw[t];
@@ -443,6 +475,15 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     // view rows of the first pass (NextEventEstimation.cuh:995-1004)
                     const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
                     for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
+                        if (tab1) {   // view attached at x1, path on to x2
+                            const float2 fs = stf ? tab_amp(S, m1, f3_cos64(vw, v, x1, xn, true)) : make_float2(0.f, 0.f);
+                            for (int t = lane / T.vwa; t < Nt; t += T.tga) {
+                                const size_t o = ((size_t)q * Nt + t) * Nv + v;
+                                const float2 f = stf ? fs : tab_amp(S, m1, f3_cos64(vw, v, tick_pos(xtc, t), tick_pos(xtn, t), true));
+                                T.s_ms[o] = c_scale(c_mul(T.b_ss[o], f), p2inv);
+                            }
+                            continue;
+                        }
                         const float fs = stf ? fview_entry<VWP>(S, vw, v, x1, xn, m1) : 0.0f;
                         for (int t = lane / T.vwa; t < Nt; t += T.tga) {
                             const size_t o = ((size_t)q * Nt + t) * Nv + v;
@@ -453,6 +494,15 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 } else {
                     const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
                     for (int l = lane % T.lw; l < Nl; l += T.lw) {
+                        if (tab1) {   // illumination attached at x1, path on to x2
+                            const float2 fs = stf ? tab_amp(S, m1, f3_cos64(il, l, x1, xn, false)) : make_float2(0.f, 0.f);
+                            for (int t = lane / T.lw; t < Nt; t += T.lg) {
+                                const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                                const float2 f = stf ? fs : tab_amp(S, m1, f3_cos64(il, l, tick_pos(xtc, t), tick_pos(xtn, t), false));
+                                T.a_ms[o] = c_scale(c_mul(T.a_ms[o], f), p2inv);
+                            }
+                            continue;
+                        }
                         const float fs = stf ? fillum<ILP>(S, il, l, x1, xn, m1) : 0.0f;
                         for (int t = lane / T.lw; t < Nt; t += T.lg) {
                             const size_t o = ((size_t)q * Nt + t) * Nl + l;
@@ -472,6 +522,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 const float ptk = k2 * MT;
                 const float c1base = k2 * S.D[mn];
                 const V3 back = funit(sub3(cur, xn));
+                const bool tabn = is_tab(S, mn);
                 int j = 0;
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                     const V3 o1 = fsrc_out(vw, v, xn);
@@ -484,7 +535,15 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     if (realv) { w = gweight<VWP>(S, vw, v, xn, kRoleView, sts); sts *= 2; }
                     else if (stn) { g1s = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts); g2s = gcomplex<VWP>(S, vw2, v, xn, kRoleView, sts); }
                     float f12s = 0.0f;
-                    if (stf) f12s = S.sym ? fview2<VWP>(S, vw, v, xn, cur, mn) : fview<VWP>(S, vw, v, xn, cur, mn) * fview<VWP>(S, vw2, v, xn, cur, mn);
+                    // tabular: u1 amplitude x conj(u2 amplitude), the view attached at x_b
+                    auto f12tab = [&](const V3& pa, const V3& pb) {
+                        const float2 f1 = tab_amp(S, mn, f3_cos64(vw, v, pa, pb, true));
+                        if (S.sym) return make_float2(f1.x * f1.x + f1.y * f1.y, 0.f);
+                        return c_mulc(f1, tab_amp(S, mn, f3_cos64(vw2, v, pa, pb, true)));
+                    };
+                    float2 f12cs = make_float2(0.f, 0.f);
+                    if (stf && tabn) f12cs = f12tab(xn, cur);
+                    else if (stf) f12s = S.sym ? fview2<VWP>(S, vw, v, xn, cur, mn) : fview<VWP>(S, vw, v, xn, cur, mn) * fview<VWP>(S, vw2, v, xn, cur, mn);
                     int k = 0;
                     const int tfirst = T.t0 + lane / T.vw;
                     float e = tfirst < T.t0 + T.tn ? __expf(-ck * tk_abs[tfirst]) : 0.0f;
@@ -492,14 +551,17 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     for (int t = tfirst; t < T.t0 + T.tn; t += T.tg, ++k) {
                         const float tau = tk_raw[t];
                         float f12 = f12s;
+                        float2 f12c = f12cs;
                         if (!stf) {
                             const V3 pa = shift_u(S, xn, mn, tau, -1.0f), pb = shift_u(S, cur, mcur, tau, -1.0f);
-                            f12 = S.sym ? fview2<VWP>(S, vw, v, pa, pb, mn) : fview<VWP>(S, vw, v, pa, pb, mn) * fview<VWP>(S, vw2, v, pa, pb, mn);
+                            if (tabn) f12c = f12tab(pa, pb);
+                            else f12 = S.sym ? fview2<VWP>(S, vw, v, pa, pb, mn) : fview<VWP>(S, vw, v, pa, pb, mn) * fview<VWP>(S, vw2, v, pa, pb, mn);
                         }
-                        const float dec = f12 * (geo ? e : __expf(-ck * tk_abs[t]));
+                        const float decay = geo ? e : __expf(-ck * tk_abs[t]);
+                        const float dec = tabn ? decay : f12 * decay;
                         e *= estep;
                         float2 c;
-                        if (realv) { steps += sts; c = make_float2(w * dec, 0.f); }
+                        if (realv) { steps += sts; c = make_float2(w * (tabn ? f12c.x * dec : dec), 0.f); }
                         else {
                             float2 g1 = g1s, g2 = g2s;
                             if (stn) steps += sts;
@@ -507,7 +569,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                                 g1 = gcomplex<VWP>(S, vw, v, shift_u(S, xn, mn, tau, -1.0f), kRoleView, steps);
                                 g2 = gcomplex<VWP>(S, vw2, v, shift_u(S, xn, mn, tau, 1.0f), kRoleView, steps);
                             }
-                            c = c_scale(c_mulc(g1, g2), dec);
+                            c = tabn ? c_scale(c_mul(c_mulc(g1, g2), f12c), dec) : c_scale(c_mulc(g1, g2), dec);
                         }
                         float2* a = accs + 32 * (j * T.tpl + k);
                         const float2 av = *a;
@@ -525,22 +587,34 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 auto fx = [&](int e, const V3& pa, const V3& pb, int m) {
                     return T.cbs ? fillum_exit<ILP>(S, il, e, pa, pb, m) : fview<VWP>(S, vw, e, pa, pb, m);
                 };
+                // tabular vertex material: complex amplitude, the source attached at x_b
+                const bool tabn = is_tab(S, mn);
+                auto fxc = [&](int e, const V3& pa, const V3& pb) {
+                    return tab_amp(S, mn, T.cbs ? f3_cos64(il, e, pa, pb, false) : f3_cos64(vw, e, pa, pb, true));
+                };
                 int j = 0;
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                     uint32_t sts = 0;
                     float2 gs = make_float2(0.f, 0.f);
                     if (stn) gs = gx(v, xn, sts);
-                    const float fs = stf ? fx(v, xn, cur, mn) : 0.0f;
+                    const float fs = (stf && !tabn) ? fx(v, xn, cur, mn) : 0.0f;
+                    const float2 fsc = (stf && tabn) ? fxc(v, xn, cur) : make_float2(0.f, 0.f);
                     int k = 0;
                     for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
                         float2 g = gs;
                         if (stn) steps += sts;
                         else g = gx(v, tick_pos(xtn, t), steps);
-                        const float f = stf ? fs : fx(v, tick_pos(xtn, t), tick_pos(xtc, t), mn);
                         float fr;
                         if (split) fr = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
                         else { const float ph = (float)Ls[t] * S.inv_lambda_f + xin; fr = ph - rintf(ph); }
-                        const float2 c = c_scale(c_mul(g, unit_phase(fr)), f);
+                        float2 c;
+                        if (tabn) {
+                            const float2 f = stf ? fsc : fxc(v, tick_pos(xtn, t), tick_pos(xtc, t));
+                            c = c_mul(c_mul(g, unit_phase(fr)), f);
+                        } else {
+                            const float f = stf ? fs : fx(v, tick_pos(xtn, t), tick_pos(xtc, t), mn);
+                            c = c_scale(c_mul(g, unit_phase(fr)), f);
+                        }
                         float2* a = accs + 32 * (j * T.tpl + k);
                         const float2 av = *a;
                         *a = make_float2(av.x + c.x, av.y + c.y);

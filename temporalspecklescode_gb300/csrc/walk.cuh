@@ -106,10 +106,18 @@ __device__ __forceinline__ V3 random_direction(int dims, Stream& rs)
 
 __device__ inline V3 sample_direction(const DevScene& S, int m, const V3& din, Stream& rs)
 {
-    if (S.scat_type[m] != SSTMC_SCATTERING_HENYEY_GREENSTEIN) return random_direction(S.dims, rs);
+    const int ty = S.scat_type[m];
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR) return random_direction(S.dims, rs);
     const float g = S.g[m];
     float c;
-    if (fabsf(g) < 0.001f) {
+    if (ty == SSTMC_SCATTERING_TABULAR) {
+        // inverse-cdf table entry round_num(xi N, N) (Scattering.cuh:1030-1037,
+        // Simulation.cuh:287-298: nearest, ties to even, clamped to N - 1)
+        const int N = S.tab_n[m];
+        int k = (int)rintf(fm(rs.uniform(), (float)N));
+        k = k < 0 ? 0 : (k >= N ? N - 1 : k);
+        c = S.tab_cos[S.tab_off[m] + k];
+    } else if (fabsf(g) < 0.001f) {
         c = fsb(fm(rs.uniform(), 2.0f), 1.0f);
     } else {
         const float xi = rs.uniform();

@@ -38,6 +38,8 @@ class Oracle:
         L.oracle_dda.restype = C.c_int32
         L.oracle_phase.argtypes = [C.POINTER(cf.SstmcConfig), C.c_int32, C.c_double, dp, dp]
         L.oracle_phase.restype = C.c_int32
+        L.oracle_amplitude.argtypes = [C.POINTER(cf.SstmcConfig), C.c_int32, C.c_double, dp, dp]
+        L.oracle_amplitude.restype = C.c_int32
         L.oracle_sample_cos.argtypes = [C.POINTER(cf.SstmcConfig), C.c_int32, C.c_uint64, C.c_uint32, C.POINTER(C.c_float)]
         L.oracle_sample_cos.restype = C.c_int32
         L.oracle_logf.argtypes = [C.c_float]
@@ -82,6 +84,13 @@ class Oracle:
         e = self.lib.oracle_phase(pc.ptr(), m, c, C.byref(a), C.byref(p))
         assert e == 0
         return a.value, p.value
+
+    def amplitude(self, pc: cf.PreparedConfig, m: int, c: float) -> complex:
+        re, im = C.c_double(), C.c_double()
+        e = self.lib.oracle_amplitude(pc.ptr(), m, c, C.byref(re), C.byref(im))
+        if e != 0:
+            raise RuntimeError(f"oracle_amplitude error {e}")
+        return complex(re.value, im.value)
 
     def sample_cos(self, pc: cf.PreparedConfig, m: int, seed: int, n: int):
         out = np.zeros(n, dtype=np.float32)

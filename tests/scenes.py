@@ -161,6 +161,42 @@ def reciprocal_point_2d(cbs: bool = True, batch_size=64, full_iteration=2):
     return cfg, 2
 
 
+def hg_table(g: float, n: int, dims: int, phase: float = 0.4) -> np.ndarray:
+    """A tabular amplitude: sqrt of the HG pdf on n equal angle steps over
+    0..pi (3D) or 0..2pi (2D), with a phase ramp exp(i phase theta) so that
+    the amplitudes are complex."""
+    th = np.linspace(0.0, np.pi if dims == 3 else 2.0 * np.pi, n)
+    c = np.cos(th)
+    dn = 1.0 + g * g - 2.0 * g * c
+    pdf = (1.0 - g * g) / dn ** (1.5 if dims == 3 else 1.0)
+    return np.sqrt(pdf) * np.exp(1j * phase * th)
+
+
+def tabular_field_3d(batch_size=64, full_iteration=2):
+    """3D field sampler, point sources, a tabular material next to an HG one,
+    moving scatterers (per-tick positions)."""
+    cfg, dims = field_point_3d(batch_size=batch_size, full_iteration=full_iteration)
+    cfg = dict(cfg)
+    cfg["scattering"] = {"type": ["Tabular", "HG", "Tabular"],
+                         "amplitudeFunction": [hg_table(0.7, 181, 3), 0.6, hg_table(0.2, 91, 3, phase=-0.8)]}
+    return cfg, dims
+
+
+def tabular_corr_2d(sym: bool = True, batch_size=64, full_iteration=2):
+    """2D correlation sampler with a tabular material (far-field sources);
+    sym=False gives u2 different illuminations and drift, so the u1 and u2
+    amplitudes differ (complex products)."""
+    cfg, dims = corr_far_2d_drift(batch_size=batch_size, full_iteration=full_iteration)
+    cfg = dict(cfg)
+    cfg["scattering"] = {"type": ["Tabular", "HG", "Tabular"],
+                         "amplitudeFunction": [hg_table(0.85, 361, 2), 0.3, hg_table(0.5, 200, 2, phase=1.1)]}
+    if sym:
+        cfg["illumination2"] = cfg["illumination"]
+        cfg["view2"] = cfg["view"]
+        cfg["sampler"] = dict(cfg["sampler"], U={"x": [0.0, 0.0, 0.0], "y": [0.0, 0.0, 0.0]})
+    return cfg, dims
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -181,4 +217,8 @@ def small_scenes():
         "speckle_2d_cbs": with_cbs(wl.speckle_2d(batch_size=48, full_iteration=2, n_dirs=6)),
         "reciprocal_far_3d_cbs": reciprocal_far_3d(),
         "reciprocal_point_2d_cbs": reciprocal_point_2d(),
+        "tabular_field_3d": tabular_field_3d(),
+        "tabular_corr_2d": tabular_corr_2d(),
+        "tabular_corr_2d_drift": tabular_corr_2d(sym=False),
+        "tabular_field_3d_cbs": with_cbs(tabular_field_3d()),
     }

@@ -181,3 +181,59 @@ def test_cbs_correlation_not_supported(oracle):
     pc = cf.prepare(cfg, dims)
     with pytest.raises(Exception):
         oracle.render(pc, 1)
+
+
+def _tabular_cfg(dims, table, g_other=0.5):
+    cfg, _ = wl.speckle_2d() if dims == 2 else wl.correlation_3d(n_side=2, n_lags=1)
+    cfg = dict(cfg)
+    cfg["scattering"] = {"type": ["Tabular", "HG"], "amplitudeFunction": [table, g_other]}
+    return cf.prepare(cfg, dims)
+
+
+@pytest.mark.parametrize("dims,g", [(2, 0.8), (3, 0.9), (3, 0.3)])
+def test_tabular_normalised_like_hg(oracle, dims, g):
+    """A table of sqrt(HG pdf) (Scattering.cuh:272-384): after the cross-section
+    normalisation the tabular amplitude and (2D) pdf match HG's at the nodes,
+    to the table's angular resolution."""
+    from tests.scenes import hg_table
+    n = 4001
+    pc = _tabular_cfg(dims, np.abs(hg_table(g, n, dims)), g)
+    th = np.linspace(0.05, 0.95, 7) * np.pi
+    for t in th:
+        a_tab = oracle.amplitude(pc, 0, math.cos(t))
+        a_hg, pdf_hg = oracle.phase(pc, 1, math.cos(t))
+        assert abs(a_tab.imag) < 1e-15
+        assert abs(a_tab.real / a_hg - 1.0) < 2e-3
+        _, pdf_tab = oracle.phase(pc, 0, math.cos(t))
+        if dims == 2:   # the 3D evaluation pdf carries sin(theta), as the reference's table
+            assert abs(pdf_tab / pdf_hg - 1.0) < 4e-3
+        else:
+            assert abs(pdf_tab / (pdf_hg * math.sin(t)) - 1.0) < 4e-3
+
+
+def test_tabular_lookup_is_nearest_entry(oracle):
+    """The amplitude is the table entry nearest the angle (round half to even),
+    scaled by one real normalisation: the complex phase of each entry is kept."""
+    n = 37
+    f = (1.0 + np.arange(n)) * np.exp(1j * 0.1 * np.arange(n) ** 1.3)
+    pc = _tabular_cfg(3, f)
+    step = np.pi / (n - 1)
+    ratios = []
+    for i in range(n):
+        for off in (-0.3, 0.0, 0.3):
+            th = min(max(i * step + off * step, 0.0), np.pi)
+            a = oracle.amplitude(pc, 0, math.cos(th))
+            ratios.append(a / f[i])
+    ratios = np.array(ratios)
+    assert np.allclose(ratios.imag, 0.0, atol=1e-12)
+    assert np.allclose(ratios.real, ratios.real[0], rtol=1e-12)
+
+
+@pytest.mark.parametrize("dims,g", [(2, 0.7), (3, 0.8)])
+def test_tabular_sampler_matches_table(oracle, dims, g):
+    """Inverse-cdf sampling of a tabular material (Scattering.cuh:1030-1037):
+    the mean scattering cosine of an HG-shaped table is g."""
+    from tests.scenes import hg_table
+    pc = _tabular_cfg(dims, hg_table(g, 2001, dims))
+    c = np.asarray(oracle.sample_cos(pc, 0, 3, 200000), dtype=np.float64)
+    assert abs(c.mean() - g) < 0.01
