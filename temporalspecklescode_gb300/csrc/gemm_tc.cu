@@ -25,9 +25,9 @@
 //   warps 1-8   split each raw box into TF32 hi / lo tiles stored in the
 //               128-byte-swizzled K-major layout the MMA descriptors
 //               describe (2-deep ring), one 8-path group per warp;
-//   warps 9-12  drain an accumulator every 128 paths into compensated FP32
+//   warps 9-12  drain an accumulator every 256 paths into compensated FP32
 //               (hi, lo) pairs kept in tensor memory too (TwoSum), so FP32
-//               rounding grows with a 128-path window rather than with the
+//               rounding grows with a 256-path window rather than with the
 //               whole path range, and add the tile to V with FP64 atomics
 //               at the end.
 // Every mbarrier wait is bounded; a wait that runs out sets SSTMC_TIMEOUT in
@@ -51,7 +51,7 @@ constexpr int kTN = 128;          // D columns per CTA (64 view entries, re / im
 constexpr int kKS = 32;           // paths per step: one 128-byte swizzle row of TF32
 constexpr int kStages = 2;        // hi / lo tiles in flight to the MMA
 constexpr int kRaw = 3;           // raw TMA boxes in flight from global memory
-constexpr int kWinSteps = 4;      // steps per accumulation window (128 paths)
+constexpr int kWinSteps = 8;      // steps per accumulation window (256 paths)
 constexpr int kSplitWarps = 8;
 constexpr int kEpiWarps = 4;
 constexpr int kThreads = (1 + kSplitWarps + kEpiWarps) * 32;  // 416
