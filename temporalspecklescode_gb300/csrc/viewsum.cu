@@ -283,10 +283,19 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
             const float c1k = c1base * dot3(qv, qv);
             const float f12 = (ilp && S.iso_all) ? S.iso_amp * S.iso_amp : pdf1[k];
             const float base = wl[k] * f12 * p2inv;
+            // tick t of element l at l + t Nl (real rows: floats, else (re, 0) pairs)
             if (geo) {
                 const float es = __expf(-c1k * tau0);
                 float e = es;
-                for (int t = 0; t < Nt; ++t) { put_ams((size_t)t * Nl + l, base * e); e *= es; }
+                if (real) {
+                    float* o = amr + l;
+#pragma unroll 4
+                    for (int t = 0; t < Nt; ++t, o += Nl) { *o = base * e; e *= es; }
+                } else {
+                    float2* o = ams + l;
+#pragma unroll 4
+                    for (int t = 0; t < Nt; ++t, o += Nl) { *o = make_float2(base * e, 0.f); e *= es; }
+                }
             } else {
                 for (int t = 0; t < Nt; ++t) put_ams((size_t)t * Nl + l, base * __expf(-c1k * S.abs_ticks[t]));
             }
