@@ -138,7 +138,7 @@ typedef struct sstmc_config {
     int32_t is_forced_inside_bin;  /* default 0; 1 is not supported */
 
     /* config.tracer (MatlabInterface.cu:1374-1457) */
-    int32_t is_cbs;                /* default 0; 1: coherent backscattering (field sampler only) */
+    int32_t is_cbs;                /* default 0; 1: coherent backscattering (correlation sampler: static scatterers) */
 
     /* build-specific */
     int32_t precision;             /* SSTMC_PRECISION_* */

@@ -359,8 +359,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     /* sampler */
     if (!cfg->t || cfg->t_num == 0) return SSTMC_INVALID_CONFIG;
     S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
-    /* CBS of the correlation sampler (the C2-C4 cross terms) is not built */
-    if (cfg->is_cbs && S->correlation) return SSTMC_NOT_SUPPORTED;
     S->cbs = cfg->is_cbs ? 1 : 0;
     if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return SSTMC_INVALID_CONFIG;
     if (S->correlation) {
@@ -376,6 +374,11 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         S->D[m] = (m < M && cfg->D) ? cfg->D[m] : 0.0;
         if (S->D[m] < 0) return SSTMC_INVALID_CONFIG; /* MatlabInterface.cu:1278-1283 */
         for (int i = 0; i < 3; ++i) S->U_f[m][i] = (m < M && cfg->U && (i < dims)) ? (float)cfg->U[3 * m + i] : 0.0f;
+        /* correlation CBS is built for static scatterers (no drift U) and real-valued
+         * phase functions (no tabular material) */
+        if (S->cbs && S->correlation && (S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f))
+            return SSTMC_NOT_SUPPORTED;
+        if (S->cbs && S->correlation && S->scat_type[m] == SSTMC_SCATTERING_TABULAR) return SSTMC_NOT_SUPPORTED;
     }
     /* field sampler: ticks sorted around the mean, TemporalSampler.cuh:958-1150 */
     S->disp_scale = calloc((size_t)OM * Nt, sizeof(float));
@@ -1054,6 +1057,103 @@ typedef struct {
     double* P1; double* P2;           /* [Nl] */
 } o_work;
 
+/* CBS of the correlation sampler, static scatterers (NextEventEstimation.cuh:
+ * 1237-1378, SourceInterface.cuh:270-354): for every vertex x_b (b >= 2) the
+ * cross terms of the direct and reversed paths,
+ *   T2 = Gl_b(l) conj(u2Gv_b(v)) C2_l1v2(x_b) x conj(u2Gl0(l)) Gv0(v) C2_v1l2(x1)
+ *   T3 = conj(u2Gl_b(l)) Gv_b(v) C3_v1l2(x_b) x Gl0(l) conj(u2Gv0(v)) C3_l1v2(x1)
+ *   T4 = Gl_b(l) conj(u2Gl_b(l)) C4_l1l2(x_b) x Gv0(v) conj(u2Gv0(v)) C4_v1v2(x1)
+ * each with the u1 path transfer exp(-k^2 |t| MT_b) (the path phase cancels),
+ * added as 0.5 (T2 + T3 + T4) (the direct term T1 takes the same 0.5).  Gl0 /
+ * Gv0 carry 1 / p2; G* at x_b are the NEE vector times the three-point
+ * amplitude of the source attached there; C = exp(-k^2 |D t| |m|^2) with
+ * m = (a + b) / 2 - (direction to the path's next point), a and b the
+ * directions from the two ends' sources into the vertex (a view's is minus
+ * its outgoing direction).  Rays traced here are not counted in the DDA
+ * statistics. */
+static void o_cbs_corr(const o_scene* S, const o_verts* V, oc* Vacc, double p2)
+{
+    int Nl = S->src[0].n, Nv = S->src[1].n, Nt = S->Nt, B = V->B;
+    const o_src *il = &S->src[0], *vw = &S->src[1], *il2 = &S->src[2], *vw2 = &S->src[3];
+    const float *x1 = V->x, *x2 = V->x + 3;
+    int m1 = V->m[0];
+    double k2 = (2.0 * O_PI / S->lambda) * (2.0 * O_PI / S->lambda);
+    uint64_t dummy = 0;
+    double d12[3]; o_dir64(x1, x2, d12);
+    oc* G0l = malloc(sizeof(oc) * Nl); oc* U0l = malloc(sizeof(oc) * Nl);
+    oc* G0v = malloc(sizeof(oc) * Nv); oc* U0v = malloc(sizeof(oc) * Nv);
+    oc* Gl = malloc(sizeof(oc) * Nl); oc* U2l = malloc(sizeof(oc) * Nl);
+    oc* Gv = malloc(sizeof(oc) * Nv); oc* U2v = malloc(sizeof(oc) * Nv);
+    double* dl = malloc(sizeof(double) * 12 * (Nl + Nv));   /* directions at x1 and x_b */
+    if (!G0l || !U0l || !G0v || !U0v || !Gl || !U2l || !Gv || !U2v || !dl) goto done;
+    double *in1 = dl, *in2 = dl + 3 * Nl, *mo1 = dl + 6 * Nl, *mo2 = dl + 6 * Nl + 3 * Nv;
+    double *in1b = dl + 6 * (Nl + Nv), *in2b = in1b + 3 * Nl, *mo1b = in1b + 6 * Nl, *mo2b = mo1b + 3 * Nv;
+    for (int l = 0; l < Nl; ++l) {
+        G0l[l] = oc_scale(oc_mul(o_g(S, il, l, x1, 0, &dummy), o_f3(S, il, l, x1, x2, m1, 0)), 1.0 / p2);
+        U0l[l] = oc_mul(o_g(S, il2, l, x1, 0, &dummy), o_f3(S, il2, l, x1, x2, m1, 0));
+        o_src_dir(il, l, x1, 0, in1 + 3 * l); o_src_dir(il2, l, x1, 0, in2 + 3 * l);
+    }
+    for (int v = 0; v < Nv; ++v) {
+        G0v[v] = oc_scale(oc_mul(o_g(S, vw, v, x1, 1, &dummy), o_f3(S, vw, v, x1, x2, m1, 1)), 1.0 / p2);
+        U0v[v] = oc_mul(o_g(S, vw2, v, x1, 1, &dummy), o_f3(S, vw2, v, x1, x2, m1, 1));
+        o_src_dir(vw, v, x1, 1, mo1 + 3 * v); o_src_dir(vw2, v, x1, 1, mo2 + 3 * v);
+        for (int i = 0; i < 3; ++i) { mo1[3 * v + i] = -mo1[3 * v + i]; mo2[3 * v + i] = -mo2[3 * v + i]; }
+    }
+    double MT = 0;
+    for (int b = 1; b < B; ++b) {
+        const float* xb = V->x + 3 * b;
+        const float* xa = V->x + 3 * (b - 1);
+        int mb = V->m[b], ma = V->m[b - 1];
+        if (b >= 2) {
+            double u[3], w[3];
+            o_dir64(V->x + 3 * (b - 2), xa, u); o_dir64(xa, xb, w);
+            double q[3] = { u[0] - w[0], u[1] - w[1], u[2] - w[2] };
+            MT += S->D[ma] * o_dot(q, q);
+        }
+        double back[3]; o_dir64(xb, xa, back);
+        for (int l = 0; l < Nl; ++l) {
+            Gl[l] = oc_mul(o_g(S, il, l, xb, 0, &dummy), o_f3(S, il, l, xb, xa, mb, 0));
+            U2l[l] = oc_mul(o_g(S, il2, l, xb, 0, &dummy), o_f3(S, il2, l, xb, xa, mb, 0));
+            o_src_dir(il, l, xb, 0, in1b + 3 * l); o_src_dir(il2, l, xb, 0, in2b + 3 * l);
+        }
+        for (int v = 0; v < Nv; ++v) {
+            Gv[v] = oc_mul(o_g(S, vw, v, xb, 1, &dummy), o_f3(S, vw, v, xb, xa, mb, 1));
+            U2v[v] = oc_mul(o_g(S, vw2, v, xb, 1, &dummy), o_f3(S, vw2, v, xb, xa, mb, 1));
+            o_src_dir(vw, v, xb, 1, mo1b + 3 * v); o_src_dir(vw2, v, xb, 1, mo2b + 3 * v);
+            for (int i = 0; i < 3; ++i) { mo1b[3 * v + i] = -mo1b[3 * v + i]; mo2b[3 * v + i] = -mo2b[3 * v + i]; }
+        }
+        for (int t = 0; t < Nt; ++t) {
+            double at = fabs(S->ticks[t]);
+            double pt = exp(-k2 * at * MT);
+            double dtD1 = k2 * fabs(S->D[m1] * S->ticks[t]), dtDb = k2 * fabs(S->D[mb] * S->ticks[t]);
+            for (int v = 0; v < Nv; ++v)
+                for (int l = 0; l < Nl; ++l) {
+                    double q2b = 0, q21 = 0, q3b = 0, q31 = 0, q4b = 0, q41 = 0;
+                    for (int i = 0; i < 3; ++i) {
+                        double e;
+                        e = 0.5 * (in1b[3 * l + i] + mo2b[3 * v + i]) - back[i]; q2b += e * e;
+                        e = 0.5 * (mo1[3 * v + i] + in2[3 * l + i]) - d12[i]; q21 += e * e;
+                        e = 0.5 * (mo1b[3 * v + i] + in2b[3 * l + i]) - back[i]; q3b += e * e;
+                        e = 0.5 * (in1[3 * l + i] + mo2[3 * v + i]) - d12[i]; q31 += e * e;
+                        e = 0.5 * (in1b[3 * l + i] + in2b[3 * l + i]) - back[i]; q4b += e * e;
+                        e = 0.5 * (mo1[3 * v + i] + mo2[3 * v + i]) - d12[i]; q41 += e * e;
+                    }
+                    oc t2 = oc_mul(oc_mul(Gl[l], oc_conj(U2v[v])), oc_mul(oc_conj(U0l[l]), G0v[v]));
+                    oc t3 = oc_mul(oc_mul(oc_conj(U2l[l]), Gv[v]), oc_mul(G0l[l], oc_conj(U0v[v])));
+                    oc t4 = oc_mul(oc_mul(Gl[l], oc_conj(U2l[l])), oc_mul(G0v[v], oc_conj(U0v[v])));
+                    t2 = oc_scale(t2, exp(-dtDb * q2b - dtD1 * q21));
+                    t3 = oc_scale(t3, exp(-dtDb * q3b - dtD1 * q31));
+                    t4 = oc_scale(t4, exp(-dtDb * q4b - dtD1 * q41));
+                    oc* dst = Vacc + ((size_t)t * Nv + v) * Nl + l;
+                    dst->re += 0.5 * pt * (t2.re + t3.re + t4.re);
+                    dst->im += 0.5 * pt * (t2.im + t3.im + t4.im);
+                }
+        }
+    }
+done:
+    free(G0l); free(U0l); free(G0v); free(U0v); free(Gl); free(U2l); free(Gv); free(U2v); free(dl);
+}
+
 /* Evaluate the NEE vectors of one walked path and accumulate into V (if not NULL).
  * Field mode: NextEventEstimation.cuh:1016-1136 (single), 1138-1458 (multiple).
  * Correlation mode: the same, with TemporalSamplerCorrelation.cuh and
@@ -1251,16 +1351,18 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                 }
             }
         }
+        if (S->cbs && Vacc) o_cbs_corr(S, V, Vacc, p2);
     }
     if (Vacc) {
-        /* CBS: (direct + reversed) / sqrt(2) (NextEventEstimation.cuh:1385-1391, :1448-1454) */
-        const double sc = S->cbs ? sqrt(0.5) : 1.0;
+        /* CBS: field (direct + reversed) / sqrt(2), correlation 0.5 (the cross terms
+         * are added by o_cbs_corr) (NextEventEstimation.cuh:1385-1391, :1448-1454) */
+        const double sc = S->cbs ? (S->correlation ? 0.5 : sqrt(0.5)) : 1.0;
         for (int t = 0; t < Nt; ++t)
             for (int v = 0; v < Nv; ++v) {
                 oc s = W->s_ms[t * Nv + v], sr = W->sr_ms[t * Nv + v];
                 for (int l = 0; l < Nl; ++l) {
                     oc c = oc_mul(W->a_ms[t * Nl + l], s);
-                    if (S->cbs) {
+                    if (S->cbs && !S->correlation) {
                         oc r = oc_mul(W->ar_ms[t * Nl + l], sr);
                         c.re += r.re; c.im += r.im;
                     }

@@ -68,7 +68,8 @@ size_t Engine::bytes_per_path(const Scene& S)
 {
     const size_t Nt = S.Nt, Nl = S.Nl, Nv = S.Nv;
     return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16
-         + (S.cfg_copy.is_cbs ? 8 * Nt * (Nl + Nv) : 0)   // CBS: the reversed path's rows
+         + ((S.cfg_copy.is_cbs && !S.correlation) ? 8 * Nt * (Nl + Nv) : 0)   // field CBS: the reversed path's rows
+         + 4                                                                  // p2 (correlation CBS)
          + walk_slot_bytes_per_path();
 }
 
@@ -101,7 +102,7 @@ int Engine::ensure(Scene& S, uint32_t paths)
         if (cudaMallocAsync(p, bytes ? bytes : 1, stream) != cudaSuccess) return false;
         return true;
     };
-    const size_t rows = S.cfg_copy.is_cbs ? 2 * (size_t)paths : paths;   // CBS: direct rows, then the reversed path's
+    const size_t rows = (S.cfg_copy.is_cbs && !S.correlation) ? 2 * (size_t)paths : paths;   // field CBS: direct rows, then the reversed path's
     bool ok = alloc((void**)&a_ms, rows * Nt * Nl * sizeof(float2)) && alloc((void**)&s_ms, rows * Nt * Nv * sizeof(float2))
            && alloc((void**)&a_ss, paths * Nt * Nl * sizeof(float2)) && alloc((void**)&b_ss, paths * Nt * Nv * sizeof(float2))
            && alloc((void**)&g2, S.correlation ? paths * Nt * Nl * sizeof(float2) : 8)
@@ -115,7 +116,8 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' path counter
            && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
            && alloc((void**)&ovf, (size_t)walk_overflow_blocks(paths) * kWalkSlotVerts * sizeof(float4))
-           && alloc((void**)&ovf_owner, (size_t)walk_overflow_blocks(paths) * sizeof(uint2));
+           && alloc((void**)&ovf_owner, (size_t)walk_overflow_blocks(paths) * sizeof(uint2))
+           && alloc((void**)&p2v, paths * sizeof(float));
     if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
     cap = paths;
     return SSTMC_NO_ERROR;
@@ -124,10 +126,10 @@ int Engine::ensure(Scene& S, uint32_t paths)
 void Engine::release()
 {
     void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts,
-                   slots, longq, ovf, ovf_owner };
+                   slots, longq, ovf, ovf_owner, p2v };
     for (void* p : ps) if (p) cudaFreeAsync(p, stream);
     counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
-    slots = nullptr; longq = nullptr; ovf = nullptr; ovf_owner = nullptr;
+    slots = nullptr; longq = nullptr; ovf = nullptr; ovf_owner = nullptr; p2v = nullptr;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
     pl = x1 = x1t = nullptr;
     m1 = nullptr; totals = nullptr; err = nullptr; V = nullptr; W = nullptr;
@@ -267,6 +269,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     T.a_ms = a_ms; T.s_ms = s_ms; T.a_ss = a_ss; T.b_ss = b_ss; T.g2 = g2; T.pl = pl;
     T.x1 = x1; T.x1t = S.correlation ? nullptr : x1t; T.m1 = m1; T.totals = totals; T.err = err;
     if (dbg) T.dda = dbg->dda;
+    if (S.correlation && S.cfg_copy.is_cbs) T.p2 = p2v;   // for the CBS cross terms (contract_chunk)
     rows_real = false;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -318,7 +321,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
             first_pass = false;
         }
     }
-    if (S.cfg_copy.is_cbs) {
+    if (S.cfg_copy.is_cbs && !S.correlation) {
         // field CBS: the reversed path's rows (Gv0 of the views, GlSum of the
         // illuminations) into the second half of the row buffers, rows n .. 2n - 1,
         // so one contraction over 2n rows sums the direct and reversed products
@@ -353,10 +356,12 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     const bool compensated = S.precision == SSTMC_PRECISION_SPLIT;
     GemmParams G;
     std::memset(&G, 0, sizeof(G));
-    // field CBS: 2n rows (direct, then reversed) and V += (direct + reversed) / sqrt(2)
-    const bool cbs = S.cfg_copy.is_cbs != 0;
+    // field CBS: 2n rows (direct, then reversed) and V += (direct + reversed) / sqrt(2);
+    // correlation CBS: V += 0.5 (direct + the cross terms of cbs_corr_kernel)
+    const bool cbs = S.cfg_copy.is_cbs != 0 && !S.correlation;
+    const bool cbs_corr = S.cfg_copy.is_cbs != 0 && S.correlation;
     G.Nt = S.Nt; G.Nl = S.Nl; G.Nv = S.Nv; G.V = V; G.K = (int)(cbs ? 2 * n : n); G.compensated = compensated ? 1 : 0;
-    G.scale = cbs ? std::sqrt(0.5) : 1.0;
+    G.scale = cbs ? std::sqrt(0.5) : (cbs_corr ? 0.5 : 1.0);
     const int tiles = ((S.Nl + 31) / 32) * ((S.Nv + 31) / 32) * S.Nt;
     const int ksplit = std::max(1, (4 * sms + tiles - 1) / tiles);
     int kchunk = (int)((G.K + ksplit - 1) / ksplit);
@@ -398,6 +403,14 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
         kc = ((kc + 255) / 256) * 256;
         P.kchunk = kc;
         e = launch_ss(S.dev, P, stream);
+        if (e) return e;
+        launches++;
+    }
+    if (cbs_corr) {
+        CbsCorrParams C;
+        std::memset(&C, 0, sizeof(C));
+        C.verts = verts; C.counts = counts; C.offsets = offsets; C.p2 = p2v; C.V = V; C.K = (int)n;
+        e = launch_cbs_corr(S.dev, C, stream);
         if (e) return e;
         launches++;
     }

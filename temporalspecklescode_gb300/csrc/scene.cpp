@@ -313,10 +313,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     if (!cfg->t || cfg->t_num == 0) return fail(SSTMC_INVALID_CONFIG, "sampler.t is required");
     S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
     if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return fail(SSTMC_INVALID_CONFIG, "unsupported sampler");
-    // coherent backscattering is built for the field sampler (reversed-path
-    // rows); the correlation sampler's C2-C4 cross terms are not
-    if (cfg->is_cbs && S->correlation)
-        return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS with the TemporalCorrelationSampler is not supported");
     D.correlation = S->correlation ? 1 : 0;
     if (S->correlation) {
         if (S->hsrc[2].type == SSTMC_SOURCE_NONE || S->hsrc[3].type == SSTMC_SOURCE_NONE)
@@ -345,6 +341,10 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     }
     D.all_static_corr = 1;
     for (int m = 0; m < kMat; ++m) if (!D.static_corr[m]) D.all_static_corr = 0;
+    // CBS of the correlation sampler is built for static scatterers (no drift U)
+    // and real phase functions
+    if (cfg->is_cbs && S->correlation && (!D.all_static_corr || D.has_tabular))
+        return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS with the TemporalCorrelationSampler needs static scatterers (U = 0) and no tabular material");
     D.ticks_geometric = S->abs_ticks[0] > 0.0f;
     for (int t = 0; t < Nt; ++t)
         if (S->abs_ticks[t] != (float)(t + 1) * S->abs_ticks[0]) D.ticks_geometric = 0;

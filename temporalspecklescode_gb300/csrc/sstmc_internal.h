@@ -34,6 +34,7 @@ struct Engine {
     float4* slots = nullptr;      // single-pass walk: first 64 vertices of each path of a chunk
     uint32_t* longq = nullptr;    // paths of the chunk that found the overflow pool empty
     float4* ovf = nullptr;        // overflow blocks of 64 vertices (pathwalk.cu)
+    float* p2v = nullptr;         // [paths] second-point probability (correlation CBS)
     uint2* ovf_owner = nullptr;
     float4* verts = nullptr;
     size_t verts_cap = 0;

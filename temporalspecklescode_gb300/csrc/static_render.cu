@@ -96,7 +96,7 @@ size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 // Byte layout of the scratch for a chunk of n paths.
 struct Layout {
     size_t V, totals, err, vtotal, ticks, W, fixed_end;
-    size_t a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, counts, misses, offsets, block_sums, slots, longq, ovf, ovf_owner, rows_end;
+    size_t a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, counts, misses, offsets, block_sums, slots, longq, ovf, ovf_owner, p2v, rows_end;
 };
 
 Layout layout(const Scene& S, bool farfar, uint32_t n)
@@ -112,7 +112,7 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.ticks = take(farfar ? Nt * sizeof(double) : 0);
     L.W = take(farfar ? (size_t)kMat * Nt * Nv * Nl * sizeof(float) : 0);
     L.fixed_end = o;
-    const size_t rows = S.cfg_copy.is_cbs ? 2 * (size_t)n : n;   // CBS: direct rows, then the reversed path's
+    const size_t rows = (S.cfg_copy.is_cbs && !S.correlation) ? 2 * (size_t)n : n;   // field CBS: direct rows, then the reversed path's
     L.a_ms = take(rows * Nt * Nl * sizeof(float2));
     L.s_ms = take(rows * Nt * Nv * sizeof(float2));
     L.a_ss = take(n * Nt * Nl * sizeof(float2));
@@ -130,6 +130,7 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.longq = take(n * sizeof(uint32_t));
     L.ovf = take((size_t)walk_overflow_blocks(n) * kWalkSlotVerts * sizeof(float4));
     L.ovf_owner = take((size_t)walk_overflow_blocks(n) * sizeof(uint2));
+    L.p2v = take(n * sizeof(float));
     L.rows_end = o;
     return L;
 }
@@ -157,6 +158,7 @@ void point_engine(Engine& E, unsigned char* base, const Layout& L)
     E.longq = reinterpret_cast<uint32_t*>(base + L.longq);
     E.ovf = reinterpret_cast<float4*>(base + L.ovf);
     E.ovf_owner = reinterpret_cast<uint2*>(base + L.ovf_owner);
+    E.p2v = reinterpret_cast<float*>(base + L.p2v);
     E.verts = reinterpret_cast<float4*>(base + L.rows_end);
     E.verts_cap = L.rows_end < kStaticScratchBytes ? (kStaticScratchBytes - L.rows_end) / sizeof(float4) : 0;
 }

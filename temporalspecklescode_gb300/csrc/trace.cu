@@ -15,6 +15,8 @@
 // multiple- and single-scattering terms -- which the contraction consumes.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "nee.cuh"
 #include "sstmc_internal.h"
 #include "trace.h"
@@ -422,6 +424,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 }
                 const float p2 = warp_sum(ps) / (float)Nl;
                 const float p2inv = CORR ? 1.0f / p2 : 1.0f / sqrtf(p2);
+                if (T.p2 && lane == 0) T.p2[q] = p2;
                 if constexpr (CORR) {
                     const bool stf = S.static_corr[m1] && S.static_corr[mn];
                     const bool realg = S.sym && S.static_corr[m1];
@@ -663,7 +666,184 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     }
 }
 
+// ---- CBS of the correlation sampler, static scatterers (NextEventEstimation.cuh:1237-1378) ----
+// For every vertex x_b (b >= 2) of every path, the cross terms of the direct
+// and reversed paths (SourceInterface.cuh:270-354 for the temporal factors):
+//   T2 = Gl_b(l) conj(u2Gv_b(v)) conj(u2Gl0(l)) Gv0(v) exp(-k^2 |t| (D_b |m2b|^2 + D_1 |m21|^2))
+//   T3 = conj(u2Gl_b(l)) Gv_b(v) Gl0(l) conj(u2Gv0(v)) exp(-k^2 |t| (D_b |m3b|^2 + D_1 |m31|^2))
+//   T4 = Gl_b(l) conj(u2Gl_b(l)) Gv0(v) conj(u2Gv0(v)) exp(-k^2 |t| (D_b |m4b|^2 + D_1 |m41|^2))
+// times the u1 path transfer exp(-k^2 |t| MT_b), V += 0.5 (T2 + T3 + T4).
+// Gl0 / Gv0 (first vertex, the path on to x2) carry 1 / p2; the vectors at x_b
+// are the NEE vector times the amplitude of the source attached at x_b with
+// the path back to x_{b-1}; m = (a + b) / 2 - (direction to the other path
+// point), a, b the directions from the two ends' sources into the vertex (a
+// view's is minus its outgoing direction).  Block = a 16 x 16 (l, v) tile for
+// a chunk of ticks and a range of paths; four 16-thread groups stage the u1 /
+// u2 illumination and view quantities of the current vertex in shared memory.
+// Its rays are not counted in the DDA statistics.
+constexpr int kCbT = 16, kCbTicks = 8;
+
+template <bool ILP, bool VWP>
+__global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ DevScene S, const CbsCorrParams P)
+{
+    __shared__ float2 g0l[2][kCbT], g0v[2][kCbT], gb_l[2][kCbT], gb_v[2][kCbT];   // [u1 / u2][element]
+    __shared__ float d0l[2][kCbT][3], d0v[2][kCbT][3], dbl[2][kCbT][3], dbv[2][kCbT][3];
+    __shared__ float geo[8];   // d12 (3), back (3), D_b, MT_b
+    const int tl = threadIdx.x % kCbT, tv = threadIdx.x / kCbT;
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const int l0 = blockIdx.x * kCbT, v0 = blockIdx.y * kCbT;
+    const int tchunks = (Nt + kCbTicks - 1) / kCbTicks;
+    const int t0 = (blockIdx.z % tchunks) * kCbTicks, tn = min(kCbTicks, Nt - t0);
+    const int ks = blockIdx.z / tchunks;
+    const int kb = ks * P.kchunk, ke = min(P.K, kb + P.kchunk);
+    const DevSource* srcl[2] = { &S.src[0], &S.src[2] };
+    const DevSource* srcv[2] = { &S.src[1], &S.src[3] };
+    // staging role of this thread: group 0 / 1: illumination u1 / u2, 2 / 3: view u1 / u2
+    const int grp = threadIdx.x / kCbT, ge = threadIdx.x % kCbT;
+    const bool stager = threadIdx.x < 4 * kCbT;
+    const bool isl = grp < 2;
+    const int u = grp & 1;
+    const int el = min((isl ? l0 : v0) + ge, (isl ? Nl : Nv) - 1);
+    float2 acc[kCbTicks];
+    double accd[kCbTicks][2];
+#pragma unroll
+    for (int i = 0; i < kCbTicks; ++i) { acc[i] = make_float2(0.f, 0.f); accd[i][0] = accd[i][1] = 0.0; }
+    int window = 0;
+    for (int p = kb; p < ke; ++p) {
+        const uint32_t B = P.counts[p];
+        if (B < 2) continue;   // uniform over the block
+        const float4* vq = P.verts + P.offsets[p];
+        const float4 v1 = vq[0], v2 = vq[1];
+        const V3 x1 = V3{ v1.x, v1.y, v1.z }, x2 = V3{ v2.x, v2.y, v2.z };
+        const int m1 = (int)(__float_as_uint(v1.w) & 15u);
+        const float p2inv = 1.0f / P.p2[p];
+        __syncthreads();   // the previous path's last vertex is consumed
+        if (stager) {
+            uint32_t st = 0;
+            if (isl) {
+                const DevSource& s = *srcl[u];
+                const float2 g = gcomplex<ILP>(S, s, el, x1, kRoleIllum, st);
+                const float f = fillum<ILP>(S, s, el, x1, x2, m1);
+                g0l[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                const V3 d = fsrc_in(s, el, x1);
+                d0l[u][ge][0] = d.x; d0l[u][ge][1] = d.y; d0l[u][ge][2] = d.z;
+            } else {
+                const DevSource& s = *srcv[u];
+                const float2 g = gcomplex<VWP>(S, s, el, x1, kRoleView, st);
+                const float f = fview_entry<VWP>(S, s, el, x1, x2, m1);
+                g0v[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                const V3 d = fsrc_out(s, el, x1);
+                d0v[u][ge][0] = -d.x; d0v[u][ge][1] = -d.y; d0v[u][ge][2] = -d.z;
+            }
+        }
+        if (threadIdx.x == 0) {
+            const V3 d = funit(sub3(x2, x1));
+            geo[0] = d.x; geo[1] = d.y; geo[2] = d.z;
+        }
+        float MT = 0.0f;
+        V3 prev = x1, cur = x1;
+        for (uint32_t b = 2; b <= B; ++b) {
+            const float4 vb = vq[b - 1];
+            const V3 xn = V3{ vb.x, vb.y, vb.z };
+            const int mn = (int)(__float_as_uint(vb.w) & 15u);
+            const int mc = (int)(__float_as_uint(vq[b - 2].w) & 15u);
+            if (b >= 3) {   // momentum transfer of the inner vertex cur
+                const V3 dq = sub3(funit(sub3(cur, prev)), funit(sub3(xn, cur)));
+                MT += S.D[mc] * dot3(dq, dq);
+            }
+            prev = cur;
+            cur = xn;
+            __syncthreads();   // the previous vertex's records are consumed
+            if (stager) {
+                uint32_t st = 0;
+                if (isl) {
+                    const DevSource& s = *srcl[u];
+                    gb_l[u][ge] = c_scale(gcomplex<ILP>(S, s, el, xn, kRoleIllum, st), fillum_exit<ILP>(S, s, el, xn, prev, mn));
+                    const V3 d = fsrc_in(s, el, xn);
+                    dbl[u][ge][0] = d.x; dbl[u][ge][1] = d.y; dbl[u][ge][2] = d.z;
+                } else {
+                    const DevSource& s = *srcv[u];
+                    gb_v[u][ge] = c_scale(gcomplex<VWP>(S, s, el, xn, kRoleView, st), fview<VWP>(S, s, el, xn, prev, mn));
+                    const V3 d = fsrc_out(s, el, xn);
+                    dbv[u][ge][0] = -d.x; dbv[u][ge][1] = -d.y; dbv[u][ge][2] = -d.z;
+                }
+            }
+            if (threadIdx.x == 0) {
+                const V3 d = funit(sub3(prev, xn));
+                geo[3] = d.x; geo[4] = d.y; geo[5] = d.z;
+                geo[6] = S.D[mn];
+                geo[7] = MT;
+            }
+            __syncthreads();
+            auto q2 = [&](const float* a, const float* c, int o) {
+                float r = 0.0f;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) { const float e = 0.5f * (a[i] + c[i]) - geo[o + i]; r = fmaf(e, e, r); }
+                return r;
+            };
+            const float D1 = S.D[m1], Db = geo[6];
+            const float a2 = S.k2 * (Db * q2(dbl[0][tl], dbv[1][tv], 3) + D1 * q2(d0v[0][tv], d0l[1][tl], 0));
+            const float a3 = S.k2 * (Db * q2(dbv[0][tv], dbl[1][tl], 3) + D1 * q2(d0l[0][tl], d0v[1][tv], 0));
+            const float a4 = S.k2 * (Db * q2(dbl[0][tl], dbl[1][tl], 3) + D1 * q2(d0v[0][tv], d0v[1][tv], 0));
+            const float2 c2 = c_mul(c_mulc(gb_l[0][tl], gb_v[1][tv]), c_mulc(g0v[0][tv], g0l[1][tl]));
+            const float2 c3 = c_mul(c_mulc(gb_v[0][tv], gb_l[1][tl]), c_mulc(g0l[0][tl], g0v[1][tv]));
+            const float2 c4 = c_mul(c_mulc(gb_l[0][tl], gb_l[1][tl]), c_mulc(g0v[0][tv], g0v[1][tv]));
+            const float ptk = S.k2 * geo[7];
+#pragma unroll
+            for (int tt = 0; tt < kCbTicks; ++tt) {
+                if (tt >= tn) break;
+                const float at = S.abs_ticks[t0 + tt];
+                const float e2 = __expf(-at * a2), e3 = __expf(-at * a3), e4 = __expf(-at * a4);
+                const float w = 0.5f * __expf(-at * ptk);
+                acc[tt].x = fmaf(w, c2.x * e2 + c3.x * e3 + c4.x * e4, acc[tt].x);
+                acc[tt].y = fmaf(w, c2.y * e2 + c3.y * e3 + c4.y * e4, acc[tt].y);
+            }
+            if (++window == 64) {   // FP32 windows folded into FP64 registers
+                window = 0;
+#pragma unroll
+                for (int tt = 0; tt < kCbTicks; ++tt) {
+                    accd[tt][0] += acc[tt].x; accd[tt][1] += acc[tt].y;
+                    acc[tt] = make_float2(0.f, 0.f);
+                }
+            }
+        }
+    }
+    const int l = l0 + tl, v = v0 + tv;
+    if (l >= Nl || v >= Nv) return;
+#pragma unroll
+    for (int tt = 0; tt < kCbTicks; ++tt) {
+        if (tt >= tn) break;
+        const size_t o = ((size_t)(t0 + tt) * Nv + v) * Nl + l;
+        atomicAdd(&P.V[o].x, accd[tt][0] + (double)acc[tt].x);
+        atomicAdd(&P.V[o].y, accd[tt][1] + (double)acc[tt].y);
+    }
+}
+
 }  // namespace
+
+int launch_cbs_corr(const DevScene& S, const CbsCorrParams& P, cudaStream_t stream)
+{
+    if (P.K <= 0) return SSTMC_NO_ERROR;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tchunks = (S.Nt + kCbTicks - 1) / kCbTicks;
+    const int tiles = ((S.src[0].n + kCbT - 1) / kCbT) * ((S.src[1].n + kCbT - 1) / kCbT) * tchunks;
+    const int want = std::max(1, (8 * sms + tiles - 1) / tiles);
+    CbsCorrParams Q = P;
+    Q.kchunk = std::max(1, (P.K + want - 1) / want);
+    const int ksplit = (P.K + Q.kchunk - 1) / Q.kchunk;
+    dim3 grid((S.src[0].n + kCbT - 1) / kCbT, (S.src[1].n + kCbT - 1) / kCbT, tchunks * ksplit);
+    const bool ip = S.src[0].type == SSTMC_SOURCE_POINT, vp = S.src[1].type == SSTMC_SOURCE_POINT;
+    if (ip) {
+        if (vp) cbs_corr_kernel<true, true><<<grid, 256, 0, stream>>>(S, Q);
+        else cbs_corr_kernel<true, false><<<grid, 256, 0, stream>>>(S, Q);
+    } else {
+        if (vp) cbs_corr_kernel<false, true><<<grid, 256, 0, stream>>>(S, Q);
+        else cbs_corr_kernel<false, false><<<grid, 256, 0, stream>>>(S, Q);
+    }
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
 
 size_t trace_smem_bytes(int Nt, int slots, int threads)
 {

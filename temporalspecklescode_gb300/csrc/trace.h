@@ -39,7 +39,20 @@ struct TraceParams {
     int real_rows;        // illum_kernel / view_kernel: a_ms and s_ms hold real floats [paths][Nt][Nl or Nv]
     int cbs;              // field CBS, reversed pass (trace_kernel): s_ms <- Gv0 [paths][Nt][Nv] (pass0),
                           // a_ms <- GlSum [paths][Nt][Nl]; v0 / vn then index illumination elements
+    float* p2;            // [paths] or null: the correlation sampler's second-point probability (CBS)
 };
+
+// Correlation-sampler CBS cross terms (trace.cu, cbs_corr_kernel): V +=
+// 0.5 (T2 + T3 + T4) over the paths [0, K) of a chunk.
+struct CbsCorrParams {
+    const float4* verts;
+    const uint32_t* counts;
+    const uint32_t* offsets;
+    const float* p2;      // [K]
+    double2* V;           // [Nt][Nv][Nl]
+    int K, kchunk;
+};
+int launch_cbs_corr(const DevScene& S, const CbsCorrParams& P, cudaStream_t stream);
 
 size_t trace_smem_bytes(int Nt, int slots, int threads);
 int launch_trace(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream);

@@ -172,6 +172,21 @@ def hg_table(g: float, n: int, dims: int, phase: float = 0.4) -> np.ndarray:
     return np.sqrt(pdf) * np.exp(1j * phase * th)
 
 
+def reciprocal_corr(make, cbs: bool = True):
+    """The correlation-sampler version of a reciprocal scene: u2 sources equal
+    to u1, Brownian D only (static scatterers, no drift)."""
+    cfg, dims = make(cbs=cbs)
+    cfg = dict(cfg)
+    cfg["illumination2"] = cfg["illumination"]
+    cfg["view2"] = cfg["view"]
+    nm = len(np.atleast_1d(cfg["medium"]["sigs"]))
+    zeros = [0.0] * nm
+    U = {"x": zeros, "y": zeros} if dims == 2 else {"x": zeros, "y": zeros, "z": zeros}
+    cfg["sampler"] = {"type": "TemporalCorrelationSampler", "t": [0.5, 1.5, 3.0],
+                      "D": [0.0] + [2e-3 * (i + 1) for i in range(nm - 1)], "U": U}
+    return cfg, dims
+
+
 def tabular_field_3d(batch_size=64, full_iteration=2):
     """3D field sampler, point sources, a tabular material next to an HG one,
     moving scatterers (per-tick positions)."""
@@ -217,6 +232,8 @@ def small_scenes():
         "speckle_2d_cbs": with_cbs(wl.speckle_2d(batch_size=48, full_iteration=2, n_dirs=6)),
         "reciprocal_far_3d_cbs": reciprocal_far_3d(),
         "reciprocal_point_2d_cbs": reciprocal_point_2d(),
+        "reciprocal_far_3d_corr_cbs": reciprocal_corr(reciprocal_far_3d),
+        "reciprocal_point_2d_corr_cbs": reciprocal_corr(reciprocal_point_2d),
         "tabular_field_3d": tabular_field_3d(),
         "tabular_corr_2d": tabular_corr_2d(),
         "tabular_corr_2d_drift": tabular_corr_2d(sym=False),

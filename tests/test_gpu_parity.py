@@ -157,7 +157,8 @@ def test_view_kernel_matches_fused_kernel(name, api, monkeypatch):
         assert err <= 2e-6, (name, k, err)
 
 
-@pytest.mark.parametrize("name", ["reciprocal_far_3d_cbs", "reciprocal_point_2d_cbs"])
+@pytest.mark.parametrize("name", ["reciprocal_far_3d_cbs", "reciprocal_point_2d_cbs",
+                                  "reciprocal_far_3d_corr_cbs", "reciprocal_point_2d_corr_cbs"])
 def test_cbs_reciprocity(name, api):
     """Field CBS on the GPU: with the views the reversed illuminations the field
     is symmetric in (l, v) (the reversed-path rows are the direct rows with the
@@ -169,11 +170,11 @@ def test_cbs_reciprocity(name, api):
     assert _sym_err(u[..., 0]) < 1e-5
 
 
-def test_cbs_correlation_refused(api):
-    """tracer.isCBS with the correlation sampler is refused with SSTMC_NOT_SUPPORTED."""
-    from tests.scenes import with_cbs
-    from temporalspecklescode_gb300 import workloads as wl
-    cfg, dims = with_cbs(wl.correlation_3d(batch_size=8, full_iteration=1, n_side=2, n_lags=1))
+def test_cbs_correlation_drift_refused(api):
+    """Correlation CBS is built for static scatterers: drift (U != 0) is refused
+    with SSTMC_NOT_SUPPORTED."""
+    from tests.scenes import with_cbs, corr_far_2d_drift
+    cfg, dims = with_cbs(corr_far_2d_drift())
     with pytest.raises(api.SstmcError) as ei:
         api.Scene(cfg, dims)
     assert ei.value.code == 5

@@ -156,8 +156,9 @@ def _sym_err(u):
     return np.linalg.norm(d) / np.linalg.norm(a)
 
 
-@pytest.mark.parametrize("make", ["reciprocal_far_3d", "reciprocal_point_2d"])
-def test_cbs_reciprocity(oracle, make):
+@pytest.mark.parametrize("make,corr", [("reciprocal_far_3d", False), ("reciprocal_point_2d", False),
+                                       ("reciprocal_far_3d", True), ("reciprocal_point_2d", True)])
+def test_cbs_reciprocity(oracle, make, corr):
     """Field CBS (NextEventEstimation.cuh:1212-1235, :1385-1391): with the views
     the reversed illuminations, each path's reversed-path product for (l=k, v=j)
     is its direct product for (l=j, v=k), so the rendered field is symmetric in
@@ -165,7 +166,10 @@ def test_cbs_reciprocity(oracle, make):
     from tests import scenes
     res = {}
     for cbs in (False, True):
-        cfg, dims = getattr(scenes, make)(cbs=cbs)
+        if corr:   # the correlation sampler's four cross terms (NextEventEstimation.cuh:1237-1378)
+            cfg, dims = scenes.reciprocal_corr(getattr(scenes, make), cbs=cbs)
+        else:
+            cfg, dims = getattr(scenes, make)(cbs=cbs)
         pc = cf.prepare(cfg, dims)
         u, it, st = oracle.render(pc, 21)
         res[cbs] = u[..., 0] if u.ndim == 4 else u
@@ -173,11 +177,11 @@ def test_cbs_reciprocity(oracle, make):
     assert _sym_err(res[False]) > 1e-3
 
 
-def test_cbs_correlation_not_supported(oracle):
-    """The correlation sampler's CBS cross terms are not built: both the oracle
-    and the library refuse the configuration."""
-    from tests.scenes import with_cbs
-    cfg, dims = with_cbs(wl.correlation_3d(batch_size=8, full_iteration=1, n_side=2, n_lags=1))
+def test_cbs_correlation_drift_not_supported(oracle):
+    """Correlation CBS is built for static scatterers: a drifting material (U != 0)
+    is refused by the oracle (and the library)."""
+    from tests.scenes import with_cbs, corr_far_2d_drift
+    cfg, dims = with_cbs(corr_far_2d_drift())
     pc = cf.prepare(cfg, dims)
     with pytest.raises(Exception):
         oracle.render(pc, 1)
