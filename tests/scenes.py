@@ -212,6 +212,18 @@ def tabular_corr_2d(sym: bool = True, batch_size=64, full_iteration=2):
     return cfg, dims
 
 
+def correlation_wide(geometric: bool = True, batch_size=24, full_iteration=2):
+    """The bench geometry at 100 x 100 sources and 12 lags: two tick chunks in
+    the single-scattering and view kernels (the second starts at tick 8), two
+    view passes, the 8-element-per-lane illumination variant; geometric=False
+    gives irregular lags (no tick chain)."""
+    cfg, dims = wl.correlation_3d(batch_size=batch_size, full_iteration=full_iteration, n_side=10, n_lags=12, dt=0.7)
+    cfg = dict(cfg)
+    if not geometric:
+        cfg["sampler"] = dict(cfg["sampler"], t=np.array([0.3, 0.9, 1.0, 2.2, 3.1, 3.3, 4.8, 5.0, 6.5, 7.7, 8.1, 9.9]))
+    return cfg, dims
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -234,6 +246,8 @@ def small_scenes():
         "reciprocal_point_2d_cbs": reciprocal_point_2d(),
         "reciprocal_far_3d_corr_cbs": reciprocal_corr(reciprocal_far_3d),
         "reciprocal_point_2d_corr_cbs": reciprocal_corr(reciprocal_point_2d),
+        "correlation_wide": correlation_wide(),
+        "correlation_wide_irregular": correlation_wide(geometric=False),
         "tabular_field_3d": tabular_field_3d(),
         "tabular_corr_2d": tabular_corr_2d(),
         "tabular_corr_2d_drift": tabular_corr_2d(sym=False),

@@ -136,7 +136,8 @@ def test_tensor_core_contraction_large_k_against_oracle(api, oracle):
 
 
 @pytest.mark.parametrize("name", ["correlation_64x64", "speckle_2d", "correlation_3d", "transmission_matrix_3d", "mcx_3d",
-                                  "homogeneous_3d", "point_2d_iso_field", "point_2d_iso_corr"])
+                                  "homogeneous_3d", "point_2d_iso_field", "point_2d_iso_corr",
+                                  "correlation_wide", "correlation_wide_irregular"])
 def test_view_kernel_matches_fused_kernel(name, api, monkeypatch):
     """The view-side kernel (default for static scenes) against the view loop
     of the fused trace kernel: identical voxel-step counts and per-path view
