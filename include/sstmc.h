@@ -135,7 +135,9 @@ typedef struct sstmc_config {
     const double* D;               /* [material count], non-negative */
     const double* U;               /* [material count x 3] (x, y, z) */
     int32_t is_temporal_amplitude; /* default 1 */
-    int32_t is_forced_inside_bin;  /* default 0; 1 is not supported */
+    int32_t is_forced_inside_bin;  /* default 0; field sampler: per vertex a tick drawn uniformly sits on the
+                                      sampled point and ticks that leave its grid cell weigh 0 (ignored by the
+                                      correlation sampler, TemporalSampler.cuh:439-534, 1637-1698) */
 
     /* config.tracer (MatlabInterface.cu:1374-1457) */
     int32_t is_cbs;                /* default 0; 1: coherent backscattering (correlation sampler: static scatterers) */

@@ -43,6 +43,7 @@ static inline void o_philox(const uint32_t key_in[2], const uint32_t ctr_in[4], 
 #define O_PURPOSE_WALK      1u
 #define O_PURPOSE_TEMPORAL  2u
 #define O_PURPOSE_WAVE      3u
+#define O_PURPOSE_FORCED    4u
 
 /* A sequential stream of 32-bit words for one (path, vertex, purpose):
  * block j = Philox(key = seed, counter = (j, a, b, tag)). */

@@ -88,6 +88,7 @@ typedef struct {
     double D[OM];
     float U_f[OM][3];
     int temporal_amp;
+    int forced_bin;       /* field sampler isForcedInsideBin */
     double lambda;
     unsigned P, full_iter;
 } o_scene;
@@ -234,7 +235,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     memset(S, 0, sizeof(*S));
     if (cfg->dims != 2 && cfg->dims != 3) return SSTMC_INVALID_CONFIG;
     int dims = S->dims = (int)cfg->dims;
-    if (cfg->is_forced_inside_bin) return SSTMC_NOT_SUPPORTED;
     if (cfg->batch_size == 0 || cfg->full_iteration == 0) return SSTMC_INVALID_CONFIG;
     if (!(cfg->lambda > 0)) return SSTMC_INVALID_CONFIG;
     S->P = cfg->batch_size; S->full_iter = cfg->full_iteration; S->lambda = cfg->lambda;
@@ -360,6 +360,8 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     if (!cfg->t || cfg->t_num == 0) return SSTMC_INVALID_CONFIG;
     S->correlation = cfg->sampler_type == SSTMC_SAMPLER_TEMPORAL_CORRELATION;
     S->cbs = cfg->is_cbs ? 1 : 0;
+    /* isForcedInsideBin exists for the field sampler only (MatlabInterface.cu:1245-1282) */
+    S->forced_bin = cfg->is_forced_inside_bin && !S->correlation;
     if (cfg->sampler_type != SSTMC_SAMPLER_TEMPORAL && !S->correlation) return SSTMC_INVALID_CONFIG;
     if (S->correlation) {
         if (S->src[2].type == SSTMC_SOURCE_NONE || S->src[3].type == SSTMC_SOURCE_NONE) return SSTMC_INVALID_CONFIG;
@@ -923,6 +925,7 @@ typedef struct {
     int* m;
     float* xi;
     float* xt;    /* cap*Nt*3 (field) */
+    float* w;     /* cap*Nt tick weights (field, isForcedInsideBin) */
 } o_verts;
 
 static int o_verts_grow(o_verts* V, int Nt)
@@ -940,17 +943,66 @@ static int o_verts_grow(o_verts* V, int Nt)
     float* xt = realloc(V->xt, (size_t)nc * Nt * 3 * sizeof(float));
     if (!xt) return SSTMC_ALLOCATION_ERROR;
     V->xt = xt;
+    float* w = realloc(V->w, (size_t)nc * Nt * sizeof(float));
+    if (!w) return SSTMC_ALLOCATION_ERROR;
+    V->w = w;
     V->cap = nc;
     return 0;
 }
 
-/* Per-tick positions of a vertex (field sampler): TemporalSampler.cuh:376-436, 540-647, 778-937. */
-static void o_temporal_positions(const o_scene* S, uint64_t seed, uint32_t pid, uint32_t b, const float x[3], int m, float* xt)
+/* Cell along one axis as Simulation.cuh:325-367 returns it: ax[c] <= x < ax[c+1],
+ * 0 below the first edge, n-1 at or beyond the last edge. */
+static int o_edge_bin(const float* ax, int n, float x)
+{
+    int c = 0;
+    while (c < n && ax[c] <= x) ++c;
+    return c > 0 ? c - 1 : 0;
+}
+
+/* isSameBinKernel (HeterogeneousMedium.cuh:708-735) */
+static int o_same_bin(const o_scene* S, const float x[3], const float p[3])
+{
+    if (!o_inside(S, p)) return 0;
+    for (int a = 0; a < S->dims; ++a)
+        if (o_edge_bin(S->ax[a], S->n[a], x[a]) != o_edge_bin(S->ax[a], S->n[a], p[a])) return 0;
+    return 1;
+}
+
+/* isForcedInsideBin (TemporalSampler.cuh:439-534 getMaterialNumTemporal and
+ * shiftRandomSampledIndex, :1637-1698 pathContribution): tick r = ceil(u Nt) - 1
+ * drawn per vertex is moved onto the sampled point x (every tick shifted by
+ * x - xt[r], read before any tick moves); ticks outside x's grid cell weigh 0,
+ * with every tick beyond them on the same side of r (tick order). */
+static int o_forced_inside_bin(const o_scene* S, uint64_t seed, uint32_t pid, uint32_t b, const float x[3],
+                               float* xt, float* w)
 {
     int Nt = S->Nt;
+    o_stream rs;
+    o_stream_init(&rs, seed, pid, b, O_PURPOSE_FORCED);
+    uint64_t k = (uint64_t)(o_next_u32(&rs) >> 8) + 1u;   /* u = k 2^-24 */
+    int r = (int)((k * (uint64_t)Nt - 1u) >> 24);
+    float sh[3] = { x[0] - xt[3 * r], x[1] - xt[3 * r + 1], x[2] - xt[3 * r + 2] };
+    int neg = -1, pos = Nt;
+    for (int t = 0; t < Nt; ++t) {
+        for (int i = 0; i < S->dims; ++i) xt[3 * t + i] = xt[3 * t + i] + sh[i];
+        if (!o_same_bin(S, x, xt + 3 * t)) {
+            if (t <= r) neg = t;
+            else if (pos == Nt) pos = t;
+        }
+    }
+    for (int t = 0; t < Nt; ++t) w[t] = (t > neg && t < pos) ? 1.0f : 0.0f;
+    return r;
+}
+
+/* Per-tick positions of a vertex (field sampler): TemporalSampler.cuh:376-436, 540-647, 778-937. */
+static int o_temporal_positions(const o_scene* S, uint64_t seed, uint32_t pid, uint32_t b, const float x[3], int m,
+                                float* xt, float* w)
+{
+    int Nt = S->Nt;
+    for (int t = 0; t < Nt; ++t) w[t] = 1.0f;
     if (!S->moving[m]) {
         for (int t = 0; t < Nt; ++t) { xt[3 * t] = x[0]; xt[3 * t + 1] = x[1]; xt[3 * t + 2] = x[2]; }
-        return;
+        return -1;
     }
     float cur[3] = { 0, 0, 0 };
     float buf[3];
@@ -977,6 +1029,7 @@ static void o_temporal_positions(const o_scene* S, uint64_t seed, uint32_t pid, 
         buf[0] = cur[0]; buf[1] = cur[1]; buf[2] = cur[2];
         xt[3 * t] = buf[0]; xt[3 * t + 1] = buf[1]; xt[3 * t + 2] = buf[2];
     }
+    return S->forced_bin ? o_forced_inside_bin(S, seed, pid, b, x, xt, w) : -1;
 }
 
 /* Walk one path: vertices x_1..x_B.  Returns error code; misses counted. */
@@ -1001,7 +1054,7 @@ static int o_walk(const o_scene* S, uint64_t seed, uint32_t pid, int u1side, o_v
     if (V->cap < 1 && o_verts_grow(V, S->Nt)) return SSTMC_ALLOCATION_ERROR;
     V->x[0] = x1[0]; V->x[1] = x1[1]; V->x[2] = x1[2]; V->m[0] = m1;
     V->xi[0] = S->correlation ? 0.0f : o_uniform(&rs);
-    if (!S->correlation) o_temporal_positions(S, seed, pid, 1u, x1, m1, V->xt);
+    if (!S->correlation) o_temporal_positions(S, seed, pid, 1u, x1, m1, V->xt, V->w);
     V->B = 1;
     float prev[3] = { x0[0], x0[1], x0[2] };
     for (uint32_t b = 1; ; ++b) {
@@ -1022,7 +1075,8 @@ static int o_walk(const o_scene* S, uint64_t seed, uint32_t pid, int u1side, o_v
         V->x[3 * b] = xn[0]; V->x[3 * b + 1] = xn[1]; V->x[3 * b + 2] = xn[2];
         V->m[b] = mn;
         V->xi[b] = S->correlation ? 0.0f : o_uniform(&rs);
-        if (!S->correlation) o_temporal_positions(S, seed, pid, b + 1, xn, mn, V->xt + (size_t)b * S->Nt * 3);
+        if (!S->correlation)
+            o_temporal_positions(S, seed, pid, b + 1, xn, mn, V->xt + (size_t)b * S->Nt * 3, V->w + (size_t)b * S->Nt);
         V->B = (int)b + 1;
     }
     return 0;
@@ -1178,7 +1232,7 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
             const float* x1t = V->xt + 3 * t;
             for (int l = 0; l < Nl; ++l) {
                 W->gl1[t * Nl + l] = o_gm(S, W->memo[0], il, l, x1t, 0, steps);
-                W->a_ss[t * Nl + l] = oc_scale(oc_mul(W->gl1[t * Nl + l], e1), 1.0 / sq1);
+                W->a_ss[t * Nl + l] = oc_scale(oc_mul(W->gl1[t * Nl + l], e1), V->w[t] / sq1);
             }
             for (int v = 0; v < Nv; ++v) W->b_ss[t * Nv + v] = o_gm(S, W->memo[1], vw, v, x1t, 1, steps);
         }
@@ -1225,6 +1279,8 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
                 const float* pa = S->temporal_amp ? xb : V->x + 3 * b;
                 const float* pb = S->temporal_amp ? xa : V->x + 3 * (b - 1);
                 oc ph; o_cexp2pi(L / S->lambda + (double)V->xi[b], &ph.re, &ph.im);
+                /* the tick weight of x_b multiplies its path contribution */
+                ph = oc_scale(ph, V->w[(size_t)b * Nt + t]);
                 for (int v = 0; v < Nv; ++v) {
                     oc g = o_gm(S, W->memo[1], vw, v, xb, 1, steps);
                     oc f = o_f3(S, vw, v, pa, pb, V->m[b], 1);
@@ -1461,7 +1517,7 @@ int32_t oracle_render(const sstmc_config* cfg, uint64_t seed, uint32_t first_wav
             sst[4] += (uint64_t)misses;
         }
         o_work_free(&W);
-        free(V.x); free(V.m); free(V.xi); free(V.xt);
+        free(V.x); free(V.m); free(V.xi); free(V.xt); free(V.w);
     }
     for (int t = 0; t < nthr; ++t) if (errs[t]) { err = errs[t]; break; }
     if (!err) {
@@ -1521,7 +1577,7 @@ int32_t oracle_trace_paths(const sstmc_config* cfg, uint64_t seed, uint32_t firs
         }
     }
     o_work_free(&W);
-    free(V.x); free(V.m); free(V.xi); free(V.xt);
+    free(V.x); free(V.m); free(V.xi); free(V.xt); free(V.w);
     o_free_scene(&S);
     return err;
 }
@@ -1579,6 +1635,20 @@ int32_t oracle_sample_cos(const sstmc_config* cfg, int32_t m, uint64_t seed, uin
             o_sample_direction(&S, m, din, &rs, nd);
             out[i] = S.dims == 2 ? nd[1] : nd[2];
         }
+    }
+    o_free_scene(&S);
+    return err;
+}
+
+int32_t oracle_tick_positions(const sstmc_config* cfg, uint64_t seed, uint32_t pid, uint32_t b, const float* x,
+                              int32_t m, float* xt, float* w, int32_t* r)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (!err && (S.correlation || m < 0 || m >= OM)) err = SSTMC_INVALID_CONFIG;
+    if (!err) {
+        float xx[3] = { x[0], x[1], S.dims == 3 ? x[2] : 0.0f };
+        *r = o_temporal_positions(&S, seed, pid, b, xx, m, xt, w);
     }
     o_free_scene(&S);
     return err;

@@ -49,6 +49,11 @@ int32_t oracle_phase(const sstmc_config* cfg, int32_t m, double c, double* amp, 
 int32_t oracle_amplitude(const sstmc_config* cfg, int32_t m, double c, double* re, double* im);
 /* Sample `n` scattering cosines of material m (FP32 walk arithmetic). */
 int32_t oracle_sample_cos(const sstmc_config* cfg, int32_t m, uint64_t seed, uint32_t n, float* out);
+/* Field sampler: per-tick positions xt [Nt x 3] and tick weights w [Nt] of a
+ * vertex at x of material m (path pid, vertex b >= 1); *r = the tick forced onto
+ * x (isForcedInsideBin), -1 when there is none. */
+int32_t oracle_tick_positions(const sstmc_config* cfg, uint64_t seed, uint32_t pid, uint32_t b, const float* x,
+                              int32_t m, float* xt, float* w, int32_t* r);
 /* Portable FP32 math of the decision path, for bit-level tests. */
 float oracle_logf(float x);
 void oracle_sincospif(float x, float* s, float* c);

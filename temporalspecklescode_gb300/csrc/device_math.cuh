@@ -25,6 +25,7 @@ __device__ __forceinline__ float fsq(float a) { return __fsqrt_rn(a); }
 constexpr uint32_t kPurposeWalk = 1u;
 constexpr uint32_t kPurposeTemporal = 2u;
 constexpr uint32_t kPurposeWave = 3u;
+constexpr uint32_t kPurposeForcedBin = 4u;
 
 __device__ __forceinline__ void philox4x32_10(uint32_t k0, uint32_t k1, uint32_t c0, uint32_t c1,
                                               uint32_t c2, uint32_t c3, uint32_t out[4])

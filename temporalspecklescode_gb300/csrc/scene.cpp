@@ -170,7 +170,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     auto fail = [&](int code, const char* msg) { if (why) *why = msg; return code; };
     if (cfg->dims != 2 && cfg->dims != 3) return fail(SSTMC_INVALID_CONFIG, "dims must be 2 or 3");
     const int dims = S->dims = (int)cfg->dims;
-    if (cfg->is_forced_inside_bin) return fail(SSTMC_NOT_SUPPORTED, "sampler.isForcedInsideBin is not supported");
     if (cfg->batch_size == 0 || cfg->full_iteration == 0 || cfg->renderings_num == 0)
         return fail(SSTMC_INVALID_CONFIG, "batchSize, fullIteration and renderingsNum must be positive");
     if (!(cfg->lambda > 0)) return fail(SSTMC_INVALID_CONFIG, "lambda must be positive");
@@ -345,6 +344,9 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     // and real phase functions
     if (cfg->is_cbs && S->correlation && (!D.all_static_corr || D.has_tabular))
         return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS with the TemporalCorrelationSampler needs static scatterers (U = 0) and no tabular material");
+    // isForcedInsideBin belongs to the field sampler; the correlation sampler has no
+    // such option and the reference ignores the field there (MatlabInterface.cu:1245-1282)
+    D.forced_bin = (cfg->is_forced_inside_bin && !S->correlation) ? 1 : 0;
     D.ticks_geometric = S->abs_ticks[0] > 0.0f;
     for (int t = 0; t < Nt; ++t)
         if (S->abs_ticks[t] != (float)(t + 1) * S->abs_ticks[0]) D.ticks_geometric = 0;

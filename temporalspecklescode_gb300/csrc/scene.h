@@ -49,6 +49,7 @@ struct DevScene {
     int single, grid_m0;          // single-cell medium and its material
     int all_static_corr;          // no material drifts (U == 0 everywhere)
     int ticks_geometric;          // |t_k| == (k + 1) |t_0| for every tick
+    int forced_bin;               // field sampler isForcedInsideBin: per-vertex tick weights in {0, 1}
     uint32_t P;
     int n[3];
     const float* ax[3];

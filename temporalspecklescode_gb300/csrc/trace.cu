@@ -25,16 +25,82 @@ namespace sstmc {
 
 namespace {
 
+__device__ __forceinline__ V3 tick_pos(const float* buf, int t) { return V3{ buf[3 * t], buf[3 * t + 1], buf[3 * t + 2] }; }
+
+// Cell index along one axis as the reference's lookup returns it
+// (Simulation.cuh:325-367): ax[c] <= x < ax[c+1]; 0 below the first edge and
+// n-1 (one past the last cell) at or beyond the last edge.
+__device__ __forceinline__ int edge_bin(const float* ax, int n, float x)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(ax + mid) <= x) lo = mid + 1; else hi = mid;
+    }
+    return lo > 0 ? lo - 1 : 0;
+}
+
+// isSameBinKernel (HeterogeneousMedium.cuh:708-735): p inside the box and in
+// the grid cell of x
+__device__ __forceinline__ bool same_bin(const DevScene& S, const V3& x, const V3& p)
+{
+    if (!inside(S, p)) return false;
+    bool same = edge_bin(S.ax[0], S.n[0], x.x) == edge_bin(S.ax[0], S.n[0], p.x)
+             && edge_bin(S.ax[1], S.n[1], x.y) == edge_bin(S.ax[1], S.n[1], p.y);
+    if (S.dims == 3) same = same && edge_bin(S.ax[2], S.n[2], x.z) == edge_bin(S.ax[2], S.n[2], p.z);
+    return same;
+}
+
+// isForcedInsideBin (TemporalSampler.cuh:439-534, 1637-1698): a tick r drawn
+// uniformly per vertex (ceil(u Nt) - 1) is moved onto the sampled point by
+// shifting the whole tick chain by x - x_t[r]; a tick whose position leaves
+// the sampled point's grid cell weighs 0, and so does every tick beyond it on
+// the same side of r (in tick order).  The weights go to buf[3 Nt + t].  The
+// reference's shift kernel reads x_t[r] while other threads of the path add
+// the shift to it (an unordered read); the shift here is the intended one,
+// taken from x_t[r] before any tick moves.
+__device__ void forced_inside_bin(const DevScene& S, uint64_t seed, uint32_t pid, uint32_t b,
+                                  const V3& x, float* buf, int lane)
+{
+    const int Nt = S.Nt;
+    float* w = buf + 3 * Nt;
+    Stream rs;
+    rs.init(seed, pid, b, kPurposeForcedBin);
+    const uint32_t k = (rs.next() >> 8) + 1u;   // u = k 2^-24 in (0, 1]
+    const int r = (int)(((uint64_t)k * (uint32_t)Nt - 1u) >> 24);
+    const float s0 = __fsub_rn(x.x, buf[3 * r]), s1 = __fsub_rn(x.y, buf[3 * r + 1]), s2 = __fsub_rn(x.z, buf[3 * r + 2]);
+    __syncwarp();
+    int neg = -1, pos = Nt;
+    for (int t = lane; t < Nt; t += 32) {
+        buf[3 * t] = fa(buf[3 * t], s0);
+        buf[3 * t + 1] = fa(buf[3 * t + 1], s1);
+        if (S.dims == 3) buf[3 * t + 2] = fa(buf[3 * t + 2], s2);
+        if (!same_bin(S, x, tick_pos(buf, t))) {
+            if (t <= r) neg = max(neg, t);
+            else pos = min(pos, t);
+        }
+    }
+    neg = __reduce_max_sync(0xffffffffu, neg);
+    pos = __reduce_min_sync(0xffffffffu, pos);
+    for (int t = lane; t < Nt; t += 32) w[t] = (t > neg && t < pos) ? 1.0f : 0.0f;
+    __syncwarp();
+}
+
 // Per-tick positions of a vertex of the field sampler (TemporalSampler.cuh:376-436,
 // 540-647, 778-937): Brownian displacement N(0, 2 dims D |dt|) along a random
 // direction plus dt U per sorted tick, cumulated outward from the mean tick.
-// Warp-cooperative; buf holds Nt*3 floats in output-tick order.
+// Warp-cooperative; buf holds Nt*3 floats in output-tick order, then (with
+// isForcedInsideBin) the Nt tick weights.
 __device__ void temporal_positions(const DevScene& S, uint64_t seed, uint32_t pid, uint32_t b,
                                    const V3& x, int m, float* buf, int lane)
 {
     const int Nt = S.Nt;
     if (!S.moving[m]) {
-        for (int t = lane; t < Nt; t += 32) { buf[3 * t] = x.x; buf[3 * t + 1] = x.y; buf[3 * t + 2] = x.z; }
+        // every tick sits on x: the forced tick does too, and all weights are 1
+        for (int t = lane; t < Nt; t += 32) {
+            buf[3 * t] = x.x; buf[3 * t + 1] = x.y; buf[3 * t + 2] = x.z;
+            if (S.forced_bin) buf[3 * Nt + t] = 1.0f;
+        }
         __syncwarp();
         return;
     }
@@ -75,9 +141,14 @@ __device__ void temporal_positions(const DevScene& S, uint64_t seed, uint32_t pi
         }
     }
     __syncwarp();
+    if (S.forced_bin) forced_inside_bin(S, seed, pid, b, x, buf, lane);
 }
 
-__device__ __forceinline__ V3 tick_pos(const float* buf, int t) { return V3{ buf[3 * t], buf[3 * t + 1], buf[3 * t + 2] }; }
+// weight of tick t of a vertex: 1, or the isForcedInsideBin weight
+__device__ __forceinline__ float tick_w(const DevScene& S, const float* buf, int t)
+{
+    return S.forced_bin ? buf[3 * S.Nt + t] : 1.0f;
+}
 
 __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, int lane)
 {
@@ -240,9 +311,9 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     double* Ls = smem_d + (size_t)wib * Nt;
     float2* accs = reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)wib * T.slots * 32 + lane;
     float* fbase = reinterpret_cast<float*>(reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)nwb * T.slots * 32);
-    float* bufA = fbase + (size_t)wib * 6 * Nt;
-    float* bufB = bufA + 3 * Nt;
-    float* tk_abs = fbase + (size_t)nwb * 6 * Nt;   // block-wide copies of |t| and t
+    float* bufA = fbase + (size_t)wib * 8 * Nt;
+    float* bufB = bufA + 4 * Nt;
+    float* tk_abs = fbase + (size_t)nwb * 8 * Nt;   // block-wide copies of |t| and t
     float* tk_raw = tk_abs + Nt;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) { tk_abs[t] = S.abs_ticks[t]; tk_raw[t] = S.ticks_f[t]; }
     __syncthreads();
@@ -356,7 +427,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                         else g = gcomplex<ILP>(S, il, l, tick_pos(xtc, t), kRoleIllum, steps);
                         const size_t o = ((size_t)q * Nt + t) * Nl + l;
                         T.a_ms[o] = g;
-                        T.a_ss[o] = c_scale(c_mul(g, e1), p1inv);
+                        T.a_ss[o] = c_scale(c_mul(g, e1), p1inv * tick_w(S, xtc, t));
                     }
                 }
                 for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
@@ -614,9 +685,10 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                         if (tabn) {
                             const float2 f = stf ? fsc : fxc(v, tick_pos(xtn, t), tick_pos(xtc, t));
                             c = c_mul(c_mul(g, unit_phase(fr)), f);
+                            if (S.forced_bin) c = c_scale(c, tick_w(S, xtn, t));
                         } else {
                             const float f = stf ? fs : fx(v, tick_pos(xtn, t), tick_pos(xtc, t), mn);
-                            c = c_scale(c_mul(g, unit_phase(fr)), f);
+                            c = c_scale(c_mul(g, unit_phase(fr)), f * tick_w(S, xtn, t));
                         }
                         float2* a = accs + 32 * (j * T.tpl + k);
                         const float2 av = *a;
@@ -849,7 +921,7 @@ size_t trace_smem_bytes(int Nt, int slots, int threads)
 {
     const int warps = threads / 32;
     return (size_t)warps * Nt * sizeof(double) + (size_t)warps * slots * 32 * sizeof(float2)
-         + (size_t)warps * 6 * Nt * sizeof(float) + 2 * (size_t)Nt * sizeof(float);
+         + (size_t)warps * 8 * Nt * sizeof(float) + 2 * (size_t)Nt * sizeof(float);
 }
 
 using TraceFn = void (*)(DevScene, TraceParams);

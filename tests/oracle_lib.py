@@ -45,6 +45,9 @@ class Oracle:
         L.oracle_logf.argtypes = [C.c_float]
         L.oracle_logf.restype = C.c_float
         L.oracle_sincospif.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.oracle_tick_positions.argtypes = [C.POINTER(cf.SstmcConfig), C.c_uint64, C.c_uint32, C.c_uint32,
+                                            C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
+                                            C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
 
     def render(self, pc: cf.PreparedConfig, seed: int, first_wave: int = 0, waves: int | None = None, threads: int = 0):
@@ -97,6 +100,19 @@ class Oracle:
         e = self.lib.oracle_sample_cos(pc.ptr(), m, C.c_uint64(seed), C.c_uint32(n), out.ctypes.data_as(C.POINTER(C.c_float)))
         assert e == 0
         return out
+
+    def tick_positions(self, pc: cf.PreparedConfig, seed: int, pid: int, b: int, x, m: int):
+        """Field sampler: (xt [Nt, 3], weights [Nt], forced tick or -1) of one vertex."""
+        nt = int(pc.struct.t_num)
+        xt = np.zeros((nt, 3), dtype=np.float32)
+        w = np.zeros(nt, dtype=np.float32)
+        r = C.c_int32()
+        xx = np.asarray(list(x) + [0.0] * (3 - len(x)), dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        e = self.lib.oracle_tick_positions(pc.ptr(), C.c_uint64(seed), C.c_uint32(pid), C.c_uint32(b),
+                                           xx.ctypes.data_as(fp), m, xt.ctypes.data_as(fp), w.ctypes.data_as(fp), C.byref(r))
+        assert e == 0, e
+        return xt, w, r.value
 
     def logf(self, x: float) -> float:
         return self.lib.oracle_logf(x)

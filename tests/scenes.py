@@ -224,6 +224,37 @@ def correlation_wide(geometric: bool = True, batch_size=24, full_iteration=2):
     return cfg, dims
 
 
+def forced_bin_3d(batch_size=64, full_iteration=2):
+    """3D field sampler with isForcedInsideBin: the point-source scene with
+    motion large enough (Brownian D and drift U against 4-5 unit cells) that
+    about half of the ticks leave their vertex's cell."""
+    cfg, dims = field_point_3d(batch_size=batch_size, full_iteration=full_iteration)
+    cfg["sampler"]["D"] = [0.0, 0.08, 0.2]
+    cfg["sampler"]["U"] = {"x": [0.0, 0.6, 0.0], "y": [0.0, 0.0, -0.4], "z": [0.0, 0.2, 0.0]}
+    cfg["sampler"]["isForcedInsideBin"] = True
+    return cfg, dims
+
+
+def forced_bin_2d(batch_size=64, full_iteration=2):
+    """2D field sampler with isForcedInsideBin, far-field sources, a 4 x 3 grid,
+    one static material next to a moving one, ticks on both sides of zero."""
+    d = wl._farfield_fan(6)
+    d2 = wl._farfield_fan(5, 0.3)
+    grid = np.array([[1, 2, 1], [2, 2, 1], [1, 2, 2], [2, 1, 1]], dtype=np.uint32)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.9, "seed": 11},
+        "scattering": {"type": ["HG", "HG", "HG"], "amplitudeFunction": [0.3, 0.7, 0.5]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-6.0, -3.0, 0.0, 2.5, 6.0], "yAxis": [-5.0, -1.0, 2.0, 5.0],
+                   "materialGrid": grid, "sigs": [0.0, 0.7, 1.2], "siga": [0.0, 0.02, 0.0]},
+        "illumination": {"type": "FarField", "direction": d}, "view": {"type": "FarField", "direction": d2},
+        "sampler": {"type": "TemporalSampler", "t": [-2.0, -1.0, 0.0, 1.0, 2.0, 3.5],
+                    "D": [0.0, 0.0, 0.15], "U": {"x": [0.0, 0.0, 0.5], "y": [0.0, 0.0, -0.3]},
+                    "isForcedInsideBin": True},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -252,4 +283,7 @@ def small_scenes():
         "tabular_corr_2d": tabular_corr_2d(),
         "tabular_corr_2d_drift": tabular_corr_2d(sym=False),
         "tabular_field_3d_cbs": with_cbs(tabular_field_3d()),
+        "forced_bin_3d": forced_bin_3d(),
+        "forced_bin_2d": forced_bin_2d(),
+        "forced_bin_2d_cbs": with_cbs(forced_bin_2d()),
     }

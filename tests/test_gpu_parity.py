@@ -198,3 +198,18 @@ def test_wavelength_vector_renders_each_wavelength(api):
         assert np.array_equal(it, itw)
         assert rel_fro(u[:, :, w], uw) <= 1e-12
     assert rel_fro(u[:, :, 0], u[:, :, 1]) > 1e-3   # the phases differ
+
+
+@pytest.mark.parametrize("make", ["static", "correlation"])
+def test_forced_inside_bin_neutral_cases(api, make):
+    """isForcedInsideBin changes nothing, bit for bit, where the reference's
+    option has no effect: every material static (all ticks on the sampled
+    point), or the correlation sampler (which has no such option)."""
+    from tests import scenes
+    cfg, dims = scenes.field_point_3d(moving=False) if make == "static" else scenes.corr_far_2d_drift()
+    forced = dict(cfg, sampler=dict(cfg["sampler"], isForcedInsideBin=True))
+    with api.Scene(cfg, dims) as s:
+        u0, _ = s.render(seed=31)
+    with api.Scene(forced, dims) as s:
+        u1, _ = s.render(seed=31)
+    assert np.array_equal(u0, u1)

@@ -241,3 +241,78 @@ def test_tabular_sampler_matches_table(oracle, dims, g):
     pc = _tabular_cfg(dims, hg_table(g, 2001, dims))
     c = np.asarray(oracle.sample_cos(pc, 0, 3, 200000), dtype=np.float64)
     assert abs(c.mean() - g) < 0.01
+
+
+def _cell(ax, v):
+    """Cell index as Simulation.cuh:325-367 returns it (n-1 at or past the last edge)."""
+    return max(int(np.searchsorted(np.asarray(ax, dtype=np.float32), np.float32(v), side="right")) - 1, 0)
+
+
+@pytest.mark.parametrize("make", ["forced_bin_3d", "forced_bin_2d"])
+def test_forced_inside_bin_restatement(oracle, make):
+    """isForcedInsideBin (TemporalSampler.cuh:439-534, 1637-1698), restated
+    independently here: the drawn tick r sits on the sampled point, the tick
+    chain is the plain one shifted by x - xt[r], and the weights are 1 exactly on
+    the ticks between the last tick <= r and the first tick > r that leave the
+    sampled point's grid cell (or the box)."""
+    from tests import scenes
+    cfg, dims = getattr(scenes, make)()
+    plain = dict(cfg, sampler=dict(cfg["sampler"], isForcedInsideBin=False))
+    pf, pp = cf.prepare(cfg, dims), cf.prepare(plain, dims)
+    med = cfg["medium"]
+    axes = [med["xAxis"], med["yAxis"]] + ([med["zAxis"]] if dims == 3 else [])
+    lo = np.array([a[0] for a in axes], dtype=np.float32)
+    hi = np.array([a[-1] for a in axes], dtype=np.float32)
+    rng = np.random.default_rng(4)
+    zeros = ones = 0
+    for pid in range(300):
+        x = np.float32(rng.uniform(lo, hi))
+        b = int(rng.integers(1, 6))
+        xf, w, r = oracle.tick_positions(pf, 9, pid, b, x, 2)
+        xp, wp, rp = oracle.tick_positions(pp, 9, pid, b, x, 2)
+        assert rp == -1 and np.all(wp == 1.0)
+        assert 0 <= r < len(w)
+        shift = (x - xp[r, :dims]).astype(np.float32)
+        assert np.array_equal(xf[:, :dims], (xp[:, :dims] + shift).astype(np.float32))
+        same = [bool(np.all(p[:dims] >= lo) and np.all(p[:dims] <= hi))
+                and all(_cell(axes[a], p[a]) == _cell(axes[a], x[a]) for a in range(dims)) for p in xf]
+        neg = max([t for t in range(len(w)) if t <= r and not same[t]], default=-1)
+        pos = min([t for t in range(len(w)) if t > r and not same[t]], default=len(w))
+        want = np.array([1.0 if neg < t < pos else 0.0 for t in range(len(w))], dtype=np.float32)
+        assert np.array_equal(w, want)
+        zeros += int((w == 0).sum()); ones += int((w == 1).sum())
+    assert zeros > 0.2 * (zeros + ones) and ones > 0.2 * (zeros + ones)
+
+
+def test_forced_inside_bin_without_motion_changes_nothing(oracle):
+    """With every material static all ticks sit on the sampled point: forcing
+    the drawn tick there moves nothing and no tick leaves the cell."""
+    from tests import scenes
+    cfg, dims = scenes.field_point_3d(moving=False)
+    forced = dict(cfg, sampler=dict(cfg["sampler"], isForcedInsideBin=True))
+    u0 = oracle.render(cf.prepare(cfg, dims), 2)[0]
+    u1 = oracle.render(cf.prepare(forced, dims), 2)[0]
+    assert np.array_equal(u0, u1)
+
+
+def test_forced_inside_bin_ignored_by_correlation_sampler(oracle):
+    """The correlation sampler has no isForcedInsideBin (MatlabInterface.cu:1245-1282):
+    the field is accepted and changes nothing."""
+    from tests import scenes
+    cfg, dims = scenes.corr_far_2d_drift()
+    forced = dict(cfg, sampler=dict(cfg["sampler"], isForcedInsideBin=True))
+    u0 = oracle.render(cf.prepare(cfg, dims), 2)[0]
+    u1 = oracle.render(cf.prepare(forced, dims), 2)[0]
+    assert np.array_equal(u0, u1)
+
+
+def test_forced_inside_bin_weights_the_render(oracle):
+    """With motion the forced render differs from the plain one, and zeroed
+    ticks lower the summed intensity."""
+    from tests import scenes
+    cfg, dims = scenes.forced_bin_2d()
+    plain = dict(cfg, sampler=dict(cfg["sampler"], isForcedInsideBin=False))
+    uf = oracle.render(cf.prepare(cfg, dims), 2)[0]
+    up = oracle.render(cf.prepare(plain, dims), 2)[0]
+    assert not np.allclose(uf, up)
+    assert np.abs(uf).sum() < np.abs(up).sum()
