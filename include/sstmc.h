@@ -60,7 +60,7 @@ extern "C" {
 #define SSTMC_SCATTERING_ISOTROPIC        1
 #define SSTMC_SCATTERING_TABULAR          2   /* table of the complex amplitude (tabular_n / tabular_f) */
 #define SSTMC_SCATTERING_HENYEY_GREENSTEIN 3
-#define SSTMC_SCATTERING_VMF_MIXTURE      4   /* not supported by this build */
+#define SSTMC_SCATTERING_VMF_MIXTURE      4   /* von Mises-Fisher mixture (vmf_n / vmf_mu / vmf_c / vmf_alpha) */
 
 /* config.medium.type (MatlabInterface.cu:896, 942) */
 #define SSTMC_MEDIUM_HETEROGENEOUS 0
@@ -153,6 +153,19 @@ typedef struct sstmc_config {
      * scene creation. */
     const uint32_t* tabular_n;     /* [scattering_num] or NULL */
     const double* tabular_f;       /* [2 x sum(tabular_n)] or NULL */
+
+    /* von Mises-Fisher mixture scattering (Scattering.cuh:613-884,
+     * MatlabInterface.cu:827-868): per material the number of mixture
+     * components (0 for the other types), and the components' mixtureMu,
+     * mixtureC and mixtureAlpha concatenated in material order.  The
+     * amplitude is sum_k alpha_k exp(mu_k cos(theta) + C_k) in 3D; in 2D the
+     * reference scatters a vMF material isotropically.  Refused with
+     * NOT_SUPPORTED: every material isotropic (|g| < 1e-4, all |mu| <= 1e-4)
+     * with a vMF material among them. */
+    const uint32_t* vmf_n;         /* [scattering_num] or NULL */
+    const double* vmf_mu;          /* [sum(vmf_n)] or NULL */
+    const double* vmf_c;           /* [sum(vmf_n)] or NULL */
+    const double* vmf_alpha;       /* [sum(vmf_n)] or NULL, each >= 0 */
 } sstmc_config;
 
 typedef struct sstmc_scene sstmc_scene;

@@ -64,6 +64,13 @@ typedef struct {
     double* tab_f;        /* normalised amplitude (re, im) */
     double* tab_pdf;      /* evaluation pdf */
     float* tab_cos;       /* cos(icdf) of the sampler */
+    /* vMF mixtures (3D): per material components and offsets; components
+     * (mu, C + log alpha); pairs (kappa, weight, log normalisation); the
+     * sampler's pairs (exclusive cdf, kappa, exp(-2 |kappa|)) in FP32 */
+    int vmf_n[OM], vmf_off[OM], vmf_poff[OM];
+    double* vmf_mc;
+    double* vmf_pd;
+    float* vmf_pf;
     double gup[OM], gd1[OM], gd2[OM];
     int iso_all;
     /* medium */
@@ -103,6 +110,7 @@ static void o_free_scene(o_scene* S)
     for (int a = 0; a < 3; ++a) { free(S->ax[a]); free(S->axd[a]); }
     free(S->grid); free(S->ticks); free(S->ticks_f); free(S->disp_scale); free(S->disp_u);
     free(S->tab_f); free(S->tab_pdf); free(S->tab_cos);
+    free(S->vmf_mc); free(S->vmf_pd); free(S->vmf_pf);
 }
 
 /* Far-field tables: FarField.cuh:71-127 (fillBuffers) in double, stored as float. */
@@ -230,6 +238,41 @@ static int o_tabular(const double* f, uint32_t N, int dims, double* fn, double* 
     return 0;
 }
 
+/* vMFnormalizationLog in 3D, SpecialFunctions.cuh:187-203 (kappa below 1e-12,
+ * negative ones included, takes the isotropic value). */
+static double o_vmf_log_norm(double x)
+{
+    if (x < 1e-12) return -log(4.0 * O_PI);
+    if (x < 5.0) return log(x) - log(4.0 * O_PI * sinh(x));
+    return log(x) - log(2.0 * O_PI) - x;
+}
+
+/* Tables of one 3D vMF mixture, Scattering.cuh:636-774 (setVonMisesFisherScattering):
+ * components (mu_k, C_k + log alpha_k); pairs j = k1 + N k2 with kappa = mu_k1 + mu_k2,
+ * weight exp(C'_k1 + C'_k2 - logN(kappa)) normalised to sum 1; exclusive cdf. */
+static void o_vmf_tables(const double* mu, const double* c, const double* alpha, uint32_t N,
+                         double* mc, double* pd, float* pf)
+{
+    uint32_t P = N * N;
+    for (uint32_t k = 0; k < N; ++k) { mc[2 * k] = mu[k]; mc[2 * k + 1] = c[k] + log(alpha[k]); }
+    double sum = 0.0;
+    for (uint32_t j = 0; j < P; ++j) {
+        uint32_t k1 = j % N, k2 = j / N;
+        double kap = mu[k1] + mu[k2];
+        double ln = o_vmf_log_norm(kap);
+        double w = exp(c[k1] + log(alpha[k1]) + c[k2] + log(alpha[k2]) - ln);
+        pd[3 * j] = kap; pd[3 * j + 1] = w; pd[3 * j + 2] = ln;
+        sum += w;
+    }
+    double cdf = 0.0;
+    for (uint32_t j = 0; j < P; ++j) {
+        double pj = pd[3 * j + 1] / sum;
+        pd[3 * j + 1] = pj;
+        pf[3 * j] = (float)cdf; pf[3 * j + 1] = (float)pd[3 * j]; pf[3 * j + 2] = (float)exp(-2.0 * fabs(pd[3 * j]));
+        cdf += pj;
+    }
+}
+
 static int o_build_scene(const sstmc_config* cfg, o_scene* S)
 {
     memset(S, 0, sizeof(*S));
@@ -243,12 +286,25 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     if (cfg->scattering_num == 0 || cfg->scattering_num > OM || !cfg->scattering_type) return SSTMC_INVALID_CONFIG;
     int M = (int)cfg->scattering_num;
     for (int m = 0; m < OM; ++m) S->scat_type[m] = SSTMC_SCATTERING_NOT_DEFINED;
-    size_t tab_total = 0, tab_pos = 0;
-    for (int m = 0; m < M; ++m)
+    size_t tab_total = 0, tab_pos = 0, vmf_comp = 0, vmf_pairs = 0, vmf_pos = 0, vmf_cpos = 0, vmf_ppos = 0;
+    for (int m = 0; m < M; ++m) {
         if (cfg->scattering_type[m] == SSTMC_SCATTERING_TABULAR) {
             if (!cfg->tabular_n || !cfg->tabular_f || cfg->tabular_n[m] < 2) return SSTMC_INVALID_CONFIG;
             tab_total += cfg->tabular_n[m];
         }
+        if (cfg->scattering_type[m] == SSTMC_SCATTERING_VMF_MIXTURE) {
+            if (!cfg->vmf_n || !cfg->vmf_mu || !cfg->vmf_c || !cfg->vmf_alpha || cfg->vmf_n[m] < 1) return SSTMC_INVALID_CONFIG;
+            vmf_comp += cfg->vmf_n[m];
+            vmf_pairs += (size_t)cfg->vmf_n[m] * cfg->vmf_n[m];
+        }
+    }
+    if (vmf_comp) {
+        S->vmf_mc = malloc(sizeof(double) * 2 * vmf_comp);
+        S->vmf_pd = malloc(sizeof(double) * 3 * vmf_pairs);
+        S->vmf_pf = malloc(sizeof(float) * 3 * vmf_pairs);
+        if (!S->vmf_mc || !S->vmf_pd || !S->vmf_pf) return SSTMC_ALLOCATION_ERROR;
+    }
+    int iso_m[OM] = { 0 }, any_vmf = 0;
     if (tab_total) {
         S->tab_f = malloc(sizeof(double) * 2 * tab_total);
         S->tab_pdf = malloc(sizeof(double) * tab_total);
@@ -258,8 +314,9 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     for (int m = 0; m < M; ++m) {
         int ty = cfg->scattering_type[m];
         double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
-        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR)
-            return SSTMC_NOT_SUPPORTED;
+        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR
+            && ty != SSTMC_SCATTERING_VMF_MIXTURE)
+            return SSTMC_INVALID_CONFIG;
         if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(fabs(g) < 1.0)) return SSTMC_INVALID_CONFIG;
         int toff = 0, tn = 0;
         if (ty == SSTMC_SCATTERING_TABULAR) {
@@ -269,13 +326,39 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
             if (e) return e;
             tab_pos += (size_t)tn;
         }
+        /* isIsotropicScattering per material, Scattering.cuh:1484-1512 */
+        int iso = ty == SSTMC_SCATTERING_ISOTROPIC || (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && fabs(g) < 0.0001);
+        int vn = 0, voff = 0, vpoff = 0;
+        if (ty == SSTMC_SCATTERING_VMF_MIXTURE) {
+            vn = (int)cfg->vmf_n[m];
+            const double *mu = cfg->vmf_mu + vmf_pos, *cc = cfg->vmf_c + vmf_pos, *al = cfg->vmf_alpha + vmf_pos;
+            vmf_pos += (size_t)vn;
+            double asum = 0.0;
+            iso = 1;   /* every |mu| <= 1e-4, Scattering.cuh:744-751 */
+            for (int k = 0; k < vn; ++k) {
+                if (!isfinite(mu[k]) || !isfinite(cc[k]) || !isfinite(al[k]) || al[k] < 0.0) return SSTMC_INVALID_CONFIG;
+                asum += al[k];
+                if (fabs(mu[k]) > 0.0001) iso = 0;
+            }
+            if (!(asum > 0.0)) return SSTMC_INVALID_CONFIG;
+            any_vmf = 1;
+            if (dims == 3) {   /* 2D: scattered isotropically (Scattering.cuh:899-905, 1093-1100) */
+                voff = (int)vmf_cpos; vpoff = (int)vmf_ppos;
+                o_vmf_tables(mu, cc, al, (uint32_t)vn, S->vmf_mc + 2 * vmf_cpos, S->vmf_pd + 3 * vmf_ppos, S->vmf_pf + 3 * vmf_ppos);
+                vmf_cpos += (size_t)vn; vmf_ppos += (size_t)vn * vn;
+            }
+        }
         int targets[2] = { m, 1 };
         int nt = (M == 1) ? 2 : 1;
         for (int q = 0; q < nt; ++q) {
             int mm = targets[q];
             S->tab_n[mm] = tn;
             S->tab_off[mm] = toff;
-            S->scat_type[mm] = ty;
+            S->vmf_n[mm] = dims == 3 ? vn : 0;
+            S->vmf_off[mm] = voff;
+            S->vmf_poff[mm] = vpoff;
+            iso_m[mm] = iso;
+            S->scat_type[mm] = (ty == SSTMC_SCATTERING_VMF_MIXTURE && dims == 2) ? SSTMC_SCATTERING_ISOTROPIC : ty;
             S->g_f[mm] = (float)g;
             S->gup[mm] = dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * O_PI)) : (1.0 - g * g) / (4.0 * O_PI);
             S->gd1[mm] = 1.0 + g * g;
@@ -284,11 +367,13 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     }
     if (M == 1) M = 2;
     S->M = M;
+    /* isIsotropicScattering over the defined materials, Scattering.cuh:1514-1528 */
     S->iso_all = 1;
-    for (int m = 0; m < OM; ++m) {
-        if (S->scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(fabs(S->g_f[m]) < 0.0001f)) S->iso_all = 0;
-        if (S->scat_type[m] == SSTMC_SCATTERING_TABULAR) S->iso_all = 0;
-    }
+    for (int m = 0; m < OM; ++m)
+        if (S->scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && !iso_m[m]) S->iso_all = 0;
+    /* all materials isotropic with a vMF among them: point sources would take the
+     * isotropic amplitude and far-field sources the mixture's (not built) */
+    if (S->iso_all && any_vmf) return SSTMC_NOT_SUPPORTED;
 
     /* medium */
     double bmin[3] = { 0, 0, 0 }, bmax[3] = { 0, 0, 0 };
@@ -380,7 +465,8 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
          * phase functions (no tabular material) */
         if (S->cbs && S->correlation && (S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f))
             return SSTMC_NOT_SUPPORTED;
-        if (S->cbs && S->correlation && S->scat_type[m] == SSTMC_SCATTERING_TABULAR) return SSTMC_NOT_SUPPORTED;
+        if (S->cbs && S->correlation && (S->scat_type[m] == SSTMC_SCATTERING_TABULAR || S->scat_type[m] == SSTMC_SCATTERING_VMF_MIXTURE))
+            return SSTMC_NOT_SUPPORTED;
     }
     /* field sampler: ticks sorted around the mean, TemporalSampler.cuh:958-1150 */
     S->disp_scale = calloc((size_t)OM * Nt, sizeof(float));
@@ -527,10 +613,32 @@ static inline void o_random_direction(int dims, o_stream* rs, float out[3])
 static void o_sample_direction(const o_scene* S, int m, const float din[3], o_stream* rs, float out[3])
 {
     int ty = S->scat_type[m];
-    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR) { o_random_direction(S->dims, rs, out); return; }
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR && ty != SSTMC_SCATTERING_VMF_MIXTURE) {
+        o_random_direction(S->dims, rs, out);
+        return;
+    }
     float g = S->g_f[m];
     float c;
-    if (ty == SSTMC_SCATTERING_TABULAR) {
+    if (ty == SSTMC_SCATTERING_VMF_MIXTURE) {
+        /* pair by the exclusive cdf (Scattering.cuh:1065-1077); the lobe's cosine
+         * by the exact inverse cdf of exp(kappa w) on [-1, 1] (the reference's
+         * Wood rejection loop, VectorType.cuh:169-203, samples the same density) */
+        const float* pf = S->vmf_pf + 3 * S->vmf_poff[m];
+        int P = S->vmf_n[m] * S->vmf_n[m];
+        float u = o_uniform(rs);
+        int j = 0;
+        while (j + 1 < P && pf[3 * (j + 1)] <= u) ++j;
+        float kap = pf[3 * j + 1], e2k = pf[3 * j + 2];
+        float v = o_uniform(rs);
+        float ak = fabsf(kap);
+        if (ak < 1e-4f) {
+            c = v * 2.0f - 1.0f;
+        } else {
+            float w = 1.0f + o_logf(v + (1.0f - v) * e2k) / ak;
+            if (w < -1.0f) w = -1.0f;
+            c = kap < 0.0f ? -w : w;
+        }
+    } else if (ty == SSTMC_SCATTERING_TABULAR) {
         /* Scattering.cuh:1030-1037: icdf entry round_num(xi N, N) (Simulation.cuh:287-298) */
         int N = S->tab_n[m];
         int k = (int)rintf(o_uniform(rs) * (float)N);
@@ -730,6 +838,25 @@ static inline int o_tab_index(const o_scene* S, int m, double c)
     return n < 0 ? 0 : (n >= N ? N - 1 : n);
 }
 
+/* vMF mixture, 3D: amplitude sum_k exp(c mu_k + C'_k) (Scattering.cuh:933-946),
+ * pdf sum_j w_j exp(c kappa_j + logN_j) (Scattering.cuh:997-1012) */
+static inline double o_vmf_amp(const o_scene* S, int m, double c)
+{
+    const double* p = S->vmf_mc + 2 * S->vmf_off[m];
+    double r = 0.0;
+    for (int k = 0; k < S->vmf_n[m]; ++k) r += exp(fma(c, p[2 * k], p[2 * k + 1]));
+    return r;
+}
+
+static inline double o_vmf_pdf(const o_scene* S, int m, double c)
+{
+    const double* p = S->vmf_pd + 3 * S->vmf_poff[m];
+    int P = S->vmf_n[m] * S->vmf_n[m];
+    double r = 0.0;
+    for (int j = 0; j < P; ++j) r += p[3 * j + 1] * exp(fma(c, p[3 * j], p[3 * j + 2]));
+    return r;
+}
+
 /* Scattering::amplitude / pdf device implementations, Scattering.cuh:895-1023 (FP64).
  * o_amp: the real amplitudes (Isotropic, HG); o_ampc below adds the tabular one. */
 static inline double o_amp(const o_scene* S, int m, double c)
@@ -740,6 +867,7 @@ static inline double o_amp(const o_scene* S, int m, double c)
         double dn = fma(S->gd2[m], c, S->gd1[m]);
         return S->dims == 2 ? sqrt(S->gup[m] / dn) : sqrt(S->gup[m] / (dn * sqrt(dn)));
     }
+    if (ty == SSTMC_SCATTERING_VMF_MIXTURE) return o_vmf_amp(S, m, c);
     return 0.0;
 }
 
@@ -747,6 +875,7 @@ static inline double o_pdf(const o_scene* S, int m, double c)
 {
     int ty = S->scat_type[m];
     if (ty == SSTMC_SCATTERING_ISOTROPIC) return S->dims == 2 ? O_ISO_PDF2 : O_ISO_PDF3;
+    if (ty == SSTMC_SCATTERING_VMF_MIXTURE) return o_vmf_pdf(S, m, c);
     if (ty == SSTMC_SCATTERING_TABULAR) return S->tab_pdf[S->tab_off[m] + o_tab_index(S, m, c)];
     if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN) {
         double dn = fma(S->gd2[m], c, S->gd1[m]);

@@ -5,8 +5,9 @@ The dict mirrors the struct that the reference's MEX functions take,
 MatlabInterface.cu:712-1672):
 
     config['simulation']   batchSize, fullIteration, renderingsNum, lambda, seed, deviceNumber
-    config['scattering']   type (list of 'Isotropic' / 'HG' / 'HenyeyGreenstein' / 'Tabular'),
-                           amplitudeFunction (list: g for HG, a complex vector for Tabular)
+    config['scattering']   type (list of 'Isotropic' / 'HG' / 'HenyeyGreenstein' / 'Tabular' / 'vMF' /
+                           'VonMisesFisher'), amplitudeFunction (list: g for HG, a complex vector for
+                           Tabular, a dict with mixtureMu / mixtureC / mixtureAlpha for vMF)
     config['medium']       type 'Heterogeneous' (xAxis, yAxis, zAxis, materialGrid, sigs, siga)
                            or 'Homogeneous' (boxMin, boxMax, sigs)
     config['illumination'] / ['view'] / ['illumination2'] / ['view2']
@@ -102,6 +103,10 @@ class SstmcConfig(C.Structure):
         ("precision", C.c_int32),
         ("tabular_n", C.POINTER(C.c_uint32)),
         ("tabular_f", C.POINTER(C.c_double)),
+        ("vmf_n", C.POINTER(C.c_uint32)),
+        ("vmf_mu", C.POINTER(C.c_double)),
+        ("vmf_c", C.POINTER(C.c_double)),
+        ("vmf_alpha", C.POINTER(C.c_double)),
     ]
 
 
@@ -230,7 +235,9 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
     st = np.zeros(len(types), dtype=np.int32)
     sg = np.zeros(len(types), dtype=np.float64)
     tn = np.zeros(len(types), dtype=np.uint32)
+    vn = np.zeros(len(types), dtype=np.uint32)
     tabs = []
+    vmfs = []
     for i, t in enumerate(types):
         if t == "Isotropic":
             st[i] = SCATTERING_ISOTROPIC
@@ -245,7 +252,20 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
             tn[i] = f.size
             tabs.append(f)
         elif t in ("vMF", "VonMisesFisher"):
+            # a struct with mixtureMu, mixtureC, mixtureAlpha (MatlabInterface.cu:827-868)
             st[i] = SCATTERING_VMF
+            cell = amps[i]
+            if not isinstance(cell, dict) or not all(k in cell for k in ("mixtureMu", "mixtureC", "mixtureAlpha")):
+                raise ConfigError(f"scattering.amplitudeFunction of vMF material {i} must be a struct with "
+                                  "mixtureMu, mixtureC and mixtureAlpha")
+            mu, cc, al = (np.asarray(cell[k], dtype=np.float64).ravel() for k in ("mixtureMu", "mixtureC", "mixtureAlpha"))
+            if mu.size < 1 or cc.size != mu.size or al.size != mu.size:
+                raise ConfigError(f"vMF material {i}: mixtureMu, mixtureC and mixtureAlpha must have the same length >= 1")
+            if not (np.all(np.isfinite(mu)) and np.all(np.isfinite(cc)) and np.all(np.isfinite(al))
+                    and np.all(al >= 0) and np.any(al > 0)):
+                raise ConfigError(f"vMF material {i}: finite values and mixtureAlpha >= 0 (not all 0) required")
+            vn[i] = mu.size
+            vmfs.append((mu, cc, al))
         else:
             raise ConfigError(f"Unsupported scattering type in material {i}: {t}")
     keep += [st, sg]
@@ -254,6 +274,13 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
         keep += [tn, tf]
         c.tabular_n = tn.ctypes.data_as(C.POINTER(C.c_uint32))
         c.tabular_f = tf.ctypes.data_as(_dp)
+    if vmfs:
+        vmu, vc, val = (np.ascontiguousarray(np.concatenate([v[j] for v in vmfs])) for j in range(3))
+        keep += [vn, vmu, vc, val]
+        c.vmf_n = vn.ctypes.data_as(C.POINTER(C.c_uint32))
+        c.vmf_mu = vmu.ctypes.data_as(_dp)
+        c.vmf_c = vc.ctypes.data_as(_dp)
+        c.vmf_alpha = val.ctypes.data_as(_dp)
     c.scattering_num = len(types)
     c.scattering_type = st.ctypes.data_as(C.POINTER(C.c_int32))
     c.scattering_g = sg.ctypes.data_as(_dp)

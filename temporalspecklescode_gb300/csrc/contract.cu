@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
             const bool vary = !scalar_fs && (corr ? S.static_corr[m] == 0 : (S.temporal_amp && S.moving[m]));
             const V3 xp = V3{ x1s[pp][0], x1s[pp][1], x1s[pp][2] };
             const int lg = min(l0 + tl, Nl - 1), vg = min(v0 + tv, Nv - 1);
-            if (is_tab(S, m)) {
+            if (is_amp64(S, m)) {
                 // tabular scattering: complex amplitude of the angle between the
                 // incoming and outgoing directions (FP64, nee.cuh); correlation:
                 // u1 amplitude x conj(u2 amplitude) x the temporal factor
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
                     double in[3], out[3];
                     src_in64(a, lg, x, in);
                     src_out64(bsrc, vg, x, out);
-                    return tab_amp(S, m, in[0] * out[0] + in[1] * out[1] + in[2] * out[2]);
+                    return amp64(S, m, in[0] * out[0] + in[1] * out[1] + in[2] * out[2]);
                 };
                 for (int tt = 0; tt < kSsT; ++tt) {
                     if (tt >= tn) break;
@@ -538,7 +538,7 @@ int launch_gemm(const GemmParams& G, cudaStream_t stream)
 int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
 {
     if (G.K <= 0) return SSTMC_NO_ERROR;
-    if (S.correlation && S.sym && S.all_static_corr && !S.has_tabular) {
+    if (S.correlation && S.sym && S.all_static_corr && !S.has_amp64) {
         // two resident blocks per SM: split the paths so the grid fills them
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);

@@ -88,9 +88,40 @@ __device__ __forceinline__ int tab_index(const DevScene& S, int m, double c)
     return n < 0 ? 0 : (n >= N ? N - 1 : n);
 }
 
-__device__ __forceinline__ float2 tab_amp(const DevScene& S, int m, double c) { return S.tab_f[S.tab_off[m] + tab_index(S, m, c)]; }
-__device__ __forceinline__ float tab_pdf(const DevScene& S, int m, double c) { return S.tab_pdf[S.tab_off[m] + tab_index(S, m, c)]; }
-__device__ __forceinline__ bool is_tab(const DevScene& S, int m) { return S.has_tabular && S.scat_type[m] == SSTMC_SCATTERING_TABULAR; }
+// vMF mixture in 3D: amplitude sum_k exp(c mu_k + C'_k) (Scattering.cuh:933-946)
+// and pdf sum_j w_j exp(c kappa_j + logN_j) (Scattering.cuh:997-1012), in FP64
+__device__ __forceinline__ double vmf_amp(const DevScene& S, int m, double c)
+{
+    const double* p = S.vmf_mc + 2 * S.vmf_off[m];
+    double r = 0.0;
+    for (int k = 0; k < S.vmf_n[m]; ++k) r += exp(fma(c, p[2 * k], p[2 * k + 1]));
+    return r;
+}
+
+__device__ __forceinline__ double vmf_pdf(const DevScene& S, int m, double c)
+{
+    const double* p = S.vmf_pd + 3 * S.vmf_poff[m];
+    const int P = S.vmf_n[m] * S.vmf_n[m];
+    double r = 0.0;
+    for (int j = 0; j < P; ++j) r += p[3 * j + 1] * exp(fma(c, p[3 * j], p[3 * j + 2]));
+    return r;
+}
+
+// Amplitude and pdf of a tabular or vMF material at scattering cosine c
+__device__ __forceinline__ float2 amp64(const DevScene& S, int m, double c)
+{
+    if (S.scat_type[m] == SSTMC_SCATTERING_VMF_MIXTURE) return make_float2((float)vmf_amp(S, m, c), 0.0f);
+    return S.tab_f[S.tab_off[m] + tab_index(S, m, c)];
+}
+__device__ __forceinline__ float pdf64(const DevScene& S, int m, double c)
+{
+    if (S.scat_type[m] == SSTMC_SCATTERING_VMF_MIXTURE) return (float)vmf_pdf(S, m, c);
+    return S.tab_pdf[S.tab_off[m] + tab_index(S, m, c)];
+}
+__device__ __forceinline__ bool is_amp64(const DevScene& S, int m)
+{
+    return S.has_amp64 && (S.scat_type[m] == SSTMC_SCATTERING_TABULAR || S.scat_type[m] == SSTMC_SCATTERING_VMF_MIXTURE);
+}
 
 // Scattering cosine of source element k attached at pa with the path
 // continuing to pb (threePointFunction, FarField.cuh:546-554,

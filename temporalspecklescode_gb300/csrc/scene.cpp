@@ -165,6 +165,43 @@ static void tabular_tables(const double* f, uint32_t N, int dims, std::vector<do
     }
 }
 
+// vMFnormalizationLog in 3D (SpecialFunctions.cuh:187-203): the log of the
+// normalisation kappa / (4 pi sinh kappa) of a vMF lobe; a kappa below 1e-12
+// (negative ones included) takes the isotropic value.
+static double vmf_log_norm(double x)
+{
+    if (x < 1e-12) return -std::log(4.0 * kPi);
+    if (x < 5.0) return std::log(x) - std::log(4.0 * kPi * std::sinh(x));
+    return std::log(x) - std::log(2.0 * kPi) - x;
+}
+
+// Tables of one 3D vMF mixture (Scattering.cuh:636-774): the amplitude's
+// components (mu_k, C_k + log alpha_k); the pdf's component pairs j = k1 + N k2
+// with kappa_j = mu_k1 + mu_k2, weight exp(C'_k1 + C'_k2 - logN(kappa_j))
+// normalised to sum 1, and the sampler's exclusive cdf of the weights.
+static void vmf_tables(const double* mu, const double* c, const double* alpha, uint32_t N,
+                       std::vector<double>& mc, std::vector<double>& pd, std::vector<float>& pf)
+{
+    for (uint32_t k = 0; k < N; ++k) { mc.push_back(mu[k]); mc.push_back(c[k] + std::log(alpha[k])); }
+    const uint32_t P = N * N;
+    std::vector<double> w(P), kap(P), ln(P);
+    double sum = 0.0;
+    for (uint32_t j = 0; j < P; ++j) {
+        const uint32_t k1 = j % N, k2 = j / N;
+        kap[j] = mu[k1] + mu[k2];
+        ln[j] = vmf_log_norm(kap[j]);
+        w[j] = std::exp(c[k1] + std::log(alpha[k1]) + c[k2] + std::log(alpha[k2]) - ln[j]);
+        sum += w[j];
+    }
+    double cdf = 0.0;
+    for (uint32_t j = 0; j < P; ++j) {
+        const double pj = w[j] / sum;
+        pd.push_back(kap[j]); pd.push_back(pj); pd.push_back(ln[j]);
+        pf.push_back((float)cdf); pf.push_back((float)kap[j]); pf.push_back((float)std::exp(-2.0 * std::fabs(kap[j])));
+        cdf += pj;
+    }
+}
+
 int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
 {
     auto fail = [&](int code, const char* msg) { if (why) *why = msg; return code; };
@@ -186,11 +223,15 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     int M = (int)cfg->scattering_num;
     for (int m = 0; m < kMat; ++m) D.scat_type[m] = SSTMC_SCATTERING_NOT_DEFINED;
     size_t tab_pos = 0;   // running offset into cfg->tabular_f (entries)
+    size_t vmf_pos = 0;   // running offset into cfg->vmf_* (components)
+    bool iso_m[kMat] = { false };   // isIsotropicScattering per material (Scattering.cuh:1484-1512)
+    bool any_vmf = false;
     for (int m = 0; m < M; ++m) {
         const int ty = cfg->scattering_type[m];
         const double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
-        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR)
-            return fail(SSTMC_NOT_SUPPORTED, "only Isotropic, HenyeyGreenstein and Tabular scattering are supported");
+        if (ty != SSTMC_SCATTERING_ISOTROPIC && ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR
+            && ty != SSTMC_SCATTERING_VMF_MIXTURE)
+            return fail(SSTMC_INVALID_CONFIG, "scattering types are Isotropic, Tabular, HenyeyGreenstein (HG) and VonMisesFisher (vMF)");
         if (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(g) < 1.0)) return fail(SSTMC_INVALID_CONFIG, "|g| must be < 1");
         int toff = 0, tn = 0;
         if (ty == SSTMC_SCATTERING_TABULAR) {
@@ -208,7 +249,34 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
                 S->tab_pdf.push_back((float)pdf[i]);
                 S->tab_cos.push_back(cosv[i]);
             }
-            D.has_tabular = 1;
+            D.has_amp64 = 1;
+        }
+        int voff = 0, vpoff = 0, vn = 0;
+        bool iso = ty == SSTMC_SCATTERING_ISOTROPIC || (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && std::fabs(g) < 0.0001);
+        if (ty == SSTMC_SCATTERING_VMF_MIXTURE) {
+            if (!cfg->vmf_n || !cfg->vmf_mu || !cfg->vmf_c || !cfg->vmf_alpha || cfg->vmf_n[m] < 1)
+                return fail(SSTMC_INVALID_CONFIG, "a vMF material needs mixtureMu, mixtureC and mixtureAlpha with at least one component");
+            vn = (int)cfg->vmf_n[m];
+            const double* mu = cfg->vmf_mu + vmf_pos;
+            const double* cc = cfg->vmf_c + vmf_pos;
+            const double* al = cfg->vmf_alpha + vmf_pos;
+            vmf_pos += (size_t)vn;
+            double asum = 0.0;
+            iso = true;   // isIsotropicScatteringVonMisesFisher: every |mu| <= 1e-4 (Scattering.cuh:744-751)
+            for (int k = 0; k < vn; ++k) {
+                if (!std::isfinite(mu[k]) || !std::isfinite(cc[k]) || !std::isfinite(al[k]) || al[k] < 0.0)
+                    return fail(SSTMC_INVALID_CONFIG, "vMF mixtures need finite values and mixtureAlpha >= 0");
+                asum += al[k];
+                if (std::fabs(mu[k]) > 0.0001) iso = false;
+            }
+            if (!(asum > 0.0)) return fail(SSTMC_INVALID_CONFIG, "vMF mixtureAlpha must not be all zero");
+            any_vmf = true;
+            if (dims == 3) {   // in 2D the reference scatters vMF materials isotropically (Scattering.cuh:899-905, 1093-1100)
+                voff = (int)(S->vmf_mc.size() / 2);
+                vpoff = (int)(S->vmf_pd.size() / 3);
+                vmf_tables(mu, cc, al, (uint32_t)vn, S->vmf_mc, S->vmf_pd, S->vmf_pf);
+                D.has_amp64 = 1;
+            }
         }
         const int targets[2] = { m, 1 };
         const int nt = (M == 1) ? 2 : 1;
@@ -216,7 +284,11 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
             const int mm = targets[q];
             D.tab_off[mm] = toff;
             D.tab_n[mm] = tn;
-            D.scat_type[mm] = ty;
+            D.vmf_n[mm] = dims == 3 ? vn : 0;
+            D.vmf_off[mm] = voff;
+            D.vmf_poff[mm] = vpoff;
+            iso_m[mm] = iso;
+            D.scat_type[mm] = (ty == SSTMC_SCATTERING_VMF_MIXTURE && dims == 2) ? SSTMC_SCATTERING_ISOTROPIC : ty;
             S->g_d[mm] = g;
             D.g[mm] = (float)g;
             D.gup[mm] = (float)(dims == 2 ? 2.0 * ((1.0 - g * g) / (4.0 * kPi)) : (1.0 - g * g) / (4.0 * kPi));
@@ -227,10 +299,15 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     }
     if (M == 1) M = 2;
     S->M = M;
+    // isIsotropicScattering over every defined material (Scattering.cuh:1514-1528)
     D.iso_all = 1;
     for (int m = 0; m < kMat; ++m)
-        if ((D.scat_type[m] == SSTMC_SCATTERING_HENYEY_GREENSTEIN && !(std::fabs(D.g[m]) < 0.0001f))
-            || D.scat_type[m] == SSTMC_SCATTERING_TABULAR) D.iso_all = 0;
+        if (D.scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && !iso_m[m]) D.iso_all = 0;
+    // With every material isotropic, the reference's point sources take the
+    // isotropic amplitude while its far-field sources evaluate a vMF mixture
+    // (PointSource.cuh:346-430); that split is not built.
+    if (D.iso_all && any_vmf)
+        return fail(SSTMC_NOT_SUPPORTED, "every material isotropic with a vMF material among them: use Isotropic");
     D.iso_amp = dims == 2 ? kIsoAmp2 : kIsoAmp3;
     D.iso_pdf = dims == 2 ? kIsoPdf2 : kIsoPdf3;
 
@@ -342,7 +419,7 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     for (int m = 0; m < kMat; ++m) if (!D.static_corr[m]) D.all_static_corr = 0;
     // CBS of the correlation sampler is built for static scatterers (no drift U)
     // and real phase functions
-    if (cfg->is_cbs && S->correlation && (!D.all_static_corr || D.has_tabular))
+    if (cfg->is_cbs && S->correlation && (!D.all_static_corr || D.has_amp64))
         return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS with the TemporalCorrelationSampler needs static scatterers (U = 0) and no tabular material");
     // isForcedInsideBin belongs to the field sampler; the correlation sampler has no
     // such option and the reference ignores the field there (MatlabInterface.cu:1245-1282)
@@ -400,12 +477,15 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     if (cudaSetDevice(S->device) != cudaSuccess) return fail(SSTMC_DEVICE_ERROR, "cudaSetDevice failed");
     int e = 0;
     for (int a = 0; a < dims && !e; ++a) e = upload(S, S->ax[a], &D.ax[a]);
-    if (!e && D.has_tabular) {
+    if (!e && D.has_amp64) {
         const float* tf = nullptr;
         e = upload(S, S->tab_f, &tf);
         D.tab_f = reinterpret_cast<const float2*>(tf);
         if (!e) e = upload(S, S->tab_pdf, &D.tab_pdf);
         if (!e) e = upload(S, S->tab_cos, &D.tab_cos);
+        if (!e) e = upload(S, S->vmf_mc, &D.vmf_mc);
+        if (!e) e = upload(S, S->vmf_pd, &D.vmf_pd);
+        if (!e) e = upload(S, S->vmf_pf, &D.vmf_pf);
     }
     if (!e) e = upload(S, S->grid, &D.grid);
     if (!e) e = upload(S, S->disp_scale, &D.disp_scale);

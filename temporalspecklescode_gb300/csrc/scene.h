@@ -72,13 +72,21 @@ struct DevScene {
     float k2;                    // (2 pi / lambda)^2
     float iso_amp, iso_pdf;
     DevSource src[4];            // illumination, view, illumination2, view2
+    // a tabular or vMF material is present: its amplitudes and pdfs are taken
+    // from an FP64 cosine through the complex-amplitude route (amp64 / pdf64)
+    int has_amp64;
     // tabular scattering (Scattering.cuh:191-482): per material its entries and
     // the offset of its rows in the concatenated tables
-    int has_tabular;
     int tab_n[kMat], tab_off[kMat];
     const float2* tab_f;         // amplitude normalised by the cross section
     const float* tab_pdf;        // evaluation pdf |f|^2 (x sin(theta) in 3D, as the reference)
     const float* tab_cos;        // cos(icdf): the sampler's scattering cosines
+    // von Mises-Fisher mixtures in 3D (Scattering.cuh:613-884): per material its
+    // component count and the offsets of its components and component pairs
+    int vmf_n[kMat], vmf_off[kMat], vmf_poff[kMat];
+    const double* vmf_mc;        // [components][2]: mu, C + log(alpha)
+    const double* vmf_pd;        // [pairs][3]: kappa = mu1 + mu2, normalised weight, log normalisation
+    const float* vmf_pf;         // [pairs][3]: exclusive cdf of the weights, kappa, exp(-2 |kappa|)
 };
 
 // Host-owned scene: normalised config, float tables and device buffers.
@@ -103,6 +111,8 @@ struct Scene {
     double g_d[kMat] = { 0 };    // HG g per material (double, for the weight tables)
     std::vector<float> tab_f, tab_pdf, tab_cos;   // tabular tables (device copies in dev.tab_*)
     std::vector<double> tab_f_d;                  // normalised amplitudes (re, im) in FP64 (weight tables)
+    std::vector<double> vmf_mc, vmf_pd;           // vMF tables (device copies in dev.vmf_*)
+    std::vector<float> vmf_pf;
     double D_d[kMat] = { 0 };    // Brownian D per material
     DevScene dev{};
     std::vector<void*> dev_allocs;

@@ -243,7 +243,7 @@ int render_static(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, d
     unsigned char* base = nullptr;
     int e = scratch_base(dev, &base);
     if (e) return e;
-    const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD && !S.dev.has_tabular;
+    const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD && !S.dev.has_amp64;
     Engine E;                  // buffers point into the scratch: never released
     E.stream = stream;
     E.timing = false;

@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             if (b == 2 && T.pass0) {
                 const V3 x12 = funit(sub3(xn, x1));
                 // tabular first material: complex amplitudes from an FP64 angle (nee.cuh)
-                const bool tab1 = is_tab(S, m1);
+                const bool tab1 = is_amp64(S, m1);
                 float ps = 0.0f;
                 if (tab1) {
                     double d12[3];
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     for (int l = lane; l < Nl; l += 32) {
                         double in[3];
                         src_in64(il, l, x1, in);
-                        ps += T.pl[(size_t)q * Nl + l] * tab_pdf(S, m1, in[0] * d12[0] + in[1] * d12[1] + in[2] * d12[2]);
+                        ps += T.pl[(size_t)q * Nl + l] * pdf64(S, m1, in[0] * d12[0] + in[1] * d12[1] + in[2] * d12[2]);
                     }
                 } else {
                     for (int l = lane; l < Nl; l += 32)
@@ -508,9 +508,9 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                         float f12s = 0.0f;
                         // tabular: u1 amplitude x conj(u2 amplitude), complex unless u1 == u2
                         auto f12tab = [&](const V3& pa, const V3& pb) {
-                            const float2 f1 = tab_amp(S, m1, f3_cos64(il, l, pa, pb, false));
+                            const float2 f1 = amp64(S, m1, f3_cos64(il, l, pa, pb, false));
                             if (S.sym) return make_float2(f1.x * f1.x + f1.y * f1.y, 0.f);
-                            return c_mulc(f1, tab_amp(S, m1, f3_cos64(il2, l, pa, pb, false)));
+                            return c_mulc(f1, amp64(S, m1, f3_cos64(il2, l, pa, pb, false)));
                         };
                         float2 f12cs = make_float2(0.f, 0.f);
                         if (stf && tab1) f12cs = f12tab(x1, xn);
@@ -550,10 +550,10 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
                     for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
                         if (tab1) {   // view attached at x1, path on to x2
-                            const float2 fs = stf ? tab_amp(S, m1, f3_cos64(vw, v, x1, xn, true)) : make_float2(0.f, 0.f);
+                            const float2 fs = stf ? amp64(S, m1, f3_cos64(vw, v, x1, xn, true)) : make_float2(0.f, 0.f);
                             for (int t = lane / T.vwa; t < Nt; t += T.tga) {
                                 const size_t o = ((size_t)q * Nt + t) * Nv + v;
-                                const float2 f = stf ? fs : tab_amp(S, m1, f3_cos64(vw, v, tick_pos(xtc, t), tick_pos(xtn, t), true));
+                                const float2 f = stf ? fs : amp64(S, m1, f3_cos64(vw, v, tick_pos(xtc, t), tick_pos(xtn, t), true));
                                 T.s_ms[o] = c_scale(c_mul(T.b_ss[o], f), p2inv);
                             }
                             continue;
@@ -569,10 +569,10 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
                     for (int l = lane % T.lw; l < Nl; l += T.lw) {
                         if (tab1) {   // illumination attached at x1, path on to x2
-                            const float2 fs = stf ? tab_amp(S, m1, f3_cos64(il, l, x1, xn, false)) : make_float2(0.f, 0.f);
+                            const float2 fs = stf ? amp64(S, m1, f3_cos64(il, l, x1, xn, false)) : make_float2(0.f, 0.f);
                             for (int t = lane / T.lw; t < Nt; t += T.lg) {
                                 const size_t o = ((size_t)q * Nt + t) * Nl + l;
-                                const float2 f = stf ? fs : tab_amp(S, m1, f3_cos64(il, l, tick_pos(xtc, t), tick_pos(xtn, t), false));
+                                const float2 f = stf ? fs : amp64(S, m1, f3_cos64(il, l, tick_pos(xtc, t), tick_pos(xtn, t), false));
                                 T.a_ms[o] = c_scale(c_mul(T.a_ms[o], f), p2inv);
                             }
                             continue;
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 const float ptk = k2 * MT;
                 const float c1base = k2 * S.D[mn];
                 const V3 back = funit(sub3(cur, xn));
-                const bool tabn = is_tab(S, mn);
+                const bool tabn = is_amp64(S, mn);
                 int j = 0;
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                     const V3 o1 = fsrc_out(vw, v, xn);
@@ -611,9 +611,9 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     float f12s = 0.0f;
                     // tabular: u1 amplitude x conj(u2 amplitude), the view attached at x_b
                     auto f12tab = [&](const V3& pa, const V3& pb) {
-                        const float2 f1 = tab_amp(S, mn, f3_cos64(vw, v, pa, pb, true));
+                        const float2 f1 = amp64(S, mn, f3_cos64(vw, v, pa, pb, true));
                         if (S.sym) return make_float2(f1.x * f1.x + f1.y * f1.y, 0.f);
-                        return c_mulc(f1, tab_amp(S, mn, f3_cos64(vw2, v, pa, pb, true)));
+                        return c_mulc(f1, amp64(S, mn, f3_cos64(vw2, v, pa, pb, true)));
                     };
                     float2 f12cs = make_float2(0.f, 0.f);
                     if (stf && tabn) f12cs = f12tab(xn, cur);
@@ -662,9 +662,9 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     return T.cbs ? fillum_exit<ILP>(S, il, e, pa, pb, m) : fview<VWP>(S, vw, e, pa, pb, m);
                 };
                 // tabular vertex material: complex amplitude, the source attached at x_b
-                const bool tabn = is_tab(S, mn);
+                const bool tabn = is_amp64(S, mn);
                 auto fxc = [&](int e, const V3& pa, const V3& pb) {
-                    return tab_amp(S, mn, T.cbs ? f3_cos64(il, e, pa, pb, false) : f3_cos64(vw, e, pa, pb, true));
+                    return amp64(S, mn, T.cbs ? f3_cos64(il, e, pa, pb, false) : f3_cos64(vw, e, pa, pb, true));
                 };
                 int j = 0;
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {

@@ -716,7 +716,7 @@ int view_max_views(const DevScene& S) { return S.correlation ? 64 * kVPP : 32 * 
 
 bool view_kernel_covers(const DevScene& S, const bool* moving_any)
 {
-    if (S.has_tabular) return false;   // complex tabular amplitudes: trace_kernel
+    if (S.has_amp64) return false;   // complex tabular amplitudes: trace_kernel
     if (S.correlation) return S.sym && S.all_static_corr;
     return !*moving_any;
 }
@@ -751,7 +751,7 @@ int launch_view(const DevScene& S, const TraceParams& T, int blocks, int threads
 
 bool illum_kernel_covers(const DevScene& S)
 {
-    return S.correlation && S.sym && S.all_static_corr && !S.has_tabular && S.src[0].n <= 32 * kMaxIllum;
+    return S.correlation && S.sym && S.all_static_corr && !S.has_amp64 && S.src[0].n <= 32 * kMaxIllum;
 }
 
 int launch_illum(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream)

@@ -255,6 +255,68 @@ def forced_bin_2d(batch_size=64, full_iteration=2):
     return cfg, 2
 
 
+def vmf_mixture(mus, alphas, iso_amp=0.28209479177387814):
+    """A vMF-mixture amplitude cell: lobes e^{mu (c - 1)} scaled to the 3D
+    isotropic amplitude (mixtureC = log(iso_amp) - mu)."""
+    mus = np.asarray(mus, dtype=np.float64)
+    return {"mixtureMu": mus, "mixtureC": np.log(iso_amp) - mus, "mixtureAlpha": np.asarray(alphas, dtype=np.float64)}
+
+
+VMF_FORWARD = ([0.0, 3.5, 22.0], [0.35, 0.45, 0.2])
+VMF_TWO_SIDED = ([0.0, 6.0, -0.8], [0.3, 0.5, 0.4])   # a backward lobe: negative-kappa pairs
+
+
+def with_vmf(scene, lobes=(VMF_FORWARD, VMF_TWO_SIDED)):
+    """The scene with material 0 an isotropic-like vMF (mu = 0) and materials
+    1, 2 (when present) the given vMF mixtures; further materials keep theirs."""
+    cfg, dims = scene
+    cfg = dict(cfg)
+    sc = cfg["scattering"]
+    types = list(sc["type"]) if not isinstance(sc["type"], str) else [sc["type"]]
+    amps = list(sc.get("amplitudeFunction", [0.0] * len(types)))
+    types[0], amps[0] = "vMF", vmf_mixture([0.0], [1.0])
+    for i, (mu, al) in enumerate(lobes):
+        if 1 + i < len(types):
+            types[1 + i], amps[1 + i] = "vMF", vmf_mixture(mu, al)
+    cfg["scattering"] = {"type": types, "amplitudeFunction": amps}
+    return cfg, dims
+
+
+def reciprocal_far_3d_vmf(cbs: bool = True, batch_size=64, full_iteration=2):
+    """The reciprocal far-field scene with vMF mixtures: a vMF amplitude depends on
+    the scattering cosine only, so with CBS the field is symmetric in (l, v)."""
+    return with_vmf(reciprocal_far_3d(cbs=cbs, batch_size=batch_size, full_iteration=full_iteration))
+
+
+def vmf_corr_3d(batch_size=96, full_iteration=2):
+    """The bench geometry (correlation sampler, point sources, one cell) with a
+    forward-peaked vMF mixture."""
+    cfg, dims = wl.correlation_3d(batch_size=batch_size, full_iteration=full_iteration, n_side=4, n_lags=4)
+    cfg = dict(cfg)
+    cfg["scattering"] = {"type": ["vMF", "vMF"],
+                         "amplitudeFunction": [vmf_mixture([0.0], [1.0]), vmf_mixture(*VMF_FORWARD)]}
+    return cfg, dims
+
+
+def vmf_2d(vmf: bool = True, batch_size=64, full_iteration=2):
+    """2D far-field field scene with a vMF material next to an HG one: the
+    reference scatters a 2D vMF material isotropically."""
+    d = wl._farfield_fan(6)
+    d2 = wl._farfield_fan(5, 0.3)
+    grid = np.array([[1, 2], [2, 1], [1, 1]], dtype=np.uint32)
+    first = ("vMF", vmf_mixture(*VMF_TWO_SIDED)) if vmf else ("Isotropic", 0.0)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.8, "seed": 13},
+        "scattering": {"type": [first[0], first[0], "HG"], "amplitudeFunction": [first[1], first[1], 0.6]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-6.0, -1.0, 2.0, 6.0], "yAxis": [-5.0, 0.5, 5.0],
+                   "materialGrid": grid, "sigs": [0.0, 0.8, 1.5], "siga": [0.0, 0.01, 0.0]},
+        "illumination": {"type": "FarField", "direction": d}, "view": {"type": "FarField", "direction": d2},
+        "sampler": {"type": "TemporalSampler", "t": [0.0, 1.0], "D": [0.0, 1e-3, 0.0], "U": {"x": [0.0, 0.0, 0.0], "y": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -286,4 +348,10 @@ def small_scenes():
         "forced_bin_3d": forced_bin_3d(),
         "forced_bin_2d": forced_bin_2d(),
         "forced_bin_2d_cbs": with_cbs(forced_bin_2d()),
+        "vmf_field_3d": with_vmf(field_point_3d()),
+        "vmf_transmission_3d": with_vmf(wl.transmission_matrix_3d(batch_size=32, full_iteration=2, n_dirs=12, grid=(8, 8, 4))),
+        "vmf_corr_3d": vmf_corr_3d(),
+        "vmf_field_3d_cbs": with_cbs(with_vmf(field_point_3d())),
+        "vmf_2d": vmf_2d(),
+        "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
     }

@@ -159,7 +159,8 @@ def test_view_kernel_matches_fused_kernel(name, api, monkeypatch):
 
 
 @pytest.mark.parametrize("name", ["reciprocal_far_3d_cbs", "reciprocal_point_2d_cbs",
-                                  "reciprocal_far_3d_corr_cbs", "reciprocal_point_2d_corr_cbs"])
+                                  "reciprocal_far_3d_corr_cbs", "reciprocal_point_2d_corr_cbs",
+                                  "reciprocal_far_3d_vmf_cbs"])
 def test_cbs_reciprocity(name, api):
     """Field CBS on the GPU: with the views the reversed illuminations the field
     is symmetric in (l, v) (the reversed-path rows are the direct rows with the
@@ -213,3 +214,25 @@ def test_forced_inside_bin_neutral_cases(api, make):
     with api.Scene(forced, dims) as s:
         u1, _ = s.render(seed=31)
     assert np.array_equal(u0, u1)
+
+
+def test_vmf_scatters_isotropically_in_2d(api):
+    """A 2D vMF material scatters isotropically, as in the reference: the render
+    equals the one with an Isotropic material, bit for bit."""
+    from tests.scenes import vmf_2d
+    out = []
+    for vmf in (True, False):
+        with api.Scene(*vmf_2d(vmf)) as s:
+            out.append(s.render(seed=8)[0])
+    assert np.array_equal(out[0], out[1])
+
+
+def test_vmf_all_isotropic_refused(api):
+    """Every material isotropic with a vMF among them: SSTMC_NOT_SUPPORTED."""
+    from tests.scenes import field_point_3d, vmf_mixture
+    cfg, dims = field_point_3d()
+    cfg = dict(cfg, scattering={"type": ["vMF", "Isotropic", "HG"],
+                                "amplitudeFunction": [vmf_mixture([0.0], [1.0]), 0.0, 0.0]})
+    with pytest.raises(api.SstmcError) as ei:
+        api.Scene(cfg, dims)
+    assert ei.value.code == 5

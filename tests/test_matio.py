@@ -41,3 +41,19 @@ def test_wavelength_vector():
     assert np.array_equal(api.wavelengths(cfg), [0.5, 0.6, 0.7])
     with pytest.raises(cf.ConfigError):
         cf.prepare(cfg, 2)   # one scene has one wavelength; the mirror splits the vector
+
+
+def test_vmf_struct_cells_round_trip(tmp_path):
+    """vMF materials are struct cells (mixtureMu / mixtureC / mixtureAlpha) inside
+    the amplitudeFunction cell array; a .mat round trip keeps every component."""
+    from tests.scenes import small_scenes
+    cfg, dims = small_scenes()["vmf_field_3d"]
+    p = str(tmp_path / "vmf.mat")
+    matio.save_config(p, cfg)
+    back = matio.load_config(p)
+    a, b = cf.prepare(cfg, dims), cf.prepare(back, dims)
+    n = int(np.ctypeslib.as_array(a.struct.vmf_n, (3,)).sum())
+    assert n == int(np.ctypeslib.as_array(b.struct.vmf_n, (3,)).sum())
+    for f in ("vmf_mu", "vmf_c", "vmf_alpha"):
+        assert np.array_equal(np.ctypeslib.as_array(getattr(a.struct, f), (n,)),
+                              np.ctypeslib.as_array(getattr(b.struct, f), (n,)))

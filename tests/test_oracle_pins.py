@@ -157,6 +157,7 @@ def _sym_err(u):
 
 
 @pytest.mark.parametrize("make,corr", [("reciprocal_far_3d", False), ("reciprocal_point_2d", False),
+                                       ("reciprocal_far_3d_vmf", False),
                                        ("reciprocal_far_3d", True), ("reciprocal_point_2d", True)])
 def test_cbs_reciprocity(oracle, make, corr):
     """Field CBS (NextEventEstimation.cuh:1212-1235, :1385-1391): with the views
@@ -316,3 +317,99 @@ def test_forced_inside_bin_weights_the_render(oracle):
     up = oracle.render(cf.prepare(plain, dims), 2)[0]
     assert not np.allclose(uf, up)
     assert np.abs(uf).sum() < np.abs(up).sum()
+
+
+def _vmf_cfg(mus, alphas, cs=None):
+    """3D scene with material 1 a vMF mixture (material 0 a mu = 0 lobe)."""
+    from tests.scenes import vmf_mixture
+    cfg, _ = wl.correlation_3d(n_side=2, n_lags=1)
+    cell = vmf_mixture(mus, alphas)
+    if cs is not None:
+        cell["mixtureC"] = np.asarray(cs, dtype=np.float64)
+    cfg["scattering"] = {"type": ["vMF", "vMF"], "amplitudeFunction": [vmf_mixture([0.0], [1.0]), cell]}
+    return cf.prepare(cfg, 3)
+
+
+@pytest.mark.parametrize("mus,alphas", [([0.0, 3.5, 22.0], [0.35, 0.45, 0.2]), ([1.0], [1.0]), ([0.5, 80.0], [0.9, 0.1])])
+def test_vmf_pdf_and_amplitude(oracle, mus, alphas):
+    """vMF mixture (Scattering.cuh:636-774, 933-1012), restated independently:
+    the amplitude is sum_k alpha_k exp(mu_k c + C_k), the pdf integrates to 1
+    over the sphere (all kappa >= 0) and is |amplitude|^2 over its integral."""
+    pc = _vmf_cfg(mus, alphas)
+    mu, al = np.asarray(mus), np.asarray(alphas)
+    C = np.log(0.28209479177387814) - mu
+    c = np.linspace(-1.0, 1.0, 40001)
+    vals = np.array([oracle.phase(pc, 1, float(x)) for x in c[::4]])
+    cs = c[::4]
+    amp_want = (al[None, :] * np.exp(mu[None, :] * cs[:, None] + C[None, :])).sum(axis=1)
+    assert np.allclose(vals[:, 0], amp_want, rtol=1e-12)
+    assert abs(2 * np.pi * np.trapezoid(vals[:, 1], cs) - 1.0) < 1e-4
+    a2 = vals[:, 0] ** 2
+    assert np.allclose(vals[:, 1], a2 / (2 * np.pi * np.trapezoid(a2, cs)), rtol=2e-4)
+
+
+def test_vmf_negative_kappa_takes_isotropic_normalisation(oracle):
+    """A pair with kappa < 1e-12 (here mu = -0.8 with itself) takes the isotropic
+    log normalisation -log(4 pi) (SpecialFunctions.cuh:187-203), so its pdf
+    integrates to sinh(|kappa|) / |kappa| rather than 1, as in the reference."""
+    pc = _vmf_cfg([-0.8], [1.0])
+    c = np.linspace(-1.0, 1.0, 20001)
+    pdf = np.array([oracle.phase(pc, 1, float(x))[1] for x in c])
+    k = 1.6
+    assert abs(2 * np.pi * np.trapezoid(pdf, c) - np.sinh(k) / k) < 1e-6
+
+
+@pytest.mark.parametrize("mus,alphas", [([0.0, 3.5, 22.0], [0.35, 0.45, 0.2]), ([0.5, 80.0], [0.9, 0.1])])
+def test_vmf_sampler_matches_pdf(oracle, mus, alphas):
+    """The walk samples a lobe pair by its weight and the lobe's cosine by the
+    exact inverse cdf: the cosines follow the pdf (chi^2 on 40 equal-mass bins)."""
+    pc = _vmf_cfg(mus, alphas)
+    n = 200000
+    x = oracle.sample_cos(pc, 1, 7, n).astype(np.float64)
+    assert np.all(np.abs(x) <= 1.0)
+    c = np.linspace(-1.0, 1.0, 400001)
+    pdf = np.array([oracle.phase(pc, 1, float(v))[1] for v in c[::20]])
+    cdf = np.concatenate([[0.0], np.cumsum(0.5 * (pdf[1:] + pdf[:-1]) * np.diff(c[::20]))]) * 2 * np.pi
+    edges = np.interp(np.linspace(0, 1, 41), cdf / cdf[-1], c[::20])
+    hist, _ = np.histogram(x, edges)
+    chi2 = np.sum((hist - n / 40) ** 2 / (n / 40))
+    assert chi2 < 90, chi2
+
+
+def test_vmf_scatters_isotropically_in_2d(oracle):
+    """In 2D the reference's vMF amplitude, pdf and sampler are the isotropic
+    ones (Scattering.cuh:899-905, 960-970, 1093-1100): the render equals the one
+    with an Isotropic material, bit for bit."""
+    from tests.scenes import vmf_2d
+    a = oracle.render(cf.prepare(*vmf_2d(True)), 3)[0]
+    b = oracle.render(cf.prepare(*vmf_2d(False)), 3)[0]
+    assert np.array_equal(a, b)
+
+
+def test_vmf_all_isotropic_refused(oracle):
+    """Every material isotropic with a vMF among them (all |mu| <= 1e-4) is
+    refused: the reference would give point sources the isotropic amplitude
+    and far-field sources the mixture's."""
+    from tests.scenes import field_point_3d, vmf_mixture
+    cfg, dims = field_point_3d()
+    cfg = dict(cfg, scattering={"type": ["vMF", "Isotropic", "HG"],
+                                "amplitudeFunction": [vmf_mixture([0.0, 5e-5], [1.0, 1.0]), 0.0, 0.0]})
+    with pytest.raises(Exception):
+        oracle.render(cf.prepare(cfg, dims), 1)
+    cfg["scattering"]["amplitudeFunction"][2] = 0.3   # one anisotropic material: accepted
+    oracle.render(cf.prepare(cfg, dims), 1)
+
+
+def test_vmf_config_validation():
+    """vMF cells need mixtureMu, mixtureC and mixtureAlpha of one length
+    (MatlabInterface.cu:827-868) and non-negative, not all zero, weights."""
+    from tests.scenes import field_point_3d
+    cfg, dims = field_point_3d()
+    bad = [{"mixtureMu": [1.0, 2.0], "mixtureC": [0.0], "mixtureAlpha": [1.0, 1.0]},
+           {"mixtureMu": [1.0], "mixtureC": [0.0]},
+           {"mixtureMu": [1.0], "mixtureC": [0.0], "mixtureAlpha": [-1.0]},
+           {"mixtureMu": [1.0], "mixtureC": [0.0], "mixtureAlpha": [0.0]}, 0.5]
+    for cell in bad:
+        c = dict(cfg, scattering={"type": ["HG", "vMF", "HG"], "amplitudeFunction": [0.1, cell, 0.2]})
+        with pytest.raises(cf.ConfigError):
+            cf.prepare(c, dims)
