@@ -324,6 +324,23 @@ def run_gpu(args, dist, rank, ws):
     roof = {"kernel": d["kernel"], "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"], "unit": d["unit"],
             "frac": d["frac"], "traffic": d["traffic"], "peak_source": pk_kind + " (" + d["peak_name"] + ")",
             "algorithmic_per_launch": d["algorithmic_per_launch"], "launches_per_step": chunks}
+    if dom == "ss" and m["correlation"]:
+        # ss_fast_kernel is bound by FP32 issue, not by HBM: its FP32 lane operations
+        # per (path, l, v) element are 6 (q^2) + 5 (pdf) + 1 (decay argument) per
+        # 8-tick chunk and 2 per tick (packed FMA into the tick sums, packed product
+        # for the next tick's decay) less one per chunk, plus 2 MUFU (rsqrt, ex2).
+        # Peak: the nominal FP32 lane rate, SMs x 128 lanes x the SM clock sampled
+        # during the timed region (a nominal figure, not a measured one).
+        import torch
+        tchunks = (Nt + 7) // 8
+        ops = float(P) * Nl * Nv * (11 * tchunks + 2 * Nt)
+        sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        lane_peak = sms * 128 * sm_mhz * 1e6 / 1e12
+        ach = ops / (mean["ms_contract_ss"] / 1000) / 1e12
+        roof["issue"] = {"unit": "FP32 lane-Tops/s", "achieved": ach, "peak": lane_peak, "frac": ach / lane_peak,
+                         "ops_per_element": 11 * tchunks + 2 * Nt, "mufu_per_element": 2 * tchunks,
+                         "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (sampled SM clock)"}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -59,7 +59,7 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
 //   vertices at their offsets.
 constexpr int kCount = 0, kWrite = 1, kSlots = 2;
 
-template <int MODE>
+template <int MODE, bool VMF>
 __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
     constexpr bool WRITE = MODE == kWrite;
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevSc
             sample_source(S, *fsrc, rs, o, d);
         } else {
             const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
-            d = sample_direction(S, mcur, din, rs);
+            d = sample_direction<VMF>(S, mcur, din, rs);
             o = cur;
         }
         V3 xn;
@@ -262,6 +262,9 @@ static int launch_scan(const WalkParams& W, cudaStream_t stream)
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 
+// the scene has vMF materials in 3D (their sampler tables are uploaded)
+static bool has_vmf(const DevScene& S) { return S.vmf_pf != nullptr; }
+
 int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
     const int threads = 128;
@@ -269,9 +272,11 @@ int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t strea
     if (W.slots) {
         if (cudaMemsetAsync(W.list_count, 0, sizeof(uint32_t), stream) != cudaSuccess
             || cudaMemsetAsync(W.ovf_count, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
-        walk_kernel<kSlots><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+        if (has_vmf(S)) walk_kernel<kSlots, true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+        else walk_kernel<kSlots, false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
     } else {
-        walk_kernel<kCount><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+        if (has_vmf(S)) walk_kernel<kCount, true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+        else walk_kernel<kCount, false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
     }
     if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
     return launch_scan(W, stream);
@@ -300,7 +305,8 @@ int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t strea
     Wn.next = W.next + 1;   // the write pass draws from the second counter (zeroed with the first)
     const uint32_t pool = W.list ? W.list_n : W.paths;
     if (pool == 0) return SSTMC_NO_ERROR;
-    walk_kernel<kWrite><<<walk_blocks(pool), threads, 0, stream>>>(S, Wn);
+    if (has_vmf(S)) walk_kernel<kWrite, true><<<walk_blocks(pool), threads, 0, stream>>>(S, Wn);
+    else walk_kernel<kWrite, false><<<walk_blocks(pool), threads, 0, stream>>>(S, Wn);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
 }
 

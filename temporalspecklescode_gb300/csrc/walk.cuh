@@ -104,38 +104,43 @@ __device__ __forceinline__ V3 random_direction(int dims, Stream& rs)
     return V3{ fm(st, cp), fm(st, sp), ct };
 }
 
+// vMF mixture cosine: a component pair j by the exclusive cdf of the pair
+// weights (Scattering.cuh:1065-1077), then the cosine of a vMF lobe of
+// concentration kappa_j.  The reference draws that cosine with Wood's
+// rejection loop (VectorType.cuh:169-203); here it is the exact inverse cdf of
+// the density ~ exp(kappa w) on [-1, 1]:
+// w = 1 + log(v + (1 - v) exp(-2 |kappa|)) / |kappa|, negated for kappa < 0.
+__device__ __forceinline__ float vmf_cosine(const DevScene& S, int m, Stream& rs)
+{
+    const float* pf = S.vmf_pf + 3 * S.vmf_poff[m];
+    const int P = S.vmf_n[m] * S.vmf_n[m];
+    const float u = rs.uniform();
+    int lo = 0, hi = P;   // pairs whose cdf is <= u
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(pf + 3 * mid) <= u) lo = mid + 1; else hi = mid;
+    }
+    const int j = lo > 0 ? lo - 1 : 0;
+    const float kap = __ldg(pf + 3 * j + 1), e2k = __ldg(pf + 3 * j + 2);
+    const float v = rs.uniform();
+    const float ak = fabsf(kap);
+    if (ak < 1e-4f) return fsb(fm(v, 2.0f), 1.0f);
+    const float w = fmaxf(-1.0f, fa(1.0f, fdv(walk_logf(fa(v, fm(fsb(1.0f, v), e2k))), ak)));
+    return kap < 0.0f ? -w : w;
+}
+
+// VMF: the scene has vMF materials (3D).  Without it the vMF branch is not
+// compiled, so scenes without vMF run the walk code they ran before vMF existed.
+template <bool VMF>
 __device__ inline V3 sample_direction(const DevScene& S, int m, const V3& din, Stream& rs)
 {
     const int ty = S.scat_type[m];
-    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR && ty != SSTMC_SCATTERING_VMF_MIXTURE)
+    if (ty != SSTMC_SCATTERING_HENYEY_GREENSTEIN && ty != SSTMC_SCATTERING_TABULAR && !(VMF && ty == SSTMC_SCATTERING_VMF_MIXTURE))
         return random_direction(S.dims, rs);
     const float g = S.g[m];
     float c;
-    if (ty == SSTMC_SCATTERING_VMF_MIXTURE) {
-        // a component pair j by the exclusive cdf of the pair weights
-        // (Scattering.cuh:1065-1077), then the cosine of a vMF lobe of
-        // concentration kappa_j.  The reference draws that cosine with Wood's
-        // rejection loop (VectorType.cuh:169-203); here it is the exact inverse
-        // cdf of the density ~ exp(kappa w) on [-1, 1]:
-        // w = 1 + log(v + (1 - v) exp(-2 |kappa|)) / |kappa|, negated for kappa < 0.
-        const float* pf = S.vmf_pf + 3 * S.vmf_poff[m];
-        const int P = S.vmf_n[m] * S.vmf_n[m];
-        const float u = rs.uniform();
-        int lo = 0, hi = P;   // pairs whose cdf is <= u
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(pf + 3 * mid) <= u) lo = mid + 1; else hi = mid;
-        }
-        const int j = lo > 0 ? lo - 1 : 0;
-        const float kap = __ldg(pf + 3 * j + 1), e2k = __ldg(pf + 3 * j + 2);
-        const float v = rs.uniform();
-        const float ak = fabsf(kap);
-        if (ak < 1e-4f) {
-            c = fsb(fm(v, 2.0f), 1.0f);
-        } else {
-            const float w = fmaxf(-1.0f, fa(1.0f, fdv(walk_logf(fa(v, fm(fsb(1.0f, v), e2k))), ak)));
-            c = kap < 0.0f ? -w : w;
-        }
+    if (VMF && ty == SSTMC_SCATTERING_VMF_MIXTURE) {
+        c = vmf_cosine(S, m, rs);
     } else if (ty == SSTMC_SCATTERING_TABULAR) {
         // inverse-cdf table entry round_num(xi N, N) (Scattering.cuh:1030-1037,
         // Simulation.cuh:287-298: nearest, ties to even, clamped to N - 1)
