@@ -317,6 +317,79 @@ def vmf_2d(vmf: bool = True, batch_size=64, full_iteration=2):
     return cfg, 2
 
 
+def one_path(correlation: bool):
+    """One path per wave, one illumination, one view, one tick."""
+    if correlation:
+        return wl.correlation_3d(batch_size=1, full_iteration=3, n_side=1, n_lags=1)
+    cfg, dims = wl.speckle_2d(batch_size=1, full_iteration=3, n_dirs=2)
+    cfg = dict(cfg)
+    cfg["illumination"] = {"type": "FarField", "direction": {"x": [0.2], "y": [0.98]}}
+    cfg["view"] = {"type": "FarField", "direction": {"x": [-0.1], "y": [0.995]}}
+    return cfg, dims
+
+
+def ragged_corr_3d(batch_size=40, full_iteration=2):
+    """The bench geometry with element and tick counts off every tile width:
+    33 illuminations, 65 views, 17 lags."""
+    cfg, dims = wl.correlation_3d(batch_size=batch_size, full_iteration=full_iteration, n_side=9, n_lags=17)
+    cfg = dict(cfg)
+    def cut(src, n):
+        loc = src["location"]
+        return {"type": "PointSource", "location": {k: np.asarray(v)[:n] for k, v in loc.items()}}
+    ill, view = cut(cfg["illumination"], 33), cut(cfg["view"], 65)
+    cfg.update(illumination=ill, illumination2=ill, view=view, view2=view)
+    return cfg, dims
+
+
+def mostly_misses_3d(batch_size=32, full_iteration=2):
+    """A point illumination 30 units from a small, thin box: about 99 % of the
+    first-vertex attempts miss, and every miss counts into iter."""
+    ill = {"type": "PointSource", "location": {"x": [0.0, 1.0], "y": [0.0, -1.0], "z": [-30.0, -30.0]}}
+    view = {"type": "PointSource", "location": {"x": [0.0, 3.0, -2.0], "y": [0.0, 1.0, 2.0], "z": [12.0, 12.0, 12.0]}}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 1.0, "seed": 9},
+        "scattering": {"type": ["HG", "HG"], "amplitudeFunction": [0.5, 0.5]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-5.0, 5.0], "yAxis": [-5.0, 5.0], "zAxis": [0.0, 5.0],
+                   "materialGrid": np.ones((1, 1, 1), dtype=np.uint32), "sigs": [0.0, 0.3], "siga": [0.0, 0.0]},
+        "illumination": ill, "view": view,
+        "sampler": {"type": "TemporalSampler", "t": [0.0], "D": [0.0, 0.0], "U": {"x": [0.0, 0.0], "y": [0.0, 0.0], "z": [0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
+def absorbing_2d(batch_size=64, full_iteration=2):
+    """Albedo 0.09: most paths end after their first vertex."""
+    cfg, dims = wl.speckle_2d(batch_size=batch_size, full_iteration=full_iteration, n_dirs=5)
+    cfg = dict(cfg)
+    cfg["medium"] = dict(cfg["medium"], sigs=[0.0, 0.3], siga=[0.0, 3.0])
+    return cfg, dims
+
+
+def ten_materials_2d(batch_size=64, full_iteration=2):
+    """All ten materials: a 5 x 4 grid of materials 1..9, HG of several g and
+    isotropic cells, Brownian motion in some, far-field sources."""
+    rng = np.random.default_rng(21)
+    grid = rng.integers(1, 10, size=(5, 4)).astype(np.uint32)
+    grid.ravel()[:9] = np.arange(1, 10)
+    types = ["HG", "HG", "Isotropic", "HG", "HG", "Isotropic", "HG", "HG", "Isotropic", "HG"]
+    amps = [0.0, 0.5, 0.0, -0.3, 0.9, 0.0, 0.1, 0.7, 0.0, 0.2]
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.9, "seed": 17},
+        "scattering": {"type": types, "amplitudeFunction": amps},
+        "medium": {"type": "Heterogeneous", "xAxis": np.linspace(-6, 6, 6), "yAxis": np.linspace(-5, 5, 5),
+                   "materialGrid": grid, "sigs": [0.0] + list(np.round(rng.uniform(0.3, 1.6, 9), 3)),
+                   "siga": [0.0] + list(np.round(rng.uniform(0.0, 0.1, 9), 3))},
+        "illumination": {"type": "FarField", "direction": wl._farfield_fan(4)},
+        "view": {"type": "FarField", "direction": wl._farfield_fan(3, 0.4)},
+        "sampler": {"type": "TemporalSampler", "t": [0.0, 1.5, 3.0],
+                    "D": [0.0, 0.0, 2e-3, 0.0, 1e-3, 0.0, 0.0, 4e-3, 0.0, 0.0],
+                    "U": {"x": [0.0] * 10, "y": [0.0] * 10}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -354,4 +427,10 @@ def small_scenes():
         "vmf_field_3d_cbs": with_cbs(with_vmf(field_point_3d())),
         "vmf_2d": vmf_2d(),
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
+        "edge_one_path_corr_3d": one_path(True),
+        "edge_one_path_field_2d": one_path(False),
+        "edge_ragged_corr_3d": ragged_corr_3d(),
+        "edge_mostly_misses_3d": mostly_misses_3d(),
+        "edge_absorbing_2d": absorbing_2d(),
+        "edge_ten_materials_2d": ten_materials_2d(),
     }

@@ -413,3 +413,21 @@ def test_vmf_config_validation():
         c = dict(cfg, scattering={"type": ["HG", "vMF", "HG"], "amplitudeFunction": [0.1, cell, 0.2]})
         with pytest.raises(cf.ConfigError):
             cf.prepare(c, dims)
+
+
+@pytest.mark.parametrize("make", ["mostly_misses_3d", "absorbing_2d"])
+def test_iter_counts_every_missed_attempt(oracle, make):
+    """iter = batchSize x fullIteration + the first-vertex attempts that missed
+    (MatlabInterface.cu:1796): the render's iter equals the paths plus the
+    per-path miss counts of the same paths, and a scene that mostly misses has
+    iter far above its path count."""
+    from tests import scenes
+    cfg, dims = getattr(scenes, make)()
+    pc = cf.prepare(cfg, dims)
+    u, it, st = oracle.render(pc, 5)
+    n = cfg["simulation"]["batchSize"] * cfg["simulation"]["fullIteration"]
+    tr = oracle.trace_paths(pc, 5, 0, n)
+    assert it == n + int(np.sum(tr["misses"]))
+    assert st["paths"] == n
+    if make == "mostly_misses_3d":
+        assert it > 50 * n

@@ -40,7 +40,8 @@ def test_server_rejects_null_handles():
 
 @pytest.mark.gpu
 def test_same_result_alone_and_in_the_mix(api):
-    names = ["speckle_2d", "correlation_3d", "transmission_matrix_3d", "corr_far_2d_drift", "field_point_3d", "mcx_3d"]
+    names = ["speckle_2d", "correlation_3d", "transmission_matrix_3d", "corr_far_2d_drift", "field_point_3d", "mcx_3d",
+             "vmf_transmission_3d", "forced_bin_2d_cbs", "tabular_corr_2d"]
     scenes = {n: api.Scene(*SCENES[n]) for n in names}
     big = api.Scene(*wl.correlation_3d(batch_size=8192, full_iteration=2, n_side=8, n_lags=8))
     try:
