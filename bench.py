@@ -325,10 +325,12 @@ def run_gpu(args, dist, rank, ws):
             "frac": d["frac"], "traffic": d["traffic"], "peak_source": pk_kind + " (" + d["peak_name"] + ")",
             "algorithmic_per_launch": d["algorithmic_per_launch"], "launches_per_step": chunks}
     if dom == "ss" and m["correlation"]:
-        # ss_fast_kernel is bound by FP32 issue, not by HBM: its FP32 lane operations
-        # per (path, l, v) element are 6 (q^2) + 5 (pdf) + 1 (decay argument) per
-        # 8-tick chunk and 2 per tick (packed FMA into the tick sums, packed product
-        # for the next tick's decay) less one per chunk, plus 2 MUFU (rsqrt, ex2).
+        # ss_fast_kernel is bound by FP32 issue, not by HBM: the algorithmic FP32 lane
+        # operations per (path, l, v) element are 6 (q^2) + 5 (pdf) + 1 (decay
+        # argument) per 8-tick chunk and 2 per tick (one product for the tick's decay
+        # power, one accumulation) less one per chunk, plus 2 MUFU (rsqrt, ex2).  The
+        # kernel issues 3 more products per chunk (a depth-3 product tree instead of
+        # a serial chain, for latency); those are not counted as work.
         # Peak: the nominal FP32 lane rate, SMs x 128 lanes x the SM clock sampled
         # during the timed region (a nominal figure, not a measured one).
         import torch

@@ -320,6 +320,13 @@ __device__ __forceinline__ unsigned long long mul2(unsigned long long a, unsigne
     return d;
 }
 
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 __device__ __forceinline__ float ex2_fast(float x)
 {
     float y;
@@ -476,12 +483,19 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 if (GEO) {
                     // e_t = e_s^(t + 1), e_s = exp(-c q^2 |t_0|): one ex2 per view, then a product chain
                     const unsigned long long es = ex2_2(arg);
-                    unsigned long long e = FIRST ? es : ex2_2(mul2(arg, pk2(start_scale, start_scale)));
-#pragma unroll
-                    for (int tt = 0; tt < kFt; ++tt) {
-                        acc[i][tt] = fma2(base, e, acc[i][tt]);
-                        if (tt + 1 < kFt) e = mul2(e, es);
-                    }
+                    const unsigned long long e = FIRST ? es : ex2_2(mul2(arg, pk2(start_scale, start_scale)));
+                    // the 8 terms base e es^k as a depth-3 product tree, summed with
+                    // packed adds: a serial chain of products (measured 5 % slower)
+                    // leaves the warps waiting on each product in turn
+                    static_assert(kFt == 8, "tick tree written for 8 ticks");
+                    const unsigned long long s2 = mul2(es, es), s4 = mul2(s2, s2);
+                    const unsigned long long b0 = mul2(base, e);
+                    const unsigned long long b1 = mul2(b0, es), b2 = mul2(b0, s2), b4 = mul2(b0, s4);
+                    const unsigned long long b3 = mul2(b1, s2), b5 = mul2(b1, s4), b6 = mul2(b2, s4), b7 = mul2(b3, s4);
+                    acc[i][0] = add2(acc[i][0], b0); acc[i][1] = add2(acc[i][1], b1);
+                    acc[i][2] = add2(acc[i][2], b2); acc[i][3] = add2(acc[i][3], b3);
+                    acc[i][4] = add2(acc[i][4], b4); acc[i][5] = add2(acc[i][5], b5);
+                    acc[i][6] = add2(acc[i][6], b6); acc[i][7] = add2(acc[i][7], b7);
                 } else {
 #pragma unroll
                     for (int tt = 0; tt < kFt; ++tt) {

@@ -582,12 +582,16 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                         if (geo) {
                             const unsigned long long as = mul2(ck, nt0);
                             const unsigned long long es = ex2_2(as);
-                            unsigned long long e = mul2(wgt, ex2_2(add2(tl, t0 == 0 ? as : mul2(as, st0))));
-#pragma unroll
-                            for (int k = 0; k < kNT; ++k) {
-                                acc[P][k] = add2(acc[P][k], e);
-                                if (k + 1 < kNT) e = mul2(e, es);
-                            }
+                            const unsigned long long e = mul2(wgt, ex2_2(add2(tl, t0 == 0 ? as : mul2(as, st0))));
+                            // e es^k for the pass's 8 ticks as a depth-3 product tree
+                            // rather than a serial chain of products
+                            static_assert(kNT == 8, "tick tree written for 8 ticks");
+                            const unsigned long long s2 = mul2(es, es), s4 = mul2(s2, s2);
+                            const unsigned long long e1 = mul2(e, es), e2 = mul2(e, s2), e3 = mul2(e1, s2);
+                            acc[P][0] = add2(acc[P][0], e); acc[P][1] = add2(acc[P][1], e1);
+                            acc[P][2] = add2(acc[P][2], e2); acc[P][3] = add2(acc[P][3], e3);
+                            acc[P][4] = add2(acc[P][4], mul2(e, s4)); acc[P][5] = add2(acc[P][5], mul2(e1, s4));
+                            acc[P][6] = add2(acc[P][6], mul2(e2, s4)); acc[P][7] = add2(acc[P][7], mul2(e3, s4));
                         } else {
 #pragma unroll
                             for (int k = 0; k < kNT; ++k) {
