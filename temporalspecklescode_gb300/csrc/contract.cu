@@ -476,9 +476,11 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 }
                 const unsigned long long q2 = pk2(q2s[0], q2s[1]);
                 const unsigned long long dn = fma2(g2, q2, omg);
+                // the row factors' product does not wait for the rsqrt; r^3 w as
+                // (r r)(r w), two levels of products after it
+                const unsigned long long w = mul2(ob, ib.y);
                 const unsigned long long r = pk2(rsqrt_fast(pk_lo(dn)), rsqrt_fast(pk_hi(dn)));
-                const unsigned long long rr = mul2(r, r);
-                const unsigned long long base = mul2(mul2(THREE ? mul2(rr, r) : rr, ob), ib.y);
+                const unsigned long long base = THREE ? mul2(mul2(r, r), mul2(r, w)) : mul2(mul2(r, r), w);
                 const unsigned long long arg = mul2(cn2, q2);
                 if (GEO) {
                     // e_t = e_s^(t + 1), e_s = exp(-c q^2 |t_0|): one ex2 per view, then a product chain

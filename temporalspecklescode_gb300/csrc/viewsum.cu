@@ -566,16 +566,18 @@ __global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevSc
                         const unsigned long long qy = fma2(oy, neg1, r2.x);
                         const unsigned long long qz = THREE ? fma2(oz, neg1, r2.y) : 0ull;
                         const unsigned long long q2 = fma2(qx, qx, THREE ? fma2(qy, qy, mul2(qz, qz)) : mul2(qy, qy));
-                        const unsigned long long rr = rsqrt_2(fma2(r4.x, q2, r4.y));
-                        unsigned long long wgt = mul2(mul2(rr, rr), r5.x);
-                        if (THREE) wgt = mul2(wgt, rr);
+                        // factors that do not wait for the rsqrt first, then r^(D-1) c
+                        // as (r r)(r c) (3D): two levels of products after the rsqrt
+                        unsigned long long cf = r5.x;
                         if constexpr (VWP) {
-                            wgt = mul2(wgt, THREE ? mul2(ri, ri) : ri);
+                            cf = mul2(cf, THREE ? mul2(ri, ri) : ri);
                             if (area) {
                                 const unsigned long long oa = THREE ? oz : oy;
-                                wgt = mul2(wgt, pk2(fabsf(pk_lo(oa)), fabsf(pk_hi(oa))));
+                                cf = mul2(cf, pk2(fabsf(pk_lo(oa)), fabsf(pk_hi(oa))));
                             }
                         }
+                        const unsigned long long rr = rsqrt_2(fma2(r4.x, q2, r4.y));
+                        const unsigned long long wgt = THREE ? mul2(mul2(rr, rr), mul2(rr, cf)) : mul2(mul2(rr, rr), cf);
                         // decorrelation exponent C = D_b |q|^2 + MT_b, exp(-tau) folded into the first factor
                         const unsigned long long ck = fma2(r3.x, q2, r3.y);
                         const unsigned long long tl = mul2(tau2, nl2e);
