@@ -60,7 +60,7 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
 constexpr int kCount = 0, kWrite = 1, kSlots = 2;
 
 template <int MODE, bool VMF>
-__global__ void __launch_bounds__(128) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
+__global__ void __launch_bounds__(128, 7) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
     constexpr bool WRITE = MODE == kWrite;
     constexpr bool COUNTS = MODE != kWrite;

@@ -318,7 +318,7 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
 // One warp per path (a kernel of its own: it needs few registers, so many
 // warps hide the latency of its row writes).
 template <int NLK, bool ILP, bool VWP, bool SINGLE>
-__global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+__global__ void __launch_bounds__(128, 8) illum_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(128) illum_kernel(const __grid_constant__ DevS
 }
 
 template <bool CORR, bool VWP, bool SINGLE, bool THREE>
-__global__ void __launch_bounds__(128) view_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+__global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     extern __shared__ __align__(16) unsigned char vsm[];
     constexpr size_t kRecBytes = CORR ? sizeof(CRec) : sizeof(VRec);
