@@ -203,10 +203,10 @@ def run_reference(args, dist, rank, ws):
 # every class streams per-path rows, so a launch's traffic scales with the
 # paths it processes.
 NCU_DRAM_BYTES_PER_PATH = {
-    "nee": (8356096 + 157391360 + 14813440 + 72855296) / 65536,   # illum_kernel + view_kernel
-    "walk": (241664 + 178944 + 18748672 + 1536) / 65536,          # walk_kernel<slots> + compact_kernel
-    "gemm": (269216256 + 3438592) / 65536,                         # gemm_tc_kernel (real rows)
-    "ss": (68522752 + 984320) / 65536,                             # ss_fast_kernel
+    "nee": (8354816 + 156937728 + 14934272 + 75123456) / 65536,   # illum_kernel + view_kernel
+    "walk": (242688 + 176896 + 18749184 + 1536) / 65536,          # walk_kernel<slots> + compact_kernel
+    "gemm": (269205504 + 3310592) / 65536,                         # gemm_tc_kernel (real rows)
+    "ss": (68522752 + 932352) / 65536,                             # ss_fast_kernel
 }
 
 
