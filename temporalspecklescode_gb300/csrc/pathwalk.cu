@@ -58,9 +58,12 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
 // MODE kWrite: replay paths (all, or the W.list of long ones) and write their
 //   vertices at their offsets.
 constexpr int kCount = 0, kWrite = 1, kSlots = 2;
+// resident walk blocks of 128 threads per SM (72 registers): the launch bound
+// and the persistent grid's size
+constexpr int kWalkBlocksPerSM = 7;
 
 template <int MODE, bool VMF>
-__global__ void __launch_bounds__(128, 7) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
+__global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
     constexpr bool WRITE = MODE == kWrite;
     constexpr bool COUNTS = MODE != kWrite;
@@ -243,13 +246,13 @@ __global__ void scan_add_kernel(uint32_t* offsets, const uint32_t* block_sums, u
 
 static int walk_blocks(uint32_t paths)
 {
-    // about 4 paths per thread, at most 8 resident blocks of 128 threads per SM
+    // about 4 paths per thread, at most one wave of resident blocks
     // (threads draw paths from the shared counter until the pool is empty)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint32_t want = (paths + 4 * 128 - 1) / (4 * 128);
-    const uint32_t cap = (uint32_t)sms * 8;
+    const uint32_t cap = (uint32_t)sms * kWalkBlocksPerSM;
     return (int)std::max<uint32_t>(1, std::min(want, cap));
 }
 
