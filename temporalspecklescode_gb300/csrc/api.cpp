@@ -378,7 +378,7 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     launches++;
     if (timing) cudaEventRecord(ev[3], stream);
     // far-field x far-field: per-material weight tables on the tensor-core GEMM
-    // (real amplitudes; a tabular material's are complex and take ss_kernel)
+    // (HG / isotropic amplitudes; tabular and vMF ones come from an FP64 angle in ss_kernel)
     const bool farfar = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD && !S.dev.has_amp64;
     if (farfar) {
         e = prepare_ss_tables(S);

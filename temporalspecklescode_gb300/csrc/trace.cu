@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             // multiple-scattering illumination vector at x2 (NEE.cuh:1525-1559, 889-1009)
             if (b == 2 && T.pass0) {
                 const V3 x12 = funit(sub3(xn, x1));
-                // tabular first material: complex amplitudes from an FP64 angle (nee.cuh)
+                // tabular or vMF first material: amplitudes and pdf from an FP64 angle (nee.cuh)
                 const bool tab1 = is_amp64(S, m1);
                 float ps = 0.0f;
                 if (tab1) {
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                         const V3 qv = V3{ 0.5f * (i1.x + i2.x) - x12.x, 0.5f * (i1.y + i2.y) - x12.y, 0.5f * (i1.z + i2.z) - x12.z };
                         const float c1k = c1base * dot3(qv, qv);
                         float f12s = 0.0f;
-                        // tabular: u1 amplitude x conj(u2 amplitude), complex unless u1 == u2
+                        // tabular / vMF: u1 amplitude x conj(u2 amplitude), complex unless u1 == u2
                         auto f12tab = [&](const V3& pa, const V3& pb) {
                             const float2 f1 = amp64(S, m1, f3_cos64(il, l, pa, pb, false));
                             if (S.sym) return make_float2(f1.x * f1.x + f1.y * f1.y, 0.f);
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     if (realv) { w = gweight<VWP>(S, vw, v, xn, kRoleView, sts); sts *= 2; }
                     else if (stn) { g1s = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts); g2s = gcomplex<VWP>(S, vw2, v, xn, kRoleView, sts); }
                     float f12s = 0.0f;
-                    // tabular: u1 amplitude x conj(u2 amplitude), the view attached at x_b
+                    // tabular / vMF: u1 amplitude x conj(u2 amplitude), the view attached at x_b
                     auto f12tab = [&](const V3& pa, const V3& pb) {
                         const float2 f1 = amp64(S, mn, f3_cos64(vw, v, pa, pb, true));
                         if (S.sym) return make_float2(f1.x * f1.x + f1.y * f1.y, 0.f);
@@ -661,7 +661,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 auto fx = [&](int e, const V3& pa, const V3& pb, int m) {
                     return T.cbs ? fillum_exit<ILP>(S, il, e, pa, pb, m) : fview<VWP>(S, vw, e, pa, pb, m);
                 };
-                // tabular vertex material: complex amplitude, the source attached at x_b
+                // tabular or vMF vertex material: FP64-angle amplitude, the source attached at x_b
                 const bool tabn = is_amp64(S, mn);
                 auto fxc = [&](int e, const V3& pa, const V3& pb) {
                     return amp64(S, mn, T.cbs ? f3_cos64(il, e, pa, pb, false) : f3_cos64(vw, e, pa, pb, true));

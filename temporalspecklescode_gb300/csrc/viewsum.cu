@@ -722,7 +722,7 @@ int view_max_views(const DevScene& S) { return S.correlation ? 64 * kVPP : 32 * 
 
 bool view_kernel_covers(const DevScene& S, const bool* moving_any)
 {
-    if (S.has_amp64) return false;   // complex tabular amplitudes: trace_kernel
+    if (S.has_amp64) return false;   // tabular / vMF amplitudes from an FP64 angle: trace_kernel
     if (S.correlation) return S.sym && S.all_static_corr;
     return !*moving_any;
 }

@@ -298,6 +298,20 @@ def vmf_corr_3d(batch_size=96, full_iteration=2):
     return cfg, dims
 
 
+def vmf_corr_drift_3d(batch_size=64, full_iteration=2):
+    """Correlation sampler, 3D, vMF mixtures, drift U != 0 and u2 illuminations
+    shifted from u1: the complex route (u1 amplitude x conj(u2 amplitude))."""
+    cfg, dims = vmf_corr_3d(batch_size=batch_size, full_iteration=full_iteration)
+    cfg = dict(cfg)
+    ill = cfg["illumination"]
+    loc = {k: np.asarray(v, dtype=np.float64) for k, v in ill["location"].items()}
+    cfg["illumination2"] = {"type": "PointSource", "location": {"x": loc["x"] + 3.0, "y": loc["y"], "z": loc["z"]}}
+    cfg["scattering"] = {"type": ["vMF", "vMF"],
+                         "amplitudeFunction": [vmf_mixture([0.0], [1.0]), vmf_mixture(*VMF_TWO_SIDED)]}
+    cfg["sampler"] = dict(cfg["sampler"], U={"x": [0.0, 0.4], "y": [0.0, -0.2], "z": [0.0, 0.1]})
+    return cfg, dims
+
+
 def vmf_2d(vmf: bool = True, batch_size=64, full_iteration=2):
     """2D far-field field scene with a vMF material next to an HG one: the
     reference scatters a 2D vMF material isotropically."""
@@ -426,6 +440,7 @@ def small_scenes():
         "vmf_corr_3d": vmf_corr_3d(),
         "vmf_field_3d_cbs": with_cbs(with_vmf(field_point_3d())),
         "vmf_2d": vmf_2d(),
+        "vmf_corr_drift_3d": vmf_corr_drift_3d(),
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
         "edge_one_path_corr_3d": one_path(True),
         "edge_one_path_field_2d": one_path(False),
