@@ -115,10 +115,11 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
            && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' path counter
            && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
-           && alloc((void**)&ovf, (size_t)walk_overflow_blocks(paths) * kWalkSlotVerts * sizeof(float4))
-           && alloc((void**)&ovf_owner, (size_t)walk_overflow_blocks(paths) * sizeof(uint2))
+           && alloc((void**)&ovf, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * kWalkSlotVerts * sizeof(float4))
+           && alloc((void**)&ovf_owner, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * sizeof(uint2))
            && alloc((void**)&p2v, paths * sizeof(float));
     if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
+    ovf_blocks = std::max(walk_overflow_blocks(paths), ovf_want);
     cap = paths;
     return SSTMC_NO_ERROR;
 }
@@ -225,7 +226,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     // the rest in overflow blocks; paths that found the pool empty are
     // listed for a replay
     Wp.slots = slots; Wp.list = longq; Wp.list_count = reinterpret_cast<uint32_t*>(vtotal + 2);
-    Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_count = Wp.list_count + 1; Wp.ovf_cap = walk_overflow_blocks(n);
+    Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_count = Wp.list_count + 1; Wp.ovf_cap = ovf_blocks;
     int e = launch_walk_count(S.dev, Wp, stream);
     if (e) return e;
     launches += 4;
@@ -256,6 +257,21 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         e = launch_walk_write(S.dev, Wp, stream);
         if (e) return e;
         launches++;
+    }
+    // The pool ran short (long paths: every path past its slot takes a block per
+    // 64 vertices); this chunk was completed by the replay.  Grow the pool for the
+    // next chunks and renders: a path of B vertices takes at most ceil(B / 64) - 1
+    // blocks, so the chunk's vertex count / 64 plus the default share suffices.
+    if (novf > Wp.ovf_cap && !fixed) {
+        const uint64_t want = std::min<uint64_t>(nverts / kWalkSlotVerts + walk_overflow_blocks(n), 1u << 30);
+        cudaFreeAsync(ovf, stream);
+        cudaFreeAsync(ovf_owner, stream);
+        ovf = nullptr; ovf_owner = nullptr; ovf_blocks = 0;
+        if (cudaMallocAsync((void**)&ovf, (size_t)want * kWalkSlotVerts * sizeof(float4), stream) != cudaSuccess
+            || cudaMallocAsync((void**)&ovf_owner, (size_t)want * sizeof(uint2), stream) != cudaSuccess)
+            return SSTMC_ALLOCATION_ERROR;
+        ovf_blocks = (uint32_t)want;
+        ovf_want = std::max(ovf_want, (uint32_t)want);
     }
     if (timing && ev[6]) cudaEventRecord(ev[6], stream);
 

@@ -34,6 +34,8 @@ struct Engine {
     float4* slots = nullptr;      // single-pass walk: first 64 vertices of each path of a chunk
     uint32_t* longq = nullptr;    // paths of the chunk that found the overflow pool empty
     float4* ovf = nullptr;        // overflow blocks of 64 vertices (pathwalk.cu)
+    uint32_t ovf_blocks = 0;      // overflow blocks allocated
+    uint32_t ovf_want = 0;        // learned pool size: a chunk that found the pool short grows it
     float* p2v = nullptr;         // [paths] second-point probability (correlation CBS)
     uint2* ovf_owner = nullptr;
     float4* verts = nullptr;

@@ -404,6 +404,16 @@ def ten_materials_2d(batch_size=64, full_iteration=2):
     return cfg, 2
 
 
+def very_long_paths_2d(batch_size=256, full_iteration=2):
+    """Optically thick, nearly non-absorbing 2D medium: paths of hundreds of
+    vertices, far past the walk's 64-vertex slots and its default overflow pool."""
+    cfg, dims = wl.speckle_2d(batch_size=batch_size, full_iteration=full_iteration, n_dirs=3)
+    cfg = dict(cfg)
+    cfg["medium"] = dict(cfg["medium"], sigs=[0.0, 4.0], siga=[0.0, 0.002])
+    cfg["scattering"] = {"type": ["HG", "HG"], "amplitudeFunction": [0.3, 0.3]}
+    return cfg, dims
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -441,6 +451,7 @@ def small_scenes():
         "vmf_field_3d_cbs": with_cbs(with_vmf(field_point_3d())),
         "vmf_2d": vmf_2d(),
         "vmf_corr_drift_3d": vmf_corr_drift_3d(),
+        "edge_very_long_paths_2d": very_long_paths_2d(),
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
         "edge_one_path_corr_3d": one_path(True),
         "edge_one_path_field_2d": one_path(False),

@@ -236,3 +236,23 @@ def test_vmf_all_isotropic_refused(api):
     with pytest.raises(api.SstmcError) as ei:
         api.Scene(cfg, dims)
     assert ei.value.code == 5
+
+
+def test_walk_overflow_pool_grows(api, oracle):
+    """Paths of hundreds of vertices exhaust the walk's default overflow pool:
+    the first render completes them through the replay pass and grows the pool,
+    the second (same seed) keeps every path in the grown pool.  Both renders are
+    identical and match the oracle."""
+    from tests.scenes import very_long_paths_2d
+    cfg, dims = very_long_paths_2d()
+    with api.Scene(cfg, dims) as s:
+        u1, it1 = s.render(seed=31)
+        st1 = s.stats()
+        u2, it2 = s.render(seed=31)
+        st2 = s.stats()
+    assert np.array_equal(u1, u2) and np.array_equal(it1, it2)
+    # far past the 64-vertex slots: the default pool (paths / 16 + 64 blocks) runs dry
+    assert st1["vertices"] == st2["vertices"] and st1["vertices"] > 100 * st1["paths"]
+    uo, ito, sto = oracle.render(cf.prepare(cfg, dims), 31)
+    assert it1[0] == ito and st1["vertices"] == sto["vertices"]
+    assert rel_fro(u1[..., 0], uo) <= REL_TOL
