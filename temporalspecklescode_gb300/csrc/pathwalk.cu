@@ -313,9 +313,10 @@ int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t strea
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
 }
 
-// One overflow block per 16 paths: paths longer than a slot are rare (about
-// 1 % at a mean of 14 vertices per path), so the pool runs dry only for
-// heavy-tailed scenes, whose overflowing paths then take the write pass.
+// Default pool: one overflow block per 16 paths.  Paths longer than a slot
+// are rare at a mean of 14 vertices per path (about 1 %); scenes with long
+// paths find the pool short, their overflowing paths take the write pass, and
+// the engine then grows the pool for its next chunks (api.cpp, trace_chunk).
 uint32_t walk_overflow_blocks(uint32_t paths) { return paths / 16 + 64; }
 
 size_t walk_slot_bytes_per_path()

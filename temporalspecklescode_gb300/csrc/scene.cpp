@@ -471,6 +471,8 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     }
     D.inv_lambda = 1.0 / cfg->lambda;
     D.inv_lambda_f = (float)D.inv_lambda;
+    D.il_h = D.inv_lambda_f;
+    D.il_l = (float)(D.inv_lambda - (double)D.il_h);
     D.k2 = (float)((2.0 * kPi / cfg->lambda) * (2.0 * kPi / cfg->lambda));
 
     // upload

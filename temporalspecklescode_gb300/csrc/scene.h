@@ -69,6 +69,7 @@ struct DevScene {
     const float* abs_ticks;      // [Nt]
     double inv_lambda;
     float inv_lambda_f;
+    float il_h, il_l;            // 1 / lambda as a float pair (hi + lo) for float-float phases
     float k2;                    // (2 pi / lambda)^2
     float iso_amp, iso_pdf;
     DevSource src[4];            // illumination, view, illumination2, view2
