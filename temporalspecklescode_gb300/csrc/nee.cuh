@@ -42,6 +42,61 @@ __device__ __forceinline__ float2 unit_phase(float f)
 // reduce a phase measured in cycles: FP64 in the split form, FP32 in the plain form
 __device__ __forceinline__ float frac_cycles(double ph) { return (float)(ph - rint(ph)); }
 
+// ---- float-float phases (split precision) ----
+// GB300 runs FP64 at a small fraction of the FP32 rate, and the field
+// sampler needs a phase per (vertex, view): the phase of a far-field view
+// o . x / lambda or of a point view |v - x| / lambda, modulo 1, to about
+// 1e-7 cycles at positions of up to ~1e5 wavelengths.  It is formed from
+// exact FP32 products and sums (FMA error terms, two-sums: Dekker / Knuth
+// error-free transformations), about 2^-48 relative, in FP32 instructions.
+// Every product and sum is explicitly rounded, so nothing is fused.
+struct FF { float h, l; };
+__device__ __forceinline__ FF two_sum(float a, float b)
+{
+    const float s = fa(a, b), bb = fsb(s, a);
+    return FF{ s, fa(fsb(a, fsb(s, bb)), fsb(b, bb)) };
+}
+__device__ __forceinline__ FF two_prod(float a, float b)
+{
+    const float p = fm(a, b);
+    return FF{ p, __fmaf_rn(a, b, -p) };
+}
+// a . b (three products) as a float pair
+__device__ __forceinline__ FF dot_ff(const V3& a, const V3& b)
+{
+    const FF p0 = two_prod(a.x, b.x), p1 = two_prod(a.y, b.y), p2 = two_prod(a.z, b.z);
+    const FF s1 = two_sum(p0.h, p1.h), s2 = two_sum(s1.h, p2.h);
+    return FF{ s2.h, fa(fa(fa(s1.l, s2.l), fa(p0.l, p1.l)), p2.l) };
+}
+// x (a float pair) times 1 / lambda (a float pair)
+__device__ __forceinline__ FF scale_ff(const FF& x, float ih, float il)
+{
+    const FF p = two_prod(x.h, ih);
+    return FF{ p.h, fa(p.l, fa(fm(x.h, il), fm(x.l, ih))) };
+}
+// (ph + t) mod 1 in [-1/2, 1/2], ph and t float pairs (|ph| <= 1/2)
+__device__ __forceinline__ float frac_ff(float ph_h, float ph_l, const FF& t)
+{
+    const float k = rintf(t.h);
+    const float f = fa(fa(ph_h, fsb(t.h, k)), fa(ph_l, t.l));   // t.h - k is exact
+    return fsb(f, rintf(f));
+}
+// |v - x| (float pair): exact differences, a float-pair sum of squares and
+// one Newton correction of the FP32 square root
+__device__ __forceinline__ FF dist_ff(const V3& v, const V3& x)
+{
+    const FF dx = two_sum(v.x, -x.x), dy = two_sum(v.y, -x.y), dz = two_sum(v.z, -x.z);
+    const FF qx = two_prod(dx.h, dx.h), qy = two_prod(dy.h, dy.h), qz = two_prod(dz.h, dz.h);
+    const FF s1 = two_sum(qx.h, qy.h), s2 = two_sum(s1.h, qz.h);
+    const float cross = fm(2.0f, fa(fa(fm(dx.h, dx.l), fm(dy.h, dy.l)), fm(dz.h, dz.l)));
+    const float sl = fa(fa(fa(s1.l, s2.l), fa(fa(qx.l, qy.l), qz.l)), cross);
+    const float r0 = __fsqrt_rn(s2.h);
+    if (!(r0 > 0.0f)) return FF{ 0.0f, 0.0f };
+    const FF r2 = two_prod(r0, r0);
+    const float res = fa(fsb(fsb(s2.h, r2.h), r2.l), sl);
+    return FF{ r0, __fdiv_rn(res, fm(2.0f, r0)) };
+}
+
 __device__ __forceinline__ float amp_dirs(const DevScene& S, int m, const V3& a, const V3& b)
 {
     const int ty = S.scat_type[m];
@@ -288,8 +343,8 @@ __device__ inline float2 gvec(const DevScene& S, const DevSource& s, int k, cons
         if (!with_phase) return make_float2(a, 0.0f);
         float f;
         if (S.precision == SSTMC_PRECISION_SPLIT) {
-            const double dx = fma((double)d.x, (double)x.x, fma((double)d.y, (double)x.y, (double)d.z * (double)x.z));
-            f = frac_cycles((role == kRoleIllum ? dx : -dx) * S.inv_lambda);
+            const FF t = scale_ff(dot_ff(d, x), S.il_h, S.il_l);
+            f = role == kRoleIllum ? frac_ff(0.0f, 0.0f, t) : frac_ff(0.0f, 0.0f, FF{ -t.h, -t.l });
         } else {
             const float dx = d.x * x.x + d.y * x.y + d.z * x.z;
             const float ph = (role == kRoleIllum ? dx : -dx) * S.inv_lambda_f;
@@ -300,12 +355,11 @@ __device__ inline float2 gvec(const DevScene& S, const DevSource& s, int k, cons
     const V3 sp = load3(s.p, k);
     const V3 dir = normalize32(S.dims, V3{ fsb(sp.x, x.x), fsb(sp.y, x.y), fsb(sp.z, x.z) });
     const float T = expf(-dda(S, x, dir, steps));
-    double r = 0.0;
+    FF r{ 0.0f, 0.0f };
     float rf;
     if (S.precision == SSTMC_PRECISION_SPLIT) {
-        const double dx = (double)x.x - (double)sp.x, dy = (double)x.y - (double)sp.y, dz = (double)x.z - (double)sp.z;
-        r = sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
-        rf = (float)r;
+        r = dist_ff(sp, x);
+        rf = r.h;
     } else {
         const V3 v = sub3(x, sp);
         rf = sqrtf(dot3(v, v));
@@ -315,7 +369,7 @@ __device__ inline float2 gvec(const DevScene& S, const DevSource& s, int k, cons
     const float a = sqrtf(at);
     if (!with_phase) return make_float2(a, 0.0f);
     float f;
-    if (S.precision == SSTMC_PRECISION_SPLIT) f = frac_cycles(r * S.inv_lambda);
+    if (S.precision == SSTMC_PRECISION_SPLIT) f = frac_ff(0.0f, 0.0f, scale_ff(r, S.il_h, S.il_l));
     else { const float ph = rf * S.inv_lambda_f; f = ph - rintf(ph); }
     return c_scale(unit_phase(f), a);
 }

@@ -311,9 +311,10 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     double* Ls = smem_d + (size_t)wib * Nt;
     float2* accs = reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)wib * T.slots * 32 + lane;
     float* fbase = reinterpret_cast<float*>(reinterpret_cast<float2*>(smem_d + (size_t)nwb * Nt) + (size_t)nwb * T.slots * 32);
-    float* bufA = fbase + (size_t)wib * 8 * Nt;
+    float* bufA = fbase + (size_t)wib * 9 * Nt;
     float* bufB = bufA + 4 * Nt;
-    float* tk_abs = fbase + (size_t)nwb * 8 * Nt;   // block-wide copies of |t| and t
+    float* phs = bufA + 8 * Nt;   // field: the path phase L_t / lambda + xi_b mod 1 of the current vertex per tick
+    float* tk_abs = fbase + (size_t)nwb * 9 * Nt;   // block-wide copies of |t| and t
     float* tk_raw = tk_abs + Nt;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) { tk_abs[t] = S.abs_ticks[t]; tk_raw[t] = S.ticks_f[t]; }
     __syncthreads();
@@ -467,9 +468,12 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     if (split) {
                         const double dx = (double)c.x - (double)a.x, dy = (double)c.y - (double)a.y, dz = (double)c.z - (double)a.z;
                         Ls[t] += sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+                        phs[t] = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
                     } else {
                         const V3 dd = sub3(c, a);
                         Ls[t] = (double)((float)Ls[t] + sqrtf(dot3(dd, dd)));
+                        const float ph = (float)Ls[t] * S.inv_lambda_f + xin;
+                        phs[t] = ph - rintf(ph);
                     }
                 }
                 __syncwarp();
@@ -678,9 +682,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                         float2 g = gs;
                         if (stn) steps += sts;
                         else g = gx(v, tick_pos(xtn, t), steps);
-                        float fr;
-                        if (split) fr = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
-                        else { const float ph = (float)Ls[t] * S.inv_lambda_f + xin; fr = ph - rintf(ph); }
+                        const float fr = phs[t];
                         float2 c;
                         if (tabn) {
                             const float2 f = stf ? fsc : fxc(v, tick_pos(xtn, t), tick_pos(xtc, t));
@@ -921,7 +923,7 @@ size_t trace_smem_bytes(int Nt, int slots, int threads)
 {
     const int warps = threads / 32;
     return (size_t)warps * Nt * sizeof(double) + (size_t)warps * slots * 32 * sizeof(float2)
-         + (size_t)warps * 8 * Nt * sizeof(float) + 2 * (size_t)Nt * sizeof(float);
+         + (size_t)warps * 9 * Nt * sizeof(float) + 2 * (size_t)Nt * sizeof(float);
 }
 
 using TraceFn = void (*)(DevScene, TraceParams);

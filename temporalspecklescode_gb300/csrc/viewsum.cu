@@ -48,60 +48,6 @@ struct VRec {
     float ph_h, ph_l;       // field: L_b / lambda + xi_b reduced to [-1/2, 1/2] cycles, as a float pair
 };
 
-// ---- float-float phases (split precision, field sampler) ----
-// GB300 runs FP64 at a small fraction of the FP32 rate, and the field
-// sampler needs a phase per (vertex, view): the phase of a far-field view
-// o . x / lambda or of a point view |v - x| / lambda, modulo 1, to about
-// 1e-7 cycles at positions of up to ~1e5 wavelengths.  It is formed from
-// exact FP32 products and sums (FMA error terms, two-sums: Dekker / Knuth
-// error-free transformations), about 2^-48 relative, in FP32 instructions.
-// Every product and sum is explicitly rounded, so nothing is fused.
-struct FF { float h, l; };
-__device__ __forceinline__ FF two_sum(float a, float b)
-{
-    const float s = fa(a, b), bb = fsb(s, a);
-    return FF{ s, fa(fsb(a, fsb(s, bb)), fsb(b, bb)) };
-}
-__device__ __forceinline__ FF two_prod(float a, float b)
-{
-    const float p = fm(a, b);
-    return FF{ p, __fmaf_rn(a, b, -p) };
-}
-// a . b (three products) as a float pair
-__device__ __forceinline__ FF dot_ff(const V3& a, const V3& b)
-{
-    const FF p0 = two_prod(a.x, b.x), p1 = two_prod(a.y, b.y), p2 = two_prod(a.z, b.z);
-    const FF s1 = two_sum(p0.h, p1.h), s2 = two_sum(s1.h, p2.h);
-    return FF{ s2.h, fa(fa(fa(s1.l, s2.l), fa(p0.l, p1.l)), p2.l) };
-}
-// x (a float pair) times 1 / lambda (a float pair)
-__device__ __forceinline__ FF scale_ff(const FF& x, float ih, float il)
-{
-    const FF p = two_prod(x.h, ih);
-    return FF{ p.h, fa(p.l, fa(fm(x.h, il), fm(x.l, ih))) };
-}
-// (ph + t) mod 1 in [-1/2, 1/2], ph and t float pairs (|ph| <= 1/2)
-__device__ __forceinline__ float frac_ff(float ph_h, float ph_l, const FF& t)
-{
-    const float k = rintf(t.h);
-    const float f = fa(fa(ph_h, fsb(t.h, k)), fa(ph_l, t.l));   // t.h - k is exact
-    return fsb(f, rintf(f));
-}
-// |v - x| (float pair): exact differences, a float-pair sum of squares and
-// one Newton correction of the FP32 square root
-__device__ __forceinline__ FF dist_ff(const V3& v, const V3& x)
-{
-    const FF dx = two_sum(v.x, -x.x), dy = two_sum(v.y, -x.y), dz = two_sum(v.z, -x.z);
-    const FF qx = two_prod(dx.h, dx.h), qy = two_prod(dy.h, dy.h), qz = two_prod(dz.h, dz.h);
-    const FF s1 = two_sum(qx.h, qy.h), s2 = two_sum(s1.h, qz.h);
-    const float cross = fm(2.0f, fa(fa(fm(dx.h, dx.l), fm(dy.h, dy.l)), fm(dz.h, dz.l)));
-    const float sl = fa(fa(fa(s1.l, s2.l), fa(fa(qx.l, qy.l), qz.l)), cross);
-    const float r0 = __fsqrt_rn(s2.h);
-    if (!(r0 > 0.0f)) return FF{ 0.0f, 0.0f };
-    const FF r2 = two_prod(r0, r0);
-    const float res = fa(fsb(fsb(s2.h, r2.h), r2.l), sl);
-    return FF{ r0, __fdiv_rn(res, fm(2.0f, r0)) };
-}
 
 // Correlation-sampler vertex record: the operands of the packed (two views
 // per instruction) inner loop are stored twice, so a 128-bit shared-memory
