@@ -38,7 +38,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "NEE path-contributions/s at <=1e-5 err vs FP64 (vs plain FP32); p50/p99 latency"
 UNIT = "contributions/s"
-WORKLOAD = "correlation_3d"
+WORKLOAD = "correlation_3d"   # the headline; --workload speckle_2d measures the 2D far-field speckle field
+WORKLOADS = ("correlation_3d", "speckle_2d")
 
 
 def _dist():
@@ -153,6 +154,8 @@ def _workload(seed: int, paths_log2: int):
     from temporalspecklescode_gb300 import workloads as wl
     waves = max(1, 1 << max(0, paths_log2 - 20))
     batch = (1 << paths_log2) // waves
+    if WORKLOAD == "speckle_2d":   # 16 x 16 far-field field speckle, one tick
+        return wl.speckle_2d(batch_size=batch, full_iteration=waves, seed=seed)
     cfg, dims = wl.correlation_3d(batch_size=batch, full_iteration=waves, seed=seed)
     return cfg, dims
 
@@ -452,6 +455,7 @@ def run_serve(args):
 
 
 def main():
+    global WORKLOAD
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -462,10 +466,13 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 15)
     ap.add_argument("--ref-sample", type=int, default=1 << 14)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD, choices=WORKLOADS,
+                    help="correlation_3d (the headline) or speckle_2d (2D far-field field speckle)")
     ap.add_argument("--serve", action="store_true", help="measure the serving mix instead of the headline workload")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-load", type=float, default=2.0, help="arrival rate / one-by-one completion rate")
     args = ap.parse_args()
+    WORKLOAD = args.workload
     if args.serve:
         run_serve(args)
         return

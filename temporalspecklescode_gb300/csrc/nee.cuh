@@ -81,6 +81,14 @@ __device__ __forceinline__ float frac_ff(float ph_h, float ph_l, const FF& t)
     const float f = fa(fa(ph_h, fsb(t.h, k)), fa(ph_l, t.l));   // t.h - k is exact
     return fsb(f, rintf(f));
 }
+// a + b for float pairs (two-sum of the high parts, renormalised)
+__device__ __forceinline__ FF add_ff(const FF& a, const FF& b)
+{
+    const FF s = two_sum(a.h, b.h);
+    const float e = fa(s.l, fa(a.l, b.l));
+    const float h = fa(s.h, e);
+    return FF{ h, fsb(e, fsb(h, s.h)) };
+}
 // |v - x| (float pair): exact differences, a float-pair sum of squares and
 // one Newton correction of the FP32 square root
 __device__ __forceinline__ FF dist_ff(const V3& v, const V3& x)

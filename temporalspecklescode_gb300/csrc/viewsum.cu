@@ -406,6 +406,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
         uint32_t steps = 0;
         float mt_carry = 0.0f;
         double l_carry = 0.0;
+        FF lc{ 0.0f, 0.0f };   // split field: path length before this block of vertices, a float pair
         for (uint32_t base = 2; base <= B; base += kVB) {
             const int nb = (int)min((uint32_t)kVB, B - base + 1);
             // ---- vertex records, lane = vertex b = base + lane ----
@@ -414,6 +415,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                 const bool act = lane < nb;
                 float dmt = 0.0f;
                 double seg = 0.0;
+                FF segf{ 0.0f, 0.0f };
                 if (act) {
                     const float4 c = vq[b - 1], p = vq[b - 2];
                     const V3 xc = V3{ c.x, c.y, c.z }, xp = V3{ p.x, p.y, p.z };
@@ -464,8 +466,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                         r.ph_h = (float)(__float_as_uint(c.w) >> 4) * (1.0f / 16777216.0f);   // xi_b, replaced below
                         r.ph_l = 0.0f;
                         if (split) {
-                            const double dx = (double)c.x - (double)p.x, dy = (double)c.y - (double)p.y, dz = (double)c.z - (double)p.z;
-                            seg = sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+                            segf = dist_ff(xc, xp);
                         } else {
                             const V3 dd = sub3(xc, xp);
                             seg = (double)sqrtf(dot3(dd, dd));
@@ -481,17 +482,24 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                     mt_carry += __shfl_sync(0xffffffffu, s, 31);
                 } else {
                     if (split) {
-                        double s = seg;
+                        // L_b / lambda + xi_b mod 1 in float-float (the path length's warp
+                        // scan included): FP64 per vertex would cost more than all views' phases
+                        FF s = segf;
 #pragma unroll
-                        for (int o = 1; o < 32; o <<= 1) { const double n = __shfl_up_sync(0xffffffffu, s, o); if (lane >= o) s += n; }
-                        if (act) {
-                            double ph = (l_carry + s) * S.inv_lambda + (double)rec[lane].ph_h;
-                            ph = ph - rint(ph);
-                            const float h = (float)ph;
-                            rec[lane].ph_h = h;
-                            rec[lane].ph_l = (float)(ph - (double)h);
+                        for (int o = 1; o < 32; o <<= 1) {
+                            const FF n{ __shfl_up_sync(0xffffffffu, s.h, o), __shfl_up_sync(0xffffffffu, s.l, o) };
+                            if (lane >= o) s = add_ff(s, n);
                         }
-                        l_carry += __shfl_sync(0xffffffffu, s, 31);
+                        if (act) {
+                            const FF t = scale_ff(add_ff(lc, s), S.il_h, S.il_l);
+                            const FF v = two_sum(fsb(t.h, rintf(t.h)), rec[lane].ph_h);   // t.h - rint(t.h) is exact; + xi_b
+                            float h = fa(v.h, fa(v.l, t.l));
+                            const float l = fsb(fa(v.l, t.l), fsb(h, v.h));
+                            h = fsb(h, rintf(h));
+                            rec[lane].ph_h = h;
+                            rec[lane].ph_l = l;
+                        }
+                        lc = add_ff(lc, FF{ __shfl_sync(0xffffffffu, s.h, 31), __shfl_sync(0xffffffffu, s.l, 31) });
                     } else {
                         float s = (float)seg;
 #pragma unroll
