@@ -414,6 +414,33 @@ def very_long_paths_2d(batch_size=256, full_iteration=2):
     return cfg, dims
 
 
+def far_phases_3d(point: bool, batch_size=64, full_iteration=2):
+    """Field sampler with the medium far from the origin and a short wavelength:
+    phases of ~1e5 cycles per NEE vector (far-field d.x / lambda or point-source
+    |v - x| / lambda) and long path phases, which FP32 alone cannot resolve."""
+    rng = np.random.default_rng(23)
+    off = np.array([4000.0, -2500.0, 3000.0])
+    grid = rng.integers(1, 3, size=(3, 3, 2)).astype(np.uint32)
+    if point:
+        ill = {"type": "PointSource", "location": {"x": off[0] + rng.uniform(-6, 6, 5), "y": off[1] + rng.uniform(-6, 6, 5),
+                                                     "z": np.full(5, off[2] - 3.0)}}
+        view = {"type": "PointSource", "location": {"x": off[0] + rng.uniform(-6, 6, 4), "y": off[1] + rng.uniform(-6, 6, 4),
+                                                      "z": np.full(4, off[2] + 12.0)}}
+    else:
+        ill = {"type": "FarField", "direction": {"x": [0.0, 0.2, -0.15], "y": [0.0, 0.1, 0.2], "z": [1.0, 0.97, 0.96]}}
+        view = {"type": "FarField", "direction": {"x": [0.05, -0.2, 0.1, 0.3], "y": [0.0, 0.1, -0.25, 0.05], "z": [1.0, 0.95, 0.96, 0.93]}}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.05, "seed": 29},
+        "scattering": {"type": ["HG", "HG", "HG"], "amplitudeFunction": [0.4, 0.6, 0.2]},
+        "medium": {"type": "Heterogeneous", "xAxis": off[0] + np.linspace(-8, 8, 4), "yAxis": off[1] + np.linspace(-8, 8, 4),
+                   "zAxis": off[2] + np.linspace(0, 9, 3), "materialGrid": grid, "sigs": [0.0, 0.6, 1.0], "siga": [0.0, 0.02, 0.01]},
+        "illumination": ill, "view": view,
+        "sampler": {"type": "TemporalSampler", "t": [0.0], "D": [0.0, 0.0, 0.0], "U": {"x": [0.0] * 3, "y": [0.0] * 3, "z": [0.0] * 3}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -452,6 +479,8 @@ def small_scenes():
         "vmf_2d": vmf_2d(),
         "vmf_corr_drift_3d": vmf_corr_drift_3d(),
         "edge_very_long_paths_2d": very_long_paths_2d(),
+        "edge_far_phases_far_3d": far_phases_3d(False),
+        "edge_far_phases_point_3d": far_phases_3d(True),
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
         "edge_one_path_corr_3d": one_path(True),
         "edge_one_path_field_2d": one_path(False),
