@@ -17,6 +17,37 @@ def mcx_fixture():
         return json.load(f)
 
 
+def mudiff_fixture():
+    import numpy as _np
+    return dict(_np.load(os.path.join(GOLDEN, "mudiff_cbs.npz")))
+
+
+def mudiff_scene(cbs: bool, correlation: bool = True, batch_size=4000, full_iteration=25):
+    """The scene of examples/mudiffCBSValidation2D.m from its fixture: a 2D
+    square of mean free path MFP with a tabular amplitude function, one
+    far-field illumination along +y, views at the fixture's angles; the
+    correlation sampler at t = 0 (an intensity) or the field sampler."""
+    fx = mudiff_fixture()
+    deg = fx["degList"]
+    view = {"type": "FarField", "direction": {"x": np.sin(deg), "y": np.cos(deg)}}
+    ill = {"type": "FarField", "direction": {"x": [0.0], "y": [1.0]}}
+    amp = fx["ampFunc"]
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 1.0, "seed": 0},
+        "scattering": {"type": ["Tabular", "Tabular"], "amplitudeFunction": [amp, amp]},
+        "medium": {"type": "Heterogeneous", "xAxis": fx["x"], "yAxis": fx["y"], "materialGrid": np.ones((1, 1), dtype=np.uint32),
+                   "sigs": [0.0, 1.0 / float(fx["MFP"])], "siga": [0.0, 0.0]},
+        "illumination": ill, "view": view,
+        "sampler": {"type": "TemporalCorrelationSampler" if correlation else "TemporalSampler", "t": [0.0],
+                    "D": [0.0, 0.0], "U": {"x": [0.0, 0.0], "y": [0.0, 0.0]}},
+        "tracer": {"type": "nee", "isCBS": cbs},
+    }
+    if correlation:
+        cfg["illumination2"] = ill
+        cfg["view2"] = view
+    return cfg, 2
+
+
 def field_point_3d(moving: bool = True, area: bool = False, batch_size=64, full_iteration=2):
     """3D field sampler with point sources, Brownian + drift motion (ticks around their mean)."""
     rng = np.random.default_rng(7)

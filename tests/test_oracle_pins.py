@@ -431,3 +431,24 @@ def test_iter_counts_every_missed_attempt(oracle, make):
     assert st["paths"] == n
     if make == "mostly_misses_3d":
         assert it > 50 * n
+
+
+def test_oracle_reproduces_mudiff_curve_outside_the_cbs_cone(oracle):
+    """The reference's own tabular-scattering validation (examples/
+    mudiffCBSValidation2D.m against the mudiff solver, examples/data/
+    mudiffCBS.mat via tests/golden/make_mudiff_fixture.py): the correlation
+    sampler at t = 0 without CBS reproduces the solver's angular intensity
+    over all 721 angles outside the coherent-backscattering cone (about 2 %
+    per angle at 1e5 paths), and falls short inside it, where the solver
+    includes the cone."""
+    from tests.scenes import mudiff_fixture, mudiff_scene
+    fx = mudiff_fixture()
+    cfg, dims = mudiff_scene(cbs=False)
+    u, it, st = oracle.render(cf.prepare(cfg, dims), 0)
+    ratio = np.abs(u.ravel()) / it / fx["mudiffRes"]
+    ang = np.degrees(fx["degList"])
+    out = np.abs(ang - 180.0) > 3.0
+    assert abs(ratio[out].mean() - 1.0) < 0.03, ratio[out].mean()
+    smooth = np.convolve(ratio[out], np.ones(11) / 11, mode="valid")
+    assert np.max(np.abs(smooth - 1.0)) < 0.06
+    assert ratio[np.argmin(np.abs(ang - 180.0))] < 0.8   # the solver's curve has the CBS peak there
