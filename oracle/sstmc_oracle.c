@@ -461,11 +461,8 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         S->D[m] = (m < M && cfg->D) ? cfg->D[m] : 0.0;
         if (S->D[m] < 0) return SSTMC_INVALID_CONFIG; /* MatlabInterface.cu:1278-1283 */
         for (int i = 0; i < 3; ++i) S->U_f[m][i] = (m < M && cfg->U && (i < dims)) ? (float)cfg->U[3 * m + i] : 0.0f;
-        /* correlation CBS is built for static scatterers (no drift U) and real-valued
-         * phase functions (no tabular material) */
+        /* correlation CBS is built for static scatterers (no drift U) */
         if (S->cbs && S->correlation && (S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f))
-            return SSTMC_NOT_SUPPORTED;
-        if (S->cbs && S->correlation && (S->scat_type[m] == SSTMC_SCATTERING_TABULAR || S->scat_type[m] == SSTMC_SCATTERING_VMF_MIXTURE))
             return SSTMC_NOT_SUPPORTED;
     }
     /* field sampler: ticks sorted around the mean, TemporalSampler.cuh:958-1150 */

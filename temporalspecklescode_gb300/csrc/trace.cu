@@ -797,15 +797,23 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
             if (isl) {
                 const DevSource& s = *srcl[u];
                 const float2 g = gcomplex<ILP>(S, s, el, x1, kRoleIllum, st);
-                const float f = fillum<ILP>(S, s, el, x1, x2, m1);
-                g0l[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                if (is_amp64(S, m1)) {   // tabular / vMF: complex amplitude from an FP64 angle
+                    g0l[u][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, x1, x2, false))), u == 0 ? p2inv : 1.0f);
+                } else {
+                    const float f = fillum<ILP>(S, s, el, x1, x2, m1);
+                    g0l[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                }
                 const V3 d = fsrc_in(s, el, x1);
                 d0l[u][ge][0] = d.x; d0l[u][ge][1] = d.y; d0l[u][ge][2] = d.z;
             } else {
                 const DevSource& s = *srcv[u];
                 const float2 g = gcomplex<VWP>(S, s, el, x1, kRoleView, st);
-                const float f = fview_entry<VWP>(S, s, el, x1, x2, m1);
-                g0v[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                if (is_amp64(S, m1)) {   // the view attached at x1 as the reversed path's first end
+                    g0v[u][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, x1, x2, true))), u == 0 ? p2inv : 1.0f);
+                } else {
+                    const float f = fview_entry<VWP>(S, s, el, x1, x2, m1);
+                    g0v[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                }
                 const V3 d = fsrc_out(s, el, x1);
                 d0v[u][ge][0] = -d.x; d0v[u][ge][1] = -d.y; d0v[u][ge][2] = -d.z;
             }
@@ -832,12 +840,16 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
                 uint32_t st = 0;
                 if (isl) {
                     const DevSource& s = *srcl[u];
-                    gb_l[u][ge] = c_scale(gcomplex<ILP>(S, s, el, xn, kRoleIllum, st), fillum_exit<ILP>(S, s, el, xn, prev, mn));
+                    const float2 g = gcomplex<ILP>(S, s, el, xn, kRoleIllum, st);
+                    gb_l[u][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, xn, prev, false)))
+                                                  : c_scale(g, fillum_exit<ILP>(S, s, el, xn, prev, mn));
                     const V3 d = fsrc_in(s, el, xn);
                     dbl[u][ge][0] = d.x; dbl[u][ge][1] = d.y; dbl[u][ge][2] = d.z;
                 } else {
                     const DevSource& s = *srcv[u];
-                    gb_v[u][ge] = c_scale(gcomplex<VWP>(S, s, el, xn, kRoleView, st), fview<VWP>(S, s, el, xn, prev, mn));
+                    const float2 g = gcomplex<VWP>(S, s, el, xn, kRoleView, st);
+                    gb_v[u][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, xn, prev, true)))
+                                                  : c_scale(g, fview<VWP>(S, s, el, xn, prev, mn));
                     const V3 d = fsrc_out(s, el, xn);
                     dbv[u][ge][0] = -d.x; dbv[u][ge][1] = -d.y; dbv[u][ge][2] = -d.z;
                 }

@@ -510,6 +510,9 @@ def small_scenes():
         "vmf_2d": vmf_2d(),
         "vmf_corr_drift_3d": vmf_corr_drift_3d(),
         "edge_very_long_paths_2d": very_long_paths_2d(),
+        "tabular_corr_2d_cbs": with_cbs(tabular_corr_2d()),
+        "vmf_corr_3d_cbs": with_cbs(vmf_corr_3d()),
+        "mudiff_corr_cbs": mudiff_scene(cbs=True, batch_size=96, full_iteration=2),
         "edge_far_phases_far_3d": far_phases_3d(False),
         "edge_far_phases_point_3d": far_phases_3d(True),
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),

@@ -452,3 +452,20 @@ def test_oracle_reproduces_mudiff_curve_outside_the_cbs_cone(oracle):
     smooth = np.convolve(ratio[out], np.ones(11) / 11, mode="valid")
     assert np.max(np.abs(smooth - 1.0)) < 0.06
     assert ratio[np.argmin(np.abs(ang - 180.0))] < 0.8   # the solver's curve has the CBS peak there
+
+
+def test_oracle_reproduces_mudiff_cbs_cone(oracle):
+    """The same validation with coherent backscattering (tracer.isCBS, the
+    correlation sampler's C2-C4 cross terms with the tabular amplitudes): the
+    solver's curve is reproduced inside the backscattering cone too, where
+    the estimator without CBS falls a third short."""
+    from tests.scenes import mudiff_fixture, mudiff_scene
+    fx = mudiff_fixture()
+    cfg, dims = mudiff_scene(cbs=True, batch_size=2000, full_iteration=25)
+    u, it, st = oracle.render(cf.prepare(cfg, dims), 0)
+    ratio = np.abs(u.ravel()) / it / fx["mudiffRes"]
+    ang = np.degrees(fx["degList"])
+    cone = np.abs(ang - 180.0) <= 2.0
+    assert np.all(np.abs(ratio[cone] - 1.0) < 0.08), ratio[cone]
+    assert abs(ratio[~cone].mean() - 1.0) < 0.03
+    assert np.abs(u.imag).max() <= 1e-9 * np.abs(u.real).max()   # u1 == u2, t = 0: real
