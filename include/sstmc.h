@@ -140,7 +140,7 @@ typedef struct sstmc_config {
                                       correlation sampler, TemporalSampler.cuh:439-534, 1637-1698) */
 
     /* config.tracer (MatlabInterface.cu:1374-1457) */
-    int32_t is_cbs;                /* default 0; 1: coherent backscattering (correlation sampler: static scatterers) */
+    int32_t is_cbs;                /* default 0; 1: coherent backscattering (correlation sampler: static scatterers, U = 0) */
 
     /* build-specific */
     int32_t precision;             /* SSTMC_PRECISION_* */
