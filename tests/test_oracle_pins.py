@@ -469,3 +469,30 @@ def test_oracle_reproduces_mudiff_cbs_cone(oracle):
     assert np.all(np.abs(ratio[cone] - 1.0) < 0.08), ratio[cone]
     assert abs(ratio[~cone].mean() - 1.0) < 0.03
     assert np.abs(u.imag).max() <= 1e-9 * np.abs(u.real).max()   # u1 == u2, t = 0: real
+
+
+def test_oracle_field_cbs_reproduces_mudiff(oracle):
+    """The field half of examples/mudiffCBSValidation2D.m: the speckle
+    intensity |u|^2 / iter averaged over renderings (200 renderings of 500
+    paths here) follows the mudiff solver away from backscattering with and
+    without CBS, and only with CBS (the reversed-path rows Gv0 / GlSum)
+    inside the cone.  Both runs walk the same paths, so the cone's gain is
+    the CBS term alone."""
+    from tests.scenes import mudiff_fixture, mudiff_scene
+    fx = mudiff_fixture()
+    ang = np.degrees(fx["degList"])
+    cone = np.abs(ang - 180.0) <= 2.0
+    out = np.abs(ang - 180.0) > 3.0
+    res = {}
+    for cbs in (False, True):
+        cfg, dims = mudiff_scene(cbs=cbs, correlation=False, batch_size=500, full_iteration=1)
+        pc = cf.prepare(cfg, dims)
+        acc = np.zeros(ang.size)
+        for r in range(200):
+            u, it, st = oracle.render(pc, 1000 + r)
+            acc += np.abs(u.ravel()) ** 2 / it
+        res[cbs] = acc / 200 / fx["mudiffRes"]
+    for cbs in (False, True):
+        assert abs(res[cbs][out].mean() - 1.0) < 0.03
+    assert abs(res[True][cone].mean() - 1.0) < 0.06
+    assert res[True][cone].mean() - res[False][cone].mean() > 0.06
