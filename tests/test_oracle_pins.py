@@ -496,3 +496,33 @@ def test_oracle_field_cbs_reproduces_mudiff(oracle):
         assert abs(res[cbs][out].mean() - 1.0) < 0.03
     assert abs(res[True][cone].mean() - 1.0) < 0.06
     assert res[True][cone].mean() - res[False][cone].mean() > 0.06
+
+
+def _wood_vmf_cosines(kappa, n, rng):
+    """Wood's rejection sampler for the vMF cosine on the sphere (Wood 1994,
+    m = 3), the method of the reference's random_vMF_cosine
+    (VectorType.cuh:169-203), written from the published algorithm."""
+    b = -kappa + np.hypot(kappa, 1.0)
+    x0 = (1.0 - b) / (1.0 + b)
+    c = kappa * x0 + 2.0 * np.log(1.0 - x0 * x0)
+    out = np.empty(0)
+    while out.size < n:
+        z = rng.uniform(size=2 * n)
+        u = rng.uniform(size=2 * n)
+        w = (1.0 - (1.0 + b) * z) / (1.0 - (1.0 - b) * z)
+        keep = kappa * w + 2.0 * np.log(1.0 - x0 * w) - c >= np.log(u)
+        out = np.concatenate([out, w[keep]])
+    return out[:n]
+
+
+@pytest.mark.parametrize("kappa", [0.5, 5.0, 60.0])
+def test_vmf_inverse_cdf_matches_wood_sampler(oracle, kappa):
+    """The walk draws a vMF lobe's cosine by the exact inverse cdf
+    w = 1 + log(v + (1 - v) e^{-2 kappa}) / kappa; the reference runs Wood's
+    rejection loop.  Both sample exp(kappa w) on [-1, 1]: a two-sample
+    Kolmogorov-Smirnov test does not tell them apart."""
+    stats = pytest.importorskip("scipy.stats")
+    pc = _vmf_cfg([kappa / 2.0], [1.0])   # one lobe: its pair has kappa = mu + mu
+    ours = np.asarray(oracle.sample_cos(pc, 1, 11, 100000), dtype=np.float64)
+    wood = _wood_vmf_cosines(kappa, 100000, np.random.default_rng(5))
+    assert stats.ks_2samp(ours, wood).pvalue > 1e-3
