@@ -142,6 +142,8 @@ def _vec3(d: Dict[str, Any], n_expected: int | None, dims: int, name: str) -> np
         raise ConfigError(f"{name} must have field z")
     if not (len(xs) == len(ys) == len(zs)):
         raise ConfigError(f"{name} x, y, z must have the same number of elements")
+    if len(xs) == 0:   # the MEX layer's array readers require at least one element
+        raise ConfigError(f"{name} must have at least one element")
     if n_expected is not None and len(xs) != n_expected:
         raise ConfigError(f"{name} must have {n_expected} elements")
     return np.ascontiguousarray(np.stack([xs, ys, zs], axis=1).reshape(-1))
@@ -346,6 +348,8 @@ def prepare(config: Dict[str, Any], dims: int, precision: int = PRECISION_SPLIT)
     else:
         raise ConfigError("Unsupported sapmler type. Available sampler types are TemporalSampler and TemporalCorrelationSampler")
     t = _arr(smp["t"])
+    if t.size == 0:
+        raise ConfigError("sampler.t must have at least one element")
     D = _arr(smp["D"])
     if D.size != mat_num:
         raise ConfigError(f"sampler.D must have {mat_num} elements")
