@@ -1,20 +1,32 @@
-"""Benchmark: NEE path-contributions/s of the 3D temporal-correlation workload.
+"""Benchmark: NEE path-contributions/s of the path tracer on one workload.
 
-Workload (one step = one render): the 3D correlation scene -- slab
-[-100,100]^2 x [0,20], sigs=[0,0.5], siga=[0,0.01], HG g=0.9, 64 point
-illuminations at z=-5 and 64 point views at z=25 on jittered 8x8 lattices,
-Brownian D=[0,1e-3], 8 lags -- with 2^22 paths (4 waves of 2^20), seeded
-synthetic inputs.  One contribution is one (path, scattering vertex,
-illumination, view, lag) term of the estimator.
+Workloads (one step = one render of seeded synthetic inputs; one contribution
+is one (path, scattering vertex, illumination, view, tick) term of the
+estimator):
+  correlation_3d (default, the headline): slab [-100,100]^2 x [0,20],
+      sigs=[0,0.5], siga=[0,0.01], HG g=0.9, 64 point illuminations at z=-5
+      and 64 point views at z=25 on jittered 8x8 lattices, Brownian
+      D=[0,1e-3], 8 lags; 2^22 paths (4 waves of 2^20).
+  speckle_2d: 2D single-bin box [-50,50]^2, sigs=[0,1], HG g=0.8, 16 x 16
+      far-field directions over [-pi/6, pi/6]; 65,536 paths.
+  transmission_matrix_3d: 64x64x32 grid over [-64,64]^2 x [0,64] of iid
+      materials {1..4}, HG g=0.85, 1024 x 1024 far-field directions on
+      20-degree cones; 2^24 paths.
+  tracking_2d_pairs: 256^2 grid with a disc (sigs=4) whose scatterers drift
+      by (0.5, 0) per frame, HG g=0.7, 128 x 128 far field, correlations of
+      all 32 x 32 frame pairs from the 63 lags t2 - t1; 2^23 paths.
 
 value : contributions / device time of the render (CUDA events on the
         library's stream; scene tables resident in HBM).
 e2e   : the same metric through the public C-ABI call a MATLAB-style user
         makes -- scene creation (host -> device upload of the config tables),
         render, read-back of u and iter, scene destruction -- timed on the host.
---impl reference: the reference has no CPU implementation and its CUDA
-        sources do not exist on the GPU host, so the reference arm times the
-        CPU FP64 restatement of its estimator (oracle/) on all host threads.
+plain_fp32 : the plain FP32 form (FP32 phases, SIMT contraction) on the same
+        workload; rel_err_vs_fp64: both forms against the FP64 oracle on a
+        path subset of the workload.
+--impl reference: the reference has no CPU implementation, so the reference
+        arm times the CPU FP64 restatement of its estimator (oracle/) on all
+        host threads.
 
 Multi-GPU (torchrun): independent replicas with disjoint seeds ("replicas
 only": the paths are i.i.d., there is no exchange step); value is the sum of
@@ -38,9 +50,21 @@ sys.path.insert(0, ROOT)
 
 METRIC = "NEE path-contributions/s at <=1e-5 err vs FP64 (vs plain FP32); p50/p99 latency"
 UNIT = "contributions/s"
-WORKLOAD = "correlation_3d"   # the headline; --workload speckle_2d measures the 2D far-field speckle field
-WORKLOADS = ("correlation_3d", "speckle_2d")
+WORKLOAD = "correlation_3d"   # the headline (3D temporal correlation, 64 x 64 x 8, 2^22 paths)
 
+# Per workload: default path count, CPU oracle sample sizes (about 10-30 s of
+# host work on 16 cores) and the path subset of the error measurement against
+# the FP64 oracle.
+WORKLOADS = {
+    # 3D temporal correlation: point sources on jittered 8x8 lattices, 8 lags
+    "correlation_3d": {"paths_log2": 22, "cpu_sample": 1 << 15, "ref_sample": 1 << 14, "err_paths": 1 << 14},
+    # 2D far-field speckle field: 16 x 16, one tick, 65,536 paths
+    "speckle_2d": {"paths_log2": 16, "cpu_sample": 1 << 16, "ref_sample": 1 << 15, "err_paths": 1 << 14},
+    # 3D transmission matrix: 1024 x 1024 far field, 64x64x32 grid of 4 materials, 2^24 paths
+    "transmission_matrix_3d": {"paths_log2": 24, "cpu_sample": 1 << 11, "ref_sample": 1 << 10, "err_paths": 1 << 8},
+    # 2D tracking: 128 x 128 far field, 256^2 grid with a drifting disc, all 32 x 32 frame pairs (63 lags)
+    "tracking_2d_pairs": {"paths_log2": 23, "cpu_sample": 1 << 6, "ref_sample": 1 << 5, "err_paths": 1 << 3},
+}
 
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -150,13 +174,25 @@ def _peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def _workload(seed: int, paths_log2: int):
+def _workload(seed: int, paths_log2: int, workload: str | None = None):
+    """The workload's scene with 2^paths_log2 paths (waves of at most 2^20)."""
     from temporalspecklescode_gb300 import workloads as wl
+    workload = workload or WORKLOAD
     waves = max(1, 1 << max(0, paths_log2 - 20))
     batch = (1 << paths_log2) // waves
-    if WORKLOAD == "speckle_2d":   # 16 x 16 far-field field speckle, one tick
+    if workload == "speckle_2d":
         return wl.speckle_2d(batch_size=batch, full_iteration=waves, seed=seed)
-    cfg, dims = wl.correlation_3d(batch_size=batch, full_iteration=waves, seed=seed)
+    if workload == "transmission_matrix_3d":
+        return wl.transmission_matrix_3d(batch_size=batch, full_iteration=waves, seed=seed)
+    if workload == "tracking_2d_pairs":
+        return wl.tracking_2d_pairs(batch_size=batch, full_iteration=waves, seed=seed)
+    return wl.correlation_3d(batch_size=batch, full_iteration=waves, seed=seed)
+
+
+def _sample_workload(paths: int, seed: int = 0):
+    cfg, dims = _workload(seed, 20)
+    cfg["simulation"]["batchSize"] = paths
+    cfg["simulation"]["fullIteration"] = 1
     return cfg, dims
 
 
@@ -164,9 +200,7 @@ def cpu_baseline(sample_paths: int, threads: int):
     """Time the CPU oracle (FP64 restatement, OpenMP) on a bounded sample."""
     from temporalspecklescode_gb300 import config as cf
     from tests.oracle_lib import Oracle
-    cfg, dims = _workload(0, 20)
-    cfg["simulation"]["batchSize"] = sample_paths
-    cfg["simulation"]["fullIteration"] = 1
+    cfg, dims = _sample_workload(sample_paths)
     pc = cf.prepare(cfg, dims)
     oracle = Oracle()
     t0 = time.perf_counter()
@@ -175,11 +209,30 @@ def cpu_baseline(sample_paths: int, threads: int):
     return st["contributions"] / dt, st, dt
 
 
+def error_vs_oracle(paths: int, threads: int):
+    """Relative Frobenius error of the split-precision and plain FP32 renders
+    against the FP64 oracle on the same seeded paths (a subset of the
+    workload: its scene with `paths` paths)."""
+    import numpy as np
+    from temporalspecklescode_gb300 import api, config as cf
+    from tests.oracle_lib import Oracle
+    cfg, dims = _sample_workload(paths, seed=0)
+    uo, ito, _ = Oracle().render(cf.prepare(cfg, dims), 7, threads=threads)
+    out = {"paths": paths}
+    for name, prec in (("split", cf.PRECISION_SPLIT), ("plain_fp32", cf.PRECISION_FP32)):
+        with api.Scene(cfg, dims, prec) as s:
+            u, it = s.render(seed=7)
+        if it[0] != ito:
+            raise RuntimeError(f"error subset: iteration count {it[0]} differs from the oracle's {ito}")
+        out[name] = float(np.linalg.norm(u[..., 0] - uo) / np.linalg.norm(uo))
+    return out
+
+
 def run_reference(args, dist, rank, ws):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = args.ref_sample
+    sample = args.ref_sample or WORKLOADS[WORKLOAD]["ref_sample"]
     times = []
     contrib = 0
     for i in range(args.warmup + args.steps):
@@ -202,29 +255,43 @@ def run_reference(args, dist, rank, ws):
 
 
 # DRAM bytes (read + write) per path of each kernel class from one ncu capture
-# of this workload at 2^16 paths (profiles/kernels_correlation_3d_2p16.md);
-# every class streams per-path rows, so a launch's traffic scales with the
-# paths it processes.
+# of the workload at a small path count; every class streams per-path rows,
+# so a launch's traffic scales with the paths it processes.
 NCU_DRAM_BYTES_PER_PATH = {
-    "nee": (8354816 + 156937728 + 14934272 + 75123456) / 65536,   # illum_kernel + view_kernel
-    "walk": (242688 + 176896 + 18749184 + 1536) / 65536,          # walk_kernel<slots> + compact_kernel
-    "gemm": (269205504 + 3310592) / 65536,                         # gemm_tc_kernel (real rows)
-    "ss": (68522752 + 932352) / 65536,                             # ss_fast_kernel
+    "correlation_3d": {   # 2^16 paths
+        "nee": (8354816 + 156937728 + 14934272 + 75123456) / 65536,   # illum_kernel + view_kernel
+        "walk": (242688 + 176896 + 18749184 + 1536) / 65536,          # walk_kernel<slots> + compact_kernel
+        "gemm": (269205504 + 3310592) / 65536,                         # gemm_tc_kernel (real rows)
+        "ss": (68522752 + 932352) / 65536,                             # ss_fast_kernel
+    },
+}
+
+KERNEL_NAMES = {
+    "correlation_3d": {"nee": "illum_kernel + view_kernel (NEE vectors)", "ss": "ss_fast_kernel (single-scattering contraction)"},
+    "speckle_2d": {"nee": "trace_kernel (illumination side) + view_kernel (NEE vectors)",
+                   "ss": "gemm_tc_kernel x materials (far x far single scattering, weight tables)"},
+    "transmission_matrix_3d": {"nee": "trace_kernel (illumination side) + view_kernel (NEE vectors)",
+                               "ss": "gemm_tc_kernel x materials (far x far single scattering, weight tables)"},
+    "tracking_2d_pairs": {"nee": "trace_kernel (fused NEE vectors, drifting scatterers)",
+                          "ss": "gemm_tc_kernel x materials (far x far single scattering, weight tables)"},
 }
 
 
-def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
+def _kernel_rooflines(scene, mean, verts_per_step, dda_per_step, chunks, peaks, rows_real):
     """Per kernel class: time per step, algorithmic bytes or flops per launch,
     achieved rate and the fraction of the measured peak."""
     m = scene.meta
     P = m["P"] * m["waves"]
     Nl, Nv, Nt = m["Nl"], m["Nv"], m["Nt"]
     hbm, tc = peaks["hbm_gbs"], peaks["bf16_tflops"]
+    ridge = tc * 1e12 / (hbm * 1e9)   # flop per byte where the two measured roofs meet
+    ncu = NCU_DRAM_BYTES_PER_PATH.get(WORKLOAD, {})
+    names = KERNEL_NAMES.get(WORKLOAD, KERNEL_NAMES["correlation_3d"])
     out = {}
 
-    def add(key, name, ms, bound, amount, note):
+    def add(key, name, ms, bound, amount, note, extra=None):
         per_launch = amount / chunks
-        traffic = NCU_DRAM_BYTES_PER_PATH[key] * P / chunks if WORKLOAD == "correlation_3d" else None
+        traffic = ncu[key] * P / chunks if key in ncu else None
         if bound == "hbm":
             ach = amount / (ms / 1000) / 1e9
             out[key] = {"kernel": name, "ms": ms, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
@@ -235,39 +302,74 @@ def _kernel_rooflines(scene, mean, verts_per_step, chunks, peaks):
             out[key] = {"kernel": name, "ms": ms, "bound": "tensor", "achieved": ach, "peak": tc, "unit": "TFLOP/s",
                         "frac": ach / tc, "peak_name": "bf16_tflops", "algorithmic_per_launch": per_launch,
                         "traffic": traffic, "note": note}
+        if extra:
+            out[key].update(extra)
 
-    # NEE vectors (illum_kernel + view_kernel): rows written once (a_ms all ticks,
-    # tick-invariant single-scattering rows at tick 0, s_ms), P_l, the vertices read.
-    # The correlation sampler's rows are real here: 4 bytes per (tick, element).
-    rb = 4.0 if m["correlation"] else 8.0
-    nee_bytes = P * (rb * Nt * Nl + 8.0 * (Nl + Nv) + rb * Nt * Nv + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
-    add("nee", "illum_kernel + view_kernel (NEE vectors)", mean["ms_nee"], "hbm", nee_bytes,
-        "FP32-issue bound: DRAM traffic equals the row bytes")
+    # NEE vectors: rows written once (a_ms all ticks, single-scattering rows, s_ms),
+    # P_l, the vertices read.  Real rows (correlation, static, u1 = u2): 4 bytes per
+    # (tick, element); complex: 8.
+    rb = 4.0 if rows_real else 8.0
+    ss_ticks = 1 if rows_real else Nt
+    nee_bytes = P * (rb * Nt * Nl + 8.0 * ss_ticks * (Nl + Nv) + rb * Nt * Nv + 4 * Nl + 13 + 12) + 16.0 * verts_per_step
+    add("nee", names["nee"], mean["ms_nee"], "hbm", nee_bytes,
+        "FP32 / voxel-step issue bound: DRAM traffic equals the row bytes",
+        {"voxel_steps_per_s": dda_per_step / (mean["ms_nee"] / 1000) if mean["ms_nee"] > 0 else None})
     # random walk: one pass into per-path slots + compaction; vertices written once, counts / misses / offsets
     add("walk", "walk_kernel (single-pass random walk) + compaction", mean["ms_walk"], "hbm", 16.0 * verts_per_step + 20.0 * P,
         "FP32-issue bound (IEEE-rounded decision path)")
-    # multiple-scattering contraction: HBM-bound at this shape (M = N = 128 per tick
-    # pair, 2 Nl Nv Nt flops per path against rb Nt (Nl + Nv) bytes read)
-    add("gemm", "gemm_tc_kernel (multiple-scattering contraction, 3xTF32)", mean["ms_contract_ms"], "hbm",
-        rb * Nt * (Nl + Nv) * P, "reads the a_ms and s_ms rows once; tensor pipe 23 % active (ncu)")
-    # single-scattering contraction: tick-0 rows read (tick-invariant form)
-    add("ss", "ss_fast_kernel (single-scattering contraction)", mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv),
-        "FP32/SFU-issue bound: one exp and one rsqrt per (path, l, v)")
+    # multiple-scattering contraction: useful flops 8 Nl Nv Nt per path for complex rows
+    # (a complex MAC), 2 Nl Nv Nt for real rows; bytes: the a_ms and s_ms rows read once.
+    # The binding roof is the one its arithmetic intensity reaches first.
+    gflops = (2.0 if rows_real else 8.0) * Nl * Nv * Nt * P
+    gbytes = rb * Nt * (Nl + Nv) * P
+    gbound = "tensor" if gflops / gbytes >= ridge else "hbm"
+    other = ({"achieved_tflops": gflops / (mean["ms_contract_ms"] / 1000) / 1e12} if gbound == "hbm"
+             else {"achieved_gbs": gbytes / (mean["ms_contract_ms"] / 1000) / 1e9})
+    other["useful_flops_per_launch"] = gflops / chunks
+    other["flop_per_byte"] = gflops / gbytes
+    add("gemm", "gemm_tc_kernel (multiple-scattering contraction, tcgen05 3xTF32)", mean["ms_contract_ms"], gbound,
+        gflops if gbound == "tensor" else gbytes,
+        "useful flops (not the 3 TF32 passes) against the measured dense bf16 peak" if gbound == "tensor"
+        else "reads the a_ms and s_ms rows once", other)
+    if WORKLOAD == "correlation_3d":
+        # single-scattering contraction: tick-0 rows read (tick-invariant form)
+        add("ss", names["ss"], mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv),
+            "FP32/SFU-issue bound: one exp and one rsqrt per (path, l, v)")
+    else:
+        # far x far: one GEMM per material over its paths, weights per (l, v, t, material)
+        sflops = 8.0 * Nl * Nv * Nt * P
+        sbytes = 8.0 * Nt * (Nl + Nv) * P
+        sbound = "tensor" if sflops / sbytes >= ridge else "hbm"
+        add("ss", names["ss"], mean["ms_contract_ss"], sbound, sflops if sbound == "tensor" else sbytes,
+            "per-material GEMMs over the paths of that first-vertex material", {"useful_flops_per_launch": sflops / chunks})
     return out
 
 
+def _render_series(scene, seeds):
+    """Render each seed; device time and statistics per render."""
+    res = []
+    for sd in seeds:
+        ts = time.perf_counter()
+        scene.render(seed=sd)
+        host_ms = 1000 * (time.perf_counter() - ts)
+        res.append((host_ms, scene.timing(), scene.stats()))
+    return res
+
+
 def run_gpu(args, dist, rank, ws):
-    import numpy as np
     from temporalspecklescode_gb300 import api, config as cf
     api.load_library()
+    spec = WORKLOADS[WORKLOAD]
+    paths_log2 = args.paths_log2 or spec["paths_log2"]
     precision = cf.PRECISION_FP32 if args.precision == "fp32" else cf.PRECISION_SPLIT
-    cfg, dims = _workload(seed=1000 * rank, paths_log2=args.paths_log2)
+    cfg, dims = _workload(seed=1000 * rank, paths_log2=paths_log2)
     scene = api.Scene(cfg, dims, precision)
     lat = []
     dev_ms = []
     parts = {"ms_trace": [], "ms_contract_ms": [], "ms_contract_ss": [], "ms_walk": [], "ms_nee": []}
     chunks = 1
     verts = 0
+    dda = 0
     contrib = 0
     launches = 0
     for i in range(args.warmup):
@@ -276,19 +378,16 @@ def run_gpu(args, dist, rank, ws):
     _barrier(dist)
     clocks.start()
     t0 = time.perf_counter()
-    for i in range(args.steps):
-        ts = time.perf_counter()
-        u, it = scene.render(seed=100 + i)
-        lat.append(1000 * (time.perf_counter() - ts))
-        tm = scene.timing()
+    for host_ms, tm, st in _render_series(scene, [100 + i for i in range(args.steps)]):
+        lat.append(host_ms)
         dev_ms.append(tm["ms_total"])
         for k in parts:
             parts[k].append(tm[k])
         launches += tm["launches"]
         chunks = tm["chunks"]
-        st = scene.stats()
         contrib += st["contributions"]
         verts += st["vertices"]
+        dda += st["dda_steps"]
     wall = time.perf_counter() - t0
     _barrier(dist)
     clk = clocks.stop()
@@ -296,6 +395,8 @@ def run_gpu(args, dist, rank, ws):
     dev_total_s = _max_over_ranks(dist, dev_total_s)
     contrib_all = _sum_over_ranks(dist, float(contrib))
     value = contrib_all / dev_total_s
+    rows_real = bool(scene.meta["correlation"]) and WORKLOAD == "correlation_3d" and precision == cf.PRECISION_SPLIT
+    heavy = statistics.mean(dev_ms) > 2000.0   # renders of seconds: fewer repeats in the side measurements
 
     # end to end through the C-ABI: create (upload) + render + read back + destroy
     e2e_t = []
@@ -303,11 +404,11 @@ def run_gpu(args, dist, rank, ws):
     # one untimed call first: the first scene created next to the resident one
     # grows the stream-ordered memory pool
     with api.Scene(cfg, dims, precision) as s2:
-        s2.render(seed=199)
-    for i in range(max(1, min(3, args.steps))):
+        u, it = s2.render(seed=199)
+    for i in range(1 if heavy else max(1, min(3, args.steps))):
         ts = time.perf_counter()
         with api.Scene(cfg, dims, precision) as s2:
-            u2, it2 = s2.render(seed=200 + i)
+            u, it = s2.render(seed=200 + i)
         e2e_t.append(time.perf_counter() - ts)
     pc = scene.prepared
     for a in pc._keep:
@@ -321,13 +422,13 @@ def run_gpu(args, dist, rank, ws):
     P = m["P"] * m["waves"]
     Nl, Nv, Nt = m["Nl"], m["Nv"], m["Nt"]
     mean = {k: statistics.mean(v) for k, v in parts.items()}
-    kernels = _kernel_rooflines(scene, mean, verts / args.steps, chunks, peaks)
+    kernels = _kernel_rooflines(scene, mean, verts / args.steps, dda / args.steps, chunks, peaks, rows_real)
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     d = kernels[dom]
     roof = {"kernel": d["kernel"], "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"], "unit": d["unit"],
             "frac": d["frac"], "traffic": d["traffic"], "peak_source": pk_kind + " (" + d["peak_name"] + ")",
             "algorithmic_per_launch": d["algorithmic_per_launch"], "launches_per_step": chunks}
-    if dom == "ss" and m["correlation"]:
+    if dom == "ss" and WORKLOAD == "correlation_3d":
         # ss_fast_kernel is bound by FP32 issue, not by HBM: the algorithmic FP32 lane
         # operations per (path, l, v) element are 6 (q^2) + 5 (pdf) + 1 (decay
         # argument) per 8-tick chunk and 2 per tick (one product for the tick's decay
@@ -347,18 +448,35 @@ def run_gpu(args, dist, rank, ws):
                          "ops_per_element": 11 * tchunks + 2 * Nt, "mufu_per_element": 2 * tchunks,
                          "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (sampled SM clock)"}
 
+    # the plain FP32 form (FP32 phases, uncompensated SIMT contraction) on the same
+    # workload and paths, for the split / plain ratio
+    plain = None
+    if precision == cf.PRECISION_SPLIT and not args.no_plain:
+        with api.Scene(cfg, dims, cf.PRECISION_FP32) as s3:
+            s3.render(seed=0)
+            series = _render_series(s3, [100 + i for i in range(1 if heavy else 3)])
+        pms = statistics.mean([tm["ms_total"] for _, tm, _ in series])
+        pval = statistics.mean([st["contributions"] for _, _, st in series]) / (pms / 1000)
+        plain = {"value": pval, "unit": UNIT, "ms_per_step": pms, "renders": len(series),
+                 "split_over_plain": value / pval if ws == 1 else None}
+
     cpu = None
+    err = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, st, dt = cpu_baseline(args.cpu_sample, threads)
+        sample = args.cpu_sample or spec["cpu_sample"]
+        v, st, dt = cpu_baseline(sample, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_sample} paths of the {WORKLOAD} workload (oracle, FP64, OpenMP), {dt:.1f} s"}
+               "sample": f"{sample} paths of the {WORKLOAD} workload (oracle, FP64, OpenMP), {dt:.1f} s"}
+        err = error_vs_oracle(spec["err_paths"], threads)
 
     lat_sorted = sorted(lat)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": statistics.mean(dev_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64 (split: FP64 path length and phase, 3xTF32 tensor-core contraction)" if precision == 0 else "f32",
+        "dtype": ("f32 (split: path length and phase reduction in float-float FP32 in the view kernel and FP64 in the "
+                  "general kernel, 3xTF32 tensor-core contraction with FP32 accumulation, FP64 output)")
+                 if precision == cf.PRECISION_SPLIT else "f32 (plain: FP32 phases, FP32 SIMT contraction)",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "paths_per_step": P, "Nl": Nl, "Nv": Nv, "Nt": Nt, "dims": dims,
                    "precision": args.precision, "parallelism": f"replicas{ws}",
@@ -370,10 +488,14 @@ def run_gpu(args, dist, rank, ws):
         "gpu_launches": int(launches),
         "roofline": roof,
         "kernels": {k: {kk: vv for kk, vv in v.items() if kk not in ("peak_name",)} for k, v in kernels.items()},
+        "plain_fp32": plain,
+        "rel_err_vs_fp64": err,
         "cpu_baseline": cpu,
         "clocks": clk,
         "wall_s": wall,
     }
+    if WORKLOAD == "tracking_2d_pairs":
+        line["config"]["frame_pairs"] = "32 x 32 frames from the 63 lags t2 - t1 (workloads.frame_pairs)"
     scene.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -462,12 +584,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="split", choices=["split", "fp32"])
-    ap.add_argument("--paths-log2", type=int, default=22)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 15)
-    ap.add_argument("--ref-sample", type=int, default=1 << 14)
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default=WORKLOAD, choices=WORKLOADS,
-                    help="correlation_3d (the headline) or speckle_2d (2D far-field field speckle)")
+    ap.add_argument("--paths-log2", type=int, default=0, help="paths per render (log2); 0: the workload's own")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="paths of the CPU oracle sample; 0: the workload's own")
+    ap.add_argument("--ref-sample", type=int, default=0, help="paths per reference-arm step; 0: the workload's own")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle sample and the error subset")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison render")
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS),
+                    help="correlation_3d (the headline), speckle_2d, transmission_matrix_3d or tracking_2d_pairs")
     ap.add_argument("--serve", action="store_true", help="measure the serving mix instead of the headline workload")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-load", type=float, default=2.0, help="arrival rate / one-by-one completion rate")

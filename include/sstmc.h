@@ -76,6 +76,12 @@ extern "C" {
 #define SSTMC_SAMPLER_TEMPORAL              0
 #define SSTMC_SAMPLER_TEMPORAL_CORRELATION  1
 
+/* ConnectionType (Simulation.cuh:80-86): the role of a source. */
+#define SSTMC_CONNECTION_ILLUMINATION  0
+#define SSTMC_CONNECTION_VIEW          1
+#define SSTMC_CONNECTION_ILLUMINATION2 2
+#define SSTMC_CONNECTION_VIEW2         3
+
 /* Contraction precision of the illumination x view accumulation. */
 #define SSTMC_PRECISION_SPLIT  0  /* default: FP64 path length + phase reduction, 3xTF32 tensor-core contraction */
 #define SSTMC_PRECISION_FP32   1  /* plain FP32 form: FP32 phase, FP32 SIMT contraction */
@@ -210,9 +216,15 @@ int32_t sstmc_render(sstmc_scene* scene, uint64_t seed, double* u_out, double* i
  *
  * The scratch is shared by every scene on a device: overlapping calls would
  * race on it, so the library serialises sstmc_render_static calls per device
- * (a call waits for any other one on that device to return).  The first call
- * on a device looks up the scratch's device address (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture. */
+ * (a call waits for any other one on that device to return).  The call waits
+ * on the host for each chunk of paths (it synchronises the scene's stream once
+ * per chunk) and returns when the render is complete.  The first call on a
+ * device looks up the scratch's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ *
+ * The 64 MiB array is part of the library's device image: every device on
+ * which the library's module is loaded holds it until the process exits,
+ * whether or not this entry point is ever called. */
 int32_t sstmc_render_static(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
 
 /* ------------------------------------------------------------------ */
@@ -269,6 +281,105 @@ const char* sstmc_error_string(int32_t code);
 
 /* Detail text of the last failed sstmc_scene_create (config validation). */
 const char* sstmc_last_error_text(void);
+
+/* ------------------------------------------------------------------ */
+/* The reference's object model, one object at a time (the plugin      */
+/* setters).  mexFunction builds Simulation -> Scattering -> Medium ->  */
+/* Sources -> Sampler -> Tracer (MatlabInterface.cu:1677-1700); these   */
+/* handles are built in the same order and the tracer renders exactly   */
+/* what the equivalent sstmc_config renders.  The caller creates every  */
+/* object and destroys it in reverse order; a sampler borrows its       */
+/* sources, medium and scattering, a tracer its sampler.  C++ callers:  */
+/* include/sstmc.hpp wraps these handles in the reference's classes.    */
+/* ------------------------------------------------------------------ */
+typedef struct sstmc_simulation sstmc_simulation;
+typedef struct sstmc_scattering sstmc_scattering;
+typedef struct sstmc_medium sstmc_medium;
+typedef struct sstmc_source sstmc_source;
+typedef struct sstmc_sampler sstmc_sampler;
+typedef struct sstmc_tracer sstmc_tracer;
+
+/* Simulation(err, batchNum, lambda, 1, gpuDeviceNumber) (Simulation.cuh:179);
+ * dims selects sstmc2D (2) or sstmc3D (3), which the reference fixes at
+ * compile time; precision is SSTMC_PRECISION_*. */
+int32_t sstmc_simulation_create(uint32_t dims, uint32_t batch_size, double lambda, int32_t device_number, int32_t precision,
+                                sstmc_simulation** out);
+int32_t sstmc_simulation_destroy(sstmc_simulation* sim);
+
+/* Scattering() and its per-material setters (Scattering.cuh:32-125):
+ * setIsotropicScattering(mat), setHenyeyGreensteinScattering(g, mat),
+ * setTabularScattering(f, N, mat) with f as N (re, im) pairs,
+ * setVonMisesFisherScattering(mu, c, alpha, mixtures, mat). */
+int32_t sstmc_scattering_create(sstmc_scattering** out);
+int32_t sstmc_scattering_set_isotropic(sstmc_scattering* s, uint32_t mat);
+int32_t sstmc_scattering_set_henyey_greenstein(sstmc_scattering* s, double g, uint32_t mat);
+int32_t sstmc_scattering_set_tabular(sstmc_scattering* s, const double* f, uint32_t n, uint32_t mat);
+int32_t sstmc_scattering_set_von_mises_fisher(sstmc_scattering* s, const double* mu, const double* c, const double* alpha,
+                                              uint32_t mixtures, uint32_t mat);
+int32_t sstmc_scattering_destroy(sstmc_scattering* s);
+
+/* HeterogeneousMedium(err, materialGrid, xAxis, nx, yAxis, ny[, zAxis, nz])
+ * (HeterogeneousMedium.cuh, MatlabInterface.cu:998-1003; z NULL in 2D; grid
+ * x fastest) and Medium::setMaterial(MediumMaterial{sigs, siga}, mat)
+ * (MediumInterface.cuh:39-135).  The homogeneous medium is the box form of
+ * config.medium (MatlabInterface.cu:896-945). */
+int32_t sstmc_medium_create_heterogeneous(const uint32_t* grid, const double* x, uint32_t nx, const double* y, uint32_t ny,
+                                          const double* z, uint32_t nz, sstmc_medium** out);
+int32_t sstmc_medium_create_homogeneous(uint32_t dims, const double box_min[3], const double box_max[3], double sigs,
+                                        sstmc_medium** out);
+int32_t sstmc_medium_set_material(sstmc_medium* m, double sigs, double siga, uint32_t mat);
+int32_t sstmc_medium_destroy(sstmc_medium* m);
+
+/* PointSource(err, simulation, medium, scattering, locations, n, isAreaSource,
+ * connectionType) and FarField(err, ..., directions, n, connectionType)
+ * (PointSource.cuh, FarField.cuh; MatlabInterface.cu:1128, 1151).  xyz: n x 3
+ * doubles; connection: SSTMC_CONNECTION_*.  getSourceSize: sstmc_source_size. */
+int32_t sstmc_source_create_point(const sstmc_simulation* sim, int32_t connection, const double* xyz, uint32_t count,
+                                  int32_t is_area_source, sstmc_source** out);
+int32_t sstmc_source_create_far_field(const sstmc_simulation* sim, int32_t connection, const double* xyz, uint32_t count,
+                                      sstmc_source** out);
+int32_t sstmc_source_size(const sstmc_source* s, uint32_t* count);
+int32_t sstmc_source_destroy(sstmc_source* s);
+
+/* TemporalSampler(err, illumination, view, simulation, medium, scattering, t,
+ * tSize, isTemporalAmplitude, isForcedInsideBin) and
+ * TemporalCorrelationSampler(err, illumination, illumination2, view, view2,
+ * simulation, medium, scattering, t, tSize) (MatlabInterface.cu:1281, 1333),
+ * setMaterial(D, U, mat) (:1299, :1350), getIlluminationSize / getViewSize /
+ * getSamplerSize and isCorrelation (SamplerInterface.cuh:132-152). */
+int32_t sstmc_sampler_create_temporal(const sstmc_simulation* sim, const sstmc_medium* medium, const sstmc_scattering* scattering,
+                                      const sstmc_source* illumination, const sstmc_source* view, const double* t, uint32_t t_num,
+                                      int32_t is_temporal_amplitude, int32_t is_forced_inside_bin, sstmc_sampler** out);
+int32_t sstmc_sampler_create_correlation(const sstmc_simulation* sim, const sstmc_medium* medium, const sstmc_scattering* scattering,
+                                         const sstmc_source* illumination, const sstmc_source* illumination2,
+                                         const sstmc_source* view, const sstmc_source* view2, const double* t, uint32_t t_num,
+                                         sstmc_sampler** out);
+int32_t sstmc_sampler_set_material(sstmc_sampler* s, double D, const double U[3], uint32_t mat);
+int32_t sstmc_sampler_shape(const sstmc_sampler* s, uint32_t* nl, uint32_t* nv, uint32_t* nt);
+int32_t sstmc_sampler_is_correlation(const sstmc_sampler* s, int32_t* is_correlation);
+/* The sstmc_config the objects describe (no counterpart: the MEX layer's
+ * config struct in reverse).  Its arrays belong to the sampler and the
+ * objects it borrows, valid until one of them changes or is destroyed. */
+int32_t sstmc_sampler_config(sstmc_sampler* s, uint32_t full_iteration, uint64_t seed, int32_t is_cbs, sstmc_config* out);
+int32_t sstmc_sampler_destroy(sstmc_sampler* s);
+
+/* NextEventEstimation(err, sampler, {fullIterationsNumber, seed, isCBS})
+ * (MatlabInterface.cu:1438): creates the device-resident scene.
+ * trace(v): one rendering into v (2 * Nl * Nv * Nt doubles, the layout of
+ * sstmc_render); updateSeed, getZeroContributionPaths (the missed first
+ * vertices of the last trace), getPhotonsBudget (its scattering vertices,
+ * the participating paths summed over path lengths), getCBS
+ * (TracerInterface.cuh:9-50).  sstmc_tracer_scene gives the scene for
+ * sstmc_last_stats / sstmc_last_timing. */
+int32_t sstmc_tracer_create_nee(sstmc_sampler* sampler, uint32_t full_iteration, uint64_t seed, int32_t is_cbs,
+                                sstmc_tracer** out);
+int32_t sstmc_tracer_trace(sstmc_tracer* t, double* v);
+int32_t sstmc_tracer_update_seed(sstmc_tracer* t, uint64_t seed);
+int32_t sstmc_tracer_zero_contribution_paths(const sstmc_tracer* t, uint64_t* out);
+int32_t sstmc_tracer_photons_budget(const sstmc_tracer* t, uint64_t* out);
+int32_t sstmc_tracer_is_cbs(const sstmc_tracer* t, int32_t* out);
+sstmc_scene* sstmc_tracer_scene(sstmc_tracer* t);
+int32_t sstmc_tracer_destroy(sstmc_tracer* t);
 
 /* ------------------------------------------------------------------ */
 /* Per-path debug trace (parity tests): run one wave of `paths` paths  */

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 OBJDIR = os.path.join(PKG, "_build")
 LIBNAME = "libsstmc_gb300.so"
-SOURCES = ["scene.cpp", "api.cpp", "errors.cpp", "pathwalk.cu", "trace.cu", "viewsum.cu", "contract.cu", "static_render.cu", "gemm_tc.cu", "serve.cpp"]
+SOURCES = ["scene.cpp", "api.cpp", "errors.cpp", "pathwalk.cu", "trace.cu", "viewsum.cu", "contract.cu", "static_render.cu", "gemm_tc.cu", "serve.cpp", "plugins.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -76,8 +76,54 @@ def load_library() -> C.CDLL:
     lib.sstmc_cancel.restype = i32
     lib.sstmc_server_stats.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(u64)]
     lib.sstmc_server_stats.restype = i32
+    _declare_objects(lib)
     _LIB = lib
     return lib
+
+
+def _declare_objects(lib: C.CDLL) -> None:
+    """Signatures of the object-model entry points (sstmc_simulation_* ..
+    sstmc_tracer_*), the reference's plugin setters."""
+    i32, u32, u64, vp, d = C.c_int32, C.c_uint32, C.c_uint64, C.c_void_p, C.c_double
+    dp, up = C.POINTER(C.c_double), C.POINTER(C.c_uint32)
+    sig = {
+        "sstmc_simulation_create": [u32, u32, d, i32, i32, C.POINTER(vp)],
+        "sstmc_simulation_destroy": [vp],
+        "sstmc_scattering_create": [C.POINTER(vp)],
+        "sstmc_scattering_set_isotropic": [vp, u32],
+        "sstmc_scattering_set_henyey_greenstein": [vp, d, u32],
+        "sstmc_scattering_set_tabular": [vp, dp, u32, u32],
+        "sstmc_scattering_set_von_mises_fisher": [vp, dp, dp, dp, u32, u32],
+        "sstmc_scattering_destroy": [vp],
+        "sstmc_medium_create_heterogeneous": [up, dp, u32, dp, u32, dp, u32, C.POINTER(vp)],
+        "sstmc_medium_create_homogeneous": [u32, dp, dp, d, C.POINTER(vp)],
+        "sstmc_medium_set_material": [vp, d, d, u32],
+        "sstmc_medium_destroy": [vp],
+        "sstmc_source_create_point": [vp, i32, dp, u32, i32, C.POINTER(vp)],
+        "sstmc_source_create_far_field": [vp, i32, dp, u32, C.POINTER(vp)],
+        "sstmc_source_size": [vp, up],
+        "sstmc_source_destroy": [vp],
+        "sstmc_sampler_create_temporal": [vp, vp, vp, vp, vp, dp, u32, i32, i32, C.POINTER(vp)],
+        "sstmc_sampler_create_correlation": [vp, vp, vp, vp, vp, vp, vp, dp, u32, C.POINTER(vp)],
+        "sstmc_sampler_set_material": [vp, d, dp, u32],
+        "sstmc_sampler_shape": [vp, up, up, up],
+        "sstmc_sampler_is_correlation": [vp, C.POINTER(i32)],
+        "sstmc_sampler_config": [vp, u32, u64, i32, C.POINTER(cf.SstmcConfig)],
+        "sstmc_sampler_destroy": [vp],
+        "sstmc_tracer_create_nee": [vp, u32, u64, i32, C.POINTER(vp)],
+        "sstmc_tracer_trace": [vp, dp],
+        "sstmc_tracer_update_seed": [vp, u64],
+        "sstmc_tracer_zero_contribution_paths": [vp, C.POINTER(u64)],
+        "sstmc_tracer_photons_budget": [vp, C.POINTER(u64)],
+        "sstmc_tracer_is_cbs": [vp, C.POINTER(i32)],
+        "sstmc_tracer_destroy": [vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = i32
+    lib.sstmc_tracer_scene.argtypes = [vp]
+    lib.sstmc_tracer_scene.restype = vp
 
 
 def error_string(code: int) -> str:

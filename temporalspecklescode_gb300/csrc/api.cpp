@@ -70,6 +70,7 @@ size_t Engine::bytes_per_path(const Scene& S)
     return 8 * Nt * (2 * Nl + 2 * Nv) + (S.correlation ? 8 * Nt * Nl : 0) + 4 * Nl + 12 + 1 + 12 * Nt + 16
          + ((S.cfg_copy.is_cbs && !S.correlation) ? 8 * Nt * (Nl + Nv) : 0)   // field CBS: the reversed path's rows
          + 4                                                                  // p2 (correlation CBS)
+         + 4 + 1                                                              // single-scattering row, partition scratch
          + walk_slot_bytes_per_path();
 }
 
@@ -117,7 +118,10 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
            && alloc((void**)&ovf, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * kWalkSlotVerts * sizeof(float4))
            && alloc((void**)&ovf_owner, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * sizeof(uint2))
-           && alloc((void**)&p2v, paths * sizeof(float));
+           && alloc((void**)&p2v, paths * sizeof(float))
+           && alloc((void**)&ss_row, paths * sizeof(uint32_t))
+           && alloc((void**)&ss_hist, ((paths + 1023) / 1024) * kMat * sizeof(uint32_t))
+           && alloc((void**)&ss_bucket, (kMat + 1) * sizeof(uint32_t));
     if (!ok) { release(); return SSTMC_ALLOCATION_ERROR; }
     ovf_blocks = std::max(walk_overflow_blocks(paths), ovf_want);
     cap = paths;
@@ -127,10 +131,11 @@ int Engine::ensure(Scene& S, uint32_t paths)
 void Engine::release()
 {
     void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts,
-                   slots, longq, ovf, ovf_owner, p2v };
+                   slots, longq, ovf, ovf_owner, p2v, ss_row, ss_hist, ss_bucket };
     for (void* p : ps) if (p) cudaFreeAsync(p, stream);
     counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
     slots = nullptr; longq = nullptr; ovf = nullptr; ovf_owner = nullptr; p2v = nullptr;
+    ss_row = ss_hist = ss_bucket = nullptr;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
     pl = x1 = x1t = nullptr;
     m1 = nullptr; totals = nullptr; err = nullptr; V = nullptr; W = nullptr;
@@ -273,6 +278,21 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         ovf_blocks = (uint32_t)want;
         ovf_want = std::max(ovf_want, (uint32_t)want);
     }
+    // far-field x far-field single scattering on the tensor cores: group the
+    // paths' single-scattering rows by first-vertex material, so each material's
+    // GEMM reads only its own rows (contract_chunk)
+    const bool farfar_tc = S.hsrc[0].type == SSTMC_SOURCE_FARFIELD && S.hsrc[1].type == SSTMC_SOURCE_FARFIELD && !S.dev.has_amp64;
+    ss_bucketed = farfar_tc && ss_row && !dbg && !S.cfg_copy.is_cbs && use_tensor_cores() && S.precision == SSTMC_PRECISION_SPLIT
+               && S.Nl % 2 == 0 && S.Nv % 2 == 0;
+    if (ss_bucketed) {
+        SsBucketParams Bp;
+        std::memset(&Bp, 0, sizeof(Bp));
+        Bp.verts = verts; Bp.counts = counts; Bp.offsets = offsets; Bp.n = n;
+        Bp.hist = ss_hist; Bp.ss_row = ss_row; Bp.bucket = ss_bucket;
+        e = launch_ss_buckets(Bp, stream);
+        if (e) return e;
+        launches += 3;
+    }
     if (timing && ev[6]) cudaEventRecord(ev[6], stream);
 
     // 2. NEE vectors per path (trace.cu)
@@ -284,6 +304,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     T.verts = verts; T.counts = counts; T.offsets = offsets; T.misses = misses;
     T.a_ms = a_ms; T.s_ms = s_ms; T.a_ss = a_ss; T.b_ss = b_ss; T.g2 = g2; T.pl = pl;
     T.x1 = x1; T.x1t = S.correlation ? nullptr : x1t; T.m1 = m1; T.totals = totals; T.err = err;
+    T.ss_row = ss_bucketed ? ss_row : nullptr;
     if (dbg) T.dda = dbg->dda;
     if (S.correlation && S.cfg_copy.is_cbs) T.p2 = p2v;   // for the CBS cross terms (contract_chunk)
     rows_real = false;
@@ -401,12 +422,26 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
         if (e) return e;
         const size_t per = (size_t)S.Nt * S.Nv * S.Nl;
         G.A = a_ss; G.B = b_ss; G.mat = m1; G.real = 0; G.K = (int)n; G.scale = 1.0;
-        for (int m : S.materials_present) {
-            G.mat_sel = m;
-            G.W = W + (size_t)m * per;
+        if (ss_bucketed && !tc) return SSTMC_MISC_ERROR;   // grouped rows are written only for the tensor-core form
+        if (ss_bucketed) {
+            // rows grouped by material: one launch, each material's GEMM over its own rows
+            G.mat = nullptr;
+            G.bucket = ss_bucket;
+            G.W = W;
+            G.wstride = per;
+            G.nmat = 0;
+            for (int m : S.materials_present) G.mats[G.nmat++] = m;
             e = gemm(G);
             if (e) return e;
             launches++;
+        } else {
+            for (int m : S.materials_present) {
+                G.mat_sel = m;
+                G.W = W + (size_t)m * per;
+                e = gemm(G);
+                if (e) return e;
+                launches++;
+            }
         }
     } else {
         SsParams P;

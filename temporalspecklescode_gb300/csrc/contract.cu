@@ -540,6 +540,115 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
         }
 }
 
+
+// ---- paths grouped by first-vertex material (far-field x far-field single scattering) ----
+// The far-field x far-field single-scattering term weighs each (l, v) by a
+// table of the first vertex's material, so its contraction runs once per
+// material over that material's paths.  A stable partition of the chunk's
+// paths by material gives each path its row in the single-scattering rows and
+// each material a contiguous row range: ss_row[q] and bucket[m] .. bucket[m + 1].
+// Three launches: per-block counts, one block scanning them, per-block ranks.
+constexpr int kBucketBlock = 1024;
+
+__device__ __forceinline__ int first_material(const SsBucketParams& P, uint32_t q)
+{
+    return P.counts[q] ? (int)(__float_as_uint(P.verts[P.offsets[q]].w) & 15u) : 0;
+}
+
+__global__ void __launch_bounds__(kBucketBlock) bucket_count_kernel(const SsBucketParams P)
+{
+    __shared__ uint32_t h[kMat];
+    if (threadIdx.x < kMat) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t q = blockIdx.x * kBucketBlock + threadIdx.x;
+    if (q < P.n) atomicAdd(&h[first_material(P, q)], 1u);
+    __syncthreads();
+    if (threadIdx.x < kMat) P.hist[blockIdx.x * kMat + threadIdx.x] = h[threadIdx.x];
+}
+
+// One block: per material the exclusive scan of the per-block counts, offset
+// by the rows of the lower materials; hist becomes each block's first row per
+// material, bucket[m] the first row of material m, bucket[kMat] = n.
+__global__ void __launch_bounds__(kBucketBlock) bucket_scan_kernel(const SsBucketParams P)
+{
+    __shared__ uint32_t warp_sums[kBucketBlock / 32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t base = 0;
+    for (int m = 0; m < kMat; ++m) {
+        if (threadIdx.x == 0) carry = base;
+        __syncthreads();
+        for (uint32_t b0 = 0; b0 < P.nblocks; b0 += kBucketBlock) {
+            const uint32_t b = b0 + threadIdx.x;
+            const uint32_t v = b < P.nblocks ? P.hist[b * kMat + m] : 0u;
+            uint32_t x = v;   // inclusive warp scan
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (lane == 31) warp_sums[w] = x;
+            __syncthreads();
+            if (w == 0) {
+                uint32_t s = warp_sums[lane];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                    if (lane >= o) s += y;
+                }
+                warp_sums[lane] = s;   // inclusive over warps
+            }
+            __syncthreads();
+            const uint32_t before = carry + (w ? warp_sums[w - 1] : 0u) + x - v;
+            if (b < P.nblocks) P.hist[b * kMat + m] = before;
+            __syncthreads();
+            if (threadIdx.x == kBucketBlock - 1) carry = before + v;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) P.bucket[m] = base;
+        base = carry;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) P.bucket[kMat] = base;
+}
+
+// Rank of each path among the earlier paths of its block with the same
+// material (warp match masks, then the earlier warps' counts): the partition
+// is stable, so the rows keep the paths' order within a material.
+__global__ void __launch_bounds__(kBucketBlock) bucket_scatter_kernel(const SsBucketParams P)
+{
+    __shared__ uint32_t wc[kBucketBlock / 32][kMat];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t q = blockIdx.x * kBucketBlock + threadIdx.x;
+    for (int i = threadIdx.x; i < (kBucketBlock / 32) * kMat; i += kBucketBlock) (&wc[0][0])[i] = 0;
+    __syncthreads();
+    const bool in = q < P.n;
+    const int m = in ? first_material(P, q) : kMat;   // kMat: no path
+    const uint32_t same = __match_any_sync(0xffffffffu, m);
+    const uint32_t rank = __popc(same & ((1u << lane) - 1u));
+    if (in && rank == 0) wc[w][m] = __popc(same);
+    __syncthreads();
+    if (in) {
+        uint32_t before = 0;
+        for (int j = 0; j < w; ++j) before += wc[j][m];
+        P.ss_row[q] = P.hist[blockIdx.x * kMat + m] + before + rank;
+    }
+}
+
+}  // namespace
+
+int launch_ss_buckets(const SsBucketParams& P, cudaStream_t stream)
+{
+    if (P.n == 0) return SSTMC_NO_ERROR;
+    SsBucketParams Q = P;
+    Q.nblocks = (P.n + kBucketBlock - 1) / kBucketBlock;
+    bucket_count_kernel<<<Q.nblocks, kBucketBlock, 0, stream>>>(Q);
+    bucket_scan_kernel<<<1, kBucketBlock, 0, stream>>>(Q);
+    bucket_scatter_kernel<<<Q.nblocks, kBucketBlock, 0, stream>>>(Q);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
+
+namespace {
 }  // namespace
 
 int launch_gemm(const GemmParams& G, cudaStream_t stream)

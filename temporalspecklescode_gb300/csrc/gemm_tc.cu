@@ -241,6 +241,7 @@ __device__ __forceinline__ void two_sum(float& hi, float& lo, float x)
 
 struct TcParams {
     GemmParams G;
+    int ksplit;        // path ranges per tile (per material with G.bucket)
     int tiles_m, tiles_n;
     int tdim;          // middle tensor dimension: Nt ticks (complex) or Nt / 2 tick pairs (real)
     CUtensorMap tmA;   // A viewed as [K paths][tdim][2 Nl floats], box 32 x 1 x 128
@@ -320,10 +321,24 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
     int bid = blockIdx.x;
     const int tn = bid % P.tiles_n; bid /= P.tiles_n;
     const int tm = bid % P.tiles_m; bid /= P.tiles_m;
-    const int t = bid % P.tdim;
-    const int ks = bid / P.tdim;
-    const int kb = ks * G.kchunk;
-    const int ke = min(G.K, kb + G.kchunk);
+    const int t = bid % P.tdim; bid /= P.tdim;
+    int kb, ke;
+    const float* W = G.W;
+    if (G.bucket) {
+        // material mats[bid % nmat]: its rows bucket[m] .. bucket[m + 1], split in
+        // ksplit ranges of whole accumulation windows, and its weight table
+        const int m = G.mats[bid % G.nmat];
+        const int ks = bid / G.nmat;
+        const int rb = (int)G.bucket[m], re = (int)G.bucket[m + 1];
+        const int win = kKS * kWinSteps;
+        const int kc = ((re - rb + P.ksplit - 1) / P.ksplit + win - 1) / win * win;
+        kb = rb + ks * kc;
+        ke = min(re, kb + kc);
+        W = G.W + (size_t)m * G.wstride;
+    } else {
+        kb = bid * G.kchunk;
+        ke = min(G.K, kb + G.kchunk);
+    }
     const int nsteps = ke > kb ? (ke - kb + kKS - 1) / kKS : 0;
     const int m0 = tm * kTM, n0 = tn * kTN;
 
@@ -476,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
                     const int nt = gn / G.Nv, v = gn - nt * G.Nv;
                     if (nt == mt && mt < 2 && tick < G.Nt) {
                         const size_t o = ((size_t)tick * G.Nv + v) * G.Nl + l;
-                        const double wv = (G.W ? (double)G.W[o] : 1.0) * (G.scale != 0.0 ? G.scale : 1.0);
+                        const double wv = (W ? (double)W[o] : 1.0) * (G.scale != 0.0 ? G.scale : 1.0);
                         atomicAdd(&G.V[o].x, ((double)hv[e] + (double)lv[e]) * wv);
                     }
                 }
@@ -502,7 +517,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_tc_kernel(const __grid_const
                     const int v = (n0 + 16 * c + 2 * j) >> 1;
                     if (l < G.Nl && v < G.Nv) {
                         const size_t o = ((size_t)t * G.Nv + v) * G.Nl + l;
-                        const double wv = (G.W ? (double)G.W[o] : 1.0) * (G.scale != 0.0 ? G.scale : 1.0);
+                        const double wv = (W ? (double)W[o] : 1.0) * (G.scale != 0.0 ? G.scale : 1.0);
                         atomicAdd(odd ? &G.V[o].y : &G.V[o].x, val * wv);
                     }
                 }
@@ -570,13 +585,34 @@ int launch_gemm_tc(const GemmParams& G, cudaStream_t stream)
     P.tiles_m = (2 * G.Nl + kTM - 1) / kTM;
     P.tiles_n = (2 * G.Nv + kTN - 1) / kTN;
     P.tdim = G.real ? G.Nt / 2 : G.Nt;
-    const long long tiles = (long long)P.tiles_m * P.tiles_n * P.tdim;
+    const long long tiles = (long long)P.tiles_m * P.tiles_n * P.tdim * (G.bucket ? G.nmat : 1);
+    // K split: fewer tiles than SMs take sms / tiles ranges each; more tiles take
+    // the smallest split (up to 8) whose CTAs fill their last wave to 95 % (one
+    // CTA per SM: a partly filled last wave idles the rest of the SMs)
     int ksplit = (int)std::max<long long>(1, sms / std::max<long long>(1, tiles));
+    if (tiles >= sms) {
+        double best = 0.0;
+        for (int ks = 1; ks <= 8; ++ks) {
+            const long long ctas = tiles * ks, waves = (ctas + sms - 1) / sms;
+            const double eff = (double)ctas / (double)(waves * sms);
+            if (eff > best + 0.02) { best = eff; ksplit = ks; }
+            if (eff >= 0.95) break;
+        }
+    }
     const int win = kKS * kWinSteps;
-    int kchunk = (G.K + ksplit - 1) / ksplit;
-    kchunk = ((kchunk + win - 1) / win) * win;
-    ksplit = (G.K + kchunk - 1) / kchunk;
-    P.G.kchunk = kchunk;
+    if (G.bucket) {
+        // the materials' row counts are on the device: at most K / nmat rows on
+        // average, at least one window per range
+        const int avg = std::max(1, G.K / std::max(1, G.nmat));
+        ksplit = std::max(1, std::min(ksplit, (avg + win - 1) / win));
+        if (G.nmat < 1 || G.nmat > kMat) return SSTMC_CUBLAS_ERROR;
+    } else {
+        int kchunk = (G.K + ksplit - 1) / ksplit;
+        kchunk = ((kchunk + win - 1) / win) * win;
+        ksplit = (G.K + kchunk - 1) / kchunk;
+        P.G.kchunk = kchunk;
+    }
+    P.ksplit = ksplit;
     // complex: 2 Nl floats (re, im) per tick; real: 2 Nl floats per tick pair
     if (!encode_rows(&P.tmA, G.A, 2 * G.Nl, P.tdim, G.K, kTM) || !encode_rows(&P.tmB, G.B, 2 * G.Nv, P.tdim, G.K, kTN))
         return SSTMC_CUBLAS_ERROR;

@@ -270,20 +270,21 @@ __device__ __forceinline__ float tau_single(const DevScene& S, const V3& o, cons
 
 // Optical depth from x along the exact direction d (a table direction), with
 // the voxel-step count of the bit-exact traversal.
-__device__ __forceinline__ float tau_dir(const DevScene& S, const V3& x, const V3& d, uint32_t& steps)
+// cell: x's packed grid cell (cell_of) when the caller has it.
+__device__ __forceinline__ float tau_dir(const DevScene& S, const V3& x, const V3& d, uint32_t& steps, uint32_t cell = kNoCell)
 {
     if (S.single) {
         if (!inside(S, x)) return 0.0f;
         steps += 1;
         return tau_single(S, x, d);
     }
-    return dda(S, x, d, steps);
+    return dda(S, x, d, steps, cell);
 }
 
 // Optical depth from x toward the point s.  Multi-cell media traverse along
 // the IEEE-normalised direction (decision path); a single cell needs no exact
 // direction.
-__device__ __forceinline__ float tau_to_point(const DevScene& S, const V3& x, const V3& s, uint32_t& steps)
+__device__ __forceinline__ float tau_to_point(const DevScene& S, const V3& x, const V3& s, uint32_t& steps, uint32_t cell = kNoCell)
 {
     if (S.single) {
         if (!inside(S, x)) return 0.0f;
@@ -291,7 +292,7 @@ __device__ __forceinline__ float tau_to_point(const DevScene& S, const V3& x, co
         return tau_single(S, x, funit(sub3(s, x)));
     }
     const V3 dir = normalize32(S.dims, V3{ fsb(s.x, x.x), fsb(s.y, x.y), fsb(s.z, x.z) });
-    return dda(S, x, dir, steps);
+    return dda(S, x, dir, steps, cell);
 }
 
 // Henyey-Greenstein pdf / amplitude from two unit directions with fast

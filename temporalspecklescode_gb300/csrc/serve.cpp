@@ -9,7 +9,10 @@
 // it on the scene's own stream with chunk buffers sized to the reservation,
 // returns the buffers to the stream-ordered pool and marks the ticket done.
 // Requests on different scenes therefore overlap on the device; requests on
-// the same scene run one after another (the scene's lock).  A render's
+// the same scene run one after another: a queued request whose scene is
+// rendering is passed over (it would only wait for the scene's lock while
+// holding a worker and a reservation), so requests on other scenes behind it
+// are admitted first.  A render's
 // result depends only on (scene, seed): the paths' random streams are keyed
 // by path id and the chunking is invisible, so a request gives the same
 // result alone and in the mix (up to the order of the FP64 accumulation).
@@ -58,6 +61,7 @@ struct sstmc_server {
     std::unordered_map<uint64_t, std::unique_ptr<ServeRequest>> reqs;
     size_t reserved = 0;
     uint32_t running = 0;
+    std::unordered_map<const sstmc_scene*, uint32_t> busy;   // scenes with a request rendering
     bool stop = false;
     uint64_t next_id = 1;
     std::vector<std::thread> workers;
@@ -70,8 +74,9 @@ struct sstmc_server {
 
 namespace {
 
-// First queued request that fits next to the requests in flight (cancelled
-// ones are completed on the way).  Caller holds srv->mu.
+// First queued request whose scene is idle and whose reservation fits next to
+// the requests in flight (cancelled ones are completed on the way).  Caller
+// holds srv->mu.
 ServeRequest* admit(sstmc_server* srv)
 {
     for (auto it = srv->queue.begin(); it != srv->queue.end();) {
@@ -84,6 +89,7 @@ ServeRequest* admit(sstmc_server* srv)
             srv->cv_done.notify_all();
             continue;
         }
+        if (srv->busy.count(r->scene)) { ++it; continue; }
         if (srv->running == 0 || srv->reserved + r->need <= srv->budget) {
             srv->queue.erase(it);
             return r;
@@ -103,6 +109,7 @@ void worker(sstmc_server* srv)
         if (!r) return;   // stopping with nothing admissible
         srv->reserved += r->need;
         srv->running++;
+        srv->busy[r->scene]++;
         r->t_start = Clock::now();
         if (!srv->any) { srv->any = true; srv->first_start = r->t_start; }
         lk.unlock();
@@ -111,6 +118,7 @@ void worker(sstmc_server* srv)
         lk.lock();
         srv->reserved -= r->need;
         srv->running--;
+        if (--srv->busy[r->scene] == 0) srv->busy.erase(r->scene);
         r->status = st;
         r->contributions = contrib;
         r->t_end = Clock::now();

@@ -37,6 +37,13 @@ struct Engine {
     uint32_t ovf_blocks = 0;      // overflow blocks allocated
     uint32_t ovf_want = 0;        // learned pool size: a chunk that found the pool short grows it
     float* p2v = nullptr;         // [paths] second-point probability (correlation CBS)
+    // far-field x far-field single scattering: the chunk's paths grouped by
+    // first-vertex material (contract.cu launch_ss_buckets); null in the
+    // static-scratch render, which contracts per material with masks instead
+    uint32_t* ss_row = nullptr;   // [paths] row of each path in a_ss / b_ss
+    uint32_t* ss_hist = nullptr;  // [ceil(paths / 1024)][kMat] scratch of the partition
+    uint32_t* ss_bucket = nullptr;  // [kMat + 1] first row of each material
+    bool ss_bucketed = false;     // the chunk's a_ss / b_ss rows are grouped (trace_chunk -> contract_chunk)
     uint2* ovf_owner = nullptr;
     float4* verts = nullptr;
     size_t verts_cap = 0;

@@ -195,7 +195,11 @@ int render_one_static(Scene& S, Engine& E, unsigned char* base, bool farfar, uin
     if (total > 0xffffffffull) return SSTMC_NOT_SUPPORTED;
     const Layout L1 = layout(S, farfar, 1);
     if (L1.rows_end + 64 * sizeof(float4) > kStaticScratchBytes) return scratch_limit("the scene's output and tables");
-    const size_t per_path = L1.rows_end - L1.fixed_end;  // upper bound (rounding included)
+    // bytes per path of the chunk buffers: the slope between two chunk sizes (the
+    // walk's overflow pool has a fixed part of 64 blocks that one path must not be
+    // charged for); the first chunk takes half of the room after the fixed part,
+    // the vertices the rest
+    const size_t per_path = std::max<size_t>(1, (layout(S, farfar, 2048).rows_end - layout(S, farfar, 1024).rows_end) / 1024);
     const size_t room = kStaticScratchBytes - L1.fixed_end;
     uint32_t n = (uint32_t)std::min<uint64_t>(total, std::max<size_t>(1, room / 2 / per_path));
     const size_t nout = (size_t)S.Nt * S.Nv * S.Nl;
@@ -236,13 +240,9 @@ int render_one_static(Scene& S, Engine& E, unsigned char* base, bool farfar, uin
     return SSTMC_NO_ERROR;
 }
 
-}  // namespace
-
-int render_static(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, double* iter_out)
+int render_static_locked(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, double* iter_out)
 {
     const int dev = S.device;
-    if (dev < 0 || dev >= kMaxDevices) return SSTMC_DEVICE_ERROR;
-    std::lock_guard<std::mutex> lk(g_dev_mu[dev]);
     unsigned char* base = nullptr;
     int e = scratch_base(dev, &base);
     if (e) return e;
@@ -282,6 +282,20 @@ int render_static(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, d
         if (e) return e;
     }
     return SSTMC_NO_ERROR;
+}
+
+}  // namespace
+
+int render_static(Scene& S, cudaStream_t stream, uint64_t seed, double* u_out, double* iter_out)
+{
+    const int dev = S.device;
+    if (dev < 0 || dev >= kMaxDevices) return SSTMC_DEVICE_ERROR;
+    std::lock_guard<std::mutex> lk(g_dev_mu[dev]);
+    const int e = render_static_locked(S, stream, seed, u_out, iter_out);
+    // an error can leave copies and kernels queued on the stream that still use
+    // the scratch: they end before the lock lets another call reuse it
+    if (e) (void)cudaStreamSynchronize(stream);
+    return e;
 }
 
 }  // namespace sstmc

@@ -152,6 +152,7 @@ __device__ __forceinline__ float tick_w(const DevScene& S, const float* buf, int
 
 __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, int lane)
 {
+    const uint32_t qs = T.ss_row ? T.ss_row[q] : q;   // row of the single-scattering rows
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
     if (T.cbs) {   // reversed pass: Gv0 rows (first pass) and this pass's GlSum entries
         if (T.pass0)
@@ -163,9 +164,9 @@ __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, i
     if (T.pass0) {
         for (int i = lane; i < Nt * Nl; i += 32) {
             T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
-            T.a_ss[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
+            T.a_ss[(size_t)qs * Nt * Nl + i] = make_float2(0.f, 0.f);
         }
-        for (int i = lane; i < Nt * Nv; i += 32) T.b_ss[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
+        for (int i = lane; i < Nt * Nv; i += 32) T.b_ss[(size_t)qs * Nt * Nv + i] = make_float2(0.f, 0.f);
     }
     if (T.views)
         for (int t = T.t0; t < T.t0 + T.tn; ++t)
@@ -177,14 +178,15 @@ __device__ void zero_rows(const DevScene& S, const TraceParams& T, uint32_t q, i
 // |g|^2 of source element k at x: the attenuation weight T c / r^(D-1)
 // (point source, PointSource.cuh:117-172) or T (far field, FarField.cuh:223-263).
 template <bool PT>
-__device__ __forceinline__ float gweight(const DevScene& S, const DevSource& s, int k, const V3& x, int role, uint32_t& steps)
+__device__ __forceinline__ float gweight(const DevScene& S, const DevSource& s, int k, const V3& x, int role, uint32_t& steps,
+                                         uint32_t cell = kNoCell)
 {
     if constexpr (!PT) {
         const V3 d = load3(s.p, k);
-        return expf(-tau_dir(S, x, role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d, steps));
+        return expf(-tau_dir(S, x, role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d, steps, cell));
     } else {
         const V3 sp = load3(s.p, k);
-        const float T = expf(-tau_to_point(S, x, sp, steps));
+        const float T = expf(-tau_to_point(S, x, sp, steps, cell));
         const V3 v = sub3(x, sp);
         const float r2 = dot3(v, v);
         float at = S.dims == 3 ? __fdividef(T * kIsoAmp3, r2) : T * rsqrtf(r2);
@@ -196,13 +198,14 @@ __device__ __forceinline__ float gweight(const DevScene& S, const DevSource& s, 
 // g with its phase.  Split precision: the argument d.x / lambda (far field)
 // or r / lambda (point source) is formed and reduced modulo one cycle in FP64.
 template <bool PT>
-__device__ __forceinline__ float2 gcomplex(const DevScene& S, const DevSource& s, int k, const V3& x, int role, uint32_t& steps)
+__device__ __forceinline__ float2 gcomplex(const DevScene& S, const DevSource& s, int k, const V3& x, int role, uint32_t& steps,
+                                           uint32_t cell = kNoCell)
 {
     const bool split = S.precision == SSTMC_PRECISION_SPLIT;
     float f, a;
     if constexpr (!PT) {
         const V3 d = load3(s.p, k);
-        a = sqrtf(expf(-tau_dir(S, x, role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d, steps)));
+        a = sqrtf(expf(-tau_dir(S, x, role == kRoleIllum ? V3{ -d.x, -d.y, -d.z } : d, steps, cell)));
         if (split) {
             const double dx = fma((double)d.x, (double)x.x, fma((double)d.y, (double)x.y, (double)d.z * (double)x.z));
             f = frac_cycles((role == kRoleIllum ? dx : -dx) * S.inv_lambda);
@@ -213,7 +216,7 @@ __device__ __forceinline__ float2 gcomplex(const DevScene& S, const DevSource& s
         }
     } else {
         const V3 sp = load3(s.p, k);
-        const float T = expf(-tau_to_point(S, x, sp, steps));
+        const float T = expf(-tau_to_point(S, x, sp, steps, cell));
         const V3 v = sub3(x, sp);
         const float r2 = dot3(v, v);
         float at = S.dims == 3 ? __fdividef(T * kIsoAmp3, r2) : T * rsqrtf(r2);
@@ -231,14 +234,15 @@ __device__ __forceinline__ float2 gcomplex(const DevScene& S, const DevSource& s
 }
 
 template <bool PT>
-__device__ __forceinline__ float pfirst_t(const DevScene& S, const DevSource& s, int l, const V3& x, uint32_t& steps)
+__device__ __forceinline__ float pfirst_t(const DevScene& S, const DevSource& s, int l, const V3& x, uint32_t& steps,
+                                          uint32_t cell = kNoCell)
 {
     if constexpr (!PT) {
         const V3 d = load3(s.p, l);
-        return expf(-tau_dir(S, x, V3{ -d.x, -d.y, -d.z }, steps)) * s.sprob[l];
+        return expf(-tau_dir(S, x, V3{ -d.x, -d.y, -d.z }, steps, cell)) * s.sprob[l];
     } else {
         const V3 sp = load3(s.p, l);
-        const float T = expf(-tau_to_point(S, x, sp, steps));
+        const float T = expf(-tau_to_point(S, x, sp, steps, cell));
         const V3 v = sub3(x, sp);
         const float r2 = dot3(v, v);
         return S.dims == 3 ? __fdividef(T, (float)(4.0 * kPi) * r2) : T * (float)(8.0 * kPi) * rsqrtf(r2);
@@ -331,6 +335,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     for (uint32_t q = gw; q < T.paths; q += nw) {
         const uint32_t pid = T.first_path + q;
         const uint32_t B = T.counts[q];
+        const uint32_t qs = T.ss_row ? T.ss_row[q] : q;   // row of the single-scattering rows
         if (B == 0) {  // the walk hit a limit (error already flagged)
             zero_rows(S, T, q, lane);
             continue;
@@ -340,6 +345,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         const V3 x1 = V3{ v1.x, v1.y, v1.z };
         const int m1 = (int)(__float_as_uint(v1.w) & 15u);
         const float xi1 = (float)(__float_as_uint(v1.w) >> 4) * (1.0f / 16777216.0f);
+        const uint32_t c1 = S.single ? kNoCell : cell_of(S, x1);   // x1's grid cell, the start of its NEE rays
         float* xtc = bufA;   // tick positions of the current vertex
         float* xtn = bufB;   // tick positions of the new vertex
         bool mov1 = false;
@@ -358,10 +364,10 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             float ps = 0.0f;
             for (int l = lane; l < Nl; l += 32) {
                 uint32_t st = 0;
-                float P = pfirst_t<ILP>(S, il, l, x1, st);
+                float P = pfirst_t<ILP>(S, il, l, x1, st, c1);
                 if (CORR) {
                     if (S.sym) st *= 2;
-                    else P = 0.5f * (P + pfirst_t<ILP>(S, il2, l, x1, st));
+                    else P = 0.5f * (P + pfirst_t<ILP>(S, il2, l, x1, st, c1));
                 }
                 steps += st;
                 T.pl[(size_t)q * Nl + l] = P;
@@ -376,14 +382,15 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     float w = 0.0f;
                     float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
                     uint32_t sts = 0;
-                    if (realg) { w = gweight<ILP>(S, il, l, x1, kRoleIllum, sts); sts *= 2; }
-                    else if (st1) { g1s = gcomplex<ILP>(S, il, l, x1, kRoleIllum, sts); g2s = gcomplex<ILP>(S, il2, l, x1, kRoleIllum, sts); }
+                    if (realg) { w = gweight<ILP>(S, il, l, x1, kRoleIllum, sts, c1); sts *= 2; }
+                    else if (st1) { g1s = gcomplex<ILP>(S, il, l, x1, kRoleIllum, sts, c1); g2s = gcomplex<ILP>(S, il2, l, x1, kRoleIllum, sts, c1); }
                     for (int t = lane / T.lw; t < Nt; t += T.lg) {
                         const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                        const size_t os = ((size_t)qs * Nt + t) * Nl + l;
                         if (realg) {
                             steps += sts;
                             T.a_ms[o] = make_float2(w, 0.f);
-                            T.a_ss[o] = make_float2(w * p1inv, 0.f);
+                            T.a_ss[os] = make_float2(w * p1inv, 0.f);
                         } else {
                             float2 g1 = g1s, g2 = g2s;
                             if (st1) steps += sts;
@@ -394,7 +401,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                             }
                             T.a_ms[o] = g1;
                             T.g2[o] = g2;
-                            T.a_ss[o] = c_scale(c_mulc(g1, g2), p1inv);
+                            T.a_ss[os] = c_scale(c_mulc(g1, g2), p1inv);
                         }
                     }
                 }
@@ -402,8 +409,8 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     float w = 0.0f;
                     float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
                     uint32_t sts = 0;
-                    if (realg) { w = gweight<VWP>(S, vw, v, x1, kRoleView, sts); sts *= 2; }
-                    else if (st1) { g1s = gcomplex<VWP>(S, vw, v, x1, kRoleView, sts); g2s = gcomplex<VWP>(S, vw2, v, x1, kRoleView, sts); }
+                    if (realg) { w = gweight<VWP>(S, vw, v, x1, kRoleView, sts, c1); sts *= 2; }
+                    else if (st1) { g1s = gcomplex<VWP>(S, vw, v, x1, kRoleView, sts, c1); g2s = gcomplex<VWP>(S, vw2, v, x1, kRoleView, sts, c1); }
                     for (int t = lane / T.vwa; t < Nt; t += T.tga) {
                         float2 b;
                         if (realg) { steps += sts; b = make_float2(w, 0.f); }
@@ -413,7 +420,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                             b = c_mulc(gcomplex<VWP>(S, vw, v, shift_u(S, x1, m1, tau, -1.0f), kRoleView, steps),
                                        gcomplex<VWP>(S, vw2, v, shift_u(S, x1, m1, tau, 1.0f), kRoleView, steps));
                         }
-                        T.b_ss[((size_t)q * Nt + t) * Nv + v] = b;
+                        T.b_ss[((size_t)qs * Nt + t) * Nv + v] = b;
                     }
                 }
             } else {
@@ -421,25 +428,24 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 for (int l = lane % T.lw; l < Nl; l += T.lw) {
                     float2 gs = make_float2(0.f, 0.f);
                     uint32_t sts = 0;
-                    if (!mov1) gs = gcomplex<ILP>(S, il, l, x1, kRoleIllum, sts);
+                    if (!mov1) gs = gcomplex<ILP>(S, il, l, x1, kRoleIllum, sts, c1);
                     for (int t = lane / T.lw; t < Nt; t += T.lg) {
                         float2 g = gs;
                         if (!mov1) steps += sts;
                         else g = gcomplex<ILP>(S, il, l, tick_pos(xtc, t), kRoleIllum, steps);
-                        const size_t o = ((size_t)q * Nt + t) * Nl + l;
-                        T.a_ms[o] = g;
-                        T.a_ss[o] = c_scale(c_mul(g, e1), p1inv * tick_w(S, xtc, t));
+                        T.a_ms[((size_t)q * Nt + t) * Nl + l] = g;
+                        T.a_ss[((size_t)qs * Nt + t) * Nl + l] = c_scale(c_mul(g, e1), p1inv * tick_w(S, xtc, t));
                     }
                 }
                 for (int v = lane % T.vwa; v < Nv; v += T.vwa) {
                     float2 gs = make_float2(0.f, 0.f);
                     uint32_t sts = 0;
-                    if (!mov1) gs = gcomplex<VWP>(S, vw, v, x1, kRoleView, sts);
+                    if (!mov1) gs = gcomplex<VWP>(S, vw, v, x1, kRoleView, sts, c1);
                     for (int t = lane / T.vwa; t < Nt; t += T.tga) {
                         float2 g = gs;
                         if (!mov1) steps += sts;
                         else g = gcomplex<VWP>(S, vw, v, tick_pos(xtc, t), kRoleView, steps);
-                        T.b_ss[((size_t)q * Nt + t) * Nv + v] = g;
+                        T.b_ss[((size_t)qs * Nt + t) * Nv + v] = g;
                     }
                 }
             }
@@ -456,6 +462,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             const V3 xn = V3{ vb.x, vb.y, vb.z };
             const int mn = (int)(__float_as_uint(vb.w) & 15u);
             const float xin = (float)(__float_as_uint(vb.w) >> 4) * (1.0f / 16777216.0f);
+            const uint32_t cn = (T.views && !S.single) ? cell_of(S, xn) : kNoCell;   // xn's grid cell
             if (CORR && b >= 3) {
                 // momentum transfer of the inner vertex cur (TemporalSamplerCorrelation.cuh:144-179)
                 const V3 dq = sub3(funit(sub3(cur, prev)), funit(sub3(xn, cur)));
@@ -610,8 +617,8 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     uint32_t sts = 0;
                     float w = 0.0f;
                     float2 g1s = make_float2(0.f, 0.f), g2s = make_float2(0.f, 0.f);
-                    if (realv) { w = gweight<VWP>(S, vw, v, xn, kRoleView, sts); sts *= 2; }
-                    else if (stn) { g1s = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts); g2s = gcomplex<VWP>(S, vw2, v, xn, kRoleView, sts); }
+                    if (realv) { w = gweight<VWP>(S, vw, v, xn, kRoleView, sts, cn); sts *= 2; }
+                    else if (stn) { g1s = gcomplex<VWP>(S, vw, v, xn, kRoleView, sts, cn); g2s = gcomplex<VWP>(S, vw2, v, xn, kRoleView, sts, cn); }
                     float f12s = 0.0f;
                     // tabular / vMF: u1 amplitude x conj(u2 amplitude), the view attached at x_b
                     auto f12tab = [&](const V3& pa, const V3& pb) {
@@ -659,8 +666,8 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 const bool stf = !S.temporal_amp || (stn && !S.moving[mcur]);
                 // the view's vector at x_b (GvSum), or for the CBS reversed pass the
                 // illumination's vector at x_b with the illumination as the path's last end (GlSum)
-                auto gx = [&](int e, const V3& p, uint32_t& st) {
-                    return T.cbs ? gcomplex<ILP>(S, il, e, p, kRoleIllum, st) : gcomplex<VWP>(S, vw, e, p, kRoleView, st);
+                auto gx = [&](int e, const V3& p, uint32_t& st, uint32_t cell) {
+                    return T.cbs ? gcomplex<ILP>(S, il, e, p, kRoleIllum, st, cell) : gcomplex<VWP>(S, vw, e, p, kRoleView, st, cell);
                 };
                 auto fx = [&](int e, const V3& pa, const V3& pb, int m) {
                     return T.cbs ? fillum_exit<ILP>(S, il, e, pa, pb, m) : fview<VWP>(S, vw, e, pa, pb, m);
@@ -674,14 +681,14 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                     uint32_t sts = 0;
                     float2 gs = make_float2(0.f, 0.f);
-                    if (stn) gs = gx(v, xn, sts);
+                    if (stn) gs = gx(v, xn, sts, cn);
                     const float fs = (stf && !tabn) ? fx(v, xn, cur, mn) : 0.0f;
                     const float2 fsc = (stf && tabn) ? fxc(v, xn, cur) : make_float2(0.f, 0.f);
                     int k = 0;
                     for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
                         float2 g = gs;
                         if (stn) steps += sts;
-                        else g = gx(v, tick_pos(xtn, t), steps);
+                        else g = gx(v, tick_pos(xtn, t), steps, kNoCell);
                         const float fr = phs[t];
                         float2 c;
                         if (tabn) {

@@ -40,6 +40,8 @@ struct TraceParams {
     int cbs;              // field CBS, reversed pass (trace_kernel): s_ms <- Gv0 [paths][Nt][Nv] (pass0),
                           // a_ms <- GlSum [paths][Nt][Nl]; v0 / vn then index illumination elements
     float* p2;            // [paths] or null: the correlation sampler's second-point probability (CBS)
+    const uint32_t* ss_row;   // [paths] or null: row of path q in a_ss / b_ss (paths grouped by first-vertex
+                              // material for the far-field x far-field contraction); null: row q
 };
 
 // Correlation-sampler CBS cross terms (trace.cu, cbs_corr_kernel): V +=

@@ -46,6 +46,7 @@ struct VRec {
     float nz0, nz1;
     uint32_t in;            // 1 inside the box
     float ph_h, ph_l;       // field: L_b / lambda + xi_b reduced to [-1/2, 1/2] cycles, as a float pair
+    uint32_t cell;          // packed grid cell of the position (multi-cell media), the start of every view's traversal
 };
 
 
@@ -61,7 +62,7 @@ struct __align__(16) CRec {
     float cw, cw_, sig, sig_;   // cw: pdf coefficient (point views: times the point-source amplitude constant); sig: sigma_t inside
     float nx0, nx1, ny0, ny1;   // distances to the box faces: x - bmin, bmax - x (single-cell media)
     float nz0, nz1;
-    uint32_t in, pad;
+    uint32_t in, cell;          // cell: packed grid cell of the position (multi-cell media)
 };
 static_assert(sizeof(CRec) == 128, "CRec layout");
 
@@ -187,8 +188,9 @@ __device__ __forceinline__ void illum_path(const DevScene& S, const TraceParams&
     float* amr = reinterpret_cast<float*>(T.a_ms) + (size_t)q * Nt * Nl;   // real rows
     const bool real = T.real_rows != 0;
     auto put_ams = [&](size_t i, float a) { if (real) amr[i] = a; else ams[i] = make_float2(a, 0.f); };
-    float2* ass = T.a_ss + (size_t)q * Nt * Nl;
-    float2* bss = T.b_ss + (size_t)q * Nt * Nv;
+    const uint32_t qs = T.ss_row ? T.ss_row[q] : q;   // row of the single-scattering rows
+    float2* ass = T.a_ss + (size_t)qs * Nt * Nl;
+    float2* bss = T.b_ss + (size_t)qs * Nt * Nv;
     if (B == 0) {   // the walk hit a limit (error already flagged)
         for (int i = lane; i < Nt * Nl; i += 32) { put_ams(i, 0.f); ass[i] = make_float2(0.f, 0.f); }
         for (int i = lane; i < Nt * Nv; i += 32) bss[i] = make_float2(0.f, 0.f);
@@ -445,7 +447,8 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                         r.nx0 = c.x - S.bmin[0]; r.nx1 = S.bmax[0] - c.x;
                         r.ny0 = c.y - S.bmin[1]; r.ny1 = S.bmax[1] - c.y;
                         r.nz0 = c.z - S.bmin[2]; r.nz1 = S.bmax[2] - c.z;
-                        r.in = in ? 1u : 0u; r.pad = 0u;
+                        r.in = in ? 1u : 0u;
+                        r.cell = SINGLE ? kNoCell : cell_of(S, xc);
                         if (b >= 3) {
                             const float4 pp = vq[b - 3];
                             const V3 up = funit(sub3(xp, V3{ pp.x, pp.y, pp.z }));
@@ -459,6 +462,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                         r.ux = u.x; r.uy = u.y; r.uz = u.z; r.k2d = S.k2 * S.D[m];
                         r.g = g; r.omg2 = omg2; r.c = cc;
                         r.in = in ? 1u : 0u;
+                        r.cell = SINGLE ? kNoCell : cell_of(S, xc);
                         r.sig = sig;
                         r.nx0 = c.x - S.bmin[0]; r.nx1 = S.bmax[0] - c.x;
                         r.ny0 = c.y - S.bmin[1]; r.ny1 = S.bmax[1] - c.y;
@@ -528,6 +532,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                     const float4 nf = *reinterpret_cast<const float4*>(&cr->nx0);
                     const float4 nz = *reinterpret_cast<const float4*>(&cr->nz0);
                     const uint32_t rin = __float_as_uint(nz.z);
+                    const uint32_t rcell = __float_as_uint(nz.w);
                     if (SINGLE) steps += rin * rays * nvalid;
 #pragma unroll
                     for (int P = 0; P < kVPP; ++P) {
@@ -569,7 +574,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                                 const V3 xb = V3{ pk_lo(r0.x), pk_lo(r0.y), pk_lo(r1.x) };
                                 uint32_t st = 0;
                                 const V3 oh = V3{ h ? pk_hi(ox) : pk_lo(ox), h ? pk_hi(oy) : pk_lo(oy), h ? pk_hi(oz) : pk_lo(oz) };
-                                tt[h] = VWP ? tau_to_point(S, xb, sv[2 * P + h], st) : tau_dir(S, xb, oh, st);
+                                tt[h] = VWP ? tau_to_point(S, xb, sv[2 * P + h], st, rcell) : tau_dir(S, xb, oh, st, rcell);
                                 steps += (lane + 32 * (2 * P + h) < nv) ? st * rays : 0u;
                             }
                             tau2 = pk2(tt[0], tt[1]);
@@ -649,7 +654,7 @@ __global__ void __launch_bounds__(128, 6) view_kernel(const __grid_constant__ De
                             tau = tm * r.sig;
                         } else {
                             uint32_t st = 0;
-                            tau = VWP ? tau_to_point(S, xb, sv[j], st) : tau_dir(S, xb, o, st);
+                            tau = VWP ? tau_to_point(S, xb, sv[j], st, r.cell) : tau_dir(S, xb, o, st, r.cell);
                             steps += vok ? st * rays : 0u;
                         }
                         const V3 df = V3{ r.ux - o.x, r.uy - o.y, r.uz - o.z };

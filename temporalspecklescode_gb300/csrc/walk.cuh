@@ -261,59 +261,104 @@ __device__ inline void sample_source(const DevScene& S, const DevSource& src, St
     d0 = V3{ dir.x, dir.y, D == 3 ? dir.z : 0.0f };
 }
 
-// FP32 parametric voxel traversal from o along d.  Returns the optical depth;
-// `steps` counts the voxels crossed.  Termination: every iteration moves one
-// axis' cell index monotonically toward that axis' far edge.
-__device__ inline float dda(const DevScene& S, const V3& o, const V3& d, uint32_t& steps)
+// Voxel traversal from o along d, starting in cell (b0, b1, b2), in D
+// dimensions.  Every per-axis quantity lives in its own register (an array
+// indexed by the crossing axis would be placed in local memory): per step the
+// three face distances, the axis crossed first and the cell's extinction.
+// Arithmetic identical to the oracle's traversal (the same IEEE operations in
+// the same order), so the optical depth and the step count are too.
+template <int D>
+__device__ __forceinline__ float dda_cells(const DevScene& S, const V3& o, const V3& d, int b0, int b1, int b2,
+                                           uint32_t& steps)
 {
-    const int D = S.dims;
-    if (!inside(S, o)) return 0.0f;
-    // single cell: one step (same arithmetic as the general loop's first step)
-    if (S.n[0] == 2 && S.n[1] == 2 && (D == 2 || S.n[2] == 2)) {
-        float tn[3] = { 0.0f, 0.0f, 0.0f };
-        for (int i = 0; i < D; ++i) {
-            const float di = comp(d, i);
-            const float inv = fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di);
-            const float face = di < 0.0f ? S.bmin[i] : S.bmax[i];
-            tn[i] = fm(fsb(face, comp(o, i)), inv);
-        }
-        const int a = D == 2 ? (tn[0] < tn[1] ? 0 : 1) : ((tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2));
-        steps += 1;
-        return ffma(tn[a], S.sigt[__ldg(S.grid)], 0.0f);
-    }
-    float inv[3];
-    int sg[3], bin[3];
-    for (int i = 0; i < D; ++i) {
-        const float di = comp(d, i);
-        inv[i] = fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di);
-        sg[i] = di < 0.0f ? -1 : 1;
-        bin[i] = bin_of(S.ax[i], S.n[i], comp(o, i));
-    }
-    if (D == 2) { inv[2] = 0.0f; sg[2] = 1; bin[2] = 0; }
+    auto inv_of = [](float di) { return fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di); };
+    const float i0 = inv_of(d.x), i1 = inv_of(d.y), i2 = D == 3 ? inv_of(d.z) : 0.0f;
+    const int s0 = d.x < 0.0f ? -1 : 1, s1 = d.y < 0.0f ? -1 : 1, s2 = (D == 3 && d.z < 0.0f) ? -1 : 1;
+    // the last cell index along each axis in the direction of travel (0 going down)
+    const int e0 = s0 > 0 ? S.n[0] - 2 : 0, e1 = s1 > 0 ? S.n[1] - 2 : 0, e2 = D == 3 ? (s2 > 0 ? S.n[2] - 2 : 0) : 0;
+    const float* ax0 = S.ax[0] + (s0 > 0 ? 1 : 0);
+    const float* ax1 = S.ax[1] + (s1 > 0 ? 1 : 0);
+    const float* ax2 = D == 3 ? S.ax[2] + (s2 > 0 ? 1 : 0) : nullptr;
     const int sx = S.n[0] - 1, sxy = (S.n[0] - 1) * (S.n[1] - 1);
     float t = 0.0f, acc = 0.0f;
     uint32_t n = 0;
     const uint32_t limit = (uint32_t)(S.n[0] + S.n[1] + (D == 3 ? S.n[2] : 0)) + 4u;
     for (;;) {
-        float tn[3];
-        for (int i = 0; i < D; ++i) {
-            const float face = __ldg(S.ax[i] + bin[i] + (sg[i] > 0 ? 1 : 0));
-            tn[i] = fm(fsb(face, comp(o, i)), inv[i]);
-        }
+        const int idx = b0 + b1 * sx + (D == 3 ? b2 * sxy : 0);
+        const unsigned char m = __ldg(S.grid + idx);
+        const float t0 = fm(fsb(__ldg(ax0 + b0), o.x), i0);
+        const float t1 = fm(fsb(__ldg(ax1 + b1), o.y), i1);
         int a;
-        if (D == 2) a = tn[0] < tn[1] ? 0 : 1;
-        else a = (tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2);
-        const int idx = bin[0] + bin[1] * sx + (D == 3 ? bin[2] * sxy : 0);
-        const float tna = tn[a];
-        acc = ffma(fsb(tna, t), S.sigt[__ldg(S.grid + idx)], acc);
+        float tna;
+        if (D == 2) {
+            a = t0 < t1 ? 0 : 1;
+            tna = a == 0 ? t0 : t1;
+        } else {
+            const float t2 = fm(fsb(__ldg(ax2 + b2), o.z), i2);
+            a = (t0 < t1 && t0 < t2) ? 0 : (t1 < t2 ? 1 : 2);
+            tna = a == 0 ? t0 : (a == 1 ? t1 : t2);
+        }
+        acc = ffma(fsb(tna, t), S.sigt[m], acc);
         t = tna;
         ++n;
-        const int ba = bin[a];
-        if ((sg[a] < 0 && ba == 0) || (sg[a] > 0 && ba == S.n[a] - 2) || n >= limit) break;
-        bin[a] = ba + sg[a];
+        const bool last = a == 0 ? b0 == e0 : (a == 1 ? b1 == e1 : b2 == e2);
+        if (last || n >= limit) break;
+        b0 += a == 0 ? s0 : 0;
+        b1 += a == 1 ? s1 : 0;
+        if (D == 3) b2 += a == 2 ? s2 : 0;
     }
     steps += n;
     return acc;
+}
+
+// Packed start cell of a point (10 bits per axis), or kNoCell when an axis
+// has more than 1024 cells: a point's cell is the same for every ray leaving
+// it, so the view-side kernels look it up once per vertex.
+constexpr uint32_t kNoCell = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t cell_of(const DevScene& S, const V3& p)
+{
+    if (S.n[0] > 1025 || S.n[1] > 1025 || (S.dims == 3 && S.n[2] > 1025)) return kNoCell;
+    const uint32_t c0 = (uint32_t)bin_of(S.ax[0], S.n[0], p.x);
+    const uint32_t c1 = (uint32_t)bin_of(S.ax[1], S.n[1], p.y);
+    const uint32_t c2 = S.dims == 3 ? (uint32_t)bin_of(S.ax[2], S.n[2], p.z) : 0u;
+    return c0 | (c1 << 10) | (c2 << 20);
+}
+
+// FP32 parametric voxel traversal from o along d.  Returns the optical depth;
+// `steps` counts the voxels crossed.  Termination: every iteration moves one
+// axis' cell index monotonically toward that axis' far edge.  cell: o's packed
+// cell (cell_of), or kNoCell to look it up here.
+__device__ inline float dda(const DevScene& S, const V3& o, const V3& d, uint32_t& steps, uint32_t cell = kNoCell)
+{
+    const int D = S.dims;
+    if (!inside(S, o)) return 0.0f;
+    // single cell: one step (same arithmetic as the general loop's first step)
+    if (S.n[0] == 2 && S.n[1] == 2 && (D == 2 || S.n[2] == 2)) {
+        auto face_t = [&](float di, float oi, float lo, float hi) {
+            const float inv = fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di);
+            return fm(fsb(di < 0.0f ? lo : hi, oi), inv);
+        };
+        const float t0 = face_t(d.x, o.x, S.bmin[0], S.bmax[0]);
+        const float t1 = face_t(d.y, o.y, S.bmin[1], S.bmax[1]);
+        float tna;
+        if (D == 2) tna = t0 < t1 ? t0 : t1;
+        else {
+            const float t2 = face_t(d.z, o.z, S.bmin[2], S.bmax[2]);
+            tna = (t0 < t1 && t0 < t2) ? t0 : (t1 < t2 ? t1 : t2);
+        }
+        steps += 1;
+        return ffma(tna, S.sigt[__ldg(S.grid)], 0.0f);
+    }
+    int b0, b1, b2;
+    if (cell != kNoCell) {
+        b0 = (int)(cell & 1023u); b1 = (int)((cell >> 10) & 1023u); b2 = (int)(cell >> 20);
+    } else {
+        b0 = bin_of(S.ax[0], S.n[0], o.x);
+        b1 = bin_of(S.ax[1], S.n[1], o.y);
+        b2 = D == 3 ? bin_of(S.ax[2], S.n[2], o.z) : 0;
+    }
+    return D == 3 ? dda_cells<3>(S, o, d, b0, b1, b2, steps) : dda_cells<2>(S, o, d, b0, b1, 0, steps);
 }
 
 }  // namespace sstmc

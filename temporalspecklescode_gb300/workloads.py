@@ -131,11 +131,66 @@ def tracking_2d(batch_size: int = 1 << 17, full_iteration: int = 64, n_dirs: int
     return cfg, 2
 
 
+def frame_lags(frames: int) -> np.ndarray:
+    """The distinct lags t2 - t1 of the frame pairs (t1, t2) of `frames`
+    frames 0 .. frames-1: -(frames-1) .. frames-1."""
+    return np.arange(-(frames - 1), frames, dtype=float)
+
+
+def tracking_2d_pairs(batch_size: int = 1 << 17, full_iteration: int = 64, n_dirs: int = 128, frames: int = 32,
+                      seed: int = 0):
+    """2D spatio-temporal tracking as frame-pair correlations, in the form the
+    reference expresses tracking (examples/trackingLinearMotion.m:61-76,
+    examples/spatioTemporalCorrelation2D.m:62-84): the correlation sampler
+    with illumination2 = illumination and view2 = view, the disc material's
+    scatterers drifting by U = (0.5, 0) per frame.
+
+    The medium is the static 256x256 grid of `tracking_2d` (background sigs=1,
+    disc of radius 16 with sigs=4, siga=0, HG g=0.7) with 128 far-field
+    illuminations and views over [-pi/6, pi/6] about +y.  The correlation
+    sampler's estimator for a frame pair (t1, t2) depends on the pair only
+    through t2 - t1 (the u1 and u2 paths take the sampled positions displaced
+    by -U (t2 - t1) / 2 and +U (t2 - t1) / 2; the grid itself does not move),
+    so the ticks are the 2 frames - 1 distinct lags (`frame_lags`) and
+    `frame_pairs` scatters the rendered lags onto the frames x frames pairs."""
+    n = 256
+    c = -128 + (np.arange(n) + 0.5)
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    mg = np.where(X * X + Y * Y <= 16 * 16, 2, 1).astype(np.uint32)
+    d = _farfield_fan(n_dirs)
+    src = {"type": "FarField", "direction": d}
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "renderingsNum": 1,
+                       "lambda": 1.0, "seed": seed},
+        "scattering": {"type": ["HG"] * 3, "amplitudeFunction": [0.7] * 3},
+        "medium": {"type": "Heterogeneous", "xAxis": np.linspace(-128, 128, n + 1), "yAxis": np.linspace(-128, 128, n + 1),
+                   "materialGrid": mg, "sigs": [0.0, 1.0, 4.0], "siga": [0.0, 0.0, 0.0]},
+        "illumination": src, "view": src, "illumination2": src, "view2": src,
+        "sampler": {"type": "TemporalCorrelationSampler", "t": frame_lags(frames), "D": [0.0, 0.0, 0.0],
+                    "U": {"x": [0.0, 0.0, 0.5], "y": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
+def frame_pairs(u: np.ndarray, frames: int) -> np.ndarray:
+    """Correlations of every frame pair from a render over `frame_lags(frames)`:
+    C[..., t1, t2] = u[..., lag index of t2 - t1] for u of shape
+    (Nl, Nv, 2 frames - 1, ...) (the tick axis third, as sstmc2D returns it).
+    Returns shape (Nl, Nv, frames, frames, ...)."""
+    if u.shape[2] != 2 * frames - 1:
+        raise ValueError(f"u has {u.shape[2]} ticks, expected the {2 * frames - 1} lags of {frames} frames")
+    t = np.arange(frames)
+    lag_index = (t[None, :] - t[:, None]) + (frames - 1)   # [t1, t2] -> index of t2 - t1
+    return u[:, :, lag_index]
+
+
 WORKLOADS = {
     "speckle_2d": speckle_2d,
     "correlation_3d": correlation_3d,
     "transmission_matrix_3d": transmission_matrix_3d,
     "tracking_2d": tracking_2d,
+    "tracking_2d_pairs": tracking_2d_pairs,
 }
 
 

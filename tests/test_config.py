@@ -107,3 +107,33 @@ def test_c_abi_refuses_empty_sources(oracle):
     pc.struct.view.count = 0
     with pytest.raises(RuntimeError, match="100"):
         oracle.render(pc, 0)
+
+
+def test_frame_pairs_indexing():
+    """frame_pairs maps the lag axis -(F-1) .. F-1 onto the F x F pairs by t2 - t1."""
+    from temporalspecklescode_gb300 import workloads as wl
+    F = 5
+    lags = wl.frame_lags(F)
+    assert lags.tolist() == list(range(-4, 5))
+    u = np.broadcast_to(lags[None, None, :, None], (2, 3, 2 * F - 1, 1)).astype(complex)
+    C = wl.frame_pairs(u, F)
+    assert C.shape == (2, 3, F, F, 1)
+    for t1 in range(F):
+        for t2 in range(F):
+            assert C[1, 2, t1, t2, 0] == t2 - t1
+
+
+def test_frame_pairs_oracle_equals_per_pair_ticks(oracle):
+    """On the oracle (FP64, every tick evaluated on its own), the lag render
+    scattered onto the frame pairs equals the render over every pair's lag."""
+    from temporalspecklescode_gb300 import config as cf
+    from temporalspecklescode_gb300 import workloads as wl
+    F = 3
+    cfg, dims = wl.tracking_2d_pairs(batch_size=6, full_iteration=1, n_dirs=4, frames=F, seed=4)
+    u, it, _ = oracle.render(cf.prepare(cfg, dims), 3)
+    pairs = np.array([t2 - t1 for t1 in range(F) for t2 in range(F)], dtype=float)
+    cfg2 = dict(cfg, sampler=dict(cfg["sampler"], t=pairs))
+    u2, it2, _ = oracle.render(cf.prepare(cfg2, dims), 3)
+    assert it == it2
+    C = wl.frame_pairs(u[..., None], F)[..., 0]
+    assert np.allclose(C, u2.reshape(4, 4, F, F), rtol=0, atol=1e-12 * np.abs(u2).max())

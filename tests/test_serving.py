@@ -107,3 +107,41 @@ def test_wait_times_out_on_an_open_request(api):
             r.wait(timeout=0.0)
         assert ex.value.code == TIMEOUT
         assert r.wait() == 0
+
+
+@pytest.mark.gpu
+def test_busy_scene_does_not_block_other_scenes(api):
+    """Two requests on one scene, then requests on two other scenes, on a
+    two-slot server: the second request on the busy scene is passed over, so
+    the other scenes' requests start on the free slot and complete while the
+    first long render is still running, instead of waiting behind it."""
+    import time
+    big = api.Scene(*wl.correlation_3d(batch_size=1 << 20, full_iteration=2, n_side=8, n_lags=8))
+    small = [api.Scene(*SCENES[n]) for n in ("speckle_2d", "corr_far_2d_drift")]
+    try:
+        big.render(seed=1)                       # warm-up: kernels loaded, pool grown
+        for s in small:
+            s.render(seed=1)
+        with api.Server(slots=2) as srv:
+            reqs = [srv.submit(big, 5), srv.submit(big, 6)] + [srv.submit(s, 7) for s in small]
+            order = []
+            t0 = time.perf_counter()
+            while len(order) < len(reqs) and time.perf_counter() - t0 < 300:
+                for i, r in enumerate(reqs):
+                    if i not in order and r.done():
+                        order.append(i)
+                time.sleep(1e-4)
+            outs = [r.result() for r in reqs]
+            st = srv.stats()
+        assert len(order) == len(reqs)
+        # both small requests finish before the first render of the busy scene
+        assert order.index(2) < order.index(0) and order.index(3) < order.index(0), order
+        assert order.index(0) < order.index(1), order
+        for s, (u, it) in zip(small, outs[2:]):
+            ua, ita = s.render(seed=7)
+            assert np.array_equal(ita, it) and rel_fro(u, ua) <= 1e-6
+        assert st["completed"] == 4
+    finally:
+        big.close()
+        for s in small:
+            s.close()

@@ -72,3 +72,55 @@ def test_static_refuses_output_larger_than_scratch(api):
         u, it = s.render_static(seed=5)
     assert np.array_equal(it, it_ref)
     assert rel_fro(u, u_ref) <= REL_TOL
+
+
+def _cudart():
+    """The CUDA runtime, to read the device's memory state from this process."""
+    import ctypes as C
+    import glob
+    cands = ["libcudart.so.13", "libcudart.so"] + sorted(glob.glob("/usr/local/cuda/lib64/libcudart.so*"))
+    for c in cands:
+        try:
+            return C.CDLL(c)
+        except OSError:
+            continue
+    pytest.skip("libcudart not found")
+
+
+def _memory_state(rt):
+    """(free device bytes, reserved and used bytes of the default memory pool)."""
+    import ctypes as C
+    free, total = C.c_size_t(), C.c_size_t()
+    assert rt.cudaSetDevice(0) == 0
+    assert rt.cudaDeviceSynchronize() == 0
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    pool = C.c_void_p()
+    assert rt.cudaDeviceGetDefaultMemPool(C.byref(pool), 0) == 0
+    reserved, used = C.c_uint64(), C.c_uint64()
+    # cudaMemPoolAttrReservedMemCurrent = 5, cudaMemPoolAttrUsedMemCurrent = 7
+    assert rt.cudaMemPoolGetAttribute(pool, 5, C.byref(reserved)) == 0
+    assert rt.cudaMemPoolGetAttribute(pool, 7, C.byref(used)) == 0
+    return free.value, reserved.value, used.value
+
+
+def test_static_render_allocates_nothing(api):
+    """The defining property: a static render leaves the device's free memory
+    and the default memory pool's reserved and used bytes as they were, while an
+    sstmc_render of the same scene right after it takes its chunk buffers from
+    the pool (which shows that the probe sees allocations).  A first static
+    render of a scene of the same kind runs before the probe, so the kernels'
+    first launches (which load their code) lie outside it."""
+    rt = _cudart()
+    cfg, dims = SCENES["correlation_3d_chunked"]
+    with api.Scene(cfg, dims) as warm:
+        warm.render_static(seed=2)
+    with api.Scene(cfg, dims) as s:
+        before = _memory_state(rt)
+        u1, it1 = s.render_static(seed=3)
+        u2, it2 = s.render_static(seed=3)
+        after = _memory_state(rt)
+        assert after == before, (before, after)
+        assert np.array_equal(it1, it2) and rel_fro(u1, u2) <= 1e-12
+        s.render(seed=3)
+        after_render = _memory_state(rt)
+        assert after_render[2] > after[2], (after, after_render)
