@@ -28,9 +28,11 @@ plain_fp32 : the plain FP32 form (FP32 phases, SIMT contraction) on the same
         arm times the CPU FP64 restatement of its estimator (oracle/) on all
         host threads.
 
-Multi-GPU (torchrun): independent replicas with disjoint seeds ("replicas
-only": the paths are i.i.d., there is no exchange step); value is the sum of
-contributions over ranks divided by the max time over ranks.
+Multi-GPU (torchrun): replicas with disjoint seeds ("replicas only": the
+paths are i.i.d.); the one exchange step sums the ranks' accumulators and
+iteration counts after each render (all_reduce, its time part of the step);
+value is the sum of contributions over ranks divided by the max time over
+ranks.
 """
 from __future__ import annotations
 
@@ -110,6 +112,23 @@ def _sum_over_ranks(dist, x: float) -> float:
         t = t.cuda()
     dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def _merge_over_ranks(dist, u, it):
+    """The replicas' one exchange step: the sum of every rank's accumulator u
+    (complex, Nl x Nv x Nt x renderings) and iteration counts, so the merged
+    render is the render of all ranks' paths (normalise by the summed iter)."""
+    import numpy as np
+    if dist is None:
+        return u, it
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.from_numpy(np.ascontiguousarray(np.stack([u.real, u.imag]))).to(dev)
+    n = torch.from_numpy(np.ascontiguousarray(it, dtype=np.float64)).to(dev)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    t = t.cpu().numpy()
+    return t[0] + 1j * t[1], n.cpu().numpy()
 
 
 class ClockSampler:
@@ -254,6 +273,41 @@ def run_reference(args, dist, rank, ws):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_gpu(args):
+    """The reference's own CUDA path (oracle/refharness.cu over the staged
+    reference headers) on the workload's scene with a reduced batch (the
+    reference materialises P x P permutation matrices and P x Nl x Nv x Nt
+    products): device time per trace from its harness, contributions per
+    trace estimated by this build's render of the same scene (the same path
+    distribution; the reference reports no vertex counts)."""
+    from temporalspecklescode_gb300 import api
+    from tests import refharness_lib as ref
+    if not ref.available():
+        print(json.dumps({"impl": "reference-gpu", "unavailable": "the reference headers are not staged (oracle/stage_reference.sh)"}))
+        return
+    batch = args.ref_gpu_batch
+    cfg, dims = _workload(0, 20)
+    cfg["simulation"]["batchSize"] = batch
+    cfg["simulation"]["fullIteration"] = args.ref_gpu_waves
+    R = args.warmup + args.steps
+    _, it_ref, ms = ref.render(cfg, dims, R, seed=0)
+    ms = ms[args.warmup:]
+    api.load_library()
+    contrib = []
+    with api.Scene(cfg, dims) as s:
+        for sd in range(3):
+            s.render(seed=100 + sd)
+            contrib.append(s.stats()["contributions"])
+    c = statistics.mean(contrib)
+    mms = statistics.mean(ms)
+    line = {"impl": "reference-gpu", "metric": METRIC, "value": c / (mms / 1000), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": mms, "higher_is_better": True,
+            "dtype": "f64 (the reference's PRECISION DOUBLE)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "paths_per_step": batch * args.ref_gpu_waves, "batch": batch,
+                       "note": "contributions per trace estimated from this build's render of the same scene"}}
+    print(json.dumps(line), flush=True)
+
+
 # DRAM bytes (read + write) per path of each kernel class from one ncu capture
 # of the workload at a small path count; every class streams per-path rows,
 # so a launch's traffic scales with the paths it processes.
@@ -345,14 +399,21 @@ def _kernel_rooflines(scene, mean, verts_per_step, dda_per_step, chunks, peaks, 
     return out
 
 
-def _render_series(scene, seeds):
-    """Render each seed; device time and statistics per render."""
+def _render_series(scene, seeds, dist=None):
+    """Render each seed; device time, statistics and (over replicas) the time
+    of merging the ranks' accumulators per render."""
     res = []
     for sd in seeds:
         ts = time.perf_counter()
-        scene.render(seed=sd)
+        u, it = scene.render(seed=sd)
         host_ms = 1000 * (time.perf_counter() - ts)
-        res.append((host_ms, scene.timing(), scene.stats()))
+        tm, st = scene.timing(), scene.stats()
+        tm["ms_merge"] = 0.0
+        if dist is not None:
+            tq = time.perf_counter()
+            _merge_over_ranks(dist, u, it)
+            tm["ms_merge"] = 1000 * (time.perf_counter() - tq)
+        res.append((host_ms, tm, st))
     return res
 
 
@@ -364,6 +425,7 @@ def run_gpu(args, dist, rank, ws):
     precision = cf.PRECISION_FP32 if args.precision == "fp32" else cf.PRECISION_SPLIT
     cfg, dims = _workload(seed=1000 * rank, paths_log2=paths_log2)
     scene = api.Scene(cfg, dims, precision)
+    wavefront = scene.autotune(args.autotune) if args.autotune else None
     lat = []
     dev_ms = []
     parts = {"ms_trace": [], "ms_contract_ms": [], "ms_contract_ss": [], "ms_walk": [], "ms_nee": []}
@@ -378,9 +440,9 @@ def run_gpu(args, dist, rank, ws):
     _barrier(dist)
     clocks.start()
     t0 = time.perf_counter()
-    for host_ms, tm, st in _render_series(scene, [100 + i for i in range(args.steps)]):
+    for host_ms, tm, st in _render_series(scene, [100 + i for i in range(args.steps)], dist):
         lat.append(host_ms)
-        dev_ms.append(tm["ms_total"])
+        dev_ms.append(tm["ms_total"] + tm["ms_merge"])   # replicas: the accumulator merge is part of the step
         for k in parts:
             parts[k].append(tm[k])
         launches += tm["launches"]
@@ -494,6 +556,8 @@ def run_gpu(args, dist, rank, ws):
         "clocks": clk,
         "wall_s": wall,
     }
+    if wavefront:
+        line["config"]["wavefront"] = f"{wavefront} paths per chunk (sstmc_scene_autotune over a {args.autotune}-path sample)"
     if WORKLOAD == "tracking_2d_pairs":
         line["config"]["frame_pairs"] = "32 x 32 frames from the 63 lags t2 - t1 (workloads.frame_pairs)"
     scene.close()
@@ -538,7 +602,9 @@ def run_serve(args):
     rng = random.Random(5)
     n_req = args.serve_requests
     picks = [rng.randrange(len(scenes)) for _ in range(n_req)]
-    for s in scenes:          # warm-up: every kernel variant once
+    for s in scenes:          # wavefront per medium, then warm-up: every kernel variant once
+        if args.autotune:
+            s.autotune(args.autotune)
         s.render(seed=1)
     # one by one (sstmc_render), back to back
     t0 = time.perf_counter()
@@ -582,7 +648,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-gpu"],
+                    help="reference: the CPU FP64 oracle; reference-gpu: the reference's own CUDA path (staged headers)")
+    ap.add_argument("--ref-gpu-batch", type=int, default=512, help="reference-gpu: batchSize per wave")
+    ap.add_argument("--ref-gpu-waves", type=int, default=4, help="reference-gpu: fullIteration")
     ap.add_argument("--precision", default="split", choices=["split", "fp32"])
     ap.add_argument("--paths-log2", type=int, default=0, help="paths per render (log2); 0: the workload's own")
     ap.add_argument("--cpu-sample", type=int, default=0, help="paths of the CPU oracle sample; 0: the workload's own")
@@ -591,6 +660,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison render")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS),
                     help="correlation_3d (the headline), speckle_2d, transmission_matrix_3d or tracking_2d_pairs")
+    ap.add_argument("--autotune", type=int, default=0,
+                    help="choose the wavefront (paths per chunk) by timing this many paths per candidate first (0: off)")
     ap.add_argument("--serve", action="store_true", help="measure the serving mix instead of the headline workload")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-load", type=float, default=2.0, help="arrival rate / one-by-one completion rate")
@@ -600,6 +671,9 @@ def main():
         run_serve(args)
         return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference-gpu":
+        run_reference_gpu(args)
+        return
     dist, rank, ws = _dist()
     if args.impl == "reference":
         run_reference(args, dist, rank, ws)

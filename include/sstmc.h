@@ -196,6 +196,18 @@ int32_t sstmc_scene_shape(const sstmc_scene* scene, uint32_t* nl, uint32_t* nv, 
  * cfg.seed for the first rendering. */
 int32_t sstmc_render(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
 
+/* Wavefront autotuner.  No counterpart in the reference, whose wavefront is
+ * batchSize paths.  Renders the scene's first sample_paths paths (at least
+ * 4096) once per candidate wavefront -- paths traced per chunk of kernel
+ * launches: powers of two from 4096 up to the sample and the device-memory
+ * budget -- timing each with CUDA events after one untimed render at that
+ * size, and keeps the fastest for the scene's later renders (sstmc_render and
+ * served requests; a smaller reservation still bounds a served chunk).  The
+ * result of a render does not depend on the wavefront beyond the order of
+ * its FP32 windowed sums.  chunk_paths (may be NULL): the chosen wavefront.
+ * Overwrites sstmc_last_stats / sstmc_last_timing. */
+int32_t sstmc_scene_autotune(sstmc_scene* scene, uint32_t sample_paths, uint64_t* chunk_paths);
+
 /* sstmc_render without device memory allocation.  No counterpart in the
  * reference: it is for callers that must not allocate device memory during a
  * render -- a host that owns a fixed device-memory budget (a serving process

@@ -48,6 +48,8 @@ def load_library() -> C.CDLL:
     lib.sstmc_scene_shape.restype = i32
     lib.sstmc_render.argtypes = [vp, u64, dp, dp]
     lib.sstmc_render.restype = i32
+    lib.sstmc_scene_autotune.argtypes = [vp, u32, C.POINTER(u64)]
+    lib.sstmc_scene_autotune.restype = i32
     lib.sstmc_render_static.argtypes = [vp, u64, dp, dp]
     lib.sstmc_render_static.restype = i32
     lib.sstmc_last_stats.argtypes = [vp, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]
@@ -156,6 +158,14 @@ class Scene:
 
     def render(self, seed: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray]:
         return self._render(self.lib.sstmc_render, seed)
+
+    def autotune(self, sample_paths: int = 1 << 18) -> int:
+        """Time the scene's first `sample_paths` paths at each candidate wavefront
+        (paths per chunk of kernel launches) and keep the fastest for later
+        renders (sstmc_scene_autotune); returns the chosen paths per chunk."""
+        n = C.c_uint64()
+        _check(self.lib.sstmc_scene_autotune(self.handle, C.c_uint32(sample_paths), C.byref(n)))
+        return n.value
 
     def render_static(self, seed: Optional[int] = None) -> Tuple[np.ndarray, np.ndarray]:
         """``render`` with no device memory allocation: every device buffer is in

@@ -468,12 +468,15 @@ int Engine::contract_chunk(Scene& S, uint32_t n)
     return SSTMC_NO_ERROR;
 }
 
-int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out)
+int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out, uint64_t limit)
 {
-    const uint64_t total = (uint64_t)S.P * S.full_iter;
-    if (total > 0xffffffffull) return SSTMC_NOT_SUPPORTED;
+    const uint64_t all = (uint64_t)S.P * S.full_iter;
+    if (all > 0xffffffffull) return SSTMC_NOT_SUPPORTED;
+    const uint64_t total = limit ? std::min(limit, all) : all;
     const size_t bud = budget ? budget : budget_bytes();
-    uint32_t chunk = (uint32_t)std::min<uint64_t>(total, std::max<uint64_t>(256, bud / bytes_per_path(S)));
+    uint64_t fit = std::max<uint64_t>(256, bud / bytes_per_path(S));
+    if (tuned_chunk) fit = std::min<uint64_t>(fit, tuned_chunk);   // the autotuner's wavefront, within the budget
+    uint32_t chunk = (uint32_t)std::min<uint64_t>(total, fit);
     chunk = std::max<uint32_t>(32, chunk);
     int e = ensure(S, chunk);
     if (e) return e;
@@ -525,7 +528,7 @@ int Engine::render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out)
         return SSTMC_DEVICE_ERROR;
     if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
     if (herr) return herr;
-    if (iter_out) *iter_out = (double)total + (double)tot[2];
+    if (iter_out) *iter_out = (double)total + (double)tot[2];   // iter = batchSize * fullIteration + missed first vertices
     S.last_vertices = tot[0];
     S.last_dda = tot[1];
     S.last_paths = tot[3];
@@ -644,6 +647,45 @@ int32_t sstmc_scene_shape(const sstmc_scene* s, uint32_t* nl, uint32_t* nv, uint
 int32_t sstmc_render(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out)
 {
     return s ? render_scene(s, seed, u_out, iter_out, 0, false, nullptr) : SSTMC_INVALID_HANDLE;
+}
+
+int32_t sstmc_scene_autotune(sstmc_scene* s, uint32_t sample_paths, uint64_t* chunk_paths)
+{
+    if (!s) return SSTMC_INVALID_HANDLE;
+    std::lock_guard<std::mutex> lk(s->mu);
+    Scene& S = s->scene;
+    Engine& E = s->engine;
+    if (cudaSetDevice(S.device) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    const uint64_t total = (uint64_t)S.P * S.full_iter;
+    const uint64_t sample = std::min<uint64_t>(total, std::max<uint32_t>(sample_paths, 1u << 12));
+    const uint64_t fit = std::max<uint64_t>(256, budget_bytes() / Engine::bytes_per_path(S));
+    const bool timing = E.timing;
+    E.timing = true;
+    E.budget = 0;
+    double best = 0.0;
+    uint32_t best_chunk = 0;
+    int e = SSTMC_NO_ERROR;
+    // candidate wavefronts: powers of two from 2^12 paths up to the sample and the memory budget
+    for (uint64_t c = 1u << 12; !e; c <<= 1) {
+        const uint64_t chunk = std::min(std::min(c, sample), fit);
+        E.release();
+        E.tuned_chunk = (uint32_t)chunk;
+        double ms = 0.0;
+        for (int rep = 0; rep < 2 && !e; ++rep) {   // the first render at a size grows the pools
+            e = E.render_one(S, 1, nullptr, nullptr, sample);
+            ms = E.ms_total;
+        }
+        if (!e && ms > 0.0) {
+            const double rate = (double)sample / ms;
+            if (rate > 1.02 * best) { best = rate; best_chunk = (uint32_t)chunk; }
+        }
+        if (chunk >= sample || chunk >= fit) break;
+    }
+    E.release();
+    E.timing = timing;
+    E.tuned_chunk = e ? 0u : best_chunk;
+    if (chunk_paths) *chunk_paths = E.tuned_chunk;
+    return e;
 }
 
 int32_t sstmc_render_static(sstmc_scene* s, uint64_t seed, double* u_out, double* iter_out)

@@ -57,6 +57,7 @@ struct Engine {
     uint64_t launches = 0, chunks = 0;
     bool timing = true;
     size_t budget = 0;    // device bytes for the chunk buffers; 0: min(16 GiB, a quarter of free memory)
+    uint32_t tuned_chunk = 0;   // paths per chunk chosen by sstmc_scene_autotune (0: from the budget)
     bool fixed = false;   // buffers carved from a fixed scratch: a chunk that outgrows them fails, nothing is allocated
 
     static size_t bytes_per_path(const Scene& S);
@@ -67,7 +68,8 @@ struct Engine {
               std::vector<std::pair<int, int>>* tchunks) const;
     int trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, PathDebug* dbg);
     int contract_chunk(Scene& S, uint32_t n);
-    int render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out);
+    // limit: render only the first `limit` paths (0: all), for the autotuner's samples
+    int render_one(Scene& S, uint64_t seed, double* u_out, double* iter_out, uint64_t limit = 0);
     int init_events();
     void destroy_events();
 };

@@ -256,3 +256,19 @@ def test_walk_overflow_pool_grows(api, oracle):
     uo, ito, sto = oracle.render(cf.prepare(cfg, dims), 31)
     assert it1[0] == ito and st1["vertices"] == sto["vertices"]
     assert rel_fro(u1[..., 0], uo) <= REL_TOL
+
+
+def test_autotuned_wavefront_keeps_the_render(api, oracle):
+    """sstmc_scene_autotune picks the wavefront (paths per chunk) from timed
+    samples; a render at the chosen wavefront traces the same paths (integer
+    statistics exact) and stays within the tolerance of the FP64 oracle."""
+    from temporalspecklescode_gb300 import workloads as wl
+    cfg, dims = wl.correlation_3d(batch_size=8192, full_iteration=2, n_side=4, n_lags=4)
+    with api.Scene(cfg, dims) as s:
+        chunk = s.autotune(sample_paths=16384)
+        assert 4096 <= chunk <= 16384 and chunk & (chunk - 1) == 0
+        u, it = s.render(seed=6)
+        st = s.stats()
+    uo, ito, sto = oracle.render(cf.prepare(cfg, dims), 6)
+    assert it[0] == ito and st["vertices"] == sto["vertices"] and st["dda_steps"] == sto["dda_steps"]
+    assert rel_fro(u[..., 0], uo) <= REL_TOL

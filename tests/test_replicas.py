@@ -1,7 +1,8 @@
-"""The multi-GPU path ("replicas only": the paths are i.i.d. and there is no
-exchange step) on CPU with gloo, world size 2: the bench's barrier and its
-sum / max reductions over ranks, the per-rank seeds, and the reference arm
-launched through torch.distributed.run, where rank 0 alone prints its line."""
+"""The multi-GPU path ("replicas only": the paths are i.i.d.; the one
+exchange step sums the ranks' accumulators) on CPU with gloo, world size 2:
+the bench's barrier, its sum / max reductions over ranks, the accumulator
+merge, the per-rank seeds, and the reference arm launched through
+torch.distributed.run, where rank 0 alone prints its line."""
 import json
 import os
 import socket
@@ -34,6 +35,10 @@ def _rank_main(rank: int, ws: int, port: int, out_dir: str):
         "max": bench._max_over_ranks(dist, [1.5, 2.5][r]),
         "seed": bench._workload(seed=1000 * r, paths_log2=10)[0]["simulation"]["seed"],
     }
+    import numpy as np
+    u = np.full((3, 2, 4, 1), (r + 1) + 1j * (10 * (r + 1)))
+    um, itm = bench._merge_over_ranks(dist, u, np.array([100.0 * (r + 1)]))
+    res["merged"] = [float(um.real.max()), float(um.real.min()), float(um.imag.max()), float(itm[0]), list(um.shape)]
     bench._barrier(dist)
     dist.destroy_process_group()
     with open(os.path.join(out_dir, f"rank{r}.json"), "w") as f:
@@ -50,6 +55,8 @@ def test_reductions_and_seeds_over_two_gloo_ranks(tmp_path):
         assert x["sum"] == 3.0          # contributions: summed over ranks
         assert x["max"] == 2.5          # time: the slowest rank
     assert res[0]["seed"] != res[1]["seed"]   # disjoint path sets per replica
+    for x in res:   # the exchange step: every rank holds the sum of both accumulators and iteration counts
+        assert x["merged"] == [3.0, 3.0, 30.0, 300.0, [3, 2, 4, 1]]
 
 
 def test_reference_arm_prints_on_rank0_only():
