@@ -417,6 +417,37 @@ def _render_series(scene, seeds, dist=None):
     return res
 
 
+def side_workload(name: str, paths_log2: int, renders: int = 2):
+    """A second workload measured in the same run at a stated path count: its
+    contributions/s (CUDA-event device time), phases and the contraction's
+    useful tensor throughput; the headline line carries it beside its own."""
+    global WORKLOAD
+    from temporalspecklescode_gb300 import api
+    saved, WORKLOAD = WORKLOAD, name
+    try:
+        cfg, dims = _workload(0, paths_log2)
+        with api.Scene(cfg, dims) as s:
+            s.render(seed=1)
+            series = _render_series(s, [50 + i for i in range(renders)])
+            m = s.meta
+    finally:
+        WORKLOAD = saved
+    ms = statistics.mean([tm["ms_total"] for _, tm, _ in series])
+    contrib = statistics.mean([st["contributions"] for _, _, st in series])
+    dda = statistics.mean([st["dda_steps"] for _, _, st in series])
+    phases = {k: statistics.mean([tm[k] for _, tm, _ in series]) for k in ("ms_walk", "ms_nee", "ms_contract_ms", "ms_contract_ss")}
+    P = m["P"] * m["waves"]
+    flops = 8.0 * m["Nl"] * m["Nv"] * m["Nt"] * P   # complex MACs of one contraction over every path's rows
+    peaks, _ = _peaks()
+    out = {"workload": name, "paths": P, "value": contrib / (ms / 1000), "unit": UNIT, "ms_per_render": ms,
+           "renders": renders, "phases_ms": phases, "voxel_steps_per_s": dda / (phases["ms_nee"] / 1000)}
+    for key, label in (("ms_contract_ms", "gemm_multiple"), ("ms_contract_ss", "gemm_single")):
+        t = phases[key] / 1000
+        if t > 0:
+            out[label] = {"useful_tflops": flops / t / 1e12, "frac_of_bf16_peak": flops / t / 1e12 / peaks["bf16_tflops"]}
+    return out
+
+
 def run_gpu(args, dist, rank, ws):
     from temporalspecklescode_gb300 import api, config as cf
     api.load_library()
@@ -522,6 +553,10 @@ def run_gpu(args, dist, rank, ws):
         plain = {"value": pval, "unit": UNIT, "ms_per_step": pms, "renders": len(series),
                  "split_over_plain": value / pval if ws == 1 else None}
 
+    side = None
+    if rank == 0 and ws == 1 and args.side_paths_log2 > 0 and WORKLOAD == "correlation_3d":
+        side = side_workload("transmission_matrix_3d", args.side_paths_log2)
+
     cpu = None
     err = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -551,6 +586,7 @@ def run_gpu(args, dist, rank, ws):
         "roofline": roof,
         "kernels": {k: {kk: vv for kk, vv in v.items() if kk not in ("peak_name",)} for k, v in kernels.items()},
         "plain_fp32": plain,
+        "other_workloads": [side] if side else [],
         "rel_err_vs_fp64": err,
         "cpu_baseline": cpu,
         "clocks": clk,
@@ -660,6 +696,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP32 comparison render")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS),
                     help="correlation_3d (the headline), speckle_2d, transmission_matrix_3d or tracking_2d_pairs")
+    ap.add_argument("--side-paths-log2", type=int, default=18,
+                    help="headline run: also measure the 1024 x 1024 transmission matrix at this many paths (0: off)")
     ap.add_argument("--autotune", type=int, default=0,
                     help="choose the wavefront (paths per chunk) by timing this many paths per candidate first (0: off)")
     ap.add_argument("--serve", action="store_true", help="measure the serving mix instead of the headline workload")

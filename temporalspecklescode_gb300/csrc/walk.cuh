@@ -311,6 +311,82 @@ __device__ __forceinline__ float dda_cells(const DevScene& S, const V3& o, const
     return acc;
 }
 
+// Two traversals from the same point o (its cell b0, b1, b2) along da and db,
+// advanced in lockstep: the two rays' loads and arithmetic are independent,
+// so each step issues twice the work behind the same latencies.  A ray that
+// has reached the grid edge keeps its state (its cell stays inside the grid,
+// so its loads stay in bounds) and its sums stop changing.  Per ray the
+// arithmetic is dda_cells', so the depths and step counts are identical.
+template <int D>
+__device__ __forceinline__ void dda_cells_pair(const DevScene& S, const V3& o, const V3& da, const V3& db, int b0, int b1, int b2,
+                                               float& tau_a, float& tau_b, uint32_t& steps_a, uint32_t& steps_b)
+{
+    auto inv_of = [](float di) { return fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di); };
+    const float ia0 = inv_of(da.x), ia1 = inv_of(da.y), ia2 = D == 3 ? inv_of(da.z) : 0.0f;
+    const float ib0 = inv_of(db.x), ib1 = inv_of(db.y), ib2 = D == 3 ? inv_of(db.z) : 0.0f;
+    const int sa0 = da.x < 0.0f ? -1 : 1, sa1 = da.y < 0.0f ? -1 : 1, sa2 = (D == 3 && da.z < 0.0f) ? -1 : 1;
+    const int sb0 = db.x < 0.0f ? -1 : 1, sb1 = db.y < 0.0f ? -1 : 1, sb2 = (D == 3 && db.z < 0.0f) ? -1 : 1;
+    const int ea0 = sa0 > 0 ? S.n[0] - 2 : 0, ea1 = sa1 > 0 ? S.n[1] - 2 : 0, ea2 = D == 3 ? (sa2 > 0 ? S.n[2] - 2 : 0) : 0;
+    const int eb0 = sb0 > 0 ? S.n[0] - 2 : 0, eb1 = sb1 > 0 ? S.n[1] - 2 : 0, eb2 = D == 3 ? (sb2 > 0 ? S.n[2] - 2 : 0) : 0;
+    const float* ax0 = S.ax[0];
+    const float* ax1 = S.ax[1];
+    const float* ax2 = D == 3 ? S.ax[2] : nullptr;
+    const int sx = S.n[0] - 1, sxy = (S.n[0] - 1) * (S.n[1] - 1);
+    const uint32_t limit = (uint32_t)(S.n[0] + S.n[1] + (D == 3 ? S.n[2] : 0)) + 4u;
+    int a0 = b0, a1 = b1, a2 = b2, c0 = b0, c1 = b1, c2 = b2;   // ray a's and ray b's cells
+    float ta = 0.0f, acca = 0.0f, tb = 0.0f, accb = 0.0f;
+    uint32_t na = 0, nb = 0;
+    bool ra = true, rb = true;   // still traversing
+    while (ra || rb) {
+        const unsigned char ma = __ldg(S.grid + a0 + a1 * sx + (D == 3 ? a2 * sxy : 0));
+        const unsigned char mb = __ldg(S.grid + c0 + c1 * sx + (D == 3 ? c2 * sxy : 0));
+        const float fa0 = __ldg(ax0 + a0 + (sa0 > 0 ? 1 : 0)), fa1 = __ldg(ax1 + a1 + (sa1 > 0 ? 1 : 0));
+        const float fb0 = __ldg(ax0 + c0 + (sb0 > 0 ? 1 : 0)), fb1 = __ldg(ax1 + c1 + (sb1 > 0 ? 1 : 0));
+        const float fa2 = D == 3 ? __ldg(ax2 + a2 + (sa2 > 0 ? 1 : 0)) : 0.0f;
+        const float fb2 = D == 3 ? __ldg(ax2 + c2 + (sb2 > 0 ? 1 : 0)) : 0.0f;
+        const float ta0 = fm(fsb(fa0, o.x), ia0), ta1 = fm(fsb(fa1, o.y), ia1);
+        const float tb0 = fm(fsb(fb0, o.x), ib0), tb1 = fm(fsb(fb1, o.y), ib1);
+        int xa, xb;
+        float tna, tnb;
+        if (D == 2) {
+            xa = ta0 < ta1 ? 0 : 1; tna = xa == 0 ? ta0 : ta1;
+            xb = tb0 < tb1 ? 0 : 1; tnb = xb == 0 ? tb0 : tb1;
+        } else {
+            const float ta2 = fm(fsb(fa2, o.z), ia2), tb2 = fm(fsb(fb2, o.z), ib2);
+            xa = (ta0 < ta1 && ta0 < ta2) ? 0 : (ta1 < ta2 ? 1 : 2);
+            xb = (tb0 < tb1 && tb0 < tb2) ? 0 : (tb1 < tb2 ? 1 : 2);
+            tna = xa == 0 ? ta0 : (xa == 1 ? ta1 : ta2);
+            tnb = xb == 0 ? tb0 : (xb == 1 ? tb1 : tb2);
+        }
+        if (ra) {
+            acca = ffma(fsb(tna, ta), S.sigt[ma], acca);
+            ta = tna;
+            ++na;
+            const bool last = xa == 0 ? a0 == ea0 : (xa == 1 ? a1 == ea1 : a2 == ea2);
+            if (last || na >= limit) ra = false;
+            else {
+                a0 += xa == 0 ? sa0 : 0;
+                a1 += xa == 1 ? sa1 : 0;
+                if (D == 3) a2 += xa == 2 ? sa2 : 0;
+            }
+        }
+        if (rb) {
+            accb = ffma(fsb(tnb, tb), S.sigt[mb], accb);
+            tb = tnb;
+            ++nb;
+            const bool last = xb == 0 ? c0 == eb0 : (xb == 1 ? c1 == eb1 : c2 == eb2);
+            if (last || nb >= limit) rb = false;
+            else {
+                c0 += xb == 0 ? sb0 : 0;
+                c1 += xb == 1 ? sb1 : 0;
+                if (D == 3) c2 += xb == 2 ? sb2 : 0;
+            }
+        }
+    }
+    tau_a = acca; tau_b = accb;
+    steps_a += na; steps_b += nb;
+}
+
 // Packed start cell of a point (10 bits per axis), or kNoCell when an axis
 // has more than 1024 cells: a point's cell is the same for every ray leaving
 // it, so the view-side kernels look it up once per vertex.
@@ -359,6 +435,23 @@ __device__ inline float dda(const DevScene& S, const V3& o, const V3& d, uint32_
         b2 = D == 3 ? bin_of(S.ax[2], S.n[2], o.z) : 0;
     }
     return D == 3 ? dda_cells<3>(S, o, d, b0, b1, b2, steps) : dda_cells<2>(S, o, d, b0, b1, 0, steps);
+}
+
+// Optical depths from o along da and db (multi-cell media, o inside the box,
+// cell = o's packed cell): two traversals in lockstep (dda_cells_pair).
+__device__ inline void dda_pair(const DevScene& S, const V3& o, const V3& da, const V3& db, uint32_t cell,
+                                float& tau_a, float& tau_b, uint32_t& steps_a, uint32_t& steps_b)
+{
+    int b0, b1, b2;
+    if (cell != kNoCell) {
+        b0 = (int)(cell & 1023u); b1 = (int)((cell >> 10) & 1023u); b2 = (int)(cell >> 20);
+    } else {
+        b0 = bin_of(S.ax[0], S.n[0], o.x);
+        b1 = bin_of(S.ax[1], S.n[1], o.y);
+        b2 = S.dims == 3 ? bin_of(S.ax[2], S.n[2], o.z) : 0;
+    }
+    if (S.dims == 3) dda_cells_pair<3>(S, o, da, db, b0, b1, b2, tau_a, tau_b, steps_a, steps_b);
+    else dda_cells_pair<2>(S, o, da, db, b0, b1, 0, tau_a, tau_b, steps_a, steps_b);
 }
 
 }  // namespace sstmc
