@@ -14,7 +14,7 @@ estimator):
       20-degree cones; 2^24 paths.
   tracking_2d_pairs: 256^2 grid with a disc (sigs=4) whose scatterers drift
       by (0.5, 0) per frame, HG g=0.7, 128 x 128 far field, correlations of
-      all 32 x 32 frame pairs from the 63 lags t2 - t1; 2^23 paths.
+      all 32 x 32 frame pairs from the 32 lags t2 - t1 >= 0 (conjugates for the rest); 2^23 paths.
 
 value : contributions / device time of the render (CUDA events on the
         library's stream; scene tables resident in HBM).
@@ -64,7 +64,7 @@ WORKLOADS = {
     "speckle_2d": {"paths_log2": 16, "cpu_sample": 1 << 16, "ref_sample": 1 << 15, "err_paths": 1 << 14},
     # 3D transmission matrix: 1024 x 1024 far field, 64x64x32 grid of 4 materials, 2^24 paths
     "transmission_matrix_3d": {"paths_log2": 24, "cpu_sample": 1 << 11, "ref_sample": 1 << 10, "err_paths": 1 << 8},
-    # 2D tracking: 128 x 128 far field, 256^2 grid with a drifting disc, all 32 x 32 frame pairs (63 lags)
+    # 2D tracking: 128 x 128 far field, 256^2 grid with a drifting disc, all 32 x 32 frame pairs (32 lags)
     "tracking_2d_pairs": {"paths_log2": 23, "cpu_sample": 1 << 6, "ref_sample": 1 << 5, "err_paths": 1 << 3},
 }
 
@@ -595,7 +595,7 @@ def run_gpu(args, dist, rank, ws):
     if wavefront:
         line["config"]["wavefront"] = f"{wavefront} paths per chunk (sstmc_scene_autotune over a {args.autotune}-path sample)"
     if WORKLOAD == "tracking_2d_pairs":
-        line["config"]["frame_pairs"] = "32 x 32 frames from the 63 lags t2 - t1 (workloads.frame_pairs)"
+        line["config"]["frame_pairs"] = "32 x 32 frame pairs from the 32 lags t2 - t1 >= 0, conjugates for t2 < t1 (workloads.frame_pairs)"
     scene.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -337,10 +337,11 @@ __global__ void __launch_bounds__(128, 8) illum_kernel(const __grid_constant__ D
     if (lane == 0) st.flush(T);
 }
 
-// Multi-cell media trace two rays per lane in lockstep (dda_pair): their
-// traversal state needs more registers, so those variants run 4 blocks per SM.
+// Multi-cell media: 5 blocks per SM (102 registers), measured faster than 6
+// (80 registers, a few spills in the traversal) on the 64x64x32-grid workload;
+// single-cell media keep 6.
 template <bool CORR, bool VWP, bool SINGLE, bool THREE>
-__global__ void __launch_bounds__(128, SINGLE ? 6 : 4) view_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+__global__ void __launch_bounds__(128, SINGLE ? 6 : 5) view_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
 {
     extern __shared__ __align__(16) unsigned char vsm[];
     constexpr size_t kRecBytes = CORR ? sizeof(CRec) : sizeof(VRec);
@@ -570,19 +571,16 @@ __global__ void __launch_bounds__(128, SINGLE ? 6 : 4) view_kernel(const __grid_
                             }
                             tau2 = mul2(pk2(tm[0], tm[1]), r5.y);
                         } else {
-                            // the pair's two traversals in lockstep (identical to one at a time)
-                            const V3 xb = V3{ pk_lo(r0.x), pk_lo(r0.y), pk_lo(r1.x) };
-                            auto dir_to = [&](int h) {
-                                return VWP ? normalize32(S.dims, V3{ fsb(sv[2 * P + h].x, xb.x), fsb(sv[2 * P + h].y, xb.y),
-                                                                     fsb(sv[2 * P + h].z, xb.z) })
-                                           : V3{ h ? pk_hi(ox) : pk_lo(ox), h ? pk_hi(oy) : pk_lo(oy), h ? pk_hi(oz) : pk_lo(oz) };
-                            };
-                            float t0 = 0.0f, t1 = 0.0f;
-                            uint32_t s0 = 0, s1 = 0;
-                            if (rin) dda_pair(S, xb, dir_to(0), dir_to(1), rcell, t0, t1, s0, s1);
-                            steps += (lane + 32 * (2 * P) < nv) ? s0 * rays : 0u;
-                            steps += (lane + 32 * (2 * P + 1) < nv) ? s1 * rays : 0u;
-                            tau2 = pk2(t0, t1);
+                            float tt[2];
+#pragma unroll
+                            for (int h = 0; h < 2; ++h) {
+                                const V3 xb = V3{ pk_lo(r0.x), pk_lo(r0.y), pk_lo(r1.x) };
+                                uint32_t st = 0;
+                                const V3 oh = V3{ h ? pk_hi(ox) : pk_lo(ox), h ? pk_hi(oy) : pk_lo(oy), h ? pk_hi(oz) : pk_lo(oz) };
+                                tt[h] = VWP ? tau_to_point(S, xb, sv[2 * P + h], st, rcell) : tau_dir(S, xb, oh, st, rcell);
+                                steps += (lane + 32 * (2 * P + h) < nv) ? st * rays : 0u;
+                            }
+                            tau2 = pk2(tt[0], tt[1]);
                         }
                         // q = u_b - o, pdf = cw (omg2 + g q^2)^(-(D-1)/2)
                         const unsigned long long qx = fma2(ox, neg1, r1.y);
@@ -632,33 +630,10 @@ __global__ void __launch_bounds__(128, SINGLE ? 6 : 4) view_kernel(const __grid_
                     const VRec r = rec[i];
                     const V3 xb = V3{ r.x, r.y, r.z };
                     if (SINGLE) steps += r.in * rays * nvalid;
-                    // multi-cell media: the optical depths toward this lane's views, two
-                    // traversals at a time in lockstep (identical to one at a time)
-                    float tauv[kVPL];
-                    if constexpr (!SINGLE) {
-#pragma unroll
-                        for (int j = 0; j < kVPL; j += 2) {
-                            tauv[j] = 0.0f;
-                            if (j + 1 < kVPL) tauv[j + 1] = 0.0f;
-                            if (j >= vpl) break;
-                            const bool two = j + 1 < vpl;
-                            auto dir_to = [&](int k) {
-                                return VWP ? normalize32(S.dims, V3{ fsb(sv[k].x, xb.x), fsb(sv[k].y, xb.y), fsb(sv[k].z, xb.z) }) : sv[k];
-                            };
-                            const V3 da = dir_to(j);
-                            const V3 db = two ? dir_to(j + 1) : da;
-                            float t0 = 0.0f, t1 = 0.0f;
-                            uint32_t s0 = 0, s1 = 0;
-                            if (r.in) dda_pair(S, xb, da, db, r.cell, t0, t1, s0, s1);
-                            tauv[j] = t0;
-                            if (j + 1 < kVPL) tauv[j + 1] = t1;
-                            steps += (lane + 32 * j < nv) ? s0 * rays : 0u;
-                            steps += (two && lane + 32 * (j + 1) < nv) ? s1 * rays : 0u;
-                        }
-                    }
 #pragma unroll
                     for (int j = 0; j < kVPL; ++j) {
                         if (j >= vpl) break;
+                        const bool vok = lane + 32 * j < nv;   // lanes past the chunk's last view count no rays
                         // direction to the view and optical depth toward it (to the grid edge)
                         V3 o;
                         float tau, ri = 1.0f;
@@ -681,7 +656,9 @@ __global__ void __launch_bounds__(128, SINGLE ? 6 : 4) view_kernel(const __grid_
                             }
                             tau = tm * r.sig;
                         } else {
-                            tau = tauv[j];
+                            uint32_t st = 0;
+                            tau = VWP ? tau_to_point(S, xb, sv[j], st, r.cell) : tau_dir(S, xb, o, st, r.cell);
+                            steps += vok ? st * rays : 0u;
                         }
                         const V3 df = V3{ r.ux - o.x, r.uy - o.y, r.uz - o.z };
                         const float q2 = dot3(df, df);

@@ -261,130 +261,105 @@ __device__ inline void sample_source(const DevScene& S, const DevSource& src, St
     d0 = V3{ dir.x, dir.y, D == 3 ? dir.z : 0.0f };
 }
 
+// One ray's traversal state: the cell, its flat index, the distances to the
+// next face along each axis, and per axis the direction's sign, the index of
+// the last cell in that direction, the flat-index stride of a step and the
+// face table offset by the side the ray leaves through.
+template <int D>
+struct Ray {
+    int b0, b1, b2, idx;
+    float t0, t1, t2;        // distance to the next face along each axis
+    float i0, i1, i2;        // 1 / direction component (clamped)
+    int s0, s1, s2;          // direction signs
+    int e0, e1, e2;          // last cell index along each axis in the direction of travel
+    int d0, d1, d2;          // flat-index step of a cell along each axis
+    const float* f0;
+    const float* f1;
+    const float* f2;         // faces the ray leaves a cell through: ax[i] + (s_i > 0)
+    float t, acc;
+    uint32_t n;
+};
+
+template <int D>
+__device__ __forceinline__ void ray_init(const DevScene& S, const V3& o, const V3& d, int b0, int b1, int b2, Ray<D>& r)
+{
+    auto inv_of = [](float di) { return fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di); };
+    const int sx = S.n[0] - 1, sxy = (S.n[0] - 1) * (S.n[1] - 1);
+    r.b0 = b0; r.b1 = b1; r.b2 = b2;
+    r.idx = b0 + b1 * sx + (D == 3 ? b2 * sxy : 0);
+    r.i0 = inv_of(d.x); r.i1 = inv_of(d.y); r.i2 = D == 3 ? inv_of(d.z) : 0.0f;
+    r.s0 = d.x < 0.0f ? -1 : 1; r.s1 = d.y < 0.0f ? -1 : 1; r.s2 = (D == 3 && d.z < 0.0f) ? -1 : 1;
+    r.e0 = r.s0 > 0 ? S.n[0] - 2 : 0; r.e1 = r.s1 > 0 ? S.n[1] - 2 : 0; r.e2 = D == 3 ? (r.s2 > 0 ? S.n[2] - 2 : 0) : 0;
+    r.d0 = r.s0; r.d1 = r.s1 * sx; r.d2 = r.s2 * sxy;
+    r.f0 = S.ax[0] + (r.s0 > 0 ? 1 : 0);
+    r.f1 = S.ax[1] + (r.s1 > 0 ? 1 : 0);
+    r.f2 = D == 3 ? S.ax[2] + (r.s2 > 0 ? 1 : 0) : nullptr;
+    r.t0 = fm(fsb(__ldg(r.f0 + b0), o.x), r.i0);
+    r.t1 = fm(fsb(__ldg(r.f1 + b1), o.y), r.i1);
+    r.t2 = D == 3 ? fm(fsb(__ldg(r.f2 + b2), o.z), r.i2) : 0.0f;
+    r.t = 0.0f; r.acc = 0.0f; r.n = 0;
+}
+
+// One cell of the traversal: the extinction of the current cell over the
+// distance to the nearest face, then the step through that face.  Returns
+// false once the ray has left its last cell (or ran into the step limit).
+// The face distances of the axes not crossed keep their values: recomputing
+// them (as a traversal that recomputes every axis per cell does) gives the
+// same numbers from the same face, origin and inverse.
+template <int D>
+__device__ __forceinline__ bool ray_step(const DevScene& S, const V3& o, Ray<D>& r, uint32_t limit)
+{
+    const unsigned char m = __ldg(S.grid + r.idx);
+    int a;
+    float tn;
+    if (D == 2) {
+        a = r.t0 < r.t1 ? 0 : 1;
+        tn = a == 0 ? r.t0 : r.t1;
+    } else {
+        a = (r.t0 < r.t1 && r.t0 < r.t2) ? 0 : (r.t1 < r.t2 ? 1 : 2);
+        tn = a == 0 ? r.t0 : (a == 1 ? r.t1 : r.t2);
+    }
+    r.acc = ffma(fsb(tn, r.t), S.sigt[m], r.acc);
+    r.t = tn;
+    ++r.n;
+    const bool last = a == 0 ? r.b0 == r.e0 : (a == 1 ? r.b1 == r.e1 : r.b2 == r.e2);
+    if (last || r.n >= limit) return false;
+    if (a == 0) {
+        r.b0 += r.s0; r.idx += r.d0;
+        r.t0 = fm(fsb(__ldg(r.f0 + r.b0), o.x), r.i0);
+    } else if (D == 2 || a == 1) {
+        r.b1 += r.s1; r.idx += r.d1;
+        r.t1 = fm(fsb(__ldg(r.f1 + r.b1), o.y), r.i1);
+    } else {
+        r.b2 += r.s2; r.idx += r.d2;
+        r.t2 = fm(fsb(__ldg(r.f2 + r.b2), o.z), r.i2);
+    }
+    return true;
+}
+
+template <int D>
+__device__ __forceinline__ uint32_t ray_limit(const DevScene& S)
+{
+    return (uint32_t)(S.n[0] + S.n[1] + (D == 3 ? S.n[2] : 0)) + 4u;
+}
+
 // Voxel traversal from o along d, starting in cell (b0, b1, b2), in D
 // dimensions.  Every per-axis quantity lives in its own register (an array
-// indexed by the crossing axis would be placed in local memory): per step the
-// three face distances, the axis crossed first and the cell's extinction.
-// Arithmetic identical to the oracle's traversal (the same IEEE operations in
-// the same order), so the optical depth and the step count are too.
+// indexed by the crossing axis would be placed in local memory).  Per cell
+// the traversal loads the cell's material and one face: the axis crossed
+// first is the only one whose face distance changes.  Arithmetic identical
+// to the oracle's traversal (the same IEEE operations in the same order), so
+// the optical depth and the step count are too.
 template <int D>
 __device__ __forceinline__ float dda_cells(const DevScene& S, const V3& o, const V3& d, int b0, int b1, int b2,
                                            uint32_t& steps)
 {
-    auto inv_of = [](float di) { return fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di); };
-    const float i0 = inv_of(d.x), i1 = inv_of(d.y), i2 = D == 3 ? inv_of(d.z) : 0.0f;
-    const int s0 = d.x < 0.0f ? -1 : 1, s1 = d.y < 0.0f ? -1 : 1, s2 = (D == 3 && d.z < 0.0f) ? -1 : 1;
-    // the last cell index along each axis in the direction of travel (0 going down)
-    const int e0 = s0 > 0 ? S.n[0] - 2 : 0, e1 = s1 > 0 ? S.n[1] - 2 : 0, e2 = D == 3 ? (s2 > 0 ? S.n[2] - 2 : 0) : 0;
-    const float* ax0 = S.ax[0] + (s0 > 0 ? 1 : 0);
-    const float* ax1 = S.ax[1] + (s1 > 0 ? 1 : 0);
-    const float* ax2 = D == 3 ? S.ax[2] + (s2 > 0 ? 1 : 0) : nullptr;
-    const int sx = S.n[0] - 1, sxy = (S.n[0] - 1) * (S.n[1] - 1);
-    float t = 0.0f, acc = 0.0f;
-    uint32_t n = 0;
-    const uint32_t limit = (uint32_t)(S.n[0] + S.n[1] + (D == 3 ? S.n[2] : 0)) + 4u;
-    for (;;) {
-        const int idx = b0 + b1 * sx + (D == 3 ? b2 * sxy : 0);
-        const unsigned char m = __ldg(S.grid + idx);
-        const float t0 = fm(fsb(__ldg(ax0 + b0), o.x), i0);
-        const float t1 = fm(fsb(__ldg(ax1 + b1), o.y), i1);
-        int a;
-        float tna;
-        if (D == 2) {
-            a = t0 < t1 ? 0 : 1;
-            tna = a == 0 ? t0 : t1;
-        } else {
-            const float t2 = fm(fsb(__ldg(ax2 + b2), o.z), i2);
-            a = (t0 < t1 && t0 < t2) ? 0 : (t1 < t2 ? 1 : 2);
-            tna = a == 0 ? t0 : (a == 1 ? t1 : t2);
-        }
-        acc = ffma(fsb(tna, t), S.sigt[m], acc);
-        t = tna;
-        ++n;
-        const bool last = a == 0 ? b0 == e0 : (a == 1 ? b1 == e1 : b2 == e2);
-        if (last || n >= limit) break;
-        b0 += a == 0 ? s0 : 0;
-        b1 += a == 1 ? s1 : 0;
-        if (D == 3) b2 += a == 2 ? s2 : 0;
-    }
-    steps += n;
-    return acc;
-}
-
-// Two traversals from the same point o (its cell b0, b1, b2) along da and db,
-// advanced in lockstep: the two rays' loads and arithmetic are independent,
-// so each step issues twice the work behind the same latencies.  A ray that
-// has reached the grid edge keeps its state (its cell stays inside the grid,
-// so its loads stay in bounds) and its sums stop changing.  Per ray the
-// arithmetic is dda_cells', so the depths and step counts are identical.
-template <int D>
-__device__ __forceinline__ void dda_cells_pair(const DevScene& S, const V3& o, const V3& da, const V3& db, int b0, int b1, int b2,
-                                               float& tau_a, float& tau_b, uint32_t& steps_a, uint32_t& steps_b)
-{
-    auto inv_of = [](float di) { return fabsf(di) < 1e-12f ? (di >= 0.0f ? 1e12f : -1e12f) : fdv(1.0f, di); };
-    const float ia0 = inv_of(da.x), ia1 = inv_of(da.y), ia2 = D == 3 ? inv_of(da.z) : 0.0f;
-    const float ib0 = inv_of(db.x), ib1 = inv_of(db.y), ib2 = D == 3 ? inv_of(db.z) : 0.0f;
-    const int sa0 = da.x < 0.0f ? -1 : 1, sa1 = da.y < 0.0f ? -1 : 1, sa2 = (D == 3 && da.z < 0.0f) ? -1 : 1;
-    const int sb0 = db.x < 0.0f ? -1 : 1, sb1 = db.y < 0.0f ? -1 : 1, sb2 = (D == 3 && db.z < 0.0f) ? -1 : 1;
-    const int ea0 = sa0 > 0 ? S.n[0] - 2 : 0, ea1 = sa1 > 0 ? S.n[1] - 2 : 0, ea2 = D == 3 ? (sa2 > 0 ? S.n[2] - 2 : 0) : 0;
-    const int eb0 = sb0 > 0 ? S.n[0] - 2 : 0, eb1 = sb1 > 0 ? S.n[1] - 2 : 0, eb2 = D == 3 ? (sb2 > 0 ? S.n[2] - 2 : 0) : 0;
-    const float* ax0 = S.ax[0];
-    const float* ax1 = S.ax[1];
-    const float* ax2 = D == 3 ? S.ax[2] : nullptr;
-    const int sx = S.n[0] - 1, sxy = (S.n[0] - 1) * (S.n[1] - 1);
-    const uint32_t limit = (uint32_t)(S.n[0] + S.n[1] + (D == 3 ? S.n[2] : 0)) + 4u;
-    int a0 = b0, a1 = b1, a2 = b2, c0 = b0, c1 = b1, c2 = b2;   // ray a's and ray b's cells
-    float ta = 0.0f, acca = 0.0f, tb = 0.0f, accb = 0.0f;
-    uint32_t na = 0, nb = 0;
-    bool ra = true, rb = true;   // still traversing
-    while (ra || rb) {
-        const unsigned char ma = __ldg(S.grid + a0 + a1 * sx + (D == 3 ? a2 * sxy : 0));
-        const unsigned char mb = __ldg(S.grid + c0 + c1 * sx + (D == 3 ? c2 * sxy : 0));
-        const float fa0 = __ldg(ax0 + a0 + (sa0 > 0 ? 1 : 0)), fa1 = __ldg(ax1 + a1 + (sa1 > 0 ? 1 : 0));
-        const float fb0 = __ldg(ax0 + c0 + (sb0 > 0 ? 1 : 0)), fb1 = __ldg(ax1 + c1 + (sb1 > 0 ? 1 : 0));
-        const float fa2 = D == 3 ? __ldg(ax2 + a2 + (sa2 > 0 ? 1 : 0)) : 0.0f;
-        const float fb2 = D == 3 ? __ldg(ax2 + c2 + (sb2 > 0 ? 1 : 0)) : 0.0f;
-        const float ta0 = fm(fsb(fa0, o.x), ia0), ta1 = fm(fsb(fa1, o.y), ia1);
-        const float tb0 = fm(fsb(fb0, o.x), ib0), tb1 = fm(fsb(fb1, o.y), ib1);
-        int xa, xb;
-        float tna, tnb;
-        if (D == 2) {
-            xa = ta0 < ta1 ? 0 : 1; tna = xa == 0 ? ta0 : ta1;
-            xb = tb0 < tb1 ? 0 : 1; tnb = xb == 0 ? tb0 : tb1;
-        } else {
-            const float ta2 = fm(fsb(fa2, o.z), ia2), tb2 = fm(fsb(fb2, o.z), ib2);
-            xa = (ta0 < ta1 && ta0 < ta2) ? 0 : (ta1 < ta2 ? 1 : 2);
-            xb = (tb0 < tb1 && tb0 < tb2) ? 0 : (tb1 < tb2 ? 1 : 2);
-            tna = xa == 0 ? ta0 : (xa == 1 ? ta1 : ta2);
-            tnb = xb == 0 ? tb0 : (xb == 1 ? tb1 : tb2);
-        }
-        if (ra) {
-            acca = ffma(fsb(tna, ta), S.sigt[ma], acca);
-            ta = tna;
-            ++na;
-            const bool last = xa == 0 ? a0 == ea0 : (xa == 1 ? a1 == ea1 : a2 == ea2);
-            if (last || na >= limit) ra = false;
-            else {
-                a0 += xa == 0 ? sa0 : 0;
-                a1 += xa == 1 ? sa1 : 0;
-                if (D == 3) a2 += xa == 2 ? sa2 : 0;
-            }
-        }
-        if (rb) {
-            accb = ffma(fsb(tnb, tb), S.sigt[mb], accb);
-            tb = tnb;
-            ++nb;
-            const bool last = xb == 0 ? c0 == eb0 : (xb == 1 ? c1 == eb1 : c2 == eb2);
-            if (last || nb >= limit) rb = false;
-            else {
-                c0 += xb == 0 ? sb0 : 0;
-                c1 += xb == 1 ? sb1 : 0;
-                if (D == 3) c2 += xb == 2 ? sb2 : 0;
-            }
-        }
-    }
-    tau_a = acca; tau_b = accb;
-    steps_a += na; steps_b += nb;
+    Ray<D> r;
+    ray_init<D>(S, o, d, b0, b1, b2, r);
+    const uint32_t limit = ray_limit<D>(S);
+    while (ray_step<D>(S, o, r, limit)) {}
+    steps += r.n;
+    return r.acc;
 }
 
 // Packed start cell of a point (10 bits per axis), or kNoCell when an axis
@@ -437,21 +412,5 @@ __device__ inline float dda(const DevScene& S, const V3& o, const V3& d, uint32_
     return D == 3 ? dda_cells<3>(S, o, d, b0, b1, b2, steps) : dda_cells<2>(S, o, d, b0, b1, 0, steps);
 }
 
-// Optical depths from o along da and db (multi-cell media, o inside the box,
-// cell = o's packed cell): two traversals in lockstep (dda_cells_pair).
-__device__ inline void dda_pair(const DevScene& S, const V3& o, const V3& da, const V3& db, uint32_t cell,
-                                float& tau_a, float& tau_b, uint32_t& steps_a, uint32_t& steps_b)
-{
-    int b0, b1, b2;
-    if (cell != kNoCell) {
-        b0 = (int)(cell & 1023u); b1 = (int)((cell >> 10) & 1023u); b2 = (int)(cell >> 20);
-    } else {
-        b0 = bin_of(S.ax[0], S.n[0], o.x);
-        b1 = bin_of(S.ax[1], S.n[1], o.y);
-        b2 = S.dims == 3 ? bin_of(S.ax[2], S.n[2], o.z) : 0;
-    }
-    if (S.dims == 3) dda_cells_pair<3>(S, o, da, db, b0, b1, b2, tau_a, tau_b, steps_a, steps_b);
-    else dda_cells_pair<2>(S, o, da, db, b0, b1, 0, tau_a, tau_b, steps_a, steps_b);
-}
 
 }  // namespace sstmc

@@ -132,9 +132,10 @@ def tracking_2d(batch_size: int = 1 << 17, full_iteration: int = 64, n_dirs: int
 
 
 def frame_lags(frames: int) -> np.ndarray:
-    """The distinct lags t2 - t1 of the frame pairs (t1, t2) of `frames`
-    frames 0 .. frames-1: -(frames-1) .. frames-1."""
-    return np.arange(-(frames - 1), frames, dtype=float)
+    """The non-negative lags t2 - t1 of the frame pairs (t1, t2) of `frames`
+    frames 0 .. frames-1: 0 .. frames-1 (the negative ones follow by
+    conjugation, `frame_pairs`)."""
+    return np.arange(frames, dtype=float)
 
 
 def tracking_2d_pairs(batch_size: int = 1 << 17, full_iteration: int = 64, n_dirs: int = 128, frames: int = 32,
@@ -151,8 +152,11 @@ def tracking_2d_pairs(batch_size: int = 1 << 17, full_iteration: int = 64, n_dir
     sampler's estimator for a frame pair (t1, t2) depends on the pair only
     through t2 - t1 (the u1 and u2 paths take the sampled positions displaced
     by -U (t2 - t1) / 2 and +U (t2 - t1) / 2; the grid itself does not move),
-    so the ticks are the 2 frames - 1 distinct lags (`frame_lags`) and
-    `frame_pairs` scatters the rendered lags onto the frames x frames pairs."""
+    and with identical u1 / u2 sources a negative lag gives, path by path, the
+    conjugate of the positive one (the two displacements trade places and every
+    u1 x conj(u2) product turns into its conjugate; Brownian terms depend on
+    |t2 - t1|).  So the ticks are the `frames` lags 0 .. frames-1
+    (`frame_lags`) and `frame_pairs` fills the frames x frames pairs."""
     n = 256
     c = -128 + (np.arange(n) + 0.5)
     X, Y = np.meshgrid(c, c, indexing="ij")
@@ -174,15 +178,18 @@ def tracking_2d_pairs(batch_size: int = 1 << 17, full_iteration: int = 64, n_dir
 
 
 def frame_pairs(u: np.ndarray, frames: int) -> np.ndarray:
-    """Correlations of every frame pair from a render over `frame_lags(frames)`:
-    C[..., t1, t2] = u[..., lag index of t2 - t1] for u of shape
-    (Nl, Nv, 2 frames - 1, ...) (the tick axis third, as sstmc2D returns it).
+    """Correlations of every frame pair from a render over `frame_lags(frames)`
+    with identical u1 / u2 sources: C[..., t1, t2] = u[..., t2 - t1] for
+    t2 >= t1 and conj(u[..., t1 - t2]) for t2 < t1, for u of shape
+    (Nl, Nv, frames, ...) (the tick axis third, as sstmc2D returns it).
     Returns shape (Nl, Nv, frames, frames, ...)."""
-    if u.shape[2] != 2 * frames - 1:
-        raise ValueError(f"u has {u.shape[2]} ticks, expected the {2 * frames - 1} lags of {frames} frames")
+    if u.shape[2] != frames:
+        raise ValueError(f"u has {u.shape[2]} ticks, expected the {frames} lags of {frames} frames")
     t = np.arange(frames)
-    lag_index = (t[None, :] - t[:, None]) + (frames - 1)   # [t1, t2] -> index of t2 - t1
-    return u[:, :, lag_index]
+    lag = t[None, :] - t[:, None]   # [t1, t2] -> t2 - t1
+    C = u[:, :, np.abs(lag)]
+    neg = (lag < 0).reshape((1, 1, frames, frames) + (1,) * (u.ndim - 3))
+    return np.where(neg, np.conj(C), C)
 
 
 WORKLOADS = {

@@ -110,22 +110,26 @@ def test_c_abi_refuses_empty_sources(oracle):
 
 
 def test_frame_pairs_indexing():
-    """frame_pairs maps the lag axis -(F-1) .. F-1 onto the F x F pairs by t2 - t1."""
+    """frame_pairs maps the lags 0 .. F-1 onto the F x F pairs by t2 - t1, and
+    the pairs with t2 < t1 onto the conjugate of lag t1 - t2."""
     from temporalspecklescode_gb300 import workloads as wl
     F = 5
     lags = wl.frame_lags(F)
-    assert lags.tolist() == list(range(-4, 5))
-    u = np.broadcast_to(lags[None, None, :, None], (2, 3, 2 * F - 1, 1)).astype(complex)
+    assert lags.tolist() == list(range(F))
+    u = np.broadcast_to((lags + 1j * (lags + 10))[None, None, :, None], (2, 3, F, 1))
     C = wl.frame_pairs(u, F)
     assert C.shape == (2, 3, F, F, 1)
     for t1 in range(F):
         for t2 in range(F):
-            assert C[1, 2, t1, t2, 0] == t2 - t1
+            d = abs(t2 - t1)
+            assert C[1, 2, t1, t2, 0] == (d + 1j * (d + 10) if t2 >= t1 else d - 1j * (d + 10))
 
 
 def test_frame_pairs_oracle_equals_per_pair_ticks(oracle):
-    """On the oracle (FP64, every tick evaluated on its own), the lag render
-    scattered onto the frame pairs equals the render over every pair's lag."""
+    """On the oracle (FP64, every tick evaluated on its own), the render over
+    the non-negative lags, filled onto the frame pairs by conjugation, equals
+    the render whose ticks are every pair's own lag t2 - t1 (negative lags
+    included): the estimator is conjugate-symmetric in the lag path by path."""
     from temporalspecklescode_gb300 import config as cf
     from temporalspecklescode_gb300 import workloads as wl
     F = 3

@@ -5,8 +5,8 @@ the FP64 oracle finishes in seconds.
   cones, a 64x64x32 grid of four iid materials; its far-field x far-field
   single-scattering GEMMs run per material.
 * tracking_2d_pairs: 128 x 128 far-field directions on a 256^2 grid whose
-  disc drifts, the correlation sampler over the 63 lags of 32 frames, and
-  the frame-pair correlations scattered from them.
+  disc drifts, the correlation sampler over the 32 lags of 32 frames, and
+  the frame-pair correlations filled from them.
 
 Integers (iteration counts, vertices, voxel steps, contributions) exact,
 fields within a relative Frobenius error of 1e-5.
@@ -66,7 +66,7 @@ def test_transmission_matrix_rows_full_shape(api, oracle):
 def test_tracking_pairs_full_shape(api, oracle):
     cfg, dims = wl.tracking_2d_pairs(batch_size=8, full_iteration=1, seed=2)
     u, uo = _render_vs_oracle(api, oracle, cfg, dims, 13)
-    assert u.shape == (128, 128, 63)
+    assert u.shape == (128, 128, 32)
     assert rel_fro(u, uo) <= REL_TOL
     C = wl.frame_pairs(u[..., None], 32)[..., 0]
     Co = wl.frame_pairs(uo[..., None], 32)[..., 0]
@@ -75,10 +75,10 @@ def test_tracking_pairs_full_shape(api, oracle):
 
 
 def test_frame_pairs_equal_per_pair_ticks(api):
-    """Rendering the 2F - 1 distinct lags and scattering them onto the F x F
-    frame pairs gives the render whose ticks are every pair's own lag t2 - t1
-    (the same paths; the two renders differ only in how the contraction
-    splits its FP32 windows)."""
+    """Rendering the F non-negative lags and filling the F x F frame pairs
+    from them (conjugates for t2 < t1) gives the render whose ticks are every
+    pair's own lag t2 - t1, negative lags included (the same paths; the two
+    renders differ only in how the contraction splits its FP32 windows)."""
     F = 4
     cfg, dims = wl.tracking_2d_pairs(batch_size=64, full_iteration=2, n_dirs=8, frames=F, seed=4)
     with api.Scene(cfg, dims) as s:
