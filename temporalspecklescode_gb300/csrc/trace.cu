@@ -332,9 +332,29 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
     unsigned long long acc_v = 0, acc_s = 0, acc_m = 0, acc_p = 0;
-    for (uint32_t q = gw; q < T.paths; q += nw) {
+    // Work items: a path (its vertices 2 .. B, or with segments 2 .. seg + 1),
+    // or in segment mode a (path, k) item of T.seg_list: vertices
+    // 2 + k seg .. min(B, 1 + (k + 1) seg) of one long path, its view sums
+    // added to the path's rows after the path's own launch wrote them.
+    const bool segm = CORR && T.seg_mode;
+    for (uint32_t it = gw;;) {
+        uint32_t q, bs = 2;
+        if (segm) {
+            uint32_t w = 0;
+            if (lane == 0) w = atomicAdd(T.seg_next, 1u);
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (w >= *T.seg_len) break;
+            const uint2 item = T.seg_list[w];
+            q = item.x;
+            bs = 2u + item.y * T.seg;
+        } else {
+            if (it >= T.paths) break;
+            q = it;
+            it += nw;
+        }
         const uint32_t pid = T.first_path + q;
         const uint32_t B = T.counts[q];
+        const uint32_t be = (CORR && T.seg) ? min(B, bs + T.seg - 1u) : B;   // last vertex of the item
         const uint32_t qs = T.ss_row ? T.ss_row[q] : q;   // row of the single-scattering rows
         if (B == 0) {  // the walk hit a limit (error already flagged)
             zero_rows(S, T, q, lane);
@@ -345,7 +365,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         const V3 x1 = V3{ v1.x, v1.y, v1.z };
         const int m1 = (int)(__float_as_uint(v1.w) & 15u);
         const float xi1 = (float)(__float_as_uint(v1.w) >> 4) * (1.0f / 16777216.0f);
-        const uint32_t c1 = S.single ? kNoCell : cell_of(S, x1);   // x1's grid cell, the start of its NEE rays
+        const uint32_t c1 = (S.single || segm) ? kNoCell : cell_of(S, x1);   // x1's grid cell, the start of its NEE rays
         float* xtc = bufA;   // tick positions of the current vertex
         float* xtn = bufB;   // tick positions of the new vertex
         bool mov1 = false;
@@ -360,7 +380,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         uint32_t steps = 0;
 
         // ---- illumination side at x1: P_l, Gl0, single-scattering rows ----
-        if (T.pass0 && !T.cbs) {
+        if (T.pass0 && !T.cbs && !segm) {
             float ps = 0.0f;
             for (int l = lane; l < Nl; l += 32) {
                 uint32_t st = 0;
@@ -456,7 +476,24 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         V3 prev = x1, cur = x1;
         int mcur = m1;
         float MT = 0.0f;
-        for (uint32_t b = 2; b <= B; ++b) {
+        if (segm) {
+            // the segment starts after vertex bs - 1: its two predecessors, and the
+            // momentum-transfer sum of the inner vertices before it (lanes over the
+            // vertices, then a warp sum)
+            const float4 pb = vq[bs - 3], cb = vq[bs - 2];
+            prev = V3{ pb.x, pb.y, pb.z };
+            cur = V3{ cb.x, cb.y, cb.z };
+            mcur = (int)(__float_as_uint(cb.w) & 15u);
+            float part = 0.0f;
+            for (uint32_t b = 3 + lane; b < bs; b += 32) {
+                const float4 a = vq[b - 3], c = vq[b - 2], n = vq[b - 1];
+                const V3 xa = V3{ a.x, a.y, a.z }, xc = V3{ c.x, c.y, c.z }, xn = V3{ n.x, n.y, n.z };
+                const V3 dq = sub3(funit(sub3(xc, xa)), funit(sub3(xn, xc)));
+                part += S.D[__float_as_uint(c.w) & 15u] * dot3(dq, dq);
+            }
+            MT = warp_sum(part);
+        }
+        for (uint32_t b = bs; b <= be; ++b) {
             if (!T.views && b > 2) break;   // the view-side kernel sums the view vectors
             const float4 vb = vq[b - 1];
             const V3 xn = V3{ vb.x, vb.y, vb.z };
@@ -710,24 +747,29 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             mcur = mn;
             float* tmp = xtc; xtc = xtn; xtn = tmp;
         }
-        if (T.pass0 && B < 2) {
+        if (T.pass0 && B < 2 && !segm) {
             if (T.cbs) for (int i = lane; i < Nt * Nv; i += 32) T.s_ms[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
             else for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
         }
-        // write the summed view vector of this chunk
+        // write the summed view vector of this chunk (a segment adds its part)
         if (T.views) {
             int j = 0;
             for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                 int k = 0;
                 for (int t = T.t0 + lane / T.vw; t < T.t0 + T.tn; t += T.tg, ++k) {
-                    if (T.cbs) T.a_ms[((size_t)q * Nt + t) * Nl + v] = accs[32 * (j * T.tpl + k)];
-                    else T.s_ms[((size_t)q * Nt + t) * Nv + v] = accs[32 * (j * T.tpl + k)];
+                    const float2 a = accs[32 * (j * T.tpl + k)];
+                    if (segm) {
+                        float2* d = T.s_ms + ((size_t)q * Nt + t) * Nv + v;
+                        atomicAdd(&d->x, a.x);
+                        atomicAdd(&d->y, a.y);
+                    } else if (T.cbs) T.a_ms[((size_t)q * Nt + t) * Nl + v] = a;
+                    else T.s_ms[((size_t)q * Nt + t) * Nv + v] = a;
                 }
             }
         }
         const uint32_t wsteps = warp_sum_u32(steps);
         if (lane == 0) {
-            if (T.pass0 && !T.cbs) {
+            if (T.pass0 && !T.cbs && !segm) {
                 if (T.m1) T.m1[q] = (unsigned char)m1;
                 if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
                 acc_v += B;
@@ -935,6 +977,32 @@ int launch_cbs_corr(const DevScene& S, const CbsCorrParams& P, cudaStream_t stre
         if (vp) cbs_corr_kernel<false, true><<<grid, 256, 0, stream>>>(S, Q);
         else cbs_corr_kernel<false, false><<<grid, 256, 0, stream>>>(S, Q);
     }
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
+}
+
+namespace {
+
+// The long paths' extra segments: for every path of more than seg + 1
+// vertices, the items (path, k) for k = 1 .. (B - 2) / seg.  The list's order
+// is that of the atomic appends; capacity cap >= total vertices / seg.
+__global__ void seg_list_kernel(const uint32_t* counts, uint32_t n, uint32_t seg, uint2* list, uint32_t cap, uint32_t* len)
+{
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint32_t B = counts[q];
+        if (B <= seg + 1u) continue;
+        const uint32_t extra = (B - 2u) / seg;
+        const uint32_t at = atomicAdd(len, extra);
+        for (uint32_t k = 1; k <= extra && at + k - 1u < cap; ++k) list[at + k - 1u] = make_uint2(q, k);
+    }
+}
+
+}  // namespace
+
+int launch_seg_list(const uint32_t* counts, uint32_t n, uint32_t seg, uint2* list, uint32_t cap, uint32_t* len, cudaStream_t stream)
+{
+    if (cudaMemsetAsync(len, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    const int blocks = (int)std::min<uint32_t>(4096, (n + 255) / 256);
+    seg_list_kernel<<<std::max(1, blocks), 256, 0, stream>>>(counts, n, seg, list, cap, len);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 

@@ -42,7 +42,20 @@ struct TraceParams {
     float* p2;            // [paths] or null: the correlation sampler's second-point probability (CBS)
     const uint32_t* ss_row;   // [paths] or null: row of path q in a_ss / b_ss (paths grouped by first-vertex
                               // material for the far-field x far-field contraction); null: row q
+    // correlation sampler, view passes: long paths in segments of `seg` vertices
+    // (0: whole paths).  A path's own launch sums vertices 2 .. seg + 1; a second
+    // launch with seg_mode = 1 takes (path, k) items from seg_list and adds the
+    // sums of vertices 2 + k seg .. 1 + (k + 1) seg to the path's rows.
+    uint32_t seg;
+    int seg_mode;
+    const uint2* seg_list;
+    const uint32_t* seg_len;  // [1] items in seg_list
+    uint32_t* seg_next;       // [1] items taken (zeroed before each segment launch)
 };
+
+// The (path, k) items of the paths longer than seg + 1 vertices (trace.cu).
+int launch_seg_list(const uint32_t* counts, uint32_t n, uint32_t seg, uint2* list, uint32_t cap, uint32_t* len,
+                    cudaStream_t stream);
 
 // Correlation-sampler CBS cross terms (trace.cu, cbs_corr_kernel): V +=
 // 0.5 (T2 + T3 + T4) over the paths [0, K) of a chunk.
