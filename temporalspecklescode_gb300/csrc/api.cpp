@@ -56,6 +56,9 @@ bool use_view_kernel()
 
 // The split-precision contraction runs on the tensor cores (gemm_tc.cu);
 // SSTMC_CONTRACTION=simt selects the SIMT form (gemm_kernel) instead.
+// vertices per segment of a long path in the correlation sampler's general kernel
+constexpr uint32_t kSegVerts = 256;
+
 bool use_tensor_cores()
 {
     const char* e = std::getenv("SSTMC_CONTRACTION");
@@ -131,11 +134,12 @@ int Engine::ensure(Scene& S, uint32_t paths)
 void Engine::release()
 {
     void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts,
-                   slots, longq, ovf, ovf_owner, p2v, ss_row, ss_hist, ss_bucket };
+                   slots, longq, ovf, ovf_owner, p2v, ss_row, ss_hist, ss_bucket, seg_list, seg_ctr };
     for (void* p : ps) if (p) cudaFreeAsync(p, stream);
     counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
     slots = nullptr; longq = nullptr; ovf = nullptr; ovf_owner = nullptr; p2v = nullptr;
     ss_row = ss_hist = ss_bucket = nullptr;
+    seg_list = nullptr; seg_cap = 0; seg_ctr = nullptr;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
     pl = x1 = x1t = nullptr;
     m1 = nullptr; totals = nullptr; err = nullptr; V = nullptr; W = nullptr;
@@ -347,14 +351,45 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         return SSTMC_NO_ERROR;
     }
     T.views = 1;
+    // correlation sampler: paths longer than kSegVerts + 1 vertices are summed in
+    // segments of kSegVerts vertices by as many warps (one warp walking a path of
+    // thousands of vertices would otherwise bound each launch); not in the
+    // static-scratch render, which allocates nothing
+    const bool segmented = S.correlation && !S.cfg_copy.is_cbs && !fixed;
+    if (segmented) {
+        const size_t want = (size_t)(nverts / kSegVerts) + 1;
+        if (want > seg_cap || !seg_ctr) {
+            if (seg_list) cudaFreeAsync(seg_list, stream);
+            seg_list = nullptr; seg_cap = 0;
+            if (!seg_ctr && cudaMallocAsync((void**)&seg_ctr, 2 * sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+            const size_t cap = want + want / 4 + 1024;
+            if (cudaMallocAsync((void**)&seg_list, cap * sizeof(uint2), stream) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+            seg_cap = cap;
+        }
+        e = launch_seg_list(counts, n, kSegVerts, seg_list, (uint32_t)std::min<size_t>(seg_cap, 0xffffffffu), seg_ctr, stream);
+        if (e) return e;
+        launches++;
+        T.seg = kSegVerts; T.seg_list = seg_list; T.seg_len = seg_ctr; T.seg_next = seg_ctr + 1;
+    }
     bool first_pass = true;
     for (auto& vc : vch) {
         for (auto& tc : tch) {
             T.pass0 = first_pass ? 1 : 0;
             T.v0 = vc.first; T.vn = vc.second; T.t0 = tc.first; T.tn = tc.second;
+            T.seg_mode = 0;
             e = launch_trace(S.dev, T, blocks, threads, stream);
             if (e) return e;
             launches++;
+            if (segmented) {
+                // the long paths' other segments, added to the rows just written
+                TraceParams Sg = T;
+                Sg.seg_mode = 1;
+                Sg.pass0 = 0;
+                if (cudaMemsetAsync(seg_ctr + 1, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+                e = launch_trace(S.dev, Sg, blocks, threads, stream);
+                if (e) return e;
+                launches++;
+            }
             first_pass = false;
         }
     }

@@ -44,6 +44,11 @@ struct Engine {
     uint32_t* ss_hist = nullptr;  // [ceil(paths / 1024)][kMat] scratch of the partition
     uint32_t* ss_bucket = nullptr;  // [kMat + 1] first row of each material
     bool ss_bucketed = false;     // the chunk's a_ss / b_ss rows are grouped (trace_chunk -> contract_chunk)
+    // correlation sampler, general kernel: (path, segment) items of the long
+    // paths (trace.cu); grown with the vertex buffer, null in the static render
+    uint2* seg_list = nullptr;
+    size_t seg_cap = 0;
+    uint32_t* seg_ctr = nullptr;  // [2] items in the list, items taken
     uint2* ovf_owner = nullptr;
     float4* verts = nullptr;
     size_t verts_cap = 0;

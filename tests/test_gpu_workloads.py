@@ -91,3 +91,25 @@ def test_frame_pairs_equal_per_pair_ticks(api):
     C = wl.frame_pairs(u, F)[..., 0]
     C2 = u2[..., 0].reshape(8, 8, F, F)
     assert rel_fro(C, C2) <= 1e-6
+
+
+def test_long_path_segments_match_oracle(api, oracle):
+    """Correlation sampler with drifting scatterers and paths of hundreds to
+    thousands of vertices: the general kernel sums such paths in segments of
+    256 vertices on separate warps (each starting from the momentum-transfer
+    sum of the vertices before it); the render matches the oracle, which walks
+    every path in one piece."""
+    cfg, dims = wl.tracking_2d_pairs(batch_size=96, full_iteration=1, n_dirs=8, frames=4, seed=6)
+    with api.Scene(cfg, dims) as s:
+        g = s.trace_paths(seed=21, first_path=0, paths=96)
+        assert g["vertices"].max() > 2 * 256 + 1   # several segments on the longest path
+        u, it = s.render(seed=21)
+        st = s.stats()
+    pc = cf.prepare(cfg, dims)
+    o = oracle.trace_paths(pc, 21, 0, 96)
+    for k in ("vertices", "vertex_hash", "dda_steps"):
+        assert np.array_equal(g[k], o[k]), k
+    assert rel_fro(g["s_ms"], o["s_ms"]) <= REL_TOL
+    uo, ito, sto = oracle.render(pc, 21)
+    assert it[0] == ito and st["dda_steps"] == sto["dda_steps"]
+    assert rel_fro(u[..., 0], uo) <= REL_TOL
