@@ -27,6 +27,9 @@ plain_fp32 : the plain FP32 form (FP32 phases, SIMT contraction) on the same
 --impl reference: the reference has no CPU implementation, so the reference
         arm times the CPU FP64 restatement of its estimator (oracle/) on all
         host threads.
+--impl reference-gpu: the reference's own CUDA path (its headers staged by
+        oracle/stage_reference.sh, built by oracle/refharness.mk) on the
+        workload's scene at a reduced batch.
 
 Multi-GPU (torchrun): replicas with disjoint seeds ("replicas only": the
 paths are i.i.d.); the one exchange step sums the ranks' accumulators and
@@ -658,21 +661,25 @@ def run_serve(args):
     with api.Server(slots=4) as srv:
         reqs = []
         submitted = []
-        t_next = time.perf_counter()
-        for i, k in enumerate(picks):
-            t_next += rng.expovariate(1.0 / mean_gap)
-            delay = t_next - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            reqs.append(srv.submit(scenes[k], 100 + i))
-            submitted.append(time.perf_counter())
-        # completion times by polling (latency = completion - submission)
-        done = [None] * len(reqs)
-        while any(d is None for d in done):
+        done = [None] * n_req
+
+        def poll():
+            # completion times by polling every 0.2 ms, also between arrivals
+            # (latency = completion - submission)
             for i, r in enumerate(reqs):
                 if done[i] is None and r.done():
                     done[i] = time.perf_counter()
             time.sleep(2e-4)
+
+        t_next = time.perf_counter()
+        for i, k in enumerate(picks):
+            t_next += rng.expovariate(1.0 / mean_gap)
+            while time.perf_counter() < t_next:
+                poll()
+            reqs.append(srv.submit(scenes[k], 100 + i))
+            submitted.append(time.perf_counter())
+        while any(d is None for d in done):
+            poll()
         for r in reqs:
             r.result()
         st = srv.stats()

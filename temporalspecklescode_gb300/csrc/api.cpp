@@ -56,7 +56,7 @@ bool use_view_kernel()
 
 // The split-precision contraction runs on the tensor cores (gemm_tc.cu);
 // SSTMC_CONTRACTION=simt selects the SIMT form (gemm_kernel) instead.
-// vertices per segment of a long path in the correlation sampler's general kernel
+// vertices per segment of a long path in the general trace kernel
 constexpr uint32_t kSegVerts = 256;
 
 bool use_tensor_cores()
@@ -351,11 +351,11 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         return SSTMC_NO_ERROR;
     }
     T.views = 1;
-    // correlation sampler: paths longer than kSegVerts + 1 vertices are summed in
-    // segments of kSegVerts vertices by as many warps (one warp walking a path of
-    // thousands of vertices would otherwise bound each launch); not in the
-    // static-scratch render, which allocates nothing
-    const bool segmented = S.correlation && !S.cfg_copy.is_cbs && !fixed;
+    // paths longer than kSegVerts + 1 vertices are summed in segments of
+    // kSegVerts vertices by as many warps (one warp walking a path of thousands
+    // of vertices would otherwise bound each launch); not in the static-scratch
+    // render, which allocates nothing, nor for CBS's reversed pass
+    const bool segmented = !S.cfg_copy.is_cbs && !fixed;
     if (segmented) {
         const size_t want = (size_t)(nverts / kSegVerts) + 1;
         if (want > seg_cap || !seg_ctr) {

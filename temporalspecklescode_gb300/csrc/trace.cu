@@ -336,7 +336,18 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     // or in segment mode a (path, k) item of T.seg_list: vertices
     // 2 + k seg .. min(B, 1 + (k + 1) seg) of one long path, its view sums
     // added to the path's rows after the path's own launch wrote them.
-    const bool segm = CORR && T.seg_mode;
+    const bool segm = T.seg_mode != 0;
+    const bool segf = !CORR && segm;   // field sampler segment: its path-length prefix is replayed
+    // path length of tick t across one segment a -> c: FP64 (split) or FP32
+    auto path_step = [&](double* L, int t, const V3& a, const V3& c) {
+        if (split) {
+            const double dx = (double)c.x - (double)a.x, dy = (double)c.y - (double)a.y, dz = (double)c.z - (double)a.z;
+            L[t] += sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+        } else {
+            const V3 dd = sub3(c, a);
+            L[t] = (double)((float)L[t] + sqrtf(dot3(dd, dd)));
+        }
+    };
     for (uint32_t it = gw;;) {
         uint32_t q, bs = 2;
         if (segm) {
@@ -354,7 +365,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         }
         const uint32_t pid = T.first_path + q;
         const uint32_t B = T.counts[q];
-        const uint32_t be = (CORR && T.seg) ? min(B, bs + T.seg - 1u) : B;   // last vertex of the item
+        const uint32_t be = T.seg ? min(B, bs + T.seg - 1u) : B;   // last vertex of the item
         const uint32_t qs = T.ss_row ? T.ss_row[q] : q;   // row of the single-scattering rows
         if (B == 0) {  // the walk hit a limit (error already flagged)
             zero_rows(S, T, q, lane);
@@ -476,7 +487,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
         V3 prev = x1, cur = x1;
         int mcur = m1;
         float MT = 0.0f;
-        if (segm) {
+        if (CORR && segm) {
             // the segment starts after vertex bs - 1: its two predecessors, and the
             // momentum-transfer sum of the inner vertices before it (lanes over the
             // vertices, then a warp sum)
@@ -493,6 +504,22 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             }
             MT = warp_sum(part);
         }
+        if (segf) {
+            // the segment starts after vertex bs - 1: replay the per-tick positions of
+            // vertices 2 .. bs - 1 and their path-length sums, the same FP64 additions in
+            // the same order as the path's own warp makes them
+            const float4 pb = vq[bs - 3], cb = vq[bs - 2];
+            prev = V3{ pb.x, pb.y, pb.z };
+            cur = V3{ cb.x, cb.y, cb.z };
+            mcur = (int)(__float_as_uint(cb.w) & 15u);
+            for (uint32_t c = 2; c < bs; ++c) {
+                const float4 vc = vq[c - 1];
+                temporal_positions(S, T.seed, pid, c, V3{ vc.x, vc.y, vc.z }, (int)(__float_as_uint(vc.w) & 15u), xtn, lane);
+                for (int t = lane; t < Nt; t += 32) path_step(Ls, t, tick_pos(xtc, t), tick_pos(xtn, t));
+                __syncwarp();
+                float* tmp = xtc; xtc = xtn; xtn = tmp;
+            }
+        }
         for (uint32_t b = bs; b <= be; ++b) {
             if (!T.views && b > 2) break;   // the view-side kernel sums the view vectors
             const float4 vb = vq[b - 1];
@@ -508,14 +535,10 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             if constexpr (!CORR) {
                 temporal_positions(S, T.seed, pid, b, xn, mn, xtn, lane);
                 for (int t = lane; t < Nt; t += 32) {
-                    const V3 a = tick_pos(xtc, t), c = tick_pos(xtn, t);
+                    path_step(Ls, t, tick_pos(xtc, t), tick_pos(xtn, t));
                     if (split) {
-                        const double dx = (double)c.x - (double)a.x, dy = (double)c.y - (double)a.y, dz = (double)c.z - (double)a.z;
-                        Ls[t] += sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
                         phs[t] = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
                     } else {
-                        const V3 dd = sub3(c, a);
-                        Ls[t] = (double)((float)Ls[t] + sqrtf(dot3(dd, dd)));
                         const float ph = (float)Ls[t] * S.inv_lambda_f + xin;
                         phs[t] = ph - rintf(ph);
                     }

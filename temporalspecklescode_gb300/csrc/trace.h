@@ -42,8 +42,7 @@ struct TraceParams {
     float* p2;            // [paths] or null: the correlation sampler's second-point probability (CBS)
     const uint32_t* ss_row;   // [paths] or null: row of path q in a_ss / b_ss (paths grouped by first-vertex
                               // material for the far-field x far-field contraction); null: row q
-    // correlation sampler, view passes: long paths in segments of `seg` vertices
-    // (0: whole paths).  A path's own launch sums vertices 2 .. seg + 1; a second
+    // view passes: long paths in segments of `seg` vertices (0: whole paths).  A path's own launch sums vertices 2 .. seg + 1; a second
     // launch with seg_mode = 1 takes (path, k) items from seg_list and adds the
     // sums of vertices 2 + k seg .. 1 + (k + 1) seg to the path's rows.
     uint32_t seg;

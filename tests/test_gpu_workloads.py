@@ -113,3 +113,24 @@ def test_long_path_segments_match_oracle(api, oracle):
     uo, ito, sto = oracle.render(pc, 21)
     assert it[0] == ito and st["dda_steps"] == sto["dda_steps"]
     assert rel_fro(u[..., 0], uo) <= REL_TOL
+
+
+def test_long_path_segments_field_sampler_match_oracle(api, oracle):
+    """The field sampler with drifting scatterers and paths of thousands of
+    vertices: each 256-vertex segment replays the per-tick positions and
+    path-length sums of the vertices before it (the same FP64 additions in the
+    same order), so its path phases are the path's own; rows and render match
+    the oracle."""
+    cfg, dims = wl.tracking_2d(batch_size=48, full_iteration=1, n_dirs=8, frames=4, seed=6)
+    with api.Scene(cfg, dims) as s:
+        g = s.trace_paths(seed=23, first_path=0, paths=48)
+        assert g["vertices"].max() > 2 * 256 + 1
+        u, it = s.render(seed=23)
+    pc = cf.prepare(cfg, dims)
+    o = oracle.trace_paths(pc, 23, 0, 48)
+    for k in ("vertices", "vertex_hash", "dda_steps"):
+        assert np.array_equal(g[k], o[k]), k
+    assert rel_fro(g["s_ms"], o["s_ms"]) <= REL_TOL
+    uo, ito, _ = oracle.render(pc, 23)
+    assert it[0] == ito
+    assert rel_fro(u[..., 0], uo) <= REL_TOL
