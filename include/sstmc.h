@@ -70,7 +70,7 @@ extern "C" {
 #define SSTMC_SOURCE_NONE          0   /* absent illumination2 / view2 */
 #define SSTMC_SOURCE_POINT         1
 #define SSTMC_SOURCE_FARFIELD      2
-#define SSTMC_SOURCE_GAUSSIANBEAM  3   /* not supported by this build */
+#define SSTMC_SOURCE_GAUSSIANBEAM  3   /* focused beams: 3D field sampler, illumination and view both GaussianBeam */
 
 /* config.sampler.type (MatlabInterface.cu:1238, 1295) */
 #define SSTMC_SAMPLER_TEMPORAL              0
@@ -92,9 +92,14 @@ extern "C" {
  * MatlabInterface.cu:1062-1215 (buildSource). */
 typedef struct sstmc_source_cfg {
     int32_t type;            /* SSTMC_SOURCE_* */
-    uint32_t count;          /* number of locations / directions */
-    const double* xyz;       /* count x 3 doubles (x, y, z); z ignored when dims == 2 */
+    uint32_t count;          /* number of locations / directions / beams */
+    const double* xyz;       /* count x 3 doubles (x, y, z); z ignored when dims == 2.  GaussianBeam: focal points */
     int32_t is_area_source;  /* PointSource isAreaSource (default 0) */
+    /* GaussianBeam (MatlabInterface.cu:1161-1200): focalDirection per beam
+     * (count x 3 doubles, used as given) and the scalar aperture; ignored by
+     * the other types */
+    const double* focal_direction;
+    double aperture;
 } sstmc_source_cfg;
 
 /* The whole MATLAB config struct (README.md:74-373). */
@@ -350,6 +355,11 @@ int32_t sstmc_source_create_point(const sstmc_simulation* sim, int32_t connectio
                                   int32_t is_area_source, sstmc_source** out);
 int32_t sstmc_source_create_far_field(const sstmc_simulation* sim, int32_t connection, const double* xyz, uint32_t count,
                                       sstmc_source** out);
+/* GaussianBeam(err, simulation, medium, scattering, focalPoints, focalDirections,
+ * aperture, beamsNum, connectionType) (GaussianBeam.cuh:62-64, MatlabInterface.cu:
+ * 1193-1194): focal points and directions n x 3 doubles, one aperture. */
+int32_t sstmc_source_create_gaussian_beam(const sstmc_simulation* sim, int32_t connection, const double* focal_points,
+                                          const double* focal_directions, uint32_t count, double aperture, sstmc_source** out);
 int32_t sstmc_source_size(const sstmc_source* s, uint32_t* count);
 int32_t sstmc_source_destroy(sstmc_source* s);
 

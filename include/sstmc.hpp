@@ -194,6 +194,20 @@ public:
     }
 };
 
+/* GaussianBeam(err, simulation, medium, scattering, focalPoints (n x 3),
+ * focalDirections (n x 3), aperture, n, connectionType) */
+class GaussianBeam : public Source {
+public:
+    GaussianBeam(ErrorType* err, const Simulation* simulation, const Medium*, const Scattering*, const double* focalPoints,
+                 const double* focalDirections, double aperture, ub32 n, ConnectionType cn)
+    {
+        const ErrorType e = simulation
+            ? sstmc_source_create_gaussian_beam(simulation->handle(), (int32_t)cn, focalPoints, focalDirections, n, aperture, &h_)
+            : SSTMC_INVALID_HANDLE;
+        if (err) *err = e;
+    }
+};
+
 /* SamplerInterface.cuh:11-176 */
 class Sampler {
 public:

@@ -3,7 +3,7 @@
 //
 // It builds the reference's objects from a scene file in the order mexFunction
 // builds them (MatlabInterface.cu:1677-1700): Simulation -> Scattering ->
-// HeterogeneousMedium + setMaterial -> PointSource / FarField (illumination,
+// HeterogeneousMedium + setMaterial -> PointSource / FarField / GaussianBeam (illumination,
 // view, and for the correlation sampler illumination2 / view2) ->
 // TemporalSampler / TemporalCorrelationSampler + setMaterial ->
 // NextEventEstimation, then renders `renderings` times with the seed
@@ -17,11 +17,13 @@
 //
 // Scene file: whitespace-separated tokens, written by tests/refharness_lib.py:
 //   batch B  full_iteration F  renderings R  seed S  lambda L
-//   scattering n  then n x (kind g), kind 0 isotropic / 3 Henyey-Greenstein
+//   scattering n  then n x (kind g), kind 0 isotropic / 3 Henyey-Greenstein,
+//                 or (4 k mu_1..mu_k c_1..c_k alpha_1..alpha_k) for a vMF mixture
 //   axis a n v_0 .. v_{n-1}    (a = 0, 1, 2)
 //   grid n m_0 .. m_{n-1}      (x fastest)
 //   materials n  then n x (sigs siga)
 //   source role type count xyz...   (role 0..3, type 1 point / 2 far field)
+//   source role 3 count xyz... dir... aperture   (a Gaussian beam per focal point)
 //   sampler type                    (0 temporal, 1 correlation)
 //   ticks n t_0 .. t_{n-1}
 //   motion n  then n x (D ux uy uz)
@@ -41,6 +43,7 @@
 #include "Implementation/Sampler/TemporalSamplerCorrelation.cuh"
 #include "Implementation/Source/PointSource.cuh"
 #include "Implementation/Source/FarField.cuh"
+#include "Implementation/Source/GaussianBeam.cuh"
 
 namespace {
 
@@ -50,11 +53,14 @@ struct SceneFile {
     double lambda = 1.0;
     std::vector<int> scat_kind;
     std::vector<double> scat_g;
+    std::vector<std::vector<double>> vmf_mu, vmf_c, vmf_alpha;
     std::vector<double> axis[3];
     std::vector<ub32> grid;
     std::vector<double> sigs, siga;
     int src_type[4] = { 0, 0, 0, 0 };
     std::vector<double> src_xyz[4];
+    std::vector<double> src_dir[4];
+    double aperture[4] = { 0, 0, 0, 0 };
     int sampler = 0;
     std::vector<double> ticks;
     std::vector<double> D, U;
@@ -74,7 +80,16 @@ bool read_scene(const char* path, SceneFile* s)
         else if (key == "scattering") {
             size_t n; in >> n;
             s->scat_kind.resize(n); s->scat_g.resize(n);
-            for (size_t i = 0; i < n; ++i) in >> s->scat_kind[i] >> s->scat_g[i];
+            s->vmf_mu.resize(n); s->vmf_c.resize(n); s->vmf_alpha.resize(n);
+            for (size_t i = 0; i < n; ++i) {
+                in >> s->scat_kind[i];
+                if (s->scat_kind[i] != 4) { in >> s->scat_g[i]; continue; }
+                size_t k; in >> k;
+                for (auto* v : { &s->vmf_mu[i], &s->vmf_c[i], &s->vmf_alpha[i] }) {
+                    v->resize(k);
+                    for (auto& x : *v) in >> x;
+                }
+            }
         } else if (key == "axis") {
             int a; size_t n; in >> a >> n;
             s->axis[a].resize(n);
@@ -92,6 +107,11 @@ bool read_scene(const char* path, SceneFile* s)
             s->src_type[role] = type;
             s->src_xyz[role].resize(3 * n);
             for (auto& v : s->src_xyz[role]) in >> v;
+            if (type == 3) {
+                s->src_dir[role].resize(3 * n);
+                for (auto& v : s->src_dir[role]) in >> v;
+                in >> s->aperture[role];
+            }
         } else if (key == "sampler") in >> s->sampler;
         else if (key == "ticks") {
             size_t n; in >> n;
@@ -123,8 +143,14 @@ int main(int argc, char** argv)
     CHECK("Simulation");
     Scattering* scattering = new Scattering();
     for (size_t m = 0; m < sc.scat_kind.size(); ++m) {
-        err = sc.scat_kind[m] == 3 ? scattering->setHenyeyGreensteinScattering(sc.scat_g[m], (ub32)m)
-                                   : scattering->setIsotropicScattering((ub32)m);
+        if (sc.scat_kind[m] == 4) {
+            std::vector<float_type> mu(sc.vmf_mu[m].begin(), sc.vmf_mu[m].end()), c(sc.vmf_c[m].begin(), sc.vmf_c[m].end()),
+                alpha(sc.vmf_alpha[m].begin(), sc.vmf_alpha[m].end());
+            err = scattering->setVonMisesFisherScattering(mu.data(), c.data(), alpha.data(), (ub32)mu.size(), (ub32)m);
+        } else {
+            err = sc.scat_kind[m] == 3 ? scattering->setHenyeyGreensteinScattering(sc.scat_g[m], (ub32)m)
+                                       : scattering->setIsotropicScattering((ub32)m);
+        }
         CHECK("Scattering");
     }
     HeterogeneousMedium* medium = new HeterogeneousMedium(&err, sc.grid.data(), sc.axis[0].data(), (ub32)sc.axis[0].size(),
@@ -147,15 +173,18 @@ int main(int argc, char** argv)
     for (int r = 0; r < 4; ++r) {
         if (!sc.src_type[r]) continue;
         const ub32 n = (ub32)(sc.src_xyz[r].size() / 3);
-        std::vector<VectorType> v(n);
+        std::vector<VectorType> v(n), dir(n);
         for (ub32 i = 0; i < n; ++i) {
 #if DIMS==3
             v[i] = VectorType(sc.src_xyz[r][3 * i], sc.src_xyz[r][3 * i + 1], sc.src_xyz[r][3 * i + 2]);
+            if (sc.src_type[r] == 3) dir[i] = VectorType(sc.src_dir[r][3 * i], sc.src_dir[r][3 * i + 1], sc.src_dir[r][3 * i + 2]);
 #else
             v[i] = VectorType(sc.src_xyz[r][3 * i], sc.src_xyz[r][3 * i + 1]);
+            if (sc.src_type[r] == 3) dir[i] = VectorType(sc.src_dir[r][3 * i], sc.src_dir[r][3 * i + 1]);
 #endif
         }
-        if (sc.src_type[r] == 1) src[r] = new PointSource(&err, simulation, medium, scattering, v.data(), n, false, roles[r]);
+        if (sc.src_type[r] == 3) src[r] = new GaussianBeam(&err, simulation, medium, scattering, v.data(), dir.data(), sc.aperture[r], n, roles[r]);
+        else if (sc.src_type[r] == 1) src[r] = new PointSource(&err, simulation, medium, scattering, v.data(), n, false, roles[r]);
         else src[r] = new FarField(&err, simulation, medium, scattering, v.data(), n, roles[r]);
         CHECK("Source");
     }

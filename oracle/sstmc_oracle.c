@@ -53,6 +53,17 @@ typedef struct {
     float* ps;       /* n*3 perpendicular S (3D) */
     float* mint; float* maxt; float* mins; float* maxs;
     double* sprob;   /* n: far-field projected-box sampling probability */
+    /* Gaussian beam (GaussianBeam.cuh): p = focal points, gdir = beam directions */
+    float* gdir;     /* n*3 */
+    double ga;       /* beam concentration 1 / aperture^2 */
+    double gnorm;    /* aperture normalisation vMFnormalizationLog(ga) */
+    int gM;          /* illumination: table stride, the most lobes of a focal material */
+    int* gfm;        /* illumination: material at each focal point */
+    double* gtab;    /* illumination: per beam tmin, tmax, dt, xy base (2 x 3) */
+    double* gpdf;    /* illumination: [n][gM][B] bin pdf */
+    double* gicdf;   /* illumination: [n][gM][B] exclusive bin cdf */
+    double* gapdf;   /* illumination: [n][gM] lobe pdf */
+    double* gaicdf;  /* illumination: [n][gM] exclusive lobe cdf */
 } o_src;
 
 typedef struct {
@@ -98,6 +109,12 @@ typedef struct {
     int forced_bin;       /* field sampler isForcedInsideBin */
     double lambda;
     unsigned P, full_iter;
+    /* Gaussian beams: per material its vMF lobes (mu, C + log alpha), in 2D and 3D */
+    int gauss;
+    int gmix_n[OM], gmix_off[OM];
+    double* gmix;
+    double gmean[3];      /* mean view direction (normalised) */
+    double sigs_d[OM];    /* scattering coefficient per material */
 } o_scene;
 
 static void o_free_scene(o_scene* S)
@@ -106,7 +123,9 @@ static void o_free_scene(o_scene* S)
         o_src* s = &S->src[i];
         free(s->p); free(s->inv); free(s->tang); free(s->pt); free(s->ps);
         free(s->mint); free(s->maxt); free(s->mins); free(s->maxs); free(s->sprob);
+        free(s->gdir); free(s->gfm); free(s->gtab); free(s->gpdf); free(s->gicdf); free(s->gapdf); free(s->gaicdf);
     }
+    free(S->gmix);
     for (int a = 0; a < 3; ++a) { free(S->ax[a]); free(S->axd[a]); }
     free(S->grid); free(S->ticks); free(S->ticks_f); free(S->disp_scale); free(S->disp_u);
     free(S->tab_f); free(S->tab_pdf); free(S->tab_cos);
@@ -180,6 +199,9 @@ static int o_prep_farfield(o_src* s, const sstmc_source_cfg* c, int dims,
     return SSTMC_NO_ERROR;
 }
 
+static double o_vmf_log_norm(double x);
+static int o_prep_gauss(o_scene* S);
+
 static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const double bmin[3], const double bmax[3])
 {
     memset(s, 0, sizeof(*s));
@@ -187,7 +209,23 @@ static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const do
     if (c->type == SSTMC_SOURCE_NONE) return SSTMC_NO_ERROR;
     if (c->count == 0 || c->xyz == NULL) return SSTMC_INVALID_CONFIG;
     if (c->type == SSTMC_SOURCE_FARFIELD) return o_prep_farfield(s, c, dims, bmin, bmax);
-    if (c->type != SSTMC_SOURCE_POINT) return SSTMC_NOT_SUPPORTED;
+    if (c->type == SSTMC_SOURCE_GAUSSIANBEAM) {
+        if (dims != 3) return SSTMC_NOT_SUPPORTED;   /* 2D beams need the complex Bessel I0 (not built) */
+        if (!c->focal_direction || !(c->aperture > 0.0) || !isfinite(c->aperture)) return SSTMC_INVALID_CONFIG;
+        s->gdir = calloc((size_t)s->n * 3, sizeof(float));
+        if (!s->gdir) return SSTMC_ALLOCATION_ERROR;
+        for (int k = 0; k < 3 * s->n; ++k) s->gdir[k] = (float)c->focal_direction[k];
+        for (int k = 0; k < s->n; ++k) {   /* a beam needs a direction */
+            const float* d = s->gdir + 3 * k;
+            if (!(d[0] != 0.0f || d[1] != 0.0f || d[2] != 0.0f) || !isfinite(d[0]) || !isfinite(d[1]) || !isfinite(d[2]))
+                return SSTMC_INVALID_CONFIG;
+        }
+        /* GaussianBeam.cuh:1056-1068: ga = 1 / aperture^2, the aperture normalised */
+        s->ga = 1.0 / (c->aperture * c->aperture);
+        s->gnorm = o_vmf_log_norm(s->ga);
+    } else if (c->type != SSTMC_SOURCE_POINT) {
+        return SSTMC_NOT_SUPPORTED;
+    }
     s->p = calloc((size_t)s->n * 3, sizeof(float));
     if (!s->p) return SSTMC_ALLOCATION_ERROR;
     for (int k = 0; k < s->n; ++k) {
@@ -299,6 +337,8 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         }
     }
     if (vmf_comp) {
+        S->gmix = malloc(sizeof(double) * 2 * vmf_comp);
+        if (!S->gmix) return SSTMC_ALLOCATION_ERROR;
         S->vmf_mc = malloc(sizeof(double) * 2 * vmf_comp);
         S->vmf_pd = malloc(sizeof(double) * 3 * vmf_pairs);
         S->vmf_pf = malloc(sizeof(float) * 3 * vmf_pairs);
@@ -328,10 +368,14 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         }
         /* isIsotropicScattering per material, Scattering.cuh:1484-1512 */
         int iso = ty == SSTMC_SCATTERING_ISOTROPIC || (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && fabs(g) < 0.0001);
-        int vn = 0, voff = 0, vpoff = 0;
+        int vn = 0, voff = 0, vpoff = 0, goff = 0;
         if (ty == SSTMC_SCATTERING_VMF_MIXTURE) {
             vn = (int)cfg->vmf_n[m];
             const double *mu = cfg->vmf_mu + vmf_pos, *cc = cfg->vmf_c + vmf_pos, *al = cfg->vmf_alpha + vmf_pos;
+            /* the lobes the Gaussian-beam terms read: mixtureMu and mixtureC + log(alpha)
+             * (Scattering.cuh:703-721), kept in 2D too */
+            goff = (int)vmf_pos;
+            for (int k = 0; k < vn; ++k) { S->gmix[2 * (vmf_pos + k)] = mu[k]; S->gmix[2 * (vmf_pos + k) + 1] = cc[k] + log(al[k]); }
             vmf_pos += (size_t)vn;
             double asum = 0.0;
             iso = 1;   /* every |mu| <= 1e-4, Scattering.cuh:744-751 */
@@ -357,6 +401,8 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
             S->vmf_n[mm] = dims == 3 ? vn : 0;
             S->vmf_off[mm] = voff;
             S->vmf_poff[mm] = vpoff;
+            S->gmix_n[mm] = vn;
+            S->gmix_off[mm] = goff;
             iso_m[mm] = iso;
             S->scat_type[mm] = (ty == SSTMC_SCATTERING_VMF_MIXTURE && dims == 2) ? SSTMC_SCATTERING_ISOTROPIC : ty;
             S->g_f[mm] = (float)g;
@@ -371,9 +417,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     S->iso_all = 1;
     for (int m = 0; m < OM; ++m)
         if (S->scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && !iso_m[m]) S->iso_all = 0;
-    /* all materials isotropic with a vMF among them: point sources would take the
-     * isotropic amplitude and far-field sources the mixture's (not built) */
-    if (S->iso_all && any_vmf) return SSTMC_NOT_SUPPORTED;
 
     /* medium */
     double bmin[3] = { 0, 0, 0 }, bmax[3] = { 0, 0, 0 };
@@ -413,6 +456,7 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     } else {
         return SSTMC_NOT_SUPPORTED;
     }
+    for (int m = 0; m < OM; ++m) S->sigs_d[m] = sigs[m];
     for (int a = 0; a < dims; ++a) for (int i = 0; i < S->n[a]; ++i) S->axd[a][i] = (double)S->ax[a][i];
     for (int a = 0; a < dims; ++a) {
         S->bmin[a] = S->ax[a][0]; S->bmax[a] = S->ax[a][S->n[a] - 1];
@@ -440,6 +484,11 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         if (e) return e;
     }
     if (S->src[0].type == SSTMC_SOURCE_NONE || S->src[1].type == SSTMC_SOURCE_NONE) return SSTMC_INVALID_CONFIG;
+    S->gauss = S->src[0].type == SSTMC_SOURCE_GAUSSIANBEAM || S->src[1].type == SSTMC_SOURCE_GAUSSIANBEAM;
+    /* all materials isotropic with a vMF among them: point sources would take the
+     * isotropic amplitude and far-field sources the mixture's (not built);
+     * Gaussian beams read the lobes themselves */
+    if (S->iso_all && any_vmf && !S->gauss) return SSTMC_NOT_SUPPORTED;
 
     /* sampler */
     if (!cfg->t || cfg->t_num == 0) return SSTMC_INVALID_CONFIG;
@@ -464,6 +513,10 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         /* correlation CBS is built for static scatterers (no drift U) */
         if (S->cbs && S->correlation && (S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f))
             return SSTMC_NOT_SUPPORTED;
+    }
+    if (S->gauss) {
+        int e = o_prep_gauss(S);
+        if (e) return e;
     }
     /* field sampler: ticks sorted around the mean, TemporalSampler.cuh:958-1150 */
     S->disp_scale = calloc((size_t)OM * Nt, sizeof(float));
@@ -607,6 +660,8 @@ static inline void o_random_direction(int dims, o_stream* rs, float out[3])
 }
 
 /* Scattering::newDirection: Scattering.cuh:1039-1115, VectorType.cuh:261-282. */
+static void o_rotate(const o_scene* S, const float din[3], float c, o_stream* rs, float out[3]);
+
 static void o_sample_direction(const o_scene* S, int m, const float din[3], o_stream* rs, float out[3])
 {
     int ty = S->scat_type[m];
@@ -659,6 +714,13 @@ static void o_sample_direction(const o_scene* S, int m, const float din[3], o_st
             c = ((1.0f + gg) - s * s) / (2.0f * g);
         }
     }
+    o_rotate(S, din, c, rs, out);
+}
+
+/* The direction at cosine c to din (VectorType.cuh:207-283, vector_rotation):
+ * a side (2D) or an azimuth (3D) from the stream. */
+static void o_rotate(const o_scene* S, const float din[3], float c, o_stream* rs, float out[3])
+{
     float sa = (o_uniform(rs) < 0.5f ? -1.0f : 1.0f) * sqrtf(fmaxf(0.0f, 1.0f - c * c));
     if (S->dims == 2) {
         out[0] = din[0] * c - din[1] * sa;
@@ -935,8 +997,14 @@ static double o_ray(const o_scene* S, const float x[3], const float df[3], const
 }
 
 /* First point probability term P_l(x): FarField.cuh:469-499, PointSource.cuh:92-115, 263-294. */
+static double o_gauss_pfirst(const o_scene* S, const o_src* s, int l, const float x1[3], int m1);
+static oc o_gauss_g(const o_scene* S, const o_src* s, int k, const float x[3], int role, uint64_t* steps);
+static oc o_gauss_f(const o_scene* S, const o_src* s, int k, const float pa[3], const float pb[3], int m, int role);
+static oc o_gauss_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v, const float xf[3], int m);
+
 static double o_pfirst(const o_scene* S, const o_src* s, int l, const float x[3], uint64_t* steps)
 {
+    if (s->type == SSTMC_SOURCE_GAUSSIANBEAM) return o_gauss_pfirst(S, s, l, x, o_inside(S, x) ? S->grid[o_cell(S, x)] : 0);
     if (s->type == SSTMC_SOURCE_FARFIELD) {
         float df[3] = { -s->p[3 * l], -s->p[3 * l + 1], -s->p[3 * l + 2] };
         double dd[3] = { df[0], df[1], df[2] };
@@ -957,6 +1025,7 @@ static double o_pfirst(const o_scene* S, const o_src* s, int l, const float x[3]
 static oc o_g(const o_scene* S, const o_src* s, int k, const float x[3], int role, uint64_t* steps)
 {
     oc g;
+    if (s->type == SSTMC_SOURCE_GAUSSIANBEAM) return o_gauss_g(S, s, k, x, role, steps);
     if (s->type == SSTMC_SOURCE_FARFIELD) {
         const float* d = s->p + 3 * k;
         float sgn = role == 0 ? -1.0f : 1.0f;
@@ -1018,6 +1087,7 @@ static void o_src_dir(const o_src* s, int k, const float x[3], int toward_source
  * FarField.cuh:546-554, PointSource.cuh:317-345.  role 0 illumination, 1 view. */
 static oc o_f3(const o_scene* S, const o_src* s, int k, const float a[3], const float b[3], int m, int role)
 {
+    if (s->type == SSTMC_SOURCE_GAUSSIANBEAM) return o_gauss_f(S, s, k, a, b, m, role);
     double ab[3]; o_dir64(a, b, ab);
     if (s->type == SSTMC_SOURCE_FARFIELD) {
         double d[3] = { s->p[3 * k], s->p[3 * k + 1], s->p[3 * k + 2] };
@@ -1033,6 +1103,7 @@ static oc o_f3(const o_scene* S, const o_src* s, int k, const float a[3], const 
  * FarField.cuh:556-599, PointSource.cuh:347-405. */
 static oc o_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v, const float x[3], int m)
 {
+    if (il->type == SSTMC_SOURCE_GAUSSIANBEAM) return o_gauss_fs(S, il, l, vw, v, x, m);
     if (il->type == SSTMC_SOURCE_POINT && S->iso_all) { oc r = { S->dims == 2 ? O_ISO_AMP2 : O_ISO_AMP3, 0.0 }; return r; }
     double in[3], out[3];
     if (il->type == SSTMC_SOURCE_FARFIELD) { in[0] = il->p[3 * l]; in[1] = il->p[3 * l + 1]; in[2] = il->p[3 * l + 2]; }
@@ -1040,6 +1111,457 @@ static oc o_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v,
     if (vw->type == SSTMC_SOURCE_FARFIELD) { out[0] = vw->p[3 * v]; out[1] = vw->p[3 * v + 1]; out[2] = vw->p[3 * v + 2]; }
     else o_dir64(x, vw->p + 3 * v, out);
     return o_ampc(S, m, o_dot(in, out));
+}
+
+/* ------------------------------------------------------------------ */
+/* Gaussian beams (3D): Implementation/Source/GaussianBeam.cuh        */
+/* ------------------------------------------------------------------ */
+#define O_GB_BINS 1000   /* zSamplesNum, GaussianBeam.cuh:62-64 */
+
+static inline oc oc_add(oc a, oc b) { oc r = { a.re + b.re, a.im + b.im }; return r; }
+static inline oc oc_sub(oc a, oc b) { oc r = { a.re - b.re, a.im - b.im }; return r; }
+static inline double oc_abs(oc a) { return sqrt(a.re * a.re + a.im * a.im); }
+static inline oc oc_div(oc a, oc b)
+{
+    double d = b.re * b.re + b.im * b.im;
+    oc r = { (a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d };
+    return r;
+}
+static inline oc oc_exp(oc a)
+{
+    double e = exp(a.re);
+    oc r = { e * cos(a.im), e * sin(a.im) };
+    return r;
+}
+/* principal square root by the half-angle form of ComplexType.cuh:109-131:
+ * s = sqrt((|re| + |z|) / 2); (s, im / 2s) for re >= 0, else (|im| / 2s, +-s) */
+static inline oc oc_sqrt(oc a)
+{
+    oc r = { 0.0, 0.0 };
+    if (a.re == 0.0 && a.im == 0.0) return r;
+    double s = sqrt((fabs(a.re) + oc_abs(a)) * 0.5);
+    if (a.re >= 0.0) { r.re = s; r.im = a.im / (2.0 * s); }
+    else { r.re = fabs(a.im) / (2.0 * s); r.im = copysign(s, a.im); }
+    return r;
+}
+/* 1 / sqrt(z) (ComplexType.cuh:133-146): the conjugate of the root over |root|^2 */
+static inline oc oc_rsqrt(oc a)
+{
+    double s2 = (fabs(a.re) + oc_abs(a)) * 0.5;
+    double mult = 1.0 / (s2 + (a.im * a.im) / (4.0 * s2));
+    double s = sqrt(s2);
+    oc r;
+    if (a.re >= 0.0) { r.re = s * mult; r.im = -a.im * mult / (2.0 * s); }
+    else { r.re = fabs(a.im) * mult / (2.0 * s); r.im = copysign(s * mult, -a.im); }
+    return r;
+}
+/* e^(c + z) - e^(c - z), each exponential dropped when its real part is at or
+ * below -10 (ComplexType.cuh:170-209, complex2timesSinh) */
+static inline oc oc_2sinh(oc z, oc c)
+{
+    oc p = oc_add(c, z), n = oc_sub(c, z), r = { 0.0, 0.0 };
+    if (p.re > -10.0) r = oc_add(r, oc_exp(p));
+    if (n.re > -10.0) r = oc_sub(r, oc_exp(n));
+    return r;
+}
+/* sum_i (a v_i + T_i)^2 over the three axes, a real, v real, T complex */
+static inline oc o_gsumsq(double a, const double v[3], const oc T[3])
+{
+    oc r = { 0.0, 0.0 };
+    for (int i = 0; i < 3; ++i) {
+        double x = a * v[i] + T[i].re, y = T[i].im;
+        r.re += x * x - y * y; r.im += 2.0 * x * y;
+    }
+    return r;
+}
+/* The beam's complex throughput ga d + i k (x - f) (GaussianBeam.cuh:530-532, 845-846) */
+static inline void o_gthroughput(const o_src* s, int l, const double x[3], double k, oc T[3])
+{
+    for (int i = 0; i < 3; ++i) {
+        T[i].re = (double)s->gdir[3 * l + i] * s->ga;
+        T[i].im = k * (x[i] - (double)s->p[3 * l + i]);
+    }
+}
+
+/* Lobe-pair proposal of the second direction for beam l at x1 (computeCdfBuffer,
+ * GaussianBeam.cuh:489-621): per pair j = i1 + M i2 of the focal material's lobes
+ * the summed real mean direction conv[j], log C[j] (1 / (4 pi) below kappa = 1e-4,
+ * as the reference) and the normalised weight w[j]. */
+static void o_gauss_pairs(const o_scene* S, const o_src* s, int l, const float x1[3], double* conv, double* logC, double* w)
+{
+    int fm = s->gfm[l], M = S->gmix_n[fm];
+    const double* mix = S->gmix + 2 * S->gmix_off[fm];
+    double k = 2.0 * O_PI / S->lambda;
+    double x[3] = { x1[0], x1[1], x1[2] };
+    oc T[3]; o_gthroughput(s, l, x, k, T);
+    double lc[64], lv[64][3];   /* per lobe: c and the real mean (M <= 8) */
+    for (int i = 0; i < M; ++i) {
+        double mu = mix[2 * i];
+        if (fabs(mu) < 1e-9) {
+            double z0[3] = { 0, 0, 0 };
+            oc C = oc_sqrt(o_gsumsq(0.0, z0, T));
+            lc[i] = C.re - log(oc_abs(C)) + mix[2 * i + 1];
+            lv[i][0] = lv[i][1] = lv[i][2] = 0.0;
+        } else {
+            oc g0 = oc_rsqrt(o_gsumsq(mu, S->gmean, T));
+            g0.re *= mu; g0.im *= mu;
+            double cv[3];
+            for (int a = 0; a < 3; ++a) cv[a] = g0.re * T[a].re - g0.im * T[a].im;
+            double r = 1.0 / sqrt(cv[0] * cv[0] + cv[1] * cv[1] + cv[2] * cv[2]);
+            double wv[3] = { r * cv[0], r * cv[1], r * cv[2] };
+            oc C = oc_sqrt(o_gsumsq(mu, wv, T));
+            lc[i] = C.re - log(oc_abs(C)) + mix[2 * i + 1] - (wv[0] * cv[0] + wv[1] * cv[1] + wv[2] * cv[2]);
+            lv[i][0] = cv[0]; lv[i][1] = cv[1]; lv[i][2] = cv[2];
+        }
+    }
+    double sum = 0.0;
+    for (int j = 0; j < M * M; ++j) {
+        int i1 = j % M, i2 = j / M;
+        double* cj = conv + 3 * j;
+        for (int a = 0; a < 3; ++a) cj[a] = lv[i1][a] + lv[i2][a];
+        double kap = sqrt(cj[0] * cj[0] + cj[1] * cj[1] + cj[2] * cj[2]);
+        logC[j] = kap < 1e-4 ? 1.0 / (4.0 * O_PI) : o_vmf_log_norm(kap);
+        w[j] = exp(lc[i1] + lc[i2] - logC[j] - 2.0 * s->ga);
+        sum += w[j];
+    }
+    for (int j = 0; j < M * M; ++j) w[j] /= sum;
+}
+
+/* Largest i < n with cdf[i] <= u (cdf[0] = 0; Simulation.cuh:325-367 up to ties) */
+static inline int o_cdf_pick(const double* cdf, int n, double u)
+{
+    int lo = 0, hi = n;
+    while (hi - lo > 1) { int mid = (lo + hi) >> 1; if (cdf[mid] <= u) lo = mid; else hi = mid; }
+    return lo;
+}
+
+/* Standard normal from two uniforms (Box-Muller, the cosine branch), in the
+ * portable FP32 functions of the walk */
+static inline float o_normal(o_stream* rs)
+{
+    float u1 = o_uniform(rs), u2 = o_uniform(rs);
+    float r = sqrtf(-2.0f * o_logf(u1));
+    float sn, cs;
+    o_sincospif(2.0f * u2, &sn, &cs);
+    return r * cs;
+}
+
+/* First vertex from a beam (sampleFirstBeam, GaussianBeam.cuh:357-418): a beam
+ * uniformly, a lobe of the focal material by its cdf, a distance bin by the
+ * lobe's cdf and a uniform offset in it, then a transverse Gaussian offset of
+ * variance w^2(dz) = (ga + |mu|) / k^2 + dz^2 / ga in the beam's xy base.  The
+ * previous point is one unit back along the beam.  Double arithmetic, the
+ * vertex rounded to float. */
+static void o_gauss_first(const o_scene* S, const o_src* s, o_stream* rs, float x0[3], float x1[3], int* beam)
+{
+    int n = s->n;
+    int l = (int)ceilf(o_uniform(rs) * (float)n) - 1;
+    if (l < 0) l = 0;
+    if (l > n - 1) l = n - 1;
+    *beam = l;
+    int fm = s->gfm[l], M = S->gmix_n[fm];
+    const double* mix = S->gmix + 2 * S->gmix_off[fm];
+    const double* tb = s->gtab + 9 * l;
+    int m = o_cdf_pick(s->gaicdf + (size_t)l * s->gM, M, (double)o_uniform(rs));
+    int b = o_cdf_pick(s->gicdf + ((size_t)l * s->gM + m) * O_GB_BINS, O_GB_BINS, (double)o_uniform(rs));
+    double uo = (double)o_uniform(rs);
+    double d[3], f[3], z[3];
+    for (int i = 0; i < 3; ++i) { d[i] = s->gdir[3 * l + i]; f[i] = s->p[3 * l + i]; }
+    double t = tb[0] + (double)b * tb[2];
+    double step = uo * tb[2];
+    for (int i = 0; i < 3; ++i) z[i] = (f[i] + t * d[i]) + step * d[i];
+    double k = 2.0 * O_PI / S->lambda;
+    double dz = (z[0] - f[0]) * d[0] + (z[1] - f[1]) * d[1] + (z[2] - f[2]) * d[2];
+    double wz = sqrt((s->ga + fabs(mix[2 * m])) / (k * k) + dz * dz / s->ga);
+    double n1 = (double)o_normal(rs), n2 = (double)o_normal(rs);
+    for (int i = 0; i < 3; ++i) {
+        x1[i] = (float)(z[i] + wz * (n1 * tb[3 + i] + n2 * tb[6 + i]));
+        x0[i] = x1[i] - s->gdir[3 * l + i];
+    }
+}
+
+/* Projection distance of p on the line f + t d (MediumInterface.cuh:138-153) */
+static inline double o_gproj(const double p[3], const double f[3], const double d[3])
+{
+    double o[3];
+    for (int i = 0; i < 3; ++i)
+        o[i] = d[i] * d[0] * (p[0] - f[0]) + d[i] * d[1] * (p[1] - f[1]) + d[i] * d[2] * (p[2] - f[2]);
+    return o[0] * d[0] + o[1] * d[1] + o[2] * d[2];
+}
+
+/* P_l(x) of a beam (firstPointProbabilityKernel, GaussianBeam.cuh:420-487): the
+ * bin pdf at x's axial offset times the transverse Gaussian, summed over the
+ * focal material's lobes with their weights, over sigs(x) (box depth in z). */
+static double o_gauss_pfirst(const o_scene* S, const o_src* s, int l, const float x1[3], int m1)
+{
+    int fm = s->gfm[l], M = S->gmix_n[fm];
+    const double* mix = S->gmix + 2 * S->gmix_off[fm];
+    const double* tb = s->gtab + 9 * l;
+    double d[3], f[3], x[3];
+    for (int i = 0; i < 3; ++i) { d[i] = s->gdir[3 * l + i]; f[i] = s->p[3 * l + i]; x[i] = x1[i]; }
+    double dz = o_gproj(x, f, d);
+    double dxy2 = 0.0;
+    for (int i = 0; i < 3; ++i) { double e = f[i] + dz * d[i] - x[i]; dxy2 += e * e; }
+    int zi;
+    if (dz < tb[0]) zi = 0;
+    else if (dz > tb[1]) zi = O_GB_BINS - 1;
+    else { zi = (int)((dz - tb[0]) / tb[2]); if (zi < 0) zi = 0; if (zi > O_GB_BINS - 1) zi = O_GB_BINS - 1; }
+    double k = 2.0 * O_PI / S->lambda;
+    double pdf = 0.0;
+    for (int m = 0; m < M; ++m) {
+        double pz = s->gpdf[((size_t)l * s->gM + m) * O_GB_BINS + zi];
+        double w2 = (s->ga + fabs(mix[2 * m])) / (k * k) + dz * dz / s->ga;
+        double pxy = exp(-dxy2 / (2.0 * w2)) / ((2.0 * w2) * O_PI);
+        pdf += s->gapdf[(size_t)l * s->gM + m] * pz * pxy;
+    }
+    return pdf / (S->sigs_d[m1] * ((double)S->bmax[2] - (double)S->bmin[2]));
+}
+
+/* Second direction at x1 for the path's beam (sampleCdfBuffer, GaussianBeam.cuh:
+ * 636-690): a lobe pair by a running-sum scan whose step back after the loop is
+ * kept, then a vMF direction about the pair's mean (the exact inverse cdf of the
+ * cosine, as for vMF scattering) */
+static void o_gauss_second_dir(const o_scene* S, const o_src* s, int l, const float x1[3], o_stream* rs, float out[3])
+{
+    int M = S->gmix_n[s->gfm[l]], P = M * M;
+    double conv[3 * 64], logC[64], w[64];
+    o_gauss_pairs(S, s, l, x1, conv, logC, w);
+    float u = o_uniform(rs);
+    double cdf = 0.0;
+    int j;
+    for (j = 0; j < P; ++j) {
+        if ((double)u < cdf) break;
+        cdf += w[j];
+    }
+    j--;
+    const double* cj = conv + 3 * j;
+    double kap = sqrt(cj[0] * cj[0] + cj[1] * cj[1] + cj[2] * cj[2]);
+    float cen[3];
+    if (kap < 1e-4) { cen[0] = 0.0f; cen[1] = 0.0f; cen[2] = 1.0f; }
+    else for (int a = 0; a < 3; ++a) cen[a] = (float)(cj[a] / kap);
+    float kf = (float)kap;
+    float v = o_uniform(rs);
+    float c;
+    if (kf < 1e-4f) {
+        c = v * 2.0f - 1.0f;
+    } else {
+        float e2k = (float)exp(-2.0 * (double)kf);
+        c = 1.0f + o_logf(v + (1.0f - v) * e2k) / kf;
+        if (c < -1.0f) c = -1.0f;
+    }
+    o_rotate(S, cen, c, rs, out);
+}
+
+/* p2 factor of beam l for the direction x1 -> x2 (sampleDirectionProbability,
+ * GaussianBeam.cuh:693-753): sum_j w_j exp(conv_j . o + log C_j) */
+static double o_gauss_pw(const o_scene* S, const o_src* s, int l, const float x1[3], const float x2[3])
+{
+    int P = S->gmix_n[s->gfm[l]] * S->gmix_n[s->gfm[l]];
+    double conv[3 * 64], logC[64], w[64];
+    o_gauss_pairs(S, s, l, x1, conv, logC, w);
+    double o[3]; o_dir64(x1, x2, o);
+    double r = 0.0;
+    for (int j = 0; j < P; ++j) r += w[j] * exp(conv[3 * j] * o[0] + conv[3 * j + 1] * o[1] + conv[3 * j + 2] * o[2] + logC[j]);
+    return r;
+}
+
+/* NEE vector of a beam: sqrt of the attenuation along the beam axis from x,
+ * backward for an illumination, forward for a view (throughputFunction,
+ * GaussianBeam.cuh:795-816, 1870-1888) */
+static oc o_gauss_g(const o_scene* S, const o_src* s, int k, const float x[3], int role, uint64_t* steps)
+{
+    float sg = role == 0 ? -1.0f : 1.0f;
+    float df[3] = { sg * s->gdir[3 * k], sg * s->gdir[3 * k + 1], sg * s->gdir[3 * k + 2] };
+    double dd[3] = { df[0], df[1], df[2] };
+    oc g = { sqrt(exp(-o_ray(S, x, df, dd, steps))), 0.0 };
+    return g;
+}
+
+/* Beam -> scatterer pa -> pb amplitude (fGaussianBeam, GaussianBeam.cuh:818-892):
+ * sum over pa's lobes of 2 sinh(sqrt(mu)) e^(log nu) / sqrt(mu), mu = sum (g w0 +
+ * ga d + i k (pa - f))^2, w0 the path direction out of pa (illumination) or into
+ * pa (view, with k negative), log nu = aperture normalisation + log 2 pi + C'. */
+static oc o_gauss_f(const o_scene* S, const o_src* s, int k, const float pa[3], const float pb[3], int m, int role)
+{
+    oc acc = { 0.0, 0.0 };
+    if (m <= 0) return acc;
+    double w0[3];
+    if (role == 0) o_dir64(pa, pb, w0);
+    else o_dir64(pb, pa, w0);
+    double kk = (role == 0 ? 2.0 : -2.0) * O_PI / S->lambda;
+    double x[3] = { pa[0], pa[1], pa[2] };
+    oc T[3]; o_gthroughput(s, k, x, kk, T);
+    double tc = s->gnorm + log(2.0 * O_PI);
+    const double* mix = S->gmix + 2 * S->gmix_off[m];
+    for (int i = 0; i < S->gmix_n[m]; ++i) {
+        oc lnu = { tc + mix[2 * i + 1], 0.0 };
+        oc sm = oc_sqrt(o_gsumsq(mix[2 * i], w0, T));
+        if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) acc.re += 2.0 * exp(lnu.re);
+        else acc = oc_add(acc, oc_div(oc_2sinh(sm, lnu), sm));
+    }
+    return acc;
+}
+
+/* Illumination beam l -> x -> view beam v (fsGaussianBeam, GaussianBeam.cuh:894-999):
+ * the lobe convolved with the illumination throughput, then integrated against the
+ * view's. */
+static oc o_gauss_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, int v, const float xf[3], int m)
+{
+    oc acc = { 0.0, 0.0 };
+    double k = 2.0 * O_PI / S->lambda;
+    double x[3] = { xf[0], xf[1], xf[2] };
+    oc aT[3], bT[3];
+    o_gthroughput(il, l, x, k, aT);
+    for (int i = 0; i < 3; ++i) {
+        bT[i].re = (double)vw->gdir[3 * v + i] * vw->ga;
+        bT[i].im = k * ((double)vw->p[3 * v + i] - x[i]);
+    }
+    double vd[3] = { vw->gdir[3 * v], vw->gdir[3 * v + 1], vw->gdir[3 * v + 2] };
+    double tc = il->gnorm + vw->gnorm + 2.0 * log(2.0 * O_PI);
+    const double* mix = S->gmix + 2 * S->gmix_off[m];
+    double z0[3] = { 0, 0, 0 };
+    for (int i = 0; i < S->gmix_n[m]; ++i) {
+        double gs = mix[2 * i];
+        oc lnu = { tc + mix[2 * i + 1], 0.0 };
+        oc C, sm, c = { 0.0, 0.0 };
+        if (fabs(gs) < 0.000001) {
+            C = oc_sqrt(o_gsumsq(0.0, z0, aT));
+            sm = oc_sqrt(o_gsumsq(0.0, z0, bT));
+        } else {
+            oc g0 = oc_rsqrt(o_gsumsq(gs, vd, aT));
+            g0.re *= gs; g0.im *= gs;
+            /* sqrt(sum (g0 aT + bT)^2), g0 complex */
+            oc q = { 0.0, 0.0 };
+            double wv[3];
+            oc aw = { 0.0, 0.0 };
+            for (int a = 0; a < 3; ++a) {
+                oc e = oc_add(oc_mul(g0, aT[a]), bT[a]);
+                q = oc_add(q, oc_mul(e, e));
+                wv[a] = g0.re * aT[a].re - g0.im * aT[a].im;
+            }
+            sm = oc_sqrt(q);
+            double ra = 1.0 / sqrt(wv[0] * wv[0] + wv[1] * wv[1] + wv[2] * wv[2]);
+            C = oc_sqrt(o_gsumsq(gs * ra, wv, aT));
+            for (int a = 0; a < 3; ++a) { aw.re += aT[a].re * wv[a]; aw.im += aT[a].im * wv[a]; }
+            c = oc_mul(g0, aw);
+            c.re *= -ra; c.im *= -ra;
+        }
+        int sbig = fabs(sm.re) > 0.0001 || fabs(sm.im) > 0.0001;
+        int cbig = fabs(C.re) > 0.0001 || fabs(C.im) > 0.0001;
+        oc cl = oc_add(c, lnu);
+        if (sbig && cbig) {
+            acc = oc_add(acc, oc_div(oc_2sinh(oc_add(C, sm), cl), oc_mul(C, sm)));
+        } else if (!sbig && !cbig) {
+            oc e = oc_exp(cl);
+            acc.re += 4.0 * e.re; acc.im += 4.0 * e.im;
+        } else if (!sbig) {
+            oc e = oc_div(oc_2sinh(C, cl), C);
+            acc.re += 2.0 * e.re; acc.im += 2.0 * e.im;
+        } else {
+            oc e = oc_div(oc_2sinh(sm, lnu), sm);
+            acc.re += 2.0 * e.re; acc.im += 2.0 * e.im;
+        }
+    }
+    return acc;
+}
+
+/* Scene tables of the beams (GaussianBeam.cuh:1029-1228, 1284-1566): the
+ * requirements, the mean view direction, and per illumination beam its focal
+ * material, axial range over the box, xy base, the distance-bin pdf and cdf of
+ * each lobe (attenuation at the bin point along the first beam's backward
+ * direction, as the reference's attenuationDirection call with one direction
+ * computes it, over w^2) and the lobe weights. */
+static int o_prep_gauss(o_scene* S)
+{
+    o_src* il = &S->src[0];
+    o_src* vw = &S->src[1];
+    if (il->type != SSTMC_SOURCE_GAUSSIANBEAM || vw->type != SSTMC_SOURCE_GAUSSIANBEAM) return SSTMC_NOT_SUPPORTED;
+    if (S->correlation || S->cbs || S->dims != 3) return SSTMC_NOT_SUPPORTED;
+    for (int m = 0; m < OM; ++m)
+        if (S->scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && S->scat_type[m] != SSTMC_SCATTERING_VMF_MIXTURE)
+            return SSTMC_NOT_SUPPORTED;
+    double mv[3] = { 0, 0, 0 }, inv = 1.0 / vw->n;
+    for (int v = 0; v < vw->n; ++v) for (int a = 0; a < 3; ++a) mv[a] = mv[a] + inv * (double)vw->gdir[3 * v + a];
+    double r = sqrt(mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]);
+    if (r < 0.0001) return SSTMC_NOT_SUPPORTED;   /* the reference draws a random direction here */
+    for (int a = 0; a < 3; ++a) S->gmean[a] = mv[a] * (1.0 / r);
+    int n = il->n, gM = 0;
+    il->gfm = malloc(sizeof(int) * n);
+    il->gtab = malloc(sizeof(double) * 9 * n);
+    if (!il->gfm || !il->gtab) return SSTMC_ALLOCATION_ERROR;
+    for (int l = 0; l < n; ++l) {
+        const float* f = il->p + 3 * l;
+        int fm = o_inside(S, f) ? S->grid[o_cell(S, f)] : 0;
+        if (fm <= 0 || S->gmix_n[fm] < 1 || S->gmix_n[fm] > 8) return SSTMC_NOT_SUPPORTED;
+        il->gfm[l] = fm;
+        if (S->gmix_n[fm] > gM) gM = S->gmix_n[fm];
+    }
+    il->gM = gM;
+    size_t nb = (size_t)n * gM * O_GB_BINS;
+    il->gpdf = calloc(nb, sizeof(double)); il->gicdf = calloc(nb, sizeof(double));
+    il->gapdf = calloc((size_t)n * gM, sizeof(double)); il->gaicdf = calloc((size_t)n * gM, sizeof(double));
+    if (!il->gpdf || !il->gicdf || !il->gapdf || !il->gaicdf) return SSTMC_ALLOCATION_ERROR;
+    double k = 2.0 * O_PI / S->lambda;
+    double back0[3] = { -(double)il->gdir[0], -(double)il->gdir[1], -(double)il->gdir[2] };
+    for (int l = 0; l < n; ++l) {
+        double d[3], f[3];
+        for (int i = 0; i < 3; ++i) { d[i] = il->gdir[3 * l + i]; f[i] = il->p[3 * l + i]; }
+        double* tb = il->gtab + 9 * l;
+        /* projectBoxToLine, MediumInterface.cuh:156-200 */
+        double tmin = 0, tmax = 0;
+        for (int c = 0; c < 8; ++c) {
+            double cp[3] = { (c & 1) ? S->axd[0][S->n[0] - 1] : S->axd[0][0], (c & 2) ? S->axd[1][S->n[1] - 1] : S->axd[1][0],
+                             (c & 4) ? S->axd[2][S->n[2] - 1] : S->axd[2][0] };
+            double t = o_gproj(cp, f, d);
+            if (c == 0 || t < tmin) tmin = t;
+            if (c == 0 || t > tmax) tmax = t;
+        }
+        tb[0] = tmin; tb[1] = tmax; tb[2] = (tmax - tmin) / (double)O_GB_BINS;
+        /* orthogonalBase, VectorType.cuh:293-314 */
+        if (fabs(1.0 - fabs(d[2])) <= 1e-12) {
+            tb[3] = 1; tb[4] = 0; tb[5] = 0; tb[6] = 0; tb[7] = 1; tb[8] = 0;
+        } else {
+            double b0[3] = { -d[1], d[0], 0.0 };
+            double rb = sqrt(b0[0] * b0[0] + b0[1] * b0[1]);
+            b0[0] /= rb; b0[1] /= rb;
+            tb[3] = b0[0]; tb[4] = b0[1]; tb[5] = 0.0;
+            tb[6] = b0[1] * d[2] - b0[2] * d[1];
+            tb[7] = b0[2] * d[0] - b0[0] * d[2];
+            tb[8] = b0[0] * d[1] - b0[1] * d[0];
+        }
+        int fm = il->gfm[l], M = S->gmix_n[fm];
+        const double* mix = S->gmix + 2 * S->gmix_off[fm];
+        for (int b = 0; b < O_GB_BINS; ++b) {
+            double t = tmin + (double)b * tb[2];
+            double z[3] = { f[0] + t * d[0], f[1] + t * d[1], f[2] + t * d[2] };
+            double T = exp(-o_tau64(S, z, back0));
+            double dz = (z[0] - f[0]) * d[0] + (z[1] - f[1]) * d[1] + (z[2] - f[2]) * d[2];
+            for (int m = 0; m < M; ++m)
+                il->gpdf[((size_t)l * gM + m) * O_GB_BINS + b] = T / ((il->ga + fabs(mix[2 * m])) / (k * k) + dz * dz / il->ga);
+        }
+        for (int m = 0; m < M; ++m) {
+            double* pdf = il->gpdf + ((size_t)l * gM + m) * O_GB_BINS;
+            double* cdf = il->gicdf + ((size_t)l * gM + m) * O_GB_BINS;
+            double run = 0.0;
+            for (int b = 0; b < O_GB_BINS; ++b) { cdf[b] = run; run += pdf[b]; }
+            double tot = pdf[O_GB_BINS - 1] + cdf[O_GB_BINS - 1];
+            for (int b = 0; b < O_GB_BINS; ++b) { pdf[b] *= (double)(O_GB_BINS - 1) / tot; cdf[b] /= tot; }
+        }
+        /* lobe weights, alphaPdfIcdfKernel (GaussianBeam.cuh:254-295) */
+        double* ap = il->gapdf + (size_t)l * gM;
+        double* ac = il->gaicdf + (size_t)l * gM;
+        double asum = 0.0;
+        for (int m = 0; m < M; ++m) {
+            double kap = fabs(mix[2 * m]);
+            double ln = kap < 1e-5 ? -log(4.0 * O_PI) : log(kap) - (kap > 10.0 ? log(2.0 * O_PI) * kap : log(4.0 * O_PI * sinh(kap)));
+            ap[m] = exp(mix[2 * m + 1] + ln);
+            asum += ap[m];
+        }
+        for (int m = 0; m < M; ++m) ap[m] /= asum;
+        double run = 0.0;
+        for (int m = 0; m < M; ++m) { ac[m] = run; run += ap[m]; }
+    }
+    return SSTMC_NO_ERROR;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1168,11 +1690,20 @@ static int o_walk(const o_scene* S, uint64_t seed, uint32_t pid, int u1side, o_v
     V->B = 0;
     uint32_t att;
     o_stream rs;
+    int beam = 0;
+    const int gauss = first->type == SSTMC_SOURCE_GAUSSIANBEAM;
     for (att = 0; att < O_MAX_ATTEMPTS; ++att) {
         o_stream_init(&rs, seed, pid, 1u, O_PURPOSE_WALK | (att << 8));
-        o_sample_source(S, first, &rs, x0, d0);
-        int e = o_woodcock(S, x0, d0, &rs, x1, &m1);
-        if (e) return e;
+        if (gauss) {
+            /* the beam places x1 itself; a point outside the medium is a miss
+             * (getMaterialInfo, GaussianBeam.cuh:1617-1618) */
+            o_gauss_first(S, first, &rs, x0, x1, &beam);
+            m1 = o_inside(S, x1) ? S->grid[o_cell(S, x1)] : 0;
+        } else {
+            o_sample_source(S, first, &rs, x0, d0);
+            int e = o_woodcock(S, x0, d0, &rs, x1, &m1);
+            if (e) return e;
+        }
         if (m1 > 0) break;
         (*misses)++;
     }
@@ -1188,9 +1719,17 @@ static int o_walk(const o_scene* S, uint64_t seed, uint32_t pid, int u1side, o_v
         const float* cur = V->x + 3 * (b - 1);
         int mb = V->m[b - 1];
         o_stream_init(&rs, seed, pid, b + 1, O_PURPOSE_WALK);
-        float diff[3] = { cur[0] - prev[0], cur[1] - prev[1], cur[2] - prev[2] };
-        float din[3]; o_normalize32(S->dims, diff, din);
-        float nd[3]; o_sample_direction(S, mb, din, &rs, nd);
+        float nd[3];
+        if (gauss && b == 1) {
+            /* the beam samples the second direction (GaussianBeam.cuh:1687-1780):
+             * uniform with isotropic scattering, else from its lobe pairs */
+            if (S->iso_all) o_random_direction(3, &rs, nd);
+            else o_gauss_second_dir(S, first, beam, cur, &rs, nd);
+        } else {
+            float diff[3] = { cur[0] - prev[0], cur[1] - prev[1], cur[2] - prev[2] };
+            float din[3]; o_normalize32(S->dims, diff, din);
+            o_sample_direction(S, mb, din, &rs, nd);
+        }
         float xn[3]; int mn = 0;
         int e = o_woodcock(S, cur, nd, &rs, xn, &mn);
         if (e) return e;
@@ -1378,6 +1917,12 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
         double x12[3]; o_dir64(x1, x2, x12);
         double p2 = 0;
         for (int l = 0; l < Nl; ++l) {
+            if (il->type == SSTMC_SOURCE_GAUSSIANBEAM) {
+                /* a zero product is replaced by 1e20 (GaussianBeam.cuh:745-751) */
+                double q = W->P1[l] * (S->iso_all ? O_ISO_PDF3 : o_gauss_pw(S, il, l, x1, x2));
+                p2 += q == 0.0 ? 1e20 : q;
+                continue;
+            }
             double in[3]; o_src_dir(il, l, x1, 0, in);
             p2 += W->P1[l] * o_pdf(S, m1, o_dot(in, x12));
         }
@@ -1783,3 +2328,59 @@ int32_t oracle_tick_positions(const sstmc_config* cfg, uint64_t seed, uint32_t p
 float oracle_logf(float x) { return o_logf(x); }
 void oracle_sincospif(float x, float* s, float* c) { o_sincospif(x, s, c); }
 void oracle_philox(const uint32_t key[2], const uint32_t ctr[4], uint32_t out[4]) { o_philox(key, ctr, out); }
+
+int32_t oracle_gauss_terms(const sstmc_config* cfg, int32_t l, int32_t v, const float* x1, int32_t m1,
+                           const float* x2, double* out)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (!err && !S.gauss) err = SSTMC_INVALID_CONFIG;
+    if (!err && (l < 0 || l >= S.src[0].n || v < 0 || v >= S.src[1].n || m1 <= 0 || m1 >= OM)) err = SSTMC_INVALID_CONFIG;
+    if (!err) {
+        const o_src *il = &S.src[0], *vw = &S.src[1];
+        uint64_t st = 0;
+        out[0] = o_gauss_pfirst(&S, il, l, x1, m1);
+        out[1] = S.iso_all ? O_ISO_PDF3 : o_gauss_pw(&S, il, l, x1, x2);
+        oc f = o_gauss_f(&S, il, l, x1, x2, m1, 0);
+        out[2] = f.re; out[3] = f.im;
+        f = o_gauss_f(&S, vw, v, x1, x2, m1, 1);
+        out[4] = f.re; out[5] = f.im;
+        f = o_gauss_fs(&S, il, l, vw, v, x1, m1);
+        out[6] = f.re; out[7] = f.im;
+        out[8] = o_gauss_g(&S, il, l, x1, 0, &st).re;
+        out[9] = o_gauss_g(&S, vw, v, x1, 1, &st).re;
+    }
+    o_free_scene(&S);
+    return err;
+}
+
+int32_t oracle_gauss_sample(const sstmc_config* cfg, uint64_t seed, uint32_t n, const float* x1_fixed, int32_t beam_fixed,
+                            float* xyz, int32_t* mat, int32_t* beam, float* dir)
+{
+    o_scene S;
+    int err = o_build_scene(cfg, &S);
+    if (!err && !S.gauss) err = SSTMC_INVALID_CONFIG;
+    if (!err) {
+        const o_src* il = &S.src[0];
+        for (uint32_t i = 0; i < n; ++i) {
+            o_stream rs;
+            o_stream_init(&rs, seed, i, 1u, O_PURPOSE_WALK);
+            float x0[3], x1[3], d[3];
+            int b = 0;
+            if (x1_fixed) {
+                for (int a = 0; a < 3; ++a) x1[a] = x1_fixed[a];
+                b = beam_fixed < 0 ? 0 : (beam_fixed >= il->n ? il->n - 1 : beam_fixed);
+            } else {
+                o_gauss_first(&S, il, &rs, x0, x1, &b);
+            }
+            int m = o_inside(&S, x1) ? S.grid[o_cell(&S, x1)] : 0;
+            o_stream_init(&rs, seed, i, 2u, O_PURPOSE_WALK);
+            if (S.iso_all) o_random_direction(3, &rs, d);
+            else o_gauss_second_dir(&S, il, b, x1, &rs, d);
+            for (int a = 0; a < 3; ++a) { xyz[3 * i + a] = x1[a]; dir[3 * i + a] = d[a]; }
+            mat[i] = m; beam[i] = b;
+        }
+    }
+    o_free_scene(&S);
+    return err;
+}

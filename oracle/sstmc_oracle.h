@@ -54,6 +54,20 @@ int32_t oracle_sample_cos(const sstmc_config* cfg, int32_t m, uint64_t seed, uin
  * x (isForcedInsideBin), -1 when there is none. */
 int32_t oracle_tick_positions(const sstmc_config* cfg, uint64_t seed, uint32_t pid, uint32_t b, const float* x,
                               int32_t m, float* xt, float* w, int32_t* r);
+/* Gaussian beams (3D): the source terms of illumination beam l and view beam
+ * v at scatterer x1 (material m1) with the path on to x2:
+ * out[0] P_l(x1), out[1] the second-direction density p_l(x1 -> x2),
+ * out[2..3] f_l(x1 -> x2), out[4..5] f_v(x2 -> x1) (x1 the view's vertex),
+ * out[6..7] fs(l, v, x1), out[8] g_l(x1), out[9] g_v(x1). */
+int32_t oracle_gauss_terms(const sstmc_config* cfg, int32_t l, int32_t v, const float* x1, int32_t m1,
+                           const float* x2, double* out);
+/* n first vertices of beam-sampled paths (misses included: material 0) and,
+ * per vertex, a second direction drawn for its beam at it: xyz[n x 3],
+ * mat[n], beam[n], dir[n x 3].  x1_fixed (may be NULL): every draw at this
+ * vertex for beam beam_fixed (the second direction only). */
+int32_t oracle_gauss_sample(const sstmc_config* cfg, uint64_t seed, uint32_t n, const float* x1_fixed, int32_t beam_fixed,
+                            float* xyz, int32_t* mat, int32_t* beam, float* dir);
+
 /* Portable FP32 math of the decision path, for bit-level tests. */
 float oracle_logf(float x);
 void oracle_sincospif(float x, float* s, float* c);

@@ -103,6 +103,7 @@ def _declare_objects(lib: C.CDLL) -> None:
         "sstmc_medium_destroy": [vp],
         "sstmc_source_create_point": [vp, i32, dp, u32, i32, C.POINTER(vp)],
         "sstmc_source_create_far_field": [vp, i32, dp, u32, C.POINTER(vp)],
+        "sstmc_source_create_gaussian_beam": [vp, i32, dp, dp, u32, C.c_double, C.POINTER(vp)],
         "sstmc_source_size": [vp, up],
         "sstmc_source_destroy": [vp],
         "sstmc_sampler_create_temporal": [vp, vp, vp, vp, vp, dp, u32, i32, i32, C.POINTER(vp)],

@@ -64,6 +64,8 @@ class SourceCfg(C.Structure):
         ("count", C.c_uint32),
         ("xyz", _dp),
         ("is_area_source", C.c_int32),
+        ("focal_direction", _dp),
+        ("aperture", C.c_double),
     ]
 
 
@@ -178,7 +180,19 @@ def _source(cfg: Dict[str, Any], name: str, dims: int, keep: list, required: boo
         s.type = SOURCE_POINT
         s.is_area_source = 1 if block.get("isAreaSource", False) else 0
     elif ty == "GaussianBeam":
-        raise ConfigError(f"{name}: GaussianBeam sources are not supported by this build")
+        # focalPoint, focalDirection (one per focal point) and a scalar aperture
+        # (MatlabInterface.cu:1161-1200)
+        if "focalPoint" not in block or "focalDirection" not in block or "aperture" not in block:
+            raise ConfigError(f"{name}: GaussianBeam needs focalPoint, focalDirection and aperture")
+        xyz = _vec3(block["focalPoint"], None, dims, f"{name}.focalPoint")
+        fd = _vec3(block["focalDirection"], len(xyz) // 3, dims, f"{name}.focalDirection")
+        ap = _arr(block["aperture"])
+        if ap.size != 1:
+            raise ConfigError(f"{name}.aperture must be a scalar")
+        keep.append(fd)
+        s.type = SOURCE_GAUSSIANBEAM
+        s.focal_direction = fd.ctypes.data_as(_dp)
+        s.aperture = float(ap[0])
     else:
         raise ConfigError(f"Unsupported source type {ty!r}. Available {name} types are PointSource, FarField and GaussianBeam.")
     keep.append(xyz)

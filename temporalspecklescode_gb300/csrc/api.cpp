@@ -319,6 +319,15 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     const size_t smem = trace_smem_bytes(S.Nt, T.slots, threads);
     const int per_sm = occupancy_blocks(S.dev, threads, smem);
     const int blocks = std::max(1, std::min((int)((n + 3) / 4), sms * std::max(1, per_sm)));
+    if (S.dev.gauss) {
+        // Gaussian beams: every row of a path in one warp (gauss_trace_kernel)
+        T.pass0 = 1; T.views = 1;
+        T.v0 = 0; T.vn = S.Nv; T.t0 = 0; T.tn = S.Nt;
+        e = launch_gauss_trace(S.dev, T, threads, stream);
+        if (e) return e;
+        launches++;
+        return SSTMC_NO_ERROR;
+    }
     bool moving_any = false;
     for (int m : S.materials_present) moving_any = moving_any || S.dev.moving[m] != 0;
     if (use_view_kernel() && !S.cfg_copy.is_cbs && view_kernel_covers(S.dev, &moving_any)) {

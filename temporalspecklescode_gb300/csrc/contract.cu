@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "contract.h"
+#include "gauss.cuh"
 #include "nee.cuh"
 
 namespace sstmc {
@@ -660,9 +661,66 @@ int launch_gemm(const GemmParams& G, cudaStream_t stream)
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
 }
 
+// Gaussian beams: V[t][v][l] += sum_p a[p][t][l] b[p][t][v] fs(l, v, x_p,t)
+// (threePointFunctionSingle, GaussianBeam.cuh:894-999).  fs depends on the
+// scatterer's position, so it is evaluated per (path, l, v) -- once for a
+// static vertex, per tick for a moving one with the temporal amplitude -- in
+// FP64 (gauss.cuh), and the products are summed in FP64.  Thread per (l, v) of
+// a 16 x 16 tile, a chunk of kSsT ticks and a range of paths.
+__global__ void __launch_bounds__(256) gauss_ss_kernel(const __grid_constant__ DevScene S, const SsParams G)
+{
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const int l = blockIdx.x * kSsL + threadIdx.x % kSsL, v = blockIdx.y * kSsV + threadIdx.x / kSsL;
+    const int tchunks = (Nt + kSsT - 1) / kSsT;
+    const int t0 = (blockIdx.z % tchunks) * kSsT;
+    const int tn = min(kSsT, Nt - t0);
+    const int ks = blockIdx.z / tchunks;
+    const int kb = ks * G.kchunk, ke = min(G.K, kb + G.kchunk);
+    if (l >= Nl || v >= Nv) return;
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    double ar[kSsT], ai[kSsT];
+#pragma unroll
+    for (int i = 0; i < kSsT; ++i) { ar[i] = 0.0; ai[i] = 0.0; }
+    for (int p = kb; p < ke; ++p) {
+        const int m = G.m1[p];
+        if (m <= 0 || m >= kMat) continue;
+        const bool stat = !S.temporal_amp || !S.moving[m];
+        CD f0{ 0.0, 0.0 };
+        if (stat) f0 = gauss_fs(S, il, l, vw, v, V3{ G.x1[3 * p], G.x1[3 * p + 1], G.x1[3 * p + 2] }, m);
+#pragma unroll
+        for (int i = 0; i < kSsT; ++i) {
+            if (i >= tn) break;
+            const int t = t0 + i;
+            CD f = f0;
+            if (!stat) {
+                const float* xt = G.x1t + ((size_t)p * Nt + t) * 3;
+                f = gauss_fs(S, il, l, vw, v, V3{ xt[0], xt[1], xt[2] }, m);
+            }
+            const float2 a = G.a[((size_t)p * Nt + t) * Nl + l];
+            const float2 b = G.b[((size_t)p * Nt + t) * Nv + v];
+            const double abr = (double)a.x * b.x - (double)a.y * b.y, abi = (double)a.x * b.y + (double)a.y * b.x;
+            ar[i] += abr * f.re - abi * f.im;
+            ai[i] += abr * f.im + abi * f.re;
+        }
+    }
+    for (int i = 0; i < tn; ++i) {
+        const size_t o = ((size_t)(t0 + i) * Nv + v) * Nl + l;
+        atomicAdd(&G.V[o].x, ar[i]);
+        atomicAdd(&G.V[o].y, ai[i]);
+    }
+}
+
 int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
 {
     if (G.K <= 0) return SSTMC_NO_ERROR;
+    if (S.gauss) {
+        const int tchunks = (S.Nt + kSsT - 1) / kSsT;
+        const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
+        dim3 grid((S.src[0].n + kSsL - 1) / kSsL, (S.src[1].n + kSsV - 1) / kSsV, tchunks * ksplit);
+        gauss_ss_kernel<<<grid, 256, 0, stream>>>(S, G);
+        return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
+    }
     if (S.correlation && S.sym && S.all_static_corr && !S.has_amp64) {
         // two resident blocks per SM: split the paths so the grid fills them
         int dev = 0, sms = 0;

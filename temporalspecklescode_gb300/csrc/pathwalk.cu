@@ -14,7 +14,7 @@
 #include <algorithm>
 
 #include "pathwalk.h"
-#include "walk.cuh"
+#include "gauss.cuh"
 
 namespace sstmc {
 
@@ -62,7 +62,9 @@ constexpr int kCount = 0, kWrite = 1, kSlots = 2;
 // and the persistent grid's size
 constexpr int kWalkBlocksPerSM = 7;
 
-template <int MODE, bool VMF>
+// GB: Gaussian-beam illumination (3D): the beam places the first vertex and
+// samples the second direction (gauss.cuh)
+template <int MODE, bool VMF, bool GB>
 __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
     constexpr bool WRITE = MODE == kWrite;
@@ -73,6 +75,7 @@ __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __gri
     uint32_t q = 0, pid = 0, att = 0, b = 1, B = 0, h = 2166136261u;
     V3 prev{ 0.f, 0.f, 0.f }, cur{ 0.f, 0.f, 0.f };
     int mcur = 0;
+    int beam = 0;   // GB: the beam of the path's first vertex
     float4* out = nullptr;
     uint32_t o0 = 0;   // vertex index stored at out[0]
     const DevSource* fsrc = &S.src[0];
@@ -131,17 +134,36 @@ __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __gri
         Stream rs;
         rs.init(W.seed, pid, b, kPurposeWalk | (b == 1 ? att << 8 : 0u));
         rs.prime2();
-        V3 o, d;
-        if (b == 1) {
-            sample_source(S, *fsrc, rs, o, d);
-        } else {
-            const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
-            d = sample_direction<VMF>(S, mcur, din, rs);
-            o = cur;
-        }
-        V3 xn;
+        V3 o, d, xn;
         int mn = 0;
-        bool ok = woodcock(S, o, d, rs, xn, mn);
+        bool ok;
+        if constexpr (GB) {
+            if (b == 1) {
+                // the beam places x1; a point outside the medium is a miss
+                gauss_first(S, *fsrc, rs, o, xn, beam);
+                mn = inside(S, xn) ? material_at(S, xn) : 0;
+                ok = true;
+            } else {
+                if (b == 2) {
+                    // uniform with isotropic scattering, else from the beam's lobe pairs
+                    d = S.iso_all ? random_direction(3, rs) : gauss_second_dir(S, *fsrc, beam, cur, rs);
+                } else {
+                    const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
+                    d = sample_direction<VMF>(S, mcur, din, rs);
+                }
+                o = cur;
+                ok = woodcock(S, o, d, rs, xn, mn);
+            }
+        } else {
+            if (b == 1) {
+                sample_source(S, *fsrc, rs, o, d);
+            } else {
+                const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
+                d = sample_direction<VMF>(S, mcur, din, rs);
+                o = cur;
+            }
+            ok = woodcock(S, o, d, rs, xn, mn);
+        }
         bool done = !ok;
         if (ok) {
             if (b == 1) {
@@ -268,18 +290,23 @@ static int launch_scan(const WalkParams& W, cudaStream_t stream)
 // the scene has vMF materials in 3D (their sampler tables are uploaded)
 static bool has_vmf(const DevScene& S) { return S.vmf_pf != nullptr; }
 
+template <int MODE>
+static void walk_launch(const DevScene& S, const WalkParams& W, int blocks, cudaStream_t stream)
+{
+    if (S.gauss) walk_kernel<MODE, true, true><<<blocks, 128, 0, stream>>>(S, W);
+    else if (has_vmf(S)) walk_kernel<MODE, true, false><<<blocks, 128, 0, stream>>>(S, W);
+    else walk_kernel<MODE, false, false><<<blocks, 128, 0, stream>>>(S, W);
+}
+
 int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
-    const int threads = 128;
     if (cudaMemsetAsync(W.next, 0, 2 * sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     if (W.slots) {
         if (cudaMemsetAsync(W.list_count, 0, sizeof(uint32_t), stream) != cudaSuccess
             || cudaMemsetAsync(W.ovf_count, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
-        if (has_vmf(S)) walk_kernel<kSlots, true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
-        else walk_kernel<kSlots, false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+        walk_launch<kSlots>(S, W, walk_blocks(W.paths), stream);
     } else {
-        if (has_vmf(S)) walk_kernel<kCount, true><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
-        else walk_kernel<kCount, false><<<walk_blocks(W.paths), threads, 0, stream>>>(S, W);
+        walk_launch<kCount>(S, W, walk_blocks(W.paths), stream);
     }
     if (cudaGetLastError() != cudaSuccess) return SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
     return launch_scan(W, stream);
@@ -303,13 +330,11 @@ int launch_walk_compact(const WalkParams& W, cudaStream_t stream)
 
 int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
-    const int threads = 128;
     WalkParams Wn = W;
     Wn.next = W.next + 1;   // the write pass draws from the second counter (zeroed with the first)
     const uint32_t pool = W.list ? W.list_n : W.paths;
     if (pool == 0) return SSTMC_NO_ERROR;
-    if (has_vmf(S)) walk_kernel<kWrite, true><<<walk_blocks(pool), threads, 0, stream>>>(S, Wn);
-    else walk_kernel<kWrite, false><<<walk_blocks(pool), threads, 0, stream>>>(S, Wn);
+    walk_launch<kWrite>(S, Wn, walk_blocks(pool), stream);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR_HetroMedium_heterogeneousSampleKernel;
 }
 

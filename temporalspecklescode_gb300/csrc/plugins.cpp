@@ -59,6 +59,8 @@ struct sstmc_source {
     int32_t type = SSTMC_SOURCE_NONE, connection = SSTMC_CONNECTION_ILLUMINATION, is_area = 0;
     uint32_t dims = 3;
     std::vector<double> xyz;
+    std::vector<double> dir;   // GaussianBeam: focal directions
+    double aperture = 0.0;
 };
 
 struct sstmc_sampler {
@@ -152,6 +154,10 @@ void source_cfg(const sstmc_source* s, sstmc_source_cfg* c)
     c->count = (uint32_t)(s->xyz.size() / 3);
     c->xyz = s->xyz.data();
     c->is_area_source = s->is_area;
+    if (s->type == SSTMC_SOURCE_GAUSSIANBEAM) {
+        c->focal_direction = s->dir.data();
+        c->aperture = s->aperture;
+    }
 }
 
 int32_t check_connection(const sstmc_source* s, int32_t want, const char* role)
@@ -318,6 +324,22 @@ int32_t sstmc_source_create_far_field(const sstmc_simulation* sim, int32_t conne
 {
     if (!sim) return SSTMC_INVALID_HANDLE;
     return make_source(SSTMC_SOURCE_FARFIELD, connection, xyz, count, 0, sim->dims, out);
+}
+
+int32_t sstmc_source_create_gaussian_beam(const sstmc_simulation* sim, int32_t connection, const double* focal_points,
+                                          const double* focal_directions, uint32_t count, double aperture, sstmc_source** out)
+{
+    if (!sim) return SSTMC_INVALID_HANDLE;
+    if (!focal_directions || count == 0 || !finite_all(focal_directions, (size_t)3 * count))
+        return invalid("a Gaussian beam needs a finite focal direction per focal point");
+    if (!(aperture > 0.0) || !std::isfinite(aperture)) return invalid("the Gaussian-beam aperture must be positive");
+    const int32_t e = make_source(SSTMC_SOURCE_GAUSSIANBEAM, connection, focal_points, count, 0, sim->dims, out);
+    if (e) return e;
+    (*out)->dir.assign(focal_directions, focal_directions + (size_t)3 * count);
+    if (sim->dims == 2)
+        for (uint32_t i = 0; i < count; ++i) (*out)->dir[3 * i + 2] = 0.0;
+    (*out)->aperture = aperture;
+    return SSTMC_NO_ERROR;
 }
 
 int32_t sstmc_source_size(const sstmc_source* s, uint32_t* count)

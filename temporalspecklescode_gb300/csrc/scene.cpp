@@ -108,7 +108,22 @@ int prep_source(Scene::HostSource* s, const sstmc_source_cfg* c, int dims, const
     if (c->type == SSTMC_SOURCE_NONE) { s->n = 0; return SSTMC_NO_ERROR; }
     if (c->count == 0 || c->xyz == nullptr) return SSTMC_INVALID_CONFIG;
     if (c->type == SSTMC_SOURCE_FARFIELD) return prep_farfield(s, c, dims, bmin, bmax);
-    if (c->type != SSTMC_SOURCE_POINT) return SSTMC_NOT_SUPPORTED;
+    if (c->type == SSTMC_SOURCE_GAUSSIANBEAM) {
+        // focal points in p, beam directions as given, ga = 1 / aperture^2
+        // (GaussianBeam.cuh:1056-1068); the tables follow in prep_gauss
+        if (dims != 3) return SSTMC_NOT_SUPPORTED;
+        if (!c->focal_direction || !(c->aperture > 0.0) || !std::isfinite(c->aperture)) return SSTMC_INVALID_CONFIG;
+        s->gdir.resize(3 * s->n);
+        for (int k = 0; k < 3 * s->n; ++k) s->gdir[k] = (float)c->focal_direction[k];
+        for (int k = 0; k < s->n; ++k) {   // a beam needs a direction
+            const float* d = s->gdir.data() + 3 * k;
+            if (!(d[0] != 0.0f || d[1] != 0.0f || d[2] != 0.0f) || !std::isfinite(d[0]) || !std::isfinite(d[1]) || !std::isfinite(d[2]))
+                return SSTMC_INVALID_CONFIG;
+        }
+        s->ga = 1.0 / (c->aperture * c->aperture);
+    } else if (c->type != SSTMC_SOURCE_POINT) {
+        return SSTMC_NOT_SUPPORTED;
+    }
     s->p.assign(3 * s->n, 0.f);
     for (int k = 0; k < s->n; ++k) {
         s->p[3 * k] = (float)c->xyz[3 * k];
@@ -202,6 +217,177 @@ static void vmf_tables(const double* mu, const double* c, const double* alpha, u
     }
 }
 
+// FP64 optical depth from o along d to the box edge, the parametric traversal
+// of the walk (HeterogeneousMedium.cuh:386-573) in double: the attenuation of
+// the Gaussian beams' distance bins, computed once per scene.
+static double tau64_host(const Scene* S, const double o[3], const double d[3])
+{
+    const int D = S->dims;
+    const DevScene& G = S->dev;
+    for (int i = 0; i < D; ++i)
+        if (!(o[i] >= (double)S->ax[i].front() && o[i] <= (double)S->ax[i].back())) return 0.0;
+    double inv[3] = { 0, 0, 0 };
+    int sg[3] = { 1, 1, 1 }, bin[3] = { 0, 0, 0 }, n[3] = { 0, 0, 0 };
+    for (int i = 0; i < D; ++i) {
+        n[i] = (int)S->ax[i].size();
+        inv[i] = std::fabs(d[i]) < 1e-12 ? (d[i] >= 0.0 ? 1e12 : -1e12) : 1.0 / d[i];
+        sg[i] = d[i] < 0.0 ? -1 : 1;
+        int lo = 0, hi = n[i];
+        while (lo < hi) { const int mid = (lo + hi) >> 1; if ((double)S->ax[i][mid] <= o[i]) lo = mid + 1; else hi = mid; }
+        int c = lo - 1;
+        c = c < 0 ? 0 : (c > n[i] - 2 ? n[i] - 2 : c);
+        bin[i] = c;
+    }
+    double t = 0.0, acc = 0.0;
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+        double tn[3] = { 0, 0, 0 };
+        for (int i = 0; i < D; ++i) tn[i] = ((double)S->ax[i][bin[i] + (sg[i] > 0 ? 1 : 0)] - o[i]) * inv[i];
+        int a;
+        if (D == 2) a = tn[0] < tn[1] ? 0 : 1;
+        else a = (tn[0] < tn[1] && tn[0] < tn[2]) ? 0 : (tn[1] < tn[2] ? 1 : 2);
+        size_t idx = (size_t)bin[0] + (size_t)bin[1] * (n[0] - 1);
+        if (D == 3) idx += (size_t)bin[2] * (n[0] - 1) * (n[1] - 1);
+        const double seg = tn[a] - t;
+        if (seg > 0) acc += seg * (double)G.sigt[S->grid[idx]];
+        if (tn[a] > t) t = tn[a];
+        if ((sg[a] < 0 && bin[a] == 0) || (sg[a] > 0 && bin[a] == n[a] - 2)) break;
+        bin[a] += sg[a];
+    }
+    return acc;
+}
+
+// Projection distance of p on the line f + t d (MediumInterface.cuh:138-153)
+static double gproj(const double p[3], const double f[3], const double d[3])
+{
+    double o[3];
+    for (int i = 0; i < 3; ++i)
+        o[i] = d[i] * d[0] * (p[0] - f[0]) + d[i] * d[1] * (p[1] - f[1]) + d[i] * d[2] * (p[2] - f[2]);
+    return o[0] * d[0] + o[1] * d[1] + o[2] * d[2];
+}
+
+// Gaussian-beam scene tables (GaussianBeam.cuh:1029-1228, 1284-1566).
+// Requirements (as the reference, or refused where it is undefined): 3D, the
+// field sampler without CBS, illumination and view both GaussianBeam, every
+// defined material a vMF mixture (of at most 8 lobes), each focal point inside
+// the medium in a vMF material, a mean view direction of norm >= 1e-4 (the
+// reference draws a random one below).  Per illumination beam: its focal
+// material, the axial range [tmin, tmax] of the box on the beam line, the xy
+// base, per lobe of the focal material the pdf and exclusive cdf of 1000
+// distance bins, attenuation at the bin point over the squared beam width
+// (T / ((ga + |mu|) / k^2 + dz^2 / ga)), normalised as the reference does (pdf
+// times (B - 1) / sum), and the lobe weights exp(C' + l(|mu|)).  The bin
+// attenuation runs along the first beam's backward direction for every beam,
+// as the reference's attenuationDirection call with one direction computes it.
+static int prep_gauss(Scene* S, bool cbs)
+{
+    DevScene& D = S->dev;
+    Scene::HostSource& il = S->hsrc[0];
+    Scene::HostSource& vw = S->hsrc[1];
+    if (il.type != SSTMC_SOURCE_GAUSSIANBEAM || vw.type != SSTMC_SOURCE_GAUSSIANBEAM) return SSTMC_NOT_SUPPORTED;
+    if (S->correlation || cbs || S->dims != 3) return SSTMC_NOT_SUPPORTED;
+    for (int m = 0; m < kMat; ++m)
+        if (D.scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && D.scat_type[m] != SSTMC_SCATTERING_VMF_MIXTURE) return SSTMC_NOT_SUPPORTED;
+    il.gnorm = vmf_log_norm(il.ga);
+    vw.gnorm = vmf_log_norm(vw.ga);
+    double mv[3] = { 0, 0, 0 };
+    const double inv = 1.0 / vw.n;
+    for (int v = 0; v < vw.n; ++v)
+        for (int a = 0; a < 3; ++a) mv[a] = mv[a] + inv * (double)vw.gdir[3 * v + a];
+    const double r = std::sqrt(mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]);
+    if (r < 0.0001) return SSTMC_NOT_SUPPORTED;
+    for (int a = 0; a < 3; ++a) D.gmean[a] = mv[a] * (1.0 / r);
+    const int n = il.n;
+    int gM = 0;
+    il.gfm.assign(n, 0);
+    il.gtab.assign((size_t)9 * n, 0.0);
+    for (int l = 0; l < n; ++l) {
+        const float* f = il.p.data() + 3 * l;
+        bool in = true;
+        for (int a = 0; a < 3; ++a) in = in && f[a] >= S->ax[a].front() && f[a] <= S->ax[a].back();
+        int fm = 0;
+        if (in) {
+            int c[3];
+            for (int a = 0; a < 3; ++a) {
+                const int na = (int)S->ax[a].size();
+                int lo = 0, hi = na;
+                while (lo < hi) { const int mid = (lo + hi) >> 1; if (S->ax[a][mid] <= f[a]) lo = mid + 1; else hi = mid; }
+                int cc = lo - 1;
+                c[a] = cc < 0 ? 0 : (cc > na - 2 ? na - 2 : cc);
+            }
+            const size_t nx = S->ax[0].size() - 1, ny = S->ax[1].size() - 1;
+            fm = S->grid[(size_t)c[0] + (size_t)c[1] * nx + (size_t)c[2] * nx * ny];
+        }
+        if (fm <= 0 || D.gmix_n[fm] < 1 || D.gmix_n[fm] > 8) return SSTMC_NOT_SUPPORTED;
+        il.gfm[l] = fm;
+        gM = std::max(gM, D.gmix_n[fm]);
+    }
+    il.gM = gM;
+    const size_t nb = (size_t)n * gM * kGaussBins;
+    il.gpdf.assign(nb, 0.0); il.gicdf.assign(nb, 0.0);
+    il.gapdf.assign((size_t)n * gM, 0.0); il.gaicdf.assign((size_t)n * gM, 0.0);
+    const double k = 2.0 * kPi / S->cfg_copy.lambda;
+    const double back0[3] = { -(double)il.gdir[0], -(double)il.gdir[1], -(double)il.gdir[2] };
+    const double lo[3] = { (double)S->ax[0].front(), (double)S->ax[1].front(), (double)S->ax[2].front() };
+    const double hi[3] = { (double)S->ax[0].back(), (double)S->ax[1].back(), (double)S->ax[2].back() };
+    for (int l = 0; l < n; ++l) {
+        double d[3], f[3];
+        for (int i = 0; i < 3; ++i) { d[i] = il.gdir[3 * l + i]; f[i] = il.p[3 * l + i]; }
+        double* tb = il.gtab.data() + 9 * l;
+        double tmin = 0, tmax = 0;   // projectBoxToLine, MediumInterface.cuh:156-200
+        for (int c = 0; c < 8; ++c) {
+            const double cp[3] = { (c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2] };
+            const double t = gproj(cp, f, d);
+            if (c == 0 || t < tmin) tmin = t;
+            if (c == 0 || t > tmax) tmax = t;
+        }
+        tb[0] = tmin; tb[1] = tmax; tb[2] = (tmax - tmin) / (double)kGaussBins;
+        if (std::fabs(1.0 - std::fabs(d[2])) <= 1e-12) {   // orthogonalBase, VectorType.cuh:293-314
+            tb[3] = 1; tb[4] = 0; tb[5] = 0; tb[6] = 0; tb[7] = 1; tb[8] = 0;
+        } else {
+            double b0[3] = { -d[1], d[0], 0.0 };
+            const double rb = std::sqrt(b0[0] * b0[0] + b0[1] * b0[1]);
+            b0[0] /= rb; b0[1] /= rb;
+            tb[3] = b0[0]; tb[4] = b0[1]; tb[5] = 0.0;
+            tb[6] = b0[1] * d[2] - b0[2] * d[1];
+            tb[7] = b0[2] * d[0] - b0[0] * d[2];
+            tb[8] = b0[0] * d[1] - b0[1] * d[0];
+        }
+        const int fm = il.gfm[l], M = D.gmix_n[fm];
+        const double* mix = S->gmix.data() + 2 * D.gmix_off[fm];
+        for (int b = 0; b < kGaussBins; ++b) {
+            const double t = tmin + (double)b * tb[2];
+            const double z[3] = { f[0] + t * d[0], f[1] + t * d[1], f[2] + t * d[2] };
+            const double T = std::exp(-tau64_host(S, z, back0));
+            const double dz = (z[0] - f[0]) * d[0] + (z[1] - f[1]) * d[1] + (z[2] - f[2]) * d[2];
+            for (int m = 0; m < M; ++m)
+                il.gpdf[((size_t)l * gM + m) * kGaussBins + b] = T / ((il.ga + std::fabs(mix[2 * m])) / (k * k) + dz * dz / il.ga);
+        }
+        for (int m = 0; m < M; ++m) {
+            double* pdf = il.gpdf.data() + ((size_t)l * gM + m) * kGaussBins;
+            double* cdf = il.gicdf.data() + ((size_t)l * gM + m) * kGaussBins;
+            double run = 0.0;
+            for (int b = 0; b < kGaussBins; ++b) { cdf[b] = run; run += pdf[b]; }
+            const double tot = pdf[kGaussBins - 1] + cdf[kGaussBins - 1];
+            for (int b = 0; b < kGaussBins; ++b) { pdf[b] *= (double)(kGaussBins - 1) / tot; cdf[b] /= tot; }
+        }
+        // lobe weights, alphaPdfIcdfKernel (GaussianBeam.cuh:254-295)
+        double* ap = il.gapdf.data() + (size_t)l * gM;
+        double* ac = il.gaicdf.data() + (size_t)l * gM;
+        double asum = 0.0;
+        for (int m = 0; m < M; ++m) {
+            const double kap = std::fabs(mix[2 * m]);
+            const double ln = kap < 1e-5 ? -std::log(4.0 * kPi)
+                                         : std::log(kap) - (kap > 10.0 ? std::log(2.0 * kPi) * kap : std::log(4.0 * kPi * std::sinh(kap)));
+            ap[m] = std::exp(mix[2 * m + 1] + ln);
+            asum += ap[m];
+        }
+        for (int m = 0; m < M; ++m) ap[m] /= asum;
+        double run = 0.0;
+        for (int m = 0; m < M; ++m) { ac[m] = run; run += ap[m]; }
+    }
+    return SSTMC_NO_ERROR;
+}
+
 int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
 {
     auto fail = [&](int code, const char* msg) { if (why) *why = msg; return code; };
@@ -251,7 +437,7 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
             }
             D.has_amp64 = 1;
         }
-        int voff = 0, vpoff = 0, vn = 0;
+        int voff = 0, vpoff = 0, vn = 0, goff = 0;
         bool iso = ty == SSTMC_SCATTERING_ISOTROPIC || (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && std::fabs(g) < 0.0001);
         if (ty == SSTMC_SCATTERING_VMF_MIXTURE) {
             if (!cfg->vmf_n || !cfg->vmf_mu || !cfg->vmf_c || !cfg->vmf_alpha || cfg->vmf_n[m] < 1)
@@ -261,6 +447,10 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
             const double* cc = cfg->vmf_c + vmf_pos;
             const double* al = cfg->vmf_alpha + vmf_pos;
             vmf_pos += (size_t)vn;
+            // the lobes the Gaussian-beam terms read, mixtureMu and mixtureC + log(alpha)
+            // (Scattering.cuh:703-721), in 2D too
+            goff = (int)(S->gmix.size() / 2);
+            for (int k = 0; k < vn; ++k) { S->gmix.push_back(mu[k]); S->gmix.push_back(cc[k] + std::log(al[k])); }
             double asum = 0.0;
             iso = true;   // isIsotropicScatteringVonMisesFisher: every |mu| <= 1e-4 (Scattering.cuh:744-751)
             for (int k = 0; k < vn; ++k) {
@@ -287,6 +477,8 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
             D.vmf_n[mm] = dims == 3 ? vn : 0;
             D.vmf_off[mm] = voff;
             D.vmf_poff[mm] = vpoff;
+            D.gmix_n[mm] = vn;
+            D.gmix_off[mm] = goff;
             iso_m[mm] = iso;
             D.scat_type[mm] = (ty == SSTMC_SCATTERING_VMF_MIXTURE && dims == 2) ? SSTMC_SCATTERING_ISOTROPIC : ty;
             S->g_d[mm] = g;
@@ -303,11 +495,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     D.iso_all = 1;
     for (int m = 0; m < kMat; ++m)
         if (D.scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && !iso_m[m]) D.iso_all = 0;
-    // With every material isotropic, the reference's point sources take the
-    // isotropic amplitude while its far-field sources evaluate a vMF mixture
-    // (PointSource.cuh:346-430); that split is not built.
-    if (D.iso_all && any_vmf)
-        return fail(SSTMC_NOT_SUPPORTED, "every material isotropic with a vMF material among them: use Isotropic");
     D.iso_amp = dims == 2 ? kIsoAmp2 : kIsoAmp3;
     D.iso_pdf = dims == 2 ? kIsoPdf2 : kIsoPdf3;
 
@@ -384,6 +571,16 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     if (S->hsrc[0].type == SSTMC_SOURCE_NONE || S->hsrc[1].type == SSTMC_SOURCE_NONE)
         return fail(SSTMC_INVALID_CONFIG, "illumination and view are required");
     S->Nl = S->hsrc[0].n; S->Nv = S->hsrc[1].n;
+    D.gauss = (S->hsrc[0].type == SSTMC_SOURCE_GAUSSIANBEAM || S->hsrc[1].type == SSTMC_SOURCE_GAUSSIANBEAM) ? 1 : 0;
+    // With every material isotropic, the reference's point sources take the
+    // isotropic amplitude while its far-field sources evaluate a vMF mixture
+    // (PointSource.cuh:346-430); that split is not built.  Gaussian beams read
+    // the lobes themselves.
+    if (D.iso_all && any_vmf && !D.gauss)
+        return fail(SSTMC_NOT_SUPPORTED, "every material isotropic with a vMF material among them: use Isotropic");
+    for (int m = 0; m < kMat; ++m) D.gsigs[m] = sigs[m];
+    D.glz = dims == 3 ? bmax[2] - bmin[2] : 0.0;
+    D.gk = 2.0 * kPi / cfg->lambda;
 
     // sampler
     if (!cfg->t || cfg->t_num == 0) return fail(SSTMC_INVALID_CONFIG, "sampler.t is required");
@@ -424,6 +621,11 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     // isForcedInsideBin belongs to the field sampler; the correlation sampler has no
     // such option and the reference ignores the field there (MatlabInterface.cu:1245-1282)
     D.forced_bin = (cfg->is_forced_inside_bin && !S->correlation) ? 1 : 0;
+    if (D.gauss) {
+        const int e = prep_gauss(S, cfg->is_cbs != 0);
+        if (e) return fail(e, "GaussianBeam sources: 3D field sampler without CBS, both illumination and view GaussianBeam, "
+                              "every material vMF, focal points inside vMF materials, a mean view direction");
+    }
     D.ticks_geometric = S->abs_ticks[0] > 0.0f;
     for (int t = 0; t < Nt; ++t)
         if (S->abs_ticks[t] != (float)(t + 1) * S->abs_ticks[0]) D.ticks_geometric = 0;
@@ -489,6 +691,7 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         if (!e) e = upload(S, S->vmf_pd, &D.vmf_pd);
         if (!e) e = upload(S, S->vmf_pf, &D.vmf_pf);
     }
+    if (!e && D.gauss) e = upload(S, S->gmix, &D.gmix);
     if (!e) e = upload(S, S->grid, &D.grid);
     if (!e) e = upload(S, S->disp_scale, &D.disp_scale);
     if (!e) e = upload(S, S->disp_u, &D.disp_u);
@@ -500,6 +703,18 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         d.type = h.type; d.n = h.n; d.is_area = h.is_area;
         if (h.type == SSTMC_SOURCE_NONE) continue;
         e = upload(S, h.p, &d.p);
+        if (!e && h.type == SSTMC_SOURCE_GAUSSIANBEAM) {
+            d.ga = h.ga; d.gnorm = h.gnorm; d.gM = h.gM;
+            e = upload(S, h.gdir, &d.gdir);
+            if (!e && !h.gfm.empty()) {
+                e = upload(S, h.gfm, &d.gfm);
+                if (!e) e = upload(S, h.gtab, &d.gtab);
+                if (!e) e = upload(S, h.gpdf, &d.gpdf);
+                if (!e) e = upload(S, h.gicdf, &d.gicdf);
+                if (!e) e = upload(S, h.gapdf, &d.gapdf);
+                if (!e) e = upload(S, h.gaicdf, &d.gaicdf);
+            }
+        }
         if (!e && h.type == SSTMC_SOURCE_FARFIELD) {
             e = upload(S, h.inv, &d.inv);
             if (!e) e = upload(S, h.tang, &d.tang);

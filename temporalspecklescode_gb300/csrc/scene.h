@@ -41,7 +41,24 @@ struct DevSource {
     const float* mins;
     const float* maxs;
     const float* sprob;  // projected-box sampling probability q_l
+    // GaussianBeam (GaussianBeam.cuh, 3D): p = focal points, gdir = beam
+    // directions, ga = 1 / aperture^2, gnorm = the aperture normalisation.
+    // Illumination only: the focal material of each beam, per beam (tmin, tmax,
+    // dt, xy base 2 x 3), the distance-bin pdf / exclusive cdf of each lobe
+    // [n][gM][kGaussBins] and the lobe pdf / exclusive cdf [n][gM].
+    const float* gdir;
+    double ga, gnorm;
+    int gM;
+    const int* gfm;
+    const double* gtab;
+    const double* gpdf;
+    const double* gicdf;
+    const double* gapdf;
+    const double* gaicdf;
 };
+
+// distance bins of a Gaussian beam's first-vertex table (zSamplesNum, GaussianBeam.cuh:62-64)
+constexpr int kGaussBins = 1000;
 
 struct DevScene {
     int dims, correlation, Nt, neg;
@@ -88,6 +105,16 @@ struct DevScene {
     const double* vmf_mc;        // [components][2]: mu, C + log(alpha)
     const double* vmf_pd;        // [pairs][3]: kappa = mu1 + mu2, normalised weight, log normalisation
     const float* vmf_pf;         // [pairs][3]: exclusive cdf of the weights, kappa, exp(-2 |kappa|)
+    // Gaussian beams: per material its vMF lobes (mu, C + log alpha) in gmix,
+    // the mean view direction, k = 2 pi / lambda, sigs per material and the
+    // box depth in z (the first-point probability's normalisation)
+    int gauss;
+    int gmix_n[kMat], gmix_off[kMat];
+    const double* gmix;
+    double gmean[3];
+    double gk;
+    double gsigs[kMat];
+    double glz;
 };
 
 // Host-owned scene: normalised config, float tables and device buffers.
@@ -104,7 +131,13 @@ struct Scene {
         int type = 0, n = 0, is_area = 0;
         std::vector<float> p, inv, tang, pt, ps, mint, maxt, mins, maxs, sprob;
         std::vector<double> sprob_d;
+        std::vector<float> gdir;
+        double ga = 0.0, gnorm = 0.0;
+        int gM = 0;
+        std::vector<int> gfm;
+        std::vector<double> gtab, gpdf, gicdf, gapdf, gaicdf;
     } hsrc[4];
+    std::vector<double> gmix;    // Gaussian beams: vMF lobes (mu, C + log alpha) per material
     std::vector<float> ax[3];
     std::vector<unsigned char> grid;
     std::vector<float> disp_scale, disp_u, ticks_f, abs_ticks;

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 
+#include "gauss.cuh"
 #include "nee.cuh"
 #include "sstmc_internal.h"
 #include "trace.h"
@@ -812,6 +813,191 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
     }
 }
 
+// ---- Gaussian beams: the field sampler's rows with beam sources (gauss.cuh) ----
+// Warp per path, lanes over the beams; FP64 source terms.  The rows are the
+// ones trace_kernel writes for the field sampler (NextEventEstimation.cuh:
+// 1385-1637 with GaussianBeam.cuh's source functions):
+//   a_ss(t, l) = g_l(x1_t) e^(2 pi i xi_1) w_t / sqrt(p1),  b_ss(t, v) = g_v(x1_t)
+//   a_ms(t, l) = g_l(x1_t) f_l(x1_t -> x2_t) / sqrt(p2)
+//   s_ms(t, v) = sum_{b >= 2} g_v(x_b,t) e^(2 pi i (L_t / lambda + xi_b)) f_v(x_{b-1},t -> x_b,t) w_b,t
+// with p1 the mean of P_l(x1) and p2 the mean of P_l(x1) p_l(x1 -> x2) (a
+// zero product counting 1e20).  The view sums are added into the path's row
+// in place (each (t, v) entry is one lane's).
+__device__ __forceinline__ float gauss_g(const DevScene& S, const DevSource& s, int k, const V3& x, bool view, uint32_t& steps)
+{
+    const V3 d = load3(s.gdir, k);
+    return sqrtf(expf(-tau_dir(S, x, view ? d : V3{ -d.x, -d.y, -d.z }, steps)));
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(128) gauss_trace_kernel(const __grid_constant__ DevScene S, const __grid_constant__ TraceParams T)
+{
+    extern __shared__ double smem_d[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const bool split = S.precision == SSTMC_PRECISION_SPLIT;
+    double* Ls = smem_d + (size_t)wib * Nt;
+    float* fb = reinterpret_cast<float*>(smem_d + (size_t)nwb * Nt) + (size_t)wib * 9 * Nt;
+    float* phs = fb + 8 * Nt;
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long acc_v = 0, acc_s = 0, acc_m = 0, acc_p = 0;
+    for (uint32_t q = gw; q < T.paths; q += nw) {
+        const uint32_t pid = T.first_path + q;
+        const uint32_t B = T.counts[q];
+        if (B == 0) {   // the walk hit a limit (error already flagged): rows zero, no material
+            zero_rows(S, T, q, lane);
+            if (lane == 0 && T.m1) T.m1[q] = 0;
+            continue;
+        }
+        float* xtc = fb;
+        float* xtn = fb + 4 * Nt;
+        const float4* vq = T.verts + T.offsets[q];
+        const float4 v1 = vq[0];
+        const V3 x1 = V3{ v1.x, v1.y, v1.z };
+        const int m1 = (int)(__float_as_uint(v1.w) & 15u);
+        const float xi1 = (float)(__float_as_uint(v1.w) >> 4) * (1.0f / 16777216.0f);
+        temporal_positions(S, T.seed, pid, 1u, x1, m1, xtc, lane);
+        for (int t = lane; t < Nt; t += 32) Ls[t] = 0.0;
+        __syncwarp();
+        const bool mov1 = S.moving[m1] != 0;
+        if (T.x1t)
+            for (int i = lane; i < 3 * Nt; i += 32) T.x1t[(size_t)q * 3 * Nt + i] = xtc[i];
+        uint32_t steps = 0;
+
+        // first vertex: P_l, p1, the illumination and single-scattering rows
+        double ps = 0.0;
+        for (int l = lane; l < Nl; l += 32) {
+            const double P = gauss_pfirst(S, il, l, x1, m1);
+            T.pl[(size_t)q * Nl + l] = (float)P;
+            ps += P;
+        }
+        const double p1 = warp_sum_d(ps) / (double)Nl;
+        const float p1inv = (float)(1.0 / sqrt(p1));
+        const float2 e1 = unit_phase(xi1);
+        for (int l = lane; l < Nl; l += 32) {
+            uint32_t sts = 0;
+            const float gs = mov1 ? 0.0f : gauss_g(S, il, l, x1, false, sts);
+            for (int t = 0; t < Nt; ++t) {
+                float g = gs;
+                if (!mov1) steps += sts;
+                else g = gauss_g(S, il, l, tick_pos(xtc, t), false, steps);
+                T.a_ms[((size_t)q * Nt + t) * Nl + l] = make_float2(g, 0.0f);
+                T.a_ss[((size_t)q * Nt + t) * Nl + l] = c_scale(e1, g * p1inv * tick_w(S, xtc, t));
+            }
+        }
+        for (int v = lane; v < Nv; v += 32) {
+            uint32_t sts = 0;
+            const float gs = mov1 ? 0.0f : gauss_g(S, vw, v, x1, true, sts);
+            for (int t = 0; t < Nt; ++t) {
+                float g = gs;
+                if (!mov1) steps += sts;
+                else g = gauss_g(S, vw, v, tick_pos(xtc, t), true, steps);
+                T.b_ss[((size_t)q * Nt + t) * Nv + v] = make_float2(g, 0.0f);
+            }
+        }
+        for (int i = lane; i < Nt * Nv; i += 32) T.s_ms[(size_t)q * Nt * Nv + i] = make_float2(0.f, 0.f);
+        if (B < 2)
+            for (int i = lane; i < Nt * Nl; i += 32) T.a_ms[(size_t)q * Nt * Nl + i] = make_float2(0.f, 0.f);
+        __syncwarp();
+
+        // later vertices
+        V3 cur = x1;
+        int mcur = m1;
+        for (uint32_t b = 2; b <= B; ++b) {
+            const float4 vb = vq[b - 1];
+            const V3 xn = V3{ vb.x, vb.y, vb.z };
+            const int mn = (int)(__float_as_uint(vb.w) & 15u);
+            const float xin = (float)(__float_as_uint(vb.w) >> 4) * (1.0f / 16777216.0f);
+            temporal_positions(S, T.seed, pid, b, xn, mn, xtn, lane);
+            for (int t = lane; t < Nt; t += 32) {
+                const V3 a = tick_pos(xtc, t), c = tick_pos(xtn, t);
+                if (split) {
+                    const double dx = (double)c.x - (double)a.x, dy = (double)c.y - (double)a.y, dz = (double)c.z - (double)a.z;
+                    Ls[t] += sqrt(fma(dx, dx, fma(dy, dy, dz * dz)));
+                    phs[t] = frac_cycles(Ls[t] * S.inv_lambda + (double)xin);
+                } else {
+                    const V3 dd = sub3(c, a);
+                    Ls[t] = (double)((float)Ls[t] + sqrtf(dot3(dd, dd)));
+                    const float ph = (float)Ls[t] * S.inv_lambda_f + xin;
+                    phs[t] = ph - rintf(ph);
+                }
+            }
+            __syncwarp();
+            if (b == 2) {
+                double qs = 0.0;
+                for (int l = lane; l < Nl; l += 32) {
+                    const double P = gauss_pfirst(S, il, l, x1, m1);
+                    const double pw = S.iso_all ? 0.079577471545947668 : gauss_pw(S, il, l, x1, xn);
+                    const double qq = P * pw;
+                    qs += qq == 0.0 ? 1e20 : qq;
+                }
+                const double p2 = warp_sum_d(qs) / (double)Nl;
+                const float p2inv = (float)(1.0 / sqrt(p2));
+                if (T.p2 && lane == 0) T.p2[q] = (float)p2;
+                const bool stf = !S.temporal_amp || (!mov1 && !S.moving[mn]);
+                for (int l = lane; l < Nl; l += 32) {
+                    CD fs{ 0.0, 0.0 };
+                    if (stf) fs = gauss_f(S, il, l, x1, xn, m1, false);
+                    for (int t = 0; t < Nt; ++t) {
+                        const CD f = stf ? fs : gauss_f(S, il, l, tick_pos(xtc, t), tick_pos(xtn, t), m1, false);
+                        const size_t o = ((size_t)q * Nt + t) * Nl + l;
+                        const float g = T.a_ms[o].x * p2inv;
+                        T.a_ms[o] = make_float2(g * (float)f.re, g * (float)f.im);
+                    }
+                }
+            }
+            const bool stn = !S.moving[mn];
+            const bool stf = !S.temporal_amp || (stn && !S.moving[mcur]);
+            for (int v = lane; v < Nv; v += 32) {
+                uint32_t sts = 0;
+                const float gs = stn ? gauss_g(S, vw, v, xn, true, sts) : 0.0f;
+                CD fs{ 0.0, 0.0 };
+                if (stf) fs = gauss_f(S, vw, v, xn, cur, mn, true);
+                for (int t = 0; t < Nt; ++t) {
+                    float g = gs;
+                    if (stn) steps += sts;
+                    else g = gauss_g(S, vw, v, tick_pos(xtn, t), true, steps);
+                    const CD f = stf ? fs : gauss_f(S, vw, v, tick_pos(xtn, t), tick_pos(xtc, t), mn, true);
+                    const float2 c = c_scale(c_mul(unit_phase(phs[t]), make_float2((float)f.re, (float)f.im)), g * tick_w(S, xtn, t));
+                    float2* d = T.s_ms + ((size_t)q * Nt + t) * Nv + v;
+                    const float2 a = *d;
+                    *d = make_float2(a.x + c.x, a.y + c.y);
+                }
+            }
+            cur = xn;
+            mcur = mn;
+            float* tmp = xtc; xtc = xtn; xtn = tmp;
+            __syncwarp();
+        }
+        const uint32_t wsteps = warp_sum_u32(steps);
+        if (lane == 0) {
+            if (T.m1) T.m1[q] = (unsigned char)m1;
+            if (T.x1) { T.x1[3 * q] = x1.x; T.x1[3 * q + 1] = x1.y; T.x1[3 * q + 2] = x1.z; }
+            acc_v += B;
+            acc_m += T.misses[q];
+            acc_p += 1;
+            if (T.dda && wsteps) atomicAdd(T.dda + q, wsteps);
+            acc_s += wsteps;
+        }
+    }
+    if (lane == 0) {
+        if (acc_v) atomicAdd(T.totals + 0, acc_v);
+        if (acc_s) atomicAdd(T.totals + 1, acc_s);
+        if (acc_m) atomicAdd(T.totals + 2, acc_m);
+        if (acc_p) atomicAdd(T.totals + 3, acc_p);
+    }
+}
+
 // ---- CBS of the correlation sampler, static scatterers (NextEventEstimation.cuh:1237-1378) ----
 // For every vertex x_b (b >= 2) of every path, the cross terms of the direct
 // and reversed paths (SourceInterface.cuh:270-354 for the temporal factors):
@@ -1056,6 +1242,29 @@ int occupancy_blocks(const DevScene& S, int threads, size_t smem)
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, threads, smem) != cudaSuccess) n = 1;
     return n > 0 ? n : 1;
+}
+
+size_t gauss_trace_smem_bytes(int Nt, int threads)
+{
+    const size_t nwb = (size_t)threads / 32;
+    return nwb * (size_t)Nt * sizeof(double) + nwb * 9 * (size_t)Nt * sizeof(float);
+}
+
+int launch_gauss_trace(const DevScene& S, const TraceParams& T, int threads, cudaStream_t stream)
+{
+    const size_t smem = gauss_trace_smem_bytes(S.Nt, threads);
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute((const void*)gauss_trace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return SSTMC_KERNEL_ERROR;
+    }
+    // four paths per block, at most one wave of resident blocks
+    int dev = 0, sms = 0, occ = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, gauss_trace_kernel, threads, smem) != cudaSuccess || occ < 1) occ = 1;
+    const int blocks = (int)std::max<uint32_t>(1u, std::min<uint32_t>((T.paths + 3) / 4, (uint32_t)(sms * occ)));
+    gauss_trace_kernel<<<blocks, threads, smem, stream>>>(S, T);
+    return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 
 int launch_trace(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream)

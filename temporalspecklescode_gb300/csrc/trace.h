@@ -69,6 +69,9 @@ struct CbsCorrParams {
 int launch_cbs_corr(const DevScene& S, const CbsCorrParams& P, cudaStream_t stream);
 
 size_t trace_smem_bytes(int Nt, int slots, int threads);
+// Gaussian-beam scenes (3D field sampler): every row of a path in one warp
+size_t gauss_trace_smem_bytes(int Nt, int threads);
+int launch_gauss_trace(const DevScene& S, const TraceParams& T, int threads, cudaStream_t stream);
 int launch_trace(const DevScene& S, const TraceParams& T, int blocks, int threads, cudaStream_t stream);
 
 }  // namespace sstmc

@@ -7,7 +7,7 @@
 //   voxel traversal (attenuation)               HeterogeneousMedium.cuh:386-573
 //   far-field / point first-vertex sampling     FarField.cuh:129-205, PointSource.cuh:72-90
 //   phase-function sampling (Iso, HG)           Scattering.cuh:1039-1115
-//   direction rotation, random direction        VectorType.cuh:261-282, 316-362
+//   direction rotation, random direction        VectorType.cuh:207-283, 316-362
 // The traversal is parametric (face distances from the ray origin, not from
 // an advanced point) so rounding does not accumulate along long rays.
 #pragma once
@@ -131,6 +131,8 @@ __device__ __forceinline__ float vmf_cosine(const DevScene& S, int m, Stream& rs
 
 // VMF: the scene has vMF materials (3D).  Without it the vMF branch is not
 // compiled, so scenes without vMF run the walk code they ran before vMF existed.
+__device__ inline V3 rotate_dir(const DevScene& S, const V3& din, float c, Stream& rs);
+
 template <bool VMF>
 __device__ inline V3 sample_direction(const DevScene& S, int m, const V3& din, Stream& rs)
 {
@@ -166,6 +168,13 @@ __device__ inline V3 sample_direction(const DevScene& S, int m, const V3& din, S
             c = fdv(fsb(fa(1.0f, gg), fm(s, s)), fm(2.0f, g));
         }
     }
+    return rotate_dir(S, din, c, rs);
+}
+
+// The direction at cosine c to din (VectorType.cuh:207-283, vector_rotation):
+// a side (2D) or an azimuth (3D) from the stream.
+__device__ inline V3 rotate_dir(const DevScene& S, const V3& din, float c, Stream& rs)
+{
     const float sgn = rs.uniform() < 0.5f ? -1.0f : 1.0f;
     const float sa = fm(sgn, fsq(fmaxf(0.0f, fsb(1.0f, fm(c, c)))));
     if (S.dims == 2) {

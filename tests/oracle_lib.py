@@ -49,6 +49,12 @@ class Oracle:
                                             C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_float),
                                             C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.oracle_philox.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        fp = C.POINTER(C.c_float)
+        ip = C.POINTER(C.c_int32)
+        L.oracle_gauss_terms.argtypes = [C.POINTER(cf.SstmcConfig), C.c_int32, C.c_int32, fp, C.c_int32, fp, dp]
+        L.oracle_gauss_terms.restype = C.c_int32
+        L.oracle_gauss_sample.argtypes = [C.POINTER(cf.SstmcConfig), C.c_uint64, C.c_uint32, fp, C.c_int32, fp, ip, ip, fp]
+        L.oracle_gauss_sample.restype = C.c_int32
 
     def render(self, pc: cf.PreparedConfig, seed: int, first_wave: int = 0, waves: int | None = None, threads: int = 0):
         m = pc.meta
@@ -128,3 +134,32 @@ class Oracle:
         o = (C.c_uint32 * 4)()
         self.lib.oracle_philox(k, c, o)
         return [int(x) for x in o]
+
+    def gauss_terms(self, pc: cf.PreparedConfig, l: int, v: int, x1, m1: int, x2) -> dict:
+        """Gaussian-beam source terms at x1 (material m1) with the path on to x2."""
+        a = np.ascontiguousarray(x1, dtype=np.float32)
+        b = np.ascontiguousarray(x2, dtype=np.float32)
+        out = np.zeros(10)
+        e = self.lib.oracle_gauss_terms(pc.ptr(), l, v, a.ctypes.data_as(C.POINTER(C.c_float)), m1,
+                                        b.ctypes.data_as(C.POINTER(C.c_float)), out.ctypes.data_as(C.POINTER(C.c_double)))
+        if e:
+            raise RuntimeError(f"oracle_gauss_terms failed: {e}")
+        return {"P": out[0], "pw": out[1], "f_illum": complex(out[2], out[3]), "f_view": complex(out[4], out[5]),
+                "fs": complex(out[6], out[7]), "g_illum": out[8], "g_view": out[9]}
+
+    def gauss_sample(self, pc: cf.PreparedConfig, seed: int, n: int, x1=None, beam: int = 0):
+        """n beam-sampled first vertices, their materials, beams and second
+        directions; with x1 given, n second directions drawn at x1 for `beam`."""
+        fix = None if x1 is None else np.ascontiguousarray(x1, dtype=np.float32)
+        xyz = np.zeros((n, 3), dtype=np.float32)
+        d = np.zeros((n, 3), dtype=np.float32)
+        mat = np.zeros(n, dtype=np.int32)
+        b = np.zeros(n, dtype=np.int32)
+        fp = C.POINTER(C.c_float)
+        ip = C.POINTER(C.c_int32)
+        e = self.lib.oracle_gauss_sample(pc.ptr(), seed, n, None if fix is None else fix.ctypes.data_as(fp), beam,
+                                         xyz.ctypes.data_as(fp), mat.ctypes.data_as(ip), b.ctypes.data_as(ip),
+                                         d.ctypes.data_as(fp))
+        if e:
+            raise RuntimeError(f"oracle_gauss_sample failed: {e}")
+        return xyz, mat, b, d

@@ -83,13 +83,19 @@ class ObjectScene:
             blk = config.get(role)
             if blk is None:
                 continue
-            key = "direction" if blk["type"] == "FarField" else "location"
-            d = blk[key]
-            xyz = np.stack([np.ravel(d["x"]), np.ravel(d["y"]),
-                            np.ravel(d["z"]) if dims == 3 else np.zeros(np.ravel(d["x"]).size)], axis=1)
-            xyz = np.ascontiguousarray(xyz.astype(np.float64).reshape(-1))
+            key = {"FarField": "direction", "GaussianBeam": "focalPoint"}.get(blk["type"], "location")
+            vec = lambda d: np.ascontiguousarray(np.stack([np.ravel(d["x"]), np.ravel(d["y"]),
+                                                           np.ravel(d["z"]) if dims == 3 else np.zeros(np.ravel(d["x"]).size)],
+                                                          axis=1).astype(np.float64).reshape(-1))
+            xyz = vec(blk[key])
             self.keep.append(xyz)
-            if blk["type"] == "FarField":
+            if blk["type"] == "GaussianBeam":
+                fd = vec(blk["focalDirection"])
+                self.keep.append(fd)
+                self.src[role] = self._make(L.sstmc_source_create_gaussian_beam, L.sstmc_source_destroy, self.sim,
+                                            CONNECTION[role], _dp(xyz), _dp(fd), xyz.size // 3,
+                                            float(np.ravel(blk["aperture"])[0]))
+            elif blk["type"] == "FarField":
                 self.src[role] = self._make(L.sstmc_source_create_far_field, L.sstmc_source_destroy, self.sim,
                                             CONNECTION[role], _dp(xyz), xyz.size // 3)
             else:

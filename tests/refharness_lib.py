@@ -39,12 +39,21 @@ def _tokens(pc: cf.PreparedConfig, renderings: int, seed: int) -> str:
            f"lambda {c.lam!r}"]
     kinds = rd(c.scattering_type, c.scattering_num)
     g = rd(c.scattering_g, c.scattering_num)
+    cells = []
+    vpos = 0
+    for k, x in zip(kinds, g):
+        if k == cf.SCATTERING_VMF:
+            n = int(c.vmf_n[len(cells)])
+            mu, cc, al = (rd(p, vpos + n)[vpos:] for p in (c.vmf_mu, c.vmf_c, c.vmf_alpha))
+            vpos += n
+            cells.append(f"4 {n} " + " ".join(repr(float(v)) for v in np.concatenate([mu, cc, al])))
+        elif k in (cf.SCATTERING_ISOTROPIC, cf.SCATTERING_HG):
+            cells.append(f"{int(k)} {float(x)!r}")
+        else:
+            raise ValueError("the harness builds isotropic, Henyey-Greenstein and vMF materials only")
     if c.scattering_num == 1:   # one cell is material 1 as well (MatlabInterface.cu:750-760)
-        kinds, g = np.repeat(kinds, 2), np.repeat(g, 2)
-    for k in kinds:
-        if k not in (cf.SCATTERING_ISOTROPIC, cf.SCATTERING_HG):
-            raise ValueError("the harness builds isotropic and Henyey-Greenstein materials only")
-    out.append(f"scattering {mat_num} " + " ".join(f"{int(k)} {float(x)!r}" for k, x in zip(kinds, g)))
+        cells = cells * 2
+    out.append(f"scattering {mat_num} " + " ".join(cells))
     if c.medium_type != cf.MEDIUM_HETEROGENEOUS:
         raise ValueError("the harness builds heterogeneous media only")
     axes = [rd(c.x_axis, c.x_axis_size), rd(c.y_axis, c.y_axis_size)] + ([rd(c.z_axis, c.z_axis_size)] if dims == 3 else [])
@@ -62,7 +71,10 @@ def _tokens(pc: cf.PreparedConfig, renderings: int, seed: int) -> str:
         if s.is_area_source:
             raise ValueError("the harness builds point sources without isAreaSource")
         xyz = rd(s.xyz, 3 * s.count)
-        out.append(f"source {role} {s.type} {s.count} " + " ".join(repr(float(v)) for v in xyz))
+        line = f"source {role} {s.type} {s.count} " + " ".join(repr(float(v)) for v in xyz)
+        if s.type == cf.SOURCE_GAUSSIANBEAM:
+            line += " " + " ".join(repr(float(v)) for v in rd(s.focal_direction, 3 * s.count)) + f" {float(s.aperture)!r}"
+        out.append(line)
     out.append(f"sampler {c.sampler_type}")
     t = rd(c.t, c.t_num)
     out.append(f"ticks {t.size} " + " ".join(repr(float(v)) for v in t))

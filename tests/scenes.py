@@ -472,6 +472,44 @@ def far_phases_3d(point: bool, batch_size=64, full_iteration=2):
     return cfg, 3
 
 
+def gauss_beams_3d(moving: bool = False, iso: bool = False, tilted: bool = False, back: bool = False,
+                   n_l: int = 3, n_v: int = 4, batch_size=64, full_iteration=2, equal_lobes: bool = False):
+    """Focused Gaussian beams (3D field sampler): vMF materials, illumination and
+    view beams focused inside a two-material slab (a three-lobe and a two-lobe
+    mixture), optionally drifting and diffusing scatterers over three ticks,
+    every lobe isotropic, tilted illumination beams, or views looking back
+    along -z (backscattering).  equal_lobes: two-lobe mixtures everywhere."""
+    lobes = [([0.0], [1.0]), ([0.0], [1.0]), ([0.0], [1.0])] if iso else \
+        [([0.0], [1.0]), ([0.0, 4.0, 15.0], [0.3, 0.5, 0.2]), ([0.0, 2.5], [0.6, 0.4])]
+    if equal_lobes:
+        lobes = [([0.0, 1.0], [0.5, 0.5]), ([0.0, 4.0], [0.5, 0.5]), ([0.0, 2.5], [0.6, 0.4])]
+    cells = [vmf_mixture(m, a) for m, a in lobes]
+    xl = np.linspace(-1.5, 1.5, n_l)
+    xv = np.linspace(-2.0, 2.0, n_v)
+    dl = np.array([0.3, 0.0, 1.0]) / np.hypot(0.3, 1.0) if tilted else np.array([0.0, 0.0, 1.0])
+    dv = np.array([0.0, 0.0, -1.0 if back else 1.0])
+    t = [0.0, 0.5, 1.0] if moving else [0.0]
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.8},
+        "scattering": {"type": ["vMF"] * 3, "amplitudeFunction": cells},
+        "medium": {"type": "Heterogeneous", "xAxis": [-12.0, 0.0, 12.0], "yAxis": [-12.0, 12.0], "zAxis": [0.0, 4.0, 10.0],
+                   "materialGrid": np.array([1, 2, 2, 1]).reshape(2, 1, 2, order="F"), "sigs": [0.0, 0.25, 0.15],
+                   "siga": [0.0, 0.01, 0.0]},
+        "illumination": {"type": "GaussianBeam",
+                         "focalPoint": {"x": xl, "y": 0.2 * xl, "z": np.full(n_l, 3.0)},
+                         "focalDirection": {"x": np.full(n_l, dl[0]), "y": np.full(n_l, dl[1]), "z": np.full(n_l, dl[2])},
+                         "aperture": 0.4},
+        "view": {"type": "GaussianBeam",
+                 "focalPoint": {"x": xv, "y": np.zeros(n_v), "z": np.full(n_v, 5.0)},
+                 "focalDirection": {"x": np.zeros(n_v), "y": np.zeros(n_v), "z": np.full(n_v, dv[2])},
+                 "aperture": 0.5},
+        "sampler": {"type": "TemporalSampler", "t": t, "D": [0.0, 0.02 if moving else 0.0, 0.0],
+                    "U": {"x": [0.0, 0.3 if moving else 0.0, 0.0], "y": [0.0, 0.0, 0.0], "z": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -518,6 +556,10 @@ def small_scenes():
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
         "edge_one_path_corr_3d": one_path(True),
         "edge_one_path_field_2d": one_path(False),
+        "gauss_3d": gauss_beams_3d(),
+        "gauss_3d_moving": gauss_beams_3d(moving=True),
+        "gauss_3d_iso": gauss_beams_3d(iso=True),
+        "gauss_3d_tilted_back": gauss_beams_3d(tilted=True, back=True),
         "edge_ragged_corr_3d": ragged_corr_3d(),
         "edge_mostly_misses_3d": mostly_misses_3d(),
         "edge_absorbing_2d": absorbing_2d(),

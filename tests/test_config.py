@@ -27,12 +27,23 @@ def test_prepare_fills_the_struct():
     assert np.array_equal(flat, grid.ravel(order="F"))
 
 
-def test_gaussian_beam_sources_are_refused():
+def test_gaussian_beam_config_fields():
+    """focalPoint, focalDirection and aperture (MatlabInterface.cu:1161-1200)
+    reach the source block; a missing field or a direction count that differs
+    from the focal points' is refused."""
     cfg, dims = _speckle()
-    cfg["illumination"] = {"type": "GaussianBeam", "focalPoint": {"x": [0.0], "y": [0.0]},
-                           "focalDirection": {"x": [0.0], "y": [1.0]}, "aperture": 0.4}
-    with pytest.raises(cf.ConfigError, match="GaussianBeam"):
-        cf.prepare(cfg, dims)
+    cfg["illumination"] = {"type": "GaussianBeam", "focalPoint": {"x": [0.0, 1.0], "y": [0.0, 2.0]},
+                           "focalDirection": {"x": [0.0, 0.6], "y": [1.0, 0.8]}, "aperture": 0.4}
+    pc = cf.prepare(cfg, dims)
+    s = pc.struct.illumination
+    assert s.type == cf.SOURCE_GAUSSIANBEAM and s.count == 2 and s.aperture == 0.4
+    assert [s.xyz[i] for i in range(6)] == [0.0, 0.0, 0.0, 1.0, 2.0, 0.0]
+    assert [s.focal_direction[i] for i in range(6)] == [0.0, 1.0, 0.0, 0.6, 0.8, 0.0]
+    bad = dict(cfg["illumination"], focalDirection={"x": [0.0], "y": [1.0]})
+    with pytest.raises(cf.ConfigError, match="focalDirection"):
+        cf.prepare(dict(cfg, illumination=bad), dims)
+    with pytest.raises(cf.ConfigError, match="aperture"):
+        cf.prepare(dict(cfg, illumination={k: v for k, v in cfg["illumination"].items() if k != "aperture"}), dims)
 
 
 @pytest.mark.parametrize("edit,match", [

@@ -27,7 +27,7 @@ from tests.plugin_builder import ObjectScene
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SCENES = scenes.small_scenes()
 NAMES = ["speckle_2d", "correlation_3d", "transmission_matrix_3d", "field_point_3d", "corr_far_2d_drift",
-         "homogeneous_3d", "tabular_corr_2d", "vmf_corr_3d", "forced_bin_3d", "reciprocal_far_3d_cbs"]
+         "homogeneous_3d", "tabular_corr_2d", "vmf_corr_3d", "forced_bin_3d", "reciprocal_far_3d_cbs", "gauss_3d_moving"]
 
 
 @pytest.fixture(scope="module")
@@ -60,6 +60,8 @@ def _arrays(c: cf.SstmcConfig):
     for role in ("illumination", "view", "illumination2", "view2"):
         s = getattr(c, role)
         out[role] = (s.type, s.count, s.is_area_source, tuple(rd(s.xyz, 3 * s.count)) if s.type else ())
+        if s.type == cf.SOURCE_GAUSSIANBEAM:
+            out[role] += (tuple(rd(s.focal_direction, 3 * s.count)), s.aperture)
     out["t"] = rd(c.t, c.t_num)
     out["D"] = rd(c.D, mat_num)
     out["U"] = rd(c.U, 3 * mat_num)

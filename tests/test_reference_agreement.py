@@ -22,6 +22,7 @@ import pytest
 
 from temporalspecklescode_gb300 import workloads as wl
 from tests import refharness_lib as ref
+from tests import scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -44,6 +45,8 @@ def _scenes():
         "correlation_3d": (wl.correlation_3d(batch_size=1024, full_iteration=2, n_side=4, n_lags=8)[0], 3, "correlation"),
         # 3D heterogeneous far field: four iid materials on a 16x16x8 grid, 12 x 12 directions
         "transmission_3d": (far3d, 3, "field"),
+        # 3D focused Gaussian beams in a two-material vMF slab (two lobes per material)
+        "gauss_3d": (scenes.gauss_beams_3d(batch_size=1024, full_iteration=2, equal_lobes=True)[0], 3, "field"),
     }
 
 
