@@ -1367,7 +1367,7 @@ static double o_gauss_pw(const o_scene* S, const o_src* s, int l, const float x1
 
 /* NEE vector of a beam: sqrt of the attenuation along the beam axis from x,
  * backward for an illumination, forward for a view (throughputFunction,
- * GaussianBeam.cuh:795-816, 1870-1888) */
+ * GaussianBeam.cuh:795-816, 1942-1965) */
 static oc o_gauss_g(const o_scene* S, const o_src* s, int k, const float x[3], int role, uint64_t* steps)
 {
     float sg = role == 0 ? -1.0f : 1.0f;

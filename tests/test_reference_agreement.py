@@ -46,7 +46,7 @@ def _scenes():
         # 3D heterogeneous far field: four iid materials on a 16x16x8 grid, 12 x 12 directions
         "transmission_3d": (far3d, 3, "field"),
         # 3D focused Gaussian beams in a two-material vMF slab (two lobes per material)
-        "gauss_3d": (scenes.gauss_beams_3d(batch_size=1024, full_iteration=2, equal_lobes=True)[0], 3, "field"),
+        "gauss_3d": (scenes.gauss_beams_3d(batch_size=1024, full_iteration=16, n_l=4, n_v=6, equal_lobes=True)[0], 3, "field"),
     }
 
 
