@@ -69,6 +69,8 @@ WORKLOADS = {
     "transmission_matrix_3d": {"paths_log2": 24, "cpu_sample": 1 << 11, "ref_sample": 1 << 10, "err_paths": 1 << 8},
     # 2D tracking: 128 x 128 far field, 256^2 grid with a drifting disc, all 32 x 32 frame pairs (32 lags)
     "tracking_2d_pairs": {"paths_log2": 23, "cpu_sample": 1 << 6, "ref_sample": 1 << 5, "err_paths": 1 << 3},
+    # 3D focused Gaussian beams: 64 x 64 beams on a confocal grid in a four-material vMF slab
+    "confocal_3d": {"paths_log2": 14, "cpu_sample": 1 << 14, "ref_sample": 1 << 12, "err_paths": 1 << 11},
 }
 
 def _dist():
@@ -208,6 +210,8 @@ def _workload(seed: int, paths_log2: int, workload: str | None = None):
         return wl.transmission_matrix_3d(batch_size=batch, full_iteration=waves, seed=seed)
     if workload == "tracking_2d_pairs":
         return wl.tracking_2d_pairs(batch_size=batch, full_iteration=waves, seed=seed)
+    if workload == "confocal_3d":
+        return wl.confocal_3d(batch_size=batch, full_iteration=waves, seed=seed)
     return wl.correlation_3d(batch_size=batch, full_iteration=waves, seed=seed)
 
 
@@ -331,6 +335,8 @@ KERNEL_NAMES = {
                                "ss": "gemm_tc_kernel x materials (far x far single scattering, weight tables)"},
     "tracking_2d_pairs": {"nee": "trace_kernel (fused NEE vectors, drifting scatterers)",
                           "ss": "gemm_tc_kernel x materials (far x far single scattering, weight tables)"},
+    "confocal_3d": {"nee": "gauss_trace_kernel (beam NEE vectors, FP64 amplitudes)",
+                    "ss": "gauss_ss_kernel (beam x beam single scattering, FP64 amplitudes)"},
 }
 
 
@@ -392,6 +398,11 @@ def _kernel_rooflines(scene, mean, verts_per_step, dda_per_step, chunks, peaks, 
         # single-scattering contraction: tick-0 rows read (tick-invariant form)
         add("ss", names["ss"], mean["ms_contract_ss"], "hbm", P * 8.0 * (Nl + Nv),
             "FP32/SFU-issue bound: one exp and one rsqrt per (path, l, v)")
+    elif WORKLOAD == "confocal_3d":
+        # beam x beam single scattering: the rows of every tick read once, V written;
+        # the FP64 amplitude per (path, l, v) bounds it, not the bytes
+        add("ss", names["ss"], mean["ms_contract_ss"], "hbm", P * 8.0 * Nt * (Nl + Nv) + 16.0 * Nl * Nv * Nt,
+            "FP64-issue bound: one beam x lobe x beam amplitude per (path, l, v)")
     else:
         # far x far: one GEMM per material over its paths, weights per (l, v, t, material)
         sflops = 8.0 * Nl * Nv * Nt * P

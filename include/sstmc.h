@@ -151,7 +151,7 @@ typedef struct sstmc_config {
                                       correlation sampler, TemporalSampler.cuh:439-534, 1637-1698) */
 
     /* config.tracer (MatlabInterface.cu:1374-1457) */
-    int32_t is_cbs;                /* default 0; 1: coherent backscattering (correlation sampler: static scatterers, U = 0) */
+    int32_t is_cbs;                /* default 0; 1: coherent backscattering (field and correlation samplers; not with Gaussian beams) */
 
     /* build-specific */
     int32_t precision;             /* SSTMC_PRECISION_* */

@@ -27,6 +27,7 @@
 //   sampler type                    (0 temporal, 1 correlation)
 //   ticks n t_0 .. t_{n-1}
 //   motion n  then n x (D ux uy uz)
+//   cbs c                           (optional: 1 renders with coherent backscattering)
 //   end
 #include <cstdio>
 #include <cstdlib>
@@ -64,6 +65,7 @@ struct SceneFile {
     int sampler = 0;
     std::vector<double> ticks;
     std::vector<double> D, U;
+    int cbs = 0;
 };
 
 bool read_scene(const char* path, SceneFile* s)
@@ -121,7 +123,8 @@ bool read_scene(const char* path, SceneFile* s)
             size_t n; in >> n;
             s->D.resize(n); s->U.resize(3 * n);
             for (size_t i = 0; i < n; ++i) in >> s->D[i] >> s->U[3 * i] >> s->U[3 * i + 1] >> s->U[3 * i + 2];
-        } else if (key == "end") return true;
+        } else if (key == "cbs") in >> s->cbs;
+        else if (key == "end") return true;
         else { std::fprintf(stderr, "unknown key %s\n", key.c_str()); return false; }
         if (!in) return false;
     }
@@ -219,7 +222,7 @@ int main(int argc, char** argv)
     NextEventEstimationOptions options;
     options.fullIterationsNumber = sc.full_iteration;
     options.seed = sc.seed;
-    options.isCBS = false;
+    options.isCBS = sc.cbs != 0;
     NextEventEstimation* tracer = new NextEventEstimation(&err, sampler, &options);
     CHECK("NextEventEstimation");
     const ub32 Nl = sampler->getIlluminationSize(), Nv = sampler->getViewSize(), Nt = sampler->getSamplerSize();

@@ -510,9 +510,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         S->D[m] = (m < M && cfg->D) ? cfg->D[m] : 0.0;
         if (S->D[m] < 0) return SSTMC_INVALID_CONFIG; /* MatlabInterface.cu:1278-1283 */
         for (int i = 0; i < 3; ++i) S->U_f[m][i] = (m < M && cfg->U && (i < dims)) ? (float)cfg->U[3 * m + i] : 0.0f;
-        /* correlation CBS is built for static scatterers (no drift U) */
-        if (S->cbs && S->correlation && (S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f))
-            return SSTMC_NOT_SUPPORTED;
     }
     if (S->gauss) {
         int e = o_prep_gauss(S);
@@ -1776,8 +1773,8 @@ typedef struct {
     double* P1; double* P2;           /* [Nl] */
 } o_work;
 
-/* CBS of the correlation sampler, static scatterers (NextEventEstimation.cuh:
- * 1237-1378, SourceInterface.cuh:270-354): for every vertex x_b (b >= 2) the
+/* CBS of the correlation sampler (NextEventEstimation.cuh:1237-1378,
+ * 1525-1600, SourceInterface.cuh:270-354): for every vertex x_b (b >= 2) the
  * cross terms of the direct and reversed paths,
  *   T2 = Gl_b(l) conj(u2Gv_b(v)) C2_l1v2(x_b) x conj(u2Gl0(l)) Gv0(v) C2_v1l2(x1)
  *   T3 = conj(u2Gl_b(l)) Gv_b(v) C3_v1l2(x_b) x Gl0(l) conj(u2Gv0(v)) C3_l1v2(x1)
@@ -1788,33 +1785,49 @@ typedef struct {
  * amplitude of the source attached there; C = exp(-k^2 |D t| |m|^2) with
  * m = (a + b) / 2 - (direction to the path's next point), a and b the
  * directions from the two ends' sources into the vertex (a view's is minus
- * its outgoing direction).  Rays traced here are not counted in the DDA
- * statistics. */
+ * its outgoing direction), the directions from the sampled (unshifted)
+ * positions (TemporalSamplerCorrelation.cuh:316-342).  Rays traced here are
+ * not counted in the DDA statistics. */
 static void o_cbs_corr(const o_scene* S, const o_verts* V, oc* Vacc, double p2)
 {
     int Nl = S->src[0].n, Nv = S->src[1].n, Nt = S->Nt, B = V->B;
     const o_src *il = &S->src[0], *vw = &S->src[1], *il2 = &S->src[2], *vw2 = &S->src[3];
     const float *x1 = V->x, *x2 = V->x + 3;
-    int m1 = V->m[0];
+    int m1 = V->m[0], m2 = V->m[1];
     double k2 = (2.0 * O_PI / S->lambda) * (2.0 * O_PI / S->lambda);
     uint64_t dummy = 0;
     double d12[3]; o_dir64(x1, x2, d12);
-    oc* G0l = malloc(sizeof(oc) * Nl); oc* U0l = malloc(sizeof(oc) * Nl);
-    oc* G0v = malloc(sizeof(oc) * Nv); oc* U0v = malloc(sizeof(oc) * Nv);
-    oc* Gl = malloc(sizeof(oc) * Nl); oc* U2l = malloc(sizeof(oc) * Nl);
-    oc* Gv = malloc(sizeof(oc) * Nv); oc* U2v = malloc(sizeof(oc) * Nv);
+    /* with drifting scatterers every vector is evaluated per tick: u1 NEE vectors
+     * at x - U t/2, u2 ones at x + U t/2, and both three-point amplitudes at the
+     * u1 positions (TemporalSamplerCorrelation.cuh:229-291, whose three-point copy
+     * takes the minus sign for every connection); static scenes need one tick */
+    int drift = 0;
+    for (int m = 0; m < OM; ++m) if (S->U_f[m][0] != 0.0f || S->U_f[m][1] != 0.0f || S->U_f[m][2] != 0.0f) drift = 1;
+    int Ne = drift ? Nt : 1;
+    oc* G0l = malloc(sizeof(oc) * Nl * Ne); oc* U0l = malloc(sizeof(oc) * Nl * Ne);
+    oc* G0v = malloc(sizeof(oc) * Nv * Ne); oc* U0v = malloc(sizeof(oc) * Nv * Ne);
+    oc* Gl = malloc(sizeof(oc) * Nl * Ne); oc* U2l = malloc(sizeof(oc) * Nl * Ne);
+    oc* Gv = malloc(sizeof(oc) * Nv * Ne); oc* U2v = malloc(sizeof(oc) * Nv * Ne);
     double* dl = malloc(sizeof(double) * 12 * (Nl + Nv));   /* directions at x1 and x_b */
     if (!G0l || !U0l || !G0v || !U0v || !Gl || !U2l || !Gv || !U2v || !dl) goto done;
     double *in1 = dl, *in2 = dl + 3 * Nl, *mo1 = dl + 6 * Nl, *mo2 = dl + 6 * Nl + 3 * Nv;
     double *in1b = dl + 6 * (Nl + Nv), *in2b = in1b + 3 * Nl, *mo1b = in1b + 6 * Nl, *mo2b = mo1b + 3 * Nv;
-    for (int l = 0; l < Nl; ++l) {
-        G0l[l] = oc_scale(oc_mul(o_g(S, il, l, x1, 0, &dummy), o_f3(S, il, l, x1, x2, m1, 0)), 1.0 / p2);
-        U0l[l] = oc_mul(o_g(S, il2, l, x1, 0, &dummy), o_f3(S, il2, l, x1, x2, m1, 0));
-        o_src_dir(il, l, x1, 0, in1 + 3 * l); o_src_dir(il2, l, x1, 0, in2 + 3 * l);
+    for (int e = 0; e < Ne; ++e) {
+        float tau = S->ticks_f[e];
+        float g1[3], g2[3], fa[3], fb[3];
+        o_shift(S, x1, m1, tau, -1.0f, g1); o_shift(S, x1, m1, tau, 1.0f, g2);
+        o_shift(S, x1, m1, tau, -1.0f, fa); o_shift(S, x2, m2, tau, -1.0f, fb);
+        for (int l = 0; l < Nl; ++l) {
+            G0l[e * Nl + l] = oc_scale(oc_mul(o_g(S, il, l, g1, 0, &dummy), o_f3(S, il, l, fa, fb, m1, 0)), 1.0 / p2);
+            U0l[e * Nl + l] = oc_mul(o_g(S, il2, l, g2, 0, &dummy), o_f3(S, il2, l, fa, fb, m1, 0));
+        }
+        for (int v = 0; v < Nv; ++v) {
+            G0v[e * Nv + v] = oc_scale(oc_mul(o_g(S, vw, v, g1, 1, &dummy), o_f3(S, vw, v, fa, fb, m1, 1)), 1.0 / p2);
+            U0v[e * Nv + v] = oc_mul(o_g(S, vw2, v, g2, 1, &dummy), o_f3(S, vw2, v, fa, fb, m1, 1));
+        }
     }
+    for (int l = 0; l < Nl; ++l) { o_src_dir(il, l, x1, 0, in1 + 3 * l); o_src_dir(il2, l, x1, 0, in2 + 3 * l); }
     for (int v = 0; v < Nv; ++v) {
-        G0v[v] = oc_scale(oc_mul(o_g(S, vw, v, x1, 1, &dummy), o_f3(S, vw, v, x1, x2, m1, 1)), 1.0 / p2);
-        U0v[v] = oc_mul(o_g(S, vw2, v, x1, 1, &dummy), o_f3(S, vw2, v, x1, x2, m1, 1));
         o_src_dir(vw, v, x1, 1, mo1 + 3 * v); o_src_dir(vw2, v, x1, 1, mo2 + 3 * v);
         for (int i = 0; i < 3; ++i) { mo1[3 * v + i] = -mo1[3 * v + i]; mo2[3 * v + i] = -mo2[3 * v + i]; }
     }
@@ -1830,18 +1843,27 @@ static void o_cbs_corr(const o_scene* S, const o_verts* V, oc* Vacc, double p2)
             MT += S->D[ma] * o_dot(q, q);
         }
         double back[3]; o_dir64(xb, xa, back);
-        for (int l = 0; l < Nl; ++l) {
-            Gl[l] = oc_mul(o_g(S, il, l, xb, 0, &dummy), o_f3(S, il, l, xb, xa, mb, 0));
-            U2l[l] = oc_mul(o_g(S, il2, l, xb, 0, &dummy), o_f3(S, il2, l, xb, xa, mb, 0));
-            o_src_dir(il, l, xb, 0, in1b + 3 * l); o_src_dir(il2, l, xb, 0, in2b + 3 * l);
+        for (int e = 0; e < Ne; ++e) {
+            float tau = S->ticks_f[e];
+            float g1[3], g2[3], fa[3], fb[3];
+            o_shift(S, xb, mb, tau, -1.0f, g1); o_shift(S, xb, mb, tau, 1.0f, g2);
+            o_shift(S, xb, mb, tau, -1.0f, fa); o_shift(S, xa, ma, tau, -1.0f, fb);
+            for (int l = 0; l < Nl; ++l) {
+                Gl[e * Nl + l] = oc_mul(o_g(S, il, l, g1, 0, &dummy), o_f3(S, il, l, fa, fb, mb, 0));
+                U2l[e * Nl + l] = oc_mul(o_g(S, il2, l, g2, 0, &dummy), o_f3(S, il2, l, fa, fb, mb, 0));
+            }
+            for (int v = 0; v < Nv; ++v) {
+                Gv[e * Nv + v] = oc_mul(o_g(S, vw, v, g1, 1, &dummy), o_f3(S, vw, v, fa, fb, mb, 1));
+                U2v[e * Nv + v] = oc_mul(o_g(S, vw2, v, g2, 1, &dummy), o_f3(S, vw2, v, fa, fb, mb, 1));
+            }
         }
+        for (int l = 0; l < Nl; ++l) { o_src_dir(il, l, xb, 0, in1b + 3 * l); o_src_dir(il2, l, xb, 0, in2b + 3 * l); }
         for (int v = 0; v < Nv; ++v) {
-            Gv[v] = oc_mul(o_g(S, vw, v, xb, 1, &dummy), o_f3(S, vw, v, xb, xa, mb, 1));
-            U2v[v] = oc_mul(o_g(S, vw2, v, xb, 1, &dummy), o_f3(S, vw2, v, xb, xa, mb, 1));
             o_src_dir(vw, v, xb, 1, mo1b + 3 * v); o_src_dir(vw2, v, xb, 1, mo2b + 3 * v);
             for (int i = 0; i < 3; ++i) { mo1b[3 * v + i] = -mo1b[3 * v + i]; mo2b[3 * v + i] = -mo2b[3 * v + i]; }
         }
         for (int t = 0; t < Nt; ++t) {
+            int e = drift ? t : 0;
             double at = fabs(S->ticks[t]);
             double pt = exp(-k2 * at * MT);
             double dtD1 = k2 * fabs(S->D[m1] * S->ticks[t]), dtDb = k2 * fabs(S->D[mb] * S->ticks[t]);
@@ -1849,17 +1871,19 @@ static void o_cbs_corr(const o_scene* S, const o_verts* V, oc* Vacc, double p2)
                 for (int l = 0; l < Nl; ++l) {
                     double q2b = 0, q21 = 0, q3b = 0, q31 = 0, q4b = 0, q41 = 0;
                     for (int i = 0; i < 3; ++i) {
-                        double e;
-                        e = 0.5 * (in1b[3 * l + i] + mo2b[3 * v + i]) - back[i]; q2b += e * e;
-                        e = 0.5 * (mo1[3 * v + i] + in2[3 * l + i]) - d12[i]; q21 += e * e;
-                        e = 0.5 * (mo1b[3 * v + i] + in2b[3 * l + i]) - back[i]; q3b += e * e;
-                        e = 0.5 * (in1[3 * l + i] + mo2[3 * v + i]) - d12[i]; q31 += e * e;
-                        e = 0.5 * (in1b[3 * l + i] + in2b[3 * l + i]) - back[i]; q4b += e * e;
-                        e = 0.5 * (mo1[3 * v + i] + mo2[3 * v + i]) - d12[i]; q41 += e * e;
+                        double d;
+                        d = 0.5 * (in1b[3 * l + i] + mo2b[3 * v + i]) - back[i]; q2b += d * d;
+                        d = 0.5 * (mo1[3 * v + i] + in2[3 * l + i]) - d12[i]; q21 += d * d;
+                        d = 0.5 * (mo1b[3 * v + i] + in2b[3 * l + i]) - back[i]; q3b += d * d;
+                        d = 0.5 * (in1[3 * l + i] + mo2[3 * v + i]) - d12[i]; q31 += d * d;
+                        d = 0.5 * (in1b[3 * l + i] + in2b[3 * l + i]) - back[i]; q4b += d * d;
+                        d = 0.5 * (mo1[3 * v + i] + mo2[3 * v + i]) - d12[i]; q41 += d * d;
                     }
-                    oc t2 = oc_mul(oc_mul(Gl[l], oc_conj(U2v[v])), oc_mul(oc_conj(U0l[l]), G0v[v]));
-                    oc t3 = oc_mul(oc_mul(oc_conj(U2l[l]), Gv[v]), oc_mul(G0l[l], oc_conj(U0v[v])));
-                    oc t4 = oc_mul(oc_mul(Gl[l], oc_conj(U2l[l])), oc_mul(G0v[v], oc_conj(U0v[v])));
+                    const oc gl = Gl[e * Nl + l], u2l = U2l[e * Nl + l], gv = Gv[e * Nv + v], u2v = U2v[e * Nv + v];
+                    const oc g0l = G0l[e * Nl + l], u0l = U0l[e * Nl + l], g0v = G0v[e * Nv + v], u0v = U0v[e * Nv + v];
+                    oc t2 = oc_mul(oc_mul(gl, oc_conj(u2v)), oc_mul(oc_conj(u0l), g0v));
+                    oc t3 = oc_mul(oc_mul(oc_conj(u2l), gv), oc_mul(g0l, oc_conj(u0v)));
+                    oc t4 = oc_mul(oc_mul(gl, oc_conj(u2l)), oc_mul(g0v, oc_conj(u0v)));
                     t2 = oc_scale(t2, exp(-dtDb * q2b - dtD1 * q21));
                     t3 = oc_scale(t3, exp(-dtDb * q3b - dtD1 * q31));
                     t4 = oc_scale(t4, exp(-dtDb * q4b - dtD1 * q41));

@@ -614,10 +614,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     }
     D.all_static_corr = 1;
     for (int m = 0; m < kMat; ++m) if (!D.static_corr[m]) D.all_static_corr = 0;
-    // CBS of the correlation sampler is built for static scatterers (no drift U)
-    // and real phase functions
-    if (cfg->is_cbs && S->correlation && !D.all_static_corr)
-        return fail(SSTMC_NOT_SUPPORTED, "tracer.isCBS with the TemporalCorrelationSampler needs static scatterers (U = 0)");
     // isForcedInsideBin belongs to the field sampler; the correlation sampler has no
     // such option and the reference ignores the field there (MatlabInterface.cu:1245-1282)
     D.forced_bin = (cfg->is_forced_inside_bin && !S->correlation) ? 1 : 0;

@@ -998,7 +998,7 @@ __global__ void __launch_bounds__(128) gauss_trace_kernel(const __grid_constant_
     }
 }
 
-// ---- CBS of the correlation sampler, static scatterers (NextEventEstimation.cuh:1237-1378) ----
+// ---- CBS of the correlation sampler (NextEventEstimation.cuh:1237-1378, 1525-1600) ----
 // For every vertex x_b (b >= 2) of every path, the cross terms of the direct
 // and reversed paths (SourceInterface.cuh:270-354 for the temporal factors):
 //   T2 = Gl_b(l) conj(u2Gv_b(v)) conj(u2Gl0(l)) Gv0(v) exp(-k^2 |t| (D_b |m2b|^2 + D_1 |m21|^2))
@@ -1015,10 +1015,14 @@ __global__ void __launch_bounds__(128) gauss_trace_kernel(const __grid_constant_
 // Its rays are not counted in the DDA statistics.
 constexpr int kCbT = 16, kCbTicks = 8;
 
-template <bool ILP, bool VWP>
+template <bool ILP, bool VWP, bool DRIFT>
 __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ DevScene S, const CbsCorrParams P)
 {
-    __shared__ float2 g0l[2][kCbT], g0v[2][kCbT], gb_l[2][kCbT], gb_v[2][kCbT];   // [u1 / u2][element]
+    // DRIFT: the vectors are staged per tick of the block's chunk (u1 NEE vectors at
+    // x - U t/2, u2 ones at x + U t/2, both amplitudes at the u1 positions); static
+    // scatterers stage one set for every tick
+    constexpr int NE = DRIFT ? kCbTicks : 1;
+    __shared__ float2 g0l[2][NE][kCbT], g0v[2][NE][kCbT], gb_l[2][NE][kCbT], gb_v[2][NE][kCbT];   // [u1 / u2][tick][element]
     __shared__ float d0l[2][kCbT][3], d0v[2][kCbT][3], dbl[2][kCbT][3], dbv[2][kCbT][3];
     __shared__ float geo[8];   // d12 (3), back (3), D_b, MT_b
     const int tl = threadIdx.x % kCbT, tv = threadIdx.x / kCbT;
@@ -1028,6 +1032,7 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
     const int t0 = (blockIdx.z % tchunks) * kCbTicks, tn = min(kCbTicks, Nt - t0);
     const int ks = blockIdx.z / tchunks;
     const int kb = ks * P.kchunk, ke = min(P.K, kb + P.kchunk);
+    const int ne = DRIFT ? tn : 1;
     const DevSource* srcl[2] = { &S.src[0], &S.src[2] };
     const DevSource* srcv[2] = { &S.src[1], &S.src[3] };
     // staging role of this thread: group 0 / 1: illumination u1 / u2, 2 / 3: view u1 / u2
@@ -1036,6 +1041,17 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
     const bool isl = grp < 2;
     const int u = grp & 1;
     const int el = min((isl ? l0 : v0) + ge, (isl ? Nl : Nv) - 1);
+    // the staged vector's positions for slot e: the NEE vector at gp, the
+    // amplitude from fa toward fb
+    auto positions = [&](int e, const V3& x, int mx, const V3& y, int my, V3& gp, V3& fa, V3& fb) {
+        gp = x; fa = x; fb = y;
+        if (DRIFT) {
+            const float tau = S.ticks_f[t0 + e];
+            gp = shift_u(S, x, mx, tau, u == 0 ? -1.0f : 1.0f);
+            fa = shift_u(S, x, mx, tau, -1.0f);
+            fb = shift_u(S, y, my, tau, -1.0f);
+        }
+    };
     float2 acc[kCbTicks];
     double accd[kCbTicks][2];
 #pragma unroll
@@ -1047,32 +1063,39 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
         const float4* vq = P.verts + P.offsets[p];
         const float4 v1 = vq[0], v2 = vq[1];
         const V3 x1 = V3{ v1.x, v1.y, v1.z }, x2 = V3{ v2.x, v2.y, v2.z };
-        const int m1 = (int)(__float_as_uint(v1.w) & 15u);
+        const int m1 = (int)(__float_as_uint(v1.w) & 15u), m2 = (int)(__float_as_uint(v2.w) & 15u);
         const float p2inv = 1.0f / P.p2[p];
         __syncthreads();   // the previous path's last vertex is consumed
         if (stager) {
             uint32_t st = 0;
-            if (isl) {
-                const DevSource& s = *srcl[u];
-                const float2 g = gcomplex<ILP>(S, s, el, x1, kRoleIllum, st);
-                if (is_amp64(S, m1)) {   // tabular / vMF: complex amplitude from an FP64 angle
-                    g0l[u][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, x1, x2, false))), u == 0 ? p2inv : 1.0f);
+            for (int e = 0; e < ne; ++e) {
+                V3 gp, fa, fb;
+                positions(e, x1, m1, x2, m2, gp, fa, fb);
+                if (isl) {
+                    const DevSource& s = *srcl[u];
+                    const float2 g = gcomplex<ILP>(S, s, el, gp, kRoleIllum, st);
+                    if (is_amp64(S, m1)) {   // tabular / vMF: complex amplitude from an FP64 angle
+                        g0l[u][e][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, fa, fb, false))), u == 0 ? p2inv : 1.0f);
+                    } else {
+                        const float f = fillum<ILP>(S, s, el, fa, fb, m1);
+                        g0l[u][e][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                    }
                 } else {
-                    const float f = fillum<ILP>(S, s, el, x1, x2, m1);
-                    g0l[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                    const DevSource& s = *srcv[u];
+                    const float2 g = gcomplex<VWP>(S, s, el, gp, kRoleView, st);
+                    if (is_amp64(S, m1)) {   // the view attached at x1 as the reversed path's first end
+                        g0v[u][e][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, fa, fb, true))), u == 0 ? p2inv : 1.0f);
+                    } else {
+                        const float f = fview_entry<VWP>(S, s, el, fa, fb, m1);
+                        g0v[u][e][ge] = c_scale(g, u == 0 ? f * p2inv : f);
+                    }
                 }
-                const V3 d = fsrc_in(s, el, x1);
+            }
+            if (isl) {
+                const V3 d = fsrc_in(*srcl[u], el, x1);
                 d0l[u][ge][0] = d.x; d0l[u][ge][1] = d.y; d0l[u][ge][2] = d.z;
             } else {
-                const DevSource& s = *srcv[u];
-                const float2 g = gcomplex<VWP>(S, s, el, x1, kRoleView, st);
-                if (is_amp64(S, m1)) {   // the view attached at x1 as the reversed path's first end
-                    g0v[u][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, x1, x2, true))), u == 0 ? p2inv : 1.0f);
-                } else {
-                    const float f = fview_entry<VWP>(S, s, el, x1, x2, m1);
-                    g0v[u][ge] = c_scale(g, u == 0 ? f * p2inv : f);
-                }
-                const V3 d = fsrc_out(s, el, x1);
+                const V3 d = fsrc_out(*srcv[u], el, x1);
                 d0v[u][ge][0] = -d.x; d0v[u][ge][1] = -d.y; d0v[u][ge][2] = -d.z;
             }
         }
@@ -1082,33 +1105,40 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
         }
         float MT = 0.0f;
         V3 prev = x1, cur = x1;
+        int mprev = m1, mcur = m1;
         for (uint32_t b = 2; b <= B; ++b) {
             const float4 vb = vq[b - 1];
             const V3 xn = V3{ vb.x, vb.y, vb.z };
             const int mn = (int)(__float_as_uint(vb.w) & 15u);
-            const int mc = (int)(__float_as_uint(vq[b - 2].w) & 15u);
             if (b >= 3) {   // momentum transfer of the inner vertex cur
                 const V3 dq = sub3(funit(sub3(cur, prev)), funit(sub3(xn, cur)));
-                MT += S.D[mc] * dot3(dq, dq);
+                MT += S.D[mcur] * dot3(dq, dq);
             }
-            prev = cur;
-            cur = xn;
+            prev = cur; mprev = mcur;
+            cur = xn; mcur = mn;
             __syncthreads();   // the previous vertex's records are consumed
             if (stager) {
                 uint32_t st = 0;
+                for (int e = 0; e < ne; ++e) {
+                    V3 gp, fa, fb;
+                    positions(e, xn, mn, prev, mprev, gp, fa, fb);
+                    if (isl) {
+                        const DevSource& s = *srcl[u];
+                        const float2 g = gcomplex<ILP>(S, s, el, gp, kRoleIllum, st);
+                        gb_l[u][e][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, fa, fb, false)))
+                                                         : c_scale(g, fillum_exit<ILP>(S, s, el, fa, fb, mn));
+                    } else {
+                        const DevSource& s = *srcv[u];
+                        const float2 g = gcomplex<VWP>(S, s, el, gp, kRoleView, st);
+                        gb_v[u][e][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, fa, fb, true)))
+                                                         : c_scale(g, fview<VWP>(S, s, el, fa, fb, mn));
+                    }
+                }
                 if (isl) {
-                    const DevSource& s = *srcl[u];
-                    const float2 g = gcomplex<ILP>(S, s, el, xn, kRoleIllum, st);
-                    gb_l[u][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, xn, prev, false)))
-                                                  : c_scale(g, fillum_exit<ILP>(S, s, el, xn, prev, mn));
-                    const V3 d = fsrc_in(s, el, xn);
+                    const V3 d = fsrc_in(*srcl[u], el, xn);
                     dbl[u][ge][0] = d.x; dbl[u][ge][1] = d.y; dbl[u][ge][2] = d.z;
                 } else {
-                    const DevSource& s = *srcv[u];
-                    const float2 g = gcomplex<VWP>(S, s, el, xn, kRoleView, st);
-                    gb_v[u][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, xn, prev, true)))
-                                                  : c_scale(g, fview<VWP>(S, s, el, xn, prev, mn));
-                    const V3 d = fsrc_out(s, el, xn);
+                    const V3 d = fsrc_out(*srcv[u], el, xn);
                     dbv[u][ge][0] = -d.x; dbv[u][ge][1] = -d.y; dbv[u][ge][2] = -d.z;
                 }
             }
@@ -1122,20 +1152,25 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
             auto q2 = [&](const float* a, const float* c, int o) {
                 float r = 0.0f;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) { const float e = 0.5f * (a[i] + c[i]) - geo[o + i]; r = fmaf(e, e, r); }
+                for (int i = 0; i < 3; ++i) { const float d = 0.5f * (a[i] + c[i]) - geo[o + i]; r = fmaf(d, d, r); }
                 return r;
             };
             const float D1 = S.D[m1], Db = geo[6];
             const float a2 = S.k2 * (Db * q2(dbl[0][tl], dbv[1][tv], 3) + D1 * q2(d0v[0][tv], d0l[1][tl], 0));
             const float a3 = S.k2 * (Db * q2(dbv[0][tv], dbl[1][tl], 3) + D1 * q2(d0l[0][tl], d0v[1][tv], 0));
             const float a4 = S.k2 * (Db * q2(dbl[0][tl], dbl[1][tl], 3) + D1 * q2(d0v[0][tv], d0v[1][tv], 0));
-            const float2 c2 = c_mul(c_mulc(gb_l[0][tl], gb_v[1][tv]), c_mulc(g0v[0][tv], g0l[1][tl]));
-            const float2 c3 = c_mul(c_mulc(gb_v[0][tv], gb_l[1][tl]), c_mulc(g0l[0][tl], g0v[1][tv]));
-            const float2 c4 = c_mul(c_mulc(gb_l[0][tl], gb_l[1][tl]), c_mulc(g0v[0][tv], g0v[1][tv]));
+            auto terms = [&](int e, float2& c2, float2& c3, float2& c4) {
+                c2 = c_mul(c_mulc(gb_l[0][e][tl], gb_v[1][e][tv]), c_mulc(g0v[0][e][tv], g0l[1][e][tl]));
+                c3 = c_mul(c_mulc(gb_v[0][e][tv], gb_l[1][e][tl]), c_mulc(g0l[0][e][tl], g0v[1][e][tv]));
+                c4 = c_mul(c_mulc(gb_l[0][e][tl], gb_l[1][e][tl]), c_mulc(g0v[0][e][tv], g0v[1][e][tv]));
+            };
+            float2 c2, c3, c4;
+            if (!DRIFT) terms(0, c2, c3, c4);
             const float ptk = S.k2 * geo[7];
 #pragma unroll
             for (int tt = 0; tt < kCbTicks; ++tt) {
                 if (tt >= tn) break;
+                if (DRIFT) terms(tt, c2, c3, c4);
                 const float at = S.abs_ticks[t0 + tt];
                 const float e2 = __expf(-at * a2), e3 = __expf(-at * a3), e4 = __expf(-at * a4);
                 const float w = 0.5f * __expf(-at * ptk);
@@ -1179,13 +1214,13 @@ int launch_cbs_corr(const DevScene& S, const CbsCorrParams& P, cudaStream_t stre
     const int ksplit = (P.K + Q.kchunk - 1) / Q.kchunk;
     dim3 grid((S.src[0].n + kCbT - 1) / kCbT, (S.src[1].n + kCbT - 1) / kCbT, tchunks * ksplit);
     const bool ip = S.src[0].type == SSTMC_SOURCE_POINT, vp = S.src[1].type == SSTMC_SOURCE_POINT;
-    if (ip) {
-        if (vp) cbs_corr_kernel<true, true><<<grid, 256, 0, stream>>>(S, Q);
-        else cbs_corr_kernel<true, false><<<grid, 256, 0, stream>>>(S, Q);
-    } else {
-        if (vp) cbs_corr_kernel<false, true><<<grid, 256, 0, stream>>>(S, Q);
-        else cbs_corr_kernel<false, false><<<grid, 256, 0, stream>>>(S, Q);
-    }
+    using Fn = void (*)(DevScene, CbsCorrParams);
+    const Fn fns[2][2][2] = {
+        { { cbs_corr_kernel<false, false, false>, cbs_corr_kernel<false, false, true> },
+          { cbs_corr_kernel<false, true, false>, cbs_corr_kernel<false, true, true> } },
+        { { cbs_corr_kernel<true, false, false>, cbs_corr_kernel<true, false, true> },
+          { cbs_corr_kernel<true, true, false>, cbs_corr_kernel<true, true, true> } } };
+    fns[ip][vp][S.all_static_corr ? 0 : 1]<<<grid, 256, 0, stream>>>(S, Q);
     return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_KERNEL_ERROR;
 }
 

@@ -192,8 +192,50 @@ def frame_pairs(u: np.ndarray, frames: int) -> np.ndarray:
     return np.where(neg, np.conj(C), C)
 
 
+def _vmf_cell(mus, alphas, amp=0.28209479177387814):
+    """vMF-mixture amplitude cell: lobes alpha_k e^{mu_k (c - 1)} scaled to the
+    3D isotropic amplitude (mixtureC = log(amp) - mu)."""
+    mus = np.asarray(mus, dtype=np.float64)
+    return {"mixtureMu": mus, "mixtureC": np.log(amp) - mus, "mixtureAlpha": np.asarray(alphas, dtype=np.float64)}
+
+
+def confocal_3d(batch_size: int = 1 << 14, full_iteration: int = 1, n_x: int = 8, n_z: int = 8, shifts=(0.0,),
+                seed: int = 0):
+    """Focused Gaussian beams (3D field sampler): a 200 x 200 x 20 slab of four
+    vMF materials (two layers, two halves in x, three forward-peaked lobes
+    each), illumination beams along +z focused on an n_x x n_z grid of the
+    x-z plane (x in [-8, 8], z in [2, 18]) and view beams focused on the same
+    grid shifted along x by each of `shifts`; aperture 0.4, lambda 1.  The
+    shape of a confocal scan: Nl = n_x n_z, Nv = Nl x len(shifts)."""
+    rng = np.random.default_rng(seed)
+    lobes = [([0.0, 1.0, 3.0], [0.5, 0.3, 0.2])] + [
+        ([0.0, float(a), float(b)], [0.2, 0.5, 0.3]) for a, b in zip(rng.uniform(2, 6, 4), rng.uniform(10, 40, 4))]
+    X, Z = np.meshgrid(np.linspace(-8, 8, n_x), np.linspace(2, 18, n_z), indexing="ij")
+    xl, zl = X.ravel(), Z.ravel()
+    xv = np.concatenate([xl + s for s in shifts])
+    zv = np.tile(zl, len(shifts))
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 1.0},
+        "scattering": {"type": ["vMF"] * 5, "amplitudeFunction": [_vmf_cell(m, a) for m, a in lobes]},
+        "medium": {"type": "Heterogeneous", "xAxis": [-100.0, 0.0, 100.0], "yAxis": [-100.0, 100.0],
+                   "zAxis": [0.0, 10.0, 20.0], "materialGrid": np.array([1, 2, 3, 4]).reshape(2, 1, 2, order="F"),
+                   "sigs": [0.0, 0.2, 0.1, 0.25, 0.05], "siga": [0.0, 0.0, 0.0, 0.0, 0.0]},
+        "illumination": {"type": "GaussianBeam", "focalPoint": {"x": xl, "y": np.zeros_like(xl), "z": zl},
+                         "focalDirection": {"x": np.zeros_like(xl), "y": np.zeros_like(xl), "z": np.ones_like(xl)},
+                         "aperture": 0.4},
+        "view": {"type": "GaussianBeam", "focalPoint": {"x": xv, "y": np.zeros_like(xv), "z": zv},
+                 "focalDirection": {"x": np.zeros_like(xv), "y": np.zeros_like(xv), "z": np.ones_like(xv)},
+                 "aperture": 0.4},
+        "sampler": {"type": "TemporalSampler", "t": [0.0], "D": [0.0] * 5,
+                    "U": {"x": [0.0] * 5, "y": [0.0] * 5, "z": [0.0] * 5}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 3
+
+
 WORKLOADS = {
     "speckle_2d": speckle_2d,
+    "confocal_3d": confocal_3d,
     "correlation_3d": correlation_3d,
     "transmission_matrix_3d": transmission_matrix_3d,
     "tracking_2d": tracking_2d,

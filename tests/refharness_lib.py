@@ -82,6 +82,8 @@ def _tokens(pc: cf.PreparedConfig, renderings: int, seed: int) -> str:
     U = rd(c.U, 3 * mat_num)
     out.append(f"motion {mat_num} " + " ".join(f"{float(D[m])!r} {float(U[3 * m])!r} {float(U[3 * m + 1])!r} {float(U[3 * m + 2])!r}"
                                                for m in range(mat_num)))
+    if c.is_cbs:
+        out.append("cbs 1")
     out.append("end")
     return "\n".join(out) + "\n"
 

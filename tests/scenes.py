@@ -556,6 +556,8 @@ def small_scenes():
         "reciprocal_far_3d_vmf_cbs": reciprocal_far_3d_vmf(),
         "edge_one_path_corr_3d": one_path(True),
         "edge_one_path_field_2d": one_path(False),
+        "corr_far_2d_drift_cbs": with_cbs(corr_far_2d_drift()),
+        "vmf_corr_drift_3d_cbs": with_cbs(vmf_corr_drift_3d()),
         "gauss_3d": gauss_beams_3d(),
         "gauss_3d_moving": gauss_beams_3d(moving=True),
         "gauss_3d_iso": gauss_beams_3d(iso=True),

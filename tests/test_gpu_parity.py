@@ -172,16 +172,6 @@ def test_cbs_reciprocity(name, api):
     assert _sym_err(u[..., 0]) < 1e-5
 
 
-def test_cbs_correlation_drift_refused(api):
-    """Correlation CBS is built for static scatterers: drift (U != 0) is refused
-    with SSTMC_NOT_SUPPORTED."""
-    from tests.scenes import with_cbs, corr_far_2d_drift
-    cfg, dims = with_cbs(corr_far_2d_drift())
-    with pytest.raises(api.SstmcError) as ei:
-        api.Scene(cfg, dims)
-    assert ei.value.code == 5
-
-
 def test_wavelength_vector_renders_each_wavelength(api):
     """sstmc2D with a lambda vector: u gains a wavelength axis (Nl, Nv, Nw, Nt, R)
     and each wavelength's slice is the single-wavelength render of the same paths."""

@@ -134,3 +134,21 @@ def test_long_path_segments_field_sampler_match_oracle(api, oracle):
     uo, ito, _ = oracle.render(pc, 23)
     assert it[0] == ito
     assert rel_fro(u[..., 0], uo) <= REL_TOL
+
+
+def test_confocal_shape_matches_oracle(api, oracle):
+    """The focused-beam workload at its full 64 x 64 beam shape on a path
+    subset: integers bit-exact, rows and render within the tolerance."""
+    cfg, dims = wl.confocal_3d(batch_size=128, full_iteration=1)
+    with api.Scene(cfg, dims) as s:
+        g = s.trace_paths(seed=9, first_path=0, paths=128)
+        u, it = s.render(seed=9)
+    pc = cf.prepare(cfg, dims)
+    o = oracle.trace_paths(pc, 9, 0, 128)
+    for k in ("vertices", "vertex_hash", "dda_steps", "misses"):
+        assert np.array_equal(g[k], o[k]), k
+    for k in ("a_ms", "s_ms", "a_ss", "b_ss"):
+        assert rel_fro(g[k], o[k]) <= REL_TOL, k
+    uo, ito, _ = oracle.render(pc, 9)
+    assert it[0] == ito
+    assert rel_fro(u[..., 0], uo) <= REL_TOL

@@ -178,14 +178,23 @@ def test_cbs_reciprocity(oracle, make, corr):
     assert _sym_err(res[False]) > 1e-3
 
 
-def test_cbs_correlation_drift_not_supported(oracle):
-    """Correlation CBS is built for static scatterers: a drifting material (U != 0)
-    is refused by the oracle (and the library)."""
+def test_cbs_correlation_drift_reduces_to_static(oracle):
+    """Correlation CBS with drifting scatterers evaluates its vectors per tick at
+    the displaced positions.  At tick 0 the displacement is zero, so a render
+    of t = [0] equals the same scene with U = 0; with a drift of 1e-7 the
+    renders over several ticks agree with U = 0 to the displacement's order."""
     from tests.scenes import with_cbs, corr_far_2d_drift
     cfg, dims = with_cbs(corr_far_2d_drift())
-    pc = cf.prepare(cfg, dims)
-    with pytest.raises(Exception):
-        oracle.render(pc, 1)
+    static = dict(cfg, sampler=dict(cfg["sampler"], U={"x": [0.0] * 3, "y": [0.0] * 3}))
+    t0 = lambda c: dict(c, sampler=dict(c["sampler"], t=[0.0]))
+    u, it, _ = oracle.render(cf.prepare(t0(cfg), dims), 1)
+    us, its, _ = oracle.render(cf.prepare(t0(static), dims), 1)
+    assert it == its and np.array_equal(u, us)
+    tiny = dict(cfg, sampler=dict(cfg["sampler"], U={"x": [0.0, 1e-7, 0.0], "y": [0.0, 0.0, -1e-7]}))
+    u, it, _ = oracle.render(cf.prepare(tiny, dims), 1)
+    us, its, _ = oracle.render(cf.prepare(static, dims), 1)
+    assert it == its
+    assert np.abs(u - us).max() <= 1e-4 * np.abs(us).max()
 
 
 def _tabular_cfg(dims, table, g_other=0.5):
