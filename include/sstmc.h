@@ -170,9 +170,10 @@ typedef struct sstmc_config {
      * components (0 for the other types), and the components' mixtureMu,
      * mixtureC and mixtureAlpha concatenated in material order.  The
      * amplitude is sum_k alpha_k exp(mu_k cos(theta) + C_k) in 3D; in 2D the
-     * reference scatters a vMF material isotropically.  Refused with
-     * NOT_SUPPORTED: every material isotropic (|g| < 1e-4, all |mu| <= 1e-4)
-     * with a vMF material among them. */
+     * reference scatters a vMF material isotropically.  With every material
+     * isotropic (|g| < 1e-4, all |mu| <= 1e-4) point sources take the
+     * isotropic amplitude and far-field sources the mixture's, as the
+     * reference's sources do. */
     const uint32_t* vmf_n;         /* [scattering_num] or NULL */
     const double* vmf_mu;          /* [sum(vmf_n)] or NULL */
     const double* vmf_c;           /* [sum(vmf_n)] or NULL */

@@ -344,7 +344,7 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
         S->vmf_pf = malloc(sizeof(float) * 3 * vmf_pairs);
         if (!S->vmf_mc || !S->vmf_pd || !S->vmf_pf) return SSTMC_ALLOCATION_ERROR;
     }
-    int iso_m[OM] = { 0 }, any_vmf = 0;
+    int iso_m[OM] = { 0 };
     if (tab_total) {
         S->tab_f = malloc(sizeof(double) * 2 * tab_total);
         S->tab_pdf = malloc(sizeof(double) * tab_total);
@@ -385,7 +385,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
                 if (fabs(mu[k]) > 0.0001) iso = 0;
             }
             if (!(asum > 0.0)) return SSTMC_INVALID_CONFIG;
-            any_vmf = 1;
             if (dims == 3) {   /* 2D: scattered isotropically (Scattering.cuh:899-905, 1093-1100) */
                 voff = (int)vmf_cpos; vpoff = (int)vmf_ppos;
                 o_vmf_tables(mu, cc, al, (uint32_t)vn, S->vmf_mc + 2 * vmf_cpos, S->vmf_pd + 3 * vmf_ppos, S->vmf_pf + 3 * vmf_ppos);
@@ -485,10 +484,6 @@ static int o_build_scene(const sstmc_config* cfg, o_scene* S)
     }
     if (S->src[0].type == SSTMC_SOURCE_NONE || S->src[1].type == SSTMC_SOURCE_NONE) return SSTMC_INVALID_CONFIG;
     S->gauss = S->src[0].type == SSTMC_SOURCE_GAUSSIANBEAM || S->src[1].type == SSTMC_SOURCE_GAUSSIANBEAM;
-    /* all materials isotropic with a vMF among them: point sources would take the
-     * isotropic amplitude and far-field sources the mixture's (not built);
-     * Gaussian beams read the lobes themselves */
-    if (S->iso_all && any_vmf && !S->gauss) return SSTMC_NOT_SUPPORTED;
 
     /* sampler */
     if (!cfg->t || cfg->t_num == 0) return SSTMC_INVALID_CONFIG;

@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
             const bool vary = !scalar_fs && (corr ? S.static_corr[m] == 0 : (S.temporal_amp && S.moving[m]));
             const V3 xp = V3{ x1s[pp][0], x1s[pp][1], x1s[pp][2] };
             const int lg = min(l0 + tl, Nl - 1), vg = min(v0 + tv, Nv - 1);
-            if (is_amp64(S, m)) {
+            if (src_amp64(S, il, m)) {
                 // tabular or vMF scattering: amplitude (FP64 angle) between the
                 // incoming and outgoing directions (FP64, nee.cuh); correlation:
                 // u1 amplitude x conj(u2 amplitude) x the temporal factor

@@ -186,6 +186,16 @@ __device__ __forceinline__ bool is_amp64(const DevScene& S, int m)
     return S.has_amp64 && (S.scat_type[m] == SSTMC_SCATTERING_TABULAR || S.scat_type[m] == SSTMC_SCATTERING_VMF_MIXTURE);
 }
 
+// The amplitude a source attached at a material-m vertex takes from an FP64
+// angle (amp64): a point source in a scene whose materials are all isotropic
+// takes the isotropic amplitude instead, also where a vMF mixture scatters
+// (PointSource.cuh:347-360, 365-399); far-field sources evaluate the mixture
+// (FarField.cuh:546-599).  The pdf of the vertex is the mixture's either way.
+__device__ __forceinline__ bool src_amp64(const DevScene& S, const DevSource& s, int m)
+{
+    return is_amp64(S, m) && !(s.type == SSTMC_SOURCE_POINT && S.iso_all);
+}
+
 // Scattering cosine of source element k attached at pa with the path
 // continuing to pb (threePointFunction, FarField.cuh:546-554,
 // PointSource.cuh:317-345): a far-field direction d (views: -d) against the

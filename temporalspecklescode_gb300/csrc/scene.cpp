@@ -411,7 +411,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
     size_t tab_pos = 0;   // running offset into cfg->tabular_f (entries)
     size_t vmf_pos = 0;   // running offset into cfg->vmf_* (components)
     bool iso_m[kMat] = { false };   // isIsotropicScattering per material (Scattering.cuh:1484-1512)
-    bool any_vmf = false;
     for (int m = 0; m < M; ++m) {
         const int ty = cfg->scattering_type[m];
         const double g = (ty == SSTMC_SCATTERING_HENYEY_GREENSTEIN && cfg->scattering_g) ? cfg->scattering_g[m] : 0.0;
@@ -460,7 +459,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
                 if (std::fabs(mu[k]) > 0.0001) iso = false;
             }
             if (!(asum > 0.0)) return fail(SSTMC_INVALID_CONFIG, "vMF mixtureAlpha must not be all zero");
-            any_vmf = true;
             if (dims == 3) {   // in 2D the reference scatters vMF materials isotropically (Scattering.cuh:899-905, 1093-1100)
                 voff = (int)(S->vmf_mc.size() / 2);
                 vpoff = (int)(S->vmf_pd.size() / 3);
@@ -572,12 +570,6 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         return fail(SSTMC_INVALID_CONFIG, "illumination and view are required");
     S->Nl = S->hsrc[0].n; S->Nv = S->hsrc[1].n;
     D.gauss = (S->hsrc[0].type == SSTMC_SOURCE_GAUSSIANBEAM || S->hsrc[1].type == SSTMC_SOURCE_GAUSSIANBEAM) ? 1 : 0;
-    // With every material isotropic, the reference's point sources take the
-    // isotropic amplitude while its far-field sources evaluate a vMF mixture
-    // (PointSource.cuh:346-430); that split is not built.  Gaussian beams read
-    // the lobes themselves.
-    if (D.iso_all && any_vmf && !D.gauss)
-        return fail(SSTMC_NOT_SUPPORTED, "every material isotropic with a vMF material among them: use Isotropic");
     for (int m = 0; m < kMat; ++m) D.gsigs[m] = sigs[m];
     D.glz = dims == 3 ? bmax[2] - bmin[2] : 0.0;
     D.gk = 2.0 * kPi / cfg->lambda;

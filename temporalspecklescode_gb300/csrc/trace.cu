@@ -550,10 +550,12 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
             // multiple-scattering illumination vector at x2 (NEE.cuh:1525-1559, 889-1009)
             if (b == 2 && T.pass0) {
                 const V3 x12 = funit(sub3(xn, x1));
-                // tabular or vMF first material: amplitudes and pdf from an FP64 angle (nee.cuh)
-                const bool tab1 = is_amp64(S, m1);
+                // tabular or vMF first material: pdf from an FP64 angle (nee.cuh), and
+                // the amplitudes unless point sources take the isotropic one
+                const bool pdf1 = is_amp64(S, m1);
+                const bool tab1 = src_amp64(S, il, m1);
                 float ps = 0.0f;
-                if (tab1) {
+                if (pdf1) {
                     double d12[3];
                     dir64(x1, xn, d12);
                     for (int l = lane; l < Nl; l += 32) {
@@ -668,7 +670,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                 const float ptk = k2 * MT;
                 const float c1base = k2 * S.D[mn];
                 const V3 back = funit(sub3(cur, xn));
-                const bool tabn = is_amp64(S, mn);
+                const bool tabn = src_amp64(S, vw, mn);
                 int j = 0;
                 for (int v = T.v0 + lane % T.vw; v < T.v0 + T.vn; v += T.vw, ++j) {
                     const V3 o1 = fsrc_out(vw, v, xn);
@@ -734,7 +736,7 @@ __global__ void __launch_bounds__(128, 6) trace_kernel(const __grid_constant__ D
                     return T.cbs ? fillum_exit<ILP>(S, il, e, pa, pb, m) : fview<VWP>(S, vw, e, pa, pb, m);
                 };
                 // tabular or vMF vertex material: FP64-angle amplitude, the source attached at x_b
-                const bool tabn = is_amp64(S, mn);
+                const bool tabn = src_amp64(S, T.cbs ? il : vw, mn);
                 auto fxc = [&](int e, const V3& pa, const V3& pb) {
                     return amp64(S, mn, T.cbs ? f3_cos64(il, e, pa, pb, false) : f3_cos64(vw, e, pa, pb, true));
                 };
@@ -1074,7 +1076,7 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
                 if (isl) {
                     const DevSource& s = *srcl[u];
                     const float2 g = gcomplex<ILP>(S, s, el, gp, kRoleIllum, st);
-                    if (is_amp64(S, m1)) {   // tabular / vMF: complex amplitude from an FP64 angle
+                    if (src_amp64(S, s, m1)) {   // tabular / vMF: complex amplitude from an FP64 angle
                         g0l[u][e][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, fa, fb, false))), u == 0 ? p2inv : 1.0f);
                     } else {
                         const float f = fillum<ILP>(S, s, el, fa, fb, m1);
@@ -1083,7 +1085,7 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
                 } else {
                     const DevSource& s = *srcv[u];
                     const float2 g = gcomplex<VWP>(S, s, el, gp, kRoleView, st);
-                    if (is_amp64(S, m1)) {   // the view attached at x1 as the reversed path's first end
+                    if (src_amp64(S, s, m1)) {   // the view attached at x1 as the reversed path's first end
                         g0v[u][e][ge] = c_scale(c_mul(g, amp64(S, m1, f3_cos64(s, el, fa, fb, true))), u == 0 ? p2inv : 1.0f);
                     } else {
                         const float f = fview_entry<VWP>(S, s, el, fa, fb, m1);
@@ -1125,12 +1127,12 @@ __global__ void __launch_bounds__(256) cbs_corr_kernel(const __grid_constant__ D
                     if (isl) {
                         const DevSource& s = *srcl[u];
                         const float2 g = gcomplex<ILP>(S, s, el, gp, kRoleIllum, st);
-                        gb_l[u][e][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, fa, fb, false)))
+                        gb_l[u][e][ge] = src_amp64(S, s, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, fa, fb, false)))
                                                          : c_scale(g, fillum_exit<ILP>(S, s, el, fa, fb, mn));
                     } else {
                         const DevSource& s = *srcv[u];
                         const float2 g = gcomplex<VWP>(S, s, el, gp, kRoleView, st);
-                        gb_v[u][e][ge] = is_amp64(S, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, fa, fb, true)))
+                        gb_v[u][e][ge] = src_amp64(S, s, mn) ? c_mul(g, amp64(S, mn, f3_cos64(s, el, fa, fb, true)))
                                                          : c_scale(g, fview<VWP>(S, s, el, fa, fb, mn));
                     }
                 }

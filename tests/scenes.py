@@ -319,6 +319,24 @@ def reciprocal_far_3d_vmf(cbs: bool = True, batch_size=64, full_iteration=2):
     return with_vmf(reciprocal_far_3d(cbs=cbs, batch_size=batch_size, full_iteration=full_iteration))
 
 
+def vmf_iso_mixed_3d(correlation: bool, batch_size=64, full_iteration=2):
+    """Every material isotropic with vMF mixtures among them (all |mu| <= 1e-4,
+    one mixture not normalised to the isotropic amplitude), point illuminations
+    and far-field views: point sources take the isotropic amplitude, far-field
+    ones the mixture's (PointSource.cuh:347-399, FarField.cuh:546-599)."""
+    cfg, dims = field_point_3d(moving=not correlation, batch_size=batch_size, full_iteration=full_iteration)
+    cfg = dict(cfg)
+    cfg["scattering"] = {"type": ["vMF", "Isotropic", "vMF"],
+                         "amplitudeFunction": [vmf_mixture([0.0], [1.0]), 0.0, vmf_mixture([0.0, 5e-5], [1.0, 0.8])]}
+    th = np.linspace(-0.3, 0.3, 4)
+    cfg["view"] = {"type": "FarField", "direction": {"x": np.sin(th), "y": 0.1 * np.sin(th), "z": np.cos(th)}}
+    if correlation:
+        cfg["illumination2"], cfg["view2"] = cfg["illumination"], cfg["view"]
+        cfg["sampler"] = {"type": "TemporalCorrelationSampler", "t": [0.5, 1.0, 2.0], "D": [0.0, 2e-3, 5e-3],
+                          "U": {"x": [0.0, 0.0, 0.0], "y": [0.0, 0.0, 0.0], "z": [0.0, 0.0, 0.0]}}
+    return cfg, dims
+
+
 def vmf_corr_3d(batch_size=96, full_iteration=2):
     """The bench geometry (correlation sampler, point sources, one cell) with a
     forward-peaked vMF mixture."""
@@ -557,6 +575,8 @@ def small_scenes():
         "edge_one_path_corr_3d": one_path(True),
         "edge_one_path_field_2d": one_path(False),
         "corr_far_2d_drift_cbs": with_cbs(corr_far_2d_drift()),
+        "vmf_iso_point_far_field_3d": vmf_iso_mixed_3d(False),
+        "vmf_iso_point_far_corr_3d": vmf_iso_mixed_3d(True),
         "vmf_corr_drift_3d_cbs": with_cbs(vmf_corr_drift_3d()),
         "gauss_3d": gauss_beams_3d(),
         "gauss_3d_moving": gauss_beams_3d(moving=True),

@@ -217,17 +217,6 @@ def test_vmf_scatters_isotropically_in_2d(api):
     assert np.array_equal(out[0], out[1])
 
 
-def test_vmf_all_isotropic_refused(api):
-    """Every material isotropic with a vMF among them: SSTMC_NOT_SUPPORTED."""
-    from tests.scenes import field_point_3d, vmf_mixture
-    cfg, dims = field_point_3d()
-    cfg = dict(cfg, scattering={"type": ["vMF", "Isotropic", "HG"],
-                                "amplitudeFunction": [vmf_mixture([0.0], [1.0]), 0.0, 0.0]})
-    with pytest.raises(api.SstmcError) as ei:
-        api.Scene(cfg, dims)
-    assert ei.value.code == 5
-
-
 def test_walk_overflow_pool_grows(api, oracle):
     """Paths of hundreds of vertices exhaust the walk's default overflow pool:
     the first render completes them through the replay pass and grows the pool,

@@ -395,18 +395,22 @@ def test_vmf_scatters_isotropically_in_2d(oracle):
     assert np.array_equal(a, b)
 
 
-def test_vmf_all_isotropic_refused(oracle):
-    """Every material isotropic with a vMF among them (all |mu| <= 1e-4) is
-    refused: the reference would give point sources the isotropic amplitude
-    and far-field sources the mixture's."""
-    from tests.scenes import field_point_3d, vmf_mixture
-    cfg, dims = field_point_3d()
-    cfg = dict(cfg, scattering={"type": ["vMF", "Isotropic", "HG"],
-                                "amplitudeFunction": [vmf_mixture([0.0, 5e-5], [1.0, 1.0]), 0.0, 0.0]})
-    with pytest.raises(Exception):
-        oracle.render(cf.prepare(cfg, dims), 1)
-    cfg["scattering"]["amplitudeFunction"][2] = 0.3   # one anisotropic material: accepted
-    oracle.render(cf.prepare(cfg, dims), 1)
+def test_vmf_all_isotropic_amplitude_split(oracle):
+    """Every material isotropic with a vMF among them (all |mu| <= 1e-4): a point
+    source's three-point amplitude is the isotropic one, a far-field source's
+    the mixture's (here twice the isotropic amplitude: two unit-weight lobes),
+    and the single-scattering amplitude follows the illumination's type
+    (PointSource.cuh:347-399, FarField.cuh:546-599)."""
+    from tests.scenes import vmf_iso_mixed_3d, vmf_mixture
+    cfg, dims = vmf_iso_mixed_3d(False)
+    cells = cfg["scattering"]["amplitudeFunction"]
+    cfg["scattering"] = {"type": cfg["scattering"]["type"],
+                         "amplitudeFunction": [cells[0], 0.0, vmf_mixture([0.0, 5e-5], [1.0, 1.0])]}
+    pc = cf.prepare(cfg, dims)
+    iso = 0.282094791773878143
+    assert abs(oracle.amplitude(pc, 2, 0.3) - iso * (1.0 + np.exp(5e-5 * (0.3 - 1.0)))) < 1e-12
+    u, it, _ = oracle.render(pc, 1)
+    assert np.all(np.isfinite(u)) and np.abs(u).max() > 0
 
 
 def test_vmf_config_validation():
