@@ -200,6 +200,7 @@ static int o_prep_farfield(o_src* s, const sstmc_source_cfg* c, int dims,
 }
 
 static double o_vmf_log_norm(double x);
+static double o_vmf_log_norm2(double x);
 static int o_prep_gauss(o_scene* S);
 
 static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const double bmin[3], const double bmax[3])
@@ -210,7 +211,6 @@ static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const do
     if (c->count == 0 || c->xyz == NULL) return SSTMC_INVALID_CONFIG;
     if (c->type == SSTMC_SOURCE_FARFIELD) return o_prep_farfield(s, c, dims, bmin, bmax);
     if (c->type == SSTMC_SOURCE_GAUSSIANBEAM) {
-        if (dims != 3) return SSTMC_NOT_SUPPORTED;   /* 2D beams need the complex Bessel I0 (not built) */
         if (!c->focal_direction || !(c->aperture > 0.0) || !isfinite(c->aperture)) return SSTMC_INVALID_CONFIG;
         s->gdir = calloc((size_t)s->n * 3, sizeof(float));
         if (!s->gdir) return SSTMC_ALLOCATION_ERROR;
@@ -222,7 +222,8 @@ static int o_prep_source(o_src* s, const sstmc_source_cfg* c, int dims, const do
         }
         /* GaussianBeam.cuh:1056-1068: ga = 1 / aperture^2, the aperture normalised */
         s->ga = 1.0 / (c->aperture * c->aperture);
-        s->gnorm = o_vmf_log_norm(s->ga);
+        s->gnorm = dims == 3 ? o_vmf_log_norm(s->ga) : o_vmf_log_norm2(s->ga);
+        if (dims == 2) for (int k = 0; k < s->n; ++k) s->gdir[3 * k + 2] = 0.0f;
     } else if (c->type != SSTMC_SOURCE_POINT) {
         return SSTMC_NOT_SUPPORTED;
     }
@@ -775,7 +776,7 @@ static void o_sample_source(const o_scene* S, const o_src* src, o_stream* rs, fl
     int l = (int)ceilf(o_uniform(rs) * (float)src->n) - 1;
     if (l < 0) l = 0;
     if (l > src->n - 1) l = src->n - 1;
-    if (src->type == SSTMC_SOURCE_POINT) {
+    if (src->type != SSTMC_SOURCE_FARFIELD) {   /* point sources, and 2D beams from their focal points */
         for (int i = 0; i < 3; ++i) x0[i] = src->p[3 * l + i];
         o_random_direction(D, rs, d0);
         return;
@@ -996,7 +997,10 @@ static oc o_gauss_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, 
 
 static double o_pfirst(const o_scene* S, const o_src* s, int l, const float x[3], uint64_t* steps)
 {
-    if (s->type == SSTMC_SOURCE_GAUSSIANBEAM) return o_gauss_pfirst(S, s, l, x, o_inside(S, x) ? S->grid[o_cell(S, x)] : 0);
+    /* 3D beams from their tables; 2D beams as point sources at their focal
+     * points (GaussianBeam.cuh:1820-1841, probabilityPointNormalizeKernel :775-793) */
+    if (s->type == SSTMC_SOURCE_GAUSSIANBEAM && S->dims == 3)
+        return o_gauss_pfirst(S, s, l, x, o_inside(S, x) ? S->grid[o_cell(S, x)] : 0);
     if (s->type == SSTMC_SOURCE_FARFIELD) {
         float df[3] = { -s->p[3 * l], -s->p[3 * l + 1], -s->p[3 * l + 2] };
         double dd[3] = { df[0], df[1], df[2] };
@@ -1173,6 +1177,70 @@ static inline void o_gthroughput(const o_src* s, int l, const double x[3], doubl
         T[i].re = (double)s->gdir[3 * l + i] * s->ga;
         T[i].im = k * (x[i] - (double)s->p[3 * l + i]);
     }
+}
+
+/* Complex modified Bessel function I0 (SpecialFunctions.cuh:42-178, besseli with
+ * nu = 0): the power series sum_k ((z/2)^2)^k / (k!)^2 to k = 20 for |z| < 5
+ * (the limit 3 + 2 sqrt(nu + 1)), else I0(z) = J0(iz) in the modulus-phase
+ * asymptotic form of Abramowitz & Stegun 9.2.28-9.2.31 (y = iz, mu = 4 nu^2 = 0):
+ * J0(y) = M cos(theta), M^2 = (2 / pi y) sum_k c_k prod_j (mu - (2j - 1)^2) / (2y)^(2k)
+ * with c_k = (2k - 1)!! / (2k)!! up to k = 10, stopping once |(2y)^(2k)| or the
+ * product exceeds 1e20, and theta = y - pi/4 + four terms in 1 / (4y).  I0(0) = 1
+ * (the reference's form evaluates 0 log 0 there). */
+static oc o_bessel_i0(oc z)
+{
+    double az = oc_abs(z);
+    if (az == 0.0) { oc one = { 1.0, 0.0 }; return one; }
+    if (az < 5.0) {
+        oc h = { 0.5 * z.re, 0.5 * z.im };
+        oc Y = { (h.re - h.im) * (h.re + h.im), 2.0 * h.re * h.im };
+        oc Bk = { 1.0, 0.0 }, res = { 1.0, 0.0 };
+        for (int k = 1; k <= 20; ++k) {
+            double d = (double)k * (double)k;
+            oc Zk = { Y.re / d, Y.im / d };
+            Bk = oc_mul(Zk, Bk);
+            res = oc_add(res, Bk);
+        }
+        return res;
+    }
+    const double mu = 0.0;
+    oc y = { -z.im, z.re };                              /* i z */
+    oc den = { 4.0 * y.re, 4.0 * y.im };
+    oc den2 = oc_mul(den, den);
+    oc th = { y.re - 0.25 * O_PI, y.im };
+    const double tc[4] = { (mu - 1.0) / 2.0, (mu - 1.0) * (mu - 25.0) / 6.0,
+                           (mu - 1.0) * (mu * mu - 114.0 * mu + 1073.0) / 5.0,
+                           (mu - 1.0) * (5.0 * mu * mu * mu - 1535.0 * mu * mu + 54703.0 * mu - 375733.0) / 14.0 };
+    for (int i = 0; i < 4; ++i) {
+        oc one = { tc[i], 0.0 };
+        th = oc_add(th, oc_div(one, den));
+        den = oc_mul(den, den2);
+    }
+    oc ct = { cos(th.re) * cosh(th.im), -sin(th.re) * sinh(th.im) };
+    oc M2 = { 1.0, 0.0 };
+    oc t2 = { 2.0 * y.re, 2.0 * y.im };
+    oc tq = oc_mul(t2, t2), tq1 = tq;
+    double mm = mu - 1.0, ck = 1.0;
+    for (int k = 1; k <= 10; ++k) {
+        ck = ck * (2.0 * k - 1.0) / (2.0 * k);
+        oc num = { ck * mm, 0.0 };
+        M2 = oc_add(M2, oc_div(num, tq));
+        tq = oc_mul(tq, tq1);
+        mm *= mu - (2.0 * k + 1.0) * (2.0 * k + 1.0);
+        if (oc_abs(tq) > 1e20 || mm > 1e20) break;
+    }
+    oc q = oc_div(M2, y);
+    q.re *= 2.0 / O_PI; q.im *= 2.0 / O_PI;
+    return oc_mul(oc_sqrt(q), ct);
+}
+
+static inline oc oc_log(oc a) { oc r = { log(oc_abs(a)), atan2(a.im, a.re) }; return r; }
+
+/* vMFnormalizationLog in 2D (SpecialFunctions.cuh:187-203): -log(2 pi) - log I0(x) */
+static double o_vmf_log_norm2(double x)
+{
+    oc z = { x, 0.0 };
+    return -log(2.0 * O_PI) - log(oc_abs(o_bessel_i0(z)));
 }
 
 /* Lobe-pair proposal of the second direction for beam l at x1 (computeCdfBuffer,
@@ -1388,7 +1456,8 @@ static oc o_gauss_f(const o_scene* S, const o_src* s, int k, const float pa[3], 
     for (int i = 0; i < S->gmix_n[m]; ++i) {
         oc lnu = { tc + mix[2 * i + 1], 0.0 };
         oc sm = oc_sqrt(o_gsumsq(mix[2 * i], w0, T));
-        if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) acc.re += 2.0 * exp(lnu.re);
+        if (S->dims == 2) acc = oc_add(acc, oc_exp(oc_add(oc_log(o_bessel_i0(sm)), lnu)));
+        else if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) acc.re += 2.0 * exp(lnu.re);
         else acc = oc_add(acc, oc_div(oc_2sinh(sm, lnu), sm));
     }
     return acc;
@@ -1438,9 +1507,13 @@ static oc o_gauss_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, 
             c = oc_mul(g0, aw);
             c.re *= -ra; c.im *= -ra;
         }
+        oc cl = oc_add(c, lnu);
+        if (S->dims == 2) {
+            acc = oc_add(acc, oc_exp(oc_add(oc_add(oc_log(o_bessel_i0(C)), oc_log(o_bessel_i0(sm))), cl)));
+            continue;
+        }
         int sbig = fabs(sm.re) > 0.0001 || fabs(sm.im) > 0.0001;
         int cbig = fabs(C.re) > 0.0001 || fabs(C.im) > 0.0001;
-        oc cl = oc_add(c, lnu);
         if (sbig && cbig) {
             acc = oc_add(acc, oc_div(oc_2sinh(oc_add(C, sm), cl), oc_mul(C, sm)));
         } else if (!sbig && !cbig) {
@@ -1468,10 +1541,10 @@ static int o_prep_gauss(o_scene* S)
     o_src* il = &S->src[0];
     o_src* vw = &S->src[1];
     if (il->type != SSTMC_SOURCE_GAUSSIANBEAM || vw->type != SSTMC_SOURCE_GAUSSIANBEAM) return SSTMC_NOT_SUPPORTED;
-    if (S->correlation || S->cbs || S->dims != 3) return SSTMC_NOT_SUPPORTED;
+    if (S->correlation || S->cbs) return SSTMC_NOT_SUPPORTED;
     for (int m = 0; m < OM; ++m)
-        if (S->scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && S->scat_type[m] != SSTMC_SCATTERING_VMF_MIXTURE)
-            return SSTMC_NOT_SUPPORTED;
+        if (S->gmix_n[m] == 0 && S->scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED) return SSTMC_NOT_SUPPORTED;
+    if (S->dims == 2) return SSTMC_NO_ERROR;   /* 2D beams sample and weigh as point sources: no tables */
     double mv[3] = { 0, 0, 0 }, inv = 1.0 / vw->n;
     for (int v = 0; v < vw->n; ++v) for (int a = 0; a < 3; ++a) mv[a] = mv[a] + inv * (double)vw->gdir[3 * v + a];
     double r = sqrt(mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]);
@@ -1683,7 +1756,7 @@ static int o_walk(const o_scene* S, uint64_t seed, uint32_t pid, int u1side, o_v
     uint32_t att;
     o_stream rs;
     int beam = 0;
-    const int gauss = first->type == SSTMC_SOURCE_GAUSSIANBEAM;
+    const int gauss = first->type == SSTMC_SOURCE_GAUSSIANBEAM && S->dims == 3;
     for (att = 0; att < O_MAX_ATTEMPTS; ++att) {
         o_stream_init(&rs, seed, pid, 1u, O_PURPOSE_WALK | (att << 8));
         if (gauss) {
@@ -1936,7 +2009,7 @@ static void o_nee(const o_scene* S, const o_verts* V, o_work* W, oc* Vacc, uint6
         double x12[3]; o_dir64(x1, x2, x12);
         double p2 = 0;
         for (int l = 0; l < Nl; ++l) {
-            if (il->type == SSTMC_SOURCE_GAUSSIANBEAM) {
+            if (il->type == SSTMC_SOURCE_GAUSSIANBEAM && D == 3) {
                 /* a zero product is replaced by 1e20 (GaussianBeam.cuh:745-751) */
                 double q = W->P1[l] * (S->iso_all ? O_ISO_PDF3 : o_gauss_pw(S, il, l, x1, x2));
                 p2 += q == 0.0 ? 1e20 : q;
@@ -2402,4 +2475,11 @@ int32_t oracle_gauss_sample(const sstmc_config* cfg, uint64_t seed, uint32_t n, 
     }
     o_free_scene(&S);
     return err;
+}
+
+void oracle_bessel_i0(double re, double im, double* out_re, double* out_im)
+{
+    oc z = { re, im };
+    oc r = o_bessel_i0(z);
+    *out_re = r.re; *out_im = r.im;
 }

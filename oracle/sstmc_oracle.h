@@ -68,6 +68,9 @@ int32_t oracle_gauss_terms(const sstmc_config* cfg, int32_t l, int32_t v, const 
 int32_t oracle_gauss_sample(const sstmc_config* cfg, uint64_t seed, uint32_t n, const float* x1_fixed, int32_t beam_fixed,
                             float* xyz, int32_t* mat, int32_t* beam, float* dir);
 
+/* The complex modified Bessel function I0 of the 2D beam amplitudes. */
+void oracle_bessel_i0(double re, double im, double* out_re, double* out_im);
+
 /* Portable FP32 math of the decision path, for bit-level tests. */
 float oracle_logf(float x);
 void oracle_sincospif(float x, float* s, float* c);

@@ -1,4 +1,6 @@
-// gauss.cuh -- focused Gaussian-beam sources in 3D (GaussianBeam.cuh).
+// gauss.cuh -- focused Gaussian-beam sources (GaussianBeam.cuh).  3D beams
+// sample from their own tables; 2D beams sample and weigh as point sources at
+// their focal points, with Bessel-I0 amplitudes.
 //
 //   first vertex from a beam        GaussianBeam.cuh:357-418 (sampleFirstBeam)
 //   first-point probability P_l     GaussianBeam.cuh:420-487
@@ -71,6 +73,57 @@ __device__ __forceinline__ CD cd_2sinh(CD z, CD c)
     if (p.re > -10.0) r = cd_add(r, cd_exp(p));
     if (n.re > -10.0) r = cd_sub(r, cd_exp(n));
     return r;
+}
+
+__device__ __forceinline__ CD cd_log(CD a) { return CD{ log(cd_abs(a)), atan2(a.im, a.re) }; }
+
+// Complex modified Bessel function I0 by the reference's algorithm
+// (SpecialFunctions.cuh:42-178, besseli with nu = 0): the power series
+// sum_k ((z/2)^2)^k / (k!)^2 to k = 20 for |z| < 5, else J0(iz) in the
+// modulus-phase asymptotic form of Abramowitz & Stegun 9.2.28-9.2.31 (the
+// modulus series to k = 10, stopping once |(2y)^(2k)| or the coefficient
+// product exceeds 1e20; four phase terms).  I0(0) = 1.
+__device__ inline CD bessel_i0(CD z)
+{
+    const double az = cd_abs(z);
+    if (az == 0.0) return CD{ 1.0, 0.0 };
+    if (az < 5.0) {
+        const CD h{ 0.5 * z.re, 0.5 * z.im };
+        const CD Y{ (h.re - h.im) * (h.re + h.im), 2.0 * h.re * h.im };
+        CD Bk{ 1.0, 0.0 }, res{ 1.0, 0.0 };
+        for (int k = 1; k <= 20; ++k) {
+            const double d = (double)k * (double)k;
+            Bk = cd_mul(CD{ Y.re / d, Y.im / d }, Bk);
+            res = cd_add(res, Bk);
+        }
+        return res;
+    }
+    const CD y{ -z.im, z.re };   // i z
+    CD den{ 4.0 * y.re, 4.0 * y.im };
+    const CD den2 = cd_mul(den, den);
+    CD th{ y.re - 0.25 * kPi, y.im };
+    const double tc[4] = { -1.0 / 2.0, 25.0 / 6.0, -1073.0 / 5.0, 375733.0 / 14.0 };
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        th = cd_add(th, cd_div(CD{ tc[i], 0.0 }, den));
+        den = cd_mul(den, den2);
+    }
+    const CD ct{ cos(th.re) * cosh(th.im), -sin(th.re) * sinh(th.im) };
+    CD M2{ 1.0, 0.0 };
+    const CD t2{ 2.0 * y.re, 2.0 * y.im };
+    CD tq = cd_mul(t2, t2);
+    const CD tq1 = tq;
+    double mm = -1.0, ck = 1.0;
+    for (int k = 1; k <= 10; ++k) {
+        ck = ck * (2.0 * k - 1.0) / (2.0 * k);
+        M2 = cd_add(M2, cd_div(CD{ ck * mm, 0.0 }, tq));
+        tq = cd_mul(tq, tq1);
+        mm *= -(2.0 * k + 1.0) * (2.0 * k + 1.0);
+        if (cd_abs(tq) > 1e20 || mm > 1e20) break;
+    }
+    CD q = cd_div(M2, y);
+    q.re *= 2.0 / kPi; q.im *= 2.0 / kPi;
+    return cd_mul(cd_sqrt(q), ct);
 }
 
 // sum_i (a v_i + T_i)^2 over the three axes (a, v real; T complex)
@@ -320,7 +373,8 @@ __device__ inline CD gauss_f(const DevScene& S, const DevSource& s, int k, const
     for (int i = 0; i < S.gmix_n[m]; ++i) {
         const CD lnu{ tc + mix[2 * i + 1], 0.0 };
         const CD sm = cd_sqrt(g_sumsq(mix[2 * i], w0, T));
-        if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) acc.re += 2.0 * exp(lnu.re);
+        if (S.dims == 2) acc = cd_add(acc, cd_exp(cd_add(cd_log(bessel_i0(sm)), lnu)));
+        else if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) acc.re += 2.0 * exp(lnu.re);
         else acc = cd_add(acc, cd_div(cd_2sinh(sm, lnu), sm));
     }
     return acc;
@@ -371,9 +425,13 @@ __device__ inline CD gauss_fs(const DevScene& S, const DevSource& il, int l, con
             c = cd_mul(g0, aw);
             c.re = dM(c.re, -ra); c.im = dM(c.im, -ra);
         }
+        const CD cl = cd_add(c, lnu);
+        if (S.dims == 2) {
+            acc = cd_add(acc, cd_exp(cd_add(cd_add(cd_log(bessel_i0(C)), cd_log(bessel_i0(sm))), cl)));
+            continue;
+        }
         const bool sbig = fabs(sm.re) > 0.0001 || fabs(sm.im) > 0.0001;
         const bool cbig = fabs(C.re) > 0.0001 || fabs(C.im) > 0.0001;
-        const CD cl = cd_add(c, lnu);
         if (sbig && cbig) {
             acc = cd_add(acc, cd_div(cd_2sinh(cd_add(C, sm), cl), cd_mul(C, sm)));
         } else if (!sbig && !cbig) {

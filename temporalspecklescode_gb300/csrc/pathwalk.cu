@@ -293,7 +293,7 @@ static bool has_vmf(const DevScene& S) { return S.vmf_pf != nullptr; }
 template <int MODE>
 static void walk_launch(const DevScene& S, const WalkParams& W, int blocks, cudaStream_t stream)
 {
-    if (S.gauss) walk_kernel<MODE, true, true><<<blocks, 128, 0, stream>>>(S, W);
+    if (S.gauss && S.dims == 3) walk_kernel<MODE, true, true><<<blocks, 128, 0, stream>>>(S, W);
     else if (has_vmf(S)) walk_kernel<MODE, true, false><<<blocks, 128, 0, stream>>>(S, W);
     else walk_kernel<MODE, false, false><<<blocks, 128, 0, stream>>>(S, W);
 }

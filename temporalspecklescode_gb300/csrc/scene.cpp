@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 
 namespace sstmc {
@@ -111,7 +112,6 @@ int prep_source(Scene::HostSource* s, const sstmc_source_cfg* c, int dims, const
     if (c->type == SSTMC_SOURCE_GAUSSIANBEAM) {
         // focal points in p, beam directions as given, ga = 1 / aperture^2
         // (GaussianBeam.cuh:1056-1068); the tables follow in prep_gauss
-        if (dims != 3) return SSTMC_NOT_SUPPORTED;
         if (!c->focal_direction || !(c->aperture > 0.0) || !std::isfinite(c->aperture)) return SSTMC_INVALID_CONFIG;
         s->gdir.resize(3 * s->n);
         for (int k = 0; k < 3 * s->n; ++k) s->gdir[k] = (float)c->focal_direction[k];
@@ -121,6 +121,7 @@ int prep_source(Scene::HostSource* s, const sstmc_source_cfg* c, int dims, const
                 return SSTMC_INVALID_CONFIG;
         }
         s->ga = 1.0 / (c->aperture * c->aperture);
+        if (dims == 2) for (int k = 0; k < s->n; ++k) s->gdir[3 * k + 2] = 0.0f;
     } else if (c->type != SSTMC_SOURCE_POINT) {
         return SSTMC_NOT_SUPPORTED;
     }
@@ -189,6 +190,45 @@ static double vmf_log_norm(double x)
     if (x < 5.0) return std::log(x) - std::log(4.0 * kPi * std::sinh(x));
     return std::log(x) - std::log(2.0 * kPi) - x;
 }
+
+// |I0(x)| of a real x >= 0, the modified Bessel function by the reference's
+// algorithm (SpecialFunctions.cuh:42-178): the power series to k = 20 below 5,
+// else the modulus-phase asymptotic form of J0(ix) (Abramowitz & Stegun
+// 9.2.28-9.2.31), on the real axis where that form holds.
+static double bessel_i0_real(double x)
+{
+    if (x == 0.0) return 1.0;
+    if (x < 5.0) {
+        const double Y = (0.5 * x) * (0.5 * x);
+        double Bk = 1.0, res = 1.0;
+        for (int k = 1; k <= 20; ++k) { Bk = (Y / ((double)k * (double)k)) * Bk; res += Bk; }
+        return res;
+    }
+    // J0(y), y = i x: M cos(theta), the phase and modulus series in y
+    const std::complex<double> y(0.0, x);
+    std::complex<double> den = 4.0 * y;
+    const std::complex<double> den2 = den * den;
+    std::complex<double> th = y - 0.25 * kPi;
+    const double tc[4] = { -1.0 / 2.0, 25.0 / 6.0, -1073.0 / 5.0, 375733.0 / 14.0 };
+    for (int i = 0; i < 4; ++i) { th += tc[i] / den; den *= den2; }
+    const std::complex<double> ct(std::cos(th.real()) * std::cosh(th.imag()), -std::sin(th.real()) * std::sinh(th.imag()));
+    std::complex<double> M2(1.0, 0.0);
+    const std::complex<double> t2 = 2.0 * y;
+    std::complex<double> tq = t2 * t2;
+    const std::complex<double> tq1 = tq;
+    double mm = -1.0, ck = 1.0;
+    for (int k = 1; k <= 10; ++k) {
+        ck = ck * (2.0 * k - 1.0) / (2.0 * k);
+        M2 += ck * mm / tq;
+        tq *= tq1;
+        mm *= -(2.0 * k + 1.0) * (2.0 * k + 1.0);
+        if (std::abs(tq) > 1e20 || mm > 1e20) break;
+    }
+    return std::abs(std::sqrt((2.0 / kPi) * (M2 / y)) * ct);
+}
+
+// vMFnormalizationLog in 2D (SpecialFunctions.cuh:187-203): -log(2 pi) - log I0(x)
+static double vmf_log_norm2(double x) { return -std::log(2.0 * kPi) - std::log(bessel_i0_real(x)); }
 
 // Tables of one 3D vMF mixture (Scattering.cuh:636-774): the amplitude's
 // components (mu_k, C_k + log alpha_k); the pdf's component pairs j = k1 + N k2
@@ -284,11 +324,12 @@ static int prep_gauss(Scene* S, bool cbs)
     Scene::HostSource& il = S->hsrc[0];
     Scene::HostSource& vw = S->hsrc[1];
     if (il.type != SSTMC_SOURCE_GAUSSIANBEAM || vw.type != SSTMC_SOURCE_GAUSSIANBEAM) return SSTMC_NOT_SUPPORTED;
-    if (S->correlation || cbs || S->dims != 3) return SSTMC_NOT_SUPPORTED;
+    if (S->correlation || cbs) return SSTMC_NOT_SUPPORTED;
     for (int m = 0; m < kMat; ++m)
-        if (D.scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED && D.scat_type[m] != SSTMC_SCATTERING_VMF_MIXTURE) return SSTMC_NOT_SUPPORTED;
-    il.gnorm = vmf_log_norm(il.ga);
-    vw.gnorm = vmf_log_norm(vw.ga);
+        if (D.gmix_n[m] == 0 && D.scat_type[m] != SSTMC_SCATTERING_NOT_DEFINED) return SSTMC_NOT_SUPPORTED;
+    il.gnorm = S->dims == 3 ? vmf_log_norm(il.ga) : vmf_log_norm2(il.ga);
+    vw.gnorm = S->dims == 3 ? vmf_log_norm(vw.ga) : vmf_log_norm2(vw.ga);
+    if (S->dims == 2) return SSTMC_NO_ERROR;   // 2D beams sample and weigh as point sources: no tables
     double mv[3] = { 0, 0, 0 };
     const double inv = 1.0 / vw.n;
     for (int v = 0; v < vw.n; ++v)

@@ -843,7 +843,7 @@ __global__ void __launch_bounds__(128) gauss_trace_kernel(const __grid_constant_
     extern __shared__ double smem_d[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n, D = S.dims;
     const bool split = S.precision == SSTMC_PRECISION_SPLIT;
     double* Ls = smem_d + (size_t)wib * Nt;
     float* fb = reinterpret_cast<float*>(smem_d + (size_t)nwb * Nt) + (size_t)wib * 9 * Nt;
@@ -877,9 +877,10 @@ __global__ void __launch_bounds__(128) gauss_trace_kernel(const __grid_constant_
         uint32_t steps = 0;
 
         // first vertex: P_l, p1, the illumination and single-scattering rows
+        // 3D beams from their tables; 2D beams as point sources at their focal points
         double ps = 0.0;
         for (int l = lane; l < Nl; l += 32) {
-            const double P = gauss_pfirst(S, il, l, x1, m1);
+            const double P = D == 3 ? gauss_pfirst(S, il, l, x1, m1) : (double)pfirst_t<true>(S, il, l, x1, steps);
             T.pl[(size_t)q * Nl + l] = (float)P;
             ps += P;
         }
@@ -938,6 +939,10 @@ __global__ void __launch_bounds__(128) gauss_trace_kernel(const __grid_constant_
             if (b == 2) {
                 double qs = 0.0;
                 for (int l = lane; l < Nl; l += 32) {
+                    if (D == 2) {   // the point-source form: the pdf of the scattering angle at x1
+                        qs += (double)T.pl[(size_t)q * Nl + l] * (double)pdf_fast(S, m1, fsrc_in(il, l, x1), funit(sub3(xn, x1)));
+                        continue;
+                    }
                     const double P = gauss_pfirst(S, il, l, x1, m1);
                     const double pw = S.iso_all ? 0.079577471545947668 : gauss_pw(S, il, l, x1, xn);
                     const double qq = P * pw;

@@ -233,7 +233,7 @@ __device__ inline void sample_source(const DevScene& S, const DevSource& src, St
     const int D = S.dims;
     int l = (int)ceilf(fm(rs.uniform(), (float)src.n)) - 1;
     l = l < 0 ? 0 : (l > src.n - 1 ? src.n - 1 : l);
-    if (src.type == SSTMC_SOURCE_POINT) {
+    if (src.type != SSTMC_SOURCE_FARFIELD) {   // point sources, and 2D beams from their focal points
         x0 = load3(src.p, l);
         d0 = random_direction(D, rs);
         return;

@@ -55,6 +55,8 @@ class Oracle:
         L.oracle_gauss_terms.restype = C.c_int32
         L.oracle_gauss_sample.argtypes = [C.POINTER(cf.SstmcConfig), C.c_uint64, C.c_uint32, fp, C.c_int32, fp, ip, ip, fp]
         L.oracle_gauss_sample.restype = C.c_int32
+        L.oracle_bessel_i0.argtypes = [C.c_double, C.c_double, dp, dp]
+        L.oracle_bessel_i0.restype = None
 
     def render(self, pc: cf.PreparedConfig, seed: int, first_wave: int = 0, waves: int | None = None, threads: int = 0):
         m = pc.meta
@@ -163,3 +165,8 @@ class Oracle:
         if e:
             raise RuntimeError(f"oracle_gauss_sample failed: {e}")
         return xyz, mat, b, d
+
+    def bessel_i0(self, z: complex) -> complex:
+        re, im = C.c_double(), C.c_double()
+        self.lib.oracle_bessel_i0(z.real, z.imag, C.byref(re), C.byref(im))
+        return complex(re.value, im.value)

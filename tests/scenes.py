@@ -528,6 +528,31 @@ def gauss_beams_3d(moving: bool = False, iso: bool = False, tilted: bool = False
     return cfg, 3
 
 
+def gauss_beams_2d(moving: bool = False, n_l: int = 3, n_v: int = 4, batch_size=64, full_iteration=2):
+    """Focused Gaussian beams in 2D (field sampler): beams act as point sources
+    at their focal points, with the Bessel-I0 amplitudes of the vMF lobes (the
+    walk scatters vMF materials isotropically in 2D)."""
+    cells = [vmf_mixture([0.0], [1.0]), vmf_mixture([0.0, 3.0], [0.5, 0.5]), vmf_mixture([0.0, 1.5, 6.0], [0.4, 0.4, 0.2])]
+    xl = np.linspace(-1.5, 1.5, n_l)
+    xv = np.linspace(-2.0, 2.0, n_v)
+    cfg = {
+        "simulation": {"batchSize": batch_size, "fullIteration": full_iteration, "lambda": 0.8},
+        "scattering": {"type": ["vMF"] * 3, "amplitudeFunction": cells},
+        "medium": {"type": "Heterogeneous", "xAxis": [-12.0, 0.0, 12.0], "yAxis": [0.0, 4.0, 10.0],
+                   "materialGrid": np.array([[1, 2], [2, 1]], dtype=np.uint32), "sigs": [0.0, 0.25, 0.15],
+                   "siga": [0.0, 0.01, 0.0]},
+        "illumination": {"type": "GaussianBeam", "focalPoint": {"x": xl, "y": np.full(n_l, 3.0)},
+                         "focalDirection": {"x": np.zeros(n_l), "y": np.ones(n_l)}, "aperture": 0.4},
+        "view": {"type": "GaussianBeam", "focalPoint": {"x": xv, "y": np.full(n_v, 5.0)},
+                 "focalDirection": {"x": np.full(n_v, 0.28), "y": np.full(n_v, 0.96)}, "aperture": 0.5},
+        "sampler": {"type": "TemporalSampler", "t": [0.0, 0.5, 1.0] if moving else [0.0],
+                    "D": [0.0, 0.02 if moving else 0.0, 0.0],
+                    "U": {"x": [0.0, 0.3 if moving else 0.0, 0.0], "y": [0.0, 0.0, 0.0]}},
+        "tracer": {"type": "nee"},
+    }
+    return cfg, 2
+
+
 def small_scenes():
     """name -> (config, dims)"""
     return {
@@ -578,6 +603,8 @@ def small_scenes():
         "vmf_iso_point_far_field_3d": vmf_iso_mixed_3d(False),
         "vmf_iso_point_far_corr_3d": vmf_iso_mixed_3d(True),
         "vmf_corr_drift_3d_cbs": with_cbs(vmf_corr_drift_3d()),
+        "gauss_2d": gauss_beams_2d(),
+        "gauss_2d_moving": gauss_beams_2d(moving=True),
         "gauss_3d": gauss_beams_3d(),
         "gauss_3d_moving": gauss_beams_3d(moving=True),
         "gauss_3d_iso": gauss_beams_3d(iso=True),

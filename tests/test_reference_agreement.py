@@ -47,6 +47,8 @@ def _scenes():
         "transmission_3d": (far3d, 3, "field"),
         # 3D focused Gaussian beams in a two-material vMF slab (two lobes per material)
         "gauss_3d": (scenes.gauss_beams_3d(batch_size=1024, full_iteration=16, n_l=4, n_v=6, equal_lobes=True)[0], 3, "field"),
+        # 2D focused Gaussian beams (point-source sampling, Bessel-I0 amplitudes)
+        "gauss_2d": (scenes.gauss_beams_2d(batch_size=1024, full_iteration=8)[0], 2, "field"),
         # 2D correlation with coherent backscattering and drifting scatterers (U != 0)
         "corr_drift_cbs_2d": (scenes.with_cbs(scenes.corr_far_2d_drift(batch_size=1024, full_iteration=4))[0], 2,
                               "correlation"),
