@@ -998,7 +998,7 @@ static oc o_gauss_fs(const o_scene* S, const o_src* il, int l, const o_src* vw, 
 static double o_pfirst(const o_scene* S, const o_src* s, int l, const float x[3], uint64_t* steps)
 {
     /* 3D beams from their tables; 2D beams as point sources at their focal
-     * points (GaussianBeam.cuh:1820-1841, probabilityPointNormalizeKernel :775-793) */
+     * points (GaussianBeam.cuh:1812-1832, probabilityPointNormalizeKernel :775-793) */
     if (s->type == SSTMC_SOURCE_GAUSSIANBEAM && S->dims == 3)
         return o_gauss_pfirst(S, s, l, x, o_inside(S, x) ? S->grid[o_cell(S, x)] : 0);
     if (s->type == SSTMC_SOURCE_FARFIELD) {
