@@ -446,9 +446,10 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 sI[2 * r] = make_float4(dir.x, dir.x, dir.y, dir.y);
                 sI[2 * r + 1] = make_float4(dir.z, dir.z, w, w);
             } else {
+                // -2 out, so that q^2 = 2 + (-2 out) . in
                 const V3 dir = fsrc_out(vw, min(v0 + c, Nv - 1), x);
                 float* o = sO + (size_t)pp * 4 * kFv + c;
-                o[0] = dir.x; o[kFv] = dir.y; o[2 * kFv] = dir.z; o[3 * kFv] = pv[u];
+                o[0] = -2.0f * dir.x; o[kFv] = -2.0f * dir.y; o[2 * kFv] = -2.0f * dir.z; o[3 * kFv] = pv[u];
             }
         }
         if (k + kFk < ke) prefetch(k + kFk);
@@ -463,19 +464,10 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
             for (int i = 0; i < 2; ++i) {
                 const ulonglong2 ia = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i)];
                 const ulonglong2 ib = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i) + 1];
-                // q^2 = |in - out|^2 per view in scalar FP32 (packed f32x2 math issues to one
-                // FMA pipe only; scalar FMAs can use the other), then both views packed:
-                // pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
-                const float ix = pk_lo(ia.x), iy = pk_lo(ia.y), iz = pk_lo(ib.x);
-                float q2s[2];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const float dxh = ix - (h ? pk_hi(ox) : pk_lo(ox));
-                    const float dyh = iy - (h ? pk_hi(oy) : pk_lo(oy));
-                    const float dzh = iz - (h ? pk_hi(oz) : pk_lo(oz));
-                    q2s[h] = fmaf(dxh, dxh, fmaf(dyh, dyh, dzh * dzh));
-                }
-                const unsigned long long q2 = pk2(q2s[0], q2s[1]);
+                // q^2 = |in - out|^2 = 2 - 2 in . out for unit directions, both views
+                // packed, z first (the largest product's cancellation against 2 is
+                // exact inside the FMA); pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
+                const unsigned long long q2 = fma2(ox, ia.x, fma2(oy, ia.y, fma2(oz, ib.x, pk2(2.0f, 2.0f))));
                 const unsigned long long dn = fma2(g2, q2, omg);
                 // the row factors' product does not wait for the rsqrt; r^3 w as
                 // (r r)(r w), two levels of products after it
@@ -669,7 +661,7 @@ int launch_gemm(const GemmParams& G, cudaStream_t stream)
 // static vertex, per tick for a moving one with the temporal amplitude -- in
 // FP64 (gauss.cuh), and the products are summed in FP64.  Thread per (l, v) of
 // a 16 x 16 tile, a chunk of kSsT ticks and a range of paths.
-__global__ void __launch_bounds__(256) gauss_ss_kernel(const __grid_constant__ DevScene S, const SsParams G)
+__global__ void __launch_bounds__(256, 1) gauss_ss_kernel(const __grid_constant__ DevScene S, const SsParams G)
 {
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
     const int l = blockIdx.x * kSsL + threadIdx.x % kSsL, v = blockIdx.y * kSsV + threadIdx.x / kSsL;
@@ -713,6 +705,151 @@ __global__ void __launch_bounds__(256) gauss_ss_kernel(const __grid_constant__ D
     }
 }
 
+// The same sum when every view beam shares one direction (the confocal
+// geometry): the lobe's convolution with the illumination throughput -- g0,
+// C, c of fsGaussianBeam -- then depends on (vertex, illumination) only.  Per
+// vertex (per path, or per path and tick for a moving scatterer) one thread
+// per illumination element stages it, one thread per view element the view
+// throughput, and each (l, v) thread finishes with one complex square root
+// and one complex exponential per lobe (the second exponential of 2 sinh as
+// e^(2 cl) / e^(cl + z)).  Arithmetic otherwise as gauss_fs (gauss.cuh); 3D,
+// at most 8 lobes per material.
+__global__ void __launch_bounds__(256, 1) gauss_ss_shared_kernel(const __grid_constant__ DevScene S, const SsParams G)
+{
+    __shared__ CD sA[kSsL][3], sB[kSsV][3];
+    __shared__ CD sG0[kSsL][8], sC[kSsL][8], sCl[kSsL][8], sE2[kSsL][8];
+    const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
+    const int tl = threadIdx.x % kSsL, tv = threadIdx.x / kSsL;
+    const int l = blockIdx.x * kSsL + tl, v = blockIdx.y * kSsV + tv;
+    const int lc = min(l, Nl - 1), vc = min(v, Nv - 1);
+    const bool act = l < Nl && v < Nv;
+    const int tchunks = (Nt + kSsT - 1) / kSsT;
+    const int t0 = (blockIdx.z % tchunks) * kSsT;
+    const int tn = min(kSsT, Nt - t0);
+    const int ks = blockIdx.z / tchunks;
+    const int kb = ks * G.kchunk, ke = min(G.K, kb + G.kchunk);
+    const DevSource& il = S.src[0];
+    const DevSource& vw = S.src[1];
+    const double k = S.gk;
+    const double vd[3] = { (double)vw.gdir[0], (double)vw.gdir[1], (double)vw.gdir[2] };
+    const double tc = il.gnorm + vw.gnorm + 2.0 * log(2.0 * kPi);
+    const double z0[3] = { 0.0, 0.0, 0.0 };
+    double ar[kSsT], ai[kSsT];
+#pragma unroll
+    for (int i = 0; i < kSsT; ++i) { ar[i] = 0.0; ai[i] = 0.0; }
+    for (int p = kb; p < ke; ++p) {
+        const int m = G.m1[p];
+        if (m <= 0 || m >= kMat) continue;
+        const int M = S.gmix_n[m];
+        const double* mix = S.gmix + 2 * S.gmix_off[m];
+        const bool stat = !S.temporal_amp || !S.moving[m];
+        // a static vertex is staged once for every tick, a moving one per tick
+        for (int s = 0; s < (stat ? 1 : tn); ++s) {
+            const float* xf = stat ? G.x1 + 3 * p : G.x1t + ((size_t)p * Nt + t0 + s) * 3;
+            const double x[3] = { (double)xf[0], (double)xf[1], (double)xf[2] };
+            __syncthreads();   // the previous vertex's staged values are consumed
+            if (tv < M) {   // thread (l, lobe)
+                CD aT[3];
+                g_throughput(il, lc, x, k, aT);
+                if (tv == 0)
+                    for (int a = 0; a < 3; ++a) sA[tl][a] = aT[a];
+                {
+                    const int i = tv;
+                    const double gs = mix[2 * i];
+                    CD C, c{ 0.0, 0.0 }, g0{ 0.0, 0.0 };
+                    if (fabs(gs) < 0.000001) {
+                        C = cd_sqrt(g_sumsq(0.0, z0, aT));
+                    } else {
+                        g0 = cd_rsqrt(g_sumsq(gs, vd, aT));
+                        g0.re = dM(g0.re, gs); g0.im = dM(g0.im, gs);
+                        double wv[3];
+                        CD aw{ 0.0, 0.0 };
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) wv[a] = dS(dM(g0.re, aT[a].re), dM(g0.im, aT[a].im));
+                        const double ra = dD(1.0, dQ(dA(dA(dM(wv[0], wv[0]), dM(wv[1], wv[1])), dM(wv[2], wv[2]))));
+                        C = cd_sqrt(g_sumsq(dM(gs, ra), wv, aT));
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) { aw.re = dA(aw.re, dM(aT[a].re, wv[a])); aw.im = dA(aw.im, dM(aT[a].im, wv[a])); }
+                        c = cd_mul(g0, aw);
+                        c.re = dM(c.re, -ra); c.im = dM(c.im, -ra);
+                    }
+                    const CD cl = cd_add(c, CD{ tc + mix[2 * i + 1], 0.0 });
+                    sG0[tl][i] = g0; sC[tl][i] = C; sCl[tl][i] = cl;
+                    sE2[tl][i] = fabs(cl.re) < 300.0 ? cd_exp(CD{ 2.0 * cl.re, 2.0 * cl.im }) : CD{ 0.0, 0.0 };
+                }
+            }
+            if (tl == 0) {
+#pragma unroll
+                for (int a = 0; a < 3; ++a) sB[tv][a] = CD{ dM((double)vw.gdir[3 * vc + a], vw.ga), dM(k, dS((double)vw.p[3 * vc + a], x[a])) };
+            }
+            __syncthreads();
+            if (!act) continue;
+            CD f{ 0.0, 0.0 };
+            for (int i = 0; i < M; ++i) {
+                const double gs = mix[2 * i];
+                const CD C = sC[tl][i], cl = sCl[tl][i];
+                CD sm;
+                if (fabs(gs) < 0.000001) {
+                    CD q{ 0.0, 0.0 };
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) q = cd_add(q, cd_mul(sB[tv][a], sB[tv][a]));
+                    sm = cd_sqrt(q);
+                } else {
+                    const CD g0 = sG0[tl][i];
+                    CD q{ 0.0, 0.0 };
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const CD e = cd_add(cd_mul(g0, sA[tl][a]), sB[tv][a]);
+                        q = cd_add(q, cd_mul(e, e));
+                    }
+                    sm = cd_sqrt(q);
+                }
+                const bool sbig = fabs(sm.re) > 0.0001 || fabs(sm.im) > 0.0001;
+                const bool cbig = fabs(C.re) > 0.0001 || fabs(C.im) > 0.0001;
+                if (sbig && cbig) {
+                    const CD z = cd_add(C, sm);
+                    const CD pos = cd_add(cl, z), neg = cd_sub(cl, z);
+                    CD r{ 0.0, 0.0 };
+                    if (fabs(cl.re) < 300.0 && fabs(pos.re) < 600.0) {
+                        const CD ep = cd_exp(pos);
+                        if (pos.re > -10.0) r = ep;
+                        if (neg.re > -10.0) r = cd_sub(r, cd_div(sE2[tl][i], ep));
+                    } else {
+                        r = cd_2sinh(z, cl);
+                    }
+                    f = cd_add(f, cd_div(r, cd_mul(C, sm)));
+                } else if (!sbig && !cbig) {
+                    const CD e = cd_exp(cl);
+                    f.re += 4.0 * e.re; f.im += 4.0 * e.im;
+                } else if (!sbig) {
+                    const CD e = cd_div(cd_2sinh(C, cl), C);
+                    f.re += 2.0 * e.re; f.im += 2.0 * e.im;
+                } else {
+                    const CD e = cd_div(cd_2sinh(sm, CD{ tc + mix[2 * i + 1], 0.0 }), sm);
+                    f.re += 2.0 * e.re; f.im += 2.0 * e.im;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < kSsT; ++i) {
+                if (i >= tn) break;
+                if (!stat && i != s) continue;
+                const int t = t0 + i;
+                const float2 a = G.a[((size_t)p * Nt + t) * Nl + l];
+                const float2 b = G.b[((size_t)p * Nt + t) * Nv + v];
+                const double abr = (double)a.x * b.x - (double)a.y * b.y, abi = (double)a.x * b.y + (double)a.y * b.x;
+                ar[i] += abr * f.re - abi * f.im;
+                ai[i] += abr * f.im + abi * f.re;
+            }
+        }
+    }
+    if (!act) return;
+    for (int i = 0; i < tn; ++i) {
+        const size_t o = ((size_t)(t0 + i) * Nv + v) * Nl + l;
+        atomicAdd(&G.V[o].x, ar[i]);
+        atomicAdd(&G.V[o].y, ai[i]);
+    }
+}
+
 int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
 {
     if (G.K <= 0) return SSTMC_NO_ERROR;
@@ -720,7 +857,10 @@ int launch_ss(const DevScene& S, const SsParams& G, cudaStream_t stream)
         const int tchunks = (S.Nt + kSsT - 1) / kSsT;
         const int ksplit = (G.K + G.kchunk - 1) / G.kchunk;
         dim3 grid((S.src[0].n + kSsL - 1) / kSsL, (S.src[1].n + kSsV - 1) / kSsV, tchunks * ksplit);
-        gauss_ss_kernel<<<grid, 256, 0, stream>>>(S, G);
+        bool lobes8 = true;
+        for (int m = 0; m < kMat; ++m) lobes8 = lobes8 && S.gmix_n[m] <= 8;
+        if (S.dims == 3 && S.src[1].gsame && lobes8) gauss_ss_shared_kernel<<<grid, 256, 0, stream>>>(S, G);
+        else gauss_ss_kernel<<<grid, 256, 0, stream>>>(S, G);
         return cudaGetLastError() == cudaSuccess ? SSTMC_NO_ERROR : SSTMC_CUBLAS_ERROR;
     }
     if (S.correlation && S.sym && S.all_static_corr && !S.has_amp64) {

@@ -734,6 +734,9 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
         e = upload(S, h.p, &d.p);
         if (!e && h.type == SSTMC_SOURCE_GAUSSIANBEAM) {
             d.ga = h.ga; d.gnorm = h.gnorm; d.gM = h.gM;
+            d.gsame = 1;
+            for (int k = 1; k < h.n; ++k)
+                for (int a = 0; a < 3; ++a) if (h.gdir[3 * k + a] != h.gdir[a]) d.gsame = 0;
             e = upload(S, h.gdir, &d.gdir);
             if (!e && !h.gfm.empty()) {
                 e = upload(S, h.gfm, &d.gfm);

@@ -49,6 +49,7 @@ struct DevSource {
     const float* gdir;
     double ga, gnorm;
     int gM;
+    int gsame;           // every beam has the same direction
     const int* gfm;
     const double* gtab;
     const double* gpdf;

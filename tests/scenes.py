@@ -491,12 +491,14 @@ def far_phases_3d(point: bool, batch_size=64, full_iteration=2):
 
 
 def gauss_beams_3d(moving: bool = False, iso: bool = False, tilted: bool = False, back: bool = False,
-                   n_l: int = 3, n_v: int = 4, batch_size=64, full_iteration=2, equal_lobes: bool = False):
+                   n_l: int = 3, n_v: int = 4, batch_size=64, full_iteration=2, equal_lobes: bool = False,
+                   fan: bool = False):
     """Focused Gaussian beams (3D field sampler): vMF materials, illumination and
     view beams focused inside a two-material slab (a three-lobe and a two-lobe
     mixture), optionally drifting and diffusing scatterers over three ticks,
     every lobe isotropic, tilted illumination beams, or views looking back
-    along -z (backscattering).  equal_lobes: two-lobe mixtures everywhere."""
+    along -z (backscattering).  equal_lobes: two-lobe mixtures everywhere.
+    fan: view beams fanned out in x, each with its own direction."""
     lobes = [([0.0], [1.0]), ([0.0], [1.0]), ([0.0], [1.0])] if iso else \
         [([0.0], [1.0]), ([0.0, 4.0, 15.0], [0.3, 0.5, 0.2]), ([0.0, 2.5], [0.6, 0.4])]
     if equal_lobes:
@@ -519,7 +521,8 @@ def gauss_beams_3d(moving: bool = False, iso: bool = False, tilted: bool = False
                          "aperture": 0.4},
         "view": {"type": "GaussianBeam",
                  "focalPoint": {"x": xv, "y": np.zeros(n_v), "z": np.full(n_v, 5.0)},
-                 "focalDirection": {"x": np.zeros(n_v), "y": np.zeros(n_v), "z": np.full(n_v, dv[2])},
+                 "focalDirection": {"x": np.linspace(-0.3, 0.3, n_v) if fan else np.zeros(n_v), "y": np.zeros(n_v),
+                                    "z": np.full(n_v, dv[2])},
                  "aperture": 0.5},
         "sampler": {"type": "TemporalSampler", "t": t, "D": [0.0, 0.02 if moving else 0.0, 0.0],
                     "U": {"x": [0.0, 0.3 if moving else 0.0, 0.0], "y": [0.0, 0.0, 0.0], "z": [0.0, 0.0, 0.0]}},
@@ -609,6 +612,8 @@ def small_scenes():
         "gauss_3d_moving": gauss_beams_3d(moving=True),
         "gauss_3d_iso": gauss_beams_3d(iso=True),
         "gauss_3d_tilted_back": gauss_beams_3d(tilted=True, back=True),
+        "gauss_3d_fan": gauss_beams_3d(fan=True),
+        "gauss_3d_fan_moving": gauss_beams_3d(fan=True, moving=True),
         "edge_ragged_corr_3d": ragged_corr_3d(),
         "edge_mostly_misses_3d": mostly_misses_3d(),
         "edge_absorbing_2d": absorbing_2d(),
