@@ -536,23 +536,23 @@ def run_gpu(args, dist, rank, ws):
             "frac": d["frac"], "traffic": d["traffic"], "peak_source": pk_kind + " (" + d["peak_name"] + ")",
             "algorithmic_per_launch": d["algorithmic_per_launch"], "launches_per_step": chunks}
     if dom == "ss" and WORKLOAD == "correlation_3d":
-        # ss_fast_kernel is bound by FP32 issue, not by HBM: the algorithmic FP32 lane
-        # operations per (path, l, v) element are 6 (q^2) + 5 (pdf) + 1 (decay
-        # argument) per 8-tick chunk and 2 per tick (one product for the tick's decay
-        # power, one accumulation) less one per chunk, plus 2 MUFU (rsqrt, ex2).  The
-        # kernel issues 3 more products per chunk (a depth-3 product tree instead of
-        # a serial chain, for latency); those are not counted as work.
+        # ss_fast_kernel is bound by FP32 issue, not by HBM.  FP32 lane operations
+        # per (path, l, v) element and 8-tick chunk, an FMA
+        # counted once: 3 (q^2 as 2 - 2 in . out) + 1 (the pdf's base) + 1 (row
+        # product) + 1 (decay argument) + 1 (first tick's exponent with the pdf's
+        # power) + 1 (first term) + 2 (squared and fourth decay powers) + 11 (the
+        # 8 tick terms: 3 products, 4 adds, 4 FMAs) = 21, plus 3 MUFU (lg2, 2 ex2).
         # Peak: the nominal FP32 lane rate, SMs x 128 lanes x the SM clock sampled
         # during the timed region (a nominal figure, not a measured one).
         import torch
         tchunks = (Nt + 7) // 8
-        ops = float(P) * Nl * Nv * (11 * tchunks + 2 * Nt)
+        ops = float(P) * Nl * Nv * 21 * tchunks
         sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
         sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
         lane_peak = sms * 128 * sm_mhz * 1e6 / 1e12
         ach = ops / (mean["ms_contract_ss"] / 1000) / 1e12
         roof["issue"] = {"unit": "FP32 lane-Tops/s", "achieved": ach, "peak": lane_peak, "frac": ach / lane_peak,
-                         "ops_per_element": 11 * tchunks + 2 * Nt, "mufu_per_element": 2 * tchunks,
+                         "ops_per_element": 21 * tchunks, "mufu_per_element": 3 * tchunks,
                          "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (sampled SM clock)"}
 
     # the plain FP32 form (FP32 phases, uncompensated SIMT contraction) on the same

@@ -285,10 +285,13 @@ __global__ void __launch_bounds__(256) ss_kernel(const __grid_constant__ DevScen
 // (SourceInterface.cuh:221-270 with q = in - out).  Each thread owns a 2 x 2
 // (illumination, view) block and all ticks of a chunk.  Per path the block
 // stages one float4 per illumination element (direction into the scatterer,
-// row value), one per view element (direction out, row value) and one per
-// path with the material constants, so the inner loop is branch-free:
-//   pdf = gup (omg2 + g q^2)^(-(D-1)/2)    (isotropic: g = 0, omg2 = 1)
+// row value), one per view element (-2 x direction out, row value) and one
+// per path with the material constants, so the inner loop is branch-free:
+//   q^2 = 2 - 2 in . out                   (unit directions)
+//   pdf = gup (omg2 + g q^2)^(-D/2)        (isotropic: g = 0, omg2 = 1)
 //   e_t = exp2(-c q^2 |tau_t|), c = k^2 D log2(e)
+// and the pdf's power is folded into the first tick's exponential:
+//   pdf e_0 = gup exp2(-(D/2) log2(omg2 + g q^2) - c q^2 |tau_0|).
 // The scalar single-scattering amplitude of point x point isotropic scenes
 // (no temporal factor, NextEventEstimation.cuh:1024-1032) is g = 0, c = 0.
 // The tick chain runs on packed FP32 pairs (the thread's two views per FMA / MUL).
@@ -334,6 +337,12 @@ __device__ __forceinline__ float ex2_fast(float x)
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+__device__ __forceinline__ float lg2_fast(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ float rsqrt_fast(float x)
 {
     float y;
@@ -344,7 +353,7 @@ __device__ __forceinline__ unsigned long long ex2_2(unsigned long long a) { retu
 
 // Accumulators are packed over the thread's view pair, so the whole tick
 // chain runs on f32x2 values: per (path, illumination element, view pair)
-// 2 rsqrt + 2 ex2 and about 30 FP32 instructions for 8 ticks.
+// 2 lg2 + 4 ex2 and 22 packed FP32 instructions for 8 ticks.
 // FIRST: the block's first tick is tick 0 (GEO chain starts at e_s).
 template <bool THREE, bool GEO, bool FIRST>
 __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__ DevScene S, const SsParams G)
@@ -466,38 +475,37 @@ __global__ void __launch_bounds__(256, 2) ss_fast_kernel(const __grid_constant__
                 const ulonglong2 ib = reinterpret_cast<const ulonglong2*>(sI)[2 * (pp * kFl + ty + 16 * i) + 1];
                 // q^2 = |in - out|^2 = 2 - 2 in . out for unit directions, both views
                 // packed, z first (the largest product's cancellation against 2 is
-                // exact inside the FMA); pdf = c r^(D-1), r = (omg2 + g q^2)^(-1/2)
+                // exact inside the FMA); pdf = c dn^(-D/2), dn = omg2 + g q^2, as
+                // exp2(-(D/2) log2 dn) inside the first tick's exponential
                 const unsigned long long q2 = fma2(ox, ia.x, fma2(oy, ia.y, fma2(oz, ib.x, pk2(2.0f, 2.0f))));
                 const unsigned long long dn = fma2(g2, q2, omg);
-                // the row factors' product does not wait for the rsqrt; r^3 w as
-                // (r r)(r w), two levels of products after it
                 const unsigned long long w = mul2(ob, ib.y);
-                const unsigned long long r = pk2(rsqrt_fast(pk_lo(dn)), rsqrt_fast(pk_hi(dn)));
-                const unsigned long long base = THREE ? mul2(mul2(r, r), mul2(r, w)) : mul2(mul2(r, r), w);
+                const unsigned long long L = pk2(lg2_fast(pk_lo(dn)), lg2_fast(pk_hi(dn)));
                 const unsigned long long arg = mul2(cn2, q2);
                 if (GEO) {
-                    // e_t = e_s^(t + 1), e_s = exp(-c q^2 |t_0|): one ex2 per view, then a product chain
+                    // e_t = e_s^(t + 1), e_s = exp(-c q^2 |t_0|): per view one ex2 for e_s
+                    // and one for the first tick's term with the pdf's power
                     const unsigned long long es = ex2_2(arg);
-                    const unsigned long long e = FIRST ? es : ex2_2(mul2(arg, pk2(start_scale, start_scale)));
-                    // the 8 terms base e es^k as a depth-3 product tree, summed with
-                    // packed adds: a serial chain of products (measured 5 % slower)
-                    // leaves the warps waiting on each product in turn, and adding
-                    // the terms by packed FMAs on the powers es^k (three instructions
-                    // fewer) measured 7 % slower
+                    const unsigned long long beta = THREE ? pk2(-1.5f, -1.5f) : pk2(-1.0f, -1.0f);
+                    const unsigned long long e = ex2_2(fma2(beta, L, FIRST ? arg : mul2(arg, pk2(start_scale, start_scale))));
+                    // the 8 terms b0 es^k: the even ones by products in a depth-2
+                    // tree, the odd ones as FMAs of their even neighbour (13 packed
+                    // instructions; a serial product chain stalled on latency, and
+                    // 8 products and 8 packed adds measured 1 % slower)
                     static_assert(kFt == 8, "tick tree written for 8 ticks");
                     const unsigned long long s2 = mul2(es, es), s4 = mul2(s2, s2);
-                    const unsigned long long b0 = mul2(base, e);
-                    const unsigned long long b1 = mul2(b0, es), b2 = mul2(b0, s2), b4 = mul2(b0, s4);
-                    const unsigned long long b3 = mul2(b1, s2), b5 = mul2(b1, s4), b6 = mul2(b2, s4), b7 = mul2(b3, s4);
-                    acc[i][0] = add2(acc[i][0], b0); acc[i][1] = add2(acc[i][1], b1);
-                    acc[i][2] = add2(acc[i][2], b2); acc[i][3] = add2(acc[i][3], b3);
-                    acc[i][4] = add2(acc[i][4], b4); acc[i][5] = add2(acc[i][5], b5);
-                    acc[i][6] = add2(acc[i][6], b6); acc[i][7] = add2(acc[i][7], b7);
+                    const unsigned long long b0 = mul2(w, e);
+                    const unsigned long long b2 = mul2(b0, s2), b4 = mul2(b0, s4), b6 = mul2(b2, s4);
+                    acc[i][0] = add2(acc[i][0], b0); acc[i][1] = fma2(b0, es, acc[i][1]);
+                    acc[i][2] = add2(acc[i][2], b2); acc[i][3] = fma2(b2, es, acc[i][3]);
+                    acc[i][4] = add2(acc[i][4], b4); acc[i][5] = fma2(b4, es, acc[i][5]);
+                    acc[i][6] = add2(acc[i][6], b6); acc[i][7] = fma2(b6, es, acc[i][7]);
                 } else {
 #pragma unroll
                     for (int tt = 0; tt < kFt; ++tt) {
                         const float ta = S.abs_ticks[min(t0 + tt, Nt - 1)];
-                        acc[i][tt] = fma2(base, ex2_2(mul2(arg, pk2(ta, ta))), acc[i][tt]);
+                        const unsigned long long beta = THREE ? pk2(-1.5f, -1.5f) : pk2(-1.0f, -1.0f);
+                        acc[i][tt] = fma2(w, ex2_2(fma2(beta, L, mul2(arg, pk2(ta, ta)))), acc[i][tt]);
                     }
                 }
             }
@@ -705,15 +713,38 @@ __global__ void __launch_bounds__(256, 1) gauss_ss_kernel(const __grid_constant_
     }
 }
 
+// Complex arithmetic for the per-element sums, contracted to FMAs (the
+// sampling code keeps gauss.cuh's explicitly rounded forms)
+__device__ __forceinline__ CD cf_add(CD a, CD b) { return CD{ a.re + b.re, a.im + b.im }; }
+__device__ __forceinline__ CD cf_sub(CD a, CD b) { return CD{ a.re - b.re, a.im - b.im }; }
+__device__ __forceinline__ CD cf_mul(CD a, CD b) { return CD{ a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re }; }
+__device__ __forceinline__ CD cf_div(CD a, CD b)
+{
+    const double r = 1.0 / (b.re * b.re + b.im * b.im);
+    return CD{ (a.re * b.re + a.im * b.im) * r, (a.im * b.re - a.re * b.im) * r };
+}
+// principal square root: s = sqrt((|re| + |z|) / 2); (s, im / 2s) for re >= 0,
+// else (|im| / 2s, +-s), with 1 / s from one reciprocal square root
+__device__ __forceinline__ CD cf_sqrt(CD a)
+{
+    if (a.re == 0.0 && a.im == 0.0) return CD{ 0.0, 0.0 };
+    const double h = 0.5 * (fabs(a.re) + sqrt(a.re * a.re + a.im * a.im));
+    const double ri = rsqrt(h), s = h * ri;
+    if (a.re >= 0.0) return CD{ s, 0.5 * a.im * ri };
+    return CD{ 0.5 * fabs(a.im) * ri, copysign(s, a.im) };
+}
+
 // The same sum when every view beam shares one direction (the confocal
 // geometry): the lobe's convolution with the illumination throughput -- g0,
 // C, c of fsGaussianBeam -- then depends on (vertex, illumination) only.  Per
 // vertex (per path, or per path and tick for a moving scatterer) one thread
 // per illumination element stages it, one thread per view element the view
-// throughput, and each (l, v) thread finishes with one complex square root
-// and one complex exponential per lobe (the second exponential of 2 sinh as
-// e^(2 cl) / e^(cl + z)).  Arithmetic otherwise as gauss_fs (gauss.cuh); 3D,
-// at most 8 lobes per material.
+// throughput, and each (l, v) thread finishes with one complex square root,
+// one complex exponential and one complex division per lobe: 2 sinh(z) e^cl
+// / (C sm) as (e^(2 (cl + z)) - e^(2 cl)) / (e^(cl + z) C sm), with each
+// exponential dropped at a real part of -10 or below as in gauss_fs
+// (gauss.cuh), whose two-exponential form runs where |Re cl| or |Re(cl + z)|
+// reaches 300.  3D, at most 8 lobes per material.
 __global__ void __launch_bounds__(256, 1) gauss_ss_shared_kernel(const __grid_constant__ DevScene S, const SsParams G)
 {
     __shared__ CD sA[kSsL][3], sB[kSsV][3];
@@ -788,36 +819,35 @@ __global__ void __launch_bounds__(256, 1) gauss_ss_shared_kernel(const __grid_co
             for (int i = 0; i < M; ++i) {
                 const double gs = mix[2 * i];
                 const CD C = sC[tl][i], cl = sCl[tl][i];
-                CD sm;
+                CD q{ 0.0, 0.0 };
                 if (fabs(gs) < 0.000001) {
-                    CD q{ 0.0, 0.0 };
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) q = cd_add(q, cd_mul(sB[tv][a], sB[tv][a]));
-                    sm = cd_sqrt(q);
+                    for (int a = 0; a < 3; ++a) q = cf_add(q, cf_mul(sB[tv][a], sB[tv][a]));
                 } else {
                     const CD g0 = sG0[tl][i];
-                    CD q{ 0.0, 0.0 };
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
-                        const CD e = cd_add(cd_mul(g0, sA[tl][a]), sB[tv][a]);
-                        q = cd_add(q, cd_mul(e, e));
+                        const CD e = cf_add(cf_mul(g0, sA[tl][a]), sB[tv][a]);
+                        q = cf_add(q, cf_mul(e, e));
                     }
-                    sm = cd_sqrt(q);
                 }
+                const CD sm = cf_sqrt(q);
                 const bool sbig = fabs(sm.re) > 0.0001 || fabs(sm.im) > 0.0001;
                 const bool cbig = fabs(C.re) > 0.0001 || fabs(C.im) > 0.0001;
                 if (sbig && cbig) {
-                    const CD z = cd_add(C, sm);
-                    const CD pos = cd_add(cl, z), neg = cd_sub(cl, z);
-                    CD r{ 0.0, 0.0 };
-                    if (fabs(cl.re) < 300.0 && fabs(pos.re) < 600.0) {
+                    const CD z = cf_add(C, sm);
+                    const CD pos = cf_add(cl, z);
+                    const double negre = cl.re - z.re;
+                    if (fabs(cl.re) < 300.0 && fabs(pos.re) < 300.0) {
+                        // (e^(cl + z) - e^(cl - z)) / (C sm) = (ep^2 - e^(2 cl)) / (ep C sm)
                         const CD ep = cd_exp(pos);
-                        if (pos.re > -10.0) r = ep;
-                        if (neg.re > -10.0) r = cd_sub(r, cd_div(sE2[tl][i], ep));
+                        CD n{ 0.0, 0.0 };
+                        if (pos.re > -10.0) n = cf_mul(ep, ep);
+                        if (negre > -10.0) n = cf_sub(n, sE2[tl][i]);
+                        f = cf_add(f, cf_div(n, cf_mul(ep, cf_mul(C, sm))));
                     } else {
-                        r = cd_2sinh(z, cl);
+                        f = cd_add(f, cd_div(cd_2sinh(z, cl), cd_mul(C, sm)));
                     }
-                    f = cd_add(f, cd_div(r, cd_mul(C, sm)));
                 } else if (!sbig && !cbig) {
                     const CD e = cd_exp(cl);
                     f.re += 4.0 * e.re; f.im += 4.0 * e.im;
