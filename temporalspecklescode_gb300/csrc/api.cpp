@@ -248,6 +248,33 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     std::memcpy(&nlong, hv + 16, 4);
     uint32_t novf = 0;
     std::memcpy(&novf, hv + 20, 4);
+    if (novf > Wp.ovf_cap && !fixed) {
+        // The overflow pool ran short.  Grow it to what the chunk can need (a
+        // path of B > 64 vertices takes ceil(B / 64) - 1 blocks, at most
+        // B / 64 + 1) and walk the chunk again: a path is a function of (seed,
+        // path id), so the second pass repeats the first, and it costs less than
+        // replaying the listed paths when many paths are long (a chunk of paths
+        // of hundreds of vertices lists most of them).
+        const uint64_t want = std::min<uint64_t>(nverts / kWalkSlotVerts + std::min<uint64_t>(n, nverts / (kWalkSlotVerts + 1)) + 64,
+                                                 1u << 30);
+        cudaFreeAsync(ovf, stream);
+        cudaFreeAsync(ovf_owner, stream);
+        ovf = nullptr; ovf_owner = nullptr; ovf_blocks = 0;
+        if (cudaMallocAsync((void**)&ovf, (size_t)want * kWalkSlotVerts * sizeof(float4), stream) != cudaSuccess
+            || cudaMallocAsync((void**)&ovf_owner, (size_t)want * sizeof(uint2), stream) != cudaSuccess)
+            return SSTMC_ALLOCATION_ERROR;
+        ovf_blocks = (uint32_t)want;
+        ovf_want = std::max(ovf_want, (uint32_t)want);
+        Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_cap = ovf_blocks;
+        e = launch_walk_count(S.dev, Wp, stream);
+        if (e) return e;
+        launches += 4;
+        if (cudaMemcpyAsync(hv, vtotal, sizeof(hv), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+        if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
+        std::memcpy(&nverts, hv, 8);
+        std::memcpy(&nlong, hv + 16, 4);
+        std::memcpy(&novf, hv + 20, 4);
+    }
     Wp.ovf_n = std::min(novf, Wp.ovf_cap);
     if (nverts > verts_cap) {
         if (fixed) return SSTMC_SCRATCH_LIMIT;

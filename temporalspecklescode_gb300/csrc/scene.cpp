@@ -19,6 +19,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <functional>
 
 namespace sstmc {
 
@@ -29,17 +30,41 @@ Scene::~Scene()
 
 namespace {
 
-template <class T>
-int upload(Scene* s, const std::vector<T>& v, const T** out)
-{
-    if (v.empty()) { *out = nullptr; return SSTMC_NO_ERROR; }
-    void* d = nullptr;
-    if (cudaMalloc(&d, v.size() * sizeof(T)) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
-    s->dev_allocs.push_back(d);
-    if (cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
-    *out = static_cast<const T*>(d);
-    return SSTMC_NO_ERROR;
-}
+// The scene's device tables, packed into one allocation and one copy: tables
+// are appended at 256-byte offsets, and each table's device pointer is set
+// once the block exists (a scene of a few dozen tables is created with one
+// cudaMalloc and one cudaMemcpy, and destroyed with one cudaFree).
+struct TablePack {
+    std::vector<unsigned char> host;
+    std::vector<std::pair<size_t, std::function<void(const unsigned char*)>>> fix;
+
+    void add_bytes(const void* data, size_t bytes, std::function<void(const unsigned char*)> set)
+    {
+        if (bytes == 0) return;
+        const size_t off = (host.size() + 255) & ~size_t(255);
+        host.resize(off + bytes);
+        std::memcpy(host.data() + off, data, bytes);
+        fix.emplace_back(off, std::move(set));
+    }
+
+    template <class T>
+    void add(const std::vector<T>& v, const T** out)
+    {
+        *out = nullptr;
+        add_bytes(v.data(), v.size() * sizeof(T), [out](const unsigned char* base) { *out = reinterpret_cast<const T*>(base); });
+    }
+
+    int commit(Scene* s)
+    {
+        if (host.empty()) return SSTMC_NO_ERROR;
+        void* d = nullptr;
+        if (cudaMalloc(&d, host.size()) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+        s->dev_allocs.push_back(d);
+        if (cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) return SSTMC_ALLOCATION_ERROR;
+        for (auto& f : fix) f.second(static_cast<const unsigned char*>(d) + f.first);
+        return SSTMC_NO_ERROR;
+    }
+};
 
 int prep_farfield(Scene::HostSource* s, const sstmc_source_cfg* c, int dims, const double bmin[3], const double bmax[3])
 {
@@ -708,57 +733,58 @@ int build_scene(const sstmc_config* cfg, Scene* S, std::string* why)
 
     // upload
     if (cudaSetDevice(S->device) != cudaSuccess) return fail(SSTMC_DEVICE_ERROR, "cudaSetDevice failed");
-    int e = 0;
-    for (int a = 0; a < dims && !e; ++a) e = upload(S, S->ax[a], &D.ax[a]);
-    if (!e && D.has_amp64) {
-        const float* tf = nullptr;
-        e = upload(S, S->tab_f, &tf);
-        D.tab_f = reinterpret_cast<const float2*>(tf);
-        if (!e) e = upload(S, S->tab_pdf, &D.tab_pdf);
-        if (!e) e = upload(S, S->tab_cos, &D.tab_cos);
-        if (!e) e = upload(S, S->vmf_mc, &D.vmf_mc);
-        if (!e) e = upload(S, S->vmf_pd, &D.vmf_pd);
-        if (!e) e = upload(S, S->vmf_pf, &D.vmf_pf);
+    TablePack pk;
+    for (int a = 0; a < dims; ++a) pk.add(S->ax[a], &D.ax[a]);
+    if (D.has_amp64) {
+        D.tab_f = nullptr;
+        pk.add_bytes(S->tab_f.data(), S->tab_f.size() * sizeof(float),
+                     [&D](const unsigned char* base) { D.tab_f = reinterpret_cast<const float2*>(base); });
+        pk.add(S->tab_pdf, &D.tab_pdf);
+        pk.add(S->tab_cos, &D.tab_cos);
+        pk.add(S->vmf_mc, &D.vmf_mc);
+        pk.add(S->vmf_pd, &D.vmf_pd);
+        pk.add(S->vmf_pf, &D.vmf_pf);
     }
-    if (!e && D.gauss) e = upload(S, S->gmix, &D.gmix);
-    if (!e) e = upload(S, S->grid, &D.grid);
-    if (!e) e = upload(S, S->disp_scale, &D.disp_scale);
-    if (!e) e = upload(S, S->disp_u, &D.disp_u);
-    if (!e) e = upload(S, S->ticks_f, &D.ticks_f);
-    if (!e) e = upload(S, S->abs_ticks, &D.abs_ticks);
-    for (int i = 0; i < 4 && !e; ++i) {
+    if (D.gauss) pk.add(S->gmix, &D.gmix);
+    pk.add(S->grid, &D.grid);
+    pk.add(S->disp_scale, &D.disp_scale);
+    pk.add(S->disp_u, &D.disp_u);
+    pk.add(S->ticks_f, &D.ticks_f);
+    pk.add(S->abs_ticks, &D.abs_ticks);
+    for (int i = 0; i < 4; ++i) {
         Scene::HostSource& h = S->hsrc[i];
         DevSource& d = D.src[i];
         d.type = h.type; d.n = h.n; d.is_area = h.is_area;
         if (h.type == SSTMC_SOURCE_NONE) continue;
-        e = upload(S, h.p, &d.p);
-        if (!e && h.type == SSTMC_SOURCE_GAUSSIANBEAM) {
+        pk.add(h.p, &d.p);
+        if (h.type == SSTMC_SOURCE_GAUSSIANBEAM) {
             d.ga = h.ga; d.gnorm = h.gnorm; d.gM = h.gM;
             d.gsame = 1;
             for (int k = 1; k < h.n; ++k)
                 for (int a = 0; a < 3; ++a) if (h.gdir[3 * k + a] != h.gdir[a]) d.gsame = 0;
-            e = upload(S, h.gdir, &d.gdir);
-            if (!e && !h.gfm.empty()) {
-                e = upload(S, h.gfm, &d.gfm);
-                if (!e) e = upload(S, h.gtab, &d.gtab);
-                if (!e) e = upload(S, h.gpdf, &d.gpdf);
-                if (!e) e = upload(S, h.gicdf, &d.gicdf);
-                if (!e) e = upload(S, h.gapdf, &d.gapdf);
-                if (!e) e = upload(S, h.gaicdf, &d.gaicdf);
+            pk.add(h.gdir, &d.gdir);
+            if (!h.gfm.empty()) {
+                pk.add(h.gfm, &d.gfm);
+                pk.add(h.gtab, &d.gtab);
+                pk.add(h.gpdf, &d.gpdf);
+                pk.add(h.gicdf, &d.gicdf);
+                pk.add(h.gapdf, &d.gapdf);
+                pk.add(h.gaicdf, &d.gaicdf);
             }
         }
-        if (!e && h.type == SSTMC_SOURCE_FARFIELD) {
-            e = upload(S, h.inv, &d.inv);
-            if (!e) e = upload(S, h.tang, &d.tang);
-            if (!e) e = upload(S, h.pt, &d.pt);
-            if (!e) e = upload(S, h.ps, &d.ps);
-            if (!e) e = upload(S, h.mint, &d.mint);
-            if (!e) e = upload(S, h.maxt, &d.maxt);
-            if (!e) e = upload(S, h.mins, &d.mins);
-            if (!e) e = upload(S, h.maxs, &d.maxs);
-            if (!e) e = upload(S, h.sprob, &d.sprob);
+        if (h.type == SSTMC_SOURCE_FARFIELD) {
+            pk.add(h.inv, &d.inv);
+            pk.add(h.tang, &d.tang);
+            pk.add(h.pt, &d.pt);
+            pk.add(h.ps, &d.ps);
+            pk.add(h.mint, &d.mint);
+            pk.add(h.maxt, &d.maxt);
+            pk.add(h.mins, &d.mins);
+            pk.add(h.maxs, &d.maxs);
+            pk.add(h.sprob, &d.sprob);
         }
     }
+    const int e = pk.commit(S);
     if (e) return fail(e, "device allocation failed");
     return SSTMC_NO_ERROR;
 }

@@ -127,8 +127,9 @@ def homogeneous_3d(batch_size=64, full_iteration=1):
 def long_paths_3d(batch_size=64, full_iteration=2):
     """Point sources inside an optically thick homogeneous cube (optical
     radius 20, no absorption): nearly every path runs past 64 vertices, so
-    the walk's overflow blocks are used, the overflow pool runs dry and the
-    write pass replays the rest."""
+    the walk's overflow blocks are used and the default overflow pool runs dry
+    (sstmc_render walks the chunk again with a grown pool; the fixed-scratch
+    sstmc_render_static replays the listed paths in the write pass)."""
     ill = {"type": "PointSource", "location": {"x": [0.0, 0.5], "y": [0.0, -0.5], "z": [5.0, 5.0]}}
     view = {"type": "PointSource", "location": {"x": [0.0, 2.0, -1.0], "y": [0.0, 0.0, 1.0], "z": [12.0, 12.0, 12.0]}}
     cfg = {

@@ -219,9 +219,9 @@ def test_vmf_scatters_isotropically_in_2d(api):
 
 def test_walk_overflow_pool_grows(api, oracle):
     """Paths of hundreds of vertices exhaust the walk's default overflow pool:
-    the first render completes them through the replay pass and grows the pool,
-    the second (same seed) keeps every path in the grown pool.  Both renders are
-    identical and match the oracle."""
+    the first render grows the pool and walks the chunk again, the second
+    (same seed) keeps every path in the grown pool from the start.  Both
+    renders are identical and match the oracle."""
     from tests.scenes import very_long_paths_2d
     cfg, dims = very_long_paths_2d()
     with api.Scene(cfg, dims) as s:
