@@ -713,41 +713,21 @@ __global__ void __launch_bounds__(256, 1) gauss_ss_kernel(const __grid_constant_
     }
 }
 
-// Complex arithmetic for the per-element sums, contracted to FMAs (the
-// sampling code keeps gauss.cuh's explicitly rounded forms)
-__device__ __forceinline__ CD cf_add(CD a, CD b) { return CD{ a.re + b.re, a.im + b.im }; }
-__device__ __forceinline__ CD cf_sub(CD a, CD b) { return CD{ a.re - b.re, a.im - b.im }; }
-__device__ __forceinline__ CD cf_mul(CD a, CD b) { return CD{ a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re }; }
-__device__ __forceinline__ CD cf_div(CD a, CD b)
-{
-    const double r = 1.0 / (b.re * b.re + b.im * b.im);
-    return CD{ (a.re * b.re + a.im * b.im) * r, (a.im * b.re - a.re * b.im) * r };
-}
-// principal square root: s = sqrt((|re| + |z|) / 2); (s, im / 2s) for re >= 0,
-// else (|im| / 2s, +-s), with 1 / s from one reciprocal square root
-__device__ __forceinline__ CD cf_sqrt(CD a)
-{
-    if (a.re == 0.0 && a.im == 0.0) return CD{ 0.0, 0.0 };
-    const double h = 0.5 * (fabs(a.re) + sqrt(a.re * a.re + a.im * a.im));
-    const double ri = rsqrt(h), s = h * ri;
-    if (a.re >= 0.0) return CD{ s, 0.5 * a.im * ri };
-    return CD{ 0.5 * fabs(a.im) * ri, copysign(s, a.im) };
-}
-
 // The same sum when every view beam shares one direction (the confocal
 // geometry): the lobe's convolution with the illumination throughput -- g0,
 // C, c of fsGaussianBeam -- then depends on (vertex, illumination) only.  Per
 // vertex (per path, or per path and tick for a moving scatterer) one thread
 // per illumination element stages it, one thread per view element the view
 // throughput, and each (l, v) thread finishes with one complex square root,
-// one complex exponential and one complex division per lobe: 2 sinh(z) e^cl
-// / (C sm) as (e^(2 (cl + z)) - e^(2 cl)) / (e^(cl + z) C sm), with each
-// exponential dropped at a real part of -10 or below as in gauss_fs
-// (gauss.cuh), whose two-exponential form runs where |Re cl| or |Re(cl + z)|
-// reaches 300.  3D, at most 8 lobes per material.
+// one complex exponential and one reciprocal per lobe: 2 sinh(z) e^cl / (C sm)
+// with e^(cl + z) = 2^kk p (c, s) from exp_parts and e^(cl - z) as e^(2 cl)
+// 2^-kk p^-1 (c, -s), each exponential dropped at a real part of -10 or below
+// as in gauss_fs (gauss.cuh), whose FP64 form runs where |Re cl| or
+// |Re(cl + z)| reaches 300 or |z| is below 0.05 (the difference of the two
+// exponentials cancels there).  3D, at most 8 lobes per material.
 __global__ void __launch_bounds__(256, 1) gauss_ss_shared_kernel(const __grid_constant__ DevScene S, const SsParams G)
 {
-    __shared__ CD sA[kSsL][3], sB[kSsV][3];
+    __shared__ CD sA[kSsL][3], sB[kSsV][3], sBi[kSsV];
     __shared__ CD sG0[kSsL][8], sC[kSsL][8], sCl[kSsL][8], sE2[kSsL][8];
     const int Nt = S.Nt, Nl = S.src[0].n, Nv = S.src[1].n;
     const int tl = threadIdx.x % kSsL, tv = threadIdx.x / kSsL;
@@ -810,8 +790,15 @@ __global__ void __launch_bounds__(256, 1) gauss_ss_shared_kernel(const __grid_co
                 }
             }
             if (tl == 0) {
+                // the view throughput, and the isotropic lobes' root sqrt(sum_a B_a^2)
+                CD q{ 0.0, 0.0 };
 #pragma unroll
-                for (int a = 0; a < 3; ++a) sB[tv][a] = CD{ dM((double)vw.gdir[3 * vc + a], vw.ga), dM(k, dS((double)vw.p[3 * vc + a], x[a])) };
+                for (int a = 0; a < 3; ++a) {
+                    const CD b = CD{ dM((double)vw.gdir[3 * vc + a], vw.ga), dM(k, dS((double)vw.p[3 * vc + a], x[a])) };
+                    sB[tv][a] = b;
+                    q = cf_add(q, cf_mul(b, b));
+                }
+                sBi[tv] = cf_sqrt(q);
             }
             __syncthreads();
             if (!act) continue;
@@ -819,32 +806,47 @@ __global__ void __launch_bounds__(256, 1) gauss_ss_shared_kernel(const __grid_co
             for (int i = 0; i < M; ++i) {
                 const double gs = mix[2 * i];
                 const CD C = sC[tl][i], cl = sCl[tl][i];
-                CD q{ 0.0, 0.0 };
+                CD sm;
                 if (fabs(gs) < 0.000001) {
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) q = cf_add(q, cf_mul(sB[tv][a], sB[tv][a]));
+                    sm = sBi[tv];
                 } else {
                     const CD g0 = sG0[tl][i];
+                    CD q{ 0.0, 0.0 };
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
                         const CD e = cf_add(cf_mul(g0, sA[tl][a]), sB[tv][a]);
                         q = cf_add(q, cf_mul(e, e));
                     }
+                    sm = cf_sqrt(q);
                 }
-                const CD sm = cf_sqrt(q);
                 const bool sbig = fabs(sm.re) > 0.0001 || fabs(sm.im) > 0.0001;
                 const bool cbig = fabs(C.re) > 0.0001 || fabs(C.im) > 0.0001;
                 if (sbig && cbig) {
                     const CD z = cf_add(C, sm);
                     const CD pos = cf_add(cl, z);
                     const double negre = cl.re - z.re;
-                    if (fabs(cl.re) < 300.0 && fabs(pos.re) < 300.0) {
-                        // (e^(cl + z) - e^(cl - z)) / (C sm) = (ep^2 - e^(2 cl)) / (ep C sm)
-                        const CD ep = cd_exp(pos);
-                        CD n{ 0.0, 0.0 };
-                        if (pos.re > -10.0) n = cf_mul(ep, ep);
-                        if (negre > -10.0) n = cf_sub(n, sE2[tl][i]);
-                        f = cf_add(f, cf_div(n, cf_mul(ep, cf_mul(C, sm))));
+                    if (fabs(cl.re) < 300.0 && fabs(pos.re) < 300.0 && fabs(negre) < 600.0 && fabs(z.re) + fabs(z.im) > 0.05) {
+                        // (e^(cl + z) - e^(cl - z)) / (C sm) with e^(cl + z) = 2^kk p (cos, sin)
+                        // and e^(cl - z) = e^(2 cl) / e^(cl + z) = e^(2 cl) 2^-kk p^-1 (cos, -sin)
+                        float pf, cf, sf;
+                        double kk;
+                        exp_parts(pos, pf, kk, cf, sf);
+                        CD r{ 0.0, 0.0 };
+                        if (pos.re > -10.0) {
+                            const double m = (double)pf * pow2i(kk);
+                            r = CD{ m * (double)cf, m * (double)sf };
+                        }
+                        if (negre > -10.0) {
+                            const CD e2 = sE2[tl][i];
+                            const double im = (double)g_rcp32(pf) * pow2i(-kk);
+                            const CD q{ im * (double)cf, -im * (double)sf };
+                            r = cf_sub(r, cf_mul(e2, q));
+                        }
+                        // / (C sm): the reciprocal of |C sm|^2 to FP32 accuracy (the
+                        // factor scales the term; |C sm| is far from FP32's range ends)
+                        const CD w = cf_mul(C, sm);
+                        const double iw = (double)g_rcp32((float)(w.re * w.re + w.im * w.im));
+                        f = cf_add(f, CD{ (r.re * w.re + r.im * w.im) * iw, (r.im * w.re - r.re * w.im) * iw });
                     } else {
                         f = cd_add(f, cd_div(cd_2sinh(z, cl), cd_mul(C, sm)));
                     }

@@ -126,6 +126,59 @@ __device__ inline CD bessel_i0(CD z)
     return cd_mul(cd_sqrt(q), ct);
 }
 
+// ---- per-element arithmetic of the NEE and single-scattering sums ----
+// Complex operations contracted to FMAs (the sampling code above keeps the
+// explicitly rounded forms).
+__device__ __forceinline__ CD cf_add(CD a, CD b) { return CD{ a.re + b.re, a.im + b.im }; }
+__device__ __forceinline__ CD cf_sub(CD a, CD b) { return CD{ a.re - b.re, a.im - b.im }; }
+__device__ __forceinline__ CD cf_mul(CD a, CD b) { return CD{ a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re }; }
+__device__ __forceinline__ float g_ex2_32(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float g_rcp32(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// e^x = 2^kk p for |x| < 700: x log2(e) split into an integer kk and a
+// fraction in FP64 (log2(e) in two parts), p = 2^fraction by the FP32
+// exponential instruction (relative error a few 1e-7)
+__device__ __forceinline__ void exp_split(double x, float& p, double& kk)
+{
+    kk = rint(x * 1.4426950408889634);
+    const double fr = fma(x, 1.4426950408889634, -kk) + x * 2.0355273740931033e-17;
+    p = g_ex2_32((float)fr);
+}
+// e^z = 2^kk p (c, s): the magnitude by exp_split, the angle reduced to
+// [-pi, pi] in FP64 (Cody and Waite's reduction with 2 pi in two parts) and
+// (c, s) its FP32 cosine and sine
+__device__ __forceinline__ void exp_parts(CD z, float& p, double& kk, float& c, float& s)
+{
+    exp_split(z.re, p, kk);
+    const double n = rint(z.im * 0.15915494309189535);
+    const double r = fma(-n, 2.4492935982947064e-16, fma(-n, 6.283185307179586, z.im));
+    __sincosf((float)r, &s, &c);
+}
+// 2^kk for an integer-valued kk in [-1022, 1023], by the exponent field
+__device__ __forceinline__ double pow2i(double kk)
+{
+    return __longlong_as_double((long long)((int)kk + 1023) << 52);
+}
+// principal square root: s = sqrt((|re| + |z|) / 2); (s, im / 2s) for re >= 0,
+// else (|im| / 2s, +-s), with 1 / s from one reciprocal square root
+__device__ __forceinline__ CD cf_sqrt(CD a)
+{
+    if (a.re == 0.0 && a.im == 0.0) return CD{ 0.0, 0.0 };
+    const double h = 0.5 * (fabs(a.re) + sqrt(a.re * a.re + a.im * a.im));
+    const double ri = rsqrt(h), s = h * ri;
+    if (a.re >= 0.0) return CD{ s, 0.5 * a.im * ri };
+    return CD{ 0.5 * fabs(a.im) * ri, copysign(s, a.im) };
+}
+
 // sum_i (a v_i + T_i)^2 over the three axes (a, v real; T complex)
 __device__ __forceinline__ CD g_sumsq(double a, const double v[3], const CD T[3])
 {
@@ -372,10 +425,39 @@ __device__ inline CD gauss_f(const DevScene& S, const DevSource& s, int k, const
     const double* mix = S.gmix + 2 * S.gmix_off[m];
     for (int i = 0; i < S.gmix_n[m]; ++i) {
         const CD lnu{ tc + mix[2 * i + 1], 0.0 };
-        const CD sm = cd_sqrt(g_sumsq(mix[2 * i], w0, T));
-        if (S.dims == 2) acc = cd_add(acc, cd_exp(cd_add(cd_log(bessel_i0(sm)), lnu)));
-        else if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) acc.re += 2.0 * exp(lnu.re);
-        else acc = cd_add(acc, cd_div(cd_2sinh(sm, lnu), sm));
+        if (S.dims == 2) {
+            const CD sm = cd_sqrt(g_sumsq(mix[2 * i], w0, T));
+            acc = cd_add(acc, cd_exp(cd_add(cd_log(bessel_i0(sm)), lnu)));
+            continue;
+        }
+        const CD sm = cf_sqrt(g_sumsq(mix[2 * i], w0, T));
+        const double lr = lnu.re, posre = lr + sm.re, negre = lr - sm.re;
+        if (fabs(sm.re) < 0.0001 && fabs(sm.im) < 0.0001) {
+            acc.re += 2.0 * exp(lr);
+        } else if (fabs(lr) < 300.0 && fabs(posre) < 300.0 && fabs(negre) < 600.0 && fabs(sm.re) + fabs(sm.im) > 0.05) {
+            // 2 sinh(sm) e^lnu / sm: e^(lnu + sm) = 2^kk p (c, s), e^(lnu - sm) =
+            // e^(2 lnu) / e^(lnu + sm) = 2^(k2 - kk) (p2 / p) (c, -s); each dropped
+            // at a real part of -10 or below
+            float pf, c, s, p2;
+            double kk, k2;
+            exp_parts(CD{ posre, sm.im }, pf, kk, c, s);
+            exp_split(2.0 * lr, p2, k2);
+            CD r{ 0.0, 0.0 };
+            if (posre > -10.0) {
+                const double mg = (double)pf * pow2i(kk);
+                r = CD{ mg * (double)c, mg * (double)s };
+            }
+            if (negre > -10.0) {
+                const double mg = (double)(p2 * g_rcp32(pf)) * pow2i(k2 - kk);
+                r.re -= mg * (double)c;
+                r.im += mg * (double)s;
+            }
+            // / sm: the reciprocal of |sm|^2 to FP32 accuracy
+            const double iw = (double)g_rcp32((float)(sm.re * sm.re + sm.im * sm.im));
+            acc = cf_add(acc, CD{ (r.re * sm.re + r.im * sm.im) * iw, (r.im * sm.re - r.re * sm.im) * iw });
+        } else {
+            acc = cd_add(acc, cd_div(cd_2sinh(sm, lnu), sm));
+        }
     }
     return acc;
 }
