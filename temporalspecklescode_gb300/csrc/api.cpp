@@ -120,6 +120,7 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
            && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' path counter
            && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
+           && alloc((void**)&first_v, (size_t)paths * 2 * sizeof(float4))
            && alloc((void**)&ovf, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * kWalkSlotVerts * sizeof(float4))
            && alloc((void**)&ovf_owner, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * sizeof(uint2))
            && alloc((void**)&p2v, paths * sizeof(float))
@@ -135,10 +136,10 @@ int Engine::ensure(Scene& S, uint32_t paths)
 void Engine::release()
 {
     void* ps[] = { a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, totals, err, V, W, counts, misses, offsets, block_sums, vtotal, verts,
-                   slots, longq, ovf, ovf_owner, p2v, ss_row, ss_hist, ss_bucket, seg_list, seg_ctr };
+                   slots, longq, first_v, ovf, ovf_owner, p2v, ss_row, ss_hist, ss_bucket, seg_list, seg_ctr };
     for (void* p : ps) if (p) cudaFreeAsync(p, stream);
     counts = misses = offsets = block_sums = nullptr; vtotal = nullptr; verts = nullptr; verts_cap = 0;
-    slots = nullptr; longq = nullptr; ovf = nullptr; ovf_owner = nullptr; p2v = nullptr;
+    slots = nullptr; longq = nullptr; first_v = nullptr; ovf = nullptr; ovf_owner = nullptr; p2v = nullptr;
     ss_row = ss_hist = ss_bucket = nullptr;
     seg_list = nullptr; seg_cap = 0; seg_ctr = nullptr;
     a_ms = s_ms = a_ss = b_ss = g2 = nullptr;
@@ -236,6 +237,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     // the rest in overflow blocks; paths that found the pool empty are
     // listed for a replay
     Wp.slots = slots; Wp.list = longq; Wp.list_count = reinterpret_cast<uint32_t*>(vtotal + 2);
+    Wp.first = first_v;
     Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_count = Wp.list_count + 1; Wp.ovf_cap = ovf_blocks;
     int e = launch_walk_count(S.dev, Wp, stream);
     if (e) return e;

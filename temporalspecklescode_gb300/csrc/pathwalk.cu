@@ -129,7 +129,33 @@ __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __gri
         }
         if (MODE != kCount && W.hash) h = hash_v(S, h, x, m);   // the debug trace's vertex hash
     };
-    if (!start(fetch())) return;
+    // non-beam walks: the path's first vertex from its record (first_vertex_kernel);
+    // false when the first vertex hit a limit (the path then ends with no vertices)
+    auto begin = [&]() -> bool {
+        const float4 r0 = W.first[2 * (size_t)q], r1 = W.first[2 * (size_t)q + 1];
+        const uint32_t w = __float_as_uint(r1.w);
+        att = (w >> 4) & 0x7ffffffu;
+        if (!(w >> 31)) return false;
+        prev = V3{ r0.x, r0.y, r0.z };
+        cur = V3{ r1.x, r1.y, r1.z };
+        mcur = (int)(w & 15u);
+        store(0, cur, mcur, r0.w);
+        B = 1; b = 2;
+        return true;
+    };
+    // the next path with work; false when the pool is drawn
+    auto next_path = [&]() -> bool {
+        for (;;) {
+            if (!start(fetch())) return false;
+            if constexpr (GB) {
+                return true;
+            } else {
+                if (begin()) return true;
+                finish(false);
+            }
+        }
+    };
+    if (!next_path()) return;
     for (;;) {
         Stream rs;
         rs.init(W.seed, pid, b, kPurposeWalk | (b == 1 ? att << 8 : 0u));
@@ -155,18 +181,15 @@ __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __gri
                 ok = woodcock(S, o, d, rs, xn, mn);
             }
         } else {
-            if (b == 1) {
-                sample_source(S, *fsrc, rs, o, d);
-            } else {
-                const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
-                d = sample_direction<VMF>(S, mcur, din, rs);
-                o = cur;
-            }
+            // b >= 2: the first vertex came from its record
+            const V3 din = normalize32(S.dims, V3{ fsb(cur.x, prev.x), fsb(cur.y, prev.y), fsb(cur.z, prev.z) });
+            d = sample_direction<VMF>(S, mcur, din, rs);
+            o = cur;
             ok = woodcock(S, o, d, rs, xn, mn);
         }
         bool done = !ok;
         if (ok) {
-            if (b == 1) {
+            if (GB && b == 1) {
                 if (mn == 0) {
                     if (++att >= kMaxAttempts) { ok = false; done = true; }
                 } else {
@@ -186,8 +209,47 @@ __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __gri
         }
         if (done) {
             finish(ok);
-            if (!start(fetch())) return;
+            if (!next_path()) return;
         }
+    }
+}
+
+// The first vertex of every path of a chunk (non-beam sources), thread per
+// path: source sampling and free flight with the miss resampling of the
+// walk's first iteration, over the same Philox streams (vertex 1, the
+// attempt count in the purpose), so the walk continues from it at vertex 2
+// with identical results.  Taking it out of the walk keeps the walk's lanes
+// on the same code: inside the walk, a warp ran the source sampling and the
+// flight from outside the medium in most of its iterations, for the few lanes
+// whose paths had just started.
+__global__ void __launch_bounds__(128) first_vertex_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
+{
+    const bool corr = S.correlation != 0;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < W.paths; q += gridDim.x * blockDim.x) {
+        const uint32_t pid = W.first_path + q;
+        const uint32_t slot = pid % S.P, wave = pid / S.P;
+        const DevSource* fsrc = (!corr || slot < u1_count_w(S, W.seed, wave)) ? &S.src[0] : &S.src[2];
+        uint32_t att = 0;
+        bool ok = true;
+        V3 o{ 0.f, 0.f, 0.f }, xn{ 0.f, 0.f, 0.f };
+        int mn = 0;
+        float xi = 0.0f;
+        for (;;) {
+            Stream rs;
+            rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
+            rs.prime2();
+            V3 d;
+            sample_source(S, *fsrc, rs, o, d);
+            if (!woodcock(S, o, d, rs, xn, mn)) { ok = false; break; }
+            if (mn == 0) {
+                if (++att >= kMaxAttempts) { ok = false; break; }
+                continue;
+            }
+            xi = corr ? 0.0f : rs.uniform();
+            break;
+        }
+        W.first[2 * (size_t)q] = make_float4(o.x, o.y, o.z, xi);
+        W.first[2 * (size_t)q + 1] = make_float4(xn.x, xn.y, xn.z, __uint_as_float((ok ? 0x80000000u : 0u) | (att << 4) | (uint32_t)mn));
     }
 }
 
@@ -301,6 +363,14 @@ static void walk_launch(const DevScene& S, const WalkParams& W, int blocks, cuda
 int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t stream)
 {
     if (cudaMemsetAsync(W.next, 0, 2 * sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+    if (!(S.gauss && S.dims == 3)) {   // the beam walk places its own first vertices
+        if (W.first == nullptr) return SSTMC_MISC_ERROR;
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const uint32_t want = (W.paths + 127) / 128;
+        first_vertex_kernel<<<(int)std::max<uint32_t>(1, std::min(want, (uint32_t)sms * 16)), 128, 0, stream>>>(S, W);
+    }
     if (W.slots) {
         if (cudaMemsetAsync(W.list_count, 0, sizeof(uint32_t), stream) != cudaSuccess
             || cudaMemsetAsync(W.ovf_count, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
@@ -339,14 +409,16 @@ int launch_walk_write(const DevScene& S, const WalkParams& W, cudaStream_t strea
 }
 
 // Default pool: one overflow block per 16 paths.  Paths longer than a slot
-// are rare at a mean of 14 vertices per path (about 1 %); scenes with long
-// paths find the pool short, their overflowing paths take the write pass, and
-// the engine then grows the pool for its next chunks (api.cpp, trace_chunk).
+// are rare at a mean of 14 vertices per path (about 1 %); a chunk of long
+// paths finds the pool short, and the engine grows it and walks the chunk
+// again (the fixed-scratch render replays the overflowing paths in the write
+// pass instead; api.cpp, trace_chunk).
 uint32_t walk_overflow_blocks(uint32_t paths) { return paths / 16 + 64; }
 
 size_t walk_slot_bytes_per_path()
 {
-    return kSlotVerts * sizeof(float4) + (kSlotVerts * sizeof(float4) + sizeof(uint2)) / 16 + 1 + sizeof(uint32_t);
+    return kSlotVerts * sizeof(float4) + (kSlotVerts * sizeof(float4) + sizeof(uint2)) / 16 + 1 + sizeof(uint32_t)
+         + 2 * sizeof(float4);   // the first-vertex record
 }
 
 }  // namespace sstmc

@@ -33,6 +33,7 @@ struct Engine {
     bool rows_real = false;       // the chunk's a_ms / s_ms are real floats (trace_chunk -> contract_chunk)
     float4* slots = nullptr;      // single-pass walk: first 64 vertices of each path of a chunk
     uint32_t* longq = nullptr;    // paths of the chunk that found the overflow pool empty
+    float4* first_v = nullptr;    // first vertex of each path of a chunk (two float4 per path)
     float4* ovf = nullptr;        // overflow blocks of 64 vertices (pathwalk.cu)
     uint32_t ovf_blocks = 0;      // overflow blocks allocated
     uint32_t ovf_want = 0;        // learned pool size: a chunk that found the pool short grows it

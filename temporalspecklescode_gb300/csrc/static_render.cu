@@ -96,7 +96,7 @@ size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 // Byte layout of the scratch for a chunk of n paths.
 struct Layout {
     size_t V, totals, err, vtotal, ticks, W, fixed_end;
-    size_t a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, counts, misses, offsets, block_sums, slots, longq, ovf, ovf_owner, p2v, rows_end;
+    size_t a_ms, s_ms, a_ss, b_ss, g2, pl, x1, x1t, m1, counts, misses, offsets, block_sums, slots, longq, first, ovf, ovf_owner, p2v, rows_end;
     uint32_t ovf_blocks;
 };
 
@@ -129,6 +129,7 @@ Layout layout(const Scene& S, bool farfar, uint32_t n)
     L.block_sums = take(((n + 1023) / 1024 + 1) * sizeof(uint32_t));
     L.slots = take((size_t)n * kWalkSlotVerts * sizeof(float4));
     L.longq = take(n * sizeof(uint32_t));
+    L.first = take((size_t)n * 2 * sizeof(float4));
     L.ovf_blocks = walk_overflow_blocks(n);
     L.ovf = take((size_t)walk_overflow_blocks(n) * kWalkSlotVerts * sizeof(float4));
     L.ovf_owner = take((size_t)walk_overflow_blocks(n) * sizeof(uint2));
@@ -158,6 +159,7 @@ void point_engine(Engine& E, unsigned char* base, const Layout& L)
     E.block_sums = reinterpret_cast<uint32_t*>(base + L.block_sums);
     E.slots = reinterpret_cast<float4*>(base + L.slots);
     E.longq = reinterpret_cast<uint32_t*>(base + L.longq);
+    E.first_v = reinterpret_cast<float4*>(base + L.first);
     E.ovf = reinterpret_cast<float4*>(base + L.ovf);
     E.ovf_owner = reinterpret_cast<uint2*>(base + L.ovf_owner);
     E.ovf_blocks = L.ovf_blocks;   // fixed: a short pool leaves its paths to the replay
