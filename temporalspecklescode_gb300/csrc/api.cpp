@@ -241,7 +241,9 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_count = Wp.list_count + 1; Wp.ovf_cap = ovf_blocks;
     int e = launch_walk_count(S.dev, Wp, stream);
     if (e) return e;
-    launches += 4;
+    // the first-vertex kernel (non-beam sources), the walk and the three scan kernels
+    const int walk_launches = (S.dev.gauss && S.dims == 3) ? 4 : 5;
+    launches += walk_launches;
     unsigned char hv[24];
     if (cudaMemcpyAsync(hv, vtotal, sizeof(hv), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
     if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
@@ -271,7 +273,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
         Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_cap = ovf_blocks;
         e = launch_walk_count(S.dev, Wp, stream);
         if (e) return e;
-        launches += 4;
+        launches += walk_launches;
         if (cudaMemcpyAsync(hv, vtotal, sizeof(hv), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
         if (cudaStreamSynchronize(stream) != cudaSuccess) return SSTMC_KERNEL_ERROR;
         std::memcpy(&nverts, hv, 8);
