@@ -40,10 +40,10 @@ size_t budget_bytes()
 {
     const char* e = std::getenv("SSTMC_CHUNK_BYTES");
     if (e) { const long long v = std::atoll(e); if (v > 0) return (size_t)v; }
-    // a quarter of the free device memory, at most 24 GiB
+    // a quarter of the free device memory, at most 32 GiB
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return (size_t)2 << 30;
-    return std::min<size_t>((size_t)24 << 30, std::max<size_t>((size_t)256 << 20, fr / 4));
+    return std::min<size_t>((size_t)32 << 30, std::max<size_t>((size_t)256 << 20, fr / 4));
 }
 
 // The view vectors of the common cases come from the view-side kernel
@@ -78,7 +78,7 @@ size_t Engine::bytes_per_path(const Scene& S)
 }
 
 // Freed chunk buffers stay cached in the device's stream-ordered pool (up
-// to 64 GiB: two scenes' chunk buffers), so a scene created after another
+// to 96 GiB: three scenes' chunk buffers), so a scene created after another
 // one was destroyed, or the next served request, reuses that memory instead
 // of mapping it again.
 static void keep_pool_memory(int device)
@@ -90,7 +90,7 @@ static void keep_pool_memory(int device)
         if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
         uint64_t keep = 0;
         cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-        keep = std::max<uint64_t>(keep, (uint64_t)64 << 30);
+        keep = std::max<uint64_t>(keep, (uint64_t)96 << 30);
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     });
 }

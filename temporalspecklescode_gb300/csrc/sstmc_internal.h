@@ -62,7 +62,7 @@ struct Engine {
     double ms_trace = 0, ms_gemm = 0, ms_ss = 0, ms_total = 0, ms_walk = 0;
     uint64_t launches = 0, chunks = 0;
     bool timing = true;
-    size_t budget = 0;    // device bytes for the chunk buffers; 0: min(24 GiB, a quarter of free memory)
+    size_t budget = 0;    // device bytes for the chunk buffers; 0: min(32 GiB, a quarter of free memory)
     uint32_t tuned_chunk = 0;   // paths per chunk chosen by sstmc_scene_autotune (0: from the budget)
     bool fixed = false;   // buffers carved from a fixed scratch: a chunk that outgrows them fails, nothing is allocated
 
