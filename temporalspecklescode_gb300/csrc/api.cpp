@@ -118,7 +118,7 @@ int Engine::ensure(Scene& S, uint32_t paths)
            && alloc((void**)&counts, paths * sizeof(uint32_t)) && alloc((void**)&misses, paths * sizeof(uint32_t))
            && alloc((void**)&offsets, paths * sizeof(uint32_t))
            && alloc((void**)&block_sums, ((paths + 1023) / 1024 + 1) * sizeof(uint32_t))
-           && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' path counter
+           && alloc((void**)&vtotal, 32)   // vertex total, the walk's two path counters, long-path and overflow-block counts, the NEE kernels' and the first-vertex kernel's path counters
            && alloc((void**)&slots, (size_t)paths * kWalkSlotVerts * sizeof(float4)) && alloc((void**)&longq, paths * sizeof(uint32_t))
            && alloc((void**)&first_v, (size_t)paths * 2 * sizeof(float4))
            && alloc((void**)&ovf, (size_t)std::max(walk_overflow_blocks(paths), ovf_want) * kWalkSlotVerts * sizeof(float4))
@@ -238,6 +238,7 @@ int Engine::trace_chunk(Scene& S, uint64_t seed, uint32_t first, uint32_t n, Pat
     // listed for a replay
     Wp.slots = slots; Wp.list = longq; Wp.list_count = reinterpret_cast<uint32_t*>(vtotal + 2);
     Wp.first = first_v;
+    Wp.first_next = reinterpret_cast<uint32_t*>(vtotal) + 7;   // bytes 28..31 of the counter block
     Wp.ovf = ovf; Wp.ovf_owner = ovf_owner; Wp.ovf_count = Wp.list_count + 1; Wp.ovf_cap = ovf_blocks;
     int e = launch_walk_count(S.dev, Wp, stream);
     if (e) return e;

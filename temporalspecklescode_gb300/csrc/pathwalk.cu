@@ -214,42 +214,62 @@ __global__ void __launch_bounds__(128, kWalkBlocksPerSM) walk_kernel(const __gri
     }
 }
 
-// The first vertex of every path of a chunk (non-beam sources), thread per
-// path: source sampling and free flight with the miss resampling of the
-// walk's first iteration, over the same Philox streams (vertex 1, the
-// attempt count in the purpose), so the walk continues from it at vertex 2
-// with identical results.  Taking it out of the walk keeps the walk's lanes
-// on the same code: inside the walk, a warp ran the source sampling and the
-// flight from outside the medium in most of its iterations, for the few lanes
-// whose paths had just started.
+// The first vertex of every path of a chunk (non-beam sources): source
+// sampling and free flight with the miss resampling of the walk's first
+// iteration, over the same Philox streams (vertex 1, the attempt count in the
+// purpose), so the walk continues from it at vertex 2 with identical results.
+// Taking it out of the walk keeps the walk's lanes on the same code: inside
+// the walk, a warp ran the source sampling and the flight from outside the
+// medium in most of its iterations, for the few lanes whose paths had just
+// started.  A thread takes one attempt per iteration and a new path from a
+// warp-aggregated counter when its path has its first vertex, so a warp's
+// time follows the mean number of attempts rather than its unluckiest lane's.
 __global__ void __launch_bounds__(128) first_vertex_kernel(const __grid_constant__ DevScene S, const __grid_constant__ WalkParams W)
 {
     const bool corr = S.correlation != 0;
-    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < W.paths; q += gridDim.x * blockDim.x) {
-        const uint32_t pid = W.first_path + q;
+    const uint32_t lane = threadIdx.x & 31u;
+    auto fetch = [&]() -> uint32_t {
+        const uint32_t mask = __activemask();
+        const int leader = __ffs(mask) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(W.first_next, (uint32_t)__popc(mask));
+        base = __shfl_sync(mask, base, leader);
+        return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+    };
+    uint32_t q = fetch();
+    if (q >= W.paths) return;
+    uint32_t pid = 0, att = 0;
+    const DevSource* fsrc = &S.src[0];
+    auto begin = [&]() {
+        pid = W.first_path + q;
         const uint32_t slot = pid % S.P, wave = pid / S.P;
-        const DevSource* fsrc = (!corr || slot < u1_count_w(S, W.seed, wave)) ? &S.src[0] : &S.src[2];
-        uint32_t att = 0;
-        bool ok = true;
-        V3 o{ 0.f, 0.f, 0.f }, xn{ 0.f, 0.f, 0.f };
+        fsrc = (!corr || slot < u1_count_w(S, W.seed, wave)) ? &S.src[0] : &S.src[2];
+        att = 0;
+    };
+    begin();
+    for (;;) {
+        Stream rs;
+        rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
+        rs.prime2();
+        V3 o, d, xn;
         int mn = 0;
+        sample_source(S, *fsrc, rs, o, d);
+        const bool flew = woodcock(S, o, d, rs, xn, mn);
+        bool done = true, ok = false;
         float xi = 0.0f;
-        for (;;) {
-            Stream rs;
-            rs.init(W.seed, pid, 1u, kPurposeWalk | (att << 8));
-            rs.prime2();
-            V3 d;
-            sample_source(S, *fsrc, rs, o, d);
-            if (!woodcock(S, o, d, rs, xn, mn)) { ok = false; break; }
-            if (mn == 0) {
-                if (++att >= kMaxAttempts) { ok = false; break; }
-                continue;
-            }
+        if (flew && mn == 0) {
+            done = ++att >= kMaxAttempts;   // a miss: another attempt, up to the limit
+        } else if (flew) {
             xi = corr ? 0.0f : rs.uniform();
-            break;
+            ok = true;
         }
-        W.first[2 * (size_t)q] = make_float4(o.x, o.y, o.z, xi);
-        W.first[2 * (size_t)q + 1] = make_float4(xn.x, xn.y, xn.z, __uint_as_float((ok ? 0x80000000u : 0u) | (att << 4) | (uint32_t)mn));
+        if (done) {
+            W.first[2 * (size_t)q] = make_float4(o.x, o.y, o.z, xi);
+            W.first[2 * (size_t)q + 1] = make_float4(xn.x, xn.y, xn.z, __uint_as_float((ok ? 0x80000000u : 0u) | (att << 4) | (uint32_t)mn));
+            q = fetch();
+            if (q >= W.paths) return;
+            begin();
+        }
     }
 }
 
@@ -368,8 +388,9 @@ int launch_walk_count(const DevScene& S, const WalkParams& W, cudaStream_t strea
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const uint32_t want = (W.paths + 127) / 128;
-        first_vertex_kernel<<<(int)std::max<uint32_t>(1, std::min(want, (uint32_t)sms * 16)), 128, 0, stream>>>(S, W);
+        if (W.first_next == nullptr || cudaMemsetAsync(W.first_next, 0, sizeof(uint32_t), stream) != cudaSuccess) return SSTMC_DEVICE_ERROR;
+        const uint32_t want = (W.paths + 4 * 128 - 1) / (4 * 128);   // about 4 paths per thread, drawn from the counter
+        first_vertex_kernel<<<(int)std::max<uint32_t>(1, std::min(want, (uint32_t)sms * 8)), 128, 0, stream>>>(S, W);
     }
     if (W.slots) {
         if (cudaMemsetAsync(W.list_count, 0, sizeof(uint32_t), stream) != cudaSuccess

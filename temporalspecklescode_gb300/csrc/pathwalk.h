@@ -31,6 +31,7 @@ struct WalkParams {
     uint32_t* next;          // [2] path counters of the count and write passes (zeroed by launch_walk_count)
     float4* first;           // [paths][2] first vertex of every path (launch_walk_count): (origin, xi),
                              // (x1, ok << 31 | attempts << 4 | material); read by the non-beam walks
+    uint32_t* first_next;    // [1] path counter of the first-vertex kernel (zeroed by launch_walk_count)
 };
 
 // Count pass (with W.slots: the single pass that also keeps the first 64
