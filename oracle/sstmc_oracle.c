@@ -743,6 +743,7 @@ static int o_woodcock(const o_scene* S, const float o[3], const float d[3], o_st
     float p[3] = { o[0], o[1], o[2] };
     int m = 0;
     unsigned steps = 0;
+    const int from_inside = o_inside(S, o);
     for (;;) {
         if (++steps > O_MAX_WOODCOCK) return SSTMC_PATH_LIMIT;
         float u = o_uniform(rs);
@@ -751,9 +752,10 @@ static int o_woodcock(const o_scene* S, const float o[3], const float d[3], o_st
         if (!o_inside(S, p)) {
             /* still outside on a ray that enters the box: move on to the entry
              * face (flight lengths are memoryless, so the first point inside
-             * keeps its distribution) */
+             * keeps its distribution); a flight that started inside the
+             * (convex) box ends at its first point outside */
             float te = 0.0f;
-            if (!o_points_toward(S, p, d, &te)) break;
+            if (from_inside || !o_points_toward(S, p, d, &te)) break;
             dist = dist + te;
         } else {
             m = S->grid[o_cell(S, p)];

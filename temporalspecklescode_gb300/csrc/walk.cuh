@@ -198,13 +198,15 @@ __device__ inline V3 rotate_dir(const DevScene& S, const V3& din, float c, Strea
 // on a ray that still enters it moves on to the entry face: flight lengths
 // are memoryless, so the first point inside is the entry plus an exponential
 // step, as with further steps outside, but one lane no longer spins alone
-// through many small steps toward a far or grazing entry.
+// through many small steps toward a far or grazing entry.  A flight that
+// starts inside the (convex) box ends at its first point outside.
 __device__ inline bool woodcock(const DevScene& S, const V3& o, const V3& d, Stream& rs, V3& out, int& mat)
 {
     float dist = 0.0f;
     V3 p = o;
     int m = 0;
     uint32_t steps = 0;
+    const bool from_inside = inside(S, o);
     for (;;) {
         if (++steps > kMaxWoodcock) return false;
         const float u = rs.uniform();
@@ -214,7 +216,7 @@ __device__ inline bool woodcock(const DevScene& S, const V3& o, const V3& d, Str
         if (S.dims == 3) p.z = ffma(dist, d.z, o.z);
         if (!inside(S, p)) {
             float te = 0.0f;
-            if (!points_toward(S, p, d, &te)) break;
+            if (from_inside || !points_toward(S, p, d, &te)) break;
             dist = fa(dist, te);
         } else {
             m = material_at(S, p);
