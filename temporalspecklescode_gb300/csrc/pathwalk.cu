@@ -58,9 +58,10 @@ __device__ __forceinline__ float4 pack_vertex(const V3& x, int m, float xi)
 // MODE kWrite: replay paths (all, or the W.list of long ones) and write their
 //   vertices at their offsets.
 constexpr int kCount = 0, kWrite = 1, kSlots = 2;
-// resident walk blocks of 128 threads per SM (72 registers): the launch bound
-// and the persistent grid's size
-constexpr int kWalkBlocksPerSM = 7;
+// resident walk blocks of 128 threads per SM (64 registers, no spills since
+// the first vertices left the walk): the launch bound and the persistent
+// grid's size
+constexpr int kWalkBlocksPerSM = 8;
 
 // GB: Gaussian-beam illumination (3D): the beam places the first vertex and
 // samples the second direction (gauss.cuh)
