@@ -199,7 +199,11 @@ int32_t sstmc_scene_shape(const sstmc_scene* scene, uint32_t* nl, uint32_t* nv, 
  * MatlabInterface.cu:1783-1801 (trace, iter, seed++ per rendering).
  * u_out: 2 * Nl * Nv * Nt * renderings_num doubles (interleaved complex),
  * iter_out: renderings_num doubles (may be NULL).  seed overrides
- * cfg.seed for the first rendering. */
+ * cfg.seed for the first rendering.  Paths are traced in chunks whose device
+ * buffers take at most min(32 GiB, a quarter of the free device memory), or
+ * the bytes given by the environment variable SSTMC_CHUNK_BYTES; freed chunk
+ * buffers stay in the device's stream-ordered memory pool (up to 96 GiB) for
+ * the next scene or render. */
 int32_t sstmc_render(sstmc_scene* scene, uint64_t seed, double* u_out, double* iter_out);
 
 /* Wavefront autotuner.  No counterpart in the reference, whose wavefront is
